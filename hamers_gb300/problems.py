@@ -1,0 +1,241 @@
+"""Initial conditions and workload definitions (host side, numpy).
+
+Every state array uses the SAMRAI layout of the conserved variables of a
+patch: shape (ncomp, G2, G1, G0), ghost width 4, x fastest.  Component order
+follows the reference's conservative variables:
+
+  single species  : rho, rho*u_k (dim), E
+  five-eqn Allaire: Z_i*rho_i (N), rho*u_k (dim), E, Z_i (N, the last one is
+                    stored as the reference's volume-fraction CellData does)
+
+The problems are the reference's convergence problems
+(problems/Euler/initial_conditions/ConvergenceSingleSpecies.cpp:77-99,
+ConvergenceFiveEqnAllaire.cpp:100-125) and seeded synthetic stand-ins for the
+benchmark workloads (a 2D periodic density wave, a shocked two-species
+interface, 3D density blobs on uneven patches, the Taylor-Green vortex).
+"""
+import math
+
+import numpy as np
+
+GHOST = 4
+MODEL_SINGLE_SPECIES = 0
+MODEL_FOUR_EQN_CONSERVATIVE = 1
+MODEL_FIVE_EQN_ALLAIRE = 2
+
+
+def ncomp_of(model, dim, nspecies):
+    if model == MODEL_SINGLE_SPECIES:
+        return dim + 2
+    if model == MODEL_FOUR_EQN_CONSERVATIVE:
+        return nspecies + dim + 1
+    return dim + 2 * nspecies + 1
+
+
+def _grid(n, xlo, dx, dim):
+    """Cell-centre coordinates over the ghost box, each (G2, G1, G0)."""
+    axes = []
+    for d in range(3):
+        if d < dim:
+            idx = np.arange(-GHOST, n[d] + GHOST, dtype=np.float64)
+            axes.append(xlo[d] + (idx + 0.5) * dx[d])
+        else:
+            axes.append(np.zeros(1))
+    z, y, x = np.meshgrid(axes[2], axes[1], axes[0], indexing="ij")
+    return [x, y, z][:dim]
+
+
+def single_species_state(rho, vel, p, gamma):
+    """Conserved variables from primitives (ideal gas)."""
+    dim = len(vel)
+    out = np.empty((dim + 2,) + rho.shape)
+    out[0] = rho
+    ke = sum(v * v for v in vel)
+    for k in range(dim):
+        out[1 + k] = rho * vel[k]
+    out[dim + 1] = p / (gamma - 1.0) + 0.5 * rho * ke
+    return out
+
+
+def five_eqn_state(Z1, rho1, rho2, vel, p, gammas):
+    """Two-species five-equation (Allaire) conserved variables."""
+    dim = len(vel)
+    g1, g2 = gammas
+    Z2 = 1.0 - Z1
+    out = np.empty((dim + 5,) + Z1.shape)
+    out[0] = Z1 * rho1
+    out[1] = Z2 * rho2
+    rho_m = out[0] + out[1]
+    gamma_m = 1.0 / (Z1 / (g1 - 1.0) + Z2 / (g2 - 1.0)) + 1.0
+    for k in range(dim):
+        out[2 + k] = rho_m * vel[k]
+    ke = sum(v * v for v in vel)
+    out[2 + dim] = p / (gamma_m - 1.0) + 0.5 * rho_m * ke
+    out[3 + dim] = Z1
+    out[4 + dim] = Z2
+    return out
+
+
+# ---------------------------------------------------------------------------
+# Convergence problems of the reference's CI (tests/*_convergence_test_*/convergence_test.py)
+# ---------------------------------------------------------------------------
+def convergence_problem(model, dim, N):
+    """Density-wave (single) or volume-fraction-wave (five-eqn) advection on [-1,1]^dim.
+
+    Returns (state, dx, dt, nsteps, exact(t) -> field on the interior, species_gamma).
+    dt = 0.001*dx, 8 steps in 2D (1 in 3D) at N=8, doubled per refinement
+    (convergence_test.py:18-23).
+    """
+    n = [N] * dim
+    dx = [2.0 / N] * dim
+    xlo = [-1.0] * dim
+    X = _grid(n, xlo, dx, dim)
+    s = sum(X)
+    ones = [np.ones_like(s) for _ in range(dim)]
+    level = int(round(math.log2(N / 8)))
+    dt = 0.001 * (2.0 / 8) / 2 ** level
+    nsteps = (8 if dim == 2 else 1) * 2 ** level
+    if model == MODEL_SINGLE_SPECIES:
+        rho = 1.0 + 0.5 * np.sin(math.pi * s)
+        Q = single_species_state(rho, ones, 1.0, 1.4)
+        gam = [1.4]
+
+        def exact(t):
+            Xi = _interior(X, dim)
+            return 1.0 + 0.5 * np.sin(math.pi * (sum(Xi) - dim * t))
+    else:
+        Z1 = 0.5 + 0.25 * np.sin(math.pi * s)
+        Q = five_eqn_state(Z1, 2.0, 1.0, ones, 1.0, (1.6, 1.4))
+        gam = [1.6, 1.4]
+
+        def exact(t):
+            Xi = _interior(X, dim)
+            return 0.5 + 0.25 * np.sin(math.pi * (sum(Xi) - dim * t))
+    return np.ascontiguousarray(Q), dx, dt, nsteps, exact, gam
+
+
+def _interior(X, dim):
+    sl = tuple([slice(GHOST, -GHOST) if d < dim else slice(None) for d in (2, 1, 0)])
+    return [x[sl] for x in X]
+
+
+def interior(Q, dim):
+    sl = (slice(None),) + tuple([slice(GHOST, -GHOST) if d < dim else slice(None) for d in (2, 1, 0)])
+    return Q[sl]
+
+
+# ---------------------------------------------------------------------------
+# Benchmark workloads
+# ---------------------------------------------------------------------------
+def density_wave_2d(N=256, amp=0.2, gamma=1.4, cfl=0.4):
+    """2D single species on [0,1]^2, rho = 1 + amp*sin(2*pi*(x+y)), u=v=1, p=1, periodic.
+
+    dt from the initial state at the given CFL (sum over directions of
+    max(|u_d|+c)/dx_d, Euler::computeSpectralRadiusesAndStableDtOnPatch).
+    """
+    n = [N, N]
+    dx = [1.0 / N, 1.0 / N]
+    X = _grid(n, [0.0, 0.0], dx, 2)
+    rho = 1.0 + amp * np.sin(2.0 * math.pi * (X[0] + X[1]))
+    ones = [np.ones_like(rho), np.ones_like(rho)]
+    Q = single_species_state(rho, ones, 1.0, gamma)
+    c = np.sqrt(gamma * 1.0 / rho)
+    dt = cfl / sum((1.0 + c).max() / d for d in dx)
+    return np.ascontiguousarray(Q), dx, dt
+
+
+def shock_interface_2d(N=1024, seed=1, gammas=(1.4, 1.67), density_ratio=3.0, mach=1.5,
+                       modes=16, amp_max=0.02, cfl=0.4):
+    """2D five-equation shock / perturbed-interface problem on [0,1]^2.
+
+    Species 1 (gamma 1.4, density 1) on the left of a tanh interface at
+    x_I(y) = 0.5 + sum_k a_k sin(2 pi k y + phi_k) (a_k ~ U[0, amp_max],
+    phi_k ~ U[0, 2 pi), seeded), species 2 (density ratio 3) on the right,
+    interface width 4 cells (0.05 -> 0.95), volume fraction clipped to
+    [1e-8, 1-1e-8].  A Mach 1.5 shock at x = 0.25 moves right into species 1
+    with the Rankine-Hugoniot post-shock state behind it.  Zero-gradient in
+    x, periodic in y.
+    """
+    rng = np.random.default_rng(seed)
+    a_k = rng.uniform(0.0, amp_max, modes)
+    phi_k = rng.uniform(0.0, 2.0 * math.pi, modes)
+    n = [N, N]
+    dx = [1.0 / N, 1.0 / N]
+    X = _grid(n, [0.0, 0.0], dx, 2)
+    x, y = X
+    xI = 0.5 + sum(a_k[k] * np.sin(2.0 * math.pi * (k + 1) * y + phi_k[k]) for k in range(modes))
+    delta = 4.0 * dx[0] / (2.0 * math.atanh(0.9))
+    Z1 = 0.5 * (1.0 - np.tanh((x - xI) / delta))
+    Z1 = np.clip(Z1, 1e-8, 1.0 - 1e-8)
+    rho1, rho2 = 1.0, density_ratio
+    g1 = gammas[0]
+    p0 = 1.0
+    # Rankine-Hugoniot jump for a shock of Mach `mach` moving into gas 1 at rest.
+    M2 = mach * mach
+    p_s = p0 * (2.0 * g1 * M2 - (g1 - 1.0)) / (g1 + 1.0)
+    rho_s = rho1 * (g1 + 1.0) * M2 / ((g1 - 1.0) * M2 + 2.0)
+    c1 = math.sqrt(g1 * p0 / rho1)
+    u_s = mach * c1 * (1.0 - rho1 / rho_s)
+    shocked = x < 0.25
+    u = np.where(shocked, u_s, 0.0)
+    v = np.zeros_like(u)
+    p = np.where(shocked, p_s, p0)
+    r1 = np.where(shocked, rho_s, rho1)
+    Q = five_eqn_state(Z1, r1, rho2, [u, v], p, gammas)
+    rho_m = Q[0] + Q[1]
+    gamma_m = 1.0 / (Z1 / (gammas[0] - 1.0) + (1.0 - Z1) / (gammas[1] - 1.0)) + 1.0
+    c = np.sqrt(gamma_m * p / rho_m)
+    dt = cfl / ((np.abs(u) + c).max() / dx[0] + (np.abs(v) + c).max() / dx[1])
+    return np.ascontiguousarray(Q), dx, dt
+
+
+def taylor_green_3d(N=128, mach=0.1, gamma=1.4):
+    """3D Taylor-Green vortex on [0, 2 pi)^3 (rho = 1, p0 = 1/(gamma M^2))."""
+    n = [N, N, N]
+    dx = [2.0 * math.pi / N] * 3
+    X = _grid(n, [0.0, 0.0, 0.0], dx, 3)
+    x, y, z = X
+    u = np.sin(x) * np.cos(y) * np.cos(z)
+    v = -np.cos(x) * np.sin(y) * np.cos(z)
+    w = np.zeros_like(u)
+    p0 = 1.0 / (gamma * mach * mach)
+    p = p0 + ((np.cos(2.0 * z) + 2.0) * (np.cos(2.0 * x) + np.cos(2.0 * y)) - 2.0) / 16.0
+    rho = np.ones_like(u)
+    Q = single_species_state(rho, [u, v, w], p, gamma)
+    return np.ascontiguousarray(Q), dx
+
+
+def blobs_patches_3d(num_patches=512, side_lo=16, side_hi=64, seed=2, nblobs=32, gamma=1.4):
+    """Uneven 3D patches (side lengths U{lo..hi} per axis, seeded) holding a
+    density field of 32 Gaussian blobs on [0,1]^3 with smoothed random
+    velocity, p = 1.  Returns a list of (n[3], xlo[3], dx[3], state).  Half
+    the patches sit on a level with twice the spacing of the other half
+    (refinement ratio 2).
+    """
+    rng = np.random.default_rng(seed)
+    amps = rng.uniform(0.0, 0.5, nblobs)
+    widths = rng.uniform(0.02, 0.1, nblobs)
+    centres = rng.uniform(0.0, 1.0, (nblobs, 3))
+    patches = []
+    for p_i in range(num_patches):
+        n = [int(v) for v in rng.integers(side_lo, side_hi + 1, 3)]
+        level = 0 if p_i < num_patches // 2 else 1
+        h = (1.0 / 256.0) / (2 ** level)
+        xlo = [float(v) for v in rng.uniform(0.0, 1.0 - max(n) * h, 3)]
+        dx = [h, h, h]
+        X = _grid(n, xlo, dx, 3)
+        rho = np.ones_like(X[0])
+        for b in range(nblobs):
+            r2 = sum((X[d] - centres[b, d]) ** 2 for d in range(3))
+            rho = rho + amps[b] * np.exp(-r2 / widths[b] ** 2)
+        vel = []
+        for d in range(3):
+            f = rng.uniform(-0.5, 0.5, X[0].shape)
+            for _ in range(3):
+                f = (np.roll(f, 1, 0) + f + np.roll(f, -1, 0)) / 3.0
+                f = (np.roll(f, 1, 1) + f + np.roll(f, -1, 1)) / 3.0
+                f = (np.roll(f, 1, 2) + f + np.roll(f, -1, 2)) / 3.0
+            vel.append(f)
+        Q = single_species_state(rho, vel, np.ones_like(rho), gamma)
+        patches.append((n, xlo, dx, np.ascontiguousarray(Q)))
+    return patches

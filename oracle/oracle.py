@@ -1,0 +1,193 @@
+"""ctypes front end of the CPU oracle (test infrastructure only).
+
+The oracle restates the reference's FP64 hot path on the CPU; it is the
+checker for the GPU path and the CPU-baseline leg of bench.py.  Nothing in the
+hamers_gb300 package imports this module.
+
+Array conventions (SAMRAI layout, x fastest):
+  state  : numpy (ncomp, G[2], G[1], G[0]) with G = n + 2*4 on the used axes
+  flux   : list over axes a of numpy (neq, n2', n1', n0'), n grown by 1 along a
+  source : numpy (neq, n2, n1, n0)
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libhmr_oracle.so")
+
+MODEL_SINGLE_SPECIES = 0
+MODEL_FOUR_EQN_CONSERVATIVE = 1
+MODEL_FIVE_EQN_ALLAIRE = 2
+SCHEME_WCNS5_JS = 0
+SCHEME_WCNS6_LD = 1
+GHOST = 4
+
+
+class _Cfg(ctypes.Structure):
+    _fields_ = [("model", ctypes.c_int), ("dim", ctypes.c_int), ("num_species", ctypes.c_int),
+                ("scheme", ctypes.c_int), ("gamma", ctypes.c_double * 8), ("p", ctypes.c_int),
+                ("q", ctypes.c_int), ("C", ctypes.c_double), ("alpha_tau", ctypes.c_double)]
+
+
+def build():
+    """Compile the oracle library with its Makefile."""
+    subprocess.check_call(["make", "-s", "-C", _HERE])
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            build()
+        L = ctypes.CDLL(_LIB_PATH)
+        dp = ctypes.POINTER(ctypes.c_double)
+        ip = ctypes.POINTER(ctypes.c_int)
+        lp = ctypes.POINTER(ctypes.c_long)
+        cp = ctypes.POINTER(_Cfg)
+        L.hmro_conv_flux_source.argtypes = [cp, ip, dp, ctypes.c_double, dp, dp, dp, lp]
+        L.hmro_rk_stage.argtypes = [cp, ip, dp, ctypes.c_int, dp, dp, dp, dp, dp, dp, dp, dp, dp]
+        L.hmro_fill_ghosts.argtypes = [cp, ip, ip, dp]
+        L.hmro_rk3_advance.argtypes = [cp, ip, dp, ctypes.c_double, ip, ctypes.c_int, dp, lp]
+        L.hmro_stage_threads.argtypes = [cp, ip, dp, ctypes.c_double, dp, ctypes.c_int]
+        L.hmro_stage_threads.restype = ctypes.c_long
+        L.hmro_num_eqn.argtypes = [cp]
+        L.hmro_num_comp.argtypes = [cp]
+        _lib = L
+    return _lib
+
+
+class Config:
+    """Flow model + scheme selection (mirrors the reference's input keys)."""
+
+    def __init__(self, model, dim, species_gamma, scheme=SCHEME_WCNS5_JS,
+                 p=2, q=4, C=1.0e9, alpha_tau=35.0):
+        self.model = int(model)
+        self.dim = int(dim)
+        self.species_gamma = [float(g) for g in species_gamma]
+        self.num_species = len(self.species_gamma)
+        self.scheme = int(scheme)
+        self.p, self.q, self.C, self.alpha_tau = int(p), int(q), float(C), float(alpha_tau)
+
+    def c(self):
+        g = (ctypes.c_double * 8)(*(self.species_gamma + [0.0] * (8 - self.num_species)))
+        return _Cfg(self.model, self.dim, self.num_species, self.scheme, g, self.p, self.q,
+                    self.C, self.alpha_tau)
+
+    @property
+    def neq(self):
+        if self.model == MODEL_SINGLE_SPECIES:
+            return self.dim + 2
+        if self.model == MODEL_FOUR_EQN_CONSERVATIVE:
+            return self.num_species + self.dim + 1
+        return self.dim + 2 * self.num_species
+
+    @property
+    def ncomp(self):
+        return self.neq + (1 if self.model == MODEL_FIVE_EQN_ALLAIRE else 0)
+
+
+def _n3(n):
+    n = list(n)
+    return n + [1] * (3 - len(n))
+
+
+def ghost_shape(cfg, n):
+    n3 = _n3(n)
+    G = [n3[d] + 2 * GHOST if d < cfg.dim else 1 for d in range(3)]
+    return (cfg.ncomp, G[2], G[1], G[0])
+
+
+def flux_shapes(cfg, n):
+    n3 = _n3(n)
+    out = []
+    for a in range(cfg.dim):
+        e = [n3[d] + (1 if d == a else 0) for d in range(3)]
+        out.append((cfg.neq, e[2], e[1], e[0]))
+    return out
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _ip(v):
+    return (ctypes.c_int * len(v))(*v)
+
+
+def _dv(v):
+    return (ctypes.c_double * len(v))(*v)
+
+
+def conv_flux_source(cfg, n, dx, dt, Q, source=None):
+    """computeConvectiveFluxAndSourceOnPatch: returns (flux list, source, stats)."""
+    n3 = _n3(n)
+    Q = np.ascontiguousarray(Q, dtype=np.float64)
+    assert Q.shape == ghost_shape(cfg, n)
+    shapes = flux_shapes(cfg, n)
+    flat = np.zeros(sum(int(np.prod(s)) for s in shapes))
+    if source is None:
+        source = np.zeros((cfg.neq, n3[2], n3[1], n3[0]))
+    source = np.ascontiguousarray(source, dtype=np.float64)
+    stats = (ctypes.c_long * 3)()
+    lib().hmro_conv_flux_source(ctypes.byref(cfg.c()), _ip(n3), _dv(list(dx) + [1.0] * (3 - len(dx))),
+                                float(dt), _dp(Q), _dp(flat), _dp(source), stats)
+    out, off = [], 0
+    for s in shapes:
+        m = int(np.prod(s))
+        out.append(flat[off:off + m].reshape(s))
+        off += m
+    return out, source, (stats[0], stats[1], stats[2])
+
+
+def rk_stage(cfg, n, dx, alpha, beta, gamma, Q_int, F_int, S_int, F_acc=None, S_acc=None):
+    """advanceSingleStepOnPatch for one stage (len(alpha) coefficient sets)."""
+    n3 = _n3(n)
+    ns = len(alpha)
+    Qi = np.ascontiguousarray(np.stack(Q_int), dtype=np.float64)
+    Fi = np.ascontiguousarray(np.stack([np.concatenate([f.ravel() for f in F]) for F in F_int]))
+    Si = np.ascontiguousarray(np.stack(S_int), dtype=np.float64)
+    Qo = np.zeros(ghost_shape(cfg, n))
+    fa = None
+    if F_acc is not None:
+        fa = np.ascontiguousarray(np.concatenate([f.ravel() for f in F_acc]))
+    lib().hmro_rk_stage(ctypes.byref(cfg.c()), _ip(n3), _dv(list(dx) + [1.0] * (3 - len(dx))), ns,
+                        _dv(alpha), _dv(beta), _dv(gamma), _dp(Qi), _dp(Fi), _dp(Si), _dp(Qo),
+                        _dp(fa) if fa is not None else None,
+                        _dp(S_acc) if S_acc is not None else None)
+    if F_acc is not None:
+        off = 0
+        for f in F_acc:
+            f.ravel()[:] = fa[off:off + f.size]
+            off += f.size
+    return Qo
+
+
+def fill_ghosts(cfg, n, periodic, Q):
+    assert Q.flags["C_CONTIGUOUS"] and Q.dtype == np.float64
+    lib().hmro_fill_ghosts(ctypes.byref(cfg.c()), _ip(_n3(n)), _ip(list(periodic) + [0] * (3 - len(periodic))),
+                           _dp(Q))
+    return Q
+
+
+def rk3_advance(cfg, n, dx, dt, periodic, nsteps, Q):
+    """nsteps SSPRK3 steps of one patch, in place; returns the face counters."""
+    assert Q.flags["C_CONTIGUOUS"] and Q.dtype == np.float64
+    stats = (ctypes.c_long * 3)()
+    lib().hmro_rk3_advance(ctypes.byref(cfg.c()), _ip(_n3(n)), _dv(list(dx) + [1.0] * (3 - len(dx))),
+                           float(dt), _ip(list(periodic) + [0] * (3 - len(periodic))), int(nsteps),
+                           _dp(Q), stats)
+    return (stats[0], stats[1], stats[2])
+
+
+def stage_threads(cfg, n, dx, dt, Q, nthreads):
+    """One RK stage of a patch split into nthreads sub-patches; returns cells updated."""
+    Q = np.ascontiguousarray(Q, dtype=np.float64)
+    return lib().hmro_stage_threads(ctypes.byref(cfg.c()), _ip(_n3(n)),
+                                    _dv(list(dx) + [1.0] * (3 - len(dx))), float(dt), _dp(Q),
+                                    int(nthreads))
