@@ -1,0 +1,638 @@
+// C ABI of the GB300 convective hot path (declarations and contracts in include/hmr.h).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <new>
+#include <vector>
+
+#include "../../include/hmr.h"
+#include "hmr_launch.h"
+
+using namespace hmr;
+
+struct hmr_ctx {
+    Variant v;
+    Params P;
+    int precision;
+    int neq, ncomp;
+    double* scratch = nullptr;
+    size_t scratch_bytes = 0;
+    Counters* counters = nullptr;
+};
+
+struct hmr_level {
+    hmr_ctx* ctx;
+    int npatch;
+    std::vector<Geom> geoms;
+    std::vector<PatchWork> work;       // host copy
+    PatchWork* d_work = nullptr;       // 3 x npatch: the worklist of each stage
+    double* d_state = nullptr;         // stage slots 1 and 2 of every patch (slot 0 is bound by the caller)
+    double* d_scratch = nullptr;
+    std::vector<size_t> state_off;     // per patch, in doubles
+    LevelArgs L = {};
+    unsigned int* d_barrier = nullptr;
+    int* d_status = nullptr;
+    int threads = 128;
+    int blocks = 0;
+    // one captured graph per substep (barrier reset + persistent kernel)
+    cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
+    double graph_dt[3] = {0.0, 0.0, 0.0};
+    bool graph_ok[3] = {false, false, false};
+    bool dirty = true;                 // worklist changed since it was uploaded
+    int bound = 0;                     // patches whose slot 0 is bound
+};
+
+static int cuda_status(cudaError_t e) { return e == cudaSuccess ? HMR_OK : (int)e; }
+
+static inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+static Geom make_geom(int dim, const hmr_patch_geometry* pg) {
+    Geom g;
+    for (int d = 0; d < 3; d++) {
+        g.n[d] = d < dim ? pg->n[d] : 1;
+        g.G[d] = d < dim ? g.n[d] + 2 * GHOST : 1;
+        g.dx[d] = d < dim ? pg->dx[d] : 1.0;
+    }
+    return g;
+}
+
+static bool valid_geom(int dim, const hmr_patch_geometry* pg) {
+    if (!pg) return false;
+    for (int d = 0; d < dim; d++) {
+        if (pg->n[d] < 1 || pg->n[d] > (1 << 20)) return false;
+        if (!(pg->dx[d] > 0.0)) return false;
+    }
+    long cells = 1;
+    for (int d = 0; d < dim; d++) cells *= (long)pg->n[d] + 2 * GHOST;
+    return cells < (1L << 40);
+}
+
+// Scratch size in doubles for one patch.
+static size_t scratch_doubles(const hmr_ctx* c, const Geom& g) {
+    const long nc = ncell_of(g);
+    size_t s = (size_t)(c->neq + 4) * nc;
+    for (int a = 0; a < c->v.dim; a++) s += (size_t)(c->neq + 1) * nface_of(g, a);
+    return s + 64;
+}
+
+static Scratch carve_scratch(const hmr_ctx* c, const Geom& g, double* base) {
+    Scratch S;
+    const long nc = ncell_of(g);
+    double* p = base;
+    S.V = p; p += (size_t)c->neq * nc;
+    S.rho = p; p += nc;
+    S.cs = p; p += nc;
+    S.theta = p; p += nc;
+    S.Omega = p; p += nc;
+    for (int a = 0; a < 3; a++) {
+        if (a < c->v.dim) {
+            const long nf = nface_of(g, a);
+            S.Fm[a] = p; p += (size_t)c->neq * nf;
+            S.um[a] = p; p += nf;
+        } else {
+            S.Fm[a] = nullptr;
+            S.um[a] = nullptr;
+        }
+    }
+    return S;
+}
+
+static int ensure_scratch(hmr_ctx* c, const Geom& g) {
+    const size_t need = scratch_doubles(c, g) * sizeof(double);
+    if (need <= c->scratch_bytes) return HMR_OK;
+    if (c->scratch) cudaFree(c->scratch);
+    c->scratch = nullptr;
+    c->scratch_bytes = 0;
+    cudaError_t e = cudaMalloc(&c->scratch, need);
+    if (e != cudaSuccess) return cuda_status(e);
+    c->scratch_bytes = need;
+    return HMR_OK;
+}
+
+static int face_launch(hmr_ctx* c, const Geom& g, const Scratch& S, cudaStream_t st) {
+    if (c->precision == HMR_PRECISION_EXACT) return hmr_exact::launch_faces(c->v, c->P, g, S, c->counters, st);
+    return hmr_fast::launch_faces(c->v, c->P, g, S, c->counters, st);
+}
+
+static int update_launch(hmr_ctx* c, const Geom& g, const Scratch& S, const UpdateArgs& U, cudaStream_t st) {
+    if (c->precision == HMR_PRECISION_EXACT) return hmr_exact::launch_update(c->v, g, S, U, st);
+    return hmr_fast::launch_update(c->v, g, S, U, st);
+}
+
+template <class C>
+static bool load_ptrs(C& out, const double* const* ptrs, int n) {
+    constexpr int cap = (int)(sizeof(out.p) / sizeof(out.p[0]));
+    for (int e = 0; e < cap; e++) out.p[e] = nullptr;
+    if (!ptrs || n < 1 || n > cap) return false;
+    for (int e = 0; e < n; e++) {
+        if (!ptrs[e]) return false;
+        out.p[e] = const_cast<double*>(ptrs[e]);
+    }
+    return true;
+}
+static bool load_comp(Comp& C, const double* const* ptrs, int n) { return load_ptrs(C, ptrs, n); }
+static bool load_flux(FluxComp& C, const double* const* ptrs, int n) { return load_ptrs(C, ptrs, n); }
+
+extern "C" {
+
+int hmr_config_default(hmr_config* cfg, int flow_model, int reconstructor, int dim, int num_species) {
+    if (!cfg) return HMR_ERR_ARGUMENT;
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->flow_model = flow_model;
+    cfg->dim = dim;
+    cfg->num_species = num_species;
+    for (int s = 0; s < HMR_MAX_SPECIES; s++) {
+        cfg->species_gamma[s] = 1.4;
+        cfg->species_R[s] = 1.0;
+    }
+    cfg->convective_flux_reconstructor = reconstructor;
+    cfg->constant_p = 2;
+    cfg->constant_q = 4;
+    cfg->constant_C = 1.0e9;
+    cfg->constant_alpha_tau = 35.0;
+    cfg->precision = HMR_PRECISION_FAST;
+    return HMR_OK;
+}
+
+int hmr_ctx_create(const hmr_config* cfg, hmr_ctx** out) {
+    if (!cfg || !out) return HMR_ERR_ARGUMENT;
+    *out = nullptr;
+    if (cfg->dim != 2 && cfg->dim != 3) return HMR_ERR_ARGUMENT;
+    if (cfg->num_species < 1 || cfg->num_species > HMR_MAX_SPECIES) return HMR_ERR_ARGUMENT;
+    if (cfg->convective_flux_reconstructor != HMR_WCNS5_JS_HLLC_HLL &&
+        cfg->convective_flux_reconstructor != HMR_WCNS6_LD_HLLC_HLL)
+        return HMR_ERR_UNSUPPORTED;
+    if (cfg->precision != HMR_PRECISION_FAST && cfg->precision != HMR_PRECISION_EXACT) return HMR_ERR_ARGUMENT;
+    if (cfg->constant_p < 1 || cfg->constant_p > 8 || cfg->constant_q < 1 || cfg->constant_q > 8)
+        return HMR_ERR_ARGUMENT;
+    int neq = 0, ncomp = 0;
+    if (cfg->flow_model == HMR_SINGLE_SPECIES) {
+        if (cfg->num_species != 1) return HMR_ERR_ARGUMENT;
+        neq = cfg->dim + 2;
+        ncomp = neq;
+    } else if (cfg->flow_model == HMR_FIVE_EQN_ALLAIRE) {
+        if (cfg->num_species != 2) return HMR_ERR_UNSUPPORTED;
+        neq = cfg->dim + 2 * cfg->num_species;
+        ncomp = neq + 1;
+    } else {
+        return HMR_ERR_UNSUPPORTED;
+    }
+    for (int s = 0; s < cfg->num_species; s++)
+        if (!(cfg->species_gamma[s] > 1.0)) return HMR_ERR_ARGUMENT;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        cudaGetLastError();
+        return HMR_ERR_NO_DEVICE;
+    }
+    hmr_ctx* c = new (std::nothrow) hmr_ctx();
+    if (!c) return HMR_ERR_ARGUMENT;
+    c->v.dim = cfg->dim;
+    c->v.model = cfg->flow_model;
+    c->v.nsp = cfg->num_species;
+    c->v.scheme = cfg->convective_flux_reconstructor;
+    for (int s = 0; s < MAX_SPECIES; s++) {
+        c->P.gamma[s] = s < cfg->num_species ? cfg->species_gamma[s] : 1.4;
+        c->P.inv_gm1[s] = double(1)/(c->P.gamma[s] - double(1));
+    }
+    c->P.p = cfg->constant_p;
+    c->P.q = cfg->constant_q;
+    c->P.C = cfg->constant_C;
+    c->P.alpha_tau = cfg->constant_alpha_tau;
+    c->precision = cfg->precision;
+    c->neq = neq;
+    c->ncomp = ncomp;
+    cudaError_t e = cudaMalloc(&c->counters, sizeof(Counters));
+    if (e == cudaSuccess) e = cudaMemset(c->counters, 0, sizeof(Counters));
+    if (e != cudaSuccess) {
+        delete c;
+        return cuda_status(e);
+    }
+    *out = c;
+    return HMR_OK;
+}
+
+int hmr_ctx_destroy(hmr_ctx* c) {
+    if (!c) return HMR_ERR_ARGUMENT;
+    if (c->scratch) cudaFree(c->scratch);
+    if (c->counters) cudaFree(c->counters);
+    delete c;
+    return HMR_OK;
+}
+
+int hmr_num_equations(const hmr_ctx* c) { return c ? c->neq : HMR_ERR_ARGUMENT; }
+int hmr_num_components(const hmr_ctx* c) { return c ? c->ncomp : HMR_ERR_ARGUMENT; }
+int hmr_num_ghosts(const hmr_ctx* c) { return c ? GHOST : HMR_ERR_ARGUMENT; }
+
+int hmr_ctx_reserve(hmr_ctx* c, const hmr_patch_geometry* pg) {
+    if (!c || !valid_geom(c->v.dim, pg)) return HMR_ERR_ARGUMENT;
+    return ensure_scratch(c, make_geom(c->v.dim, pg));
+}
+
+int hmr_read_counters(hmr_ctx* c, unsigned long long out[2], int reset) {
+    if (!c || !out) return HMR_ERR_ARGUMENT;
+    Counters h;
+    cudaError_t e = cudaMemcpy(&h, c->counters, sizeof(h), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_status(e);
+    out[0] = h.fallback;
+    out[1] = h.hllc_hll;
+    if (reset) e = cudaMemset(c->counters, 0, sizeof(Counters));
+    return cuda_status(e);
+}
+
+// Cells + sensor + faces of one patch into the context scratch.
+static int patch_faces(hmr_ctx* c, const Geom& g, const Comp& Q, Scratch& S, cudaStream_t st) {
+    int r = ensure_scratch(c, g);
+    if (r) return r;
+    S = carve_scratch(c, g, c->scratch);
+    r = hmr_cells::launch_cells(c->v, c->P, g, Q, S, st);
+    if (r) return r;
+    r = hmr_cells::launch_sensor(c->v, g, S, st);
+    if (r) return r;
+    return face_launch(c, g, S, st);
+}
+
+int hmr_conv_flux_source_patch(hmr_ctx* c, const hmr_patch_geometry* pg, const double* const* Q, double dt,
+                               double* const* flux, double* const* source, void* stream) {
+    if (!c || !valid_geom(c->v.dim, pg)) return HMR_ERR_ARGUMENT;
+    Comp q, S;
+    FluxComp F;
+    if (!load_comp(q, Q, c->ncomp)) return HMR_ERR_ARGUMENT;
+    if (!load_flux(F, flux, c->v.dim * c->neq)) return HMR_ERR_ARGUMENT;
+    if (!load_comp(S, source, c->neq)) return HMR_ERR_ARGUMENT;
+    const Geom g = make_geom(c->v.dim, pg);
+    cudaStream_t st = as_stream(stream);
+    Scratch scr;
+    int r = patch_faces(c, g, q, scr, st);
+    if (r) return r;
+    UpdateArgs U;
+    std::memset(&U, 0, sizeof(U));
+    U.Qint[0] = q;
+    U.nst = 1;
+    U.alpha[0] = 0.0;
+    U.beta = 0.0;
+    U.dt = dt;
+    U.Fout = F;
+    U.Sout = S;
+    for (int e = 0; e < MAX_COMP; e++) U.Qout.p[e] = nullptr;
+    return update_launch(c, g, scr, U, st);
+}
+
+int hmr_rk_substep_patch(hmr_ctx* c, const hmr_patch_geometry* pg, int stage, const double* alpha, double beta,
+                         const double* const* const* Q_int, double dt, double* const* Q_out, void* stream) {
+    if (!c || !valid_geom(c->v.dim, pg) || !alpha || !Q_int || stage < 0 || stage > 2) return HMR_ERR_ARGUMENT;
+    UpdateArgs U;
+    std::memset(&U, 0, sizeof(U));
+    for (int s = 0; s <= stage; s++)
+        if (!load_comp(U.Qint[s], Q_int[s], c->ncomp)) return HMR_ERR_ARGUMENT;
+    if (!load_comp(U.Qout, Q_out, c->ncomp)) return HMR_ERR_ARGUMENT;
+    for (int s = 0; s <= stage; s++) U.alpha[s] = alpha[s];
+    U.nst = stage + 1;
+    U.beta = beta;
+    U.dt = dt;
+    for (int e = 0; e < 3 * MAX_COMP; e++) U.Fout.p[e] = nullptr;
+    for (int e = 0; e < MAX_COMP; e++) U.Sout.p[e] = nullptr;
+    const Geom g = make_geom(c->v.dim, pg);
+    cudaStream_t st = as_stream(stream);
+    Scratch scr;
+    int r = patch_faces(c, g, U.Qint[stage], scr, st);
+    if (r) return r;
+    return update_launch(c, g, scr, U, st);
+}
+
+int hmr_rk_stage_patch(hmr_ctx* c, const hmr_patch_geometry* pg, int ncoef, const double* alpha,
+                       const double* beta, const double* gamma, const double* const* const* Q_int,
+                       const double* const* const* F_int, const double* const* const* S_int, double* const* Q,
+                       double* const* flux_acc, double* const* source_acc, void* stream) {
+    if (!c || !valid_geom(c->v.dim, pg) || ncoef < 1 || ncoef > 4 || !alpha || !beta) return HMR_ERR_ARGUMENT;
+    if (!Q_int || !F_int || !S_int) return HMR_ERR_ARGUMENT;
+    Comp Qi[4], Si[4], Qo, Sa;
+    FluxComp Fi[4], Fa;
+    for (int n = 0; n < ncoef; n++) {
+        if (!load_comp(Qi[n], Q_int[n], c->ncomp)) return HMR_ERR_ARGUMENT;
+        if (!load_flux(Fi[n], F_int[n], c->v.dim * c->neq)) return HMR_ERR_ARGUMENT;
+        if (!load_comp(Si[n], S_int[n], c->neq)) return HMR_ERR_ARGUMENT;
+    }
+    if (!load_comp(Qo, Q, c->ncomp)) return HMR_ERR_ARGUMENT;
+    const bool acc = flux_acc != nullptr || source_acc != nullptr;
+    if (acc) {
+        if (!gamma || !load_flux(Fa, flux_acc, c->v.dim * c->neq) || !load_comp(Sa, source_acc, c->neq))
+            return HMR_ERR_ARGUMENT;
+    } else {
+        for (int e = 0; e < 3 * MAX_COMP; e++) Fa.p[e] = nullptr;
+        for (int e = 0; e < MAX_COMP; e++) Sa.p[e] = nullptr;
+    }
+    const Geom g = make_geom(c->v.dim, pg);
+    return hmr_cells::launch_rk_stage(c->v, g, ncoef, alpha, beta, acc ? gamma : nullptr, Qi, Fi, Si, Qo, Fa, Sa,
+                                      as_stream(stream));
+}
+
+int hmr_fill_ghosts_patch(hmr_ctx* c, const hmr_patch_geometry* pg, double* const* Q, const int* periodic,
+                          void* stream) {
+    if (!c || !valid_geom(c->v.dim, pg)) return HMR_ERR_ARGUMENT;
+    Comp q;
+    if (!load_comp(q, Q, c->ncomp)) return HMR_ERR_ARGUMENT;
+    const Geom g = make_geom(c->v.dim, pg);
+    return hmr_cells::launch_fill(c->v.dim, g, q, c->ncomp, periodic, as_stream(stream));
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batched level.
+// ---------------------------------------------------------------------------
+static const double RK3_ALPHA[3][3] = {{1.0, 0, 0}, {3.0/4.0, 1.0/4.0, 0}, {1.0/3.0, 0.0, 2.0/3.0}};
+static const double RK3_BETA[3] = {1.0, 1.0/4.0, 2.0/3.0};
+
+static int level_max_blocks(hmr_level* lv, int threads, int* blocks) {
+    hmr_ctx* c = lv->ctx;
+    if (c->precision == HMR_PRECISION_EXACT) return hmr_exact::level_max_blocks(c->v, threads, blocks);
+    return hmr_fast::level_max_blocks(c->v, threads, blocks);
+}
+
+static LevelArgs stage_args(hmr_level* lv, int stage, double dt) {
+    LevelArgs L = lv->L;
+    L.work = lv->d_work + (size_t)stage * lv->npatch;
+    for (int s = 0; s < 3; s++) L.alpha[s] = s <= stage ? RK3_ALPHA[stage][s] : 0.0;
+    L.nst = stage + 1;
+    L.beta = RK3_BETA[stage];
+    L.dt = dt;
+    L.barrier = lv->d_barrier;
+    L.status = lv->d_status;
+    return L;
+}
+
+// Barrier reset + persistent kernel of one substep, enqueued on st.
+static int level_enqueue(hmr_level* lv, int stage, double dt, int threads, int blocks, cudaStream_t st) {
+    hmr_ctx* c = lv->ctx;
+    cudaError_t e = cudaMemsetAsync(lv->d_barrier, 0, sizeof(unsigned int), st);
+    if (e != cudaSuccess) return cuda_status(e);
+    const LevelArgs L = stage_args(lv, stage, dt);
+    if (c->precision == HMR_PRECISION_EXACT) return hmr_exact::launch_level(c->v, c->P, L, blocks, threads, st);
+    return hmr_fast::launch_level(c->v, c->P, L, blocks, threads, st);
+}
+
+// Rebuilds the three per-stage worklists (they differ only in the output slot) and uploads them.
+static int level_upload(hmr_level* lv) {
+    std::vector<PatchWork> all((size_t)3 * lv->npatch);
+    for (int s = 0; s < 3; s++) {
+        const int out_slot = s == 2 ? 0 : s + 1;
+        for (int p = 0; p < lv->npatch; p++) {
+            PatchWork w = lv->work[p];
+            w.Qout = w.Q[out_slot];
+            all[(size_t)s * lv->npatch + p] = w;
+        }
+    }
+    cudaError_t e = cudaMemcpy(lv->d_work, all.data(), all.size() * sizeof(PatchWork), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_status(e);
+    lv->dirty = false;
+    for (int s = 0; s < 3; s++) lv->graph_ok[s] = false;
+    return HMR_OK;
+}
+
+static void level_drop_graphs(hmr_level* lv) {
+    for (int s = 0; s < 3; s++) {
+        if (lv->graph[s]) cudaGraphExecDestroy(lv->graph[s]);
+        lv->graph[s] = nullptr;
+        lv->graph_ok[s] = false;
+    }
+}
+
+// Captures (memset + persistent kernel) of one substep into a graph.
+static int level_capture(hmr_level* lv, int stage, double dt) {
+    if (lv->graph[stage]) {
+        cudaGraphExecDestroy(lv->graph[stage]);
+        lv->graph[stage] = nullptr;
+    }
+    cudaStream_t cs;
+    cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_status(e);
+    cudaGraph_t graph = nullptr;
+    int r = cuda_status(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    if (r == HMR_OK) {
+        r = level_enqueue(lv, stage, dt, lv->threads, lv->blocks, cs);
+        cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
+        if (r == HMR_OK && e2 != cudaSuccess) r = cuda_status(e2);
+    }
+    if (r == HMR_OK) {
+        e = cudaGraphInstantiate(&lv->graph[stage], graph, 0);
+        if (e != cudaSuccess) r = cuda_status(e);
+    }
+    if (graph) cudaGraphDestroy(graph);
+    cudaStreamDestroy(cs);
+    if (r == HMR_OK) {
+        lv->graph_ok[stage] = true;
+        lv->graph_dt[stage] = dt;
+    }
+    return r;
+}
+
+extern "C" {
+
+int hmr_level_create(hmr_ctx* c, int np, const hmr_patch_geometry* geoms, hmr_level** out) {
+    if (!c || np < 1 || !geoms || !out) return HMR_ERR_ARGUMENT;
+    *out = nullptr;
+    for (int p = 0; p < np; p++)
+        if (!valid_geom(c->v.dim, &geoms[p])) return HMR_ERR_ARGUMENT;
+    hmr_level* lv = new (std::nothrow) hmr_level();
+    if (!lv) return HMR_ERR_ARGUMENT;
+    lv->ctx = c;
+    lv->npatch = np;
+    size_t state_tot = 0, scratch_tot = 0;
+    std::vector<size_t> scr_off(np);
+    long off_fill = 0, off_cells = 0, off_sensor = 0, off_face[3] = {0, 0, 0}, off_update = 0;
+    lv->work.resize(np);
+    for (int p = 0; p < np; p++) {
+        const Geom g = make_geom(c->v.dim, &geoms[p]);
+        lv->geoms.push_back(g);
+        lv->state_off.push_back(state_tot);
+        state_tot += (size_t)2 * c->ncomp * ncell_of(g);
+        scr_off[p] = scratch_tot;
+        scratch_tot += (scratch_doubles(c, g) + 31) / 32 * 32;
+        PatchWork& w = lv->work[p];
+        w.g = g;
+        for (int a = 0; a < 3; a++) w.periodic[a] = 0;
+        w.off_fill = off_fill;
+        off_fill += ncell_of(g);
+        w.off_cells = off_cells;
+        off_cells += ncell_of(g);
+        w.off_sensor = off_sensor;
+        off_sensor += (long)(g.n[0] + 4) * (g.n[1] + 4) * (c->v.dim == 3 ? g.n[2] + 4 : 1);
+        for (int a = 0; a < 3; a++) {
+            w.off_face[a] = off_face[a];
+            if (a < c->v.dim) off_face[a] += nface_of(g, a);
+        }
+        w.off_update = off_update;
+        off_update += ninterior_of(g);
+    }
+    cudaError_t e = cudaMalloc(&lv->d_state, state_tot * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemset(lv->d_state, 0, state_tot * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&lv->d_scratch, scratch_tot * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&lv->d_work, (size_t)3 * np * sizeof(PatchWork));
+    if (e == cudaSuccess) e = cudaMalloc(&lv->d_barrier, sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMalloc(&lv->d_status, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(lv->d_status, 0, sizeof(int));
+    if (e != cudaSuccess) {
+        hmr_level_destroy(lv);
+        return cuda_status(e);
+    }
+    for (int p = 0; p < np; p++) {
+        PatchWork& w = lv->work[p];
+        const long nc = ncell_of(w.g);
+        w.S = carve_scratch(c, w.g, lv->d_scratch + scr_off[p]);
+        for (int comp = 0; comp < MAX_COMP; comp++) w.Q[0].p[comp] = nullptr;
+        for (int s = 1; s < 3; s++)
+            for (int comp = 0; comp < MAX_COMP; comp++)
+                w.Q[s].p[comp] = comp < c->ncomp
+                    ? lv->d_state + lv->state_off[p] + (size_t)(s - 1) * c->ncomp * nc + (size_t)comp * nc
+                    : nullptr;
+        w.Qout = w.Q[1];
+    }
+    lv->L.npatch = np;
+    lv->L.ncomp = c->ncomp;
+    lv->L.total_fill = off_fill;
+    lv->L.total_cells = off_cells;
+    lv->L.total_sensor = off_sensor;
+    for (int a = 0; a < 3; a++) lv->L.total_face[a] = off_face[a];
+    lv->L.total_update = off_update;
+    lv->L.timeout_ns = 2000000000ull;
+    lv->L.barrier_extra = 0;
+    lv->threads = 128;
+    int r = level_max_blocks(lv, lv->threads, &lv->blocks);
+    if (r || lv->blocks < 1) {
+        hmr_level_destroy(lv);
+        return r ? r : HMR_ERR_UNSUPPORTED;
+    }
+    *out = lv;
+    return HMR_OK;
+}
+
+int hmr_level_destroy(hmr_level* lv) {
+    if (!lv) return HMR_ERR_ARGUMENT;
+    level_drop_graphs(lv);
+    if (lv->d_state) cudaFree(lv->d_state);
+    if (lv->d_scratch) cudaFree(lv->d_scratch);
+    if (lv->d_work) cudaFree(lv->d_work);
+    if (lv->d_barrier) cudaFree(lv->d_barrier);
+    if (lv->d_status) cudaFree(lv->d_status);
+    delete lv;
+    return HMR_OK;
+}
+
+int hmr_level_bind_state(hmr_level* lv, int p, double* const* comps) {
+    if (!lv || p < 0 || p >= lv->npatch) return HMR_ERR_ARGUMENT;
+    Comp q;
+    if (!load_comp(q, comps, lv->ctx->ncomp)) return HMR_ERR_ARGUMENT;
+    if (lv->work[p].Q[0].p[0] == nullptr) lv->bound++;
+    lv->work[p].Q[0] = q;
+    lv->dirty = true;
+    return HMR_OK;
+}
+
+int hmr_level_set_periodic(hmr_level* lv, int p, const int* periodic) {
+    if (!lv || p < 0 || p >= lv->npatch || !periodic) return HMR_ERR_ARGUMENT;
+    for (int a = 0; a < 3; a++) lv->work[p].periodic[a] = a < lv->ctx->v.dim ? (periodic[a] != 0) : 0;
+    lv->dirty = true;
+    return HMR_OK;
+}
+
+int hmr_level_state(hmr_level* lv, int p, int slot, double** comps_out) {
+    if (!lv || p < 0 || p >= lv->npatch || slot < 0 || slot > 2 || !comps_out) return HMR_ERR_ARGUMENT;
+    for (int e = 0; e < lv->ctx->ncomp; e++) comps_out[e] = lv->work[p].Q[slot].p[e];
+    return HMR_OK;
+}
+
+int hmr_level_substep(hmr_level* lv, int stage, double dt, void* stream) {
+    if (!lv || stage < 0 || stage > 2) return HMR_ERR_ARGUMENT;
+    if (lv->bound != lv->npatch) return HMR_ERR_STATE;
+    if (lv->dirty) {
+        int r = level_upload(lv);
+        if (r) return r;
+    }
+    if (!lv->graph_ok[stage] || lv->graph_dt[stage] != dt) {
+        int r = level_capture(lv, stage, dt);
+        if (r) return r;
+    }
+    return cuda_status(cudaGraphLaunch(lv->graph[stage], as_stream(stream)));
+}
+
+int hmr_level_step(hmr_level* lv, double dt, void* stream) {
+    for (int s = 0; s < 3; s++) {
+        int r = hmr_level_substep(lv, s, dt, stream);
+        if (r) return r;
+    }
+    return HMR_OK;
+}
+
+int hmr_level_check(hmr_level* lv) {
+    if (!lv) return HMR_ERR_ARGUMENT;
+    int status = 0;
+    cudaError_t e = cudaMemcpy(&status, lv->d_status, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_status(e);
+    if (status) {
+        e = cudaMemset(lv->d_status, 0, sizeof(int));
+        if (e != cudaSuccess) return cuda_status(e);
+        return HMR_ERR_BARRIER;
+    }
+    return HMR_OK;
+}
+
+int hmr_level_barrier_diagnostic(hmr_level* lv, unsigned int extra_arrivals, unsigned long long timeout_ns) {
+    if (!lv || timeout_ns == 0 || timeout_ns > 10000000000ull || extra_arrivals > 1) return HMR_ERR_ARGUMENT;
+    lv->L.barrier_extra = extra_arrivals;
+    lv->L.timeout_ns = timeout_ns;
+    level_drop_graphs(lv);
+    return HMR_OK;
+}
+
+int hmr_level_autotune(hmr_level* lv, double dt, int* threads_out, int* bpsm_out, void* stream) {
+    if (!lv) return HMR_ERR_ARGUMENT;
+    if (lv->bound != lv->npatch) return HMR_ERR_STATE;
+    if (lv->dirty) {
+        int r = level_upload(lv);
+        if (r) return r;
+    }
+    cudaStream_t st = as_stream(stream);
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int cand_threads[3] = {64, 128, 256};
+    float best = 1e30f;
+    int best_t = lv->threads, best_b = lv->blocks;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    for (int ti = 0; ti < 3; ti++) {
+        const int t = cand_threads[ti];
+        int maxb = 0;
+        if (level_max_blocks(lv, t, &maxb) || maxb < 1) continue;
+        const int max_per_sm = std::max(1, maxb / sms);
+        for (int bps = 1; bps <= max_per_sm; bps++) {
+            // Substep 0 reads slot 0 and writes slot 1: repeated launches leave the state unchanged.
+            if (level_enqueue(lv, 0, dt, t, bps * sms, st)) continue;
+            cudaEventRecord(e0, st);
+            for (int rep = 0; rep < 2; rep++) level_enqueue(lv, 0, dt, t, bps * sms, st);
+            cudaEventRecord(e1, st);
+            if (cudaEventSynchronize(e1) != cudaSuccess) continue;
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms < best) {
+                best = ms;
+                best_t = t;
+                best_b = bps * sms;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (best_t != lv->threads || best_b != lv->blocks) level_drop_graphs(lv);
+    lv->threads = best_t;
+    lv->blocks = best_b;
+    if (threads_out) *threads_out = best_t;
+    if (bpsm_out) *bpsm_out = best_b / sms;
+    return hmr_level_check(lv);
+}
+
+}  // extern "C"

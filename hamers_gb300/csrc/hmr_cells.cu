@@ -1,0 +1,196 @@
+// Cell-centred kernels, always in the reference's operation order
+// (built with -DHMR_FAST=0 --fmad=false): derived cell data, shock-sensor
+// inputs, single-patch ghost fill and the general Runge-Kutta stage
+// combination of Euler::advanceSingleStepOnPatch (src/apps/Euler/Euler.cpp:1003-1680).
+#include <cuda_runtime.h>
+
+#include "hmr_launch.h"
+
+namespace hmr_cells {
+
+using namespace hmr;
+
+template <int D, int M, int N>
+struct VT {
+    static constexpr int DIM = D, MODEL = M, NSP = N;
+};
+
+template <class F>
+static int dispatch(const Variant& v, F f) {
+    if (v.model == SINGLE_SPECIES && v.nsp == 1) {
+        if (v.dim == 2) return f(VT<2, SINGLE_SPECIES, 1>{});
+        if (v.dim == 3) return f(VT<3, SINGLE_SPECIES, 1>{});
+    }
+    if (v.model == FIVE_EQN_ALLAIRE && v.nsp == 2) {
+        if (v.dim == 2) return f(VT<2, FIVE_EQN_ALLAIRE, 2>{});
+        if (v.dim == 3) return f(VT<3, FIVE_EQN_ALLAIRE, 2>{});
+    }
+    return -2;
+}
+
+constexpr int THREADS = 256;
+
+static inline int grid_for(long items) {
+    long b = (items + THREADS - 1) / THREADS;
+    if (b < 1) b = 1;
+    if (b > (1L << 30)) b = 1L << 30;
+    return (int)b;
+}
+
+template <int DIM, int MODEL, int NSP>
+__global__ void __launch_bounds__(THREADS) cells_kernel(Params P, Geom g, Comp Q, Scratch S) {
+    const long n = ncell_of(g);
+    for (long x = (long)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (long)gridDim.x * blockDim.x)
+        cells_item<DIM, MODEL, NSP>(P, g, Q, S, x);
+}
+
+template <int DIM, int MODEL, int NSP>
+__global__ void __launch_bounds__(THREADS) sensor_kernel(Geom g, Scratch S) {
+    const long n = (long)(g.n[0] + 4) * (g.n[1] + 4) * (DIM == 3 ? g.n[2] + 4 : 1);
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x)
+        sensor_item<DIM, MODEL, NSP>(g, S, t);
+}
+
+struct Periodic {
+    int p[3];
+};
+
+template <int DIM>
+__global__ void __launch_bounds__(THREADS) fill_kernel(Geom g, Comp Q, int ncomp, Periodic per) {
+    const long n = ncell_of(g);
+    for (long x = (long)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (long)gridDim.x * blockDim.x)
+        fill_item<DIM>(g, Q, ncomp, per.p, x);
+}
+
+int launch_cells(const Variant& v, const Params& P, const Geom& g, const Comp& Q, const Scratch& S,
+                 cudaStream_t st) {
+    return dispatch(v, [&](auto t) {
+        using T = decltype(t);
+        cells_kernel<T::DIM, T::MODEL, T::NSP><<<grid_for(ncell_of(g)), THREADS, 0, st>>>(P, g, Q, S);
+        return (int)cudaPeekAtLastError();
+    });
+}
+
+int launch_sensor(const Variant& v, const Geom& g, const Scratch& S, cudaStream_t st) {
+    return dispatch(v, [&](auto t) {
+        using T = decltype(t);
+        const long n = (long)(g.n[0] + 4) * (g.n[1] + 4) * (T::DIM == 3 ? g.n[2] + 4 : 1);
+        sensor_kernel<T::DIM, T::MODEL, T::NSP><<<grid_for(n), THREADS, 0, st>>>(g, S);
+        return (int)cudaPeekAtLastError();
+    });
+}
+
+int launch_fill(int dim, const Geom& g, const Comp& Q, int ncomp, const int* periodic, cudaStream_t st) {
+    Periodic per;
+    for (int a = 0; a < 3; a++) per.p[a] = periodic ? periodic[a] : 0;
+    if (dim == 2) fill_kernel<2><<<grid_for(ncell_of(g)), THREADS, 0, st>>>(g, Q, ncomp, per);
+    else fill_kernel<3><<<grid_for(ncell_of(g)), THREADS, 0, st>>>(g, Q, ncomp, per);
+    return (int)cudaPeekAtLastError();
+}
+
+// ---------------------------------------------------------------------------
+// General stage combination (any number of coefficient sets), one thread per
+// interior cell and equation set:  Q = 0; for n: Q += alpha_n Q_n;
+// Q += beta_n (-(F_R-F_L)/dx - ... + S_n); F += gamma_n F_n; S += gamma_n S_n.
+// ---------------------------------------------------------------------------
+struct StageArgs {
+    int ncoef;
+    double alpha[4], beta[4], gamma[4];
+    Comp Q[4];
+    FluxComp F[4];
+    Comp S[4];
+    Comp Qout;
+    FluxComp Facc;
+    Comp Sacc;
+};
+
+template <int DIM, int MODEL, int NSP>
+__global__ void __launch_bounds__(THREADS) rk_stage_kernel(Geom g, StageArgs A) {
+    using M = Model<DIM, MODEL, NSP>;
+    constexpr int NEQ = M::NEQ;
+    const long nint = ninterior_of(g);
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < nint; t += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % g.n[0]);
+        const int j = (int)((t / g.n[0]) % g.n[1]);
+        const int k = DIM == 3 ? (int)(t / ((long)g.n[0] * g.n[1])) : 0;
+        const long x = cidx<DIM>(g, i, j, k);
+        const long fx0 = side_idx<DIM, 0>(g, i, j, k), fx1 = side_idx<DIM, 0>(g, i + 1, j, k);
+        const long fy0 = side_idx<DIM, 1>(g, i, j, k), fy1 = side_idx<DIM, 1>(g, i, j + 1, k);
+        long fz0 = 0, fz1 = 0;
+        if (DIM == 3) { fz0 = side_idx<DIM, 2>(g, i, j, k); fz1 = side_idx<DIM, 2>(g, i, j, k + 1); }
+        double q[NEQ];
+#pragma unroll
+        for (int e = 0; e < NEQ; e++) q[e] = 0.0;
+        for (int n = 0; n < A.ncoef; n++) {
+            if (A.alpha[n] != 0.0) {
+#pragma unroll
+                for (int e = 0; e < NEQ; e++) q[e] = add_(q[e], mul_(A.alpha[n], A.Q[n].p[e][x]));
+            }
+            if (A.beta[n] != 0.0) {
+#pragma unroll
+                for (int e = 0; e < NEQ; e++) {
+                    const double* Fx = A.F[n].p[e];
+                    const double* Fy = A.F[n].p[NEQ + e];
+                    double div = sub_(-(Fx[fx1] - Fx[fx0])/g.dx[0], (Fy[fy1] - Fy[fy0])/g.dx[1]);
+                    if (DIM == 3) {
+                        const double* Fz = A.F[n].p[2 * NEQ + e];
+                        div = sub_(div, (Fz[fz1] - Fz[fz0])/g.dx[2]);
+                    }
+                    q[e] = add_(q[e], mul_(A.beta[n], add_(div, A.S[n].p[e][t])));
+                }
+                if (MODEL == FIVE_EQN_ALLAIRE) {
+                    double zl = 1.0;
+#pragma unroll
+                    for (int s = 0; s < NSP - 1; s++) zl = sub_(zl, q[M::IZ + s]);
+                    A.Qout.p[M::NCOMP - 1][x] = zl;
+                }
+            }
+            if (A.gamma[n] != 0.0 && A.Facc.p[0] != nullptr) {
+                // Time-integrated flux and source for refluxing (Euler.cpp:1420-1470 / 1560-1640).
+#pragma unroll
+                for (int e = 0; e < NEQ; e++) {
+                    double* Fx = A.Facc.p[e];
+                    double* Fy = A.Facc.p[NEQ + e];
+                    Fx[fx0] = add_(Fx[fx0], mul_(A.gamma[n], A.F[n].p[e][fx0]));
+                    if (i == g.n[0] - 1) Fx[fx1] = add_(Fx[fx1], mul_(A.gamma[n], A.F[n].p[e][fx1]));
+                    Fy[fy0] = add_(Fy[fy0], mul_(A.gamma[n], A.F[n].p[NEQ + e][fy0]));
+                    if (j == g.n[1] - 1) Fy[fy1] = add_(Fy[fy1], mul_(A.gamma[n], A.F[n].p[NEQ + e][fy1]));
+                    if (DIM == 3) {
+                        double* Fz = A.Facc.p[2 * NEQ + e];
+                        Fz[fz0] = add_(Fz[fz0], mul_(A.gamma[n], A.F[n].p[2 * NEQ + e][fz0]));
+                        if (k == g.n[2] - 1) Fz[fz1] = add_(Fz[fz1], mul_(A.gamma[n], A.F[n].p[2 * NEQ + e][fz1]));
+                    }
+                    A.Sacc.p[e][t] = add_(A.Sacc.p[e][t], mul_(A.gamma[n], A.S[n].p[e][t]));
+                }
+            }
+        }
+#pragma unroll
+        for (int e = 0; e < NEQ; e++) A.Qout.p[e][x] = q[e];
+    }
+}
+
+int launch_rk_stage(const Variant& v, const Geom& g, int ncoef, const double* alpha, const double* beta,
+                    const double* gamma, const Comp* Qint, const FluxComp* Fint, const Comp* Sint, const Comp& Qout,
+                    const FluxComp& Facc, const Comp& Sacc, cudaStream_t st) {
+    if (ncoef < 1 || ncoef > 4) return -1;
+    StageArgs A;
+    A.ncoef = ncoef;
+    for (int n = 0; n < ncoef; n++) {
+        A.alpha[n] = alpha[n];
+        A.beta[n] = beta[n];
+        A.gamma[n] = gamma ? gamma[n] : 0.0;
+        A.Q[n] = Qint[n];
+        A.F[n] = Fint[n];
+        A.S[n] = Sint[n];
+    }
+    A.Qout = Qout;
+    A.Facc = Facc;
+    A.Sacc = Sacc;
+    return dispatch(v, [&](auto t) {
+        using T = decltype(t);
+        rk_stage_kernel<T::DIM, T::MODEL, T::NSP><<<grid_for(ninterior_of(g)), THREADS, 0, st>>>(g, A);
+        return (int)cudaPeekAtLastError();
+    });
+}
+
+}  // namespace hmr_cells

@@ -1,0 +1,239 @@
+// Face and update kernels of one arithmetic form.  Built twice from this
+// file: -DHMR_FAST=0 --fmad=false (namespace hmr_exact) and -DHMR_FAST=1
+// (namespace hmr_fast).
+#include <cuda_runtime.h>
+
+#include "hmr_launch.h"
+
+#if HMR_FAST
+#define HMR_NS hmr_fast
+#else
+#define HMR_NS hmr_exact
+#endif
+
+namespace HMR_NS {
+
+using namespace hmr;
+
+template <int D, int M, int N, int S>
+struct VT {
+    static constexpr int DIM = D, MODEL = M, NSP = N, SCHEME = S;
+};
+
+template <class F>
+static int dispatch(const Variant& v, F f) {
+#define HMR_CASE(D_, M_, N_, S_) \
+    if (v.dim == D_ && v.model == M_ && v.nsp == N_ && v.scheme == S_) return f(VT<D_, M_, N_, S_>{});
+    HMR_CASE(2, SINGLE_SPECIES, 1, WCNS5_JS)
+    HMR_CASE(2, SINGLE_SPECIES, 1, WCNS6_LD)
+    HMR_CASE(3, SINGLE_SPECIES, 1, WCNS5_JS)
+    HMR_CASE(3, SINGLE_SPECIES, 1, WCNS6_LD)
+    HMR_CASE(2, FIVE_EQN_ALLAIRE, 2, WCNS5_JS)
+    HMR_CASE(2, FIVE_EQN_ALLAIRE, 2, WCNS6_LD)
+    HMR_CASE(3, FIVE_EQN_ALLAIRE, 2, WCNS5_JS)
+    HMR_CASE(3, FIVE_EQN_ALLAIRE, 2, WCNS6_LD)
+#undef HMR_CASE
+    return -2;
+}
+
+constexpr int FACE_THREADS = 128;
+constexpr int UPDATE_THREADS = 128;
+
+template <int DIM, int MODEL, int NSP, int SCHEME, int A>
+__global__ void __launch_bounds__(FACE_THREADS)
+faces_kernel(Params P, Geom g, Scratch S, Counters* cnt) {
+    const long nf = nface_of(g, A);
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < nf; t += (long)gridDim.x * blockDim.x)
+        face_item<DIM, MODEL, NSP, SCHEME, A>(P, g, S, t, cnt);
+}
+
+template <int DIM, int MODEL, int NSP>
+__global__ void __launch_bounds__(UPDATE_THREADS)
+update_kernel(Geom g, Scratch S, UpdateArgs U) {
+    const long n = ninterior_of(g);
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x)
+        update_item<DIM, MODEL, NSP>(g, S, U, t);
+}
+
+static inline int grid_for(long items, int threads) {
+    long b = (items + threads - 1) / threads;
+    if (b < 1) b = 1;
+    if (b > (1L << 30)) b = 1L << 30;
+    return (int)b;
+}
+
+int launch_faces(const Variant& v, const Params& P, const Geom& g, const Scratch& S, Counters* cnt,
+                 cudaStream_t st) {
+    return dispatch(v, [&](auto t) {
+        using T = decltype(t);
+        faces_kernel<T::DIM, T::MODEL, T::NSP, T::SCHEME, 0>
+            <<<grid_for(nface_of(g, 0), FACE_THREADS), FACE_THREADS, 0, st>>>(P, g, S, cnt);
+        faces_kernel<T::DIM, T::MODEL, T::NSP, T::SCHEME, 1>
+            <<<grid_for(nface_of(g, 1), FACE_THREADS), FACE_THREADS, 0, st>>>(P, g, S, cnt);
+        if constexpr (T::DIM == 3)
+            faces_kernel<T::DIM, T::MODEL, T::NSP, T::SCHEME, 2>
+                <<<grid_for(nface_of(g, 2), FACE_THREADS), FACE_THREADS, 0, st>>>(P, g, S, cnt);
+        return (int)cudaPeekAtLastError();
+    });
+}
+
+int launch_update(const Variant& v, const Geom& g, const Scratch& S, const UpdateArgs& U, cudaStream_t st) {
+    return dispatch(v, [&](auto t) {
+        using T = decltype(t);
+        update_kernel<T::DIM, T::MODEL, T::NSP>
+            <<<grid_for(ninterior_of(g), UPDATE_THREADS), UPDATE_THREADS, 0, st>>>(g, S, U);
+        return (int)cudaPeekAtLastError();
+    });
+}
+
+// ---------------------------------------------------------------------------
+// Batched form: one persistent kernel per RK substep over every patch of a
+// level.  Phases are separated by a grid barrier; inside a phase the items of
+// all patches form one flat index space that the resident blocks stride over,
+// so small and large patches share the SMs evenly.
+// ---------------------------------------------------------------------------
+
+// Grid barrier on a monotonically increasing arrival counter.  Barrier number
+// b (1-based) is passed when the counter reaches b*gridDim.x.  The wait is
+// bounded: after timeout_ns it raises the status flag and returns false, and
+// every later barrier of the launch returns false at once, so all blocks
+// leave the kernel.  `extra` > 0 makes the target unreachable (used only by
+// the test that checks this give-up path).
+__device__ __forceinline__ bool grid_barrier(unsigned int* counter, int* status, unsigned int b,
+                                             unsigned long long timeout_ns, unsigned int extra) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(counter, 1u);
+        const unsigned int target = b * (gridDim.x + extra);
+        unsigned long long t0;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+        int ok = 1;
+        while (true) {
+            const unsigned int c = *((volatile unsigned int*)counter);
+            if (c >= target) break;
+            if (*((volatile int*)status) != 0) { ok = 0; break; }
+            unsigned long long t1;
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
+            if (t1 - t0 > timeout_ns) {
+                atomicExch(status, 1);
+                ok = 0;
+                break;
+            }
+            __nanosleep(64);
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// Patch holding flat item t of a phase (prefix offsets, binary search).
+template <class OffF>
+__device__ __forceinline__ int find_patch(const PatchWork* W, int np, long t, OffF off) {
+    int lo = 0, hi = np - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (off(W[mid]) <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+constexpr int LEVEL_MAX_THREADS = 256;
+
+template <int DIM, int MODEL, int NSP, int SCHEME>
+__global__ void __launch_bounds__(LEVEL_MAX_THREADS)
+level_kernel(Params P, LevelArgs L) {
+    const long stride = (long)gridDim.x * blockDim.x;
+    const long t0 = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const PatchWork* W = L.work;
+    const int np = L.npatch;
+    unsigned int b = 0;
+#define HMR_BARRIER() \
+    if (!grid_barrier(L.barrier, L.status, ++b, L.timeout_ns, L.barrier_extra)) return
+
+    // Phase 0: ghost fill of the input stage (periodic or zero-gradient per patch).
+    for (long t = t0; t < L.total_fill; t += stride) {
+        const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_fill; });
+        fill_item<DIM>(W[p].g, W[p].Q[L.nst - 1], L.ncomp, W[p].periodic, t - W[p].off_fill);
+    }
+    HMR_BARRIER();
+    for (long t = t0; t < L.total_cells; t += stride) {
+        const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_cells; });
+        cells_item<DIM, MODEL, NSP>(P, W[p].g, W[p].Q[L.nst - 1], W[p].S, t - W[p].off_cells);
+    }
+    HMR_BARRIER();
+    for (long t = t0; t < L.total_sensor; t += stride) {
+        const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_sensor; });
+        sensor_item<DIM, MODEL, NSP>(W[p].g, W[p].S, t - W[p].off_sensor);
+    }
+    HMR_BARRIER();
+    for (long t = t0; t < L.total_face[0]; t += stride) {
+        const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_face[0]; });
+        face_item<DIM, MODEL, NSP, SCHEME, 0>(P, W[p].g, W[p].S, t - W[p].off_face[0], nullptr);
+    }
+    for (long t = t0; t < L.total_face[1]; t += stride) {
+        const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_face[1]; });
+        face_item<DIM, MODEL, NSP, SCHEME, 1>(P, W[p].g, W[p].S, t - W[p].off_face[1], nullptr);
+    }
+    if constexpr (DIM == 3) {
+        for (long t = t0; t < L.total_face[2]; t += stride) {
+            const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_face[2]; });
+            face_item<DIM, MODEL, NSP, SCHEME, 2>(P, W[p].g, W[p].S, t - W[p].off_face[2], nullptr);
+        }
+    }
+    HMR_BARRIER();
+#undef HMR_BARRIER
+    for (long t = t0; t < L.total_update; t += stride) {
+        const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_update; });
+        const PatchWork& w = W[p];
+        UpdateArgs U;
+        for (int s = 0; s < 3; s++) U.Qint[s] = w.Q[s];
+        for (int s = 0; s < 3; s++) U.alpha[s] = L.alpha[s];
+        U.nst = L.nst;
+        U.beta = L.beta;
+        U.dt = L.dt;
+        U.Qout = w.Qout;
+        U.Fout.p[0] = nullptr;   // flux/source outputs are not produced by the batched form
+        U.Sout.p[0] = nullptr;
+        update_item<DIM, MODEL, NSP>(w.g, w.S, U, t - w.off_update);
+    }
+}
+
+int level_max_blocks(const Variant& v, int threads, int* blocks) {
+    return dispatch(v, [&](auto t) {
+        using T = decltype(t);
+        int per_sm = 0;
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &per_sm, level_kernel<T::DIM, T::MODEL, T::NSP, T::SCHEME>, threads, 0);
+        if (e != cudaSuccess) return (int)e;
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        *blocks = per_sm * sms;
+        return 0;
+    });
+}
+
+int launch_level(const Variant& v, const Params& P, const LevelArgs& L, int blocks, int threads,
+                 cudaStream_t st) {
+    return dispatch(v, [&](auto t) {
+        using T = decltype(t);
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(blocks);
+        cfg.blockDim = dim3(threads);
+        cfg.dynamicSmemBytes = 0;
+        cfg.stream = st;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        return (int)cudaLaunchKernelEx(&cfg, level_kernel<T::DIM, T::MODEL, T::NSP, T::SCHEME>, P, L);
+    });
+}
+
+}  // namespace HMR_NS

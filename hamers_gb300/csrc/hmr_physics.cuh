@@ -1,0 +1,691 @@
+// Device physics of the WCNS56 / HLLC-HLL convective path (FP64).
+//
+// Model and scheme are template parameters so every variant compiles to
+// straight-line register code.  HMR_FAST selects the arithmetic form:
+//   HMR_FAST == 0 : the reference's operation order, built with --fmad=false;
+//                   results are bitwise equal to the CPU oracle.
+//   HMR_FAST == 1 : algebraically regrouped (shared reciprocals, single
+//                   normalisations) and FMA-contracted; agrees with the
+//                   reference to rounding (<= 1e-12 relative).
+// Formulas and the reference lines they follow:
+//   WCNS5-JS  src/flow/convective_flux_reconstructors/WCNS56/ConvectiveFluxReconstructorWCNS5-JS-HLLC-HLL.cpp:24-164
+//   WCNS6-LD  src/flow/convective_flux_reconstructors/WCNS56/ConvectiveFluxReconstructorWCNS6-LD-HLLC-HLL.cpp:24-319
+//   projection / characteristic transforms / bounds
+//             src/flow/flow_models/single-species/FlowModelBasicUtilitiesSingleSpecies.cpp:3013,4638,5882,7023
+//             src/flow/flow_models/five-eqn_Allaire/FlowModelBasicUtilitiesFiveEqnAllaire.cpp:5446,7474,8232,9201
+//   HLLC, HLLC-HLL
+//             src/flow/flow_models/single-species/Riemann_solvers/FlowModelRiemannSolverSingleSpeciesHLLC-HLL.cpp:889-1027
+//             src/flow/flow_models/five-eqn_Allaire/Riemann_solvers/FlowModelRiemannSolverFiveEqnAllaireHLLC-HLL.cpp:1283-1503
+//   ideal-gas EOS and volume-fraction mixing rule
+//             src/util/mixing_rules/equations_of_state/ideal_gas/EquationOfStateIdealGas.cpp:29-43,561-575,1093-1107
+//             src/util/mixing_rules/equations_of_state/ideal_gas/EquationOfStateMixingRulesIdealGas.cpp:7404-7800
+#pragma once
+
+#ifndef HMR_FAST
+#define HMR_FAST 1
+#endif
+
+#define HMR_EPS 1.0e-15  // HAMERS_EPSILON
+
+namespace hmr {
+
+enum { SINGLE_SPECIES = 0, FOUR_EQN_CONSERVATIVE = 1, FIVE_EQN_ALLAIRE = 2 };
+enum { WCNS5_JS = 0, WCNS6_LD = 1 };
+
+constexpr int MAX_SPECIES = 4;
+constexpr int MAX_COMP = 12;
+
+// Scheme and species constants shared by every kernel of a context.
+struct Params {
+    double gamma[MAX_SPECIES];         // species_gamma
+    double inv_gm1[MAX_SPECIES];       // 1/(gamma_i - 1)
+    int p, q;                          // WCNS constants
+    double C, alpha_tau;
+};
+
+template <int DIM, int MODEL, int NSP>
+struct Model {
+    static constexpr int NEQ = MODEL == SINGLE_SPECIES ? DIM + 2
+                             : (MODEL == FIVE_EQN_ALLAIRE ? DIM + 2 * NSP : NSP + DIM + 1);
+    static constexpr int NCOMP = NEQ + (MODEL == FIVE_EQN_ALLAIRE ? 1 : 0);
+    static constexpr int IU = MODEL == SINGLE_SPECIES ? 1 : NSP;            // first velocity in V
+    static constexpr int IP = MODEL == SINGLE_SPECIES ? DIM + 1 : NSP + DIM; // pressure in V
+    static constexpr int IZ = NSP + DIM + 1;                                  // first volume fraction in V (five)
+    static constexpr int NPROJ = MODEL == SINGLE_SPECIES ? 2 : NSP + 2;
+    static constexpr int IE = MODEL == SINGLE_SPECIES ? DIM + 1 : NSP + DIM; // total energy in Q
+};
+
+__device__ __forceinline__ double ipow_d(double b, int e) {
+    double r = b;
+    for (int i = 1; i < e; i++) r *= b;
+    return r;
+}
+
+// ----------------------------------------------------------------------------
+// Mixture gamma from volume fractions.
+// ----------------------------------------------------------------------------
+template <int NSP>
+__device__ __forceinline__ double gamma_all(const Params& P, const double* Z) {
+    double xi = 0.0;
+#pragma unroll
+    for (int s = 0; s < NSP; s++) xi += Z[s]*P.inv_gm1[s];
+    return double(1)/xi + double(1);
+}
+
+template <int NSP>
+__device__ __forceinline__ double gamma_last(const Params& P, const double* Z /* NSP-1 */) {
+    double xi = 0.0;
+    double Zl = 1.0;
+#pragma unroll
+    for (int s = 0; s < NSP - 1; s++) {
+        xi += Z[s]*P.inv_gm1[s];
+        Zl -= Z[s];
+    }
+    xi += Zl/(P.gamma[NSP - 1] - double(1));
+    return double(1)/xi + double(1);
+}
+
+// ----------------------------------------------------------------------------
+// Cell derived data: primitive variables V, density, sound speed.
+// single: FlowModelSingleSpecies.cpp:2649-3180; five: FlowModelFiveEqnAllaire.cpp:3734-4877.
+// Always evaluated in the reference's operation order with explicitly
+// rounded products (never contracted into FMAs), in both arithmetic forms:
+// the shock sensor is built from these values, and identical inputs keep
+// its HLLC / HLLC-HLL choice identical between the exact and fast forms.
+// ----------------------------------------------------------------------------
+__device__ __forceinline__ double mul_(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double add_(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub_(double a, double b) { return __dsub_rn(a, b); }
+
+template <int NSP>
+__device__ __forceinline__ double gamma_all_x(const Params& P, const double* Z) {
+    double xi = 0.0;
+#pragma unroll
+    for (int s = 0; s < NSP; s++) xi = add_(xi, mul_(Z[s], P.inv_gm1[s]));
+    return add_(double(1)/xi, double(1));
+}
+
+template <int DIM, int MODEL, int NSP>
+__device__ __forceinline__ void cell_derived(const Params& P, const double* Q, double* V,
+                                             double& rho, double& cs) {
+    using M = Model<DIM, MODEL, NSP>;
+    if constexpr (MODEL == SINGLE_SPECIES) {
+        const double gamma = P.gamma[0];
+        rho = Q[0];
+        double u[DIM];
+#pragma unroll
+        for (int k = 0; k < DIM; k++) u[k] = Q[1 + k]/rho;
+        double ke = mul_(u[0], u[0]);
+#pragma unroll
+        for (int k = 1; k < DIM; k++) ke = add_(ke, mul_(u[k], u[k]));
+        const double eps = sub_(Q[DIM + 1]/rho, mul_(double(1)/double(2), ke));
+        const double p = mul_(mul_(sub_(gamma, double(1)), rho), eps);
+        cs = sqrt(mul_(gamma, p)/rho);
+        V[0] = rho;
+#pragma unroll
+        for (int k = 0; k < DIM; k++) V[1 + k] = u[k];
+        V[DIM + 1] = p;
+    } else {
+        double r = 0.0;
+#pragma unroll
+        for (int s = 0; s < NSP; s++) r = add_(r, Q[s]);
+        rho = r;
+        double Y[NSP];
+        double u[DIM];
+#pragma unroll
+        for (int s = 0; s < NSP; s++) Y[s] = Q[s]/r;
+#pragma unroll
+        for (int k = 0; k < DIM; k++) u[k] = Q[NSP + k]/r;
+        double ke = mul_(u[0], u[0]);
+#pragma unroll
+        for (int k = 1; k < DIM; k++) ke = add_(ke, mul_(u[k], u[k]));
+        double Z[NSP];
+#pragma unroll
+        for (int s = 0; s < NSP; s++) Z[s] = Q[M::IZ + s];
+        const double gamma = gamma_all_x<NSP>(P, Z);
+        const double eps = sub_(Q[NSP + DIM]/r, mul_(double(1)/double(2), ke));
+        const double p = mul_(mul_(sub_(gamma, double(1)), r), eps);
+        const double Gamma = sub_(gamma, double(1));
+        const double Psi = p/r;
+        double c2 = mul_(Gamma, p)/r;
+#pragma unroll
+        for (int s = 0; s < NSP; s++) c2 = add_(c2, mul_(Y[s], Psi));
+        cs = sqrt(c2);
+#pragma unroll
+        for (int s = 0; s < NSP; s++) V[s] = Q[s];
+#pragma unroll
+        for (int k = 0; k < DIM; k++) V[NSP + k] = u[k];
+        V[NSP + DIM] = p;
+#pragma unroll
+        for (int s = 0; s < NSP - 1; s++) V[M::IZ + s] = Z[s];
+    }
+}
+
+// ----------------------------------------------------------------------------
+// Characteristic projection of one cell's primitive state for a face normal to A.
+// ----------------------------------------------------------------------------
+template <int DIM, int MODEL, int NSP>
+struct FaceProj {
+    // exact form keeps the projection means; fast form keeps derived factors
+    double rb, cb;
+    double zb[NSP];
+#if HMR_FAST
+    double hrc;      // 1/2*rb*cb
+    double ic2;      // 1/(cb*cb)
+    double irc;      // 1/(rb*cb)
+    double zr[NSP];  // zb/(rb*cb*cb)
+    double hz[NSP];  // 1/2*zb/cb
+#endif
+};
+
+template <int DIM, int MODEL, int NSP>
+__device__ __forceinline__ void face_proj_setup(FaceProj<DIM, MODEL, NSP>& F) {
+#if HMR_FAST
+    if constexpr (MODEL == SINGLE_SPECIES) {
+        F.hrc = double(1)/double(2)*F.rb*F.cb;
+        F.ic2 = double(1)/(F.cb*F.cb);
+        F.irc = double(1)/(F.rb*F.cb);
+    } else {
+        F.hrc = double(1)/double(2)*F.rb*F.cb;
+        const double irc = double(1)/(F.rb*F.cb);
+        F.irc = irc;
+        const double icb = irc*F.rb;          // 1/cb
+#pragma unroll
+        for (int s = 0; s < NSP; s++) {
+            F.zr[s] = F.zb[s]*irc*icb;
+            F.hz[s] = double(1)/double(2)*F.zb[s]*icb;
+        }
+    }
+#endif
+}
+
+template <int DIM, int MODEL, int NSP, int A>
+__device__ __forceinline__ void char_from_prim(const FaceProj<DIM, MODEL, NSP>& F, const double* V, double* W) {
+    using M = Model<DIM, MODEL, NSP>;
+    if constexpr (MODEL == SINGLE_SPECIES) {
+        const double un = V[1 + A];
+        const double p = V[DIM + 1];
+#if HMR_FAST
+        const double hp = double(1)/double(2)*p;
+        W[0] = hp - F.hrc*un;
+        W[1] = V[0] - F.ic2*p;
+        W[DIM + 1] = hp + F.hrc*un;
+#else
+        W[0] = -double(1)/double(2)*F.rb*F.cb*un + double(1)/double(2)*p;
+        W[1] = V[0] - double(1)/(F.cb*F.cb)*p;
+        W[DIM + 1] = double(1)/double(2)*F.rb*F.cb*un + double(1)/double(2)*p;
+#endif
+        int t = 2;
+#pragma unroll
+        for (int k = 0; k < DIM; k++) if (k != A) W[t++] = V[1 + k];
+    } else {
+        const double un = V[NSP + A];
+        const double p = V[NSP + DIM];
+#pragma unroll
+        for (int s = 0; s < NSP; s++) {
+#if HMR_FAST
+            W[1 + s] = V[s] - F.zr[s]*p;
+#else
+            W[1 + s] = V[s] - F.zb[s]/(F.rb*F.cb*F.cb)*p;
+#endif
+        }
+#pragma unroll
+        for (int s = 0; s < NSP - 1; s++) W[NSP + DIM + s] = V[M::IZ + s];
+#if HMR_FAST
+        W[0] = un - F.irc*p;
+        W[M::NEQ - 1] = un + F.irc*p;
+#else
+        W[0] = un - double(1)/(F.rb*F.cb)*p;
+        W[M::NEQ - 1] = un + double(1)/(F.rb*F.cb)*p;
+#endif
+        int t = NSP + 1;
+#pragma unroll
+        for (int k = 0; k < DIM; k++) if (k != A) W[t++] = V[NSP + k];
+    }
+}
+
+template <int DIM, int MODEL, int NSP, int A>
+__device__ __forceinline__ void prim_from_char(const FaceProj<DIM, MODEL, NSP>& F, const double* W, double* V) {
+    using M = Model<DIM, MODEL, NSP>;
+    constexpr int L = M::NEQ - 1;
+    if constexpr (MODEL == SINGLE_SPECIES) {
+#if HMR_FAST
+        V[0] = F.ic2*(W[0] + W[L]) + W[1];
+        V[1 + A] = F.irc*(W[L] - W[0]);
+#else
+        V[0] = double(1)/(F.cb*F.cb)*W[0] + W[1] + double(1)/(F.cb*F.cb)*W[L];
+        V[1 + A] = -double(1)/(F.rb*F.cb)*W[0] + double(1)/(F.rb*F.cb)*W[L];
+#endif
+        int t = 2;
+#pragma unroll
+        for (int k = 0; k < DIM; k++) if (k != A) V[1 + k] = W[t++];
+        V[DIM + 1] = W[0] + W[L];
+    } else {
+#pragma unroll
+        for (int s = 0; s < NSP; s++) {
+#if HMR_FAST
+            V[s] = F.hz[s]*(W[L] - W[0]) + W[s + 1];
+#else
+            V[s] = -double(1)/double(2)*F.zb[s]/F.cb*W[0] + W[s + 1] +
+                double(1)/double(2)*F.zb[s]/F.cb*W[L];
+#endif
+        }
+#pragma unroll
+        for (int s = 0; s < NSP - 1; s++) V[M::IZ + s] = W[NSP + DIM + s];
+        int t = NSP + 1;
+#pragma unroll
+        for (int k = 0; k < DIM; k++) {
+            if (k == A) {
+#if HMR_FAST
+                V[NSP + k] = double(1)/double(2)*(W[0] + W[L]);
+#else
+                V[NSP + k] = double(1)/double(2)*W[0] + double(1)/double(2)*W[L];
+#endif
+            } else {
+                V[NSP + k] = W[t++];
+            }
+        }
+#if HMR_FAST
+        V[NSP + DIM] = F.hrc*(W[L] - W[0]);
+#else
+        V[NSP + DIM] = -double(1)/double(2)*F.rb*F.cb*W[0] + double(1)/double(2)*F.rb*F.cb*W[L];
+#endif
+    }
+}
+
+// ----------------------------------------------------------------------------
+// WCNS5-JS (U[m] = characteristic variable at cell face-3+m).
+// ----------------------------------------------------------------------------
+__device__ __forceinline__ void js_betas(const double* U, double& b0, double& b1, double& b2) {
+    b0 = double(1)/double(3)*(U[0]*(double(4)*U[0] - double(19)*U[1] + double(11)*U[2]) +
+         U[1]*(double(25)*U[1] - double(31)*U[2]) + double(10)*U[2]*U[2]);
+    b1 = double(1)/double(3)*(U[1]*(double(4)*U[1] - double(13)*U[2] + double(5)*U[3]) +
+         double(13)*U[2]*(U[2] - U[3]) + double(4)*U[3]*U[3]);
+    b2 = double(1)/double(3)*(U[2]*(double(10)*U[2] - double(31)*U[3] + double(11)*U[4]) +
+         U[3]*(double(25)*U[3] - double(19)*U[4]) + double(4)*U[4]*U[4]);
+}
+
+__device__ __forceinline__ void js_betas_tilde(const double* U, double& b0, double& b1, double& b2) {
+    b0 = double(1)/double(3)*(U[5]*(double(4)*U[5] - double(19)*U[4] + double(11)*U[3]) +
+         U[4]*(double(25)*U[4] - double(31)*U[3]) + double(10)*U[3]*U[3]);
+    b1 = double(1)/double(3)*(U[4]*(double(4)*U[4] - double(13)*U[3] + double(5)*U[2]) +
+         double(13)*U[3]*(U[3] - U[2]) + double(4)*U[2]*U[2]);
+    b2 = double(1)/double(3)*(U[3]*(double(10)*U[3] - double(31)*U[2] + double(11)*U[1]) +
+         U[2]*(double(25)*U[2] - double(19)*U[1]) + double(4)*U[1]*U[1]);
+}
+
+// Weighted 5-point midpoint value: S0..S4 are the stencil values ordered from
+// the upwind side (U[0..4] for the minus side, U[5..1] for the plus side).
+__device__ __forceinline__ double js_interp(double b0, double b1, double b2, int p,
+                                            double S0, double S1, double S2, double S3, double S4) {
+#if HMR_FAST
+    // w_k = d_k/(b_k+eps)^p / sum_j d_j/(b_j+eps)^p, evaluated with one reciprocal.
+    const double e0 = ipow_d(b0 + HMR_EPS, p), e1 = ipow_d(b1 + HMR_EPS, p), e2 = ipow_d(b2 + HMR_EPS, p);
+    const double a0 = double(1)/double(16)*(e1*e2);
+    const double a1 = double(5)/double(8)*(e0*e2);
+    const double a2 = double(5)/double(16)*(e0*e1);
+    const double r = double(1)/(a0 + a1 + a2);
+    const double w0 = a0*r, w1 = a1*r, w2 = a2*r;
+#else
+    double w0 = double(1.0)/double(16)/ipow_d(b0 + HMR_EPS, p);
+    double w1 = double(5.0)/double(8)/ipow_d(b1 + HMR_EPS, p);
+    double w2 = double(5.0)/double(16)/ipow_d(b2 + HMR_EPS, p);
+    const double ws = w0 + w1 + w2;
+    w0 = w0/ws; w1 = w1/ws; w2 = w2/ws;
+#endif
+    return double(3)/double(8)*w0*S0 +
+        (-double(10)/double(8)*w0 - double(1)/double(8)*w1)*S1 +
+        (double(15)/double(8)*w0 + double(6)/double(8)*w1 + double(3)/double(8)*w2)*S2 +
+        (double(3)/double(8)*w1 + double(6)/double(8)*w2)*S3 -
+        double(1)/double(8)*w2*S4;
+}
+
+__device__ __forceinline__ void js_pair(const double* U, int p, double& Um, double& Up) {
+    double b0, b1, b2;
+    js_betas(U, b0, b1, b2);
+    Um = js_interp(b0, b1, b2, p, U[0], U[1], U[2], U[3], U[4]);
+    js_betas_tilde(U, b0, b1, b2);
+    Up = js_interp(b0, b1, b2, p, U[5], U[4], U[3], U[2], U[1]);
+}
+
+// ----------------------------------------------------------------------------
+// WCNS6-LD.
+// ----------------------------------------------------------------------------
+__device__ __forceinline__ double ld_sigma(const double* U) {
+    const double a1 = U[2] - U[1];
+    const double a2 = U[3] - U[2];
+    const double a3 = U[4] - U[3];
+    const double t1 = fabs(a1 - a2)/(fabs(a1) + fabs(a2) + HMR_EPS);
+    const double t2 = fabs(a2 - a3)/(fabs(a2) + fabs(a3) + HMR_EPS);
+    return fmax(t1, t2);
+}
+
+// beta_3 with the stencil ordered from the upwind side (S0..S5).
+__device__ __forceinline__ double ld_beta3(double S0, double S1, double S2, double S3, double S4, double S5) {
+    return double(1)/double(232243200)*(S0*(double(525910327)*S0 -
+         double(4562164630)*S1 + double(7799501420)*S2 -
+         double(6610694540)*S3 + double(2794296070)*S4 -
+         double(472758974)*S5) + double(5)*S1*
+        (double(2146987907)*S1 - double(7722406988)*S2 +
+         double(6763559276)*S3 - double(2926461814)*S4 +
+         double(503766638)*S5) + double(20)*S2*
+        (double(1833221603)*S2 - double(3358664662)*S3 +
+         double(1495974539)*S4 - double(263126407)*S5) +
+        double(20)*S3*(double(1607794163)*S3 -
+         double(1486026707)*S4 + double(268747951)*S5) +
+        double(5)*S4*(double(1432381427)*S4 -
+         double(536951582)*S5) +
+        double(263126407)*S5*S5);
+}
+
+__device__ __forceinline__ double ld_interp(const double* b, double sigma, const Params& P,
+                                            double S0, double S1, double S2, double S3, double S4, double S5) {
+    const double tau_5 = fabs(b[0] - b[2]);
+    const double beta_avg = double(1)/double(8)*(b[0] + b[2] + double(6)*b[1]);
+    const double tau_6 = fabs(b[3] - beta_avg);
+    double o0, o1, o2, o3;
+#if HMR_FAST
+    const double r0 = double(1)/(b[0] + HMR_EPS);
+    const double r1 = double(1)/(b[1] + HMR_EPS);
+    const double r2 = double(1)/(b[2] + HMR_EPS);
+    const double r3 = double(1)/(b[3] + HMR_EPS);
+    double u0 = double(1)/double(16)*(double(1) + ipow_d(tau_5*r0, P.p));
+    double u1 = double(5)/double(8)*(double(1) + ipow_d(tau_5*r1, P.p));
+    double u2 = double(5)/double(16)*(double(1) + ipow_d(tau_5*r2, P.p));
+    const double ru = double(1)/(u0 + u1 + u2);
+    u0 *= ru; u1 *= ru; u2 *= ru;
+    o0 = double(1)/double(32)*(P.C + ipow_d(tau_6*r0, P.q));
+    o1 = double(15)/double(32)*(P.C + ipow_d(tau_6*r1, P.q));
+    o2 = double(15)/double(32)*(P.C + ipow_d(tau_6*r2, P.q));
+    o3 = double(1)/double(32)*(P.C + ipow_d(tau_6*r3, P.q));
+    const double ro = double(1)/(o0 + o1 + o2 + o3);
+    o0 *= ro; o1 *= ro; o2 *= ro; o3 *= ro;
+    const bool blend = tau_6 > P.alpha_tau*(beta_avg + HMR_EPS);
+#else
+    double u0 = double(1)/double(16)*(double(1) + ipow_d(tau_5/(b[0] + HMR_EPS), P.p));
+    double u1 = double(5)/double(8)*(double(1) + ipow_d(tau_5/(b[1] + HMR_EPS), P.p));
+    double u2 = double(5)/double(16)*(double(1) + ipow_d(tau_5/(b[2] + HMR_EPS), P.p));
+    const double us = u0 + u1 + u2;
+    u0 = u0/us; u1 = u1/us; u2 = u2/us;
+    o0 = double(1)/double(32)*(P.C + ipow_d(tau_6/(b[0] + HMR_EPS), P.q));
+    o1 = double(15)/double(32)*(P.C + ipow_d(tau_6/(b[1] + HMR_EPS), P.q));
+    o2 = double(15)/double(32)*(P.C + ipow_d(tau_6/(b[2] + HMR_EPS), P.q));
+    o3 = double(1)/double(32)*(P.C + ipow_d(tau_6/(b[3] + HMR_EPS), P.q));
+    const double os = o0 + o1 + o2 + o3;
+    o0 = o0/os; o1 = o1/os; o2 = o2/os; o3 = o3/os;
+    const double R_tau = tau_6/(beta_avg + HMR_EPS);
+    const bool blend = R_tau > P.alpha_tau;
+#endif
+    if (blend) {
+        o0 = sigma*u0 + (double(1) - sigma)*o0;
+        o1 = sigma*u1 + (double(1) - sigma)*o1;
+        o2 = sigma*u2 + (double(1) - sigma)*o2;
+        o3 = (double(1) - sigma)*o3;
+    }
+    return double(3)/double(8)*o0*S0 +
+        (-double(10)/double(8)*o0 - double(1)/double(8)*o1)*S1 +
+        (double(15)/double(8)*o0 + double(6)/double(8)*o1 + double(3)/double(8)*o2)*S2 +
+        (double(3)/double(8)*o1 + double(6)/double(8)*o2 + double(15)/double(8)*o3)*S3 +
+        (-double(1)/double(8)*o2 - double(10)/double(8)*o3)*S4 +
+        double(3)/double(8)*o3*S5;
+}
+
+__device__ __forceinline__ void ld_pair(const double* U, const Params& P, double& Um, double& Up) {
+    const double sigma = ld_sigma(U);
+    double b[4];
+    js_betas(U, b[0], b[1], b[2]);
+    b[3] = ld_beta3(U[0], U[1], U[2], U[3], U[4], U[5]);
+    Um = ld_interp(b, sigma, P, U[0], U[1], U[2], U[3], U[4], U[5]);
+    js_betas_tilde(U, b[0], b[1], b[2]);
+    b[3] = ld_beta3(U[5], U[4], U[3], U[2], U[1], U[0]);
+    Up = ld_interp(b, sigma, P, U[5], U[4], U[3], U[2], U[1], U[0]);
+}
+
+// ----------------------------------------------------------------------------
+// Bounds check of a reconstructed face state.
+// ----------------------------------------------------------------------------
+template <int DIM, int MODEL, int NSP>
+__device__ __forceinline__ bool face_bounded(const Params& P, const double* V) {
+    using M = Model<DIM, MODEL, NSP>;
+    if constexpr (MODEL == SINGLE_SPECIES) {
+        return (V[0] > 0.0) && (V[DIM + 1] > 0.0);
+    } else {
+        bool ok = true;
+        double Z[NSP];
+        Z[NSP - 1] = 1.0;
+#pragma unroll
+        for (int s = 0; s < NSP - 1; s++) {
+            Z[s] = V[M::IZ + s];
+            Z[NSP - 1] -= Z[s];
+            ok = ok && (Z[s] > -1000.0 && Z[s] < 1000.0);
+        }
+        ok = ok && (Z[NSP - 1] > -1000.0 && Z[NSP - 1] < 1000.0);
+        double rho = 0.0;
+#pragma unroll
+        for (int s = 0; s < NSP; s++) rho += V[s];
+        double Y[NSP];
+#pragma unroll
+        for (int s = 0; s < NSP; s++) {
+            Y[s] = V[s]/rho;
+            ok = ok && (Y[s] > -0.001 && Y[s] < 1.001);
+        }
+#pragma unroll
+        for (int s = 0; s < NSP; s++) ok = ok && (V[s] > 0.0);
+        const double p = V[NSP + DIM];
+        const double gamma = gamma_all<NSP>(P, Z);
+#if HMR_FAST
+        double c2 = (gamma - double(1))*p;
+#pragma unroll
+        for (int s = 0; s < NSP; s++) c2 += Y[s]*p;
+#else
+        const double Gamma = gamma - double(1);
+        const double Psi = p/rho;
+        double c2 = Gamma*p/rho;
+#pragma unroll
+        for (int s = 0; s < NSP; s++) c2 += Y[s]*Psi;
+#endif
+        ok = ok && (c2 > 0.0);
+        return ok;
+    }
+}
+
+// ----------------------------------------------------------------------------
+// Face thermodynamics of one reconstructed state (Riemann drivers).
+// ----------------------------------------------------------------------------
+template <int DIM, int MODEL, int NSP>
+__device__ __forceinline__ void face_thermo(const Params& P, const double* V, double& rho, double& cs,
+                                            double& eps) {
+    using M = Model<DIM, MODEL, NSP>;
+    if constexpr (MODEL == SINGLE_SPECIES) {
+        const double gamma = P.gamma[0];
+        rho = V[0];
+        const double p = V[DIM + 1];
+#if HMR_FAST
+        const double ri = double(1)/rho;
+        cs = sqrt(gamma*p*ri);
+        eps = p*ri*P.inv_gm1[0];
+#else
+        cs = sqrt(gamma*p/rho);
+        eps = p/((gamma - double(1))*rho);
+#endif
+    } else {
+        double r = 0.0;
+#pragma unroll
+        for (int s = 0; s < NSP; s++) r += V[s];
+        rho = r;
+        const double p = V[NSP + DIM];
+        const double gamma = gamma_last<NSP>(P, V + M::IZ);
+#if HMR_FAST
+        const double ri = double(1)/r;
+        const double Psi = p*ri;
+        double c2 = (gamma - double(1))*Psi;
+#pragma unroll
+        for (int s = 0; s < NSP; s++) c2 += (V[s]*ri)*Psi;
+        cs = sqrt(c2);
+        eps = Psi/(gamma - double(1));
+#else
+        double Y[NSP];
+#pragma unroll
+        for (int s = 0; s < NSP; s++) Y[s] = V[s]/r;
+        const double Gamma = gamma - double(1);
+        const double Psi = p/r;
+        double c2 = Gamma*p/r;
+#pragma unroll
+        for (int s = 0; s < NSP; s++) c2 += Y[s]*Psi;
+        cs = sqrt(c2);
+        eps = p/((gamma - double(1))*r);
+#endif
+    }
+}
+
+// Conserved state and physical flux of one face state.
+template <int DIM, int MODEL, int NSP, int A>
+__device__ __forceinline__ void face_QF(const double* V, double rho, double eps, double* Q, double* F) {
+    using M = Model<DIM, MODEL, NSP>;
+    if constexpr (MODEL == SINGLE_SPECIES) {
+        const double p = V[DIM + 1];
+        Q[0] = V[0];
+#pragma unroll
+        for (int k = 0; k < DIM; k++) Q[1 + k] = V[0]*V[1 + k];
+        double ke = V[1]*V[1];
+#pragma unroll
+        for (int k = 1; k < DIM; k++) ke = ke + V[1 + k]*V[1 + k];
+        Q[DIM + 1] = V[0]*(eps + double(1)/double(2)*ke);
+        F[0] = Q[1 + A];
+#pragma unroll
+        for (int k = 0; k < DIM; k++) {
+            if (k == A) F[1 + k] = Q[1 + A]*V[1 + k] + p;
+            else F[1 + k] = Q[1 + A]*V[1 + k];
+        }
+        F[DIM + 1] = V[1 + A]*(Q[DIM + 1] + p);
+    } else {
+        const double p = V[NSP + DIM];
+        const double un = V[NSP + A];
+#pragma unroll
+        for (int s = 0; s < NSP; s++) Q[s] = V[s];
+#pragma unroll
+        for (int k = 0; k < DIM; k++) Q[NSP + k] = rho*V[NSP + k];
+        double ke = V[NSP]*V[NSP];
+#pragma unroll
+        for (int k = 1; k < DIM; k++) ke = ke + V[NSP + k]*V[NSP + k];
+        Q[NSP + DIM] = rho*(eps + double(1)/double(2)*ke);
+#pragma unroll
+        for (int s = 0; s < NSP - 1; s++) Q[M::IZ + s] = V[M::IZ + s];
+#pragma unroll
+        for (int s = 0; s < NSP; s++) F[s] = un*V[s];
+#pragma unroll
+        for (int k = 0; k < DIM; k++) {
+            if (k == A) F[NSP + k] = un*Q[NSP + k] + p;
+            else F[NSP + k] = un*Q[NSP + k];
+        }
+        F[NSP + DIM] = un*(Q[NSP + DIM] + p);
+#pragma unroll
+        for (int s = 0; s < NSP - 1; s++) F[M::IZ + s] = un*V[M::IZ + s];
+    }
+}
+
+template <int DIM, int MODEL, int NSP, int A>
+__device__ __forceinline__ constexpr bool hll_comp(int e) {
+    if constexpr (MODEL == SINGLE_SPECIES) {
+        return e == 0 || (e >= 1 && e <= DIM && (e - 1) != A);
+    } else {
+        return e < NSP || (e >= NSP && e < NSP + DIM && (e - NSP) != A) || e > NSP + DIM;
+    }
+}
+
+// Midpoint flux of one face: HLLC, or HLLC-HLL when use_hll is set (the
+// shock sensor's choice, WCNS56-HLLC-HLL.cpp:1090-1113).  Also returns the
+// HLLC midpoint normal velocity.
+template <int DIM, int MODEL, int NSP, int A>
+__device__ __forceinline__ void riemann(const Params& P, const double* VL, const double* VR, bool use_hll,
+                                        double* Fout, double& u_mid) {
+    using M = Model<DIM, MODEL, NSP>;
+    constexpr int NEQ = M::NEQ;
+    constexpr int IU = M::IU;
+    constexpr int IP = M::IP;
+    double rhoL, cL, epsL, rhoR, cR, epsR;
+    face_thermo<DIM, MODEL, NSP>(P, VL, rhoL, cL, epsL);
+    face_thermo<DIM, MODEL, NSP>(P, VR, rhoR, cR, epsR);
+    const double uL = VL[IU + A], uR = VR[IU + A];
+    const double pL = VL[IP], pR = VR[IP];
+    const double u_average = double(1)/double(2)*(uL + uR);
+    const double c_average = double(1)/double(2)*(cL + cR);
+    const double s_L = fmin(u_average - c_average, uL - cL);
+    const double s_R = fmax(u_average + c_average, uR + cR);
+    const double s_minus = fmin(0.0, s_L);
+    const double s_plus = fmax(0.0, s_R);
+    const double s_star = (pR - pL + rhoL*uL*(s_L - uL) - rhoR*uR*(s_R - uR))/
+        (rhoL*(s_L - uL) - rhoR*(s_R - uR));
+
+    const bool left = s_star > 0.0;
+    const double* VK = left ? VL : VR;
+    const double rhoK = left ? rhoL : rhoR;
+    const double epsK = left ? epsL : epsR;
+    const double sK = left ? s_L : s_R;
+    const double uK = left ? uL : uR;
+    const double pK = left ? pL : pR;
+    const double s_pm = left ? s_minus : s_plus;
+    double QK[NEQ], FK[NEQ], Qs[NEQ];
+    face_QF<DIM, MODEL, NSP, A>(VK, rhoK, epsK, QK, FK);
+    const double Chi = (sK - uK)/(sK - s_star);
+    if constexpr (MODEL == SINGLE_SPECIES) {
+        Qs[0] = Chi*VK[0];
+#pragma unroll
+        for (int k = 0; k < DIM; k++) {
+            if (k == A) Qs[1 + k] = Chi*VK[0]*s_star;
+            else Qs[1 + k] = Chi*QK[1 + k];
+        }
+        Qs[DIM + 1] = Chi*(QK[DIM + 1] + (s_star - uK)*(VK[0]*s_star + pK/(sK - uK)));
+    } else {
+#pragma unroll
+        for (int s = 0; s < NSP; s++) Qs[s] = Chi*VK[s];
+#pragma unroll
+        for (int k = 0; k < DIM; k++) {
+            if (k == A) Qs[NSP + k] = Chi*rhoK*s_star;
+            else Qs[NSP + k] = Chi*QK[NSP + k];
+        }
+        Qs[NSP + DIM] = Chi*(QK[NSP + DIM] + (s_star - uK)*(rhoK*s_star + pK/(sK - uK)));
+#pragma unroll
+        for (int s = 0; s < NSP - 1; s++) Qs[M::IZ + s] = Chi*VK[M::IZ + s];
+    }
+#pragma unroll
+    for (int e = 0; e < NEQ; e++) Fout[e] = FK[e] + s_pm*(Qs[e] - QK[e]);
+    u_mid = uK + s_pm*(Chi - double(1));
+
+    if (use_hll) {
+        // HLL for mass/partial densities, transverse momenta and volume
+        // fractions, blended with HLLC by the velocity-jump direction.
+        double QL[NEQ], FL[NEQ], QR[NEQ], FR[NEQ];
+        face_QF<DIM, MODEL, NSP, A>(VL, rhoL, epsL, QL, FL);
+        face_QF<DIM, MODEL, NSP, A>(VR, rhoR, epsR, QR, FR);
+        double diff[DIM];
+#pragma unroll
+        for (int k = 0; k < DIM; k++) diff[k] = VR[IU + k] - VL[IU + k];
+        double vsq = diff[0]*diff[0];
+#pragma unroll
+        for (int k = 1; k < DIM; k++) vsq = vsq + diff[k]*diff[k];
+        const double vel_mag = sqrt(vsq);
+        double alpha_1, alpha_2;
+        if (vel_mag < HMR_EPS) {
+            alpha_1 = 1.0;
+            alpha_2 = 0.0;
+        } else {
+            alpha_1 = fabs(diff[A])/vel_mag;
+            alpha_2 = sqrt(double(1) - alpha_1*alpha_1);
+        }
+        const double beta_1 = double(1)/double(2)*(double(1) + alpha_1/(alpha_1 + alpha_2));
+        const double beta_2 = double(1) - beta_1;
+#pragma unroll
+        for (int e = 0; e < NEQ; e++) {
+            if (hll_comp<DIM, MODEL, NSP, A>(e)) {
+                double Fh;
+                if (s_L > 0.0) Fh = FL[e];
+                else if (s_R < 0.0) Fh = FR[e];
+                else Fh = (s_R*FL[e] - s_L*FR[e] + s_R*s_L*(QR[e] - QL[e]))/(s_R - s_L);
+                Fout[e] = beta_1*Fout[e] + beta_2*Fh;
+            }
+        }
+    }
+}
+
+}  // namespace hmr

@@ -1,0 +1,326 @@
+"""Host-side mirror of the reference's patch-level interface, over the C ABI.
+
+Names follow HAMeRS:
+  FlowModel                     -- FlowModelManager + ideal-gas mixing rules
+                                   (include/flow/flow_models/FlowModel.hpp:59-572)
+  ConvectiveFluxReconstructor   -- ConvectiveFluxReconstructorManager product
+                                   (include/flow/convective_flux_reconstructors/ConvectiveFluxReconstructor.hpp:23-124)
+  Euler                         -- the RungeKuttaPatchStrategy of src/apps/Euler/Euler.cpp
+                                   (computeFluxesAndSourcesOnPatch :904, advanceSingleStepOnPatch :1003)
+  RungeKuttaLevelIntegrator     -- SSPRK3 stage loop (RungeKuttaLevelIntegrator.cpp:1672-1748)
+  BatchedLevel                  -- all patches of a level per substep in one persistent kernel
+
+Patch data are torch tensors on the CUDA device in SAMRAI layout:
+conserved variables (ncomp, G2, G1, G0) over the ghost box (ghost width 4),
+face fluxes [axis] -> (neq, ...) and sources (neq, n2, n1, n0).  torch is used
+for device memory and streams only; every computation runs in libhmr_gb300.so.
+Errors from the library raise HmrError (argument errors are raised before any
+work is queued, mirroring TBOX_ERROR in the reference).
+"""
+import ctypes
+
+import torch
+
+from . import _lib as L
+
+GHOST = 4
+
+_FLOW_MODELS = {
+    "SINGLE_SPECIES": L.HMR_SINGLE_SPECIES,
+    "FOUR_EQN_CONSERVATIVE": L.HMR_FOUR_EQN_CONSERVATIVE,
+    "FIVE_EQN_ALLAIRE": L.HMR_FIVE_EQN_ALLAIRE,
+}
+_RECONSTRUCTORS = {
+    "WCNS5_JS_HLLC_HLL": L.HMR_WCNS5_JS_HLLC_HLL,
+    "WCNS6_LD_HLLC_HLL": L.HMR_WCNS6_LD_HLLC_HLL,
+}
+
+# SSPRK(3,3), RungeKuttaLevelIntegrator.cpp:3909-3927
+RK3_ALPHA = [[1.0], [3.0 / 4.0, 1.0 / 4.0], [1.0 / 3.0, 0.0, 2.0 / 3.0]]
+RK3_BETA = [[1.0], [0.0, 1.0 / 4.0], [0.0, 0.0, 2.0 / 3.0]]
+RK3_GAMMA = [[1.0 / 6.0], [0.0, 1.0 / 6.0], [0.0, 0.0, 2.0 / 3.0]]
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+class FlowModel:
+    """Flow model selection: 'SINGLE_SPECIES' or 'FIVE_EQN_ALLAIRE', ideal gas."""
+
+    def __init__(self, flow_model, dim, species_gamma, species_R=None):
+        if flow_model not in _FLOW_MODELS:
+            raise ValueError(f"unknown flow model {flow_model!r}")
+        self.name = flow_model
+        self.model = _FLOW_MODELS[flow_model]
+        self.dim = int(dim)
+        self.species_gamma = [float(g) for g in species_gamma]
+        self.num_species = len(self.species_gamma)
+        self.species_R = [float(r) for r in (species_R or [1.0] * self.num_species)]
+
+    def getNumberOfEquations(self):
+        if self.model == L.HMR_SINGLE_SPECIES:
+            return self.dim + 2
+        if self.model == L.HMR_FOUR_EQN_CONSERVATIVE:
+            return self.num_species + self.dim + 1
+        return self.dim + 2 * self.num_species
+
+    def getNumberOfComponents(self):
+        return self.getNumberOfEquations() + (1 if self.model == L.HMR_FIVE_EQN_ALLAIRE else 0)
+
+
+class Patch:
+    """One patch: interior size n, spacing dx, conserved variables on the ghost box."""
+
+    def __init__(self, n, dx, data):
+        self.n = [int(v) for v in n]
+        self.dx = [float(v) for v in dx]
+        self.data = data
+
+    def geometry(self):
+        g = L.PatchGeometry()
+        for d in range(3):
+            g.n[d] = self.n[d] if d < len(self.n) else 1
+            g.dx[d] = self.dx[d] if d < len(self.dx) else 1.0
+        return g
+
+
+def _comp_ptrs(t, ncomp):
+    if not (t.is_cuda and t.dtype == torch.float64 and t.is_contiguous()):
+        raise ValueError("patch arrays must be contiguous float64 CUDA tensors")
+    if t.shape[0] < ncomp:
+        raise ValueError(f"expected {ncomp} components, got {t.shape[0]}")
+    return [t[e].data_ptr() for e in range(ncomp)]
+
+
+class ConvectiveFluxReconstructor:
+    """WCNS5-JS / WCNS6-LD + HLLC-HLL reconstructor behind the C ABI.
+
+    db keys follow the reference's input database: constant_p, constant_q,
+    constant_C, constant_alpha_tau (ConvectiveFluxReconstructorWCNS6-LD-HLLC-HLL.cpp:343-361).
+    precision: 'fast' (default, <= 1e-12 relative) or 'exact' (bitwise to the reference order).
+    """
+
+    def __init__(self, name, flow_model, db=None, precision="fast"):
+        if name not in _RECONSTRUCTORS:
+            raise ValueError(f"unknown convective flux reconstructor {name!r}")
+        db = db or {}
+        lib = L.load()
+        cfg = L.Config()
+        L.check("hmr_config_default", lib.hmr_config_default(
+            ctypes.byref(cfg), flow_model.model, _RECONSTRUCTORS[name], flow_model.dim, flow_model.num_species))
+        for s in range(flow_model.num_species):
+            cfg.species_gamma[s] = flow_model.species_gamma[s]
+            cfg.species_R[s] = flow_model.species_R[s]
+        cfg.constant_p = int(db.get("constant_p", 2))
+        cfg.constant_q = int(db.get("constant_q", 4))
+        cfg.constant_C = float(db.get("constant_C", 1.0e9))
+        cfg.constant_alpha_tau = float(db.get("constant_alpha_tau", 35.0))
+        cfg.precision = L.HMR_PRECISION_EXACT if precision == "exact" else L.HMR_PRECISION_FAST
+        self.flow_model = flow_model
+        self.name = name
+        self.precision = precision
+        self._lib = lib
+        ctx = ctypes.c_void_p()
+        L.check("hmr_ctx_create", lib.hmr_ctx_create(ctypes.byref(cfg), ctypes.byref(ctx)))
+        self.ctx = ctx
+        self.neq = lib.hmr_num_equations(ctx)
+        self.ncomp = lib.hmr_num_components(ctx)
+
+    def close(self):
+        if self.ctx:
+            self._lib.hmr_ctx_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def getConvectiveFluxNumberOfGhostCells(self):
+        return self._lib.hmr_num_ghosts(self.ctx)
+
+    def allocateFlux(self, patch):
+        dim = self.flow_model.dim
+        n3 = list(patch.n) + [1] * (3 - len(patch.n))
+        out = []
+        for a in range(dim):
+            e = [n3[d] + (1 if d == a else 0) for d in range(3)]
+            out.append(torch.zeros((self.neq, e[2], e[1], e[0]), dtype=torch.float64, device=patch.data.device))
+        return out
+
+    def allocateSource(self, patch):
+        n3 = list(patch.n) + [1] * (3 - len(patch.n))
+        return torch.zeros((self.neq, n3[2], n3[1], n3[0]), dtype=torch.float64, device=patch.data.device)
+
+    def reserve(self, patch):
+        g = patch.geometry()
+        L.check("hmr_ctx_reserve", self._lib.hmr_ctx_reserve(self.ctx, ctypes.byref(g)))
+
+    def computeConvectiveFluxAndSourceOnPatch(self, patch, convective_flux, source, dt, stream=None):
+        """dt-scaled face fluxes (overwritten) and advective source (+=)."""
+        g = patch.geometry()
+        q, _k1 = L.ptr_array(_comp_ptrs(patch.data, self.ncomp))
+        fptrs = []
+        for a in range(self.flow_model.dim):
+            fptrs += _comp_ptrs(convective_flux[a], self.neq)
+        f, _k2 = L.ptr_array(fptrs)
+        s, _k3 = L.ptr_array(_comp_ptrs(source, self.neq))
+        L.check("hmr_conv_flux_source_patch", self._lib.hmr_conv_flux_source_patch(
+            self.ctx, ctypes.byref(g), q, float(dt), f, s, _stream_ptr(stream)))
+
+    def readCounters(self, reset=True):
+        out = (ctypes.c_ulonglong * 2)()
+        L.check("hmr_read_counters", self._lib.hmr_read_counters(self.ctx, out, 1 if reset else 0))
+        return int(out[0]), int(out[1])
+
+
+class Euler:
+    """Patch strategy: flux + RK stage on one patch (src/apps/Euler/Euler.cpp)."""
+
+    def __init__(self, reconstructor):
+        self.rec = reconstructor
+        self._lib = reconstructor._lib
+
+    def computeFluxesAndSourcesOnPatch(self, patch, flux, source, dt, stream=None):
+        source.zero_()   # Euler.cpp:916-932
+        self.rec.computeConvectiveFluxAndSourceOnPatch(patch, flux, source, dt, stream)
+
+    def advanceSingleStepOnPatch(self, patch, alpha, beta, gamma, Q_int, F_int, S_int,
+                                 flux_acc=None, source_acc=None, stream=None):
+        """Q = sum alpha_n Q_int[n] + beta_n (-div F_int[n] + S_int[n]) written into patch.data."""
+        rec = self.rec
+        nc = len(alpha)
+        g = patch.geometry()
+        a = (ctypes.c_double * nc)(*alpha)
+        b = (ctypes.c_double * nc)(*beta)
+        c = (ctypes.c_double * nc)(*gamma)
+        qi, k1 = L.ptr_array2([_comp_ptrs(t, rec.ncomp) for t in Q_int])
+        fi, k2 = L.ptr_array2([sum((_comp_ptrs(f, rec.neq) for f in F), []) for F in F_int])
+        si, k3 = L.ptr_array2([_comp_ptrs(t, rec.neq) for t in S_int])
+        qo, k4 = L.ptr_array(_comp_ptrs(patch.data, rec.ncomp))
+        fa = sa = None
+        keep = []
+        if flux_acc is not None:
+            fa, k5 = L.ptr_array(sum((_comp_ptrs(f, rec.neq) for f in flux_acc), []))
+            sa, k6 = L.ptr_array(_comp_ptrs(source_acc, rec.neq))
+            keep += [k5, k6]
+        L.check("hmr_rk_stage_patch", self._lib.hmr_rk_stage_patch(
+            rec.ctx, ctypes.byref(g), nc, a, b, c, qi, fi, si, qo, fa, sa, _stream_ptr(stream)))
+
+    def fillGhosts(self, patch, periodic, stream=None):
+        g = patch.geometry()
+        q, _k = L.ptr_array(_comp_ptrs(patch.data, self.rec.ncomp))
+        per = (ctypes.c_int * 3)(*(list(periodic) + [0] * (3 - len(periodic))))
+        L.check("hmr_fill_ghosts_patch", self._lib.hmr_fill_ghosts_patch(
+            self.rec.ctx, ctypes.byref(g), q, per, _stream_ptr(stream)))
+
+    def substep(self, patch, stage, Q_int, dt, out, stream=None):
+        """Fused flux + update of SSPRK3 stage `stage`: out = sum alpha Q_int + beta (-div F(Q_int[stage]) + S)."""
+        rec = self.rec
+        g = patch.geometry()
+        alpha = (ctypes.c_double * 3)(*(RK3_ALPHA[stage] + [0.0] * (2 - stage)))
+        qi, k1 = L.ptr_array2([_comp_ptrs(t, rec.ncomp) for t in Q_int[:stage + 1]])
+        qo, k2 = L.ptr_array(_comp_ptrs(out, rec.ncomp))
+        L.check("hmr_rk_substep_patch", self._lib.hmr_rk_substep_patch(
+            rec.ctx, ctypes.byref(g), int(stage), alpha, RK3_BETA[stage][stage], qi, float(dt), qo,
+            _stream_ptr(stream)))
+
+
+class RungeKuttaLevelIntegrator:
+    """SSPRK3 on one patch with ghost fill between stages (per-patch form)."""
+
+    def __init__(self, euler, patch, periodic):
+        self.euler = euler
+        self.patch = patch
+        self.periodic = list(periodic)
+        self.stages = [torch.empty_like(patch.data) for _ in range(2)]
+        euler.rec.reserve(patch)
+
+    def advance(self, dt, nsteps=1, stream=None):
+        p = self.patch
+        Q0, Q1, Q2 = p.data, self.stages[0], self.stages[1]
+        views = [Patch(p.n, p.dx, Q) for Q in (Q0, Q1, Q2)]
+        for _ in range(nsteps):
+            self.euler.fillGhosts(views[0], self.periodic, stream)
+            self.euler.substep(views[0], 0, [Q0], dt, Q1, stream)
+            self.euler.fillGhosts(views[1], self.periodic, stream)
+            self.euler.substep(views[1], 1, [Q0, Q1], dt, Q2, stream)
+            self.euler.fillGhosts(views[2], self.periodic, stream)
+            self.euler.substep(views[2], 2, [Q0, Q1, Q2], dt, Q0, stream)
+        self.euler.fillGhosts(views[0], self.periodic, stream)
+
+
+class BatchedLevel:
+    """Every patch of a level advanced by one persistent kernel per SSPRK3 substep."""
+
+    def __init__(self, reconstructor, geometries):
+        self.rec = reconstructor
+        self._lib = reconstructor._lib
+        n = len(geometries)
+        arr = (L.PatchGeometry * n)()
+        self.shapes = []
+        dim = reconstructor.flow_model.dim
+        for i, (nn, dx) in enumerate(geometries):
+            for d in range(3):
+                arr[i].n[d] = nn[d] if d < dim else 1
+                arr[i].dx[d] = dx[d] if d < dim else 1.0
+            G = [nn[d] + 2 * GHOST if d < dim else 1 for d in range(3)]
+            self.shapes.append((reconstructor.ncomp, G[2], G[1], G[0]))
+        lv = ctypes.c_void_p()
+        L.check("hmr_level_create", self._lib.hmr_level_create(reconstructor.ctx, n, arr, ctypes.byref(lv)))
+        self.level = lv
+        self.npatch = n
+
+    def close(self):
+        if self.level:
+            self._lib.hmr_level_destroy(self.level)
+            self.level = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def bind(self, patch, data):
+        """Binds a patch's conserved-variable tensor (ncomp, G2, G1, G0) as its slot-0 state."""
+        if tuple(data.shape) != self.shapes[patch]:
+            raise ValueError(f"patch {patch}: expected shape {self.shapes[patch]}, got {tuple(data.shape)}")
+        q, _k = L.ptr_array(_comp_ptrs(data, self.rec.ncomp))
+        L.check("hmr_level_bind_state", self._lib.hmr_level_bind_state(self.level, int(patch), q))
+
+    def state_pointers(self, patch, slot=0):
+        arr = (ctypes.POINTER(ctypes.c_double) * self.rec.ncomp)()
+        L.check("hmr_level_state", self._lib.hmr_level_state(
+            self.level, int(patch), int(slot), ctypes.cast(arr, L.DPP)))
+        return [ctypes.cast(arr[e], ctypes.c_void_p).value for e in range(self.rec.ncomp)]
+
+    def substep(self, stage, dt, stream=None):
+        L.check("hmr_level_substep", self._lib.hmr_level_substep(self.level, int(stage), float(dt),
+                                                                 _stream_ptr(stream)))
+
+    def set_periodic(self, patch, periodic):
+        per = (ctypes.c_int * 3)(*(list(periodic) + [0] * (3 - len(periodic))))
+        L.check("hmr_level_set_periodic", self._lib.hmr_level_set_periodic(self.level, int(patch), per))
+
+    def check(self):
+        """Raises HmrError(HMR_ERR_BARRIER) if a persistent-kernel barrier gave up."""
+        L.check("hmr_level_check", self._lib.hmr_level_check(self.level))
+
+    def barrier_diagnostic(self, extra_arrivals, timeout_ns):
+        L.check("hmr_level_barrier_diagnostic", self._lib.hmr_level_barrier_diagnostic(
+            self.level, int(extra_arrivals), int(timeout_ns)))
+
+    def step(self, dt, stream=None):
+        L.check("hmr_level_step", self._lib.hmr_level_step(self.level, float(dt), _stream_ptr(stream)))
+
+    def autotune(self, dt, stream=None):
+        t = ctypes.c_int()
+        b = ctypes.c_int()
+        L.check("hmr_level_autotune", self._lib.hmr_level_autotune(
+            self.level, float(dt), ctypes.byref(t), ctypes.byref(b), _stream_ptr(stream)))
+        return t.value, b.value

@@ -1,0 +1,185 @@
+/*
+ * hmr.h -- C ABI of the GB300 (sm_103a) FP64 convective hot path of HAMeRS.
+ *
+ * The entry points replace the per-patch calls that HAMeRS makes from its
+ * Runge-Kutta level integrator (src/algs/integrator/RungeKuttaLevelIntegrator.cpp:1717-1743):
+ *
+ *   ConvectiveFluxReconstructor::computeConvectiveFluxAndSourceOnPatch
+ *       include/flow/convective_flux_reconstructors/ConvectiveFluxReconstructor.hpp:73-81
+ *       (WCNS56 implementation: src/flow/convective_flux_reconstructors/WCNS56/
+ *        ConvectiveFluxReconstructorWCNS56-HLLC-HLL.cpp:40-2656)
+ *   RungeKuttaPatchStrategy::advanceSingleStepOnPatch
+ *       include/algs/patch_strategy/RungeKuttaPatchStrategy.hpp (implemented by
+ *       src/apps/Euler/Euler.cpp:1003-1680)
+ *   the per-patch stage loop of RungeKuttaLevelIntegrator::advanceLevel
+ *       src/algs/integrator/RungeKuttaLevelIntegrator.cpp:1672-1748 (batched form)
+ *
+ * Conventions (identical to SAMRAI's pdat layout used by the reference):
+ *   - every array is FP64 in device memory, x fastest, then y, then z;
+ *   - a patch's conserved variables are CellData on the ghost box (interior
+ *     grown by hmr_num_ghosts() = 4 cells), one array per component, in the
+ *     flow model's order:
+ *       single species          : rho, rho*u_k (dim), E
+ *       five-equation (Allaire) : Z_i*rho_i (N), rho*u_k (dim), E, Z_i (N; the
+ *                                 last volume fraction is stored as the
+ *                                 reference's depth-N CellData stores it)
+ *   - face fluxes are SideData with zero ghosts: for axis a the array spans
+ *     the interior grown by one cell along a; arrays are ordered axis-major,
+ *     flux[a*neq + e];
+ *   - sources are CellData with zero ghosts (neq arrays).
+ * Pointer arrays (double* const*) live in host memory; the arrays they point
+ * to live in device memory.  All work is enqueued on the given CUDA stream
+ * (cudaStream_t passed as void*, NULL for the legacy default stream).
+ *
+ * Errors: every function returns an hmr_status.  0 is success; negative
+ * values reject arguments before any work is queued; positive values report
+ * a CUDA error code (the context stays usable unless the CUDA error is sticky).
+ * Nothing is thrown across the ABI.  A context is not thread-safe; use one
+ * context per host thread / stream.
+ */
+#ifndef HMR_H
+#define HMR_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HMR_MAX_SPECIES 4
+#define HMR_MAX_COMPONENTS 12
+
+typedef enum {
+    HMR_OK = 0,
+    HMR_ERR_ARGUMENT = -1,
+    HMR_ERR_UNSUPPORTED = -2,
+    HMR_ERR_NO_DEVICE = -3,
+    HMR_ERR_STATE = -4,
+    HMR_ERR_BARRIER = -5
+} hmr_status;
+
+/* FlowModelManager model names (src/flow/flow_models/FlowModelManager.cpp). */
+typedef enum {
+    HMR_SINGLE_SPECIES = 0,
+    HMR_FOUR_EQN_CONSERVATIVE = 1,
+    HMR_FIVE_EQN_ALLAIRE = 2
+} hmr_flow_model;
+
+/* ConvectiveFluxReconstructorManager names
+ * (src/flow/convective_flux_reconstructors/ConvectiveFluxReconstructorManager.cpp:40-91). */
+typedef enum {
+    HMR_WCNS5_JS_HLLC_HLL = 0,
+    HMR_WCNS6_LD_HLLC_HLL = 1
+} hmr_reconstructor;
+
+typedef enum {
+    HMR_PRECISION_FAST = 0,   /* regrouped FP64 with FMA; <= 1e-12 relative to the reference */
+    HMR_PRECISION_EXACT = 1   /* the reference's operation order, no FMA: bitwise equal to it */
+} hmr_precision;
+
+typedef struct {
+    int flow_model;                            /* hmr_flow_model */
+    int dim;                                   /* 2 or 3 */
+    int num_species;
+    double species_gamma[HMR_MAX_SPECIES];     /* Equation_of_state_mixing_rules.species_gamma */
+    double species_R[HMR_MAX_SPECIES];         /* Equation_of_state_mixing_rules.species_R */
+    int convective_flux_reconstructor;         /* hmr_reconstructor */
+    int constant_p;                            /* WCNS constant p (default 2) */
+    int constant_q;                            /* WCNS6-LD constant q (default 4) */
+    double constant_C;                         /* WCNS6-LD constant C (default 1e9) */
+    double constant_alpha_tau;                 /* WCNS6-LD constant alpha_tau (default 35) */
+    int precision;                             /* hmr_precision */
+} hmr_config;
+
+typedef struct {
+    int n[3];          /* interior cells per axis (n[2] ignored in 2D) */
+    double dx[3];      /* grid spacing (CartesianPatchGeometry::getDx) */
+} hmr_patch_geometry;
+
+typedef struct hmr_ctx hmr_ctx;
+typedef struct hmr_level hmr_level;
+
+/* Fills cfg with the reference's defaults for the given model, scheme and dimension. */
+int hmr_config_default(hmr_config* cfg, int flow_model, int reconstructor, int dim, int num_species);
+
+/* Context: FlowModel + ConvectiveFluxReconstructor of one configuration.
+ * Replaces the construction in FlowModelManager / ConvectiveFluxReconstructorManager
+ * (ConvectiveFluxReconstructorManager.cpp:14-152).  Owns scratch memory. */
+int hmr_ctx_create(const hmr_config* cfg, hmr_ctx** out);
+int hmr_ctx_destroy(hmr_ctx* ctx);
+/* FlowModel::getNumberOfEquations (include/flow/flow_models/FlowModel.hpp). */
+int hmr_num_equations(const hmr_ctx* ctx);
+/* Number of stored conserved components (neq, plus the last volume fraction of the five-equation model). */
+int hmr_num_components(const hmr_ctx* ctx);
+/* ConvectiveFluxReconstructor::getConvectiveFluxNumberOfGhostCells (ConvectiveFluxReconstructor.hpp:46-50). */
+int hmr_num_ghosts(const hmr_ctx* ctx);
+/* Pre-sizes the context's scratch for patches up to this geometry (needed before stream capture). */
+int hmr_ctx_reserve(hmr_ctx* ctx, const hmr_patch_geometry* geom);
+/* Face counters accumulated by the flux entry points since the last reset:
+ * out[0] = faces reverted to first order by the bounds check,
+ * out[1] = faces where the shock sensor selected HLLC-HLL.  Synchronises the device. */
+int hmr_read_counters(hmr_ctx* ctx, unsigned long long out[2], int reset);
+
+/* ConvectiveFluxReconstructorWCNS56::computeConvectiveFluxAndSourceOnPatch
+ * (ConvectiveFluxReconstructorWCNS56-HLLC-HLL.cpp:40-2656): dt-scaled convective face
+ * fluxes (overwritten) and the advective source (accumulated, +=) of one patch whose
+ * ghost cells are filled. */
+int hmr_conv_flux_source_patch(hmr_ctx* ctx, const hmr_patch_geometry* geom, const double* const* Q,
+                               double dt, double* const* flux, double* const* source, void* stream);
+
+/* Euler::advanceSingleStepOnPatch (src/apps/Euler/Euler.cpp:1003-1680) for one stage:
+ *   Q = sum_n alpha[n] Q_int[n] + beta[n] * (-div F_int[n] + S_int[n]),
+ *   flux_acc += gamma[n] F_int[n], source_acc += gamma[n] S_int[n] (both optional, NULL to skip),
+ * followed by updateCellDataOfConservativeVariables.  num_coeffs <= 4.  Q's interior is written. */
+int hmr_rk_stage_patch(hmr_ctx* ctx, const hmr_patch_geometry* geom, int num_coeffs,
+                       const double* alpha, const double* beta, const double* gamma,
+                       const double* const* const* Q_int, const double* const* const* F_int,
+                       const double* const* const* S_int, double* const* Q,
+                       double* const* flux_acc, double* const* source_acc, void* stream);
+
+/* Fused flux + stage update of stage `stage` of a Shu-Osher scheme whose flux weight is
+ * non-zero only for the current stage (SSPRK3 is): computes the convective flux and source
+ * of Q_int[stage] and writes Q_out = sum_n alpha[n] Q_int[n] + beta * (-div F + S) on the
+ * interior.  Q_int has stage+1 states; Q_int[stage] must have its ghost cells filled. */
+int hmr_rk_substep_patch(hmr_ctx* ctx, const hmr_patch_geometry* geom, int stage, const double* alpha,
+                         double beta, const double* const* const* Q_int, double dt, double* const* Q_out,
+                         void* stream);
+
+/* Single-patch ghost fill: periodic along axes with periodic[a] != 0, zero-gradient otherwise
+ * (one-patch equivalent of the SAMRAI fill schedule, RungeKuttaLevelIntegrator.cpp:1568,1701). */
+int hmr_fill_ghosts_patch(hmr_ctx* ctx, const hmr_patch_geometry* geom, double* const* Q,
+                          const int* periodic, void* stream);
+
+/* Batched form: every patch of a level advanced by one persistent kernel per RK substep over a
+ * device-resident worklist (replaces the patch loop of RungeKuttaLevelIntegrator.cpp:1717-1743).
+ * The caller owns each patch's state (slot 0, bound with hmr_level_bind_state); the level owns
+ * the intermediate stage buffers (slots 1, 2), the scratch and the captured step graph. */
+int hmr_level_create(hmr_ctx* ctx, int num_patches, const hmr_patch_geometry* geoms, hmr_level** out);
+int hmr_level_destroy(hmr_level* level);
+/* Binds the caller's ghost-box arrays (ncomp device pointers) as slot 0 of a patch. */
+int hmr_level_bind_state(hmr_level* level, int patch, double* const* comps);
+/* Device pointers of the stage-`slot` state of a patch (slot 0: the bound arrays). */
+int hmr_level_state(hmr_level* level, int patch, int slot, double** comps_out);
+/* Ghost fill of a patch whose box spans the whole domain: periodic along axes with
+ * periodic[a] != 0, zero-gradient on the others (default: zero-gradient everywhere). */
+int hmr_level_set_periodic(hmr_level* level, int patch, const int* periodic);
+/* Runs substep `stage` (0..2 of SSPRK3) for all patches as one captured CUDA graph (barrier
+ * reset + one persistent kernel: ghost fill, cells, sensor, faces, update).  Reads slots
+ * 0..stage, writes slot stage+1 (slot 0 for the last stage).  The graph is captured on the
+ * first call for a given dt, so the first call should precede any outer stream capture. */
+int hmr_level_substep(hmr_level* level, int stage, double dt, void* stream);
+/* One SSPRK3 step: the three substep graphs in order. */
+int hmr_level_step(hmr_level* level, double dt, void* stream);
+/* Synchronises and reports whether a barrier of a persistent kernel gave up
+ * (HMR_ERR_BARRIER, flag cleared) since the last check. */
+int hmr_level_check(hmr_level* level);
+/* Diagnostic: bound every barrier wait by timeout_ns and, with extra_arrivals = 1, make the
+ * first barrier unreachable so that the give-up path can be tested.  Use (0, 2e9) to restore. */
+int hmr_level_barrier_diagnostic(hmr_level* level, unsigned int extra_arrivals, unsigned long long timeout_ns);
+/* Autotuner: times the persistent kernel of this level at 64/128/256 threads per block and
+ * every resident block count per SM, keeps the fastest.  Returns the chosen shape. */
+int hmr_level_autotune(hmr_level* level, double dt, int* threads_out, int* blocks_per_sm_out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HMR_H */

@@ -1,0 +1,70 @@
+"""Shared helpers of the test suite: problem set-ups and comparisons."""
+import math
+
+import numpy as np
+
+from hamers_gb300 import problems as P
+from oracle import oracle as O
+
+GHOST = 4
+
+
+def n3(n):
+    return list(n) + [1] * (3 - len(n))
+
+
+def smooth_state(model, dim, n, seed=0, amp=0.3, species_gamma=None):
+    """A smooth but non-trivial state with every component varying (ghost box)."""
+    rng = np.random.default_rng(seed)
+    nn = n3(n)
+    G = [nn[d] + 2 * GHOST if d < dim else 1 for d in range(3)]
+    axes = [np.arange(G[d]) / max(1, nn[d]) for d in range(3)]
+    z, y, x = np.meshgrid(axes[2], axes[1], axes[0], indexing="ij")
+    X = [x, y, z][:dim]
+
+    def wave(k):
+        ph = rng.uniform(0, 2 * math.pi, 3)
+        return sum(np.sin(2 * math.pi * (d + 1) * X[d] + ph[d] + k) for d in range(dim))
+
+    vel = [0.3 * wave(1 + k) for k in range(dim)]
+    p = 1.0 + 0.2 * wave(7)
+    if model == O.MODEL_SINGLE_SPECIES:
+        rho = 1.0 + amp * wave(3) / dim
+        return np.ascontiguousarray(P.single_species_state(rho, vel, p, (species_gamma or [1.4])[0]))
+    Z1 = 0.5 + 0.4 * np.tanh(2.0 * wave(5))
+    return np.ascontiguousarray(P.five_eqn_state(Z1, 1.0 + 0.2 * wave(9), 3.0, vel, p,
+                                                 tuple(species_gamma or [1.4, 1.67])))
+
+
+def shock_state(model, dim, n, seed=0, species_gamma=None):
+    """Discontinuous data: a pressure/density jump plus a shear layer (exercises HLLC-HLL and LD switches)."""
+    rng = np.random.default_rng(seed)
+    nn = n3(n)
+    G = [nn[d] + 2 * GHOST if d < dim else 1 for d in range(3)]
+    axes = [(np.arange(G[d]) - GHOST + 0.5) / max(1, nn[d]) for d in range(3)]
+    z, y, x = np.meshgrid(axes[2], axes[1], axes[0], indexing="ij")
+    X = [x, y, z][:dim]
+    front = 0.45 + 0.05 * np.sin(2 * math.pi * X[1])
+    left = X[0] < front
+    u = np.where(left, 0.8, -0.1) + 0.01 * rng.standard_normal(x.shape)
+    v = np.where(X[1] < 0.5, 0.3, -0.3)
+    vel = [u, v] + ([0.1 * np.sin(2 * math.pi * X[2])] if dim == 3 else [])
+    p = np.where(left, 4.0, 1.0)
+    if model == O.MODEL_SINGLE_SPECIES:
+        rho = np.where(left, 2.5, 1.0)
+        return np.ascontiguousarray(P.single_species_state(rho, vel, p, (species_gamma or [1.4])[0]))
+    Z1 = np.clip(np.where(X[0] < 0.6, 1.0 - 1e-6, 1e-6), 1e-8, 1 - 1e-8)
+    return np.ascontiguousarray(P.five_eqn_state(Z1, np.where(left, 2.0, 1.0), 3.0, vel, p,
+                                                 tuple(species_gamma or [1.4, 1.67])))
+
+
+def rel_err(a, b):
+    """max |a-b| / max(|b|, component scale), component scale = max |b| of that component."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    worst = 0.0
+    for e in range(b.shape[0]):
+        scale = max(np.abs(b[e]).max(), 1e-300)
+        den = np.maximum(np.abs(b[e]), scale)
+        worst = max(worst, float((np.abs(a[e] - b[e]) / den).max()))
+    return worst

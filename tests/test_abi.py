@@ -1,0 +1,58 @@
+"""The C-ABI library loads and exports every symbol include/hmr.h declares (no GPU needed)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from hamers_gb300 import _lib as L
+from hamers_gb300 import build
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    src = open(os.path.join(ROOT, "include", "hmr.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"^int\s+(hmr_\w+)\s*\(", src, flags=re.M)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return L.load()
+
+
+def test_header_and_binding_agree():
+    assert declared_functions() == sorted(L.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+
+
+def test_config_defaults_match_reference(lib):
+    cfg = L.Config()
+    assert lib.hmr_config_default(ctypes.byref(cfg), L.HMR_FIVE_EQN_ALLAIRE, L.HMR_WCNS6_LD_HLLC_HLL, 2, 2) == 0
+    assert (cfg.constant_p, cfg.constant_q, cfg.constant_C, cfg.constant_alpha_tau) == (2, 4, 1.0e9, 35.0)
+    assert cfg.precision == L.HMR_PRECISION_FAST
+
+
+@pytest.mark.parametrize("field,value", [("dim", 1), ("dim", 4), ("num_species", 0), ("constant_p", 0),
+                                         ("convective_flux_reconstructor", 7), ("precision", 9)])
+def test_ctx_create_rejects_bad_config_before_touching_a_device(lib, field, value):
+    cfg = L.Config()
+    lib.hmr_config_default(ctypes.byref(cfg), L.HMR_SINGLE_SPECIES, L.HMR_WCNS5_JS_HLLC_HLL, 2, 1)
+    setattr(cfg, field, value)
+    ctx = ctypes.c_void_p()
+    rc = lib.hmr_ctx_create(ctypes.byref(cfg), ctypes.byref(ctx))
+    assert rc in (L.HMR_ERR_ARGUMENT, L.HMR_ERR_UNSUPPORTED)
+    assert not ctx.value
+
+
+def test_null_arguments_are_rejected(lib):
+    assert lib.hmr_ctx_create(None, None) == L.HMR_ERR_ARGUMENT
+    assert lib.hmr_ctx_destroy(None) == L.HMR_ERR_ARGUMENT
+    assert lib.hmr_conv_flux_source_patch(None, None, None, 0.0, None, None, None) == L.HMR_ERR_ARGUMENT
+    assert lib.hmr_level_destroy(None) == L.HMR_ERR_ARGUMENT

@@ -1,0 +1,155 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle.
+
+Exact form: bitwise equality (same operation order, no FMA contraction).
+Fast form: max relative error <= 1e-12 per component, relative to
+max(|reference|, component scale) -- the benchmark spec's tolerance.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.helpers import n3, rel_err, shock_state, smooth_state
+
+TOL_FAST = 1e-12
+
+VARIANTS = [
+    # model, dim, scheme, n, species_gamma
+    (O.MODEL_SINGLE_SPECIES, 2, O.SCHEME_WCNS5_JS, (37, 29), [1.4]),
+    (O.MODEL_SINGLE_SPECIES, 2, O.SCHEME_WCNS6_LD, (37, 29), [1.4]),
+    (O.MODEL_SINGLE_SPECIES, 3, O.SCHEME_WCNS5_JS, (13, 11, 9), [1.4]),
+    (O.MODEL_SINGLE_SPECIES, 3, O.SCHEME_WCNS6_LD, (13, 11, 9), [1.4]),
+    (O.MODEL_FIVE_EQN_ALLAIRE, 2, O.SCHEME_WCNS5_JS, (33, 27), [1.4, 1.67]),
+    (O.MODEL_FIVE_EQN_ALLAIRE, 2, O.SCHEME_WCNS6_LD, (33, 27), [1.4, 1.67]),
+    (O.MODEL_FIVE_EQN_ALLAIRE, 3, O.SCHEME_WCNS5_JS, (12, 10, 9), [1.4, 1.09]),
+    (O.MODEL_FIVE_EQN_ALLAIRE, 3, O.SCHEME_WCNS6_LD, (12, 10, 9), [1.4, 1.09]),
+]
+IDS = ["%s-%dd-%s" % ("single" if m == 0 else "five", d, "js" if s == 0 else "ld") for m, d, s, _, _ in VARIANTS]
+
+NAMES = {O.MODEL_SINGLE_SPECIES: "SINGLE_SPECIES", O.MODEL_FIVE_EQN_ALLAIRE: "FIVE_EQN_ALLAIRE"}
+SCHEMES = {O.SCHEME_WCNS5_JS: "WCNS5_JS_HLLC_HLL", O.SCHEME_WCNS6_LD: "WCNS6_LD_HLLC_HLL"}
+
+
+def make(model, dim, scheme, gam, precision):
+    from hamers_gb300 import flow
+    fm = flow.FlowModel(NAMES[model], dim, gam)
+    return flow.ConvectiveFluxReconstructor(SCHEMES[scheme], fm, precision=precision)
+
+
+def gpu_flux(rec, n, dx, dt, Qnp):
+    import torch
+    from hamers_gb300 import flow
+    Q = torch.from_numpy(Qnp).cuda()
+    patch = flow.Patch(n, dx, Q)
+    F = rec.allocateFlux(patch)
+    S = rec.allocateSource(patch)
+    rec.computeConvectiveFluxAndSourceOnPatch(patch, F, S, dt)
+    torch.cuda.synchronize()
+    return [f.cpu().numpy() for f in F], S.cpu().numpy()
+
+
+def states(model, dim, n, gam):
+    return [("smooth", smooth_state(model, dim, n, seed=1, species_gamma=gam)),
+            ("shock", shock_state(model, dim, n, seed=2, species_gamma=gam))]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("variant", VARIANTS, ids=IDS)
+def test_flux_source_exact_is_bitwise(cuda, variant):
+    model, dim, scheme, n, gam = variant
+    cfg = O.Config(model, dim, gam, scheme)
+    rec = make(model, dim, scheme, gam, "exact")
+    dx = [1.0 / v for v in n]
+    dt = 1.3e-3
+    for label, Q in states(model, dim, n, gam):
+        Fo, So, st = O.conv_flux_source(cfg, n, dx, dt, Q)
+        Fg, Sg = gpu_flux(rec, n, dx, dt, Q)
+        for a in range(dim):
+            assert np.array_equal(Fg[a], Fo[a]), f"{label}: flux axis {a} differs (max {np.abs(Fg[a]-Fo[a]).max()})"
+        assert np.array_equal(Sg, So), f"{label}: source differs"
+        fb, hh = rec.readCounters()
+        assert (fb, hh) == (st[1], st[2]), f"{label}: counters {fb, hh} vs oracle {st[1:]}"
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("variant", VARIANTS, ids=IDS)
+def test_flux_source_fast_within_tolerance(cuda, variant):
+    model, dim, scheme, n, gam = variant
+    cfg = O.Config(model, dim, gam, scheme)
+    rec = make(model, dim, scheme, gam, "fast")
+    dx = [1.0 / v for v in n]
+    dt = 1.3e-3
+    for label, Q in states(model, dim, n, gam):
+        Fo, So, st = O.conv_flux_source(cfg, n, dx, dt, Q)
+        Fg, Sg = gpu_flux(rec, n, dx, dt, Q)
+        for a in range(dim):
+            err = rel_err(Fg[a], Fo[a])
+            assert err <= TOL_FAST, f"{label}: flux axis {a} rel err {err:.3e}"
+        if model == O.MODEL_FIVE_EQN_ALLAIRE:
+            err = rel_err(Sg[-1:], So[-1:])
+            assert err <= TOL_FAST, f"{label}: source rel err {err:.3e}"
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("variant", VARIANTS, ids=IDS)
+@pytest.mark.parametrize("precision", ["exact", "fast"])
+def test_rk3_steps(cuda, variant, precision):
+    """Two SSPRK3 steps with periodic ghost fill: the fused substep path against the oracle."""
+    import torch
+    from hamers_gb300 import flow
+    model, dim, scheme, n, gam = variant
+    cfg = O.Config(model, dim, gam, scheme)
+    rec = make(model, dim, scheme, gam, precision)
+    dx = [1.0 / v for v in n]
+    dt = 2.0e-3
+    Q = smooth_state(model, dim, n, seed=3, species_gamma=gam)
+    per = [1] * dim
+    Qo = Q.copy()
+    O.fill_ghosts(cfg, n, per, Qo)
+    O.rk3_advance(cfg, n, dx, dt, per, 2, Qo)
+    Qg = torch.from_numpy(Q).cuda()
+    integ = flow.RungeKuttaLevelIntegrator(flow.Euler(rec), flow.Patch(n, dx, Qg), per)
+    integ.advance(dt, nsteps=2)
+    out = Qg.cpu().numpy()
+    if precision == "exact":
+        assert np.array_equal(out, Qo), f"max diff {np.abs(out - Qo).max()}"
+    else:
+        err = rel_err(out, Qo)
+        assert err <= TOL_FAST, f"rel err {err:.3e}"
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("variant", VARIANTS[:1] + VARIANTS[4:5] + VARIANTS[6:7], ids=[IDS[0], IDS[4], IDS[6]])
+def test_rk_stage_general(cuda, variant):
+    """advanceSingleStepOnPatch with all three coefficient sets and flux/source accumulation."""
+    import torch
+    from hamers_gb300 import flow
+    model, dim, scheme, n, gam = variant
+    cfg = O.Config(model, dim, gam, scheme)
+    rec = make(model, dim, scheme, gam, "exact")
+    eu = flow.Euler(rec)
+    dx = [1.0 / v for v in n]
+    rng = np.random.default_rng(5)
+    Qs = [smooth_state(model, dim, n, seed=10 + k, species_gamma=gam) for k in range(3)]
+    Fs, Ss = [], []
+    for k in range(3):
+        F, S, _ = O.conv_flux_source(cfg, n, dx, 1e-3, Qs[k])
+        Fs.append(F)
+        Ss.append(S + 1e-3 * rng.standard_normal(S.shape))
+    alpha, beta, gamma = [0.3, 0.2, 0.5], [0.1, 0.25, 0.6], [0.2, 0.3, 0.5]
+    Facc = [np.full(f.shape, 0.5) for f in Fs[0]]
+    Sacc = np.full(Ss[0].shape, 0.25)
+    Qo = O.rk_stage(cfg, n, dx, alpha, beta, gamma, Qs, Fs, Ss, F_acc=Facc, S_acc=Sacc)
+    tQ = [torch.from_numpy(q).cuda() for q in Qs]
+    tF = [[torch.from_numpy(f).cuda() for f in F] for F in Fs]
+    tS = [torch.from_numpy(s).cuda() for s in Ss]
+    tFa = [torch.full(f.shape, 0.5, dtype=torch.float64, device="cuda") for f in Fs[0]]
+    tSa = torch.full(Ss[0].shape, 0.25, dtype=torch.float64, device="cuda")
+    out = torch.zeros_like(tQ[0])
+    eu.advanceSingleStepOnPatch(flow.Patch(n, dx, out), alpha, beta, gamma, tQ, tF, tS, tFa, tSa)
+    torch.cuda.synchronize()
+    g = 4
+    sl = (slice(None),) + tuple(slice(g, -g) if d < dim else slice(None) for d in (2, 1, 0))
+    assert np.array_equal(out.cpu().numpy()[sl], Qo[sl])
+    for a in range(dim):
+        assert np.array_equal(tFa[a].cpu().numpy(), Facc[a])
+    assert np.array_equal(tSa.cpu().numpy(), Sacc)

@@ -1,0 +1,47 @@
+"""Pins the oracle to the reference's own tests.
+
+The reference's CI runs its convergence problems and asserts the final L2
+rate (tests/2D_convergence_test_single_species/convergence_test.py:8-16,281):
+rate > 4.8 for WCNS5_JS_HLLC_HLL and > 5.8 for WCNS6_LD_HLLC_HLL, on grids
+N = 8, 16, 32, 64 with 8x8 patches, dt = 0.001*dx, 8*N/8 steps in 2D (N/8 in 3D).
+A periodic single level of 8x8 patches equals one periodic N x N patch, so the
+oracle runs one patch.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from hamers_gb300 import problems as P
+from oracle import oracle as O
+
+EXPECTED = {O.SCHEME_WCNS5_JS: 4.8, O.SCHEME_WCNS6_LD: 5.8}
+
+
+def l2_errors(model, dim, scheme, levels):
+    errs = []
+    for N in levels:
+        Q, dx, dt, nsteps, exact, gam = P.convergence_problem(model, dim, N)
+        cfg = O.Config(model, dim, gam, scheme)
+        O.fill_ghosts(cfg, [N] * dim, [1] * dim, Q)
+        O.rk3_advance(cfg, [N] * dim, dx, dt, [1] * dim, nsteps, Q)
+        Qi = P.interior(Q, dim)
+        field = Qi[0] if model == O.MODEL_SINGLE_SPECIES else Qi[-2]
+        e = np.abs(exact(nsteps * dt) - field)
+        errs.append(math.sqrt((e ** 2).mean()))
+    return errs
+
+
+@pytest.mark.parametrize("model", [O.MODEL_SINGLE_SPECIES, O.MODEL_FIVE_EQN_ALLAIRE], ids=["single", "five"])
+@pytest.mark.parametrize("scheme", [O.SCHEME_WCNS5_JS, O.SCHEME_WCNS6_LD], ids=["js", "ld"])
+def test_convergence_2d(model, scheme):
+    errs = l2_errors(model, 2, scheme, [8, 16, 32, 64])
+    rate = math.log2(errs[-2] / errs[-1])
+    assert rate > EXPECTED[scheme], (errs, rate)
+
+
+@pytest.mark.parametrize("model", [O.MODEL_SINGLE_SPECIES, O.MODEL_FIVE_EQN_ALLAIRE], ids=["single", "five"])
+def test_convergence_3d_js(model):
+    errs = l2_errors(model, 3, O.SCHEME_WCNS5_JS, [8, 16, 32])
+    rate = math.log2(errs[-2] / errs[-1])
+    assert rate > EXPECTED[O.SCHEME_WCNS5_JS], (errs, rate)
