@@ -162,59 +162,58 @@ __device__ __forceinline__ void cell_derived(const Params& P, const double* Q, d
 }
 
 // ----------------------------------------------------------------------------
-// Characteristic projection of one cell's primitive state for a face normal to A.
+// Characteristic projection at a face normal to A.
+//
+// Everything from the cell primitives to the smoothness indicators is
+// evaluated in the reference's operation order with explicitly rounded
+// products, in both arithmetic forms.  Smoothness indicators cancel heavily
+// on smooth data and the eps-regularised weights amplify their rounding near
+// discontinuities, so the reference's own rounding in W and beta is part of
+// its result at the 1e-12 level; reproducing it bit for bit keeps the fast
+// form within tolerance and keeps every discrete decision (the WCNS6-LD
+// tau-switch) identical.  The per-face factors below are the reference's
+// subexpressions, computed once per face instead of once per offset (same
+// bits).
 // ----------------------------------------------------------------------------
 template <int DIM, int MODEL, int NSP>
 struct FaceProj {
-    // exact form keeps the projection means; fast form keeps derived factors
-    double rb, cb;
-    double zb[NSP];
-#if HMR_FAST
-    double hrc;      // 1/2*rb*cb
-    double ic2;      // 1/(cb*cb)
-    double irc;      // 1/(rb*cb)
-    double zr[NSP];  // zb/(rb*cb*cb)
-    double hz[NSP];  // 1/2*zb/cb
-#endif
+    double rb, cb;          // projection means
+    double zb[NSP];         // partial-density means (five-equation model)
+    double m_hrc, p_hrc;    // (-1/2*rb)*cb, (1/2*rb)*cb
+    double ic2;             // 1/(cb*cb)
+    double irc;             // 1/(rb*cb)
+    double zr[NSP];         // zb/((rb*cb)*cb)
+    double hz[NSP];         // (1/2*zb)/cb
 };
 
 template <int DIM, int MODEL, int NSP>
 __device__ __forceinline__ void face_proj_setup(FaceProj<DIM, MODEL, NSP>& F) {
-#if HMR_FAST
-    if constexpr (MODEL == SINGLE_SPECIES) {
-        F.hrc = double(1)/double(2)*F.rb*F.cb;
-        F.ic2 = double(1)/(F.cb*F.cb);
-        F.irc = double(1)/(F.rb*F.cb);
-    } else {
-        F.hrc = double(1)/double(2)*F.rb*F.cb;
-        const double irc = double(1)/(F.rb*F.cb);
-        F.irc = irc;
-        const double icb = irc*F.rb;          // 1/cb
+    F.m_hrc = mul_(mul_(-double(1)/double(2), F.rb), F.cb);
+    F.p_hrc = mul_(mul_(double(1)/double(2), F.rb), F.cb);
+    F.ic2 = double(1)/mul_(F.cb, F.cb);
+    F.irc = double(1)/mul_(F.rb, F.cb);
+    if constexpr (MODEL != SINGLE_SPECIES) {
+        const double rcc = mul_(mul_(F.rb, F.cb), F.cb);
 #pragma unroll
         for (int s = 0; s < NSP; s++) {
-            F.zr[s] = F.zb[s]*irc*icb;
-            F.hz[s] = double(1)/double(2)*F.zb[s]*icb;
+            F.zr[s] = F.zb[s]/rcc;
+            F.hz[s] = mul_(double(1)/double(2), F.zb[s])/F.cb;
         }
     }
-#endif
 }
 
+// single: FlowModelBasicUtilitiesSingleSpecies.cpp:6135-6246 (2D), 3D block after it;
+// five:   FlowModelBasicUtilitiesFiveEqnAllaire.cpp:8540-8760 (2D), 3D block after it.
 template <int DIM, int MODEL, int NSP, int A>
 __device__ __forceinline__ void char_from_prim(const FaceProj<DIM, MODEL, NSP>& F, const double* V, double* W) {
     using M = Model<DIM, MODEL, NSP>;
     if constexpr (MODEL == SINGLE_SPECIES) {
         const double un = V[1 + A];
         const double p = V[DIM + 1];
-#if HMR_FAST
-        const double hp = double(1)/double(2)*p;
-        W[0] = hp - F.hrc*un;
-        W[1] = V[0] - F.ic2*p;
-        W[DIM + 1] = hp + F.hrc*un;
-#else
-        W[0] = -double(1)/double(2)*F.rb*F.cb*un + double(1)/double(2)*p;
-        W[1] = V[0] - double(1)/(F.cb*F.cb)*p;
-        W[DIM + 1] = double(1)/double(2)*F.rb*F.cb*un + double(1)/double(2)*p;
-#endif
+        const double hp = mul_(double(1)/double(2), p);
+        W[0] = add_(mul_(F.m_hrc, un), hp);
+        W[1] = sub_(V[0], mul_(F.ic2, p));
+        W[DIM + 1] = add_(mul_(F.p_hrc, un), hp);
         int t = 2;
 #pragma unroll
         for (int k = 0; k < DIM; k++) if (k != A) W[t++] = V[1 + k];
@@ -222,28 +221,19 @@ __device__ __forceinline__ void char_from_prim(const FaceProj<DIM, MODEL, NSP>& 
         const double un = V[NSP + A];
         const double p = V[NSP + DIM];
 #pragma unroll
-        for (int s = 0; s < NSP; s++) {
-#if HMR_FAST
-            W[1 + s] = V[s] - F.zr[s]*p;
-#else
-            W[1 + s] = V[s] - F.zb[s]/(F.rb*F.cb*F.cb)*p;
-#endif
-        }
+        for (int s = 0; s < NSP; s++) W[1 + s] = sub_(V[s], mul_(F.zr[s], p));
 #pragma unroll
         for (int s = 0; s < NSP - 1; s++) W[NSP + DIM + s] = V[M::IZ + s];
-#if HMR_FAST
-        W[0] = un - F.irc*p;
-        W[M::NEQ - 1] = un + F.irc*p;
-#else
-        W[0] = un - double(1)/(F.rb*F.cb)*p;
-        W[M::NEQ - 1] = un + double(1)/(F.rb*F.cb)*p;
-#endif
+        W[0] = sub_(un, mul_(F.irc, p));
+        W[M::NEQ - 1] = add_(un, mul_(F.irc, p));
         int t = NSP + 1;
 #pragma unroll
         for (int k = 0; k < DIM; k++) if (k != A) W[t++] = V[NSP + k];
     }
 }
 
+// single: FlowModelBasicUtilitiesSingleSpecies.cpp:7279-7330 (2D) and the 3D block;
+// five:   FlowModelBasicUtilitiesFiveEqnAllaire.cpp:9201-... (2D block).
 template <int DIM, int MODEL, int NSP, int A>
 __device__ __forceinline__ void prim_from_char(const FaceProj<DIM, MODEL, NSP>& F, const double* W, double* V) {
     using M = Model<DIM, MODEL, NSP>;
@@ -253,8 +243,8 @@ __device__ __forceinline__ void prim_from_char(const FaceProj<DIM, MODEL, NSP>& 
         V[0] = F.ic2*(W[0] + W[L]) + W[1];
         V[1 + A] = F.irc*(W[L] - W[0]);
 #else
-        V[0] = double(1)/(F.cb*F.cb)*W[0] + W[1] + double(1)/(F.cb*F.cb)*W[L];
-        V[1 + A] = -double(1)/(F.rb*F.cb)*W[0] + double(1)/(F.rb*F.cb)*W[L];
+        V[0] = F.ic2*W[0] + W[1] + F.ic2*W[L];
+        V[1 + A] = -F.irc*W[0] + F.irc*W[L];
 #endif
         int t = 2;
 #pragma unroll
@@ -266,8 +256,7 @@ __device__ __forceinline__ void prim_from_char(const FaceProj<DIM, MODEL, NSP>& 
 #if HMR_FAST
             V[s] = F.hz[s]*(W[L] - W[0]) + W[s + 1];
 #else
-            V[s] = -double(1)/double(2)*F.zb[s]/F.cb*W[0] + W[s + 1] +
-                double(1)/double(2)*F.zb[s]/F.cb*W[L];
+            V[s] = -F.hz[s]*W[0] + W[s + 1] + F.hz[s]*W[L];
 #endif
         }
 #pragma unroll
@@ -286,9 +275,9 @@ __device__ __forceinline__ void prim_from_char(const FaceProj<DIM, MODEL, NSP>& 
             }
         }
 #if HMR_FAST
-        V[NSP + DIM] = F.hrc*(W[L] - W[0]);
+        V[NSP + DIM] = F.p_hrc*(W[L] - W[0]);
 #else
-        V[NSP + DIM] = -double(1)/double(2)*F.rb*F.cb*W[0] + double(1)/double(2)*F.rb*F.cb*W[L];
+        V[NSP + DIM] = F.m_hrc*W[0] + F.p_hrc*W[L];
 #endif
     }
 }
@@ -296,22 +285,28 @@ __device__ __forceinline__ void prim_from_char(const FaceProj<DIM, MODEL, NSP>& 
 // ----------------------------------------------------------------------------
 // WCNS5-JS (U[m] = characteristic variable at cell face-3+m).
 // ----------------------------------------------------------------------------
-__device__ __forceinline__ void js_betas(const double* U, double& b0, double& b1, double& b2) {
-    b0 = double(1)/double(3)*(U[0]*(double(4)*U[0] - double(19)*U[1] + double(11)*U[2]) +
-         U[1]*(double(25)*U[1] - double(31)*U[2]) + double(10)*U[2]*U[2]);
-    b1 = double(1)/double(3)*(U[1]*(double(4)*U[1] - double(13)*U[2] + double(5)*U[3]) +
-         double(13)*U[2]*(U[2] - U[3]) + double(4)*U[3]*U[3]);
-    b2 = double(1)/double(3)*(U[2]*(double(10)*U[2] - double(31)*U[3] + double(11)*U[4]) +
-         U[3]*(double(25)*U[3] - double(19)*U[4]) + double(4)*U[4]*U[4]);
+// Smoothness indicators of the 3-point sub-stencils, S0..S4 ordered from the
+// upwind side (U[0..4] for the minus side, U[5..1] for the plus side), every
+// product explicitly rounded: see the note above char_from_prim.  WCNS6-LD's
+// tau-switch (R_tau > alpha_tau) is a discrete decision on these values.
+__device__ __forceinline__ double lin3x(double c0, double a0, double c1, double a1, double c2, double a2) {
+    return add_(sub_(mul_(c0, a0), mul_(c1, a1)), mul_(c2, a2));
 }
 
-__device__ __forceinline__ void js_betas_tilde(const double* U, double& b0, double& b1, double& b2) {
-    b0 = double(1)/double(3)*(U[5]*(double(4)*U[5] - double(19)*U[4] + double(11)*U[3]) +
-         U[4]*(double(25)*U[4] - double(31)*U[3]) + double(10)*U[3]*U[3]);
-    b1 = double(1)/double(3)*(U[4]*(double(4)*U[4] - double(13)*U[3] + double(5)*U[2]) +
-         double(13)*U[3]*(U[3] - U[2]) + double(4)*U[2]*U[2]);
-    b2 = double(1)/double(3)*(U[3]*(double(10)*U[3] - double(31)*U[2] + double(11)*U[1]) +
-         U[2]*(double(25)*U[2] - double(19)*U[1]) + double(4)*U[1]*U[1]);
+__device__ __forceinline__ void js_betas_x(double S0, double S1, double S2, double S3, double S4,
+                                           double& b0, double& b1, double& b2) {
+    // b0 = 1/3*(S0*(4*S0 - 19*S1 + 11*S2) + S1*(25*S1 - 31*S2) + 10*S2*S2)
+    b0 = mul_(double(1)/double(3), add_(add_(mul_(S0, lin3x(4.0, S0, 19.0, S1, 11.0, S2)),
+                                            mul_(S1, sub_(mul_(25.0, S1), mul_(31.0, S2)))),
+                                       mul_(mul_(10.0, S2), S2)));
+    // b1 = 1/3*(S1*(4*S1 - 13*S2 + 5*S3) + 13*S2*(S2 - S3) + 4*S3*S3)
+    b1 = mul_(double(1)/double(3), add_(add_(mul_(S1, lin3x(4.0, S1, 13.0, S2, 5.0, S3)),
+                                            mul_(mul_(13.0, S2), sub_(S2, S3))),
+                                       mul_(mul_(4.0, S3), S3)));
+    // b2 = 1/3*(S2*(10*S2 - 31*S3 + 11*S4) + S3*(25*S3 - 19*S4) + 4*S4*S4)
+    b2 = mul_(double(1)/double(3), add_(add_(mul_(S2, lin3x(10.0, S2, 31.0, S3, 11.0, S4)),
+                                            mul_(S3, sub_(mul_(25.0, S3), mul_(19.0, S4)))),
+                                       mul_(mul_(4.0, S4), S4)));
 }
 
 // Weighted 5-point midpoint value: S0..S4 are the stencil values ordered from
@@ -342,9 +337,9 @@ __device__ __forceinline__ double js_interp(double b0, double b1, double b2, int
 
 __device__ __forceinline__ void js_pair(const double* U, int p, double& Um, double& Up) {
     double b0, b1, b2;
-    js_betas(U, b0, b1, b2);
+    js_betas_x(U[0], U[1], U[2], U[3], U[4], b0, b1, b2);
     Um = js_interp(b0, b1, b2, p, U[0], U[1], U[2], U[3], U[4]);
-    js_betas_tilde(U, b0, b1, b2);
+    js_betas_x(U[5], U[4], U[3], U[2], U[1], b0, b1, b2);
     Up = js_interp(b0, b1, b2, p, U[5], U[4], U[3], U[2], U[1]);
 }
 
@@ -360,29 +355,37 @@ __device__ __forceinline__ double ld_sigma(const double* U) {
     return fmax(t1, t2);
 }
 
-// beta_3 with the stencil ordered from the upwind side (S0..S5).
+// beta_3 with the stencil ordered from the upwind side (S0..S5), every
+// product explicitly rounded (see js_betas_x).
 __device__ __forceinline__ double ld_beta3(double S0, double S1, double S2, double S3, double S4, double S5) {
-    return double(1)/double(232243200)*(S0*(double(525910327)*S0 -
-         double(4562164630)*S1 + double(7799501420)*S2 -
-         double(6610694540)*S3 + double(2794296070)*S4 -
-         double(472758974)*S5) + double(5)*S1*
-        (double(2146987907)*S1 - double(7722406988)*S2 +
-         double(6763559276)*S3 - double(2926461814)*S4 +
-         double(503766638)*S5) + double(20)*S2*
-        (double(1833221603)*S2 - double(3358664662)*S3 +
-         double(1495974539)*S4 - double(263126407)*S5) +
-        double(20)*S3*(double(1607794163)*S3 -
-         double(1486026707)*S4 + double(268747951)*S5) +
-        double(5)*S4*(double(1432381427)*S4 -
-         double(536951582)*S5) +
-        double(263126407)*S5*S5);
+    // S0*(525910327*S0 - 4562164630*S1 + 7799501420*S2 - 6610694540*S3 + 2794296070*S4 - 472758974*S5)
+    const double t0 = mul_(S0, sub_(add_(sub_(add_(sub_(mul_(525910327.0, S0), mul_(4562164630.0, S1)),
+                                                  mul_(7799501420.0, S2)), mul_(6610694540.0, S3)),
+                                        mul_(2794296070.0, S4)), mul_(472758974.0, S5)));
+    // 5*S1*(2146987907*S1 - 7722406988*S2 + 6763559276*S3 - 2926461814*S4 + 503766638*S5)
+    const double t1 = mul_(mul_(5.0, S1), add_(sub_(add_(sub_(mul_(2146987907.0, S1), mul_(7722406988.0, S2)),
+                                                        mul_(6763559276.0, S3)), mul_(2926461814.0, S4)),
+                                              mul_(503766638.0, S5)));
+    // 20*S2*(1833221603*S2 - 3358664662*S3 + 1495974539*S4 - 263126407*S5)
+    const double t2 = mul_(mul_(20.0, S2), sub_(add_(sub_(mul_(1833221603.0, S2), mul_(3358664662.0, S3)),
+                                                    mul_(1495974539.0, S4)), mul_(263126407.0, S5)));
+    // 20*S3*(1607794163*S3 - 1486026707*S4 + 268747951*S5)
+    const double t3 = mul_(mul_(20.0, S3), add_(sub_(mul_(1607794163.0, S3), mul_(1486026707.0, S4)),
+                                               mul_(268747951.0, S5)));
+    // 5*S4*(1432381427*S4 - 536951582*S5)
+    const double t4 = mul_(mul_(5.0, S4), sub_(mul_(1432381427.0, S4), mul_(536951582.0, S5)));
+    // 263126407*S5*S5
+    const double t5 = mul_(mul_(263126407.0, S5), S5);
+    return mul_(double(1)/double(232243200), add_(add_(add_(add_(add_(t0, t1), t2), t3), t4), t5));
 }
 
 __device__ __forceinline__ double ld_interp(const double* b, double sigma, const Params& P,
                                             double S0, double S1, double S2, double S3, double S4, double S5) {
     const double tau_5 = fabs(b[0] - b[2]);
-    const double beta_avg = double(1)/double(8)*(b[0] + b[2] + double(6)*b[1]);
+    const double beta_avg = mul_(double(1)/double(8), add_(add_(b[0], b[2]), mul_(double(6), b[1])));
     const double tau_6 = fabs(b[3] - beta_avg);
+    const double R_tau = tau_6/(beta_avg + HMR_EPS);
+    const bool blend = R_tau > P.alpha_tau;
     double o0, o1, o2, o3;
 #if HMR_FAST
     const double r0 = double(1)/(b[0] + HMR_EPS);
@@ -400,7 +403,6 @@ __device__ __forceinline__ double ld_interp(const double* b, double sigma, const
     o3 = double(1)/double(32)*(P.C + ipow_d(tau_6*r3, P.q));
     const double ro = double(1)/(o0 + o1 + o2 + o3);
     o0 *= ro; o1 *= ro; o2 *= ro; o3 *= ro;
-    const bool blend = tau_6 > P.alpha_tau*(beta_avg + HMR_EPS);
 #else
     double u0 = double(1)/double(16)*(double(1) + ipow_d(tau_5/(b[0] + HMR_EPS), P.p));
     double u1 = double(5)/double(8)*(double(1) + ipow_d(tau_5/(b[1] + HMR_EPS), P.p));
@@ -413,8 +415,6 @@ __device__ __forceinline__ double ld_interp(const double* b, double sigma, const
     o3 = double(1)/double(32)*(P.C + ipow_d(tau_6/(b[3] + HMR_EPS), P.q));
     const double os = o0 + o1 + o2 + o3;
     o0 = o0/os; o1 = o1/os; o2 = o2/os; o3 = o3/os;
-    const double R_tau = tau_6/(beta_avg + HMR_EPS);
-    const bool blend = R_tau > P.alpha_tau;
 #endif
     if (blend) {
         o0 = sigma*u0 + (double(1) - sigma)*o0;
@@ -433,10 +433,10 @@ __device__ __forceinline__ double ld_interp(const double* b, double sigma, const
 __device__ __forceinline__ void ld_pair(const double* U, const Params& P, double& Um, double& Up) {
     const double sigma = ld_sigma(U);
     double b[4];
-    js_betas(U, b[0], b[1], b[2]);
+    js_betas_x(U[0], U[1], U[2], U[3], U[4], b[0], b[1], b[2]);
     b[3] = ld_beta3(U[0], U[1], U[2], U[3], U[4], U[5]);
     Um = ld_interp(b, sigma, P, U[0], U[1], U[2], U[3], U[4], U[5]);
-    js_betas_tilde(U, b[0], b[1], b[2]);
+    js_betas_x(U[5], U[4], U[3], U[2], U[1], b[0], b[1], b[2]);
     b[3] = ld_beta3(U[5], U[4], U[3], U[2], U[1], U[0]);
     Up = ld_interp(b, sigma, P, U[5], U[4], U[3], U[2], U[1], U[0]);
 }
