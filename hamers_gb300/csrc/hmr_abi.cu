@@ -21,6 +21,7 @@ struct hmr_ctx {
     double* scratch = nullptr;
     size_t scratch_bytes = 0;
     Counters* counters = nullptr;
+    unsigned int* redo_count = nullptr;
 };
 
 struct hmr_level {
@@ -33,8 +34,10 @@ struct hmr_level {
     double* d_scratch = nullptr;
     std::vector<size_t> state_off;     // per patch, in doubles
     LevelArgs L = {};
-    unsigned int* d_barrier = nullptr;
+    unsigned int* d_barrier = nullptr;   // [0] barrier arrivals, [1] redo-queue length
     int* d_status = nullptr;
+    unsigned long long* d_redo = nullptr;
+    long redo_cap = 0;
     int threads = 128;
     int blocks = 0;
     // one captured graph per substep (barrier reset + persistent kernel)
@@ -70,12 +73,19 @@ static bool valid_geom(int dim, const hmr_patch_geometry* pg) {
     return cells < (1L << 40);
 }
 
-// Scratch size in doubles for one patch.
+// Scratch size in doubles for one patch (cell data, midpoint fluxes and
+// velocities, and the queue of faces handed to the exact form).
 static size_t scratch_doubles(const hmr_ctx* c, const Geom& g) {
     const long nc = ncell_of(g);
     size_t s = (size_t)(c->neq + 4) * nc;
-    for (int a = 0; a < c->v.dim; a++) s += (size_t)(c->neq + 1) * nface_of(g, a);
+    for (int a = 0; a < c->v.dim; a++) s += (size_t)(c->neq + 2) * nface_of(g, a);
     return s + 64;
+}
+
+static long total_faces(const hmr_ctx* c, const Geom& g) {
+    long t = 0;
+    for (int a = 0; a < c->v.dim; a++) t += nface_of(g, a);
+    return t;
 }
 
 static Scratch carve_scratch(const hmr_ctx* c, const Geom& g, double* base) {
@@ -113,8 +123,13 @@ static int ensure_scratch(hmr_ctx* c, const Geom& g) {
 }
 
 static int face_launch(hmr_ctx* c, const Geom& g, const Scratch& S, cudaStream_t st) {
-    if (c->precision == HMR_PRECISION_EXACT) return hmr_exact::launch_faces(c->v, c->P, g, S, c->counters, st);
-    return hmr_fast::launch_faces(c->v, c->P, g, S, c->counters, st);
+    Redo R;
+    // The queue follows the per-axis arrays carved by carve_scratch.
+    R.list = reinterpret_cast<unsigned long long*>(S.um[c->v.dim - 1] + nface_of(g, c->v.dim - 1));
+    R.count = c->redo_count;
+    R.cap = (unsigned long long)total_faces(c, g);
+    if (c->precision == HMR_PRECISION_EXACT) return hmr_exact::launch_faces(c->v, c->P, g, S, c->counters, R, st);
+    return hmr_fast::launch_faces(c->v, c->P, g, S, c->counters, R, st);
 }
 
 static int update_launch(hmr_ctx* c, const Geom& g, const Scratch& S, const UpdateArgs& U, cudaStream_t st) {
@@ -206,6 +221,7 @@ int hmr_ctx_create(const hmr_config* cfg, hmr_ctx** out) {
     c->ncomp = ncomp;
     cudaError_t e = cudaMalloc(&c->counters, sizeof(Counters));
     if (e == cudaSuccess) e = cudaMemset(c->counters, 0, sizeof(Counters));
+    if (e == cudaSuccess) e = cudaMalloc(&c->redo_count, sizeof(unsigned int));
     if (e != cudaSuccess) {
         delete c;
         return cuda_status(e);
@@ -218,6 +234,7 @@ int hmr_ctx_destroy(hmr_ctx* c) {
     if (!c) return HMR_ERR_ARGUMENT;
     if (c->scratch) cudaFree(c->scratch);
     if (c->counters) cudaFree(c->counters);
+    if (c->redo_count) cudaFree(c->redo_count);
     delete c;
     return HMR_OK;
 }
@@ -361,13 +378,16 @@ static LevelArgs stage_args(hmr_level* lv, int stage, double dt) {
     L.dt = dt;
     L.barrier = lv->d_barrier;
     L.status = lv->d_status;
+    L.redo.list = lv->d_redo;
+    L.redo.count = lv->d_barrier + 1;
+    L.redo.cap = (unsigned long long)lv->redo_cap;
     return L;
 }
 
 // Barrier reset + persistent kernel of one substep, enqueued on st.
 static int level_enqueue(hmr_level* lv, int stage, double dt, int threads, int blocks, cudaStream_t st) {
     hmr_ctx* c = lv->ctx;
-    cudaError_t e = cudaMemsetAsync(lv->d_barrier, 0, sizeof(unsigned int), st);
+    cudaError_t e = cudaMemsetAsync(lv->d_barrier, 0, 2 * sizeof(unsigned int), st);
     if (e != cudaSuccess) return cuda_status(e);
     const LevelArgs L = stage_args(lv, stage, dt);
     if (c->precision == HMR_PRECISION_EXACT) return hmr_exact::launch_level(c->v, c->P, L, blocks, threads, st);
@@ -466,12 +486,14 @@ int hmr_level_create(hmr_ctx* c, int np, const hmr_patch_geometry* geoms, hmr_le
         }
         w.off_update = off_update;
         off_update += ninterior_of(g);
+        lv->redo_cap += total_faces(c, g);
     }
     cudaError_t e = cudaMalloc(&lv->d_state, state_tot * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&lv->d_redo, (size_t)lv->redo_cap * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMemset(lv->d_state, 0, state_tot * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&lv->d_scratch, scratch_tot * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&lv->d_work, (size_t)3 * np * sizeof(PatchWork));
-    if (e == cudaSuccess) e = cudaMalloc(&lv->d_barrier, sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMalloc(&lv->d_barrier, 2 * sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMalloc(&lv->d_status, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(lv->d_status, 0, sizeof(int));
     if (e != cudaSuccess) {
@@ -517,6 +539,7 @@ int hmr_level_destroy(hmr_level* lv) {
     if (lv->d_work) cudaFree(lv->d_work);
     if (lv->d_barrier) cudaFree(lv->d_barrier);
     if (lv->d_status) cudaFree(lv->d_status);
+    if (lv->d_redo) cudaFree(lv->d_redo);
     delete lv;
     return HMR_OK;
 }

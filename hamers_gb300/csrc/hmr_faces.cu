@@ -39,12 +39,31 @@ static int dispatch(const Variant& v, F f) {
 constexpr int FACE_THREADS = 128;
 constexpr int UPDATE_THREADS = 128;
 
+// The exact form computes every face; the fast form queues the faces it hands
+// back (see face_item) for redo_kernel.
 template <int DIM, int MODEL, int NSP, int SCHEME, int A>
 __global__ void __launch_bounds__(FACE_THREADS)
-faces_kernel(Params P, Geom g, Scratch S, Counters* cnt) {
+faces_kernel(Params P, Geom g, Scratch S, Counters* cnt, Redo R) {
     const long nf = nface_of(g, A);
-    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < nf; t += (long)gridDim.x * blockDim.x)
-        face_item<DIM, MODEL, NSP, SCHEME, A>(P, g, S, t, cnt);
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < nf; t += (long)gridDim.x * blockDim.x) {
+        if (face_item<!HMR_FAST, DIM, MODEL, NSP, SCHEME, A>(P, g, S, t, cnt)) redo_push(R, A, t);
+    }
+}
+
+// Exact recomputation of the queued faces of one patch.
+template <int DIM, int MODEL, int NSP, int SCHEME>
+__global__ void __launch_bounds__(FACE_THREADS)
+redo_kernel(Params P, Geom g, Scratch S, Counters* cnt, Redo R) {
+    const unsigned long long n = min((unsigned long long)*R.count, R.cap);
+    for (unsigned long long r = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; r < n;
+         r += (unsigned long long)gridDim.x * blockDim.x) {
+        const unsigned long long v = R.list[r];
+        const int a = (int)(v >> 56);
+        const long t = (long)(v & ((1ull << 56) - 1));
+        if (a == 0) face_item<true, DIM, MODEL, NSP, SCHEME, 0>(P, g, S, t, cnt);
+        else if (a == 1) face_item<true, DIM, MODEL, NSP, SCHEME, 1>(P, g, S, t, cnt);
+        else if constexpr (DIM == 3) face_item<true, DIM, MODEL, NSP, SCHEME, 2>(P, g, S, t, cnt);
+    }
 }
 
 template <int DIM, int MODEL, int NSP>
@@ -63,16 +82,26 @@ static inline int grid_for(long items, int threads) {
 }
 
 int launch_faces(const Variant& v, const Params& P, const Geom& g, const Scratch& S, Counters* cnt,
-                 cudaStream_t st) {
+                 const Redo& R, cudaStream_t st) {
     return dispatch(v, [&](auto t) {
         using T = decltype(t);
+        if (HMR_FAST) {
+            cudaError_t e = cudaMemsetAsync(R.count, 0, sizeof(unsigned int), st);
+            if (e != cudaSuccess) return (int)e;
+        }
         faces_kernel<T::DIM, T::MODEL, T::NSP, T::SCHEME, 0>
-            <<<grid_for(nface_of(g, 0), FACE_THREADS), FACE_THREADS, 0, st>>>(P, g, S, cnt);
+            <<<grid_for(nface_of(g, 0), FACE_THREADS), FACE_THREADS, 0, st>>>(P, g, S, cnt, R);
         faces_kernel<T::DIM, T::MODEL, T::NSP, T::SCHEME, 1>
-            <<<grid_for(nface_of(g, 1), FACE_THREADS), FACE_THREADS, 0, st>>>(P, g, S, cnt);
+            <<<grid_for(nface_of(g, 1), FACE_THREADS), FACE_THREADS, 0, st>>>(P, g, S, cnt, R);
         if constexpr (T::DIM == 3)
             faces_kernel<T::DIM, T::MODEL, T::NSP, T::SCHEME, 2>
-                <<<grid_for(nface_of(g, 2), FACE_THREADS), FACE_THREADS, 0, st>>>(P, g, S, cnt);
+                <<<grid_for(nface_of(g, 2), FACE_THREADS), FACE_THREADS, 0, st>>>(P, g, S, cnt, R);
+        if (HMR_FAST) {
+            int dev = 0, sms = 1;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            redo_kernel<T::DIM, T::MODEL, T::NSP, T::SCHEME><<<sms * 2, FACE_THREADS, 0, st>>>(P, g, S, cnt, R);
+        }
         return (int)cudaPeekAtLastError();
     });
 }
@@ -171,20 +200,46 @@ level_kernel(Params P, LevelArgs L) {
         sensor_item<DIM, MODEL, NSP>(W[p].g, W[p].S, t - W[p].off_sensor);
     }
     HMR_BARRIER();
+    constexpr bool X = !HMR_FAST;
     for (long t = t0; t < L.total_face[0]; t += stride) {
         const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_face[0]; });
-        face_item<DIM, MODEL, NSP, SCHEME, 0>(P, W[p].g, W[p].S, t - W[p].off_face[0], nullptr);
+        if (face_item<X, DIM, MODEL, NSP, SCHEME, 0>(P, W[p].g, W[p].S, t - W[p].off_face[0], nullptr))
+            redo_push(L.redo, 0, t);
     }
     for (long t = t0; t < L.total_face[1]; t += stride) {
         const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_face[1]; });
-        face_item<DIM, MODEL, NSP, SCHEME, 1>(P, W[p].g, W[p].S, t - W[p].off_face[1], nullptr);
+        if (face_item<X, DIM, MODEL, NSP, SCHEME, 1>(P, W[p].g, W[p].S, t - W[p].off_face[1], nullptr))
+            redo_push(L.redo, 1, t);
     }
     if constexpr (DIM == 3) {
         for (long t = t0; t < L.total_face[2]; t += stride) {
             const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_face[2]; });
-            face_item<DIM, MODEL, NSP, SCHEME, 2>(P, W[p].g, W[p].S, t - W[p].off_face[2], nullptr);
+            if (face_item<X, DIM, MODEL, NSP, SCHEME, 2>(P, W[p].g, W[p].S, t - W[p].off_face[2], nullptr))
+                redo_push(L.redo, 2, t);
         }
     }
+#if HMR_FAST
+    HMR_BARRIER();
+    {
+        // Exact recomputation of the faces the fast form handed back.
+        const unsigned long long nredo = min((unsigned long long)*((volatile unsigned int*)L.redo.count), L.redo.cap);
+        for (unsigned long long r = (unsigned long long)t0; r < nredo; r += (unsigned long long)stride) {
+            const unsigned long long v = L.redo.list[r];
+            const int a = (int)(v >> 56);
+            const long t = (long)(v & ((1ull << 56) - 1));
+            if (a == 0) {
+                const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_face[0]; });
+                face_item<true, DIM, MODEL, NSP, SCHEME, 0>(P, W[p].g, W[p].S, t - W[p].off_face[0], nullptr);
+            } else if (a == 1) {
+                const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_face[1]; });
+                face_item<true, DIM, MODEL, NSP, SCHEME, 1>(P, W[p].g, W[p].S, t - W[p].off_face[1], nullptr);
+            } else if constexpr (DIM == 3) {
+                const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_face[2]; });
+                face_item<true, DIM, MODEL, NSP, SCHEME, 2>(P, W[p].g, W[p].S, t - W[p].off_face[2], nullptr);
+            }
+        }
+    }
+#endif
     HMR_BARRIER();
 #undef HMR_BARRIER
     for (long t = t0; t < L.total_update; t += stride) {

@@ -128,10 +128,64 @@ __device__ __forceinline__ void sensor_item(const Geom& g, const Scratch& S, lon
 }
 
 // ---------------------------------------------------------------------------
-// Phase 3: one midpoint face normal to axis A.  item over faces(A).
+// Reconstruction + Riemann solve of one face from its characteristic stencil
+// W (6 x NEQ): WCNS interpolation, inverse projection, bounds check with
+// first-order fallback (WCNS56-HLLC-HLL.cpp:899-1032), HLLC / HLLC-HLL.
+// Returns the bounds flag; `margin` is the relative distance to the nearest
+// bound of the reconstructed states.
 // ---------------------------------------------------------------------------
-template <int DIM, int MODEL, int NSP, int SCHEME, int A>
-__device__ __forceinline__ void face_item(const Params& P, const Geom& g, const Scratch& S, long t,
+template <bool X, int DIM, int MODEL, int NSP, int SCHEME, int A>
+__device__ __forceinline__ bool face_eval(const Params& P, const FaceProj<DIM, MODEL, NSP>& F,
+                                          const double (&W)[6][Model<DIM, MODEL, NSP>::NEQ], const Scratch& S,
+                                          long nc, long xL, long xR, bool use_hll, double rref, double pref,
+                                          double* Fo, double& umid, double& margin) {
+    using M = Model<DIM, MODEL, NSP>;
+    constexpr int NEQ = M::NEQ;
+    double Wm[NEQ], Wp[NEQ];
+#pragma unroll
+    for (int e = 0; e < NEQ; e++) {
+        double U[6];
+#pragma unroll
+        for (int m = 0; m < 6; m++) U[m] = W[m][e];
+        if constexpr (SCHEME == WCNS5_JS) js_pair<X>(U, P.p, Wm[e], Wp[e]);
+        else ld_pair<X>(U, P, Wm[e], Wp[e]);
+    }
+    double VL[NEQ], VR[NEQ];
+    prim_from_char<X, DIM, MODEL, NSP, A>(F, Wm, VL);
+    prim_from_char<X, DIM, MODEL, NSP, A>(F, Wp, VR);
+    double mL, mR;
+    const bool ok = face_bounded<DIM, MODEL, NSP>(P, VL, mL) & face_bounded<DIM, MODEL, NSP>(P, VR, mR);
+    if constexpr (MODEL == SINGLE_SPECIES) {
+        // relative margins: density against the projection density, pressure against the cell pressures
+        mL = fmin(fabs(VL[0])/rref, fabs(VL[M::IP])/pref);
+        mR = fmin(fabs(VR[0])/rref, fabs(VR[M::IP])/pref);
+    }
+    margin = fmin(mL, mR);
+    if (!ok) {
+#pragma unroll
+        for (int e = 0; e < NEQ; e++) {
+            VL[e] = S.V[e * nc + xL];
+            VR[e] = S.V[e * nc + xR];
+        }
+    }
+    riemann<X, DIM, MODEL, NSP, A>(P, VL, VR, use_hll, Fo, umid);
+    return ok;
+}
+
+// ---------------------------------------------------------------------------
+// Phase 3: one midpoint face normal to axis A.  item over faces(A).
+//
+// The exact form (X = true) is the reference's operation order.  The fast form
+// (X = false) hands a face back (returns true) instead of computing it where
+// the reference's own result is ill-conditioned, and the caller queues it for
+// the exact form: HLLC-HLL faces (the blending weight sqrt(1 - alpha_1^2)
+// amplifies rounding when the velocity jump is almost purely normal),
+// first-order fallback faces, and faces whose reconstructed states lie within
+// 1e-9 (relative) of a bounds threshold.  Every other face of the fast form is
+// within rounding of the exact one.
+// ---------------------------------------------------------------------------
+template <bool X, int DIM, int MODEL, int NSP, int SCHEME, int A>
+__device__ __forceinline__ bool face_item(const Params& P, const Geom& g, const Scratch& S, long t,
                                           Counters* cnt) {
     using M = Model<DIM, MODEL, NSP>;
     constexpr int NEQ = M::NEQ;
@@ -145,13 +199,20 @@ __device__ __forceinline__ void face_item(const Params& P, const Geom& g, const 
     const long xR = cidx<DIM>(g, i, j, k);      // cell on the + side of the face
     const long xL = xR - st;
 
+    // Ducros-like sensor (WCNS56-HLLC-HLL.cpp:1066-1088); exact inputs.
+    const double theta_avg = 0.5*(S.theta[xL] + S.theta[xR]);
+    const double Omega_avg = 0.5*(S.Omega[xL] + S.Omega[xR]);
+    const double s = -theta_avg/(fabs(theta_avg) + Omega_avg + HMR_EPS);
+    const bool use_hll = s > 0.65;
+    if (!X && use_hll) return true;
+
     // Projection means (SIMPLE averaging).
     FaceProj<DIM, MODEL, NSP> F;
     F.rb = double(1)/double(2)*(S.rho[xL] + S.rho[xR]);
     F.cb = double(1)/double(2)*(S.cs[xL] + S.cs[xR]);
     if constexpr (MODEL != SINGLE_SPECIES) {
 #pragma unroll
-        for (int s = 0; s < NSP; s++) F.zb[s] = double(1)/double(2)*(S.V[s * nc + xL] + S.V[s * nc + xR]);
+        for (int q = 0; q < NSP; q++) F.zb[q] = double(1)/double(2)*(S.V[q * nc + xL] + S.V[q * nc + xR]);
     }
     face_proj_setup(F);
 
@@ -166,38 +227,14 @@ __device__ __forceinline__ void face_item(const Params& P, const Geom& g, const 
         char_from_prim<DIM, MODEL, NSP, A>(F, Vc, W[m]);
     }
 
-    // WCNS interpolation of each characteristic variable to the midpoint.
-    double Wm[NEQ], Wp[NEQ];
-#pragma unroll
-    for (int e = 0; e < NEQ; e++) {
-        double U[6];
-#pragma unroll
-        for (int m = 0; m < 6; m++) U[m] = W[m][e];
-        if constexpr (SCHEME == WCNS5_JS) js_pair(U, P.p, Wm[e], Wp[e]);
-        else ld_pair(U, P, Wm[e], Wp[e]);
-    }
-    double VL[NEQ], VR[NEQ];
-    prim_from_char<DIM, MODEL, NSP, A>(F, Wm, VL);
-    prim_from_char<DIM, MODEL, NSP, A>(F, Wp, VR);
+    double pref = 1.0;
+    if constexpr (MODEL == SINGLE_SPECIES)
+        pref = fmax(fabs(S.V[M::IP * nc + xL]), fabs(S.V[M::IP * nc + xR]));
+    double Fo[NEQ], umid, margin;
+    const bool ok = face_eval<X, DIM, MODEL, NSP, SCHEME, A>(P, F, W, S, nc, xL, xR, use_hll, F.rb, pref, Fo,
+                                                             umid, margin);
+    if (!X && (!ok || margin < 1.0e-9)) return true;
 
-    // Bounds check and first-order fallback (WCNS56-HLLC-HLL.cpp:934-1032).
-    const bool ok = face_bounded<DIM, MODEL, NSP>(P, VL) && face_bounded<DIM, MODEL, NSP>(P, VR);
-    if (!ok) {
-#pragma unroll
-        for (int e = 0; e < NEQ; e++) {
-            VL[e] = S.V[e * nc + xL];
-            VR[e] = S.V[e * nc + xR];
-        }
-    }
-
-    // Ducros-like sensor (WCNS56-HLLC-HLL.cpp:1066-1088).
-    const double theta_avg = 0.5*(S.theta[xL] + S.theta[xR]);
-    const double Omega_avg = 0.5*(S.Omega[xL] + S.Omega[xR]);
-    const double s = -theta_avg/(fabs(theta_avg) + Omega_avg + HMR_EPS);
-    const bool use_hll = s > 0.65;
-
-    double Fo[NEQ], umid;
-    riemann<DIM, MODEL, NSP, A>(P, VL, VR, use_hll, Fo, umid);
     const long nf = nface_of(g, A);
 #pragma unroll
     for (int e = 0; e < NEQ; e++) S.Fm[A][e * nf + t] = Fo[e];
@@ -213,6 +250,20 @@ __device__ __forceinline__ void face_item(const Params& P, const Geom& g, const 
             if (hh) atomicAdd(&cnt->hllc_hll, (unsigned long long)__popc(hh));
         }
     }
+    return false;
+}
+
+// Queue of faces the fast form hands to the exact form: entries are
+// (axis << 56) | item, item being the face's index in the face phase.
+struct Redo {
+    unsigned long long* list;
+    unsigned int* count;
+    unsigned long long cap;
+};
+
+__device__ __forceinline__ void redo_push(const Redo& R, int axis, long item) {
+    const unsigned long long idx = atomicAdd(R.count, 1u);
+    if (idx < R.cap) R.list[idx] = ((unsigned long long)axis << 56) | (unsigned long long)item;
 }
 
 // ---------------------------------------------------------------------------

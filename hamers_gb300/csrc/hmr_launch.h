@@ -45,6 +45,7 @@ struct LevelArgs {
     int* status;             // device error flag (barrier give-up)
     unsigned long long timeout_ns;   // bound of every barrier wait
     unsigned int barrier_extra;      // diagnostic: arrivals that never come (0 in normal use)
+    Redo redo;                       // faces handed from the fast to the exact form (count zeroed per launch)
 };
 
 }  // namespace hmr
@@ -63,7 +64,7 @@ int launch_rk_stage(const hmr::Variant& v, const hmr::Geom& g, int ncoef, const 
 #define HMR_DECLARE_FACE_LAUNCHERS(NS)                                                                       \
     namespace NS {                                                                                           \
     int launch_faces(const hmr::Variant& v, const hmr::Params& P, const hmr::Geom& g, const hmr::Scratch& S, \
-                     hmr::Counters* cnt, cudaStream_t st);                                                   \
+                     hmr::Counters* cnt, const hmr::Redo& R, cudaStream_t st);                               \
     int launch_update(const hmr::Variant& v, const hmr::Geom& g, const hmr::Scratch& S,                      \
                       const hmr::UpdateArgs& U, cudaStream_t st);                                            \
     int launch_level(const hmr::Variant& v, const hmr::Params& P, const hmr::LevelArgs& L, int blocks,       \

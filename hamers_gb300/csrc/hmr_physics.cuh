@@ -62,30 +62,6 @@ __device__ __forceinline__ double ipow_d(double b, int e) {
 }
 
 // ----------------------------------------------------------------------------
-// Mixture gamma from volume fractions.
-// ----------------------------------------------------------------------------
-template <int NSP>
-__device__ __forceinline__ double gamma_all(const Params& P, const double* Z) {
-    double xi = 0.0;
-#pragma unroll
-    for (int s = 0; s < NSP; s++) xi += Z[s]*P.inv_gm1[s];
-    return double(1)/xi + double(1);
-}
-
-template <int NSP>
-__device__ __forceinline__ double gamma_last(const Params& P, const double* Z /* NSP-1 */) {
-    double xi = 0.0;
-    double Zl = 1.0;
-#pragma unroll
-    for (int s = 0; s < NSP - 1; s++) {
-        xi += Z[s]*P.inv_gm1[s];
-        Zl -= Z[s];
-    }
-    xi += Zl/(P.gamma[NSP - 1] - double(1));
-    return double(1)/xi + double(1);
-}
-
-// ----------------------------------------------------------------------------
 // Cell derived data: primitive variables V, density, sound speed.
 // single: FlowModelSingleSpecies.cpp:2649-3180; five: FlowModelFiveEqnAllaire.cpp:3734-4877.
 // Always evaluated in the reference's operation order with explicitly
@@ -232,32 +208,62 @@ __device__ __forceinline__ void char_from_prim(const FaceProj<DIM, MODEL, NSP>& 
     }
 }
 
+// ----------------------------------------------------------------------------
+// From here on every routine has two forms selected by the template flag X:
+//   X = true : the reference's operation order with every product explicitly
+//              rounded (__dmul_rn / __dadd_rn / __dsub_rn, never contracted),
+//              bitwise equal to the reference in either translation unit;
+//   X = false: regrouped for fewer FP64 instructions (shared reciprocals,
+//              one normalisation per weight set, FMA contraction).
+// The fast kernels run X = false and recompute a face with X = true where the
+// reference's own result is ill-conditioned (see face_item).
+// ----------------------------------------------------------------------------
+template <bool X>
+__device__ __forceinline__ double ipow_(double b, int e) {
+    double r = b;
+    for (int i = 1; i < e; i++) r = X ? mul_(r, b) : r*b;
+    return r;
+}
+
+// Mixture gamma from N-1 volume fractions (side data of the Riemann drivers),
+// EquationOfStateMixingRulesIdealGas.cpp:7599-7800.
+template <bool X, int NSP>
+__device__ __forceinline__ double gamma_last(const Params& P, const double* Z) {
+    double xi = 0.0;
+    double Zl = 1.0;
+#pragma unroll
+    for (int s = 0; s < NSP - 1; s++) {
+        xi = X ? add_(xi, mul_(Z[s], P.inv_gm1[s])) : xi + Z[s]*P.inv_gm1[s];
+        Zl = X ? sub_(Zl, Z[s]) : Zl - Z[s];
+    }
+    xi = X ? add_(xi, Zl/sub_(P.gamma[NSP - 1], double(1))) : xi + Zl*P.inv_gm1[NSP - 1];
+    return X ? add_(double(1)/xi, double(1)) : double(1)/xi + double(1);
+}
+
 // single: FlowModelBasicUtilitiesSingleSpecies.cpp:7279-7330 (2D) and the 3D block;
 // five:   FlowModelBasicUtilitiesFiveEqnAllaire.cpp:9201-... (2D block).
-template <int DIM, int MODEL, int NSP, int A>
+template <bool X, int DIM, int MODEL, int NSP, int A>
 __device__ __forceinline__ void prim_from_char(const FaceProj<DIM, MODEL, NSP>& F, const double* W, double* V) {
     using M = Model<DIM, MODEL, NSP>;
     constexpr int L = M::NEQ - 1;
     if constexpr (MODEL == SINGLE_SPECIES) {
-#if HMR_FAST
-        V[0] = F.ic2*(W[0] + W[L]) + W[1];
-        V[1 + A] = F.irc*(W[L] - W[0]);
-#else
-        V[0] = F.ic2*W[0] + W[1] + F.ic2*W[L];
-        V[1 + A] = -F.irc*W[0] + F.irc*W[L];
-#endif
+        if constexpr (X) {
+            V[0] = add_(add_(mul_(F.ic2, W[0]), W[1]), mul_(F.ic2, W[L]));
+            V[1 + A] = add_(mul_(-F.irc, W[0]), mul_(F.irc, W[L]));
+            V[DIM + 1] = add_(W[0], W[L]);
+        } else {
+            V[0] = F.ic2*(W[0] + W[L]) + W[1];
+            V[1 + A] = F.irc*(W[L] - W[0]);
+            V[DIM + 1] = W[0] + W[L];
+        }
         int t = 2;
 #pragma unroll
         for (int k = 0; k < DIM; k++) if (k != A) V[1 + k] = W[t++];
-        V[DIM + 1] = W[0] + W[L];
     } else {
 #pragma unroll
         for (int s = 0; s < NSP; s++) {
-#if HMR_FAST
-            V[s] = F.hz[s]*(W[L] - W[0]) + W[s + 1];
-#else
-            V[s] = -F.hz[s]*W[0] + W[s + 1] + F.hz[s]*W[L];
-#endif
+            if constexpr (X) V[s] = add_(add_(mul_(-F.hz[s], W[0]), W[s + 1]), mul_(F.hz[s], W[L]));
+            else V[s] = F.hz[s]*(W[L] - W[0]) + W[s + 1];
         }
 #pragma unroll
         for (int s = 0; s < NSP - 1; s++) V[M::IZ + s] = W[NSP + DIM + s];
@@ -265,20 +271,14 @@ __device__ __forceinline__ void prim_from_char(const FaceProj<DIM, MODEL, NSP>& 
 #pragma unroll
         for (int k = 0; k < DIM; k++) {
             if (k == A) {
-#if HMR_FAST
-                V[NSP + k] = double(1)/double(2)*(W[0] + W[L]);
-#else
-                V[NSP + k] = double(1)/double(2)*W[0] + double(1)/double(2)*W[L];
-#endif
+                if constexpr (X) V[NSP + k] = add_(mul_(double(1)/double(2), W[0]), mul_(double(1)/double(2), W[L]));
+                else V[NSP + k] = double(1)/double(2)*(W[0] + W[L]);
             } else {
                 V[NSP + k] = W[t++];
             }
         }
-#if HMR_FAST
-        V[NSP + DIM] = F.p_hrc*(W[L] - W[0]);
-#else
-        V[NSP + DIM] = F.m_hrc*W[0] + F.p_hrc*W[L];
-#endif
+        if constexpr (X) V[NSP + DIM] = add_(mul_(F.m_hrc, W[0]), mul_(F.p_hrc, W[L]));
+        else V[NSP + DIM] = F.p_hrc*(W[L] - W[0]);
     }
 }
 
@@ -309,54 +309,66 @@ __device__ __forceinline__ void js_betas_x(double S0, double S1, double S2, doub
                                        mul_(mul_(4.0, S4), S4)));
 }
 
-// Weighted 5-point midpoint value: S0..S4 are the stencil values ordered from
-// the upwind side (U[0..4] for the minus side, U[5..1] for the plus side).
+// Weighted 5-point midpoint value from the stencil S0..S4 (upwind first).
+template <bool X>
 __device__ __forceinline__ double js_interp(double b0, double b1, double b2, int p,
                                             double S0, double S1, double S2, double S3, double S4) {
-#if HMR_FAST
-    // w_k = d_k/(b_k+eps)^p / sum_j d_j/(b_j+eps)^p, evaluated with one reciprocal.
-    const double e0 = ipow_d(b0 + HMR_EPS, p), e1 = ipow_d(b1 + HMR_EPS, p), e2 = ipow_d(b2 + HMR_EPS, p);
-    const double a0 = double(1)/double(16)*(e1*e2);
-    const double a1 = double(5)/double(8)*(e0*e2);
-    const double a2 = double(5)/double(16)*(e0*e1);
-    const double r = double(1)/(a0 + a1 + a2);
-    const double w0 = a0*r, w1 = a1*r, w2 = a2*r;
-#else
-    double w0 = double(1.0)/double(16)/ipow_d(b0 + HMR_EPS, p);
-    double w1 = double(5.0)/double(8)/ipow_d(b1 + HMR_EPS, p);
-    double w2 = double(5.0)/double(16)/ipow_d(b2 + HMR_EPS, p);
-    const double ws = w0 + w1 + w2;
-    w0 = w0/ws; w1 = w1/ws; w2 = w2/ws;
-#endif
-    return double(3)/double(8)*w0*S0 +
-        (-double(10)/double(8)*w0 - double(1)/double(8)*w1)*S1 +
-        (double(15)/double(8)*w0 + double(6)/double(8)*w1 + double(3)/double(8)*w2)*S2 +
-        (double(3)/double(8)*w1 + double(6)/double(8)*w2)*S3 -
-        double(1)/double(8)*w2*S4;
+    double w0, w1, w2;
+    if constexpr (X) {
+        // ConvectiveFluxReconstructorWCNS5-JS-HLLC-HLL.cpp:96-117
+        w0 = double(1.0)/double(16)/ipow_<true>(add_(b0, HMR_EPS), p);
+        w1 = double(5.0)/double(8)/ipow_<true>(add_(b1, HMR_EPS), p);
+        w2 = double(5.0)/double(16)/ipow_<true>(add_(b2, HMR_EPS), p);
+        const double ws = add_(add_(w0, w1), w2);
+        w0 = w0/ws; w1 = w1/ws; w2 = w2/ws;
+        const double t0 = mul_(mul_(double(3)/double(8), w0), S0);
+        const double t1 = mul_(sub_(mul_(-double(10)/double(8), w0), mul_(double(1)/double(8), w1)), S1);
+        const double t2 = mul_(add_(add_(mul_(double(15)/double(8), w0), mul_(double(6)/double(8), w1)),
+                                    mul_(double(3)/double(8), w2)), S2);
+        const double t3 = mul_(add_(mul_(double(3)/double(8), w1), mul_(double(6)/double(8), w2)), S3);
+        const double t4 = mul_(mul_(double(1)/double(8), w2), S4);
+        return sub_(add_(add_(add_(t0, t1), t2), t3), t4);
+    } else {
+        // w_k = d_k/(b_k+eps)^p / sum_j d_j/(b_j+eps)^p with a single reciprocal:
+        // w_k = d_k prod_{j!=k} e_j / sum_m d_m prod_{j!=m} e_j.
+        const double e0 = ipow_<false>(b0 + HMR_EPS, p), e1 = ipow_<false>(b1 + HMR_EPS, p),
+                     e2 = ipow_<false>(b2 + HMR_EPS, p);
+        const double a0 = double(1)/double(16)*(e1*e2);
+        const double a1 = double(5)/double(8)*(e0*e2);
+        const double a2 = double(5)/double(16)*(e0*e1);
+        const double r = double(1)/(a0 + a1 + a2);
+        w0 = a0*r; w1 = a1*r; w2 = a2*r;
+        return double(3)/double(8)*w0*S0 +
+            (-double(10)/double(8)*w0 - double(1)/double(8)*w1)*S1 +
+            (double(15)/double(8)*w0 + double(6)/double(8)*w1 + double(3)/double(8)*w2)*S2 +
+            (double(3)/double(8)*w1 + double(6)/double(8)*w2)*S3 -
+            double(1)/double(8)*w2*S4;
+    }
 }
 
+template <bool X>
 __device__ __forceinline__ void js_pair(const double* U, int p, double& Um, double& Up) {
     double b0, b1, b2;
     js_betas_x(U[0], U[1], U[2], U[3], U[4], b0, b1, b2);
-    Um = js_interp(b0, b1, b2, p, U[0], U[1], U[2], U[3], U[4]);
+    Um = js_interp<X>(b0, b1, b2, p, U[0], U[1], U[2], U[3], U[4]);
     js_betas_x(U[5], U[4], U[3], U[2], U[1], b0, b1, b2);
-    Up = js_interp(b0, b1, b2, p, U[5], U[4], U[3], U[2], U[1]);
+    Up = js_interp<X>(b0, b1, b2, p, U[5], U[4], U[3], U[2], U[1]);
 }
 
 // ----------------------------------------------------------------------------
 // WCNS6-LD.
 // ----------------------------------------------------------------------------
-__device__ __forceinline__ double ld_sigma(const double* U) {
-    const double a1 = U[2] - U[1];
-    const double a2 = U[3] - U[2];
-    const double a3 = U[4] - U[3];
-    const double t1 = fabs(a1 - a2)/(fabs(a1) + fabs(a2) + HMR_EPS);
-    const double t2 = fabs(a2 - a3)/(fabs(a2) + fabs(a3) + HMR_EPS);
+__device__ __forceinline__ double ld_sigma(const double* U) {  // WCNS6-LD-HLLC-HLL.cpp:24-41
+    const double a1 = sub_(U[2], U[1]);
+    const double a2 = sub_(U[3], U[2]);
+    const double a3 = sub_(U[4], U[3]);
+    const double t1 = fabs(sub_(a1, a2))/add_(add_(fabs(a1), fabs(a2)), HMR_EPS);
+    const double t2 = fabs(sub_(a2, a3))/add_(add_(fabs(a2), fabs(a3)), HMR_EPS);
     return fmax(t1, t2);
 }
 
 // beta_3 with the stencil ordered from the upwind side (S0..S5), every
-// product explicitly rounded (see js_betas_x).
+// product explicitly rounded (see js_betas_x).  WCNS6-LD-HLLC-HLL.cpp:70-83.
 __device__ __forceinline__ double ld_beta3(double S0, double S1, double S2, double S3, double S4, double S5) {
     // S0*(525910327*S0 - 4562164630*S1 + 7799501420*S2 - 6610694540*S3 + 2794296070*S4 - 472758974*S5)
     const double t0 = mul_(S0, sub_(add_(sub_(add_(sub_(mul_(525910327.0, S0), mul_(4562164630.0, S1)),
@@ -379,75 +391,103 @@ __device__ __forceinline__ double ld_beta3(double S0, double S1, double S2, doub
     return mul_(double(1)/double(232243200), add_(add_(add_(add_(add_(t0, t1), t2), t3), t4), t5));
 }
 
+// WCNS6-LD weights and midpoint value (WCNS6-LD-HLLC-HLL.cpp:158-222), stencil S0..S5 from
+// the upwind side; b[0..3] are that side's smoothness indicators.
+template <bool X>
 __device__ __forceinline__ double ld_interp(const double* b, double sigma, const Params& P,
                                             double S0, double S1, double S2, double S3, double S4, double S5) {
-    const double tau_5 = fabs(b[0] - b[2]);
+    // Decision inputs are always exact: tau_5, tau_6, beta_avg, R_tau.
+    const double tau_5 = fabs(sub_(b[0], b[2]));
     const double beta_avg = mul_(double(1)/double(8), add_(add_(b[0], b[2]), mul_(double(6), b[1])));
-    const double tau_6 = fabs(b[3] - beta_avg);
-    const double R_tau = tau_6/(beta_avg + HMR_EPS);
+    const double tau_6 = fabs(sub_(b[3], beta_avg));
+    const double R_tau = tau_6/add_(beta_avg, HMR_EPS);
     const bool blend = R_tau > P.alpha_tau;
-    double o0, o1, o2, o3;
-#if HMR_FAST
-    const double r0 = double(1)/(b[0] + HMR_EPS);
-    const double r1 = double(1)/(b[1] + HMR_EPS);
-    const double r2 = double(1)/(b[2] + HMR_EPS);
-    const double r3 = double(1)/(b[3] + HMR_EPS);
-    double u0 = double(1)/double(16)*(double(1) + ipow_d(tau_5*r0, P.p));
-    double u1 = double(5)/double(8)*(double(1) + ipow_d(tau_5*r1, P.p));
-    double u2 = double(5)/double(16)*(double(1) + ipow_d(tau_5*r2, P.p));
-    const double ru = double(1)/(u0 + u1 + u2);
-    u0 *= ru; u1 *= ru; u2 *= ru;
-    o0 = double(1)/double(32)*(P.C + ipow_d(tau_6*r0, P.q));
-    o1 = double(15)/double(32)*(P.C + ipow_d(tau_6*r1, P.q));
-    o2 = double(15)/double(32)*(P.C + ipow_d(tau_6*r2, P.q));
-    o3 = double(1)/double(32)*(P.C + ipow_d(tau_6*r3, P.q));
-    const double ro = double(1)/(o0 + o1 + o2 + o3);
-    o0 *= ro; o1 *= ro; o2 *= ro; o3 *= ro;
-#else
-    double u0 = double(1)/double(16)*(double(1) + ipow_d(tau_5/(b[0] + HMR_EPS), P.p));
-    double u1 = double(5)/double(8)*(double(1) + ipow_d(tau_5/(b[1] + HMR_EPS), P.p));
-    double u2 = double(5)/double(16)*(double(1) + ipow_d(tau_5/(b[2] + HMR_EPS), P.p));
-    const double us = u0 + u1 + u2;
-    u0 = u0/us; u1 = u1/us; u2 = u2/us;
-    o0 = double(1)/double(32)*(P.C + ipow_d(tau_6/(b[0] + HMR_EPS), P.q));
-    o1 = double(15)/double(32)*(P.C + ipow_d(tau_6/(b[1] + HMR_EPS), P.q));
-    o2 = double(15)/double(32)*(P.C + ipow_d(tau_6/(b[2] + HMR_EPS), P.q));
-    o3 = double(1)/double(32)*(P.C + ipow_d(tau_6/(b[3] + HMR_EPS), P.q));
-    const double os = o0 + o1 + o2 + o3;
-    o0 = o0/os; o1 = o1/os; o2 = o2/os; o3 = o3/os;
-#endif
-    if (blend) {
-        o0 = sigma*u0 + (double(1) - sigma)*o0;
-        o1 = sigma*u1 + (double(1) - sigma)*o1;
-        o2 = sigma*u2 + (double(1) - sigma)*o2;
-        o3 = (double(1) - sigma)*o3;
+    double u0, u1, u2, o0, o1, o2, o3;
+    if constexpr (X) {
+        u0 = mul_(double(1)/double(16), add_(double(1), ipow_<true>(tau_5/add_(b[0], HMR_EPS), P.p)));
+        u1 = mul_(double(5)/double(8), add_(double(1), ipow_<true>(tau_5/add_(b[1], HMR_EPS), P.p)));
+        u2 = mul_(double(5)/double(16), add_(double(1), ipow_<true>(tau_5/add_(b[2], HMR_EPS), P.p)));
+        const double us = add_(add_(u0, u1), u2);
+        u0 = u0/us; u1 = u1/us; u2 = u2/us;
+        o0 = mul_(double(1)/double(32), add_(P.C, ipow_<true>(tau_6/add_(b[0], HMR_EPS), P.q)));
+        o1 = mul_(double(15)/double(32), add_(P.C, ipow_<true>(tau_6/add_(b[1], HMR_EPS), P.q)));
+        o2 = mul_(double(15)/double(32), add_(P.C, ipow_<true>(tau_6/add_(b[2], HMR_EPS), P.q)));
+        o3 = mul_(double(1)/double(32), add_(P.C, ipow_<true>(tau_6/add_(b[3], HMR_EPS), P.q)));
+        const double os = add_(add_(add_(o0, o1), o2), o3);
+        o0 = o0/os; o1 = o1/os; o2 = o2/os; o3 = o3/os;
+        if (blend) {
+            const double ms = sub_(double(1), sigma);
+            o0 = add_(mul_(sigma, u0), mul_(ms, o0));
+            o1 = add_(mul_(sigma, u1), mul_(ms, o1));
+            o2 = add_(mul_(sigma, u2), mul_(ms, o2));
+            o3 = mul_(ms, o3);
+        }
+        const double t0 = mul_(mul_(double(3)/double(8), o0), S0);
+        const double t1 = mul_(sub_(mul_(-double(10)/double(8), o0), mul_(double(1)/double(8), o1)), S1);
+        const double t2 = mul_(add_(add_(mul_(double(15)/double(8), o0), mul_(double(6)/double(8), o1)),
+                                    mul_(double(3)/double(8), o2)), S2);
+        const double t3 = mul_(add_(add_(mul_(double(3)/double(8), o1), mul_(double(6)/double(8), o2)),
+                                    mul_(double(15)/double(8), o3)), S3);
+        const double t4 = mul_(sub_(mul_(-double(1)/double(8), o2), mul_(double(10)/double(8), o3)), S4);
+        const double t5 = mul_(mul_(double(3)/double(8), o3), S5);
+        return add_(add_(add_(add_(add_(t0, t1), t2), t3), t4), t5);
+    } else {
+        const double r0 = double(1)/(b[0] + HMR_EPS);
+        const double r1 = double(1)/(b[1] + HMR_EPS);
+        const double r2 = double(1)/(b[2] + HMR_EPS);
+        const double r3 = double(1)/(b[3] + HMR_EPS);
+        u0 = double(1)/double(16)*(double(1) + ipow_<false>(tau_5*r0, P.p));
+        u1 = double(5)/double(8)*(double(1) + ipow_<false>(tau_5*r1, P.p));
+        u2 = double(5)/double(16)*(double(1) + ipow_<false>(tau_5*r2, P.p));
+        const double ru = double(1)/(u0 + u1 + u2);
+        u0 *= ru; u1 *= ru; u2 *= ru;
+        o0 = double(1)/double(32)*(P.C + ipow_<false>(tau_6*r0, P.q));
+        o1 = double(15)/double(32)*(P.C + ipow_<false>(tau_6*r1, P.q));
+        o2 = double(15)/double(32)*(P.C + ipow_<false>(tau_6*r2, P.q));
+        o3 = double(1)/double(32)*(P.C + ipow_<false>(tau_6*r3, P.q));
+        const double ro = double(1)/(o0 + o1 + o2 + o3);
+        o0 *= ro; o1 *= ro; o2 *= ro; o3 *= ro;
+        if (blend) {
+            o0 = sigma*u0 + (double(1) - sigma)*o0;
+            o1 = sigma*u1 + (double(1) - sigma)*o1;
+            o2 = sigma*u2 + (double(1) - sigma)*o2;
+            o3 = (double(1) - sigma)*o3;
+        }
+        return double(3)/double(8)*o0*S0 +
+            (-double(10)/double(8)*o0 - double(1)/double(8)*o1)*S1 +
+            (double(15)/double(8)*o0 + double(6)/double(8)*o1 + double(3)/double(8)*o2)*S2 +
+            (double(3)/double(8)*o1 + double(6)/double(8)*o2 + double(15)/double(8)*o3)*S3 +
+            (-double(1)/double(8)*o2 - double(10)/double(8)*o3)*S4 +
+            double(3)/double(8)*o3*S5;
     }
-    return double(3)/double(8)*o0*S0 +
-        (-double(10)/double(8)*o0 - double(1)/double(8)*o1)*S1 +
-        (double(15)/double(8)*o0 + double(6)/double(8)*o1 + double(3)/double(8)*o2)*S2 +
-        (double(3)/double(8)*o1 + double(6)/double(8)*o2 + double(15)/double(8)*o3)*S3 +
-        (-double(1)/double(8)*o2 - double(10)/double(8)*o3)*S4 +
-        double(3)/double(8)*o3*S5;
 }
 
+template <bool X>
 __device__ __forceinline__ void ld_pair(const double* U, const Params& P, double& Um, double& Up) {
     const double sigma = ld_sigma(U);
     double b[4];
     js_betas_x(U[0], U[1], U[2], U[3], U[4], b[0], b[1], b[2]);
     b[3] = ld_beta3(U[0], U[1], U[2], U[3], U[4], U[5]);
-    Um = ld_interp(b, sigma, P, U[0], U[1], U[2], U[3], U[4], U[5]);
+    Um = ld_interp<X>(b, sigma, P, U[0], U[1], U[2], U[3], U[4], U[5]);
     js_betas_x(U[5], U[4], U[3], U[2], U[1], b[0], b[1], b[2]);
     b[3] = ld_beta3(U[5], U[4], U[3], U[2], U[1], U[0]);
-    Up = ld_interp(b, sigma, P, U[5], U[4], U[3], U[2], U[1], U[0]);
+    Up = ld_interp<X>(b, sigma, P, U[5], U[4], U[3], U[2], U[1], U[0]);
 }
 
 // ----------------------------------------------------------------------------
-// Bounds check of a reconstructed face state.
+// Bounds check of a reconstructed face state.  Always exact (a discrete
+// decision).  `margin` receives how far the state is from the nearest bound,
+// relative to its scale, so that the fast kernels can recompute faces whose
+// decision could depend on rounding.
+// single: FlowModelBasicUtilitiesSingleSpecies.cpp:3013-3440;
+// five:   FlowModelBasicUtilitiesFiveEqnAllaire.cpp:5446-7347, bounds
+//         FlowModelBasicUtilitiesFiveEqnAllaire.hpp:24-27.
 // ----------------------------------------------------------------------------
 template <int DIM, int MODEL, int NSP>
-__device__ __forceinline__ bool face_bounded(const Params& P, const double* V) {
+__device__ __forceinline__ bool face_bounded(const Params& P, const double* V, double& margin) {
     using M = Model<DIM, MODEL, NSP>;
     if constexpr (MODEL == SINGLE_SPECIES) {
+        margin = fmin(fabs(V[0]), fabs(V[DIM + 1]));
         return (V[0] > 0.0) && (V[DIM + 1] > 0.0);
     } else {
         bool ok = true;
@@ -456,43 +496,45 @@ __device__ __forceinline__ bool face_bounded(const Params& P, const double* V) {
 #pragma unroll
         for (int s = 0; s < NSP - 1; s++) {
             Z[s] = V[M::IZ + s];
-            Z[NSP - 1] -= Z[s];
+            Z[NSP - 1] = sub_(Z[NSP - 1], Z[s]);
             ok = ok && (Z[s] > -1000.0 && Z[s] < 1000.0);
         }
         ok = ok && (Z[NSP - 1] > -1000.0 && Z[NSP - 1] < 1000.0);
         double rho = 0.0;
 #pragma unroll
-        for (int s = 0; s < NSP; s++) rho += V[s];
+        for (int s = 0; s < NSP; s++) rho = add_(rho, V[s]);
         double Y[NSP];
+        double m = 1.0e300;
 #pragma unroll
         for (int s = 0; s < NSP; s++) {
             Y[s] = V[s]/rho;
             ok = ok && (Y[s] > -0.001 && Y[s] < 1.001);
+            m = fmin(m, fmin(fabs(Y[s] + 0.001), fabs(1.001 - Y[s])));
         }
 #pragma unroll
-        for (int s = 0; s < NSP; s++) ok = ok && (V[s] > 0.0);
+        for (int s = 0; s < NSP; s++) {
+            ok = ok && (V[s] > 0.0);
+            m = fmin(m, fabs(Y[s]));
+        }
         const double p = V[NSP + DIM];
-        const double gamma = gamma_all<NSP>(P, Z);
-#if HMR_FAST
-        double c2 = (gamma - double(1))*p;
-#pragma unroll
-        for (int s = 0; s < NSP; s++) c2 += Y[s]*p;
-#else
-        const double Gamma = gamma - double(1);
+        const double gamma = gamma_all_x<NSP>(P, Z);
+        const double Gamma = sub_(gamma, double(1));
         const double Psi = p/rho;
-        double c2 = Gamma*p/rho;
+        double c2 = mul_(Gamma, p)/rho;
 #pragma unroll
-        for (int s = 0; s < NSP; s++) c2 += Y[s]*Psi;
-#endif
+        for (int s = 0; s < NSP; s++) c2 = add_(c2, mul_(Y[s], Psi));
         ok = ok && (c2 > 0.0);
+        margin = fmin(m, fabs(c2)/fmax(fabs(mul_(Gamma, p)/rho), 1e-300));
         return ok;
     }
 }
 
 // ----------------------------------------------------------------------------
 // Face thermodynamics of one reconstructed state (Riemann drivers).
+// single: EquationOfStateIdealGas.cpp:5806 (c), :6135 (eps)
+// five:   FlowModelRiemannSolverFiveEqnAllaireHLLC.cpp:4824-6097 (rho, Y, Gamma, c, eps)
 // ----------------------------------------------------------------------------
-template <int DIM, int MODEL, int NSP>
+template <bool X, int DIM, int MODEL, int NSP>
 __device__ __forceinline__ void face_thermo(const Params& P, const double* V, double& rho, double& cs,
                                             double& eps) {
     using M = Model<DIM, MODEL, NSP>;
@@ -500,87 +542,90 @@ __device__ __forceinline__ void face_thermo(const Params& P, const double* V, do
         const double gamma = P.gamma[0];
         rho = V[0];
         const double p = V[DIM + 1];
-#if HMR_FAST
-        const double ri = double(1)/rho;
-        cs = sqrt(gamma*p*ri);
-        eps = p*ri*P.inv_gm1[0];
-#else
-        cs = sqrt(gamma*p/rho);
-        eps = p/((gamma - double(1))*rho);
-#endif
+        if constexpr (X) {
+            cs = sqrt(mul_(gamma, p)/rho);
+            eps = p/mul_(sub_(gamma, double(1)), rho);
+        } else {
+            const double ri = double(1)/rho;
+            cs = sqrt(gamma*p*ri);
+            eps = p*ri*P.inv_gm1[0];
+        }
     } else {
         double r = 0.0;
 #pragma unroll
-        for (int s = 0; s < NSP; s++) r += V[s];
+        for (int s = 0; s < NSP; s++) r = X ? add_(r, V[s]) : r + V[s];
         rho = r;
         const double p = V[NSP + DIM];
-        const double gamma = gamma_last<NSP>(P, V + M::IZ);
-#if HMR_FAST
-        const double ri = double(1)/r;
-        const double Psi = p*ri;
-        double c2 = (gamma - double(1))*Psi;
+        const double gamma = gamma_last<X, NSP>(P, V + M::IZ);
+        if constexpr (X) {
+            double Y[NSP];
 #pragma unroll
-        for (int s = 0; s < NSP; s++) c2 += (V[s]*ri)*Psi;
-        cs = sqrt(c2);
-        eps = Psi/(gamma - double(1));
-#else
-        double Y[NSP];
+            for (int s = 0; s < NSP; s++) Y[s] = V[s]/r;
+            const double Gamma = sub_(gamma, double(1));
+            const double Psi = p/r;
+            double c2 = mul_(Gamma, p)/r;
 #pragma unroll
-        for (int s = 0; s < NSP; s++) Y[s] = V[s]/r;
-        const double Gamma = gamma - double(1);
-        const double Psi = p/r;
-        double c2 = Gamma*p/r;
+            for (int s = 0; s < NSP; s++) c2 = add_(c2, mul_(Y[s], Psi));
+            cs = sqrt(c2);
+            eps = p/mul_(sub_(gamma, double(1)), r);
+        } else {
+            const double ri = double(1)/r;
+            const double Psi = p*ri;
+            double c2 = (gamma - double(1))*Psi;
 #pragma unroll
-        for (int s = 0; s < NSP; s++) c2 += Y[s]*Psi;
-        cs = sqrt(c2);
-        eps = p/((gamma - double(1))*r);
-#endif
+            for (int s = 0; s < NSP; s++) c2 += (V[s]*ri)*Psi;
+            cs = sqrt(c2);
+            eps = Psi/(gamma - double(1));
+        }
     }
 }
 
 // Conserved state and physical flux of one face state.
-template <int DIM, int MODEL, int NSP, int A>
+template <bool X, int DIM, int MODEL, int NSP, int A>
 __device__ __forceinline__ void face_QF(const double* V, double rho, double eps, double* Q, double* F) {
     using M = Model<DIM, MODEL, NSP>;
     if constexpr (MODEL == SINGLE_SPECIES) {
         const double p = V[DIM + 1];
         Q[0] = V[0];
 #pragma unroll
-        for (int k = 0; k < DIM; k++) Q[1 + k] = V[0]*V[1 + k];
-        double ke = V[1]*V[1];
+        for (int k = 0; k < DIM; k++) Q[1 + k] = X ? mul_(V[0], V[1 + k]) : V[0]*V[1 + k];
+        double ke = X ? mul_(V[1], V[1]) : V[1]*V[1];
 #pragma unroll
-        for (int k = 1; k < DIM; k++) ke = ke + V[1 + k]*V[1 + k];
-        Q[DIM + 1] = V[0]*(eps + double(1)/double(2)*ke);
+        for (int k = 1; k < DIM; k++) ke = X ? add_(ke, mul_(V[1 + k], V[1 + k])) : ke + V[1 + k]*V[1 + k];
+        Q[DIM + 1] = X ? mul_(V[0], add_(eps, mul_(double(1)/double(2), ke)))
+                       : V[0]*(eps + double(1)/double(2)*ke);
         F[0] = Q[1 + A];
 #pragma unroll
         for (int k = 0; k < DIM; k++) {
-            if (k == A) F[1 + k] = Q[1 + A]*V[1 + k] + p;
-            else F[1 + k] = Q[1 + A]*V[1 + k];
+            if (k == A) F[1 + k] = X ? add_(mul_(Q[1 + A], V[1 + k]), p) : Q[1 + A]*V[1 + k] + p;
+            else F[1 + k] = X ? mul_(Q[1 + A], V[1 + k]) : Q[1 + A]*V[1 + k];
         }
-        F[DIM + 1] = V[1 + A]*(Q[DIM + 1] + p);
+        F[DIM + 1] = X ? mul_(V[1 + A], add_(Q[DIM + 1], p)) : V[1 + A]*(Q[DIM + 1] + p);
     } else {
         const double p = V[NSP + DIM];
         const double un = V[NSP + A];
 #pragma unroll
         for (int s = 0; s < NSP; s++) Q[s] = V[s];
 #pragma unroll
-        for (int k = 0; k < DIM; k++) Q[NSP + k] = rho*V[NSP + k];
-        double ke = V[NSP]*V[NSP];
+        for (int k = 0; k < DIM; k++) Q[NSP + k] = X ? mul_(rho, V[NSP + k]) : rho*V[NSP + k];
+        double ke = X ? mul_(V[NSP], V[NSP]) : V[NSP]*V[NSP];
 #pragma unroll
-        for (int k = 1; k < DIM; k++) ke = ke + V[NSP + k]*V[NSP + k];
-        Q[NSP + DIM] = rho*(eps + double(1)/double(2)*ke);
+        for (int k = 1; k < DIM; k++)
+            ke = X ? add_(ke, mul_(V[NSP + k], V[NSP + k])) : ke + V[NSP + k]*V[NSP + k];
+        Q[NSP + DIM] = X ? mul_(rho, add_(eps, mul_(double(1)/double(2), ke)))
+                         : rho*(eps + double(1)/double(2)*ke);
 #pragma unroll
         for (int s = 0; s < NSP - 1; s++) Q[M::IZ + s] = V[M::IZ + s];
 #pragma unroll
-        for (int s = 0; s < NSP; s++) F[s] = un*V[s];
+        for (int s = 0; s < NSP; s++) F[s] = X ? mul_(un, V[s]) : un*V[s];
 #pragma unroll
         for (int k = 0; k < DIM; k++) {
-            if (k == A) F[NSP + k] = un*Q[NSP + k] + p;
-            else F[NSP + k] = un*Q[NSP + k];
+            if (k == A) F[NSP + k] = X ? add_(mul_(un, Q[NSP + k]), p) : un*Q[NSP + k] + p;
+            else F[NSP + k] = X ? mul_(un, Q[NSP + k]) : un*Q[NSP + k];
         }
-        F[NSP + DIM] = un*(Q[NSP + DIM] + p);
+        F[NSP + DIM] = X ? mul_(un, add_(Q[NSP + DIM], p)) : un*(Q[NSP + DIM] + p);
 #pragma unroll
-        for (int s = 0; s < NSP - 1; s++) F[M::IZ + s] = un*V[M::IZ + s];
+        for (int s = 0; s < NSP - 1; s++) F[M::IZ + s] = X ? mul_(un, V[M::IZ + s]) : un*V[M::IZ + s];
     }
 }
 
@@ -594,9 +639,11 @@ __device__ __forceinline__ constexpr bool hll_comp(int e) {
 }
 
 // Midpoint flux of one face: HLLC, or HLLC-HLL when use_hll is set (the
-// shock sensor's choice, WCNS56-HLLC-HLL.cpp:1090-1113).  Also returns the
-// HLLC midpoint normal velocity.
-template <int DIM, int MODEL, int NSP, int A>
+// shock sensor's choice, WCNS56-HLLC-HLL.cpp:1090-1113), and the HLLC
+// midpoint normal velocity.
+//  HLLC:     FlowModelRiemannSolverSingleSpeciesHLLC.cpp:604-692 (five: ...FiveEqnAllaireHLLC.cpp:848-990)
+//  HLLC-HLL: FlowModelRiemannSolverSingleSpeciesHLLC-HLL.cpp:889-1027 (five: ...FiveEqnAllaireHLLC-HLL.cpp:1283-1503)
+template <bool X, int DIM, int MODEL, int NSP, int A>
 __device__ __forceinline__ void riemann(const Params& P, const double* VL, const double* VR, bool use_hll,
                                         double* Fout, double& u_mid) {
     using M = Model<DIM, MODEL, NSP>;
@@ -604,18 +651,29 @@ __device__ __forceinline__ void riemann(const Params& P, const double* VL, const
     constexpr int IU = M::IU;
     constexpr int IP = M::IP;
     double rhoL, cL, epsL, rhoR, cR, epsR;
-    face_thermo<DIM, MODEL, NSP>(P, VL, rhoL, cL, epsL);
-    face_thermo<DIM, MODEL, NSP>(P, VR, rhoR, cR, epsR);
+    face_thermo<X, DIM, MODEL, NSP>(P, VL, rhoL, cL, epsL);
+    face_thermo<X, DIM, MODEL, NSP>(P, VR, rhoR, cR, epsR);
     const double uL = VL[IU + A], uR = VR[IU + A];
     const double pL = VL[IP], pR = VR[IP];
-    const double u_average = double(1)/double(2)*(uL + uR);
-    const double c_average = double(1)/double(2)*(cL + cR);
-    const double s_L = fmin(u_average - c_average, uL - cL);
-    const double s_R = fmax(u_average + c_average, uR + cR);
+    double s_L, s_R, s_star;
+    if constexpr (X) {
+        const double u_average = mul_(double(1)/double(2), add_(uL, uR));
+        const double c_average = mul_(double(1)/double(2), add_(cL, cR));
+        s_L = fmin(sub_(u_average, c_average), sub_(uL, cL));
+        s_R = fmax(add_(u_average, c_average), add_(uR, cR));
+        const double num = sub_(add_(sub_(pR, pL), mul_(mul_(rhoL, uL), sub_(s_L, uL))),
+                                mul_(mul_(rhoR, uR), sub_(s_R, uR)));
+        const double den = sub_(mul_(rhoL, sub_(s_L, uL)), mul_(rhoR, sub_(s_R, uR)));
+        s_star = num/den;
+    } else {
+        const double u_average = double(1)/double(2)*(uL + uR);
+        const double c_average = double(1)/double(2)*(cL + cR);
+        s_L = fmin(u_average - c_average, uL - cL);
+        s_R = fmax(u_average + c_average, uR + cR);
+        s_star = (pR - pL + rhoL*uL*(s_L - uL) - rhoR*uR*(s_R - uR))/(rhoL*(s_L - uL) - rhoR*(s_R - uR));
+    }
     const double s_minus = fmin(0.0, s_L);
     const double s_plus = fmax(0.0, s_R);
-    const double s_star = (pR - pL + rhoL*uL*(s_L - uL) - rhoR*uR*(s_R - uR))/
-        (rhoL*(s_L - uL) - rhoR*(s_R - uR));
 
     const bool left = s_star > 0.0;
     const double* VK = left ? VL : VR;
@@ -626,44 +684,49 @@ __device__ __forceinline__ void riemann(const Params& P, const double* VL, const
     const double pK = left ? pL : pR;
     const double s_pm = left ? s_minus : s_plus;
     double QK[NEQ], FK[NEQ], Qs[NEQ];
-    face_QF<DIM, MODEL, NSP, A>(VK, rhoK, epsK, QK, FK);
-    const double Chi = (sK - uK)/(sK - s_star);
+    face_QF<X, DIM, MODEL, NSP, A>(VK, rhoK, epsK, QK, FK);
+    const double Chi = X ? sub_(sK, uK)/sub_(sK, s_star) : (sK - uK)/(sK - s_star);
+    // Energy of the star state: Chi*(E_K + (s* - u_K)*(rho_K s* + p_K/(s_K - u_K)))
+    const double rK = (MODEL == SINGLE_SPECIES) ? VK[0] : rhoK;
+    double QsE;
+    if constexpr (X) QsE = mul_(Chi, add_(QK[M::IE], mul_(sub_(s_star, uK), add_(mul_(rK, s_star), pK/sub_(sK, uK)))));
+    else QsE = Chi*(QK[M::IE] + (s_star - uK)*(rK*s_star + pK/(sK - uK)));
     if constexpr (MODEL == SINGLE_SPECIES) {
-        Qs[0] = Chi*VK[0];
+        Qs[0] = X ? mul_(Chi, VK[0]) : Chi*VK[0];
 #pragma unroll
         for (int k = 0; k < DIM; k++) {
-            if (k == A) Qs[1 + k] = Chi*VK[0]*s_star;
-            else Qs[1 + k] = Chi*QK[1 + k];
+            if (k == A) Qs[1 + k] = X ? mul_(mul_(Chi, VK[0]), s_star) : Chi*VK[0]*s_star;
+            else Qs[1 + k] = X ? mul_(Chi, QK[1 + k]) : Chi*QK[1 + k];
         }
-        Qs[DIM + 1] = Chi*(QK[DIM + 1] + (s_star - uK)*(VK[0]*s_star + pK/(sK - uK)));
+        Qs[DIM + 1] = QsE;
     } else {
 #pragma unroll
-        for (int s = 0; s < NSP; s++) Qs[s] = Chi*VK[s];
+        for (int s = 0; s < NSP; s++) Qs[s] = X ? mul_(Chi, VK[s]) : Chi*VK[s];
 #pragma unroll
         for (int k = 0; k < DIM; k++) {
-            if (k == A) Qs[NSP + k] = Chi*rhoK*s_star;
-            else Qs[NSP + k] = Chi*QK[NSP + k];
+            if (k == A) Qs[NSP + k] = X ? mul_(mul_(Chi, rhoK), s_star) : Chi*rhoK*s_star;
+            else Qs[NSP + k] = X ? mul_(Chi, QK[NSP + k]) : Chi*QK[NSP + k];
         }
-        Qs[NSP + DIM] = Chi*(QK[NSP + DIM] + (s_star - uK)*(rhoK*s_star + pK/(sK - uK)));
+        Qs[NSP + DIM] = QsE;
 #pragma unroll
-        for (int s = 0; s < NSP - 1; s++) Qs[M::IZ + s] = Chi*VK[M::IZ + s];
+        for (int s = 0; s < NSP - 1; s++) Qs[M::IZ + s] = X ? mul_(Chi, VK[M::IZ + s]) : Chi*VK[M::IZ + s];
     }
 #pragma unroll
-    for (int e = 0; e < NEQ; e++) Fout[e] = FK[e] + s_pm*(Qs[e] - QK[e]);
-    u_mid = uK + s_pm*(Chi - double(1));
+    for (int e = 0; e < NEQ; e++) Fout[e] = X ? add_(FK[e], mul_(s_pm, sub_(Qs[e], QK[e]))) : FK[e] + s_pm*(Qs[e] - QK[e]);
+    u_mid = X ? add_(uK, mul_(s_pm, sub_(Chi, double(1)))) : uK + s_pm*(Chi - double(1));
 
     if (use_hll) {
         // HLL for mass/partial densities, transverse momenta and volume
-        // fractions, blended with HLLC by the velocity-jump direction.
+        // fractions, blended with HLLC by the direction of the velocity jump.
         double QL[NEQ], FL[NEQ], QR[NEQ], FR[NEQ];
-        face_QF<DIM, MODEL, NSP, A>(VL, rhoL, epsL, QL, FL);
-        face_QF<DIM, MODEL, NSP, A>(VR, rhoR, epsR, QR, FR);
+        face_QF<X, DIM, MODEL, NSP, A>(VL, rhoL, epsL, QL, FL);
+        face_QF<X, DIM, MODEL, NSP, A>(VR, rhoR, epsR, QR, FR);
         double diff[DIM];
 #pragma unroll
         for (int k = 0; k < DIM; k++) diff[k] = VR[IU + k] - VL[IU + k];
-        double vsq = diff[0]*diff[0];
+        double vsq = X ? mul_(diff[0], diff[0]) : diff[0]*diff[0];
 #pragma unroll
-        for (int k = 1; k < DIM; k++) vsq = vsq + diff[k]*diff[k];
+        for (int k = 1; k < DIM; k++) vsq = X ? add_(vsq, mul_(diff[k], diff[k])) : vsq + diff[k]*diff[k];
         const double vel_mag = sqrt(vsq);
         double alpha_1, alpha_2;
         if (vel_mag < HMR_EPS) {
@@ -671,9 +734,10 @@ __device__ __forceinline__ void riemann(const Params& P, const double* VL, const
             alpha_2 = 0.0;
         } else {
             alpha_1 = fabs(diff[A])/vel_mag;
-            alpha_2 = sqrt(double(1) - alpha_1*alpha_1);
+            alpha_2 = sqrt(X ? sub_(double(1), mul_(alpha_1, alpha_1)) : double(1) - alpha_1*alpha_1);
         }
-        const double beta_1 = double(1)/double(2)*(double(1) + alpha_1/(alpha_1 + alpha_2));
+        const double beta_1 = X ? mul_(double(1)/double(2), add_(double(1), alpha_1/add_(alpha_1, alpha_2)))
+                                : double(1)/double(2)*(double(1) + alpha_1/(alpha_1 + alpha_2));
         const double beta_2 = double(1) - beta_1;
 #pragma unroll
         for (int e = 0; e < NEQ; e++) {
@@ -681,8 +745,11 @@ __device__ __forceinline__ void riemann(const Params& P, const double* VL, const
                 double Fh;
                 if (s_L > 0.0) Fh = FL[e];
                 else if (s_R < 0.0) Fh = FR[e];
+                else if constexpr (X)
+                    Fh = add_(sub_(mul_(s_R, FL[e]), mul_(s_L, FR[e])), mul_(mul_(s_R, s_L), sub_(QR[e], QL[e])))/
+                         sub_(s_R, s_L);
                 else Fh = (s_R*FL[e] - s_L*FR[e] + s_R*s_L*(QR[e] - QL[e]))/(s_R - s_L);
-                Fout[e] = beta_1*Fout[e] + beta_2*Fh;
+                Fout[e] = X ? add_(mul_(beta_1, Fout[e]), mul_(beta_2, Fh)) : beta_1*Fout[e] + beta_2*Fh;
             }
         }
     }

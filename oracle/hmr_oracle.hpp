@@ -473,7 +473,7 @@ inline bool hll_component(const Config& c, int a, int e) {
 // single-species HLLC.cpp:3060-3070 pattern).
 template <class T>
 inline void riemann_face(const Config& c, int a, const T* VL, const T* VR,
-                         T* F_hllc, T* F_hllc_hll, T& u_mid) {
+                         T* F_hllc, T* F_hllc_hll, T& u_mid, bool need_hll = true) {
     const int dim = c.dim;
     const int neq = num_eqn(c);
     const int ip = (c.model == MODEL_SINGLE_SPECIES) ? dim + 1 : c.num_species + dim;
@@ -501,12 +501,12 @@ inline void riemann_face(const Config& c, int a, const T* VL, const T* VR,
 
     // HLL part (HLLC-HLL only): HLLC-HLL.cpp:949-970
     T F_hll[16];
-    for (int e = 0; e < neq; e++) {
+    for (int e = 0; e < neq && need_hll; e++) {
         if (!hll_component(c, a, e)) continue;
         F_hll[e] = (s_R*FL[e] - s_L*FR[e] + s_R*s_L*(QR[e] - QL[e]))/(s_R - s_L);
         if (s_val(s_L) > 0.0) F_hll[e] = FL[e];
     }
-    if (s_val(s_R) < 0.0) {
+    if (need_hll && s_val(s_R) < 0.0) {
         for (int e = 0; e < neq; e++) if (hll_component(c, a, e)) F_hll[e] = FR[e];
     }
 
@@ -541,6 +541,10 @@ inline void riemann_face(const Config& c, int a, const T* VL, const T* VR,
     for (int e = 0; e < neq; e++) F_hllc[e] = FK[e] + s_pm*(Qs[e] - QK[e]);
     u_mid = uK + s_pm*(Chi - double(1));
 
+    if (!need_hll) {
+        for (int e = 0; e < neq; e++) F_hllc_hll[e] = F_hllc[e];
+        return;
+    }
     // Hybridization weights: HLLC-HLL.cpp:998-1026
     T diff[3];
     for (int k = 0; k < dim; k++) diff[k] = VR[iu + k] - VL[iu + k];
@@ -738,6 +742,10 @@ void compute_derived(const Config& c, const Box& b, const T* const* Q, Derived<T
 // Velocity component index inside V.
 inline int vel_index(const Config& c) { return c.model == MODEL_SINGLE_SPECIES ? 1 : c.num_species; }
 
+// When set, the HLL part of HLLC-HLL is evaluated only on faces whose sensor
+// selects it (the results are unchanged; used by the operation counter).
+inline bool g_minimal_hll = false;
+
 // Per-face counters reported back to the caller.
 struct Stats {
     long faces;          // midpoint faces reconstructed
@@ -909,13 +917,16 @@ void conv_flux_source(const Config& c, const int* n, const double* dx, double dt
             const long f = fs.idx(i, j, k);
             T VL[16], VR[16], Fc[16], Fh[16], um;
             for (int e = 0; e < neq; e++) { VL[e] = Vm[(size_t)e * nf + f]; VR[e] = Vp[(size_t)e * nf + f]; }
-            riemann_face(c, a, VL, VR, Fc, Fh, um);
             const long xL = b.cell(i - off[0], j - off[1], k - off[2]);
             const long xR = b.cell(i, j, k);
             const T theta_avg = 0.5*(theta[xL] + theta[xR]);
             const T Omega_avg = 0.5*(Omega[xL] + Omega[xR]);
             const T s = -theta_avg/(s_fabs(theta_avg) + Omega_avg + EPS);
             const bool use_hll = s_val(s) > 0.65;
+            // The reference evaluates both midpoint fluxes on every face
+            // (WCNS56-HLLC-HLL.cpp:1038-1064); the HLL part only matters where
+            // the sensor selects it, which is all the op counter charges.
+            riemann_face(c, a, VL, VR, Fc, Fh, um, !g_minimal_hll || use_hll);
             if (use_hll) cnt_hll++;
             for (int e = 0; e < neq; e++) Fmid[a][(size_t)e * nf + f] = use_hll ? Fh[e] : Fc[e];
             umid[a][f] = um;

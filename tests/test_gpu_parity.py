@@ -87,6 +87,19 @@ def test_flux_source_fast_within_tolerance(cuda, variant):
         if model == O.MODEL_FIVE_EQN_ALLAIRE:
             err = rel_err(Sg[-1:], So[-1:])
             assert err <= TOL_FAST, f"{label}: source rel err {err:.3e}"
+        # Fallback and HLLC-HLL faces are always evaluated in the exact form.
+        fb, hh = rec.readCounters()
+        assert (fb, hh) == (st[1], st[2]), f"{label}: counters {fb, hh} vs oracle {st[1:]}"
+
+
+# Over several substeps the fast form is compared with a looser bound: a state
+# that differs in the last bit can flip a discrete decision of the reference
+# algorithm at a later substep (the WCNS6-LD tau-switch R_tau > alpha_tau, the
+# shock sensor on near-zero dilatation), after which the two trajectories
+# differ by the size of that switch.  Per call, on identical inputs, the fast
+# form stays within 1e-12 (test above); the exact form stays bitwise equal
+# over any number of steps.
+TOL_FAST_STEPS = {O.SCHEME_WCNS5_JS: 1e-9, O.SCHEME_WCNS6_LD: 1e-5}
 
 
 @pytest.mark.gpu
@@ -114,7 +127,7 @@ def test_rk3_steps(cuda, variant, precision):
         assert np.array_equal(out, Qo), f"max diff {np.abs(out - Qo).max()}"
     else:
         err = rel_err(out, Qo)
-        assert err <= TOL_FAST, f"rel err {err:.3e}"
+        assert err <= TOL_FAST_STEPS[scheme], f"rel err {err:.3e}"
 
 
 @pytest.mark.gpu
