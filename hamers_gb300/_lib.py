@@ -19,6 +19,7 @@ HMR_ERR_UNSUPPORTED = -2
 HMR_ERR_NO_DEVICE = -3
 HMR_ERR_STATE = -4
 HMR_ERR_BARRIER = -5
+HMR_ERR_CAPACITY = -6
 
 HMR_SINGLE_SPECIES = 0
 HMR_FOUR_EQN_CONSERVATIVE = 1
@@ -35,6 +36,7 @@ EXPORTS = [
     "hmr_rk_stage_patch", "hmr_rk_substep_patch", "hmr_fill_ghosts_patch", "hmr_level_create",
     "hmr_level_destroy", "hmr_level_bind_state", "hmr_level_set_periodic", "hmr_level_state",
     "hmr_level_substep", "hmr_level_step", "hmr_level_check", "hmr_level_barrier_diagnostic", "hmr_level_autotune",
+    "hmr_rk_substep_patch_noalloc",
 ]
 
 
@@ -68,7 +70,7 @@ class HmrError(RuntimeError):
     def __init__(self, where, code):
         names = {HMR_ERR_ARGUMENT: "HMR_ERR_ARGUMENT", HMR_ERR_UNSUPPORTED: "HMR_ERR_UNSUPPORTED",
                  HMR_ERR_NO_DEVICE: "HMR_ERR_NO_DEVICE", HMR_ERR_STATE: "HMR_ERR_STATE",
-                 HMR_ERR_BARRIER: "HMR_ERR_BARRIER"}
+                 HMR_ERR_BARRIER: "HMR_ERR_BARRIER", HMR_ERR_CAPACITY: "HMR_ERR_CAPACITY"}
         super().__init__(f"{where} failed: {names.get(code, 'cudaError %d' % code)}")
         self.code = code
 
@@ -115,6 +117,8 @@ def load():
     L.hmr_level_barrier_diagnostic.argtypes = [vp, ctypes.c_uint, ctypes.c_ulonglong]
     L.hmr_level_step.argtypes = [vp, ctypes.c_double, vp]
     L.hmr_level_autotune.argtypes = [vp, ctypes.c_double, ip, ip, vp]
+    L.hmr_rk_substep_patch_noalloc.argtypes = [cfgp, gp, ctypes.c_int, dp, ctypes.c_double, DPPP,
+                                               ctypes.c_double, DPP, vp]
     for name in EXPORTS:
         getattr(L, name).restype = ctypes.c_int
     _lib = L

@@ -23,6 +23,7 @@ UNITS = [
     ("hmr_faces.cu", "hmr_faces_exact.o", ["-DHMR_FAST=0", "--fmad=false"]),
     ("hmr_faces.cu", "hmr_faces_fast.o", ["-DHMR_FAST=1", "--fmad=true"]),
     ("hmr_abi.cu", "hmr_abi.o", ["-DHMR_FAST=0", "--fmad=false"]),
+    ("hmr_noalloc.cu", "hmr_noalloc.o", ["-DHMR_FAST=0", "--fmad=false"]),
 ]
 
 

@@ -53,7 +53,8 @@ typedef enum {
     HMR_ERR_UNSUPPORTED = -2,
     HMR_ERR_NO_DEVICE = -3,
     HMR_ERR_STATE = -4,
-    HMR_ERR_BARRIER = -5
+    HMR_ERR_BARRIER = -5,
+    HMR_ERR_CAPACITY = -6     /* patch too large for hmr_rk_substep_patch_noalloc's fixed scratch */
 } hmr_status;
 
 /* FlowModelManager model names (src/flow/flow_models/FlowModelManager.cpp). */
@@ -177,6 +178,30 @@ int hmr_level_barrier_diagnostic(hmr_level* level, unsigned int extra_arrivals, 
 /* Autotuner: times the persistent kernel of this level at 64/128/256 threads per block and
  * every resident block count per SM, keeps the fastest.  Returns the chosen shape. */
 int hmr_level_autotune(hmr_level* level, double dt, int* threads_out, int* blocks_per_sm_out, void* stream);
+
+/* Fixed device scratch of hmr_rk_substep_patch_noalloc: 32 MiB, held on every GPU that loads
+ * the library until the process exits. */
+#define HMR_NOALLOC_SCRATCH_BYTES (32u << 20)
+
+/* hmr_rk_substep_patch without any allocation.  No counterpart in the reference: it exists for
+ * callers that cannot allocate device memory at the point of the call -- hosts whose device memory
+ * is owned by their own pool allocator, code that must not trigger the implicit device
+ * synchronisation of cudaMalloc/cudaFree inside a time-step loop, and plugin environments that
+ * forbid allocation.  It takes the configuration directly (creating an hmr_ctx allocates) and
+ * keeps its scratch in a file-scope device array of HMR_NOALLOC_SCRATCH_BYTES.
+ *   - Same arguments and result as hmr_rk_substep_patch (stage < 3, Q_int[stage] ghost-filled).
+ *   - Patches whose scratch exceeds the array are rejected with HMR_ERR_CAPACITY before any work
+ *     is queued: square/cubic patches fit up to 453^2 (2D single species), 397^2 (2D five-equation),
+ *     48^3 (3D single species) and 44^3 (3D five-equation) cells.
+ *   - The first call on a device resolves the array's device address (cudaGetSymbolAddress with
+ *     that device current) and caches it; make that first call before any stream capture.
+ *   - Allocates nothing: no cudaMalloc, cudaFree or allocating library call.  The face counters
+ *     of hmr_read_counters are not updated.
+ *   - Every call shares the one array and leaves its contents behind; calls whose work overlaps
+ *     on the GPU (different streams without ordering) race on it.  Serialise them. */
+int hmr_rk_substep_patch_noalloc(const hmr_config* cfg, const hmr_patch_geometry* geom, int stage,
+                                 const double* alpha, double beta, const double* const* const* Q_int,
+                                 double dt, double* const* Q_out, void* stream);
 
 #ifdef __cplusplus
 }
