@@ -1,8 +1,9 @@
 """Builds the CUDA library libhmr_gb300.so in-tree (sm_103a only).
 
-hmr_faces.cu is compiled twice: the exact form (-DHMR_FAST=0 --fmad=false,
-the reference's operation order, bitwise equal to it) and the fast form
-(-DHMR_FAST=1).  The cell-data kernels are always exact.
+hmr_faces.cu is compiled once per arithmetic form -- the exact form
+(-DHMR_FAST=0 --fmad=false, the reference's operation order, bitwise equal to
+it) and the fast form (-DHMR_FAST=1) -- and flow model (-DHMR_MODEL=0/1/2), six
+translation units compiled in parallel.  The cell-data kernels are always exact.
 """
 import os
 import shutil
@@ -20,10 +21,12 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", os.path
 
 UNITS = [
     ("hmr_cells.cu", "hmr_cells.o", ["-DHMR_FAST=0", "--fmad=false"]),
-    ("hmr_faces.cu", "hmr_faces_exact.o", ["-DHMR_FAST=0", "--fmad=false"]),
-    ("hmr_faces.cu", "hmr_faces_fast.o", ["-DHMR_FAST=1", "--fmad=true"]),
     ("hmr_abi.cu", "hmr_abi.o", ["-DHMR_FAST=0", "--fmad=false"]),
     ("hmr_noalloc.cu", "hmr_noalloc.o", ["-DHMR_FAST=0", "--fmad=false"]),
+] + [
+    ("hmr_faces.cu", "hmr_faces_%s_m%d.o" % (form, model),
+     ["-DHMR_FAST=%d" % fast, "--fmad=%s" % ("true" if fast else "false"), "-DHMR_MODEL=%d" % model])
+    for form, fast in (("exact", 0), ("fast", 1)) for model in (0, 1, 2)
 ]
 
 

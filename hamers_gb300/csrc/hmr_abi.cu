@@ -192,11 +192,17 @@ int hmr_ctx_create(const hmr_config* cfg, hmr_ctx** out) {
         if (cfg->num_species != 2) return HMR_ERR_UNSUPPORTED;
         neq = cfg->dim + 2 * cfg->num_species;
         ncomp = neq + 1;
+    } else if (cfg->flow_model == HMR_FOUR_EQN_CONSERVATIVE) {
+        if (cfg->num_species != 2) return HMR_ERR_UNSUPPORTED;
+        neq = cfg->num_species + cfg->dim + 1;
+        ncomp = neq;
     } else {
         return HMR_ERR_UNSUPPORTED;
     }
-    for (int s = 0; s < cfg->num_species; s++)
+    for (int s = 0; s < cfg->num_species; s++) {
         if (!(cfg->species_gamma[s] > 1.0)) return HMR_ERR_ARGUMENT;
+        if (cfg->flow_model == HMR_FOUR_EQN_CONSERVATIVE && !(cfg->species_R[s] > 0.0)) return HMR_ERR_ARGUMENT;
+    }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
         cudaGetLastError();
@@ -208,10 +214,7 @@ int hmr_ctx_create(const hmr_config* cfg, hmr_ctx** out) {
     c->v.model = cfg->flow_model;
     c->v.nsp = cfg->num_species;
     c->v.scheme = cfg->convective_flux_reconstructor;
-    for (int s = 0; s < MAX_SPECIES; s++) {
-        c->P.gamma[s] = s < cfg->num_species ? cfg->species_gamma[s] : 1.4;
-        c->P.inv_gm1[s] = double(1)/(c->P.gamma[s] - double(1));
-    }
+    species_params(cfg->species_gamma, cfg->species_R, cfg->num_species, c->P);
     c->P.p = cfg->constant_p;
     c->P.q = cfg->constant_q;
     c->P.C = cfg->constant_C;

@@ -25,6 +25,10 @@ static int dispatch(const Variant& v, F f) {
         if (v.dim == 2) return f(VT<2, FIVE_EQN_ALLAIRE, 2>{});
         if (v.dim == 3) return f(VT<3, FIVE_EQN_ALLAIRE, 2>{});
     }
+    if (v.model == FOUR_EQN_CONSERVATIVE && v.nsp == 2) {
+        if (v.dim == 2) return f(VT<2, FOUR_EQN_CONSERVATIVE, 2>{});
+        if (v.dim == 3) return f(VT<3, FOUR_EQN_CONSERVATIVE, 2>{});
+    }
     return -2;
 }
 

@@ -1,14 +1,21 @@
-// Face and update kernels of one arithmetic form.  Built twice from this
-// file: -DHMR_FAST=0 --fmad=false (namespace hmr_exact) and -DHMR_FAST=1
-// (namespace hmr_fast).
+// Face and update kernels of one arithmetic form and one flow model.  Built
+// six times from this file: -DHMR_FAST=0 --fmad=false (namespace
+// hmr_exact_m<model>) and -DHMR_FAST=1 (namespace hmr_fast_m<model>), with
+// -DHMR_MODEL=0 (single species), 1 (four-equation) or 2 (five-equation).
 #include <cuda_runtime.h>
 
 #include "hmr_launch.h"
 
+#ifndef HMR_MODEL
+#error "HMR_MODEL must be defined: 0 single species, 1 four-equation, 2 five-equation"
+#endif
+
+#define HMR_CAT2(a, b) a##b
+#define HMR_CAT(a, b) HMR_CAT2(a, b)
 #if HMR_FAST
-#define HMR_NS hmr_fast
+#define HMR_NS HMR_CAT(hmr_fast_m, HMR_MODEL)
 #else
-#define HMR_NS hmr_exact
+#define HMR_NS HMR_CAT(hmr_exact_m, HMR_MODEL)
 #endif
 
 namespace HMR_NS {
@@ -20,19 +27,17 @@ struct VT {
     static constexpr int DIM = D, MODEL = M, NSP = N, SCHEME = S;
 };
 
+// Variants of this translation unit: 2D/3D x WCNS5-JS/WCNS6-LD of its model
+// (one species for the single-species model, two for the multi-species ones).
 template <class F>
 static int dispatch(const Variant& v, F f) {
-#define HMR_CASE(D_, M_, N_, S_) \
-    if (v.dim == D_ && v.model == M_ && v.nsp == N_ && v.scheme == S_) return f(VT<D_, M_, N_, S_>{});
-    HMR_CASE(2, SINGLE_SPECIES, 1, WCNS5_JS)
-    HMR_CASE(2, SINGLE_SPECIES, 1, WCNS6_LD)
-    HMR_CASE(3, SINGLE_SPECIES, 1, WCNS5_JS)
-    HMR_CASE(3, SINGLE_SPECIES, 1, WCNS6_LD)
-    HMR_CASE(2, FIVE_EQN_ALLAIRE, 2, WCNS5_JS)
-    HMR_CASE(2, FIVE_EQN_ALLAIRE, 2, WCNS6_LD)
-    HMR_CASE(3, FIVE_EQN_ALLAIRE, 2, WCNS5_JS)
-    HMR_CASE(3, FIVE_EQN_ALLAIRE, 2, WCNS6_LD)
-#undef HMR_CASE
+    constexpr int M_ = HMR_MODEL;
+    constexpr int N_ = M_ == SINGLE_SPECIES ? 1 : 2;
+    if (v.model != M_ || v.nsp != N_) return -2;
+    if (v.dim == 2 && v.scheme == WCNS5_JS) return f(VT<2, M_, N_, WCNS5_JS>{});
+    if (v.dim == 2 && v.scheme == WCNS6_LD) return f(VT<2, M_, N_, WCNS6_LD>{});
+    if (v.dim == 3 && v.scheme == WCNS5_JS) return f(VT<3, M_, N_, WCNS5_JS>{});
+    if (v.dim == 3 && v.scheme == WCNS6_LD) return f(VT<3, M_, N_, WCNS6_LD>{});
     return -2;
 }
 

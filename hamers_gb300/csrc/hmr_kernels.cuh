@@ -159,6 +159,13 @@ __device__ __forceinline__ bool face_eval(const Params& P, const FaceProj<DIM, M
         // relative margins: density against the projection density, pressure against the cell pressures
         mL = fmin(fabs(VL[0])/rref, fabs(VL[M::IP])/pref);
         mR = fmin(fabs(VR[0])/rref, fabs(VR[M::IP])/pref);
+    } else if constexpr (MODEL == FOUR_EQN_CONSERVATIVE) {
+        // add density and pressure, relative like the single-species model
+        double rL = 0.0, rR = 0.0;
+#pragma unroll
+        for (int s = 0; s < NSP; s++) { rL += VL[s]; rR += VR[s]; }
+        mL = fmin(mL, fmin(fabs(rL)/rref, fabs(VL[M::IP])/pref));
+        mR = fmin(mR, fmin(fabs(rR)/rref, fabs(VR[M::IP])/pref));
     }
     margin = fmin(mL, mR);
     if (!ok) {
@@ -228,7 +235,7 @@ __device__ __forceinline__ bool face_item(const Params& P, const Geom& g, const 
     }
 
     double pref = 1.0;
-    if constexpr (MODEL == SINGLE_SPECIES)
+    if constexpr (MODEL != FIVE_EQN_ALLAIRE)
         pref = fmax(fabs(S.V[M::IP * nc + xL]), fabs(S.V[M::IP * nc + xR]));
     double Fo[NEQ], umid, margin;
     const bool ok = face_eval<X, DIM, MODEL, NSP, SCHEME, A>(P, F, W, S, nc, xL, xR, use_hll, F.rb, pref, Fo,

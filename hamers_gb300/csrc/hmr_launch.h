@@ -11,6 +11,18 @@
 
 namespace hmr {
 
+// Species constants of Params from species_gamma / species_R, as the
+// ideal-gas mixing rules derive them (EquationOfStateMixingRulesIdealGas.cpp:107-120).
+inline void species_params(const double* gamma, const double* R, int nsp, Params& P) {
+    for (int s = 0; s < MAX_SPECIES; s++) {
+        P.gamma[s] = s < nsp ? gamma[s] : 1.4;
+        const double Rs = s < nsp ? R[s] : 1.0;
+        P.inv_gm1[s] = double(1)/(P.gamma[s] - double(1));
+        P.cp[s] = P.gamma[s]/(P.gamma[s] - double(1))*Rs;
+        P.cv[s] = double(1)/(P.gamma[s] - double(1))*Rs;
+    }
+}
+
 struct Variant {
     int dim;
     int model;
@@ -61,6 +73,9 @@ int launch_rk_stage(const hmr::Variant& v, const hmr::Geom& g, int ncoef, const 
                     cudaStream_t st);
 }
 
+// hmr_faces.cu is built once per arithmetic form and flow model (six
+// translation units compiled in parallel); each defines these launchers in
+// namespace <form>_m<model>.
 #define HMR_DECLARE_FACE_LAUNCHERS(NS)                                                                       \
     namespace NS {                                                                                           \
     int launch_faces(const hmr::Variant& v, const hmr::Params& P, const hmr::Geom& g, const hmr::Scratch& S, \
@@ -72,5 +87,40 @@ int launch_rk_stage(const hmr::Variant& v, const hmr::Geom& g, int ncoef, const 
     int level_max_blocks(const hmr::Variant& v, int threads, int* blocks);                                   \
     }
 
-HMR_DECLARE_FACE_LAUNCHERS(hmr_exact)
-HMR_DECLARE_FACE_LAUNCHERS(hmr_fast)
+HMR_DECLARE_FACE_LAUNCHERS(hmr_exact_m0)
+HMR_DECLARE_FACE_LAUNCHERS(hmr_exact_m1)
+HMR_DECLARE_FACE_LAUNCHERS(hmr_exact_m2)
+HMR_DECLARE_FACE_LAUNCHERS(hmr_fast_m0)
+HMR_DECLARE_FACE_LAUNCHERS(hmr_fast_m1)
+HMR_DECLARE_FACE_LAUNCHERS(hmr_fast_m2)
+
+// Per-form entry points: route to the translation unit of the variant's model.
+#define HMR_ROUTE(NS, FN, ...)                                            \
+    switch (v.model) {                                                    \
+    case hmr::SINGLE_SPECIES: return NS##_m0::FN(__VA_ARGS__);            \
+    case hmr::FOUR_EQN_CONSERVATIVE: return NS##_m1::FN(__VA_ARGS__);     \
+    case hmr::FIVE_EQN_ALLAIRE: return NS##_m2::FN(__VA_ARGS__);          \
+    default: return -2;                                                   \
+    }
+
+#define HMR_DEFINE_FACE_ROUTER(NS)                                                                             \
+    namespace NS {                                                                                             \
+    inline int launch_faces(const hmr::Variant& v, const hmr::Params& P, const hmr::Geom& g,                   \
+                            const hmr::Scratch& S, hmr::Counters* cnt, const hmr::Redo& R, cudaStream_t st) {  \
+        HMR_ROUTE(NS, launch_faces, v, P, g, S, cnt, R, st)                                                    \
+    }                                                                                                          \
+    inline int launch_update(const hmr::Variant& v, const hmr::Geom& g, const hmr::Scratch& S,                 \
+                             const hmr::UpdateArgs& U, cudaStream_t st) {                                      \
+        HMR_ROUTE(NS, launch_update, v, g, S, U, st)                                                           \
+    }                                                                                                          \
+    inline int launch_level(const hmr::Variant& v, const hmr::Params& P, const hmr::LevelArgs& L, int blocks,  \
+                            int threads, cudaStream_t st) {                                                    \
+        HMR_ROUTE(NS, launch_level, v, P, L, blocks, threads, st)                                              \
+    }                                                                                                          \
+    inline int level_max_blocks(const hmr::Variant& v, int threads, int* blocks) {                             \
+        HMR_ROUTE(NS, level_max_blocks, v, threads, blocks)                                                    \
+    }                                                                                                          \
+    }
+
+HMR_DEFINE_FACE_ROUTER(hmr_exact)
+HMR_DEFINE_FACE_ROUTER(hmr_fast)

@@ -81,11 +81,16 @@ extern "C" int hmr_rk_substep_patch_noalloc(const hmr_config* cfg, const hmr_pat
     } else if (cfg->flow_model == HMR_FIVE_EQN_ALLAIRE && cfg->num_species == 2) {
         neq = dim + 4;
         ncomp = neq + 1;
+    } else if (cfg->flow_model == HMR_FOUR_EQN_CONSERVATIVE && cfg->num_species == 2) {
+        neq = dim + 3;
+        ncomp = neq;
     } else {
         return HMR_ERR_UNSUPPORTED;
     }
-    for (int s = 0; s < cfg->num_species; s++)
+    for (int s = 0; s < cfg->num_species; s++) {
         if (!(cfg->species_gamma[s] > 1.0)) return HMR_ERR_ARGUMENT;
+        if (cfg->flow_model == HMR_FOUR_EQN_CONSERVATIVE && !(cfg->species_R[s] > 0.0)) return HMR_ERR_ARGUMENT;
+    }
 
     Geom g;
     for (int d = 0; d < 3; d++) {
@@ -126,10 +131,7 @@ extern "C" int hmr_rk_substep_patch_noalloc(const hmr_config* cfg, const hmr_pat
     v.nsp = cfg->num_species;
     v.scheme = cfg->convective_flux_reconstructor;
     Params P;
-    for (int s = 0; s < MAX_SPECIES; s++) {
-        P.gamma[s] = s < cfg->num_species ? cfg->species_gamma[s] : 1.4;
-        P.inv_gm1[s] = double(1)/(P.gamma[s] - double(1));
-    }
+    species_params(cfg->species_gamma, cfg->species_R, cfg->num_species, P);
     P.p = cfg->constant_p;
     P.q = cfg->constant_q;
     P.C = cfg->constant_C;

@@ -16,9 +16,10 @@
 //   HLLC, HLLC-HLL
 //             src/flow/flow_models/single-species/Riemann_solvers/FlowModelRiemannSolverSingleSpeciesHLLC-HLL.cpp:889-1027
 //             src/flow/flow_models/five-eqn_Allaire/Riemann_solvers/FlowModelRiemannSolverFiveEqnAllaireHLLC-HLL.cpp:1283-1503
-//   ideal-gas EOS and volume-fraction mixing rule
+//             src/flow/flow_models/four-eqn_conservative/Riemann_solvers/FlowModelRiemannSolverFourEqnConservativeHLLC-HLL.cpp:1073-1245
+//   ideal-gas EOS and volume-/mass-fraction mixing rules
 //             src/util/mixing_rules/equations_of_state/ideal_gas/EquationOfStateIdealGas.cpp:29-43,561-575,1093-1107
-//             src/util/mixing_rules/equations_of_state/ideal_gas/EquationOfStateMixingRulesIdealGas.cpp:7404-7800
+//             src/util/mixing_rules/equations_of_state/ideal_gas/EquationOfStateMixingRulesIdealGas.cpp:107-120,6367-6420,6946-7150,7404-7800
 #pragma once
 
 #ifndef HMR_FAST
@@ -39,6 +40,8 @@ constexpr int MAX_COMP = 12;
 struct Params {
     double gamma[MAX_SPECIES];         // species_gamma
     double inv_gm1[MAX_SPECIES];       // 1/(gamma_i - 1)
+    double cp[MAX_SPECIES];            // species c_p = gamma_i/(gamma_i - 1)*R_i (four-equation model)
+    double cv[MAX_SPECIES];            // species c_v = 1/(gamma_i - 1)*R_i
     int p, q;                          // WCNS constants
     double C, alpha_tau;
 };
@@ -51,6 +54,7 @@ struct Model {
     static constexpr int IU = MODEL == SINGLE_SPECIES ? 1 : NSP;            // first velocity in V
     static constexpr int IP = MODEL == SINGLE_SPECIES ? DIM + 1 : NSP + DIM; // pressure in V
     static constexpr int IZ = NSP + DIM + 1;                                  // first volume fraction in V (five)
+    static constexpr int NZ = MODEL == FIVE_EQN_ALLAIRE ? NSP - 1 : 0;       // volume fractions in the equations
     static constexpr int NPROJ = MODEL == SINGLE_SPECIES ? 2 : NSP + 2;
     static constexpr int IE = MODEL == SINGLE_SPECIES ? DIM + 1 : NSP + DIM; // total energy in Q
 };
@@ -81,6 +85,40 @@ __device__ __forceinline__ double gamma_all_x(const Params& P, const double* Z) 
     return add_(double(1)/xi, double(1));
 }
 
+// Four-equation model: mass-fraction mixture c_p, c_v and gamma = c_p/c_v
+// (EquationOfStateMixingRulesIdealGas.cpp:6946-7150).
+template <bool X, int NSP>
+__device__ __forceinline__ double mix_mass(const Params& P, const double* Y, double& cv) {
+    double cp = 0.0;
+    cv = 0.0;
+#pragma unroll
+    for (int s = 0; s < NSP; s++) {
+        cp = X ? add_(cp, mul_(Y[s], P.cp[s])) : cp + Y[s]*P.cp[s];
+        cv = X ? add_(cv, mul_(Y[s], P.cv[s])) : cv + Y[s]*P.cv[s];
+    }
+    return cp/cv;
+}
+
+// Four-equation model, reference order: squared sound speed
+// Gamma p/rho + sum Y_i Psi_i with Psi_i = ((c_p,i - gamma c_v,i)/c_v + gamma - 1) eps
+// and eps = p/((gamma - 1) rho) (EquationOfStateMixingRulesIdealGas.cpp:6367-6420,
+// FlowModelFourEqnConservative.cpp:5087-5445).  Returns c^2; eps is the
+// internal energy from (rho, p, Y) (EquationOfStateIdealGas.cpp:6291).
+template <int NSP>
+__device__ __forceinline__ double four_c2_x(const Params& P, double rho, double p, const double* Y, double& eps) {
+    double cv;
+    const double gamma = mix_mass<true, NSP>(P, Y, cv);
+    const double Gamma = sub_(gamma, double(1));
+    eps = p/mul_(sub_(gamma, double(1)), rho);
+    double c2 = mul_(Gamma, p)/rho;
+#pragma unroll
+    for (int s = 0; s < NSP; s++) {
+        const double Psi = mul_(sub_(add_(sub_(P.cp[s], mul_(gamma, P.cv[s]))/cv, gamma), double(1)), eps);
+        c2 = add_(c2, mul_(Y[s], Psi));
+    }
+    return c2;
+}
+
 template <int DIM, int MODEL, int NSP>
 __device__ __forceinline__ void cell_derived(const Params& P, const double* Q, double* V,
                                              double& rho, double& cs) {
@@ -101,6 +139,32 @@ __device__ __forceinline__ void cell_derived(const Params& P, const double* Q, d
 #pragma unroll
         for (int k = 0; k < DIM; k++) V[1 + k] = u[k];
         V[DIM + 1] = p;
+    } else if constexpr (MODEL == FOUR_EQN_CONSERVATIVE) {
+        // FlowModelFourEqnConservative.cpp:3877-5445
+        double r = 0.0;
+#pragma unroll
+        for (int s = 0; s < NSP; s++) r = add_(r, Q[s]);
+        rho = r;
+        double Y[NSP];
+        double u[DIM];
+#pragma unroll
+        for (int s = 0; s < NSP; s++) Y[s] = Q[s]/r;
+#pragma unroll
+        for (int k = 0; k < DIM; k++) u[k] = Q[NSP + k]/r;
+        double ke = mul_(u[0], u[0]);
+#pragma unroll
+        for (int k = 1; k < DIM; k++) ke = add_(ke, mul_(u[k], u[k]));
+        double cv;
+        const double gamma = mix_mass<true, NSP>(P, Y, cv);
+        const double eps = sub_(Q[NSP + DIM]/r, mul_(double(1)/double(2), ke));
+        const double p = mul_(mul_(sub_(gamma, double(1)), r), eps);
+        double eps_p;
+        cs = sqrt(four_c2_x<NSP>(P, r, p, Y, eps_p));
+#pragma unroll
+        for (int s = 0; s < NSP; s++) V[s] = Q[s];
+#pragma unroll
+        for (int k = 0; k < DIM; k++) V[NSP + k] = u[k];
+        V[NSP + DIM] = p;
     } else {
         double r = 0.0;
 #pragma unroll
@@ -199,7 +263,7 @@ __device__ __forceinline__ void char_from_prim(const FaceProj<DIM, MODEL, NSP>& 
 #pragma unroll
         for (int s = 0; s < NSP; s++) W[1 + s] = sub_(V[s], mul_(F.zr[s], p));
 #pragma unroll
-        for (int s = 0; s < NSP - 1; s++) W[NSP + DIM + s] = V[M::IZ + s];
+        for (int s = 0; s < M::NZ; s++) W[NSP + DIM + s] = V[M::IZ + s];
         W[0] = sub_(un, mul_(F.irc, p));
         W[M::NEQ - 1] = add_(un, mul_(F.irc, p));
         int t = NSP + 1;
@@ -266,7 +330,7 @@ __device__ __forceinline__ void prim_from_char(const FaceProj<DIM, MODEL, NSP>& 
             else V[s] = F.hz[s]*(W[L] - W[0]) + W[s + 1];
         }
 #pragma unroll
-        for (int s = 0; s < NSP - 1; s++) V[M::IZ + s] = W[NSP + DIM + s];
+        for (int s = 0; s < M::NZ; s++) V[M::IZ + s] = W[NSP + DIM + s];
         int t = NSP + 1;
 #pragma unroll
         for (int k = 0; k < DIM; k++) {
@@ -489,6 +553,24 @@ __device__ __forceinline__ bool face_bounded(const Params& P, const double* V, d
     if constexpr (MODEL == SINGLE_SPECIES) {
         margin = fmin(fabs(V[0]), fabs(V[DIM + 1]));
         return (V[0] > 0.0) && (V[DIM + 1] > 0.0);
+    } else if constexpr (MODEL == FOUR_EQN_CONSERVATIVE) {
+        // FlowModelBasicUtilitiesFourEqnConservative.cpp:3737-4510, bounds
+        // FlowModelBasicUtilitiesFourEqnConservative.hpp:24-25: Y in (-0.001, 1.001), rho > 0, p > 0.
+        // margin covers the mass fractions; the caller adds density and pressure.
+        double rho = 0.0;
+#pragma unroll
+        for (int s = 0; s < NSP; s++) rho = add_(rho, V[s]);
+        bool ok = true;
+        double m = 1.0e300;
+#pragma unroll
+        for (int s = 0; s < NSP; s++) {
+            const double Y = V[s]/rho;
+            ok = ok && (Y > -0.001 && Y < 1.001);
+            m = fmin(m, fmin(fabs(Y + 0.001), fabs(1.001 - Y)));
+        }
+        ok = ok && (rho > 0.0) && (V[NSP + DIM] > 0.0);
+        margin = m;
+        return ok;
     } else {
         bool ok = true;
         double Z[NSP];
@@ -549,6 +631,33 @@ __device__ __forceinline__ void face_thermo(const Params& P, const double* V, do
             const double ri = double(1)/rho;
             cs = sqrt(gamma*p*ri);
             eps = p*ri*P.inv_gm1[0];
+        }
+    } else if constexpr (MODEL == FOUR_EQN_CONSERVATIVE) {
+        // FlowModelRiemannSolverFourEqnConservativeHLLC-HLL.cpp:5530-5680 (2D x block)
+        double r = 0.0;
+#pragma unroll
+        for (int s = 0; s < NSP; s++) r = X ? add_(r, V[s]) : r + V[s];
+        rho = r;
+        const double p = V[NSP + DIM];
+        double Y[NSP];
+        if constexpr (X) {
+#pragma unroll
+            for (int s = 0; s < NSP; s++) Y[s] = V[s]/r;
+            cs = sqrt(four_c2_x<NSP>(P, r, p, Y, eps));
+        } else {
+            const double ri = double(1)/r;
+#pragma unroll
+            for (int s = 0; s < NSP; s++) Y[s] = V[s]*ri;
+            double cv;
+            const double gamma = mix_mass<false, NSP>(P, Y, cv);
+            const double icv = double(1)/cv;
+            const double gm1 = gamma - double(1);
+            const double pr = p*ri;
+            eps = pr/gm1;
+            double c2 = gm1*pr;
+#pragma unroll
+            for (int s = 0; s < NSP; s++) c2 += Y[s]*(((P.cp[s] - gamma*P.cv[s])*icv + gm1)*eps);
+            cs = sqrt(c2);
         }
     } else {
         double r = 0.0;
@@ -615,7 +724,7 @@ __device__ __forceinline__ void face_QF(const double* V, double rho, double eps,
         Q[NSP + DIM] = X ? mul_(rho, add_(eps, mul_(double(1)/double(2), ke)))
                          : rho*(eps + double(1)/double(2)*ke);
 #pragma unroll
-        for (int s = 0; s < NSP - 1; s++) Q[M::IZ + s] = V[M::IZ + s];
+        for (int s = 0; s < M::NZ; s++) Q[M::IZ + s] = V[M::IZ + s];
 #pragma unroll
         for (int s = 0; s < NSP; s++) F[s] = X ? mul_(un, V[s]) : un*V[s];
 #pragma unroll
@@ -625,7 +734,7 @@ __device__ __forceinline__ void face_QF(const double* V, double rho, double eps,
         }
         F[NSP + DIM] = X ? mul_(un, add_(Q[NSP + DIM], p)) : un*(Q[NSP + DIM] + p);
 #pragma unroll
-        for (int s = 0; s < NSP - 1; s++) F[M::IZ + s] = X ? mul_(un, V[M::IZ + s]) : un*V[M::IZ + s];
+        for (int s = 0; s < M::NZ; s++) F[M::IZ + s] = X ? mul_(un, V[M::IZ + s]) : un*V[M::IZ + s];
     }
 }
 
@@ -709,7 +818,7 @@ __device__ __forceinline__ void riemann(const Params& P, const double* VL, const
         }
         Qs[NSP + DIM] = QsE;
 #pragma unroll
-        for (int s = 0; s < NSP - 1; s++) Qs[M::IZ + s] = X ? mul_(Chi, VK[M::IZ + s]) : Chi*VK[M::IZ + s];
+        for (int s = 0; s < M::NZ; s++) Qs[M::IZ + s] = X ? mul_(Chi, VK[M::IZ + s]) : Chi*VK[M::IZ + s];
     }
 #pragma unroll
     for (int e = 0; e < NEQ; e++) Fout[e] = X ? add_(FK[e], mul_(s_pm, sub_(Qs[e], QK[e]))) : FK[e] + s_pm*(Qs[e] - QK[e]);

@@ -48,7 +48,7 @@ def _stream_ptr(stream):
 
 
 class FlowModel:
-    """Flow model selection: 'SINGLE_SPECIES' or 'FIVE_EQN_ALLAIRE', ideal gas."""
+    """Flow model selection: 'SINGLE_SPECIES', 'FOUR_EQN_CONSERVATIVE' or 'FIVE_EQN_ALLAIRE', ideal gas."""
 
     def __init__(self, flow_model, dim, species_gamma, species_R=None):
         if flow_model not in _FLOW_MODELS:

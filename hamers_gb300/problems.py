@@ -5,6 +5,7 @@ patch: shape (ncomp, G2, G1, G0), ghost width 4, x fastest.  Component order
 follows the reference's conservative variables:
 
   single species  : rho, rho*u_k (dim), E
+  four-eqn conservative: rho*Y_i (N), rho*u_k (dim), E
   five-eqn Allaire: Z_i*rho_i (N), rho*u_k (dim), E, Z_i (N, the last one is
                     stored as the reference's volume-fraction CellData does)
 
@@ -76,13 +77,41 @@ def five_eqn_state(Z1, rho1, rho2, vel, p, gammas):
     return out
 
 
+def four_eqn_state(rho_Y, vel, p, gammas, Rs):
+    """Four-equation (conservative) conserved variables from partial densities.
+
+    Ideal-gas mixture with mass fractions: c_p = sum Y_i c_p,i, c_v = sum Y_i c_v,i,
+    gamma = c_p/c_v, species c_p,i = gamma_i/(gamma_i-1) R_i, c_v,i = R_i/(gamma_i-1)
+    (EquationOfStateMixingRulesIdealGas.cpp:107-120).
+    """
+    dim = len(vel)
+    N = len(rho_Y)
+    rho = sum(rho_Y)
+    cp = sum(rY / rho * g / (g - 1.0) * R for rY, g, R in zip(rho_Y, gammas, Rs))
+    cv = sum(rY / rho / (g - 1.0) * R for rY, g, R in zip(rho_Y, gammas, Rs))
+    gamma_m = cp / cv
+    out = np.empty((N + dim + 1,) + rho.shape)
+    for si in range(N):
+        out[si] = rho_Y[si]
+    for k in range(dim):
+        out[N + k] = rho * vel[k]
+    ke = sum(v * v for v in vel)
+    out[N + dim] = p / (gamma_m - 1.0) + 0.5 * rho * ke
+    return out
+
+
+FOUR_EQN_GAMMA = [1.6, 1.4]
+FOUR_EQN_R = [1.0, 2.5]
+
+
 # ---------------------------------------------------------------------------
 # Convergence problems of the reference's CI (tests/*_convergence_test_*/convergence_test.py)
 # ---------------------------------------------------------------------------
 def convergence_problem(model, dim, N):
     """Density-wave (single) or volume-fraction-wave (five-eqn) advection on [-1,1]^dim.
 
-    Returns (state, dx, dt, nsteps, exact(t) -> field on the interior, species_gamma).
+    Returns (state, dx, dt, nsteps, exact(t) -> field on the interior, species_gamma);
+    the four-equation variant advects a mass-fraction wave (field: rho*Y_1 at rho = 1).
     dt = 0.001*dx, 8 steps in 2D (1 in 3D) at N=8, doubled per refinement
     (convergence_test.py:18-23).
     """
@@ -103,6 +132,17 @@ def convergence_problem(model, dim, N):
         def exact(t):
             Xi = _interior(X, dim)
             return 1.0 + 0.5 * np.sin(math.pi * (sum(Xi) - dim * t))
+    elif model == MODEL_FOUR_EQN_CONSERVATIVE:
+        # Mass-fraction wave at uniform density, velocity and pressure (the
+        # reference has no four-equation convergence test; same set-up as its
+        # five-equation one with mass instead of volume fractions).
+        Y1 = 0.5 + 0.25 * np.sin(math.pi * s)
+        Q = four_eqn_state([Y1, 1.0 - Y1], ones, 1.0, FOUR_EQN_GAMMA, FOUR_EQN_R)
+        gam = list(FOUR_EQN_GAMMA)
+
+        def exact(t):
+            Xi = _interior(X, dim)
+            return 0.5 + 0.25 * np.sin(math.pi * (sum(Xi) - dim * t))
     else:
         Z1 = 0.5 + 0.25 * np.sin(math.pi * s)
         Q = five_eqn_state(Z1, 2.0, 1.0, ones, 1.0, (1.6, 1.4))
@@ -206,7 +246,7 @@ def taylor_green_3d(N=128, mach=0.1, gamma=1.4):
 
 
 def blobs_patches_3d(num_patches=512, side_lo=16, side_hi=64, seed=2, nblobs=32, gamma=1.4):
-    """Uneven 3D patches (side lengths U{lo..hi} per axis, seeded) holding a
+    """Uneven cubic 3D patches (side length U{lo..hi} per patch, seeded) holding a
     density field of 32 Gaussian blobs on [0,1]^3 with smoothed random
     velocity, p = 1.  Returns a list of (n[3], xlo[3], dx[3], state).  Half
     the patches sit on a level with twice the spacing of the other half
@@ -218,7 +258,7 @@ def blobs_patches_3d(num_patches=512, side_lo=16, side_hi=64, seed=2, nblobs=32,
     centres = rng.uniform(0.0, 1.0, (nblobs, 3))
     patches = []
     for p_i in range(num_patches):
-        n = [int(v) for v in rng.integers(side_lo, side_hi + 1, 3)]
+        n = [int(rng.integers(side_lo, side_hi + 1))] * 3
         level = 0 if p_i < num_patches // 2 else 1
         h = (1.0 / 256.0) / (2 ** level)
         xlo = [float(v) for v in rng.uniform(0.0, 1.0 - max(n) * h, 3)]
@@ -239,3 +279,45 @@ def blobs_patches_3d(num_patches=512, side_lo=16, side_hi=64, seed=2, nblobs=32,
         Q = single_species_state(rho, vel, np.ones_like(rho), gamma)
         patches.append((n, xlo, dx, np.ascontiguousarray(Q)))
     return patches
+
+
+def blobs_patches_3d_device(num_patches=512, side_lo=16, side_hi=64, seed=2, nblobs=32, gamma=1.4,
+                            device="cuda"):
+    """blobs_patches_3d evaluated with torch on the device (same recipe and seeds
+    for the layout and the blobs, cubic patches with E[side^3] ~ 87k cells, ~44.6 M
+    cells for 512 patches; the smoothed random velocity uses torch's generator).
+    Returns a list of (n[3], dx[3], state tensor (5, G2, G1, G0))."""
+    import torch
+    rng = np.random.default_rng(seed)
+    amps = rng.uniform(0.0, 0.5, nblobs)
+    widths = rng.uniform(0.02, 0.1, nblobs)
+    centres = rng.uniform(0.0, 1.0, (nblobs, 3))
+    gen = torch.Generator(device=device)
+    gen.manual_seed(seed)
+    out = []
+    for p_i in range(num_patches):
+        n = [int(rng.integers(side_lo, side_hi + 1))] * 3
+        level = 0 if p_i < num_patches // 2 else 1
+        h = (1.0 / 256.0) / (2 ** level)
+        xlo = [float(v) for v in rng.uniform(0.0, 1.0 - max(n) * h, 3)]
+        axes = [xlo[d] + (torch.arange(-GHOST, n[d] + GHOST, device=device, dtype=torch.float64) + 0.5) * h
+                for d in range(3)]
+        z, y, x = torch.meshgrid(axes[2], axes[1], axes[0], indexing="ij")
+        rho = torch.ones_like(x)
+        for b in range(nblobs):
+            r2 = (x - centres[b, 0]) ** 2 + (y - centres[b, 1]) ** 2 + (z - centres[b, 2]) ** 2
+            rho = rho + amps[b] * torch.exp(-r2 / widths[b] ** 2)
+        vel = []
+        for d in range(3):
+            f = torch.rand(x.shape, generator=gen, device=device, dtype=torch.float64) - 0.5
+            for _ in range(3):
+                for ax in range(3):
+                    f = (torch.roll(f, 1, ax) + f + torch.roll(f, -1, ax)) / 3.0
+            vel.append(f)
+        Q = torch.empty((5,) + tuple(x.shape), dtype=torch.float64, device=device)
+        Q[0] = rho
+        for d in range(3):
+            Q[1 + d] = rho * vel[d]
+        Q[4] = 1.0 / (gamma - 1.0) + 0.5 * rho * (vel[0] ** 2 + vel[1] ** 2 + vel[2] ** 2)
+        out.append((n, [h, h, h], Q.contiguous()))
+    return out

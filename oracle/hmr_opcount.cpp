@@ -51,6 +51,7 @@ double hmro_count_ops(int model, int dim, int nsp, int scheme, const double* gam
     hmro::Config c;
     c.model = model; c.dim = dim; c.num_species = nsp; c.scheme = scheme;
     for (int i = 0; i < 8; i++) c.gamma[i] = i < nsp ? gamma[i] : 1.4;
+    for (int i = 0; i < 8; i++) c.R[i] = 1.0;
     c.p = 2; c.q = 4; c.C = 1.0e9; c.alpha_tau = 35.0;
     const hmro::Box b = hmro::make_box(dim, n, 4);
     const int ncomp = hmro::num_comp(c), neq = hmro::num_eqn(c);

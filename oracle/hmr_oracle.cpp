@@ -18,6 +18,7 @@ struct hmro_config {
     int num_species;
     int scheme;
     double gamma[8];
+    double R[8];
     int p;
     int q;
     double C;
@@ -31,6 +32,7 @@ static Config to_cfg(const hmro_config* c) {
     k.num_species = c->num_species;
     k.scheme = c->scheme;
     for (int i = 0; i < 8; i++) k.gamma[i] = c->gamma[i];
+    for (int i = 0; i < 8; i++) k.R[i] = c->R[i];
     k.p = c->p;
     k.q = c->q;
     k.C = c->C;

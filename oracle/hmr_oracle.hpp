@@ -52,6 +52,7 @@ struct Config {
     int num_species;
     int scheme;
     double gamma[8];     // species_gamma
+    double R[8];         // species_R (four-equation model: species heat capacities)
     int p;               // constant_p  (JS default 2, WCNS5-JS-HLLC-HLL.cpp:188-191; LD default 2)
     int q;               // constant_q  (LD default 4, WCNS6-LD-HLLC-HLL.cpp:343-361)
     double C;            // constant_C  (LD default 1e9)
@@ -65,6 +66,8 @@ inline int num_eqn(const Config& c) {
     if (c.model == MODEL_FOUR_EQN_CONSERVATIVE) return c.num_species + c.dim + 1;
     return c.dim + 2 * c.num_species;
 }
+// Number of volume fractions in the equations (five-equation model only).
+inline int num_vf(const Config& c) { return c.model == MODEL_FIVE_EQN_ALLAIRE ? c.num_species - 1 : 0; }
 // Number of stored conserved components: the five-equation model also keeps
 // the last volume fraction (CellVariable of depth N, FlowModelFiveEqnAllaire.cpp:130-140).
 inline int num_comp(const Config& c) {
@@ -337,6 +340,41 @@ inline T gamma_mix_last(const Config& c, const T* Z /* N-1 */) {
     return double(1)/xi + double(1);
 }
 
+// Four-equation (conservative) model, ideal-gas mixture with mass fractions,
+// EquationOfStateMixingRulesIdealGas.cpp:4677-5143 (c_p, c_v weighted by Y,
+// gamma = c_p/c_v), species c_p = gamma/(gamma-1)*R, c_v = 1/(gamma-1)*R
+// (:113-119), and the partial-density derivative of pressure
+// Psi_i = ((c_p,i - gamma c_v,i)/c_v + gamma - 1) eps, eps = p/((gamma-1) rho)
+// (:3102-3157, array form :6367-6420).
+inline double species_cp(const Config& c, int s) { return c.gamma[s]/(c.gamma[s] - double(1))*c.R[s]; }
+inline double species_cv(const Config& c, int s) { return double(1)/(c.gamma[s] - double(1))*c.R[s]; }
+
+template <class T>
+inline void mix_mass(const Config& c, const T* Y, T& gamma, T& cv) {
+    T cp = T(0.0);
+    cv = T(0.0);
+    for (int si = 0; si < c.num_species; si++) {
+        cp += Y[si]*species_cp(c, si);
+        cv += Y[si]*species_cv(c, si);
+    }
+    gamma = cp/cv;
+}
+
+// Sound speed of the four-equation model from rho, p and the mass fractions.
+template <class T>
+inline T four_sound_speed(const Config& c, const T& rho, const T& p, const T* Y) {
+    T gamma, cv;
+    mix_mass(c, Y, gamma, cv);
+    const T Gamma = gamma - double(1);
+    const T eps = p/((gamma - double(1))*rho);
+    T c2 = Gamma*p/rho;
+    for (int si = 0; si < c.num_species; si++) {
+        const T Psi = ((species_cp(c, si) - gamma*species_cv(c, si))/cv + gamma - double(1))*eps;
+        c2 += Y[si]*Psi;
+    }
+    return s_sqrt(c2);
+}
+
 // Face thermodynamics used by the Riemann drivers (density, sound speed,
 // specific internal energy of one reconstructed state V).
 //  single: EquationOfStateIdealGas.cpp:5806 (c = sqrt(gamma*p/rho)), :6135 (eps = p/((gamma-1)*rho))
@@ -350,6 +388,18 @@ inline void face_thermo(const Config& c, const T* V, T& rho, T& cs, T& eps) {
         rho = V[0];
         const T& p = V[dim + 1];
         cs = s_sqrt(gamma*p/rho);
+        eps = p/((gamma - double(1))*rho);
+    } else if (c.model == MODEL_FOUR_EQN_CONSERVATIVE) {
+        // FlowModelRiemannSolverFourEqnConservativeHLLC-HLL.cpp:5013-6180 (2D block)
+        const int N = c.num_species;
+        rho = T(0.0);
+        for (int si = 0; si < N; si++) rho += V[si];
+        const T& p = V[N + dim];
+        T Y[8];
+        for (int si = 0; si < N; si++) Y[si] = V[si]/rho;
+        cs = four_sound_speed(c, rho, p, Y);
+        T gamma, cv;
+        mix_mass(c, Y, gamma, cv);
         eps = p/((gamma - double(1))*rho);
     } else {
         const int N = c.num_species;
@@ -381,6 +431,20 @@ inline int face_bounded(const Config& c, const T* V) {
     if (c.model == MODEL_SINGLE_SPECIES) {
         ok &= (s_val(V[0]) > 0.0) ? 1 : 0;
         ok &= (s_val(V[dim + 1]) > 0.0) ? 1 : 0;
+        return ok;
+    }
+    if (c.model == MODEL_FOUR_EQN_CONSERVATIVE) {
+        // FlowModelBasicUtilitiesFourEqnConservative.cpp:3737-4540, bounds
+        // FlowModelBasicUtilitiesFourEqnConservative.hpp:24-25: Y in (-0.001, 1.001), rho > 0, p > 0.
+        const int N = c.num_species;
+        T rho = T(0.0);
+        for (int si = 0; si < N; si++) rho += V[si];
+        for (int si = 0; si < N; si++) {
+            const T Y = V[si]/rho;
+            ok &= (s_val(Y) > -0.001 && s_val(Y) < 1.001) ? 1 : 0;
+        }
+        ok &= (s_val(rho) > 0.0) ? 1 : 0;
+        ok &= (s_val(V[N + dim]) > 0.0) ? 1 : 0;
         return ok;
     }
     const int N = c.num_species;
@@ -442,14 +506,14 @@ inline void face_QF(const Config& c, int a, const T* V, const T& rho, const T& e
     T ke = V[N]*V[N];
     for (int k = 1; k < dim; k++) ke = ke + V[N + k]*V[N + k];
     Q[N + dim] = rho*(eps + double(1)/double(2)*ke);
-    for (int si = 0; si < N - 1; si++) Q[N + dim + 1 + si] = V[N + dim + 1 + si];
+    for (int si = 0; si < num_vf(c); si++) Q[N + dim + 1 + si] = V[N + dim + 1 + si];
     for (int si = 0; si < N; si++) F[si] = un*V[si];
     for (int k = 0; k < dim; k++) {
         if (k == a) F[N + k] = un*Q[N + k] + p;
         else F[N + k] = un*Q[N + k];
     }
     F[N + dim] = un*(Q[N + dim] + p);
-    for (int si = 0; si < N - 1; si++) F[N + dim + 1 + si] = un*V[N + dim + 1 + si];
+    for (int si = 0; si < num_vf(c); si++) F[N + dim + 1 + si] = un*V[N + dim + 1 + si];
 }
 
 // Is component e advected with the HLL flux inside HLLC-HLL (mass/partial
@@ -536,7 +600,7 @@ inline void riemann_face(const Config& c, int a, const T* VL, const T* VR,
             else Qs[N + k] = Chi*QK[N + k];
         }
         Qs[N + dim] = Chi*(QK[N + dim] + (s_star - uK)*(rhoK*s_star + pK/(sK - uK)));
-        for (int si = 0; si < N - 1; si++) Qs[N + dim + 1 + si] = Chi*VK[N + dim + 1 + si];
+        for (int si = 0; si < num_vf(c); si++) Qs[N + dim + 1 + si] = Chi*VK[N + dim + 1 + si];
     }
     for (int e = 0; e < neq; e++) F_hllc[e] = FK[e] + s_pm*(Qs[e] - QK[e]);
     u_mid = uK + s_pm*(Chi - double(1));
@@ -594,11 +658,11 @@ inline void char_from_prim(const Config& c, int a, const T* proj, const T* V, T*
     for (int si = 0; si < N; si++) {
         W[1 + si] = V[si] - proj[si]/(rb*cb*cb)*p;
     }
-    for (int si = 0; si < N - 1; si++) W[N + dim + si] = V[N + dim + 1 + si];
+    for (int si = 0; si < num_vf(c); si++) W[N + dim + si] = V[N + dim + 1 + si];
     W[0] = un - double(1)/(rb*cb)*p;
     int t = N + 1;
     for (int k = 0; k < dim; k++) if (k != a) W[t++] = V[N + k];
-    W[2*N + dim - 1] = un + double(1)/(rb*cb)*p;
+    W[num_eqn(c) - 1] = un + double(1)/(rb*cb)*p;
 }
 
 //  single: FlowModelBasicUtilitiesSingleSpecies.cpp:7023-7474 (2D :7279-7330)
@@ -620,14 +684,14 @@ inline void prim_from_char(const Config& c, int a, const T* proj, const T* W, T*
         return;
     }
     const int N = c.num_species;
-    const int last = 2*N + dim - 1;
+    const int last = num_eqn(c) - 1;
     const T& rb = proj[N];
     const T& cb = proj[N + 1];
     for (int si = 0; si < N; si++) {
         V[si] = -double(1)/double(2)*proj[si]/cb*W[0] + W[si + 1] +
             double(1)/double(2)*proj[si]/cb*W[last];
     }
-    for (int si = 0; si < N - 1; si++) V[N + dim + 1 + si] = W[N + dim + si];
+    for (int si = 0; si < num_vf(c); si++) V[N + dim + 1 + si] = W[N + dim + si];
     int t = N + 1;
     for (int k = 0; k < dim; k++) {
         if (k == a) V[N + k] = double(1)/double(2)*W[0] + double(1)/double(2)*W[last];
@@ -695,6 +759,38 @@ void compute_derived(const Config& c, const Box& b, const T* const* Q, Derived<T
                     else F[(size_t)(1 + k) * nc + x] = u[a]*Q[1 + k][x];
                 }
                 F[(size_t)(dim + 1) * nc + x] = u[a]*(E + p);
+            }
+        } else if (c.model == MODEL_FOUR_EQN_CONSERVATIVE) {
+            // FlowModelFourEqnConservative.cpp:3877-5499: density, mass fractions,
+            // velocity, internal energy, pressure (mass-fraction mixture), sound speed.
+            const int N = c.num_species;
+            T rho = T(0.0);
+            for (int si = 0; si < N; si++) rho += Q[si][x];
+            T Y[8];
+            for (int si = 0; si < N; si++) Y[si] = Q[si][x]/rho;
+            T u[3];
+            for (int k = 0; k < dim; k++) u[k] = Q[N + k][x]/rho;
+            const T& E = Q[N + dim][x];
+            T ke = u[0]*u[0];
+            for (int k = 1; k < dim; k++) ke = ke + u[k]*u[k];
+            const T eps = E/rho - double(1)/double(2)*ke;
+            T gamma, cv;
+            mix_mass(c, Y, gamma, cv);
+            const T p = (gamma - double(1))*rho*eps;
+            const T cs = four_sound_speed(c, rho, p, Y);
+            D.rho[x] = rho;
+            D.cs[x] = cs;
+            for (int si = 0; si < N; si++) D.V[(size_t)si * nc + x] = Q[si][x];
+            for (int k = 0; k < dim; k++) D.V[(size_t)(N + k) * nc + x] = u[k];
+            D.V[(size_t)(N + dim) * nc + x] = p;
+            for (int a = 0; a < dim; a++) {
+                T* F = &D.Fn[(size_t)a * neq * nc];
+                for (int si = 0; si < N; si++) F[(size_t)si * nc + x] = u[a]*Q[si][x];
+                for (int k = 0; k < dim; k++) {
+                    if (k == a) F[(size_t)(N + k) * nc + x] = u[a]*Q[N + k][x] + p;
+                    else F[(size_t)(N + k) * nc + x] = u[a]*Q[N + k][x];
+                }
+                F[(size_t)(N + dim) * nc + x] = u[a]*(E + p);
             }
         } else {
             const int N = c.num_species;
@@ -772,6 +868,7 @@ void conv_flux_source(const Config& c, const int* n, const double* dx, double dt
     compute_derived(c, b, Q, D);
     const int iu = vel_index(c);
     const bool five = (c.model == MODEL_FIVE_EQN_ALLAIRE);
+    const bool multi = (c.model != MODEL_SINGLE_SPECIES);
     const int N = c.num_species;
 
     // Velocity derivatives, dilatation and vorticity magnitude on the
@@ -809,7 +906,7 @@ void conv_flux_source(const Config& c, const int* n, const double* dx, double dt
     std::vector<std::vector<T>> Fmid(dim), umid(dim);
     std::vector<FaceSet> FS(dim);
     long cnt_faces = 0, cnt_fallback = 0, cnt_hll = 0;
-    const int nproj = five ? N + 2 : 2;
+    const int nproj = multi ? N + 2 : 2;
 
     for (int a = 0; a < dim; a++) {
         const FaceSet fs = make_faces(b, a);
@@ -835,7 +932,9 @@ void conv_flux_source(const Config& c, const int* n, const double* dx, double dt
             const long f = fs.idx(i, j, k);
             const long xL = b.cell(i - off[0], j - off[1], k - off[2]);
             const long xR = b.cell(i, j, k);
-            if (five) {
+            if (multi) {
+                // five: FlowModelBasicUtilitiesFiveEqnAllaire.cpp:7474; four:
+                // FlowModelBasicUtilitiesFourEqnConservative.cpp:4638 (same means)
                 for (int si = 0; si < N; si++)
                     proj[(size_t)si * nf + f] = double(1)/double(2)*(Q[si][xL] + Q[si][xR]);
                 proj[(size_t)N * nf + f] = double(1)/double(2)*(D.rho[xL] + D.rho[xR]);

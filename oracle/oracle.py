@@ -28,7 +28,8 @@ GHOST = 4
 
 class _Cfg(ctypes.Structure):
     _fields_ = [("model", ctypes.c_int), ("dim", ctypes.c_int), ("num_species", ctypes.c_int),
-                ("scheme", ctypes.c_int), ("gamma", ctypes.c_double * 8), ("p", ctypes.c_int),
+                ("scheme", ctypes.c_int), ("gamma", ctypes.c_double * 8), ("R", ctypes.c_double * 8),
+                ("p", ctypes.c_int),
                 ("q", ctypes.c_int), ("C", ctypes.c_double), ("alpha_tau", ctypes.c_double)]
 
 
@@ -66,17 +67,19 @@ class Config:
     """Flow model + scheme selection (mirrors the reference's input keys)."""
 
     def __init__(self, model, dim, species_gamma, scheme=SCHEME_WCNS5_JS,
-                 p=2, q=4, C=1.0e9, alpha_tau=35.0):
+                 p=2, q=4, C=1.0e9, alpha_tau=35.0, species_R=None):
         self.model = int(model)
         self.dim = int(dim)
         self.species_gamma = [float(g) for g in species_gamma]
         self.num_species = len(self.species_gamma)
+        self.species_R = [float(r) for r in (species_R or [1.0] * self.num_species)]
         self.scheme = int(scheme)
         self.p, self.q, self.C, self.alpha_tau = int(p), int(q), float(C), float(alpha_tau)
 
     def c(self):
         g = (ctypes.c_double * 8)(*(self.species_gamma + [0.0] * (8 - self.num_species)))
-        return _Cfg(self.model, self.dim, self.num_species, self.scheme, g, self.p, self.q,
+        r = (ctypes.c_double * 8)(*(self.species_R + [0.0] * (8 - self.num_species)))
+        return _Cfg(self.model, self.dim, self.num_species, self.scheme, g, r, self.p, self.q,
                     self.C, self.alpha_tau)
 
     @property

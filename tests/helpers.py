@@ -31,6 +31,11 @@ def smooth_state(model, dim, n, seed=0, amp=0.3, species_gamma=None):
     if model == O.MODEL_SINGLE_SPECIES:
         rho = 1.0 + amp * wave(3) / dim
         return np.ascontiguousarray(P.single_species_state(rho, vel, p, (species_gamma or [1.4])[0]))
+    if model == O.MODEL_FOUR_EQN_CONSERVATIVE:
+        Y1 = 0.5 + 0.4 * np.tanh(2.0 * wave(5))
+        rho = 1.0 + amp * wave(3) / dim
+        return np.ascontiguousarray(P.four_eqn_state([rho * Y1, rho * (1.0 - Y1)], vel, p,
+                                                     species_gamma or P.FOUR_EQN_GAMMA, P.FOUR_EQN_R))
     Z1 = 0.5 + 0.4 * np.tanh(2.0 * wave(5))
     return np.ascontiguousarray(P.five_eqn_state(Z1, 1.0 + 0.2 * wave(9), 3.0, vel, p,
                                                  tuple(species_gamma or [1.4, 1.67])))
@@ -53,6 +58,11 @@ def shock_state(model, dim, n, seed=0, species_gamma=None):
     if model == O.MODEL_SINGLE_SPECIES:
         rho = np.where(left, 2.5, 1.0)
         return np.ascontiguousarray(P.single_species_state(rho, vel, p, (species_gamma or [1.4])[0]))
+    if model == O.MODEL_FOUR_EQN_CONSERVATIVE:
+        Y1 = np.clip(np.where(X[0] < 0.6, 1.0 - 1e-6, 1e-6), 1e-8, 1 - 1e-8)
+        rho = np.where(left, 2.0, 1.0) * (1.0 + 0.5 * (X[0] >= 0.6))
+        return np.ascontiguousarray(P.four_eqn_state([rho * Y1, rho * (1.0 - Y1)], vel, p,
+                                                     species_gamma or P.FOUR_EQN_GAMMA, P.FOUR_EQN_R))
     Z1 = np.clip(np.where(X[0] < 0.6, 1.0 - 1e-6, 1e-6), 1e-8, 1 - 1e-8)
     return np.ascontiguousarray(P.five_eqn_state(Z1, np.where(left, 2.0, 1.0), 3.0, vel, p,
                                                  tuple(species_gamma or [1.4, 1.67])))

@@ -7,6 +7,7 @@ max(|reference|, component scale) -- the benchmark spec's tolerance.
 import numpy as np
 import pytest
 
+from hamers_gb300 import problems as P
 from oracle import oracle as O
 from tests.helpers import n3, rel_err, shock_state, smooth_state
 
@@ -22,16 +23,30 @@ VARIANTS = [
     (O.MODEL_FIVE_EQN_ALLAIRE, 2, O.SCHEME_WCNS6_LD, (33, 27), [1.4, 1.67]),
     (O.MODEL_FIVE_EQN_ALLAIRE, 3, O.SCHEME_WCNS5_JS, (12, 10, 9), [1.4, 1.09]),
     (O.MODEL_FIVE_EQN_ALLAIRE, 3, O.SCHEME_WCNS6_LD, (12, 10, 9), [1.4, 1.09]),
+    (O.MODEL_FOUR_EQN_CONSERVATIVE, 2, O.SCHEME_WCNS5_JS, (31, 26), P.FOUR_EQN_GAMMA),
+    (O.MODEL_FOUR_EQN_CONSERVATIVE, 2, O.SCHEME_WCNS6_LD, (31, 26), P.FOUR_EQN_GAMMA),
+    (O.MODEL_FOUR_EQN_CONSERVATIVE, 3, O.SCHEME_WCNS5_JS, (11, 10, 9), P.FOUR_EQN_GAMMA),
+    (O.MODEL_FOUR_EQN_CONSERVATIVE, 3, O.SCHEME_WCNS6_LD, (11, 10, 9), P.FOUR_EQN_GAMMA),
 ]
-IDS = ["%s-%dd-%s" % ("single" if m == 0 else "five", d, "js" if s == 0 else "ld") for m, d, s, _, _ in VARIANTS]
+MODEL_IDS = {O.MODEL_SINGLE_SPECIES: "single", O.MODEL_FOUR_EQN_CONSERVATIVE: "four", O.MODEL_FIVE_EQN_ALLAIRE: "five"}
+IDS = ["%s-%dd-%s" % (MODEL_IDS[m], d, "js" if s == 0 else "ld") for m, d, s, _, _ in VARIANTS]
 
-NAMES = {O.MODEL_SINGLE_SPECIES: "SINGLE_SPECIES", O.MODEL_FIVE_EQN_ALLAIRE: "FIVE_EQN_ALLAIRE"}
+NAMES = {O.MODEL_SINGLE_SPECIES: "SINGLE_SPECIES", O.MODEL_FOUR_EQN_CONSERVATIVE: "FOUR_EQN_CONSERVATIVE",
+         O.MODEL_FIVE_EQN_ALLAIRE: "FIVE_EQN_ALLAIRE"}
 SCHEMES = {O.SCHEME_WCNS5_JS: "WCNS5_JS_HLLC_HLL", O.SCHEME_WCNS6_LD: "WCNS6_LD_HLLC_HLL"}
+
+
+def species_R(model):
+    return P.FOUR_EQN_R if model == O.MODEL_FOUR_EQN_CONSERVATIVE else None
+
+
+def ocfg(model, dim, gam, scheme):
+    return O.Config(model, dim, gam, scheme, species_R=species_R(model))
 
 
 def make(model, dim, scheme, gam, precision):
     from hamers_gb300 import flow
-    fm = flow.FlowModel(NAMES[model], dim, gam)
+    fm = flow.FlowModel(NAMES[model], dim, gam, species_R=species_R(model))
     return flow.ConvectiveFluxReconstructor(SCHEMES[scheme], fm, precision=precision)
 
 
@@ -56,7 +71,7 @@ def states(model, dim, n, gam):
 @pytest.mark.parametrize("variant", VARIANTS, ids=IDS)
 def test_flux_source_exact_is_bitwise(cuda, variant):
     model, dim, scheme, n, gam = variant
-    cfg = O.Config(model, dim, gam, scheme)
+    cfg = ocfg(model, dim, gam, scheme)
     rec = make(model, dim, scheme, gam, "exact")
     dx = [1.0 / v for v in n]
     dt = 1.3e-3
@@ -74,7 +89,7 @@ def test_flux_source_exact_is_bitwise(cuda, variant):
 @pytest.mark.parametrize("variant", VARIANTS, ids=IDS)
 def test_flux_source_fast_within_tolerance(cuda, variant):
     model, dim, scheme, n, gam = variant
-    cfg = O.Config(model, dim, gam, scheme)
+    cfg = ocfg(model, dim, gam, scheme)
     rec = make(model, dim, scheme, gam, "fast")
     dx = [1.0 / v for v in n]
     dt = 1.3e-3
@@ -110,7 +125,7 @@ def test_rk3_steps(cuda, variant, precision):
     import torch
     from hamers_gb300 import flow
     model, dim, scheme, n, gam = variant
-    cfg = O.Config(model, dim, gam, scheme)
+    cfg = ocfg(model, dim, gam, scheme)
     rec = make(model, dim, scheme, gam, precision)
     dx = [1.0 / v for v in n]
     dt = 2.0e-3
@@ -131,13 +146,13 @@ def test_rk3_steps(cuda, variant, precision):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("variant", VARIANTS[:1] + VARIANTS[4:5] + VARIANTS[6:7], ids=[IDS[0], IDS[4], IDS[6]])
+@pytest.mark.parametrize("variant", [VARIANTS[i] for i in (0, 4, 6, 10)], ids=[IDS[i] for i in (0, 4, 6, 10)])
 def test_rk_stage_general(cuda, variant):
     """advanceSingleStepOnPatch with all three coefficient sets and flux/source accumulation."""
     import torch
     from hamers_gb300 import flow
     model, dim, scheme, n, gam = variant
-    cfg = O.Config(model, dim, gam, scheme)
+    cfg = ocfg(model, dim, gam, scheme)
     rec = make(model, dim, scheme, gam, "exact")
     eu = flow.Euler(rec)
     dx = [1.0 / v for v in n]

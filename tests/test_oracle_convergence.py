@@ -22,17 +22,19 @@ def l2_errors(model, dim, scheme, levels):
     errs = []
     for N in levels:
         Q, dx, dt, nsteps, exact, gam = P.convergence_problem(model, dim, N)
-        cfg = O.Config(model, dim, gam, scheme)
+        cfg = O.Config(model, dim, gam, scheme,
+                       species_R=P.FOUR_EQN_R if model == O.MODEL_FOUR_EQN_CONSERVATIVE else None)
         O.fill_ghosts(cfg, [N] * dim, [1] * dim, Q)
         O.rk3_advance(cfg, [N] * dim, dx, dt, [1] * dim, nsteps, Q)
         Qi = P.interior(Q, dim)
-        field = Qi[0] if model == O.MODEL_SINGLE_SPECIES else Qi[-2]
+        field = {O.MODEL_SINGLE_SPECIES: Qi[0], O.MODEL_FOUR_EQN_CONSERVATIVE: Qi[0]}.get(model, Qi[-2])
         e = np.abs(exact(nsteps * dt) - field)
         errs.append(math.sqrt((e ** 2).mean()))
     return errs
 
 
-@pytest.mark.parametrize("model", [O.MODEL_SINGLE_SPECIES, O.MODEL_FIVE_EQN_ALLAIRE], ids=["single", "five"])
+@pytest.mark.parametrize("model", [O.MODEL_SINGLE_SPECIES, O.MODEL_FOUR_EQN_CONSERVATIVE, O.MODEL_FIVE_EQN_ALLAIRE],
+                         ids=["single", "four", "five"])
 @pytest.mark.parametrize("scheme", [O.SCHEME_WCNS5_JS, O.SCHEME_WCNS6_LD], ids=["js", "ld"])
 def test_convergence_2d(model, scheme):
     errs = l2_errors(model, 2, scheme, [8, 16, 32, 64])
@@ -40,7 +42,8 @@ def test_convergence_2d(model, scheme):
     assert rate > EXPECTED[scheme], (errs, rate)
 
 
-@pytest.mark.parametrize("model", [O.MODEL_SINGLE_SPECIES, O.MODEL_FIVE_EQN_ALLAIRE], ids=["single", "five"])
+@pytest.mark.parametrize("model", [O.MODEL_SINGLE_SPECIES, O.MODEL_FOUR_EQN_CONSERVATIVE, O.MODEL_FIVE_EQN_ALLAIRE],
+                         ids=["single", "four", "five"])
 def test_convergence_3d_js(model):
     errs = l2_errors(model, 3, O.SCHEME_WCNS5_JS, [8, 16, 32])
     rate = math.log2(errs[-2] / errs[-1])
