@@ -36,7 +36,7 @@ EXPORTS = [
     "hmr_rk_stage_patch", "hmr_rk_substep_patch", "hmr_fill_ghosts_patch", "hmr_level_create",
     "hmr_level_destroy", "hmr_level_bind_state", "hmr_level_set_periodic", "hmr_level_state",
     "hmr_level_substep", "hmr_level_step", "hmr_level_check", "hmr_level_barrier_diagnostic", "hmr_level_autotune",
-    "hmr_rk_substep_patch_noalloc",
+    "hmr_rk_substep_patch_noalloc", "hmr_rk_substep_vjp_patch", "hmr_fill_ghosts_vjp_patch",
 ]
 
 
@@ -119,6 +119,9 @@ def load():
     L.hmr_level_autotune.argtypes = [vp, ctypes.c_double, ip, ip, vp]
     L.hmr_rk_substep_patch_noalloc.argtypes = [cfgp, gp, ctypes.c_int, dp, ctypes.c_double, DPPP,
                                                ctypes.c_double, DPP, vp]
+    L.hmr_rk_substep_vjp_patch.argtypes = [vp, gp, ctypes.c_int, dp, ctypes.c_double, DPPP, ctypes.c_double,
+                                           DPP, DPPP, vp]
+    L.hmr_fill_ghosts_vjp_patch.argtypes = [vp, gp, DPP, ip, vp]
     for name in EXPORTS:
         getattr(L, name).restype = ctypes.c_int
     _lib = L

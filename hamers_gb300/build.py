@@ -27,6 +27,9 @@ UNITS = [
     ("hmr_faces.cu", "hmr_faces_%s_m%d.o" % (form, model),
      ["-DHMR_FAST=%d" % fast, "--fmad=%s" % ("true" if fast else "false"), "-DHMR_MODEL=%d" % model])
     for form, fast in (("exact", 0), ("fast", 1)) for model in (0, 1, 2)
+] + [
+    ("hmr_vjp.cu", "hmr_vjp_m%d.o" % model, ["-DHMR_FAST=0", "--fmad=false", "-DHMR_MODEL=%d" % model])
+    for model in (0, 1, 2)
 ]
 
 

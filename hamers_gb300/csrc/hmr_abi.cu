@@ -22,6 +22,8 @@ struct hmr_ctx {
     size_t scratch_bytes = 0;
     Counters* counters = nullptr;
     unsigned int* redo_count = nullptr;
+    double* vjp = nullptr;             // face contributions of the substep adjoint
+    size_t vjp_bytes = 0;
 };
 
 struct hmr_level {
@@ -238,6 +240,7 @@ int hmr_ctx_destroy(hmr_ctx* c) {
     if (c->scratch) cudaFree(c->scratch);
     if (c->counters) cudaFree(c->counters);
     if (c->redo_count) cudaFree(c->redo_count);
+    if (c->vjp) cudaFree(c->vjp);
     delete c;
     return HMR_OK;
 }
@@ -347,6 +350,60 @@ int hmr_rk_stage_patch(hmr_ctx* c, const hmr_patch_geometry* pg, int ncoef, cons
     const Geom g = make_geom(c->v.dim, pg);
     return hmr_cells::launch_rk_stage(c->v, g, ncoef, alpha, beta, acc ? gamma : nullptr, Qi, Fi, Si, Qo, Fa, Sa,
                                       as_stream(stream));
+}
+
+int hmr_rk_substep_vjp_patch(hmr_ctx* c, const hmr_patch_geometry* pg, int stage, const double* alpha,
+                             double beta, const double* const* const* Q_int, double dt,
+                             const double* const* Qbar_out, double* const* const* Qbar_int, void* stream) {
+    if (!c || !valid_geom(c->v.dim, pg) || !alpha || !Q_int || !Qbar_out || !Qbar_int || stage < 0 || stage > 2)
+        return HMR_ERR_ARGUMENT;
+    VjpArgs A;
+    std::memset(&A, 0, sizeof(A));
+    if (!load_comp(A.Qs, Q_int[stage], c->ncomp)) return HMR_ERR_ARGUMENT;
+    if (!load_comp(A.Qbo, Qbar_out, c->ncomp)) return HMR_ERR_ARGUMENT;
+    for (int s = 0; s <= stage; s++)
+        if (!load_comp(A.Qbi[s], Qbar_int[s], c->ncomp)) return HMR_ERR_ARGUMENT;
+    for (int s = 0; s <= stage; s++) A.alpha[s] = alpha[s];
+    A.nst = stage + 1;
+    A.beta = beta;
+    A.dt = dt;
+    const Geom g = make_geom(c->v.dim, pg);
+    cudaStream_t st = as_stream(stream);
+    int r = ensure_scratch(c, g);
+    if (r) return r;
+    const Scratch S = carve_scratch(c, g, c->scratch);
+    size_t need = 0;
+    for (int a = 0; a < c->v.dim; a++) need += (size_t)(6 * c->neq + 2) * nface_of(g, a);
+    need *= sizeof(double);
+    if (need > c->vjp_bytes) {
+        if (c->vjp) cudaFree(c->vjp);
+        c->vjp = nullptr;
+        c->vjp_bytes = 0;
+        cudaError_t e = cudaMalloc(&c->vjp, need);
+        if (e != cudaSuccess) return cuda_status(e);
+        c->vjp_bytes = need;
+    }
+    double* p = c->vjp;
+    for (int a = 0; a < 3; a++) {
+        A.Cb[a] = a < c->v.dim ? p : nullptr;
+        if (a < c->v.dim) p += (size_t)(6 * c->neq + 2) * nface_of(g, a);
+    }
+    if (beta != 0.0) {
+        r = hmr_cells::launch_cells(c->v, c->P, g, A.Qs, S, st);
+        if (r) return r;
+        r = hmr_cells::launch_sensor(c->v, g, S, st);
+        if (r) return r;
+    }
+    return hmr_vjp::launch_vjp(c->v, c->P, g, S, A, st);
+}
+
+int hmr_fill_ghosts_vjp_patch(hmr_ctx* c, const hmr_patch_geometry* pg, double* const* Qbar, const int* periodic,
+                              void* stream) {
+    if (!c || !valid_geom(c->v.dim, pg)) return HMR_ERR_ARGUMENT;
+    Comp q;
+    if (!load_comp(q, Qbar, c->ncomp)) return HMR_ERR_ARGUMENT;
+    const Geom g = make_geom(c->v.dim, pg);
+    return hmr_cells::launch_fill_vjp(c->v.dim, g, q, c->ncomp, periodic, as_stream(stream));
 }
 
 int hmr_fill_ghosts_patch(hmr_ctx* c, const hmr_patch_geometry* pg, double* const* Q, const int* periodic,

@@ -92,6 +92,72 @@ int launch_fill(int dim, const Geom& g, const Comp& Q, int ncomp, const int* per
     return (int)cudaPeekAtLastError();
 }
 
+// Adjoint of the single-patch ghost fill: every ghost cell's adjoint is added
+// to the interior cell it was copied from (a gather per interior cell over the
+// ghost cells of its preimage, so no two threads write one cell), then the
+// ghost adjoints are cleared.
+__device__ __forceinline__ int fill_src(int v, int n, int periodic) {
+    if (v >= 0 && v < n) return v;
+    if (periodic) return ((v % n) + n) % n;
+    return v < 0 ? 0 : n - 1;
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(THREADS) fill_vjp_gather_kernel(Geom g, Comp Qb, int ncomp, Periodic per) {
+    const long n = ninterior_of(g);
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+        const int c[3] = {(int)(t % g.n[0]), (int)((t / g.n[0]) % g.n[1]),
+                          DIM == 3 ? (int)(t / ((long)g.n[0] * g.n[1])) : 0};
+        // per axis: the coordinates (this one first) whose fill source is c[a]
+        int pre[3][9], np[3];
+        for (int a = 0; a < 3; a++) {
+            pre[a][0] = c[a];
+            np[a] = 1;
+            if (a >= DIM) continue;
+            for (int v = -GHOST; v < g.n[a] + GHOST; v++) {
+                if (v >= 0 && v < g.n[a]) continue;
+                if (fill_src(v, g.n[a], per.p[a]) == c[a] && np[a] < 9) pre[a][np[a]++] = v;
+            }
+        }
+        const long y = cidx<DIM>(g, c[0], c[1], c[2]);
+        for (int e = 0; e < ncomp; e++) {
+            double acc = 0.0;
+            for (int a2 = 0; a2 < np[2]; a2++)
+                for (int a1 = 0; a1 < np[1]; a1++)
+                    for (int a0 = 0; a0 < np[0]; a0++) {
+                        if (a0 == 0 && a1 == 0 && a2 == 0) continue;
+                        acc += Qb.p[e][cidx<DIM>(g, pre[0][a0], pre[1][a1], pre[2][a2])];
+                    }
+            if (acc != 0.0) Qb.p[e][y] += acc;
+        }
+    }
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(THREADS) fill_vjp_clear_kernel(Geom g, Comp Qb, int ncomp) {
+    const long n = ncell_of(g);
+    for (long x = (long)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(x % g.G[0]) - GHOST;
+        const int j = (int)((x / g.G[0]) % g.G[1]) - GHOST;
+        const int k = DIM == 3 ? (int)(x / ((long)g.G[0] * g.G[1])) - GHOST : 0;
+        if (i >= 0 && i < g.n[0] && j >= 0 && j < g.n[1] && k >= 0 && k < g.n[2]) continue;
+        for (int e = 0; e < ncomp; e++) Qb.p[e][x] = 0.0;
+    }
+}
+
+int launch_fill_vjp(int dim, const Geom& g, const Comp& Qb, int ncomp, const int* periodic, cudaStream_t st) {
+    Periodic per;
+    for (int a = 0; a < 3; a++) per.p[a] = periodic ? periodic[a] : 0;
+    if (dim == 2) {
+        fill_vjp_gather_kernel<2><<<grid_for(ninterior_of(g)), THREADS, 0, st>>>(g, Qb, ncomp, per);
+        fill_vjp_clear_kernel<2><<<grid_for(ncell_of(g)), THREADS, 0, st>>>(g, Qb, ncomp);
+    } else {
+        fill_vjp_gather_kernel<3><<<grid_for(ninterior_of(g)), THREADS, 0, st>>>(g, Qb, ncomp, per);
+        fill_vjp_clear_kernel<3><<<grid_for(ncell_of(g)), THREADS, 0, st>>>(g, Qb, ncomp);
+    }
+    return (int)cudaPeekAtLastError();
+}
+
 // ---------------------------------------------------------------------------
 // General stage combination (any number of coefficient sets), one thread per
 // interior cell and equation set:  Q = 0; for n: Q += alpha_n Q_n;

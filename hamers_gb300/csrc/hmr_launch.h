@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include "hmr_kernels.cuh"
+#include "hmr_vjp_items.cuh"
 
 namespace hmr {
 
@@ -67,6 +68,8 @@ int launch_cells(const hmr::Variant& v, const hmr::Params& P, const hmr::Geom& g
                  const hmr::Scratch& S, cudaStream_t st);
 int launch_sensor(const hmr::Variant& v, const hmr::Geom& g, const hmr::Scratch& S, cudaStream_t st);
 int launch_fill(int dim, const hmr::Geom& g, const hmr::Comp& Q, int ncomp, const int* periodic, cudaStream_t st);
+int launch_fill_vjp(int dim, const hmr::Geom& g, const hmr::Comp& Qb, int ncomp, const int* periodic,
+                    cudaStream_t st);
 int launch_rk_stage(const hmr::Variant& v, const hmr::Geom& g, int ncoef, const double* alpha,
                     const double* beta, const double* gamma, const hmr::Comp* Qint, const hmr::FluxComp* Fint,
                     const hmr::Comp* Sint, const hmr::Comp& Qout, const hmr::FluxComp& Facc, const hmr::Comp& Sacc,
@@ -124,3 +127,20 @@ HMR_DECLARE_FACE_LAUNCHERS(hmr_fast_m2)
 
 HMR_DEFINE_FACE_ROUTER(hmr_exact)
 HMR_DEFINE_FACE_ROUTER(hmr_fast)
+
+// Substep adjoint, one translation unit per flow model (hmr_vjp.cu).
+#define HMR_DECLARE_VJP_LAUNCHER(NS)                                                                           \
+    namespace NS {                                                                                             \
+    int launch_vjp(const hmr::Variant& v, const hmr::Params& P, const hmr::Geom& g, const hmr::Scratch& S,     \
+                   const hmr::VjpArgs& A, cudaStream_t st);                                                    \
+    }
+HMR_DECLARE_VJP_LAUNCHER(hmr_vjp_m0)
+HMR_DECLARE_VJP_LAUNCHER(hmr_vjp_m1)
+HMR_DECLARE_VJP_LAUNCHER(hmr_vjp_m2)
+
+namespace hmr_vjp {
+inline int launch_vjp(const hmr::Variant& v, const hmr::Params& P, const hmr::Geom& g, const hmr::Scratch& S,
+                      const hmr::VjpArgs& A, cudaStream_t st) {
+    HMR_ROUTE(hmr_vjp, launch_vjp, v, P, g, S, A, st)
+}
+}

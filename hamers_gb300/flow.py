@@ -230,28 +230,101 @@ class Euler:
             _stream_ptr(stream)))
 
 
+    def substepVJP(self, patch, stage, Q_int, dt, Qbar_out, Qbar_int, stream=None):
+        """Adjoint of substep(): accumulates into Qbar_int[n] (n <= stage, ghost boxes) the
+        vector-Jacobian product of Qbar_out with the substep at the stage states Q_int."""
+        rec = self.rec
+        g = patch.geometry()
+        alpha = (ctypes.c_double * 3)(*(RK3_ALPHA[stage] + [0.0] * (2 - stage)))
+        qi, k1 = L.ptr_array2([_comp_ptrs(t, rec.ncomp) for t in Q_int[:stage + 1]])
+        qb, k2 = L.ptr_array(_comp_ptrs(Qbar_out, rec.ncomp))
+        qbi, k3 = L.ptr_array2([_comp_ptrs(t, rec.ncomp) for t in Qbar_int[:stage + 1]])
+        L.check("hmr_rk_substep_vjp_patch", self._lib.hmr_rk_substep_vjp_patch(
+            rec.ctx, ctypes.byref(g), int(stage), alpha, RK3_BETA[stage][stage], qi, float(dt), qb, qbi,
+            _stream_ptr(stream)))
+
+    def fillGhostsVJP(self, patch, periodic, stream=None):
+        """Adjoint of fillGhosts() applied to the adjoint array patch.data."""
+        g = patch.geometry()
+        q, _k = L.ptr_array(_comp_ptrs(patch.data, self.rec.ncomp))
+        per = (ctypes.c_int * 3)(*(list(periodic) + [0] * (3 - len(periodic))))
+        L.check("hmr_fill_ghosts_vjp_patch", self._lib.hmr_fill_ghosts_vjp_patch(
+            self.rec.ctx, ctypes.byref(g), q, per, _stream_ptr(stream)))
+
+
 class RungeKuttaLevelIntegrator:
-    """SSPRK3 on one patch with ghost fill between stages (per-patch form)."""
+    """SSPRK3 on one patch with ghost fill between stages (per-patch form).
+
+    advance(..., checkpoint_every=K) records the state every K steps;
+    adjoint(Qbar) then runs the reverse sweep of that advance segment by
+    segment, recomputing each segment's stage states from its checkpoint."""
 
     def __init__(self, euler, patch, periodic):
         self.euler = euler
         self.patch = patch
         self.periodic = list(periodic)
         self.stages = [torch.empty_like(patch.data) for _ in range(2)]
+        self._record = None
         euler.rec.reserve(patch)
 
-    def advance(self, dt, nsteps=1, stream=None):
+    def _step(self, Q0, Q1, Q2, dt, stream):
+        p = self.patch
+        views = [Patch(p.n, p.dx, Q) for Q in (Q0, Q1, Q2)]
+        self.euler.fillGhosts(views[0], self.periodic, stream)
+        self.euler.substep(views[0], 0, [Q0], dt, Q1, stream)
+        self.euler.fillGhosts(views[1], self.periodic, stream)
+        self.euler.substep(views[1], 1, [Q0, Q1], dt, Q2, stream)
+        self.euler.fillGhosts(views[2], self.periodic, stream)
+        self.euler.substep(views[2], 2, [Q0, Q1, Q2], dt, Q0, stream)
+
+    def advance(self, dt, nsteps=1, stream=None, checkpoint_every=0):
         p = self.patch
         Q0, Q1, Q2 = p.data, self.stages[0], self.stages[1]
-        views = [Patch(p.n, p.dx, Q) for Q in (Q0, Q1, Q2)]
-        for _ in range(nsteps):
-            self.euler.fillGhosts(views[0], self.periodic, stream)
-            self.euler.substep(views[0], 0, [Q0], dt, Q1, stream)
-            self.euler.fillGhosts(views[1], self.periodic, stream)
-            self.euler.substep(views[1], 1, [Q0, Q1], dt, Q2, stream)
-            self.euler.fillGhosts(views[2], self.periodic, stream)
-            self.euler.substep(views[2], 2, [Q0, Q1, Q2], dt, Q0, stream)
-        self.euler.fillGhosts(views[0], self.periodic, stream)
+        if checkpoint_every:
+            self._record = {"dt": dt, "nsteps": nsteps, "every": int(checkpoint_every),
+                            "ckpt": {0: Q0.clone()}}
+        for step in range(nsteps):
+            self._step(Q0, Q1, Q2, dt, stream)
+            if checkpoint_every and (step + 1) % checkpoint_every == 0 and step + 1 < nsteps:
+                self._record["ckpt"][step + 1] = Q0.clone()
+        self.euler.fillGhosts(Patch(p.n, p.dx, Q0), self.periodic, stream)
+
+    def adjoint(self, Qbar, stream=None):
+        """Reverse sweep of the last recorded advance.  Qbar: adjoint of the final state
+        (ghost box); returns the adjoint of the initial state (ghost box, ghosts zero)."""
+        rec = self._record
+        if rec is None:
+            raise RuntimeError("adjoint() needs a preceding advance(..., checkpoint_every=K)")
+        p, eu, per, dt = self.patch, self.euler, self.periodic, rec["dt"]
+        Xb = Qbar.clone()
+        eu.fillGhostsVJP(Patch(p.n, p.dx, Xb), per, stream)          # final ghost fill
+        starts = sorted(rec["ckpt"])
+        ends = starts[1:] + [rec["nsteps"]]
+        for s0, s1 in reversed(list(zip(starts, ends))):
+            # recompute the segment, keeping every step's ghost-filled stage states
+            X = rec["ckpt"][s0].clone()
+            S1, S2 = torch.empty_like(X), torch.empty_like(X)
+            saved = []
+            for _ in range(s0, s1):
+                views = [Patch(p.n, p.dx, Q) for Q in (X, S1, S2)]
+                eu.fillGhosts(views[0], per, stream)
+                eu.substep(views[0], 0, [X], dt, S1, stream)
+                eu.fillGhosts(views[1], per, stream)
+                eu.substep(views[1], 1, [X, S1], dt, S2, stream)
+                eu.fillGhosts(views[2], per, stream)
+                saved.append((X.clone(), S1.clone(), S2.clone()))
+                eu.substep(views[2], 2, [X, S1, S2], dt, X, stream)
+            for X0, X1, X2 in reversed(saved):
+                view = Patch(p.n, p.dx, X0)
+                Xn, B1, B2 = torch.zeros_like(Xb), torch.zeros_like(Xb), torch.zeros_like(Xb)
+                eu.substepVJP(view, 2, [X0, X1, X2], dt, Xb, [Xn, B1, B2], stream)
+                eu.fillGhostsVJP(Patch(p.n, p.dx, B2), per, stream)
+                eu.substepVJP(view, 1, [X0, X1], dt, B2, [Xn, B1], stream)
+                eu.fillGhostsVJP(Patch(p.n, p.dx, B1), per, stream)
+                eu.substepVJP(view, 0, [X0], dt, B1, [Xn], stream)
+                eu.fillGhostsVJP(Patch(p.n, p.dx, Xn), per, stream)
+                Xb = Xn
+        return Xb
 
 
 class BatchedLevel:

@@ -149,6 +149,27 @@ int hmr_rk_substep_patch(hmr_ctx* ctx, const hmr_patch_geometry* geom, int stage
 int hmr_fill_ghosts_patch(hmr_ctx* ctx, const hmr_patch_geometry* geom, double* const* Q,
                           const int* periodic, void* stream);
 
+/* Adjoint (vector-Jacobian product) of hmr_rk_substep_patch.  No counterpart in the reference,
+ * which has no derivative code.  For the adjoint Qbar_out of the substep's output (ghost-box
+ * arrays; interior read) it accumulates into Qbar_int[n] (n = 0..stage, ghost boxes, caller
+ * zeroes them) the product of Qbar_out with the Jacobian of the output with respect to Q_int[n]:
+ * alpha[n] Qbar_out on the interior, plus, for n = stage, beta times the transposed Jacobian of
+ * the flux divergence and source, which also reaches the ghost cells of Qbar_int[stage] (fold it
+ * into the interior with hmr_fill_ghosts_vjp_patch when the ghosts were filled from it).
+ * The forward values are recomputed in the reference's operation order, so every discrete choice
+ * (bounds fallback, shock sensor, HLLC side, WCNS6-LD switch, min/max) is the forward substep's;
+ * derivatives follow that branch (|x|, min, max and sqrt(0) take the one-sided conventions of the
+ * oracle's tangent).  Same arguments as hmr_rk_substep_patch otherwise; uses the context's
+ * scratch plus (6 neq + 2) doubles per midpoint face of its own. */
+int hmr_rk_substep_vjp_patch(hmr_ctx* ctx, const hmr_patch_geometry* geom, int stage, const double* alpha,
+                             double beta, const double* const* const* Q_int, double dt,
+                             const double* const* Qbar_out, double* const* const* Qbar_int, void* stream);
+
+/* Adjoint of hmr_fill_ghosts_patch: adds the adjoint of every ghost cell to the interior cell it is
+ * copied from and zeroes the ghost adjoints.  No counterpart in the reference. */
+int hmr_fill_ghosts_vjp_patch(hmr_ctx* ctx, const hmr_patch_geometry* geom, double* const* Qbar,
+                              const int* periodic, void* stream);
+
 /* Batched form: every patch of a level advanced by one persistent kernel per RK substep over a
  * device-resident worklist (replaces the patch loop of RungeKuttaLevelIntegrator.cpp:1717-1743).
  * The caller owns each patch's state (slot 0, bound with hmr_level_bind_state); the level owns

@@ -17,6 +17,7 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "libhmr_oracle.so")
+_TAN_PATH = os.path.join(_HERE, "_build", "libhmr_tangent.so")
 
 MODEL_SINGLE_SPECIES = 0
 MODEL_FOUR_EQN_CONSERVATIVE = 1
@@ -61,6 +62,23 @@ def lib():
         L.hmro_num_comp.argtypes = [cp]
         _lib = L
     return _lib
+
+
+_tan = None
+
+
+def tangent_lib():
+    global _tan
+    if _tan is None:
+        if not os.path.exists(_TAN_PATH):
+            build()
+        L = ctypes.CDLL(_TAN_PATH)
+        dp = ctypes.POINTER(ctypes.c_double)
+        ip = ctypes.POINTER(ctypes.c_int)
+        L.hmro_tangent_substep.argtypes = [ctypes.POINTER(_Cfg), ip, dp, ctypes.c_double, ctypes.c_int, dp,
+                                           ctypes.c_double, dp, dp, dp, dp]
+        _tan = L
+    return _tan
 
 
 class Config:
@@ -194,3 +212,20 @@ def stage_threads(cfg, n, dx, dt, Q, nthreads):
     return lib().hmro_stage_threads(ctypes.byref(cfg.c()), _ip(_n3(n)),
                                     _dv(list(dx) + [1.0] * (3 - len(dx))), float(dt), _dp(Q),
                                     int(nthreads))
+
+
+def tangent_substep(cfg, n, dx, dt, stage, alpha, beta, Q_int, dQ_int):
+    """Fused substep (hmr_rk_substep_patch's forward) and its tangent along dQ_int.
+
+    Q_int, dQ_int: lists of stage+1 ghost-box states; returns (Q_out, dQ_out)
+    over the ghost box (interior written, ghosts zero)."""
+    shape = ghost_shape(cfg, n)
+    Qi = np.ascontiguousarray(np.stack([np.asarray(q, dtype=np.float64) for q in Q_int[:stage + 1]]))
+    dQi = np.ascontiguousarray(np.stack([np.asarray(q, dtype=np.float64) for q in dQ_int[:stage + 1]]))
+    assert Qi.shape[1:] == shape and dQi.shape == Qi.shape
+    Qo = np.zeros(shape)
+    dQo = np.zeros(shape)
+    tangent_lib().hmro_tangent_substep(ctypes.byref(cfg.c()), _ip(_n3(n)), _dv(list(dx) + [1.0] * (3 - len(dx))),
+                                       float(dt), int(stage), _dv(list(alpha)[:stage + 1]), float(beta),
+                                       _dp(Qi), _dp(dQi), _dp(Qo), _dp(dQo))
+    return Qo, dQo

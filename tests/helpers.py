@@ -78,3 +78,50 @@ def rel_err(a, b):
         den = np.maximum(np.abs(b[e]), scale)
         worst = max(worst, float((np.abs(a[e] - b[e]) / den).max()))
     return worst
+
+
+def noisy_shock_state(model, dim, n, seed=0, species_gamma=None, rel=1e-3):
+    """shock_state with seeded relative noise on every conserved component.
+
+    Piecewise-constant stencils leave the WCNS smoothness indicators at the
+    rounding level of their expanded quadratic forms (~1e-16 |U|^2, the scale
+    of HAMERS_EPSILON = 1e-15), where the reference's weights -- and any
+    derivative of them -- are ill-conditioned; the noise keeps every stencil
+    resolved for the derivative checks."""
+    Q = shock_state(model, dim, n, seed=seed, species_gamma=species_gamma)
+    rng = np.random.default_rng(seed + 1000)
+    return np.ascontiguousarray(Q * (1.0 + rel * rng.standard_normal(Q.shape)))
+
+
+def vortex_state(model, dim, n, seed=0, species_gamma=None):
+    """Smooth periodic state with a Taylor-Green velocity field for the finite-difference checks.
+
+    Each velocity component is scaled by 1/(n sin(2 pi/n)) of its own axis, so that
+    the 2nd-order central dilatation of the shock sensor vanishes to rounding, and
+    with even n on every axis no cell centre lies on a zero line of the vorticity:
+    the sensor never selects HLLC-HLL (whose blending weights depend on the direction
+    of the near-zero velocity jump across a face and have derivatives of order
+    1/|jump|), and no stencil is constant (where the WCNS smoothness indicators are
+    rounding noise of the size of HAMERS_EPSILON)."""
+    rng = np.random.default_rng(seed)
+    nn = n3(n)
+    assert all(nn[d] % 2 == 0 for d in range(dim)), "vortex_state needs even sizes"
+    G = [nn[d] + 2 * GHOST if d < dim else 1 for d in range(3)]
+    axes = [2 * math.pi * (np.arange(G[d]) - GHOST + 0.5) / max(1, nn[d]) for d in range(3)]
+    z, y, x = np.meshgrid(axes[2], axes[1], axes[0], indexing="ij")
+    ph = rng.uniform(0, 2 * math.pi, 3)
+    cz = np.cos(z) if dim == 3 else 1.0
+    sx = 1.0 / (nn[0] * math.sin(2 * math.pi / nn[0]))
+    sy = 1.0 / (nn[1] * math.sin(2 * math.pi / nn[1]))
+    vel = [2.0 * sx * np.sin(x) * np.cos(y) * cz, -2.0 * sy * np.cos(x) * np.sin(y) * cz]
+    if dim == 3:
+        vel.append(0.0 * x)
+    p = 1.0 + 0.1 * np.cos(2 * x + ph[0]) * np.cos(y + ph[1])
+    rho = 1.0 + 0.2 * np.sin(x + y + ph[2])
+    if model == O.MODEL_SINGLE_SPECIES:
+        return np.ascontiguousarray(P.single_species_state(rho, vel, p, (species_gamma or [1.4])[0]))
+    Y1 = 0.5 + 0.3 * np.sin(x + ph[2]) * np.cos(y)
+    if model == O.MODEL_FOUR_EQN_CONSERVATIVE:
+        return np.ascontiguousarray(P.four_eqn_state([rho * Y1, rho * (1.0 - Y1)], vel, p,
+                                                     species_gamma or P.FOUR_EQN_GAMMA, P.FOUR_EQN_R))
+    return np.ascontiguousarray(P.five_eqn_state(Y1, rho, 3.0, vel, p, tuple(species_gamma or [1.4, 1.67])))
