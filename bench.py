@@ -60,6 +60,7 @@ def parse():
     ap.add_argument("--no-uneven", action="store_true",
                     help="skip the batched-vs-per-patch measurement on uneven 3D patches")
     ap.add_argument("--no-peak", action="store_true", help="skip the FP64 peak microbenchmark")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint/forward cost measurement")
     ap.add_argument("--uneven-patches", type=int, default=512)
     return ap.parse_args()
 
@@ -210,6 +211,70 @@ def uneven_batched_vs_patch(args, flow):
             "batched_over_per_patch": t_patch / t_batched,
             "batched_ms_per_step": t_batched, "per_patch_ms_per_step": t_patch,
             "launch_shape": {"threads": tuned[0], "blocks_per_sm": tuned[1]}}
+
+
+def adjoint_cost(args, flow, Qnp, n, dx, dt, reps=3):
+    """Cost of the hand-written adjoint against the forward on the same workload.
+
+    One SSPRK3 step of the patch (zero-gradient x, periodic y): forward = ghost
+    fill + fused substep for the three stages (per-patch form); adjoint = the
+    three substep VJPs plus the three ghost-fill VJPs of the same step, given its
+    stage states.  Both device-timed with CUDA events, mean of `reps` steps."""
+    import torch
+    fm = flow.FlowModel("FIVE_EQN_ALLAIRE", 2, [1.4, 1.67])
+    per = [0, 1]
+    out = {}
+    Q0 = torch.from_numpy(Qnp).cuda()
+    stream = torch.cuda.current_stream()
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    for prec in ("fast", "exact"):
+        rec = flow.ConvectiveFluxReconstructor("WCNS6_LD_HLLC_HLL", fm, precision=prec)
+        drv = PatchDriver(flow, rec, n, dx, Q0.clone(), per)
+        drv.step(dt)
+        torch.cuda.synchronize()
+        e[0].record(stream)
+        for _ in range(reps):
+            drv.step(dt)
+        e[1].record(stream)
+        torch.cuda.synchronize()
+        out["forward_%s_ms_per_step" % prec] = e[0].elapsed_time(e[1]) / reps
+        if prec == "exact":
+            # stage states of one step, ghost-filled as the forward sees them
+            eu = drv.eu
+            X = Q0.clone()
+            S1, S2 = torch.empty_like(X), torch.empty_like(X)
+            views = [flow.Patch([n, n], dx, q) for q in (X, S1, S2)]
+            eu.fillGhosts(views[0], per)
+            eu.substep(views[0], 0, [X], dt, S1)
+            eu.fillGhosts(views[1], per)
+            eu.substep(views[1], 1, [X, S1], dt, S2)
+            eu.fillGhosts(views[2], per)
+            Xb = torch.randn_like(X)
+            bufs = [torch.zeros_like(X) for _ in range(3)]
+
+            def reverse():
+                for b in bufs:
+                    b.zero_()
+                eu.substepVJP(views[0], 2, [X, S1, S2], dt, Xb, bufs)
+                eu.fillGhostsVJP(flow.Patch([n, n], dx, bufs[2]), per)
+                eu.substepVJP(views[0], 1, [X, S1], dt, bufs[2], bufs[:2])
+                eu.fillGhostsVJP(flow.Patch([n, n], dx, bufs[1]), per)
+                eu.substepVJP(views[0], 0, [X], dt, bufs[1], bufs[:1])
+                eu.fillGhostsVJP(flow.Patch([n, n], dx, bufs[0]), per)
+
+            reverse()
+            torch.cuda.synchronize()
+            e[0].record(stream)
+            for _ in range(reps):
+                reverse()
+            e[1].record(stream)
+            torch.cuda.synchronize()
+            out["adjoint_ms_per_step"] = e[0].elapsed_time(e[1]) / reps
+        rec.close()
+    out["adjoint_over_forward_fast"] = out["adjoint_ms_per_step"] / out["forward_fast_ms_per_step"]
+    out["adjoint_over_forward_exact"] = out["adjoint_ms_per_step"] / out["forward_exact_ms_per_step"]
+    out["workload"] = f"{WORKLOAD}; one SSPRK3 step, per-patch form, adjoint with given stage states"
+    return out
 
 
 def cpu_baseline_oracle(Q, n, dx, dt, budget_s=15.0, threads=None):
@@ -432,6 +497,11 @@ def main():
         "host_wall_ms_per_step": t_host * 1e3 / args.steps,
     }
     with_clocks = None
+    if not args.no_adjoint:
+        try:
+            line["adjoint"] = adjoint_cost(args, flow, Qnp, n, dx, dt)
+        except Exception as exc:  # report, never lose the headline line
+            line["adjoint"] = {"error": str(exc)[:300]}
     if not args.no_uneven:
         try:
             line["batched_vs_per_patch"] = uneven_batched_vs_patch(args, flow)

@@ -28,7 +28,7 @@ UNITS = [
      ["-DHMR_FAST=%d" % fast, "--fmad=%s" % ("true" if fast else "false"), "-DHMR_MODEL=%d" % model])
     for form, fast in (("exact", 0), ("fast", 1)) for model in (0, 1, 2)
 ] + [
-    ("hmr_vjp.cu", "hmr_vjp_m%d.o" % model, ["-DHMR_FAST=0", "--fmad=false", "-DHMR_MODEL=%d" % model])
+    ("hmr_vjp.cu", "hmr_vjp_m%d.o" % model, ["-DHMR_FAST=0", "--fmad=true", "-DHMR_MODEL=%d" % model])
     for model in (0, 1, 2)
 ]
 

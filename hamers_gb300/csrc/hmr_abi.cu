@@ -372,8 +372,13 @@ int hmr_rk_substep_vjp_patch(hmr_ctx* c, const hmr_patch_geometry* pg, int stage
     int r = ensure_scratch(c, g);
     if (r) return r;
     const Scratch S = carve_scratch(c, g, c->scratch);
+    // per face: contributions (6 neq + 2), reconstructed-value adjoints (2 neq) and values
+    // (2 neq), smoothness indicators (9 neq), projection factors and their partial
+    // adjoints (9 + 4 nsp), bounds flag (1)
+    const size_t per_face = (size_t)(6 * c->neq + 2) + (size_t)(2 * c->neq) + (size_t)(2 * c->neq) +
+                            (size_t)(9 * c->neq) + (size_t)(9 + 4 * c->v.nsp) + 1;
     size_t need = 0;
-    for (int a = 0; a < c->v.dim; a++) need += (size_t)(6 * c->neq + 2) * nface_of(g, a);
+    for (int a = 0; a < c->v.dim; a++) need += per_face * nface_of(g, a);
     need *= sizeof(double);
     if (need > c->vjp_bytes) {
         if (c->vjp) cudaFree(c->vjp);
@@ -385,8 +390,16 @@ int hmr_rk_substep_vjp_patch(hmr_ctx* c, const hmr_patch_geometry* pg, int stage
     }
     double* p = c->vjp;
     for (int a = 0; a < 3; a++) {
-        A.Cb[a] = a < c->v.dim ? p : nullptr;
-        if (a < c->v.dim) p += (size_t)(6 * c->neq + 2) * nface_of(g, a);
+        A.Cb[a] = A.Wb[a] = A.Wv[a] = A.Kb[a] = A.Fp[a] = nullptr;
+        A.okf[a] = nullptr;
+        if (a >= c->v.dim) continue;
+        const long nf = nface_of(g, a);
+        A.Cb[a] = p; p += (size_t)(6 * c->neq + 2) * nf;
+        A.Wb[a] = p; p += (size_t)(2 * c->neq) * nf;
+        A.Wv[a] = p; p += (size_t)(2 * c->neq) * nf;
+        A.Kb[a] = p; p += (size_t)(9 * c->neq) * nf;
+        A.Fp[a] = p; p += (size_t)(9 + 4 * c->v.nsp) * nf;
+        A.okf[a] = reinterpret_cast<unsigned char*>(p); p += nf;   // one double per face reserved
     }
     if (beta != 0.0) {
         r = hmr_cells::launch_cells(c->v, c->P, g, A.Qs, S, st);

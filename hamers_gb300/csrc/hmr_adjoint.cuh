@@ -73,15 +73,15 @@ __device__ __forceinline__ void ld_beta3_bwd(const double* S, double bb3, double
 // WCNS5-JS, one side: S[0..4] from the upwind side, obar = adjoint of the
 // midpoint value; accumulates Sb[0..4].
 // ----------------------------------------------------------------------------
-__device__ __forceinline__ void js_side_bwd(int p, const double* S, double obar, double* Sb) {
-    double b0, b1, b2;
-    js_betas_x(S[0], S[1], S[2], S[3], S[4], b0, b1, b2);
-    const double e0 = b0 + HMR_EPS, e1 = b1 + HMR_EPS, e2 = b2 + HMR_EPS;
-    const double a0 = (double(1)/double(16))/ipow0(e0, p);
-    const double a1 = (double(5)/double(8))/ipow0(e1, p);
-    const double a2 = (double(5)/double(16))/ipow0(e2, p);
-    const double A = a0 + a1 + a2;
-    const double w0 = a0/A, w1 = a1/A, w2 = a2/A;
+__device__ __forceinline__ void js_side_bwd(int p, const double* S, double b0, double b1, double b2, double obar,
+                                            double* Sb) {
+    // alpha_k = d_k/(b_k + eps)^p, w_k = alpha_k/sum alpha (reciprocals: derivative values only)
+    const double r0 = double(1)/(b0 + HMR_EPS), r1 = double(1)/(b1 + HMR_EPS), r2 = double(1)/(b2 + HMR_EPS);
+    const double a0 = (double(1)/double(16))*ipow0(r0, p);
+    const double a1 = (double(5)/double(8))*ipow0(r1, p);
+    const double a2 = (double(5)/double(16))*ipow0(r2, p);
+    const double iA = double(1)/(a0 + a1 + a2);
+    const double w0 = a0*iA, w1 = a1*iA, w2 = a2*iA;
     const double q0 = 3.0/8.0*S[0] - 10.0/8.0*S[1] + 15.0/8.0*S[2];
     const double q1 = -1.0/8.0*S[1] + 6.0/8.0*S[2] + 3.0/8.0*S[3];
     const double q2 = 3.0/8.0*S[2] + 6.0/8.0*S[3] - 1.0/8.0*S[4];
@@ -90,22 +90,34 @@ __device__ __forceinline__ void js_side_bwd(int p, const double* S, double obar,
     Sb[2] += obar*(15.0/8.0*w0 + 6.0/8.0*w1 + 3.0/8.0*w2);
     Sb[3] += obar*(3.0/8.0*w1 + 6.0/8.0*w2);
     Sb[4] += obar*(-1.0/8.0*w2);
-    const double wb0 = obar*q0, wb1 = obar*q1, wb2 = obar*q2;
-    const double dot = wb0*w0 + wb1*w1 + wb2*w2;
-    const double ab0 = (wb0 - dot)/A, ab1 = (wb1 - dot)/A, ab2 = (wb2 - dot)/A;
-    const double bb0 = -ab0*p*a0/e0, bb1 = -ab1*p*a1/e1, bb2 = -ab2*p*a2/e2;
+    // d out/d b_k = sum_j q_j dw_j/db_k = -p r_k w_k (q_k - out)
+    const double out = w0*q0 + w1*q1 + w2*q2;
+    const double bb0 = -obar*p*r0*w0*(q0 - out);
+    const double bb1 = -obar*p*r1*w1*(q1 - out);
+    const double bb2 = -obar*p*r2*w2*(q2 - out);
     js_betas_bwd(S, bb0, bb1, bb2, Sb);
 }
 
-// Both sides of one characteristic variable: U[0..5] at cells face-3..face+2.
-__device__ __forceinline__ void js_pair_bwd(const double* U, int p, double Umb, double Upb, double* Ub) {
+// Forward of both sides (the operations of js_pair<true>) keeping the smoothness
+// indicators: b[0..2] of the minus side, b[3..5] of the plus side.
+__device__ __forceinline__ void js_pair_keep(const double* U, int p, double& Um, double& Up, double* b) {
+    js_betas_x(U[0], U[1], U[2], U[3], U[4], b[0], b[1], b[2]);
+    Um = js_interp<true>(b[0], b[1], b[2], p, U[0], U[1], U[2], U[3], U[4]);
+    js_betas_x(U[5], U[4], U[3], U[2], U[1], b[3], b[4], b[5]);
+    Up = js_interp<true>(b[3], b[4], b[5], p, U[5], U[4], U[3], U[2], U[1]);
+}
+
+// Both sides of one characteristic variable: U[0..5] at cells face-3..face+2,
+// b the indicators kept by js_pair_keep.
+__device__ __forceinline__ void js_pair_bwd(const double* U, const double* b, int p, double Umb, double Upb,
+                                            double* Ub) {
     double Sb[5] = {0, 0, 0, 0, 0};
-    js_side_bwd(p, U, Umb, Sb);
+    js_side_bwd(p, U, b[0], b[1], b[2], Umb, Sb);
 #pragma unroll
     for (int j = 0; j < 5; j++) Ub[j] += Sb[j];
     const double R[5] = {U[5], U[4], U[3], U[2], U[1]};
     double Rb[5] = {0, 0, 0, 0, 0};
-    js_side_bwd(p, R, Upb, Rb);
+    js_side_bwd(p, R, b[3], b[4], b[5], Upb, Rb);
 #pragma unroll
     for (int j = 0; j < 5; j++) Ub[5 - j] += Rb[j];
 }
@@ -138,40 +150,41 @@ __device__ __forceinline__ void ld_sigma_bwd(const double* U, double sigb, doubl
 }
 
 // One side: S[0..5] from the upwind side.  Accumulates Sb and the adjoint of sigma.
-__device__ __forceinline__ void ld_side_bwd(const Params& P, double sigma, const double* S, double obar,
-                                            double* Sb, double& sigb) {
-    double b[4];
-    js_betas_x(S[0], S[1], S[2], S[3], S[4], b[0], b[1], b[2]);
-    b[3] = ld_beta3(S[0], S[1], S[2], S[3], S[4], S[5]);
+__device__ __forceinline__ void ld_side_bwd(const Params& P, double sigma, const double* S, const double* b,
+                                            double obar, double* Sb, double& sigb) {
     // decision inputs, exactly as in ld_interp<true>
     const double tau_5 = fabs(sub_(b[0], b[2]));
     const double beta_avg = mul_(double(1)/double(8), add_(add_(b[0], b[2]), mul_(double(6), b[1])));
     const double tau_6 = fabs(sub_(b[3], beta_avg));
     const double R_tau = tau_6/add_(beta_avg, HMR_EPS);
     const bool blend = R_tau > P.alpha_tau;
+    // weights, with reciprocals (derivative values only)
     const double du[3] = {1.0/16.0, 5.0/8.0, 5.0/16.0};
     const double dc[4] = {1.0/32.0, 15.0/32.0, 15.0/32.0, 1.0/32.0};
-    double r[4], xu[3], xo[4], ur[3], orw[4];
+    double r[4], xu[3], xo[4], pu1[3], po1[4], ur[3], orw[4];
 #pragma unroll
     for (int k = 0; k < 4; k++) r[k] = double(1)/(b[k] + HMR_EPS);
     double Us = 0.0, Os = 0.0;
 #pragma unroll
     for (int k = 0; k < 3; k++) {
         xu[k] = tau_5*r[k];
-        ur[k] = du[k]*(1.0 + ipow0(xu[k], P.p));
+        pu1[k] = ipow0(xu[k], P.p - 1);
+        ur[k] = du[k]*(1.0 + pu1[k]*xu[k]);
         Us += ur[k];
     }
 #pragma unroll
     for (int k = 0; k < 4; k++) {
         xo[k] = tau_6*r[k];
-        orw[k] = dc[k]*(P.C + ipow0(xo[k], P.q));
+        po1[k] = ipow0(xo[k], P.q - 1);
+        orw[k] = dc[k]*(P.C + po1[k]*xo[k]);
         Os += orw[k];
     }
+    const double iUs = double(1)/Us, iOs = double(1)/Os;
     double u[3], o[4], of[4];
 #pragma unroll
-    for (int k = 0; k < 3; k++) u[k] = ur[k]/Us;
+    for (int k = 0; k < 3; k++) u[k] = ur[k]*iUs;
 #pragma unroll
-    for (int k = 0; k < 4; k++) o[k] = orw[k]/Os;
+    for (int k = 0; k < 4; k++) o[k] = orw[k]*iOs;
     if (blend) {
 #pragma unroll
         for (int k = 0; k < 3; k++) of[k] = sigma*u[k] + (1.0 - sigma)*o[k];
@@ -210,17 +223,17 @@ __device__ __forceinline__ void ld_side_bwd(const Params& P, double sigma, const
     const double doto = ob[0]*o[0] + ob[1]*o[1] + ob[2]*o[2] + ob[3]*o[3];
     double rb[4] = {0, 0, 0, 0}, bb[4];
     double tau5b = 0.0, tau6b = 0.0;
+    if (blend) {
 #pragma unroll
-    for (int k = 0; k < 3; k++) {
-        const double urb = (ub[k] - dotu)/Us;
-        const double xub = urb*du[k]*P.p*ipow0(xu[k], P.p - 1);
-        tau5b += xub*r[k];
-        rb[k] += xub*tau_5;
+        for (int k = 0; k < 3; k++) {
+            const double xub = (ub[k] - dotu)*iUs*du[k]*P.p*pu1[k];
+            tau5b += xub*r[k];
+            rb[k] += xub*tau_5;
+        }
     }
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-        const double orb = (ob[k] - doto)/Os;
-        const double xob = orb*dc[k]*P.q*ipow0(xo[k], P.q - 1);
+        const double xob = (ob[k] - doto)*iOs*dc[k]*P.q*po1[k];
         tau6b += xob*r[k];
         rb[k] += xob*tau_6;
     }
@@ -239,16 +252,30 @@ __device__ __forceinline__ void ld_side_bwd(const Params& P, double sigma, const
     ld_beta3_bwd(S, bb[3], Sb);
 }
 
-__device__ __forceinline__ void ld_pair_bwd(const double* U, const Params& P, double Umb, double Upb, double* Ub) {
+// Forward of both sides (the operations of ld_pair<true>) keeping the smoothness
+// indicators b[0..3] (minus side), b[4..7] (plus side) and sigma (b[8]).
+__device__ __forceinline__ void ld_pair_keep(const double* U, const Params& P, double& Um, double& Up, double* b) {
     const double sigma = ld_sigma(U);
+    js_betas_x(U[0], U[1], U[2], U[3], U[4], b[0], b[1], b[2]);
+    b[3] = ld_beta3(U[0], U[1], U[2], U[3], U[4], U[5]);
+    Um = ld_interp<true>(b, sigma, P, U[0], U[1], U[2], U[3], U[4], U[5]);
+    js_betas_x(U[5], U[4], U[3], U[2], U[1], b[4], b[5], b[6]);
+    b[7] = ld_beta3(U[5], U[4], U[3], U[2], U[1], U[0]);
+    Up = ld_interp<true>(b + 4, sigma, P, U[5], U[4], U[3], U[2], U[1], U[0]);
+    b[8] = sigma;
+}
+
+__device__ __forceinline__ void ld_pair_bwd(const double* U, const double* b, const Params& P, double Umb,
+                                            double Upb, double* Ub) {
+    const double sigma = b[8];
     double sigb = 0.0;
     double Sb[6] = {0, 0, 0, 0, 0, 0};
-    ld_side_bwd(P, sigma, U, Umb, Sb, sigb);
+    ld_side_bwd(P, sigma, U, b, Umb, Sb, sigb);
 #pragma unroll
     for (int j = 0; j < 6; j++) Ub[j] += Sb[j];
     const double R[6] = {U[5], U[4], U[3], U[2], U[1], U[0]};
     double Rb[6] = {0, 0, 0, 0, 0, 0};
-    ld_side_bwd(P, sigma, R, Upb, Rb, sigb);
+    ld_side_bwd(P, sigma, R, b + 4, Upb, Rb, sigb);
 #pragma unroll
     for (int j = 0; j < 6; j++) Ub[5 - j] += Rb[j];
     ld_sigma_bwd(U, sigb, Ub);
@@ -695,8 +722,12 @@ __device__ __forceinline__ double char_one(const FaceProj<DIM, MODEL, NSP>& F, c
         const double p = V[NSP + DIM];
         if (e == 0) return sub_(un, mul_(F.irc, p));
         if (e == M::NEQ - 1) return add_(un, mul_(F.irc, p));
-        if (e >= 1 && e <= NSP) return sub_(V[e - 1], mul_(F.zr[e - 1], p));
-        if (e >= NSP + DIM) return V[M::IZ + (e - NSP - DIM)];
+#pragma unroll
+        for (int s = 0; s < NSP; s++)
+            if (e == 1 + s) return sub_(V[s], mul_(F.zr[s], p));
+#pragma unroll
+        for (int s = 0; s < M::NZ; s++)
+            if (e == NSP + DIM + s) return V[M::IZ + s];
         int t = NSP + 1;
 #pragma unroll
         for (int k = 0; k < DIM; k++) {
@@ -730,13 +761,19 @@ __device__ __forceinline__ void char_one_bwd(const FaceProj<DIM, MODEL, NSP>& F,
         const double p = V[NSP + DIM];
         if (e == 0) { Vb[NSP + A] += Wb; Vb[NSP + DIM] -= F.irc*Wb; Fb.irc -= Wb*p; return; }
         if (e == M::NEQ - 1) { Vb[NSP + A] += Wb; Vb[NSP + DIM] += F.irc*Wb; Fb.irc += Wb*p; return; }
-        if (e >= 1 && e <= NSP) {
-            Vb[e - 1] += Wb;
-            Vb[NSP + DIM] -= F.zr[e - 1]*Wb;
-            Fb.zr[e - 1] -= Wb*p;
-            return;
+#pragma unroll
+        for (int s = 0; s < NSP; s++) {
+            if (e == 1 + s) {
+                Vb[s] += Wb;
+                Vb[NSP + DIM] -= F.zr[s]*Wb;
+                Fb.zr[s] -= Wb*p;
+                return;
+            }
         }
-        if (e >= NSP + DIM) { Vb[M::IZ + (e - NSP - DIM)] += Wb; return; }
+#pragma unroll
+        for (int s = 0; s < M::NZ; s++) {
+            if (e == NSP + DIM + s) { Vb[M::IZ + s] += Wb; return; }
+        }
         int t = NSP + 1;
 #pragma unroll
         for (int k = 0; k < DIM; k++) {

@@ -1,8 +1,10 @@
 // Kernels of the vector-Jacobian product of one fused RK substep of one patch
 // (the adjoint of hmr_rk_substep_patch; items in hmr_vjp_items.cuh), for one
 // flow model.  Built once per model (-DHMR_MODEL=0/1/2, namespace
-// hmr_vjp_m<model>), with --fmad=false so that the forward values recomputed
-// here are the reference's bits.
+// hmr_vjp_m<model>).  The forward values it recomputes are evaluated with
+// explicitly rounded operations (the X = true forms), so they are the
+// reference's bits -- and every branch the forward's -- while the reverse
+// arithmetic may be contracted into FMAs.
 #include <cuda_runtime.h>
 
 #include "hmr_launch.h"
@@ -39,12 +41,65 @@ static int dispatch(const Variant& v, F f) {
 
 constexpr int VJP_THREADS = 128;
 
-template <int DIM, int MODEL, int NSP, int SCHEME, int AX>
+static inline int grid_for(long items, int threads) {
+    long b = (items + threads - 1) / threads;
+    if (b < 1) b = 1;
+    if (b > (1L << 30)) b = 1L << 30;
+    return (int)b;
+}
+
+template <int DIM, int MODEL, int NSP, int AX>
 __global__ void __launch_bounds__(VJP_THREADS)
-face_bwd_kernel(Params P, Geom g, Scratch S, VjpArgs VA) {
+face_proj_kernel(Geom g, Scratch S, VjpArgs VA) {
     const long nf = nface_of(g, AX);
     for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < nf; t += (long)gridDim.x * blockDim.x)
-        face_bwd_item<DIM, MODEL, NSP, SCHEME, AX>(P, g, S, VA, t);
+        face_proj_item<DIM, MODEL, NSP, AX>(g, S, VA, t);
+}
+
+template <int DIM, int MODEL, int NSP, int SCHEME, int AX>
+__global__ void __launch_bounds__(VJP_THREADS)
+face_fwd_weno_kernel(Params P, Geom g, Scratch S, VjpArgs VA) {
+    const long n = nface_of(g, AX) * Model<DIM, MODEL, NSP>::NEQ;
+    for (long u = (long)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (long)gridDim.x * blockDim.x)
+        face_fwd_weno_item<DIM, MODEL, NSP, SCHEME, AX>(P, g, S, VA, u);
+}
+
+template <int DIM, int MODEL, int NSP, int SCHEME, int AX>
+__global__ void __launch_bounds__(VJP_THREADS)
+face_bwd_riemann_kernel(Params P, Geom g, Scratch S, VjpArgs VA) {
+    const long nf = nface_of(g, AX);
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < nf; t += (long)gridDim.x * blockDim.x)
+        face_bwd_riemann_item<DIM, MODEL, NSP, SCHEME, AX>(P, g, S, VA, t);
+}
+
+template <int DIM, int MODEL, int NSP, int SCHEME, int AX>
+__global__ void __launch_bounds__(VJP_THREADS)
+face_bwd_weno_kernel(Params P, Geom g, Scratch S, VjpArgs VA) {
+    const long n = nface_of(g, AX) * Model<DIM, MODEL, NSP>::NEQ;
+    for (long u = (long)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (long)gridDim.x * blockDim.x)
+        face_bwd_weno_item<DIM, MODEL, NSP, SCHEME, AX>(P, g, S, VA, u);
+}
+
+template <int DIM, int MODEL, int NSP, int AX>
+__global__ void __launch_bounds__(VJP_THREADS)
+face_bwd_char_kernel(Geom g, Scratch S, VjpArgs VA) {
+    const long nf = nface_of(g, AX);
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < nf; t += (long)gridDim.x * blockDim.x)
+        face_bwd_char_item<DIM, MODEL, NSP, AX>(g, S, VA, t);
+}
+
+template <class T, int AX>
+static void launch_face_axis(const Params& P, const Geom& g, const Scratch& S, const VjpArgs& A, cudaStream_t st) {
+    const long nf = nface_of(g, AX);
+    constexpr int NEQ = Model<T::DIM, T::MODEL, T::NSP>::NEQ;
+    face_proj_kernel<T::DIM, T::MODEL, T::NSP, AX><<<grid_for(nf, VJP_THREADS), VJP_THREADS, 0, st>>>(g, S, A);
+    face_fwd_weno_kernel<T::DIM, T::MODEL, T::NSP, T::SCHEME, AX>
+        <<<grid_for(nf * NEQ, VJP_THREADS), VJP_THREADS, 0, st>>>(P, g, S, A);
+    face_bwd_riemann_kernel<T::DIM, T::MODEL, T::NSP, T::SCHEME, AX>
+        <<<grid_for(nf, VJP_THREADS), VJP_THREADS, 0, st>>>(P, g, S, A);
+    face_bwd_weno_kernel<T::DIM, T::MODEL, T::NSP, T::SCHEME, AX>
+        <<<grid_for(nf * NEQ, VJP_THREADS), VJP_THREADS, 0, st>>>(P, g, S, A);
+    face_bwd_char_kernel<T::DIM, T::MODEL, T::NSP, AX><<<grid_for(nf, VJP_THREADS), VJP_THREADS, 0, st>>>(g, S, A);
 }
 
 template <int DIM, int MODEL, int NSP>
@@ -55,25 +110,14 @@ cell_bwd_kernel(Params P, Geom g, Scratch S, VjpArgs VA) {
         cell_bwd_item<DIM, MODEL, NSP>(P, g, S, VA, x);
 }
 
-static inline int grid_for(long items, int threads) {
-    long b = (items + threads - 1) / threads;
-    if (b < 1) b = 1;
-    if (b > (1L << 30)) b = 1L << 30;
-    return (int)b;
-}
-
 int launch_vjp(const Variant& v, const Params& P, const Geom& g, const Scratch& S, const VjpArgs& A,
                cudaStream_t st) {
     return dispatch(v, [&](auto t) {
         using T = decltype(t);
         if (A.beta != 0.0) {
-            face_bwd_kernel<T::DIM, T::MODEL, T::NSP, T::SCHEME, 0>
-                <<<grid_for(nface_of(g, 0), VJP_THREADS), VJP_THREADS, 0, st>>>(P, g, S, A);
-            face_bwd_kernel<T::DIM, T::MODEL, T::NSP, T::SCHEME, 1>
-                <<<grid_for(nface_of(g, 1), VJP_THREADS), VJP_THREADS, 0, st>>>(P, g, S, A);
-            if constexpr (T::DIM == 3)
-                face_bwd_kernel<T::DIM, T::MODEL, T::NSP, T::SCHEME, 2>
-                    <<<grid_for(nface_of(g, 2), VJP_THREADS), VJP_THREADS, 0, st>>>(P, g, S, A);
+            launch_face_axis<T, 0>(P, g, S, A, st);
+            launch_face_axis<T, 1>(P, g, S, A, st);
+            if constexpr (T::DIM == 3) launch_face_axis<T, 2>(P, g, S, A, st);
         }
         cell_bwd_kernel<T::DIM, T::MODEL, T::NSP>
             <<<grid_for(ncell_of(g), VJP_THREADS), VJP_THREADS, 0, st>>>(P, g, S, A);

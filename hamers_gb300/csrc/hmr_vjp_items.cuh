@@ -7,12 +7,12 @@
 // with the five-equation model's last volume fraction rewritten as 1 - sum.
 // For the adjoint Qb_out of Q_out, after the forward cell data and sensor of
 // Q_s are in the scratch:
-//   face_bwd_item (per axis, per midpoint face): adjoint of the midpoint flux
-//     and midpoint velocity from the flux formula and source; forward
-//     recompute of the face (projection, WCNS, inverse projection, bounds,
-//     Riemann solve) and its reverse, down to the primitive variables of the
-//     six stencil cells and the projection means, written per face and
-//     stencil offset (no atomics, deterministic);
+//   face items (per axis, per midpoint face; see the face phase below):
+//     adjoint of the midpoint flux and midpoint velocity from the flux formula
+//     and source; forward recompute of the face (projection, WCNS, inverse
+//     projection, bounds, Riemann solve) and its reverse, down to the
+//     primitive variables of the six stencil cells and the projection means,
+//     written per face and stencil offset (no atomics, deterministic);
 //   cell_bwd_item (per ghost-box cell): gathers those contributions, adds the
 //     node-flux and advective-source terms, reverses the cell data (primitive
 //     variables, density, sound speed) to the conserved variables and
@@ -33,6 +33,11 @@ struct VjpArgs {
     double beta;
     double dt;
     double* Cb[3];    // per axis: (6*NEQ + 2) x nface(a) face contributions
+    double* Wb[3];    // per axis: 2*NEQ x nface(a) adjoints of the reconstructed characteristic values
+    double* Wv[3];    // per axis: 2*NEQ x nface(a) reconstructed characteristic values (forward)
+    double* Kb[3];    // per axis: 9*NEQ x nface(a) forward smoothness indicators (and WCNS6-LD sigma)
+    double* Fp[3];    // per axis: FaceLayout<NSP>::NFP x nface(a) projection factors and partial adjoints
+    unsigned char* okf[3];   // per axis: nface(a) bounds flags
 };
 
 // Adjoint of the pre-rewrite stage output (component e < NEQ) at a cell:
@@ -85,137 +90,302 @@ __device__ __forceinline__ double usrc_bar(const Geom& g, const VjpArgs& A, int 
 }
 
 // ---------------------------------------------------------------------------
-// Face phase of the adjoint (axis AX).
+// Face phase of the adjoint (axis AX), in three items so that no kernel holds
+// the whole face in registers:
+//   face_bwd_riemann_item (per face): adjoints of the midpoint flux and velocity,
+//     forward recompute of the face up to the Riemann solve and its reverse, the
+//     inverse projection's reverse -> adjoints of the reconstructed
+//     characteristic values (Wb) and partial adjoints of the projection factors;
+//     first-order-fallback faces write their final contributions directly;
+//   face_bwd_weno_item (per face and characteristic variable): reverse of the
+//     WCNS interpolation -> adjoints of the six stencil values (into Cb);
+//   face_bwd_char_item (per face): reverse of the characteristic projection and
+//     of the projection means -> final per-face contributions (Cb).
+// Per-face buffers of axis AX, nf faces each (VjpArgs):
+//   Cb : (6*NEQ + 2) x nf   contributions to V of the six stencil cells, then rho, c
+//   Wb : 2*NEQ x nf         adjoints of the minus/plus reconstructed values
+//   Fp : NFP x nf           face projection factors, then their partial adjoints
+//   okf: nf                 bounds flag of the face (0: first-order fallback)
 // ---------------------------------------------------------------------------
+template <int NSP>
+struct FaceLayout {
+    static constexpr int F = 6 + 3 * NSP;          // rb, cb, m_hrc, p_hrc, ic2, irc, zb[], zr[], hz[]
+    static constexpr int NFP = F + 3 + NSP;         // + adjoints of p_hrc, ic2, irc, hz[]
+};
+
+template <int DIM, int MODEL, int NSP>
+__device__ __forceinline__ void store_proj(double* Fp, long nf, long t, const FaceProj<DIM, MODEL, NSP>& F) {
+    Fp[0 * nf + t] = F.rb; Fp[1 * nf + t] = F.cb; Fp[2 * nf + t] = F.m_hrc; Fp[3 * nf + t] = F.p_hrc;
+    Fp[4 * nf + t] = F.ic2; Fp[5 * nf + t] = F.irc;
+    if constexpr (MODEL == SINGLE_SPECIES) return;
+#pragma unroll
+    for (int q = 0; q < NSP; q++) {
+        Fp[(6 + q) * nf + t] = F.zb[q];
+        Fp[(6 + NSP + q) * nf + t] = F.zr[q];
+        Fp[(6 + 2 * NSP + q) * nf + t] = F.hz[q];
+    }
+}
+
+template <int DIM, int MODEL, int NSP>
+__device__ __forceinline__ void load_proj(const double* Fp, long nf, long t, FaceProj<DIM, MODEL, NSP>& F) {
+    F.rb = Fp[0 * nf + t]; F.cb = Fp[1 * nf + t]; F.m_hrc = Fp[2 * nf + t]; F.p_hrc = Fp[3 * nf + t];
+    F.ic2 = Fp[4 * nf + t]; F.irc = Fp[5 * nf + t];
+    if constexpr (MODEL == SINGLE_SPECIES) return;
+#pragma unroll
+    for (int q = 0; q < NSP; q++) {
+        F.zb[q] = Fp[(6 + q) * nf + t];
+        F.zr[q] = Fp[(6 + NSP + q) * nf + t];
+        F.hz[q] = Fp[(6 + 2 * NSP + q) * nf + t];
+    }
+}
+
+// Face coordinates of item t of axis AX: (i, j, k), the cell on the + side and the stride.
+template <int DIM, int AX>
+__device__ __forceinline__ void face_coords(const Geom& g, long t, int& i, int& j, int& k, long& xR, long& st) {
+    const int e0 = g.n[0] + (AX == 0 ? 3 : 0);
+    const int e1 = g.n[1] + (AX == 1 ? 3 : 0);
+    i = (int)(t % e0) - (AX == 0);
+    j = (int)((t / e0) % e1) - (AX == 1);
+    k = DIM == 3 ? (int)(t / ((long)e0 * e1)) - (AX == 2) : 0;
+    xR = cidx<DIM>(g, i, j, k);
+    st = (AX == 0) ? 1 : (AX == 1 ? (long)g.G[0] : (long)g.G[0] * g.G[1]);
+}
+
+// Projection means and factors of face t (as face_item computes them).
+template <int DIM, int MODEL, int NSP, int AX>
+__device__ __forceinline__ void face_proj_item(const Geom& g, const Scratch& S, const VjpArgs& VA, long t) {
+    const long nf = nface_of(g, AX);
+    const long nc = ncell_of(g);
+    int i, j, k;
+    long xR, st;
+    face_coords<DIM, AX>(g, t, i, j, k, xR, st);
+    const long xL = xR - st;
+    FaceProj<DIM, MODEL, NSP> F;
+    F.rb = double(1)/double(2)*(S.rho[xL] + S.rho[xR]);
+    F.cb = double(1)/double(2)*(S.cs[xL] + S.cs[xR]);
+    if constexpr (MODEL != SINGLE_SPECIES) {
+#pragma unroll
+        for (int q = 0; q < NSP; q++) F.zb[q] = double(1)/double(2)*(S.V[q * nc + xL] + S.V[q * nc + xR]);
+    }
+    face_proj_setup(F);
+    store_proj<DIM, MODEL, NSP>(VA.Fp[AX], nf, t, F);
+}
+
+// Characteristic stencil U[0..5] of variable e at face t.
+template <int DIM, int MODEL, int NSP, int AX>
+__device__ __forceinline__ void char_stencil(const Geom& g, const Scratch& S, const FaceProj<DIM, MODEL, NSP>& F,
+                                             long xR, long st, int e, double* U) {
+    constexpr int NEQ = Model<DIM, MODEL, NSP>::NEQ;
+    const long nc = ncell_of(g);
+#pragma unroll
+    for (int m = 0; m < 6; m++) {
+        double Vm[NEQ];
+        const long x = xR + (m - 3) * st;
+#pragma unroll
+        for (int q = 0; q < NEQ; q++) Vm[q] = S.V[q * nc + x];
+        U[m] = char_one<DIM, MODEL, NSP, AX>(F, Vm, e);
+    }
+}
+
+// Item u = e*nf + t: forward WCNS interpolation of variable e at face t (exact
+// form), keeping the reconstructed values and the smoothness indicators.
 template <int DIM, int MODEL, int NSP, int SCHEME, int AX>
-__device__ __forceinline__ void face_bwd_item(const Params& P, const Geom& g, const Scratch& S, const VjpArgs& VA,
-                                              long t) {
+__device__ __forceinline__ void face_fwd_weno_item(const Params& P, const Geom& g, const Scratch& S,
+                                                   const VjpArgs& VA, long u) {
+    const long nf = nface_of(g, AX);
+    const long t = u % nf;
+    const int e = (int)(u / nf);
+    int i, j, k;
+    long xR, st;
+    face_coords<DIM, AX>(g, t, i, j, k, xR, st);
+    FaceProj<DIM, MODEL, NSP> F;
+    load_proj<DIM, MODEL, NSP>(VA.Fp[AX], nf, t, F);
+    double U[6], b[9], Wm, Wp;
+    char_stencil<DIM, MODEL, NSP, AX>(g, S, F, xR, st, e, U);
+    constexpr int NB = SCHEME == WCNS5_JS ? 6 : 9;
+    if constexpr (SCHEME == WCNS5_JS) js_pair_keep(U, P.p, Wm, Wp, b);
+    else ld_pair_keep(U, P, Wm, Wp, b);
+    VA.Wv[AX][(long)(2 * e) * nf + t] = Wm;
+    VA.Wv[AX][(long)(2 * e + 1) * nf + t] = Wp;
+#pragma unroll
+    for (int q = 0; q < NB; q++) VA.Kb[AX][(long)(NB * e + q) * nf + t] = b[q];
+}
+
+template <int DIM, int MODEL, int NSP, int SCHEME, int AX>
+__device__ __forceinline__ void face_bwd_riemann_item(const Params& P, const Geom& g, const Scratch& S,
+                                                      const VjpArgs& VA, long t) {
     using M = Model<DIM, MODEL, NSP>;
+    using FL = FaceLayout<NSP>;
     constexpr int NEQ = M::NEQ;
     const long nf = nface_of(g, AX);
     const long nc = ncell_of(g);
-    const long st = (AX == 0) ? 1 : (AX == 1 ? (long)g.G[0] : (long)g.G[0] * g.G[1]);
-    double* Cb = VA.Cb[AX];
-    {
-        const int e0 = g.n[0] + (AX == 0 ? 3 : 0);
-        const int e1 = g.n[1] + (AX == 1 ? 3 : 0);
-        const int i = (int)(t % e0) - (AX == 0);
-        const int j = (int)((t / e0) % e1) - (AX == 1);
-        const int k = DIM == 3 ? (int)(t / ((long)e0 * e1)) - (AX == 2) : 0;
-        const int fa = AX == 0 ? i : (AX == 1 ? j : k);     // face coordinate along AX, in [-1, n+1]
-        const long xR = cidx<DIM>(g, i, j, k);
-        const long xL = xR - st;
+    int i, j, k;
+    long xR, st;
+    face_coords<DIM, AX>(g, t, i, j, k, xR, st);
+    const int fa = AX == 0 ? i : (AX == 1 ? j : k);     // face coordinate along AX, in [-1, n+1]
+    const long xL = xR - st;
 
-        // adjoints of the midpoint flux and midpoint velocity of this face
-        double Fmb[NEQ];
+    // adjoints of the midpoint flux and midpoint velocity of this face
+    double Fmb[NEQ];
+#pragma unroll
+    for (int e = 0; e < NEQ; e++)
+        Fmb[e] = VA.dt*(double(23)/double(15)*Fface_bar<DIM, MODEL, NSP, AX>(g, VA, i, j, k, fa, e) +
+                        double(1)/double(30)*(Fface_bar<DIM, MODEL, NSP, AX>(g, VA, i, j, k, fa - 1, e) +
+                                              Fface_bar<DIM, MODEL, NSP, AX>(g, VA, i, j, k, fa + 1, e)));
+    double umb = 0.0;
+    if constexpr (MODEL == FIVE_EQN_ALLAIRE) {
+        umb = (double(3)/double(2)*(usrc_bar<DIM, MODEL, NSP, AX>(g, VA, i, j, k, fa - 1) -
+                                    usrc_bar<DIM, MODEL, NSP, AX>(g, VA, i, j, k, fa)) +
+               double(1)/double(30)*(usrc_bar<DIM, MODEL, NSP, AX>(g, VA, i, j, k, fa - 2) -
+                                     usrc_bar<DIM, MODEL, NSP, AX>(g, VA, i, j, k, fa + 1)))/g.dx[AX];
+    }
+
+    // forward recompute (the exact form of face_item); the projection and the
+    // reconstructed characteristic values come from face_proj_item / face_fwd_weno_item
+    const double theta_avg = 0.5*(S.theta[xL] + S.theta[xR]);
+    const double Omega_avg = 0.5*(S.Omega[xL] + S.Omega[xR]);
+    const double sensor = -theta_avg/(fabs(theta_avg) + Omega_avg + HMR_EPS);
+    const bool use_hll = sensor > 0.65;
+    FaceProj<DIM, MODEL, NSP> F;
+    load_proj<DIM, MODEL, NSP>(VA.Fp[AX], nf, t, F);
+    double Wm[NEQ], Wp[NEQ];
+#pragma unroll
+    for (int e = 0; e < NEQ; e++) {
+        Wm[e] = VA.Wv[AX][(long)(2 * e) * nf + t];
+        Wp[e] = VA.Wv[AX][(long)(2 * e + 1) * nf + t];
+    }
+    double VL[NEQ], VR[NEQ];
+    prim_from_char<true, DIM, MODEL, NSP, AX>(F, Wm, VL);
+    prim_from_char<true, DIM, MODEL, NSP, AX>(F, Wp, VR);
+    double mL, mR;
+    const bool ok = face_bounded<DIM, MODEL, NSP>(P, VL, mL) & face_bounded<DIM, MODEL, NSP>(P, VR, mR);
+    if (!ok) {
+#pragma unroll
+        for (int e = 0; e < NEQ; e++) { VL[e] = S.V[e * nc + xL]; VR[e] = S.V[e * nc + xR]; }
+    }
+
+    // reverse of the Riemann solve
+    double VLb[NEQ], VRb[NEQ];
+#pragma unroll
+    for (int e = 0; e < NEQ; e++) { VLb[e] = 0.0; VRb[e] = 0.0; }
+    double umid;
+    riemann_bwd<DIM, MODEL, NSP, AX>(P, VL, VR, use_hll, Fmb, umb, VLb, VRb, umid);
+    if constexpr (MODEL == FIVE_EQN_ALLAIRE) S.um[AX][t] = umid;
+    VA.okf[AX][t] = ok ? 1 : 0;
+    double* Cb = VA.Cb[AX];
+    if (!ok) {
+        // first order: the face states are the two cells' primitive variables
+#pragma unroll
+        for (int m = 0; m < 6; m++)
+#pragma unroll
+            for (int e = 0; e < NEQ; e++)
+                Cb[(long)(m * NEQ + e) * nf + t] = m == 2 ? VLb[e] : (m == 3 ? VRb[e] : 0.0);
+        Cb[(long)(6 * NEQ) * nf + t] = 0.0;
+        Cb[(long)(6 * NEQ + 1) * nf + t] = 0.0;
+        return;
+    }
+    double Wmb[NEQ], Wpb[NEQ];
+#pragma unroll
+    for (int e = 0; e < NEQ; e++) { Wmb[e] = 0.0; Wpb[e] = 0.0; }
+    FaceProjBar<NSP> Fb;
+    Fb.p_hrc = 0.0; Fb.ic2 = 0.0; Fb.irc = 0.0;
+#pragma unroll
+    for (int q = 0; q < NSP; q++) { Fb.zr[q] = 0.0; Fb.hz[q] = 0.0; }
+    prim_from_char_bwd<DIM, MODEL, NSP, AX>(F, Wm, VLb, Wmb, Fb);
+    prim_from_char_bwd<DIM, MODEL, NSP, AX>(F, Wp, VRb, Wpb, Fb);
+    double* Wb = VA.Wb[AX];
+#pragma unroll
+    for (int e = 0; e < NEQ; e++) {
+        Wb[(long)(2 * e) * nf + t] = Wmb[e];
+        Wb[(long)(2 * e + 1) * nf + t] = Wpb[e];
+    }
+    double* Fp = VA.Fp[AX];
+    Fp[(long)(FL::F + 0) * nf + t] = Fb.p_hrc;
+    Fp[(long)(FL::F + 1) * nf + t] = Fb.ic2;
+    Fp[(long)(FL::F + 2) * nf + t] = Fb.irc;
+#pragma unroll
+    for (int q = 0; q < NSP; q++) Fp[(long)(FL::F + 3 + q) * nf + t] = Fb.hz[q];
+}
+
+// Item u = e*nf + t: characteristic variable e of face t.
+template <int DIM, int MODEL, int NSP, int SCHEME, int AX>
+__device__ __forceinline__ void face_bwd_weno_item(const Params& P, const Geom& g, const Scratch& S,
+                                                   const VjpArgs& VA, long u) {
+    using M = Model<DIM, MODEL, NSP>;
+    constexpr int NEQ = M::NEQ;
+    const long nf = nface_of(g, AX);
+    const long t = u % nf;
+    const int e = (int)(u / nf);
+    if (!VA.okf[AX][t]) return;
+    const long nc = ncell_of(g);
+    int i, j, k;
+    long xR, st;
+    face_coords<DIM, AX>(g, t, i, j, k, xR, st);
+    FaceProj<DIM, MODEL, NSP> F;
+    load_proj<DIM, MODEL, NSP>(VA.Fp[AX], nf, t, F);
+    double U[6], Ub[6] = {0, 0, 0, 0, 0, 0};
+    char_stencil<DIM, MODEL, NSP, AX>(g, S, F, xR, st, e, U);
+    const double Wmb = VA.Wb[AX][(long)(2 * e) * nf + t];
+    const double Wpb = VA.Wb[AX][(long)(2 * e + 1) * nf + t];
+    constexpr int NB = SCHEME == WCNS5_JS ? 6 : 9;
+    double b[NB];
+#pragma unroll
+    for (int q = 0; q < NB; q++) b[q] = VA.Kb[AX][(long)(NB * e + q) * nf + t];
+    if constexpr (SCHEME == WCNS5_JS) js_pair_bwd(U, b, P.p, Wmb, Wpb, Ub);
+    else ld_pair_bwd(U, b, P, Wmb, Wpb, Ub);
+    double* Cb = VA.Cb[AX];
+#pragma unroll
+    for (int m = 0; m < 6; m++) Cb[(long)(m * NEQ + e) * nf + t] = Ub[m];
+}
+
+template <int DIM, int MODEL, int NSP, int AX>
+__device__ __forceinline__ void face_bwd_char_item(const Geom& g, const Scratch& S, const VjpArgs& VA, long t) {
+    using M = Model<DIM, MODEL, NSP>;
+    using FL = FaceLayout<NSP>;
+    constexpr int NEQ = M::NEQ;
+    const long nf = nface_of(g, AX);
+    if (!VA.okf[AX][t]) return;
+    const long nc = ncell_of(g);
+    int i, j, k;
+    long xR, st;
+    face_coords<DIM, AX>(g, t, i, j, k, xR, st);
+    const double* Fp = VA.Fp[AX];
+    FaceProj<DIM, MODEL, NSP> F;
+    load_proj<DIM, MODEL, NSP>(Fp, nf, t, F);
+    FaceProjBar<NSP> Fb;
+    Fb.p_hrc = Fp[(long)(FL::F + 0) * nf + t];
+    Fb.ic2 = Fp[(long)(FL::F + 1) * nf + t];
+    Fb.irc = Fp[(long)(FL::F + 2) * nf + t];
+#pragma unroll
+    for (int q = 0; q < NSP; q++) { Fb.hz[q] = Fp[(long)(FL::F + 3 + q) * nf + t]; Fb.zr[q] = 0.0; }
+    double* Cb = VA.Cb[AX];
+    double zbb[NSP];
+#pragma unroll
+    for (int q = 0; q < NSP; q++) zbb[q] = 0.0;
+#pragma unroll
+    for (int m = 0; m < 6; m++) {
+        double Vm[NEQ], Vb[NEQ];
+        const long x = xR + (m - 3) * st;
+#pragma unroll
+        for (int q = 0; q < NEQ; q++) { Vm[q] = S.V[q * nc + x]; Vb[q] = 0.0; }
 #pragma unroll
         for (int e = 0; e < NEQ; e++)
-            Fmb[e] = VA.dt*(double(23)/double(15)*Fface_bar<DIM, MODEL, NSP, AX>(g, VA, i, j, k, fa, e) +
-                            double(1)/double(30)*(Fface_bar<DIM, MODEL, NSP, AX>(g, VA, i, j, k, fa - 1, e) +
-                                                  Fface_bar<DIM, MODEL, NSP, AX>(g, VA, i, j, k, fa + 1, e)));
-        double umb = 0.0;
-        if constexpr (MODEL == FIVE_EQN_ALLAIRE) {
-            umb = (double(3)/double(2)*(usrc_bar<DIM, MODEL, NSP, AX>(g, VA, i, j, k, fa - 1) -
-                                        usrc_bar<DIM, MODEL, NSP, AX>(g, VA, i, j, k, fa)) +
-                   double(1)/double(30)*(usrc_bar<DIM, MODEL, NSP, AX>(g, VA, i, j, k, fa - 2) -
-                                         usrc_bar<DIM, MODEL, NSP, AX>(g, VA, i, j, k, fa + 1)))/g.dx[AX];
-        }
-
-        // forward recompute (the exact form of face_item)
-        const double theta_avg = 0.5*(S.theta[xL] + S.theta[xR]);
-        const double Omega_avg = 0.5*(S.Omega[xL] + S.Omega[xR]);
-        const double sensor = -theta_avg/(fabs(theta_avg) + Omega_avg + HMR_EPS);
-        const bool use_hll = sensor > 0.65;
-        FaceProj<DIM, MODEL, NSP> F;
-        F.rb = double(1)/double(2)*(S.rho[xL] + S.rho[xR]);
-        F.cb = double(1)/double(2)*(S.cs[xL] + S.cs[xR]);
-        if constexpr (MODEL != SINGLE_SPECIES) {
+            char_one_bwd<DIM, MODEL, NSP, AX>(F, Vm, e, Cb[(long)(m * NEQ + e) * nf + t], Vb, Fb);
+        // row m held the WCNS adjoints of the stencil values; it now takes the primitive-variable ones
 #pragma unroll
-            for (int q = 0; q < NSP; q++) F.zb[q] = double(1)/double(2)*(S.V[q * nc + xL] + S.V[q * nc + xR]);
-        }
-        face_proj_setup(F);
-        double Vc[6][NEQ];
-#pragma unroll
-        for (int m = 0; m < 6; m++) {
-            const long x = xR + (m - 3) * st;
-#pragma unroll
-            for (int e = 0; e < NEQ; e++) Vc[m][e] = S.V[e * nc + x];
-        }
-        double Wm[NEQ], Wp[NEQ];
-#pragma unroll
-        for (int e = 0; e < NEQ; e++) {
-            double U[6];
-#pragma unroll
-            for (int m = 0; m < 6; m++) U[m] = char_one<DIM, MODEL, NSP, AX>(F, Vc[m], e);
-            if constexpr (SCHEME == WCNS5_JS) js_pair<true>(U, P.p, Wm[e], Wp[e]);
-            else ld_pair<true>(U, P, Wm[e], Wp[e]);
-        }
-        double VL[NEQ], VR[NEQ];
-        prim_from_char<true, DIM, MODEL, NSP, AX>(F, Wm, VL);
-        prim_from_char<true, DIM, MODEL, NSP, AX>(F, Wp, VR);
-        double mL, mR;
-        const bool ok = face_bounded<DIM, MODEL, NSP>(P, VL, mL) & face_bounded<DIM, MODEL, NSP>(P, VR, mR);
-        if (!ok) {
-#pragma unroll
-            for (int e = 0; e < NEQ; e++) { VL[e] = Vc[2][e]; VR[e] = Vc[3][e]; }
-        }
-
-        // reverse
-        double VLb[NEQ], VRb[NEQ];
-#pragma unroll
-        for (int e = 0; e < NEQ; e++) { VLb[e] = 0.0; VRb[e] = 0.0; }
-        double umid;
-        riemann_bwd<DIM, MODEL, NSP, AX>(P, VL, VR, use_hll, Fmb, umb, VLb, VRb, umid);
-        if constexpr (MODEL == FIVE_EQN_ALLAIRE) S.um[AX][t] = umid;
-
-        double Vb[6][NEQ];
-#pragma unroll
-        for (int m = 0; m < 6; m++)
-#pragma unroll
-            for (int e = 0; e < NEQ; e++) Vb[m][e] = 0.0;
-        double rbb = 0.0, cbb = 0.0;
-        if (ok) {
-            double Wmb[NEQ], Wpb[NEQ];
-#pragma unroll
-            for (int e = 0; e < NEQ; e++) { Wmb[e] = 0.0; Wpb[e] = 0.0; }
-            FaceProjBar<NSP> Fb;
-            Fb.p_hrc = 0.0; Fb.ic2 = 0.0; Fb.irc = 0.0;
-#pragma unroll
-            for (int q = 0; q < NSP; q++) { Fb.zr[q] = 0.0; Fb.hz[q] = 0.0; }
-            prim_from_char_bwd<DIM, MODEL, NSP, AX>(F, Wm, VLb, Wmb, Fb);
-            prim_from_char_bwd<DIM, MODEL, NSP, AX>(F, Wp, VRb, Wpb, Fb);
-#pragma unroll
-            for (int e = 0; e < NEQ; e++) {
-                double U[6], Ub[6] = {0, 0, 0, 0, 0, 0};
-#pragma unroll
-                for (int m = 0; m < 6; m++) U[m] = char_one<DIM, MODEL, NSP, AX>(F, Vc[m], e);
-                if constexpr (SCHEME == WCNS5_JS) js_pair_bwd(U, P.p, Wmb[e], Wpb[e], Ub);
-                else ld_pair_bwd(U, P, Wmb[e], Wpb[e], Ub);
-#pragma unroll
-                for (int m = 0; m < 6; m++) char_one_bwd<DIM, MODEL, NSP, AX>(F, Vc[m], e, Ub[m], Vb[m], Fb);
-            }
-            double zbb[NSP];
-#pragma unroll
-            for (int q = 0; q < NSP; q++) zbb[q] = 0.0;
-            face_proj_bwd<DIM, MODEL, NSP>(F, Fb, rbb, cbb, zbb);
-            if constexpr (MODEL != SINGLE_SPECIES) {
-#pragma unroll
-                for (int q = 0; q < NSP; q++) {
-                    Vb[2][q] += 0.5*zbb[q];
-                    Vb[3][q] += 0.5*zbb[q];
-                }
-            }
-        } else {
-#pragma unroll
-            for (int e = 0; e < NEQ; e++) { Vb[2][e] += VLb[e]; Vb[3][e] += VRb[e]; }
-        }
-#pragma unroll
-        for (int m = 0; m < 6; m++)
-#pragma unroll
-            for (int e = 0; e < NEQ; e++) Cb[(long)(m * NEQ + e) * nf + t] = Vb[m][e];
-        Cb[(long)(6 * NEQ) * nf + t] = rbb;
-        Cb[(long)(6 * NEQ + 1) * nf + t] = cbb;
+        for (int e = 0; e < NEQ; e++) Cb[(long)(m * NEQ + e) * nf + t] = Vb[e];
     }
+    double rbb = 0.0, cbb = 0.0;
+    face_proj_bwd<DIM, MODEL, NSP>(F, Fb, rbb, cbb, zbb);
+    if constexpr (MODEL != SINGLE_SPECIES) {
+#pragma unroll
+        for (int q = 0; q < NSP; q++) {
+            Cb[(long)(2 * NEQ + q) * nf + t] += 0.5*zbb[q];
+            Cb[(long)(3 * NEQ + q) * nf + t] += 0.5*zbb[q];
+        }
+    }
+    Cb[(long)(6 * NEQ) * nf + t] = rbb;
+    Cb[(long)(6 * NEQ + 1) * nf + t] = cbb;
 }
 
 // ---------------------------------------------------------------------------
