@@ -72,6 +72,21 @@ def dist_env():
     return rank, world, local
 
 
+def replica_throughput(local_ms, cells_per_step, steps, world, device):
+    """Whole-job throughput of `world` independent replicas (one per GPU, no
+    data-path collective): the timed region is the slowest rank's (max over
+    ranks), every rank advanced cells_per_step * steps cell-updates.
+    Returns (max_ms, cell-updates/s)."""
+    total_ms = float(local_ms)
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([total_ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    return total_ms, world * cells_per_step * steps / (total_ms * 1e-3)
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -436,12 +451,8 @@ def main():
     step_ms = [ev[k][0].elapsed_time(ev[k][3]) for k in range(args.steps)]
     sub_ms = [ev[k][s].elapsed_time(ev[k][s + 1]) for k in range(args.steps) for s in range(3)]
     total_ms = ev[0][0].elapsed_time(ev[-1][3])
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
     cells_per_step = n * n * 3
-    value = world * cells_per_step * args.steps / (total_ms * 1e-3)
+    total_ms, value = replica_throughput(total_ms, cells_per_step, args.steps, world, "cuda")
 
     # End-to-end through the public API: pinned host state in, step, state out.
     host_in = Q0.cpu().pin_memory()

@@ -327,6 +327,14 @@ class RungeKuttaLevelIntegrator:
         return Xb
 
 
+class _DeviceArray:
+    """A device FP64 array (pointer + shape) exposed through __cuda_array_interface__."""
+
+    def __init__(self, ptr, shape):
+        self.__cuda_array_interface__ = {"shape": tuple(int(v) for v in shape), "typestr": "<f8",
+                                         "data": (int(ptr), False), "version": 3}
+
+
 class BatchedLevel:
     """Every patch of a level advanced by one persistent kernel per SSPRK3 substep."""
 
@@ -371,6 +379,13 @@ class BatchedLevel:
         L.check("hmr_level_state", self._lib.hmr_level_state(
             self.level, int(patch), int(slot), ctypes.cast(arr, L.DPP)))
         return [ctypes.cast(arr[e], ctypes.c_void_p).value for e in range(self.rec.ncomp)]
+
+    def state(self, patch, slot):
+        """Tensor view (ncomp, G2, G1, G0) of a patch's stage-`slot` state (slot 0: the bound
+        tensor; slots 1, 2: the intermediate stage states owned by the level)."""
+        ptrs = self.state_pointers(patch, slot)
+        comps = [torch.as_tensor(_DeviceArray(ptr, self.shapes[patch][1:]), device="cuda") for ptr in ptrs]
+        return torch.stack(comps)
 
     def substep(self, stage, dt, stream=None):
         L.check("hmr_level_substep", self._lib.hmr_level_substep(self.level, int(stage), float(dt),

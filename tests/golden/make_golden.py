@@ -1,0 +1,72 @@
+"""Generates the golden fixtures of the convective path from the CPU oracle.
+
+The reference ships no golden flux vectors (its tests pin only the order of
+accuracy), so these fixtures freeze the oracle's output on small seeded inputs:
+for each of the 12 variants (model x dimension x scheme), the dt-scaled face
+fluxes, the source and the face counters of computeConvectiveFluxAndSourceOnPatch
+on a smooth and a shock state, and the interior state after one SSPRK3 step with
+periodic ghost fill.  The inputs are regenerated from their seeds (tests/helpers.py).
+
+    python tests/golden/make_golden.py      # rewrites tests/golden/convective_fixtures.npz
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+from hamers_gb300 import problems as P  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+from tests.helpers import shock_state, smooth_state  # noqa: E402
+
+OUT = os.path.join(HERE, "convective_fixtures.npz")
+
+MODELS = [(O.MODEL_SINGLE_SPECIES, "single", [1.4], None),
+          (O.MODEL_FOUR_EQN_CONSERVATIVE, "four", P.FOUR_EQN_GAMMA, P.FOUR_EQN_R),
+          (O.MODEL_FIVE_EQN_ALLAIRE, "five", [1.4, 1.67], None)]
+SIZES = {2: (8, 6), 3: (4, 4, 4)}
+DT = 1.3e-3
+
+
+def cases():
+    for model, mname, gam, R in MODELS:
+        for dim in (2, 3):
+            for scheme, sname in ((O.SCHEME_WCNS5_JS, "js"), (O.SCHEME_WCNS6_LD, "ld")):
+                yield model, mname, gam, R, dim, scheme, sname
+
+
+def inputs(model, dim, gam, label):
+    n = SIZES[dim]
+    gen = smooth_state if label == "smooth" else shock_state
+    return n, gen(model, dim, n, seed=7, species_gamma=gam)
+
+
+def compute():
+    out = {}
+    for model, mname, gam, R, dim, scheme, sname in cases():
+        cfg = O.Config(model, dim, gam, scheme, species_R=R)
+        for label in ("smooth", "shock"):
+            key = f"{mname}_{dim}d_{sname}_{label}"
+            n, Q = inputs(model, dim, gam, label)
+            dx = [1.0 / v for v in n]
+            F, S, st = O.conv_flux_source(cfg, n, dx, DT, Q)
+            for a, f in enumerate(F):
+                out[f"{key}_flux{a}"] = f
+            out[f"{key}_source"] = S
+            out[f"{key}_counters"] = np.array(st[1:], dtype=np.int64)
+            Qs = Q.copy()
+            O.fill_ghosts(cfg, n, [1] * dim, Qs)
+            O.rk3_advance(cfg, n, dx, DT, [1] * dim, 1, Qs)
+            sl = (slice(None),) + tuple(slice(4, -4) if d < dim else slice(None) for d in (2, 1, 0))
+            out[f"{key}_rk3"] = np.ascontiguousarray(Qs[sl])
+    return out
+
+
+if __name__ == "__main__":
+    O.build()
+    np.savez_compressed(OUT, **compute())
+    print("wrote", OUT, os.path.getsize(OUT), "bytes")
