@@ -27,6 +27,8 @@ import sys
 import threading
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
@@ -61,6 +63,8 @@ def parse():
                     help="skip the batched-vs-per-patch measurement on uneven 3D patches")
     ap.add_argument("--no-peak", action="store_true", help="skip the FP64 peak microbenchmark")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint/forward cost measurement")
+    ap.add_argument("--c5", action="store_true",
+                    help="also run the 3-level 3D five-equation batched substep + amplitude adjoint")
     ap.add_argument("--uneven-patches", type=int, default=512)
     return ap.parse_args()
 
@@ -292,6 +296,97 @@ def adjoint_cost(args, flow, Qnp, n, dx, dt, reps=3):
     return out
 
 
+def c5_level_and_adjoint(args, flow, base=128, reps=3):
+    """3D five-equation shock / perturbed interface (gamma 1.4/1.09, density ratio 3, Mach 1.5)
+    on a seeded 3-level layout (ratio 2, ~512^3 finest-equivalent) of uneven patches with sides
+    U{16..64} (seed 4), WCNS6-LD + HLLC-HLL: one batched RK substep over every patch of every
+    level (one persistent kernel, ghosts from the analytic initial state) against per-patch
+    launches, and the adjoint of that substep with respect to the 64 interface-mode amplitudes
+    (per-patch VJPs chained through the differentiable initial condition)."""
+    import torch
+    from hamers_gb300 import problems as P
+    layout = P.amr_layout_3d(base=base, seed=4)
+    amps, waves, phases = P.shock_interface_3d_modes(64, seed=4)
+    a = torch.tensor(amps, dtype=torch.float64, device="cuda")
+    finest = min(dx[0] for _, _, _, dx in layout)
+    fm = flow.FlowModel("FIVE_EQN_ALLAIRE", 3, [1.4, 1.09])
+    rec = flow.ConvectiveFluxReconstructor("WCNS6_LD_HLLC_HLL", fm, precision=args.precision)
+    states = [P.shock_interface_3d_patch(lo, n, dx, a, waves, phases, finest) for _, lo, n, dx in layout]
+    cells = sum(n[0] * n[1] * n[2] for _, _, n, _ in layout)
+    # dt at CFL 0.4 on the finest level (post-shock speed + sound speed bound)
+    dt = 0.4 * finest / (3.0 * 3.0)
+    lv = flow.BatchedLevel(rec, [(n, dx) for _, _, n, dx in layout])
+    for p, Q in enumerate(states):
+        lv.bind(p, Q)
+        lv.set_periodic(p, [2, 2, 2])
+    stream = torch.cuda.current_stream()
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    lv.substep(0, dt)
+    torch.cuda.synchronize()
+    lv.check()
+    e[0].record(stream)
+    for _ in range(reps):
+        lv.substep(0, dt)
+    e[1].record(stream)
+    torch.cuda.synchronize()
+    lv.check()
+    t_batched = e[0].elapsed_time(e[1]) / reps
+    # per-patch launches of the same substep
+    eu = flow.Euler(rec)
+    big = max(range(len(layout)), key=lambda i: np.prod(layout[i][2]))
+    rec.reserve(flow.Patch(layout[big][2], layout[big][3], states[big]))
+    outs = [torch.empty_like(Q) for Q in states]
+    views = [flow.Patch(n, dx, Q) for (_, _, n, dx), Q in zip(layout, states)]
+
+    def per_patch():
+        for v, Q, o in zip(views, states, outs):
+            eu.substep(v, 0, [Q], dt, o)
+
+    per_patch()
+    torch.cuda.synchronize()
+    e[0].record(stream)
+    for _ in range(reps):
+        per_patch()
+    e[1].record(stream)
+    torch.cuda.synchronize()
+    t_patch = e[0].elapsed_time(e[1]) / reps
+    # adjoint of J = sum_p <w_p, Q_out,p> (w_p seeded) with respect to the 64 amplitudes
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(4)
+    W = [torch.randn(Q.shape, dtype=torch.float64, device="cuda", generator=gen) for Q in states]
+    bars = [torch.zeros_like(Q) for Q in states]
+
+    def reverse():
+        for v, Q, w, b in zip(views, states, W, bars):
+            b.zero_()
+            eu.substepVJP(v, 0, [Q], dt, w, [b])
+
+    reverse()
+    torch.cuda.synchronize()
+    e[0].record(stream)
+    for _ in range(reps):
+        reverse()
+    e[1].record(stream)
+    torch.cuda.synchronize()
+    t_adj = e[0].elapsed_time(e[1]) / reps
+    a_req = a.clone().requires_grad_(True)
+    grad = torch.zeros_like(a)
+    for (_, lo, n, dx), b in zip(layout, bars):
+        Qa = P.shock_interface_3d_patch(lo, n, dx, a_req, waves, phases, finest)
+        grad += torch.autograd.grad(Qa, a_req, grad_outputs=b)[0]
+    lv.close()
+    rec.close()
+    return {"workload": "3D five-eqn Allaire shock/interface, 3 levels (ratio 2, 512^3 finest-equivalent), "
+                        f"{len(layout)} uneven patches (side 16-64, seed 4), WCNS6-LD + HLLC-HLL, one RK substep; "
+                        "adjoint w.r.t. 64 interface-mode amplitudes",
+            "cells": cells, "patches": len(layout), "precision": args.precision,
+            "batched_substep_ms": t_batched, "batched_cell_updates_per_s": cells / (t_batched * 1e-3),
+            "per_patch_substep_ms": t_patch, "per_patch_cell_updates_per_s": cells / (t_patch * 1e-3),
+            "batched_over_per_patch": t_patch / t_batched,
+            "adjoint_substep_ms": t_adj, "adjoint_over_batched_forward": t_adj / t_batched,
+            "grad_amplitudes_norm": float(grad.norm())}
+
+
 def cpu_baseline_oracle(Q, n, dx, dt, budget_s=15.0, threads=None):
     """Oracle stage throughput on the host cores on a bounded sample (rows of the patch)."""
     from oracle import oracle as O
@@ -513,6 +608,11 @@ def main():
             line["adjoint"] = adjoint_cost(args, flow, Qnp, n, dx, dt)
         except Exception as exc:  # report, never lose the headline line
             line["adjoint"] = {"error": str(exc)[:300]}
+    if args.c5:
+        try:
+            line["c5"] = c5_level_and_adjoint(args, flow)
+        except Exception as exc:  # report, never lose the headline line
+            line["c5"] = {"error": str(exc)[:300]}
     if not args.no_uneven:
         try:
             line["batched_vs_per_patch"] = uneven_batched_vs_patch(args, flow)

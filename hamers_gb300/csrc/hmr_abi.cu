@@ -629,7 +629,10 @@ int hmr_level_bind_state(hmr_level* lv, int p, double* const* comps) {
 
 int hmr_level_set_periodic(hmr_level* lv, int p, const int* periodic) {
     if (!lv || p < 0 || p >= lv->npatch || !periodic) return HMR_ERR_ARGUMENT;
-    for (int a = 0; a < 3; a++) lv->work[p].periodic[a] = a < lv->ctx->v.dim ? (periodic[a] != 0) : 0;
+    for (int a = 0; a < 3; a++) {
+        if (a < lv->ctx->v.dim && (periodic[a] < 0 || periodic[a] > 2)) return HMR_ERR_ARGUMENT;
+        lv->work[p].periodic[a] = a < lv->ctx->v.dim ? periodic[a] : 0;
+    }
     lv->dirty = true;
     return HMR_OK;
 }

@@ -98,7 +98,7 @@ int launch_fill(int dim, const Geom& g, const Comp& Q, int ncomp, const int* per
 // ghost adjoints are cleared.
 __device__ __forceinline__ int fill_src(int v, int n, int periodic) {
     if (v >= 0 && v < n) return v;
-    if (periodic) return ((v % n) + n) % n;
+    if (periodic == 1) return ((v % n) + n) % n;
     return v < 0 ? 0 : n - 1;
 }
 
@@ -113,7 +113,7 @@ __global__ void __launch_bounds__(THREADS) fill_vjp_gather_kernel(Geom g, Comp Q
         for (int a = 0; a < 3; a++) {
             pre[a][0] = c[a];
             np[a] = 1;
-            if (a >= DIM) continue;
+            if (a >= DIM || per.p[a] == 2) continue;   // provided ghosts are not copies of this cell
             for (int v = -GHOST; v < g.n[a] + GHOST; v++) {
                 if (v >= 0 && v < g.n[a]) continue;
                 if (fill_src(v, g.n[a], per.p[a]) == c[a] && np[a] < 9) pre[a][np[a]++] = v;
@@ -134,13 +134,20 @@ __global__ void __launch_bounds__(THREADS) fill_vjp_gather_kernel(Geom g, Comp Q
 }
 
 template <int DIM>
-__global__ void __launch_bounds__(THREADS) fill_vjp_clear_kernel(Geom g, Comp Qb, int ncomp) {
+__global__ void __launch_bounds__(THREADS) fill_vjp_clear_kernel(Geom g, Comp Qb, int ncomp, Periodic per) {
     const long n = ncell_of(g);
     for (long x = (long)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (long)gridDim.x * blockDim.x) {
-        const int i = (int)(x % g.G[0]) - GHOST;
-        const int j = (int)((x / g.G[0]) % g.G[1]) - GHOST;
-        const int k = DIM == 3 ? (int)(x / ((long)g.G[0] * g.G[1])) - GHOST : 0;
-        if (i >= 0 && i < g.n[0] && j >= 0 && j < g.n[1] && k >= 0 && k < g.n[2]) continue;
+        const int c[3] = {(int)(x % g.G[0]) - GHOST, (int)((x / g.G[0]) % g.G[1]) - GHOST,
+                          DIM == 3 ? (int)(x / ((long)g.G[0] * g.G[1])) - GHOST : 0};
+        bool inside = true, provided = false;
+        for (int a = 0; a < DIM; a++) {
+            if (c[a] < 0 || c[a] >= g.n[a]) {
+                inside = false;
+                provided = provided || per.p[a] == 2;
+            }
+        }
+        // provided ghosts keep their adjoints (they belong to whatever supplied the values)
+        if (inside || provided) continue;
         for (int e = 0; e < ncomp; e++) Qb.p[e][x] = 0.0;
     }
 }
@@ -150,10 +157,10 @@ int launch_fill_vjp(int dim, const Geom& g, const Comp& Qb, int ncomp, const int
     for (int a = 0; a < 3; a++) per.p[a] = periodic ? periodic[a] : 0;
     if (dim == 2) {
         fill_vjp_gather_kernel<2><<<grid_for(ninterior_of(g)), THREADS, 0, st>>>(g, Qb, ncomp, per);
-        fill_vjp_clear_kernel<2><<<grid_for(ncell_of(g)), THREADS, 0, st>>>(g, Qb, ncomp);
+        fill_vjp_clear_kernel<2><<<grid_for(ncell_of(g)), THREADS, 0, st>>>(g, Qb, ncomp, per);
     } else {
         fill_vjp_gather_kernel<3><<<grid_for(ninterior_of(g)), THREADS, 0, st>>>(g, Qb, ncomp, per);
-        fill_vjp_clear_kernel<3><<<grid_for(ncell_of(g)), THREADS, 0, st>>>(g, Qb, ncomp);
+        fill_vjp_clear_kernel<3><<<grid_for(ncell_of(g)), THREADS, 0, st>>>(g, Qb, ncomp, per);
     }
     return (int)cudaPeekAtLastError();
 }

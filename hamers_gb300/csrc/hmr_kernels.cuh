@@ -432,8 +432,10 @@ __device__ __forceinline__ void update_item(const Geom& g, const Scratch& S, con
 }
 
 // ---------------------------------------------------------------------------
-// Ghost fill of a single patch: periodic on axes with periodic[a] != 0,
-// zero-gradient otherwise.  item over the ghost box (interior items skip).
+// Ghost fill of a single patch, per axis: mode 0 zero-gradient, 1 periodic,
+// 2 provided by the caller (left untouched: neighbour copies, coarse-fine
+// interpolation or analytic values).  item over the ghost box (interior
+// items skip).
 // ---------------------------------------------------------------------------
 template <int DIM>
 __device__ __forceinline__ void fill_item(const Geom& g, const Comp& Q, int ncomp, const int* periodic, long x) {
@@ -448,8 +450,9 @@ __device__ __forceinline__ void fill_item(const Geom& g, const Comp& Q, int ncom
         s[a] = c[a];
         if (a >= DIM) continue;
         if (c[a] < 0 || c[a] >= g.n[a]) {
+            if (periodic[a] == 2) return;
             inside = false;
-            if (periodic[a]) s[a] = ((c[a] % g.n[a]) + g.n[a]) % g.n[a];
+            if (periodic[a] == 1) s[a] = ((c[a] % g.n[a]) + g.n[a]) % g.n[a];
             else s[a] = c[a] < 0 ? 0 : g.n[a] - 1;
         }
     }

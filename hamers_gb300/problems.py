@@ -321,3 +321,87 @@ def blobs_patches_3d_device(num_patches=512, side_lo=16, side_hi=64, seed=2, nbl
         Q[4] = 1.0 / (gamma - 1.0) + 0.5 * rho * (vel[0] ** 2 + vel[1] ** 2 + vel[2] ** 2)
         out.append((n, [h, h, h], Q.contiguous()))
     return out
+
+
+# ---------------------------------------------------------------------------
+# 3D five-equation shock / perturbed interface on a 3-level layout of uneven patches
+# ---------------------------------------------------------------------------
+def _tile(length, lo, hi, rng):
+    """Split `length` cells into segments of U{lo..hi} cells (the last one takes the rest)."""
+    segs, r = [], int(length)
+    while r > hi:
+        s = int(rng.integers(lo, min(hi, r - lo) + 1))
+        segs.append(s)
+        r -= s
+    segs.append(r)
+    return segs
+
+
+def amr_layout_3d(base=128, seed=4, side_lo=16, side_hi=64, x_ranges=((0.0, 1.0), (0.30, 0.70), (0.40, 0.60))):
+    """Seeded 3-level layout on [0,1]^3 (refinement ratio 2): level l has base*2^l cells per unit
+    length, covers x in x_ranges[l] (all of y and z) and is tiled by boxes whose side lengths along
+    each axis are drawn from U{side_lo..side_hi}.  Returns a list of (level, lo[3], n[3], dx[3])
+    with lo the box's first cell index at its level's resolution."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for lev, (x0, x1) in enumerate(x_ranges):
+        N = base * 2 ** lev
+        xlo, xhi = int(round(x0 * N)), int(round(x1 * N))
+        axes = [_tile(xhi - xlo, side_lo, side_hi, rng), _tile(N, side_lo, side_hi, rng),
+                _tile(N, side_lo, side_hi, rng)]
+        starts = [np.concatenate([[0], np.cumsum(a)[:-1]]) for a in axes]
+        dx = [1.0 / N] * 3
+        for a0, s0 in zip(axes[0], starts[0]):
+            for a1, s1 in zip(axes[1], starts[1]):
+                for a2, s2 in zip(axes[2], starts[2]):
+                    out.append((lev, [xlo + int(s0), int(s1), int(s2)], [int(a0), int(a1), int(a2)], dx))
+    return out
+
+
+def shock_interface_3d_modes(modes=64, seed=4, amp_max=0.01):
+    """The 64-mode interface perturbation of the 3D shock/interface problem: amplitudes
+    a_k ~ U[0, amp_max], wavenumbers (m_k, l_k) over an 8x8 grid, phases ~ U[0, 2 pi) (seeded)."""
+    rng = np.random.default_rng(seed + 1)
+    side = int(round(math.sqrt(modes)))
+    ml = [(1 + k // side, 1 + k % side) for k in range(modes)]
+    return rng.uniform(0.0, amp_max, modes), np.array(ml, dtype=np.float64), rng.uniform(0.0, 2 * math.pi, modes)
+
+
+def shock_interface_3d_patch(lo, n, dx, amps, waves, phases, finest_dx, gammas=(1.4, 1.09),
+                             density_ratio=3.0, mach=1.5):
+    """Conserved variables (8, G2, G1, G0) of one patch's ghost box (torch, on the amplitudes'
+    device, differentiable with respect to `amps`): species 1 (density 1) left of the interface
+    x_I(y, z) = 0.5 + sum_k a_k sin(2 pi (m_k y + l_k z) + phi_k), species 2 (density ratio 3)
+    right of it, tanh profile 4 finest cells wide, volume fraction clipped to [1e-8, 1 - 1e-8];
+    a Mach 1.5 shock at x = 0.25 moving into species 1 with the Rankine-Hugoniot state behind it.
+    Ghost cells hold the same analytic values (no fill needed)."""
+    import torch
+    dev, dt_ = amps.device, torch.float64
+    idx = [torch.arange(-GHOST, n[d] + GHOST, device=dev, dtype=dt_) for d in range(3)]
+    xs = [(lo[d] + idx[d] + 0.5) * dx[d] for d in range(3)]
+    z, y, x = torch.meshgrid(xs[2], xs[1], xs[0], indexing="ij")
+    w = torch.as_tensor(waves, device=dev, dtype=dt_)
+    ph = torch.as_tensor(phases, device=dev, dtype=dt_)
+    arg = 2.0 * math.pi * (w[:, 0, None, None] * y[:, :, 0][None] + w[:, 1, None, None] * z[:, :, 0][None]) \
+        + ph[:, None, None]
+    xI = 0.5 + (amps[:, None, None] * torch.sin(arg)).sum(dim=0)          # (G2, G1)
+    delta = 4.0 * finest_dx / (2.0 * math.atanh(0.9))
+    Z1 = 0.5 * (1.0 - torch.tanh((x - xI[:, :, None]) / delta))
+    Z1 = torch.clamp(Z1, 1e-8, 1.0 - 1e-8)
+    g1, g2 = gammas
+    p0, rho1, rho2 = 1.0, 1.0, density_ratio
+    M2 = mach * mach
+    p_s = p0 * (2.0 * g1 * M2 - (g1 - 1.0)) / (g1 + 1.0)
+    rho_s = rho1 * (g1 + 1.0) * M2 / ((g1 - 1.0) * M2 + 2.0)
+    u_s = mach * math.sqrt(g1 * p0 / rho1) * (1.0 - rho1 / rho_s)
+    shocked = x < 0.25
+    u = torch.where(shocked, torch.full_like(x, u_s), torch.zeros_like(x))
+    p = torch.where(shocked, torch.full_like(x, p_s), torch.full_like(x, p0))
+    r1 = torch.where(shocked, torch.full_like(x, rho_s), torch.full_like(x, rho1))
+    Z2 = 1.0 - Z1
+    zr1, zr2 = Z1 * r1, Z2 * rho2
+    rho = zr1 + zr2
+    gamma_m = 1.0 / (Z1 / (g1 - 1.0) + Z2 / (g2 - 1.0)) + 1.0
+    E = p / (gamma_m - 1.0) + 0.5 * rho * u * u
+    zero = torch.zeros_like(x)
+    return torch.stack([zr1, zr2, rho * u, zero, zero, E, Z1, Z2])

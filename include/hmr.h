@@ -144,8 +144,16 @@ int hmr_rk_substep_patch(hmr_ctx* ctx, const hmr_patch_geometry* geom, int stage
                          double beta, const double* const* const* Q_int, double dt, double* const* Q_out,
                          void* stream);
 
-/* Single-patch ghost fill: periodic along axes with periodic[a] != 0, zero-gradient otherwise
- * (one-patch equivalent of the SAMRAI fill schedule, RungeKuttaLevelIntegrator.cpp:1568,1701). */
+/* Ghost fill modes per axis (the `periodic` arrays below). */
+typedef enum {
+    HMR_FILL_ZERO_GRADIENT = 0,   /* copy of the nearest interior cell (extrapolation boundary) */
+    HMR_FILL_PERIODIC = 1,        /* periodic image within the patch */
+    HMR_FILL_PROVIDED = 2         /* ghost cells supplied by the caller are left untouched */
+} hmr_fill_mode;
+
+/* Single-patch ghost fill, mode per axis (hmr_fill_mode; any other non-zero value of older callers
+ * is rejected by hmr_level_set_periodic and read as zero-gradient here) -- the one-patch equivalent
+ * of the SAMRAI fill schedule, RungeKuttaLevelIntegrator.cpp:1568,1701. */
 int hmr_fill_ghosts_patch(hmr_ctx* ctx, const hmr_patch_geometry* geom, double* const* Q,
                           const int* periodic, void* stream);
 
@@ -165,8 +173,9 @@ int hmr_rk_substep_vjp_patch(hmr_ctx* ctx, const hmr_patch_geometry* geom, int s
                              double beta, const double* const* const* Q_int, double dt,
                              const double* const* Qbar_out, double* const* const* Qbar_int, void* stream);
 
-/* Adjoint of hmr_fill_ghosts_patch: adds the adjoint of every ghost cell to the interior cell it is
- * copied from and zeroes the ghost adjoints.  No counterpart in the reference. */
+/* Adjoint of hmr_fill_ghosts_patch: adds the adjoint of every filled ghost cell to the interior
+ * cell it is copied from and zeroes it; ghost cells along HMR_FILL_PROVIDED axes keep their
+ * adjoints (they belong to whatever supplied the values).  No counterpart in the reference. */
 int hmr_fill_ghosts_vjp_patch(hmr_ctx* ctx, const hmr_patch_geometry* geom, double* const* Qbar,
                               const int* periodic, void* stream);
 
@@ -180,8 +189,9 @@ int hmr_level_destroy(hmr_level* level);
 int hmr_level_bind_state(hmr_level* level, int patch, double* const* comps);
 /* Device pointers of the stage-`slot` state of a patch (slot 0: the bound arrays). */
 int hmr_level_state(hmr_level* level, int patch, int slot, double** comps_out);
-/* Ghost fill of a patch whose box spans the whole domain: periodic along axes with
- * periodic[a] != 0, zero-gradient on the others (default: zero-gradient everywhere). */
+/* Ghost fill mode per axis of a patch in the batched substeps (hmr_fill_mode; default
+ * HMR_FILL_ZERO_GRADIENT): HMR_FILL_PERIODIC for a patch spanning a periodic direction,
+ * HMR_FILL_PROVIDED where the caller supplies the ghost cells. */
 int hmr_level_set_periodic(hmr_level* level, int patch, const int* periodic);
 /* Runs substep `stage` (0..2 of SSPRK3) for all patches as one captured CUDA graph (barrier
  * reset + one persistent kernel: ghost fill, cells, sensor, faces, update).  Reads slots
