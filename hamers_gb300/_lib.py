@@ -20,6 +20,7 @@ HMR_ERR_NO_DEVICE = -3
 HMR_ERR_STATE = -4
 HMR_ERR_BARRIER = -5
 HMR_ERR_CAPACITY = -6
+HMR_FILL_ZERO_GRADIENT, HMR_FILL_PERIODIC, HMR_FILL_PROVIDED = 0, 1, 2
 
 HMR_SINGLE_SPECIES = 0
 HMR_FOUR_EQN_CONSERVATIVE = 1
@@ -37,6 +38,7 @@ EXPORTS = [
     "hmr_level_destroy", "hmr_level_bind_state", "hmr_level_set_periodic", "hmr_level_state",
     "hmr_level_substep", "hmr_level_step", "hmr_level_check", "hmr_level_barrier_diagnostic", "hmr_level_autotune",
     "hmr_rk_substep_patch_noalloc", "hmr_rk_substep_vjp_patch", "hmr_fill_ghosts_vjp_patch",
+    "hmr_spectral_radius_patch", "hmr_level_step_cfl", "hmr_level_last_dt",
 ]
 
 
@@ -122,6 +124,9 @@ def load():
     L.hmr_rk_substep_vjp_patch.argtypes = [vp, gp, ctypes.c_int, dp, ctypes.c_double, DPPP, ctypes.c_double,
                                            DPP, DPPP, vp]
     L.hmr_fill_ghosts_vjp_patch.argtypes = [vp, gp, DPP, ip, vp]
+    L.hmr_spectral_radius_patch.argtypes = [vp, gp, DPP, dp, vp]
+    L.hmr_level_step_cfl.argtypes = [vp, ctypes.c_double, vp]
+    L.hmr_level_last_dt.argtypes = [vp, dp]
     for name in EXPORTS:
         getattr(L, name).restype = ctypes.c_int
     _lib = L

@@ -48,6 +48,11 @@ struct hmr_level {
     bool graph_ok[3] = {false, false, false};
     bool dirty = true;                 // worklist changed since it was uploaded
     int bound = 0;                     // patches whose slot 0 is bound
+    // step with the stable time step computed on the device (spectral radius -> dt -> 3 substeps)
+    unsigned long long* d_srmax = nullptr;
+    double* d_dt = nullptr;
+    cudaGraphExec_t cfl_graph = nullptr;
+    double cfl_graph_cfl = 0.0;
 };
 
 static int cuda_status(cudaError_t e) { return e == cudaSuccess ? HMR_OK : (int)e; }
@@ -410,6 +415,16 @@ int hmr_rk_substep_vjp_patch(hmr_ctx* c, const hmr_patch_geometry* pg, int stage
     return hmr_vjp::launch_vjp(c->v, c->P, g, S, A, st);
 }
 
+int hmr_spectral_radius_patch(hmr_ctx* c, const hmr_patch_geometry* pg, const double* const* Q, double* d_max,
+                              void* stream) {
+    if (!c || !valid_geom(c->v.dim, pg) || !d_max) return HMR_ERR_ARGUMENT;
+    Comp q;
+    if (!load_comp(q, Q, c->ncomp)) return HMR_ERR_ARGUMENT;
+    const Geom g = make_geom(c->v.dim, pg);
+    return hmr_cells::launch_spectral_patch(c->v, c->P, g, q, reinterpret_cast<unsigned long long*>(d_max),
+                                            as_stream(stream));
+}
+
 int hmr_fill_ghosts_vjp_patch(hmr_ctx* c, const hmr_patch_geometry* pg, double* const* Qbar, const int* periodic,
                               void* stream) {
     if (!c || !valid_geom(c->v.dim, pg)) return HMR_ERR_ARGUMENT;
@@ -449,6 +464,7 @@ static LevelArgs stage_args(hmr_level* lv, int stage, double dt) {
     L.nst = stage + 1;
     L.beta = RK3_BETA[stage];
     L.dt = dt;
+    L.dt_dev = nullptr;
     L.barrier = lv->d_barrier;
     L.status = lv->d_status;
     L.redo.list = lv->d_redo;
@@ -491,6 +507,8 @@ static void level_drop_graphs(hmr_level* lv) {
         lv->graph[s] = nullptr;
         lv->graph_ok[s] = false;
     }
+    if (lv->cfl_graph) cudaGraphExecDestroy(lv->cfl_graph);
+    lv->cfl_graph = nullptr;
 }
 
 // Captures (memset + persistent kernel) of one substep into a graph.
@@ -569,6 +587,8 @@ int hmr_level_create(hmr_ctx* c, int np, const hmr_patch_geometry* geoms, hmr_le
     if (e == cudaSuccess) e = cudaMalloc(&lv->d_barrier, 2 * sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMalloc(&lv->d_status, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(lv->d_status, 0, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&lv->d_srmax, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc(&lv->d_dt, sizeof(double));
     if (e != cudaSuccess) {
         hmr_level_destroy(lv);
         return cuda_status(e);
@@ -613,6 +633,8 @@ int hmr_level_destroy(hmr_level* lv) {
     if (lv->d_barrier) cudaFree(lv->d_barrier);
     if (lv->d_status) cudaFree(lv->d_status);
     if (lv->d_redo) cudaFree(lv->d_redo);
+    if (lv->d_srmax) cudaFree(lv->d_srmax);
+    if (lv->d_dt) cudaFree(lv->d_dt);
     delete lv;
     return HMR_OK;
 }
@@ -663,6 +685,70 @@ int hmr_level_step(hmr_level* lv, double dt, void* stream) {
         if (r) return r;
     }
     return HMR_OK;
+}
+
+// One graph: running max of the spectral radius over the slot-0 states -> dt = (1/max)*cfl on
+// the device -> the three substeps reading that dt.
+static int level_capture_cfl(hmr_level* lv, double cfl) {
+    if (lv->cfl_graph) {
+        cudaGraphExecDestroy(lv->cfl_graph);
+        lv->cfl_graph = nullptr;
+    }
+    hmr_ctx* c = lv->ctx;
+    cudaStream_t cs;
+    cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_status(e);
+    cudaGraph_t graph = nullptr;
+    int r = cuda_status(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    if (r == HMR_OK) {
+        r = cuda_status(cudaMemsetAsync(lv->d_srmax, 0, sizeof(unsigned long long), cs));
+        if (r == HMR_OK)
+            r = hmr_cells::launch_spectral_level(c->v, c->P, lv->d_work, lv->npatch, lv->L.total_update,
+                                                 lv->d_srmax, cs);
+        if (r == HMR_OK) r = hmr_cells::launch_stable_dt(lv->d_srmax, cfl, lv->d_dt, cs);
+        for (int stage = 0; stage < 3 && r == HMR_OK; stage++) {
+            r = cuda_status(cudaMemsetAsync(lv->d_barrier, 0, 2 * sizeof(unsigned int), cs));
+            if (r != HMR_OK) break;
+            LevelArgs L = stage_args(lv, stage, 0.0);
+            L.dt_dev = lv->d_dt;
+            r = c->precision == HMR_PRECISION_EXACT
+                ? hmr_exact::launch_level(c->v, c->P, L, lv->blocks, lv->threads, cs)
+                : hmr_fast::launch_level(c->v, c->P, L, lv->blocks, lv->threads, cs);
+        }
+        cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
+        if (r == HMR_OK && e2 != cudaSuccess) r = cuda_status(e2);
+    }
+    if (r == HMR_OK) {
+        e = cudaGraphInstantiate(&lv->cfl_graph, graph, 0);
+        if (e != cudaSuccess) r = cuda_status(e);
+    }
+    if (graph) cudaGraphDestroy(graph);
+    cudaStreamDestroy(cs);
+    if (r == HMR_OK) lv->cfl_graph_cfl = cfl;
+    return r;
+}
+
+int hmr_level_step_cfl(hmr_level* lv, double cfl, void* stream) {
+    if (!lv || !(cfl > 0.0)) return HMR_ERR_ARGUMENT;
+    if (lv->bound != lv->npatch) return HMR_ERR_STATE;
+    if (lv->dirty) {
+        int r = level_upload(lv);
+        if (r) return r;
+        if (lv->cfl_graph) {
+            cudaGraphExecDestroy(lv->cfl_graph);
+            lv->cfl_graph = nullptr;
+        }
+    }
+    if (!lv->cfl_graph || lv->cfl_graph_cfl != cfl) {
+        int r = level_capture_cfl(lv, cfl);
+        if (r) return r;
+    }
+    return cuda_status(cudaGraphLaunch(lv->cfl_graph, as_stream(stream)));
+}
+
+int hmr_level_last_dt(hmr_level* lv, double* dt) {
+    if (!lv || !dt) return HMR_ERR_ARGUMENT;
+    return cuda_status(cudaMemcpy(dt, lv->d_dt, sizeof(double), cudaMemcpyDeviceToHost));
 }
 
 int hmr_level_check(hmr_level* lv) {

@@ -166,6 +166,108 @@ int launch_fill_vjp(int dim, const Geom& g, const Comp& Qb, int ncomp, const int
 }
 
 // ---------------------------------------------------------------------------
+// Stable time step: spectral radius sum_d (|u_d| + c)/dx_d, max over interior cells
+// (Euler.cpp:489-900: MAX_WAVE_SPEED_d = |u_d| + c, FlowModelSingleSpecies.cpp:3959;
+// spectral radius max_lambda_d/dx_d, summed over the directions in axis order; the
+// level's dt is the minimum over patches of 1/max times the CFL number,
+// RungeKuttaLevelIntegrator.cpp:1846-1916).  The max of non-negative doubles is taken
+// on their bit patterns, which order like the values; the result does not depend on
+// the order of the reduction.
+// ---------------------------------------------------------------------------
+template <int DIM, int MODEL, int NSP>
+__device__ __forceinline__ double spectral_cell(const Params& P, const Geom& g, const Comp& Q, long x) {
+    using M = Model<DIM, MODEL, NSP>;
+    double q[M::NCOMP], V[M::NEQ], rho, cs;
+#pragma unroll
+    for (int e = 0; e < M::NCOMP; e++) q[e] = Q.p[e][x];
+    cell_derived<DIM, MODEL, NSP>(P, q, V, rho, cs);
+    double s = add_(fabs(V[M::IU]), cs)/g.dx[0];
+#pragma unroll
+    for (int d = 1; d < DIM; d++) s = add_(s, add_(fabs(V[M::IU + d]), cs)/g.dx[d]);
+    return s;
+}
+
+__device__ __forceinline__ void block_max_to(double v, unsigned long long* d_max) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    __shared__ double s_w[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) s_w[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        v = lane < nw ? s_w[lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (lane == 0 && v > 0.0) atomicMax(d_max, (unsigned long long)__double_as_longlong(v));
+    }
+}
+
+template <int DIM, int MODEL, int NSP>
+__global__ void __launch_bounds__(THREADS) spectral_patch_kernel(Params P, Geom g, Comp Q, unsigned long long* d_max) {
+    const long n = ninterior_of(g);
+    double m = 0.0;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % g.n[0]), j = (int)((t / g.n[0]) % g.n[1]);
+        const int k = DIM == 3 ? (int)(t / ((long)g.n[0] * g.n[1])) : 0;
+        m = fmax(m, spectral_cell<DIM, MODEL, NSP>(P, g, Q, cidx<DIM>(g, i, j, k)));
+    }
+    block_max_to(m, d_max);
+}
+
+template <int DIM, int MODEL, int NSP>
+__global__ void __launch_bounds__(THREADS) spectral_level_kernel(Params P, const PatchWork* W, int np, long total,
+                                                                  unsigned long long* d_max) {
+    double m = 0.0;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        int lo = 0, hi = np - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (W[mid].off_update <= t) lo = mid;
+            else hi = mid - 1;
+        }
+        const Geom& g = W[lo].g;
+        const long u = t - W[lo].off_update;
+        const int i = (int)(u % g.n[0]), j = (int)((u / g.n[0]) % g.n[1]);
+        const int k = DIM == 3 ? (int)(u / ((long)g.n[0] * g.n[1])) : 0;
+        m = fmax(m, spectral_cell<DIM, MODEL, NSP>(P, g, W[lo].Q[0], cidx<DIM>(g, i, j, k)));
+    }
+    block_max_to(m, d_max);
+}
+
+__global__ void stable_dt_kernel(const unsigned long long* d_max, double cfl, double* d_dt) {
+    const double m = __longlong_as_double((long long)*d_max);
+    *d_dt = mul_(double(1)/m, cfl);
+}
+
+int launch_spectral_patch(const Variant& v, const Params& P, const Geom& g, const Comp& Q,
+                          unsigned long long* d_max, cudaStream_t st) {
+    return dispatch(v, [&](auto t) {
+        using T = decltype(t);
+        int blocks = grid_for(ninterior_of(g));
+        if (blocks > 4096) blocks = 4096;
+        spectral_patch_kernel<T::DIM, T::MODEL, T::NSP><<<blocks, THREADS, 0, st>>>(P, g, Q, d_max);
+        return (int)cudaPeekAtLastError();
+    });
+}
+
+int launch_spectral_level(const Variant& v, const Params& P, const PatchWork* work, int npatch, long total,
+                          unsigned long long* d_max, cudaStream_t st) {
+    return dispatch(v, [&](auto t) {
+        using T = decltype(t);
+        int blocks = grid_for(total);
+        if (blocks > 4096) blocks = 4096;
+        spectral_level_kernel<T::DIM, T::MODEL, T::NSP><<<blocks, THREADS, 0, st>>>(P, work, npatch, total, d_max);
+        return (int)cudaPeekAtLastError();
+    });
+}
+
+int launch_stable_dt(const unsigned long long* d_max, double cfl, double* d_dt, cudaStream_t st) {
+    stable_dt_kernel<<<1, 1, 0, st>>>(d_max, cfl, d_dt);
+    return (int)cudaPeekAtLastError();
+}
+
+// ---------------------------------------------------------------------------
 // General stage combination (any number of coefficient sets), one thread per
 // interior cell and equation set:  Q = 0; for n: Q += alpha_n Q_n;
 // Q += beta_n (-(F_R-F_L)/dx - ... + S_n); F += gamma_n F_n; S += gamma_n S_n.

@@ -255,7 +255,7 @@ level_kernel(Params P, LevelArgs L) {
         for (int s = 0; s < 3; s++) U.alpha[s] = L.alpha[s];
         U.nst = L.nst;
         U.beta = L.beta;
-        U.dt = L.dt;
+        U.dt = L.dt_dev ? *L.dt_dev : L.dt;
         U.Qout = w.Qout;
         U.Fout.p[0] = nullptr;   // flux/source outputs are not produced by the batched form
         U.Sout.p[0] = nullptr;

@@ -59,6 +59,7 @@ struct LevelArgs {
     unsigned long long timeout_ns;   // bound of every barrier wait
     unsigned int barrier_extra;      // diagnostic: arrivals that never come (0 in normal use)
     Redo redo;                       // faces handed from the fast to the exact form (count zeroed per launch)
+    const double* dt_dev;            // when set, the time step is read from this device value instead of dt
 };
 
 }  // namespace hmr
@@ -70,6 +71,14 @@ int launch_sensor(const hmr::Variant& v, const hmr::Geom& g, const hmr::Scratch&
 int launch_fill(int dim, const hmr::Geom& g, const hmr::Comp& Q, int ncomp, const int* periodic, cudaStream_t st);
 int launch_fill_vjp(int dim, const hmr::Geom& g, const hmr::Comp& Qb, int ncomp, const int* periodic,
                     cudaStream_t st);
+// Stable time step (Euler::computeSpectralRadiusesAndStableDtOnPatch): running max over interior
+// cells of sum_d (|u_d| + c)/dx_d into *d_max (bits of a non-negative double), per patch or over a
+// level's worklist (slot-0 states), and dt = (1/max)*cfl.
+int launch_spectral_patch(const hmr::Variant& v, const hmr::Params& P, const hmr::Geom& g, const hmr::Comp& Q,
+                          unsigned long long* d_max, cudaStream_t st);
+int launch_spectral_level(const hmr::Variant& v, const hmr::Params& P, const hmr::PatchWork* work, int npatch,
+                          long total_interior, unsigned long long* d_max, cudaStream_t st);
+int launch_stable_dt(const unsigned long long* d_max, double cfl, double* d_dt, cudaStream_t st);
 int launch_rk_stage(const hmr::Variant& v, const hmr::Geom& g, int ncoef, const double* alpha,
                     const double* beta, const double* gamma, const hmr::Comp* Qint, const hmr::FluxComp* Fint,
                     const hmr::Comp* Sint, const hmr::Comp& Qout, const hmr::FluxComp& Facc, const hmr::Comp& Sacc,

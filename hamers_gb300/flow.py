@@ -243,6 +243,17 @@ class Euler:
             rec.ctx, ctypes.byref(g), int(stage), alpha, RK3_BETA[stage][stage], qi, float(dt), qb, qbi,
             _stream_ptr(stream)))
 
+    def spectralRadius(self, patch, out=None, stream=None):
+        """Max over the interior of sum_d (|u_d| + c)/dx_d (Euler::computeSpectralRadiusesAndStableDtOnPatch);
+        max-reduced into the device scalar `out` if given (running max), else returned (synchronises)."""
+        g = patch.geometry()
+        q, _k = L.ptr_array(_comp_ptrs(patch.data, self.rec.ncomp))
+        dst = out if out is not None else torch.zeros(1, dtype=torch.float64, device=patch.data.device)
+        L.check("hmr_spectral_radius_patch", self._lib.hmr_spectral_radius_patch(
+            self.rec.ctx, ctypes.byref(g), q, ctypes.cast(ctypes.c_void_p(dst.data_ptr()), ctypes.POINTER(ctypes.c_double)),
+            _stream_ptr(stream)))
+        return None if out is not None else float(dst.item())
+
     def fillGhostsVJP(self, patch, periodic, stream=None):
         """Adjoint of fillGhosts() applied to the adjoint array patch.data."""
         g = patch.geometry()
@@ -402,6 +413,16 @@ class BatchedLevel:
     def barrier_diagnostic(self, extra_arrivals, timeout_ns):
         L.check("hmr_level_barrier_diagnostic", self._lib.hmr_level_barrier_diagnostic(
             self.level, int(extra_arrivals), int(timeout_ns)))
+
+    def step_cfl(self, cfl, stream=None):
+        """One SSPRK3 step with dt = (1/max spectral radius)*cfl computed on the device
+        from the current states (no host synchronisation)."""
+        L.check("hmr_level_step_cfl", self._lib.hmr_level_step_cfl(self.level, float(cfl), _stream_ptr(stream)))
+
+    def last_dt(self):
+        dt = ctypes.c_double()
+        L.check("hmr_level_last_dt", self._lib.hmr_level_last_dt(self.level, ctypes.byref(dt)))
+        return dt.value
 
     def step(self, dt, stream=None):
         L.check("hmr_level_step", self._lib.hmr_level_step(self.level, float(dt), _stream_ptr(stream)))

@@ -157,6 +157,14 @@ typedef enum {
 int hmr_fill_ghosts_patch(hmr_ctx* ctx, const hmr_patch_geometry* geom, double* const* Q,
                           const int* periodic, void* stream);
 
+/* Stable time step of a patch (Euler::computeSpectralRadiusesAndStableDtOnPatch,
+ * src/apps/Euler/Euler.cpp:489-900): the maximum over interior cells of
+ * sum_d (|u_d| + c)/dx_d is max-reduced into *d_max (a device double holding a non-negative
+ * value: 0.0 to start, or a previous patch's value for a running maximum over a level).
+ * The level's time step is then (1/max)*CFL (RungeKuttaLevelIntegrator.cpp:1846-1916). */
+int hmr_spectral_radius_patch(hmr_ctx* ctx, const hmr_patch_geometry* geom, const double* const* Q,
+                              double* d_max, void* stream);
+
 /* Adjoint (vector-Jacobian product) of hmr_rk_substep_patch.  No counterpart in the reference,
  * which has no derivative code.  For the adjoint Qbar_out of the substep's output (ghost-box
  * arrays; interior read) it accumulates into Qbar_int[n] (n = 0..stage, ghost boxes, caller
@@ -202,6 +210,13 @@ int hmr_level_substep(hmr_level* level, int stage, double dt, void* stream);
 int hmr_level_step(hmr_level* level, double dt, void* stream);
 /* Synchronises and reports whether a barrier of a persistent kernel gave up
  * (HMR_ERR_BARRIER, flag cleared) since the last check. */
+/* One SSPRK3 step whose time step is computed on the device from the slot-0 states,
+ * dt = (1/max spectral radius)*cfl over every patch of the level, inside the same captured
+ * graph as the three substeps: no host synchronisation per step.  The graph is cached for
+ * the cfl value. */
+int hmr_level_step_cfl(hmr_level* level, double cfl, void* stream);
+/* Time step used by the last hmr_level_step_cfl (synchronises). */
+int hmr_level_last_dt(hmr_level* level, double* dt);
 int hmr_level_check(hmr_level* level);
 /* Diagnostic: bound every barrier wait by timeout_ns and, with extra_arrivals = 1, make the
  * first barrier unreachable so that the give-up path can be tested.  Use (0, 2e9) to restore. */

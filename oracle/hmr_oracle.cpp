@@ -160,6 +160,31 @@ int hmro_rk3_advance(const hmro_config* cfg, const int* n, const double* dx, dou
     return 0;
 }
 
+// Euler::computeSpectralRadiusesAndStableDtOnPatch (Euler.cpp:489-900) for one
+// patch: max over interior cells of sum_d (|u_d| + c)/dx_d (max wave speed
+// |u_d| + c, FlowModelSingleSpecies.cpp:3959 and the other models' analogues).
+double hmro_spectral_radius(const hmro_config* cfg, const int* n, const double* dx, const double* Q) {
+    const Config c = to_cfg(cfg);
+    const Box b = make_box(c.dim, n, 4);
+    const int ncomp = num_comp(c);
+    std::vector<const double*> q(ncomp);
+    for (int e = 0; e < ncomp; e++) q[e] = Q + (size_t)e * b.ncell();
+    Derived<double> D;
+    compute_derived(c, b, q.data(), D);
+    const int iu = vel_index(c);
+    const long nc = b.ncell();
+    double m = 0.0;
+    for (int k = 0; k < b.n[2]; k++)
+    for (int j = 0; j < b.n[1]; j++)
+    for (int i = 0; i < b.n[0]; i++) {
+        const long x = b.cell(i, j, k);
+        double s = (std::fabs(D.V[(size_t)iu * nc + x]) + D.cs[x])/dx[0];
+        for (int d = 1; d < c.dim; d++) s = s + (std::fabs(D.V[(size_t)(iu + d) * nc + x]) + D.cs[x])/dx[d];
+        m = std::fmax(m, s);
+    }
+    return m;
+}
+
 // CPU baseline: the patch is split along its slowest axis into nthreads
 // equal sub-patches (as SAMRAI's partitioner would hand one patch to each
 // rank); every std::thread advances its own sub-patch through one RK stage

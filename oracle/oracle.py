@@ -58,6 +58,8 @@ def lib():
         L.hmro_rk3_advance.argtypes = [cp, ip, dp, ctypes.c_double, ip, ctypes.c_int, dp, lp]
         L.hmro_stage_threads.argtypes = [cp, ip, dp, ctypes.c_double, dp, ctypes.c_int]
         L.hmro_stage_threads.restype = ctypes.c_long
+        L.hmro_spectral_radius.argtypes = [cp, ip, dp, dp]
+        L.hmro_spectral_radius.restype = ctypes.c_double
         L.hmro_num_eqn.argtypes = [cp]
         L.hmro_num_comp.argtypes = [cp]
         _lib = L
@@ -229,3 +231,10 @@ def tangent_substep(cfg, n, dx, dt, stage, alpha, beta, Q_int, dQ_int):
                                        float(dt), int(stage), _dv(list(alpha)[:stage + 1]), float(beta),
                                        _dp(Qi), _dp(dQi), _dp(Qo), _dp(dQo))
     return Qo, dQo
+
+
+def spectral_radius(cfg, n, dx, Q):
+    """Max over interior cells of sum_d (|u_d| + c)/dx_d (the stable dt is (1/that)*CFL)."""
+    Q = np.ascontiguousarray(Q, dtype=np.float64)
+    return lib().hmro_spectral_radius(ctypes.byref(cfg.c()), _ip(_n3(n)), _dv(list(dx) + [1.0] * (3 - len(dx))),
+                                      _dp(Q))

@@ -2,8 +2,8 @@
 
 Checked against the oracle patch by patch (exact form: bitwise over two steps;
 fast form: 1e-12 over one substep), with uneven patch sizes, periodic and
-zero-gradient ghost fills, the launch-shape autotuner, and the bounded grid
-barrier's give-up path (a barrier that can never complete raises the level's
+zero-gradient ghost fills, the launch-shape autotuner, the stable time step
+computed on the device, and the bounded grid barrier's give-up path (a barrier that can never complete raises the level's
 error flag within its time limit, and the level works again afterwards).
 """
 import numpy as np
@@ -155,3 +155,54 @@ def test_barrier_gives_up_within_its_limit_and_level_recovers(cuda):
         sl = (slice(None),) + tuple(slice(4, -4) if a < dim else slice(None) for a in (2, 1, 0))
         assert np.array_equal(states[p].cpu().numpy()[sl], Qo[sl])
     lv.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("variant", LEVEL_CASES, ids=LEVEL_IDS)
+def test_spectral_radius_matches_oracle(cuda, variant):
+    """Euler::computeSpectralRadiusesAndStableDtOnPatch's max over the interior, bitwise."""
+    import torch
+    from hamers_gb300 import flow
+    model, dim, scheme, n, gam = variant
+    cfg = ocfg(model, dim, gam, scheme)
+    eu = flow.Euler(make(model, dim, scheme, gam, "exact"))
+    dx = [1.0 / (v + 1) for v in n]
+    Q = smooth_state(model, dim, n, seed=90, species_gamma=gam)
+    got = eu.spectralRadius(flow.Patch(n, dx, torch.from_numpy(Q).cuda()))
+    assert got == O.spectral_radius(cfg, n, dx, Q)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("variant", [VARIANTS[i] for i in (0, 6)], ids=[IDS[i] for i in (0, 6)])
+def test_cfl_step_computes_dt_on_the_device(cuda, variant):
+    """step_cfl: dt = min over patches of 1/spectral radius, times the CFL number, computed in
+    the graph; the step equals a host-driven step with that dt (exact form, bitwise)."""
+    import torch
+    from hamers_gb300 import flow
+    model, dim, scheme, _, gam = variant
+    cfg = ocfg(model, dim, gam, scheme)
+    rec = make(model, dim, scheme, gam, "exact")
+    sizes, periodic = _patches(dim, 13)
+    Q0 = [smooth_state(model, dim, n, seed=100 + p, species_gamma=gam) for p, n in enumerate(sizes)]
+    geoms = [(list(n), [1.0 / (v + p) for v in n]) for p, n in enumerate(sizes)]
+    cfl = 0.4
+    dt = min(1.0 / O.spectral_radius(cfg, n, dx, q) for (n, dx), q in zip(geoms, Q0)) * cfl
+    results = []
+    for mode in ("cfl", "host"):
+        lv = flow.BatchedLevel(rec, geoms)
+        states = [torch.from_numpy(q).cuda() for q in Q0]
+        for p, Q in enumerate(states):
+            lv.bind(p, Q)
+            lv.set_periodic(p, periodic[p])
+        if mode == "cfl":
+            lv.step_cfl(cfl)
+            torch.cuda.synchronize()
+            assert lv.last_dt() == dt
+        else:
+            lv.step(dt)
+        torch.cuda.synchronize()
+        lv.check()
+        results.append([Q.cpu().numpy() for Q in states])
+        lv.close()
+    for a, b in zip(*results):
+        assert np.array_equal(a, b)
