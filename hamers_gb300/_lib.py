@@ -38,7 +38,7 @@ EXPORTS = [
     "hmr_level_destroy", "hmr_level_bind_state", "hmr_level_set_periodic", "hmr_level_state",
     "hmr_level_substep", "hmr_level_step", "hmr_level_check", "hmr_level_barrier_diagnostic", "hmr_level_autotune",
     "hmr_rk_substep_patch_noalloc", "hmr_rk_substep_vjp_patch", "hmr_fill_ghosts_vjp_patch",
-    "hmr_spectral_radius_patch", "hmr_level_step_cfl", "hmr_level_last_dt",
+    "hmr_spectral_radius_patch", "hmr_level_step_cfl", "hmr_level_last_dt", "hmr_level_set_layout",
 ]
 
 
@@ -127,6 +127,7 @@ def load():
     L.hmr_spectral_radius_patch.argtypes = [vp, gp, DPP, dp, vp]
     L.hmr_level_step_cfl.argtypes = [vp, ctypes.c_double, vp]
     L.hmr_level_last_dt.argtypes = [vp, dp]
+    L.hmr_level_set_layout.argtypes = [vp, ip, ip, ip]
     for name in EXPORTS:
         getattr(L, name).restype = ctypes.c_int
     _lib = L

@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -49,6 +50,13 @@ struct hmr_level {
     bool dirty = true;                 // worklist changed since it was uploaded
     int bound = 0;                     // patches whose slot 0 is bound
     // step with the stable time step computed on the device (spectral radius -> dt -> 3 substeps)
+    // ghost exchange between patches (hmr_level_set_layout)
+    GhostCopy* d_copies = nullptr;
+    int ncopy = 0;
+    long total_copy = 0;
+    bool exchange = false;
+    int dom[3] = {1, 1, 1};
+    int dom_periodic[3] = {0, 0, 0};
     unsigned long long* d_srmax = nullptr;
     double* d_dt = nullptr;
     cudaGraphExec_t cfl_graph = nullptr;
@@ -465,6 +473,14 @@ static LevelArgs stage_args(hmr_level* lv, int stage, double dt) {
     L.beta = RK3_BETA[stage];
     L.dt = dt;
     L.dt_dev = nullptr;
+    L.exchange = lv->exchange ? 1 : 0;
+    L.copies = lv->d_copies;
+    L.ncopy = lv->ncopy;
+    L.total_copy = lv->total_copy;
+    for (int a = 0; a < 3; a++) {
+        L.dom[a] = lv->dom[a];
+        L.dom_periodic[a] = lv->dom_periodic[a];
+    }
     L.barrier = lv->d_barrier;
     L.status = lv->d_status;
     L.redo.list = lv->d_redo;
@@ -564,7 +580,10 @@ int hmr_level_create(hmr_ctx* c, int np, const hmr_patch_geometry* geoms, hmr_le
         scratch_tot += (scratch_doubles(c, g) + 31) / 32 * 32;
         PatchWork& w = lv->work[p];
         w.g = g;
-        for (int a = 0; a < 3; a++) w.periodic[a] = 0;
+        for (int a = 0; a < 3; a++) {
+            w.periodic[a] = 0;
+            w.lo[a] = 0;
+        }
         w.off_fill = off_fill;
         off_fill += ncell_of(g);
         w.off_cells = off_cells;
@@ -634,6 +653,7 @@ int hmr_level_destroy(hmr_level* lv) {
     if (lv->d_status) cudaFree(lv->d_status);
     if (lv->d_redo) cudaFree(lv->d_redo);
     if (lv->d_srmax) cudaFree(lv->d_srmax);
+    if (lv->d_copies) cudaFree(lv->d_copies);
     if (lv->d_dt) cudaFree(lv->d_dt);
     delete lv;
     return HMR_OK;
@@ -656,6 +676,90 @@ int hmr_level_set_periodic(hmr_level* lv, int p, const int* periodic) {
         lv->work[p].periodic[a] = a < lv->ctx->v.dim ? periodic[a] : 0;
     }
     lv->dirty = true;
+    return HMR_OK;
+}
+
+int hmr_level_set_layout(hmr_level* lv, const int* lo, const int* domain, const int* periodic) {
+    if (!lv || !lo || !domain || !periodic) return HMR_ERR_ARGUMENT;
+    const int dim = lv->ctx->v.dim;
+    int dom[3] = {1, 1, 1}, per[3] = {0, 0, 0};
+    for (int a = 0; a < dim; a++) {
+        if (domain[a] < 1 || periodic[a] < 0 || periodic[a] > 1) return HMR_ERR_ARGUMENT;
+        dom[a] = domain[a];
+        per[a] = periodic[a];
+    }
+    const int np = lv->npatch;
+    // boxes in the level's index space; they must lie in the domain and not overlap
+    std::vector<std::array<int, 3>> blo(np), bhi(np);
+    for (int p = 0; p < np; p++) {
+        for (int a = 0; a < 3; a++) {
+            blo[p][a] = a < dim ? lo[3 * p + a] : 0;
+            bhi[p][a] = blo[p][a] + lv->geoms[p].n[a];
+            if (blo[p][a] < 0 || bhi[p][a] > dom[a]) return HMR_ERR_ARGUMENT;
+        }
+    }
+    for (int p = 0; p < np; p++)
+        for (int q = p + 1; q < np; q++) {
+            bool overlap = true;
+            for (int a = 0; a < dim; a++) overlap = overlap && blo[p][a] < bhi[q][a] && blo[q][a] < bhi[p][a];
+            if (overlap) return HMR_ERR_ARGUMENT;
+        }
+    // ghost-cell copies: the ghost box of every patch against the interior of every patch
+    // and of its periodic images
+    std::vector<GhostCopy> copies;
+    long total = 0;
+    int kmax[3] = {0, 0, 0};
+    for (int a = 0; a < dim; a++)
+        if (per[a]) kmax[a] = (GHOST + dom[a] - 1) / dom[a];
+    for (int p = 0; p < np; p++) {
+        int glo[3], ghi[3];
+        for (int a = 0; a < 3; a++) {
+            glo[a] = a < dim ? blo[p][a] - GHOST : 0;
+            ghi[a] = a < dim ? bhi[p][a] + GHOST : 1;
+        }
+        for (int q = 0; q < np; q++)
+            for (int k0 = -kmax[0]; k0 <= kmax[0]; k0++)
+                for (int k1 = -kmax[1]; k1 <= kmax[1]; k1++)
+                    for (int k2 = -kmax[2]; k2 <= kmax[2]; k2++) {
+                        const int sh[3] = {k0 * dom[0], k1 * dom[1], k2 * dom[2]};
+                        if (q == p && k0 == 0 && k1 == 0 && k2 == 0) continue;
+                        GhostCopy cp;
+                        bool empty = false;
+                        for (int a = 0; a < 3; a++) {
+                            const int il = std::max(glo[a], blo[q][a] + sh[a]);
+                            const int ih = std::min(ghi[a], bhi[q][a] + sh[a]);
+                            if (ih <= il) { empty = true; break; }
+                            cp.dlo[a] = il - blo[p][a];
+                            cp.slo[a] = il - (blo[q][a] + sh[a]);
+                            cp.ext[a] = ih - il;
+                        }
+                        if (empty) continue;
+                        cp.dst = p;
+                        cp.src = q;
+                        cp.off = total;
+                        total += (long)cp.ext[0] * cp.ext[1] * cp.ext[2];
+                        copies.push_back(cp);
+                    }
+    }
+    if (lv->d_copies) cudaFree(lv->d_copies);
+    lv->d_copies = nullptr;
+    lv->ncopy = (int)copies.size();
+    lv->total_copy = total;
+    if (!copies.empty()) {
+        cudaError_t e = cudaMalloc(&lv->d_copies, copies.size() * sizeof(GhostCopy));
+        if (e == cudaSuccess)
+            e = cudaMemcpy(lv->d_copies, copies.data(), copies.size() * sizeof(GhostCopy), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cuda_status(e);
+    }
+    for (int p = 0; p < np; p++)
+        for (int a = 0; a < 3; a++) lv->work[p].lo[a] = blo[p][a];
+    for (int a = 0; a < 3; a++) {
+        lv->dom[a] = dom[a];
+        lv->dom_periodic[a] = per[a];
+    }
+    lv->exchange = true;
+    lv->dirty = true;
+    level_drop_graphs(lv);
     return HMR_OK;
 }
 

@@ -189,10 +189,39 @@ level_kernel(Params P, LevelArgs L) {
 #define HMR_BARRIER() \
     if (!grid_barrier(L.barrier, L.status, ++b, L.timeout_ns, L.barrier_extra)) return
 
-    // Phase 0: ghost fill of the input stage (periodic or zero-gradient per patch).
-    for (long t = t0; t < L.total_fill; t += stride) {
-        const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_fill; });
-        fill_item<DIM>(W[p].g, W[p].Q[L.nst - 1], L.ncomp, W[p].periodic, t - W[p].off_fill);
+    // Phase 0: ghost fill of the input stage: per patch (periodic, zero-gradient or provided
+    // per axis), or, with a level layout, copies from neighbouring patches and periodic
+    // images followed by zero-gradient at the domain's non-periodic faces.
+    if (L.exchange) {
+        const int sl = L.nst - 1;
+        for (long t = t0; t < L.total_copy; t += stride) {
+            int lo = 0, hi = L.ncopy - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (L.copies[mid].off <= t) lo = mid;
+                else hi = mid - 1;
+            }
+            const GhostCopy& cp = L.copies[lo];
+            const long u = t - cp.off;
+            const int a0 = (int)(u % cp.ext[0]);
+            const int a1 = (int)((u / cp.ext[0]) % cp.ext[1]);
+            const int a2 = (int)(u / ((long)cp.ext[0] * cp.ext[1]));
+            const PatchWork& wd = W[cp.dst];
+            const PatchWork& ws = W[cp.src];
+            const long xd = cidx<DIM>(wd.g, cp.dlo[0] + a0, cp.dlo[1] + a1, cp.dlo[2] + a2);
+            const long xs = cidx<DIM>(ws.g, cp.slo[0] + a0, cp.slo[1] + a1, cp.slo[2] + a2);
+            for (int e = 0; e < L.ncomp; e++) wd.Q[sl].p[e][xd] = ws.Q[sl].p[e][xs];
+        }
+        HMR_BARRIER();
+        for (long t = t0; t < L.total_fill; t += stride) {
+            const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_fill; });
+            domain_fill_item<DIM>(W[p].g, W[p].Q[sl], L.ncomp, W[p].lo, L.dom, L.dom_periodic, t - W[p].off_fill);
+        }
+    } else {
+        for (long t = t0; t < L.total_fill; t += stride) {
+            const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_fill; });
+            fill_item<DIM>(W[p].g, W[p].Q[L.nst - 1], L.ncomp, W[p].periodic, t - W[p].off_fill);
+        }
     }
     HMR_BARRIER();
     for (long t = t0; t < L.total_cells; t += stride) {

@@ -461,4 +461,30 @@ __device__ __forceinline__ void fill_item(const Geom& g, const Comp& Q, int ncom
     for (int e = 0; e < ncomp; e++) Q.p[e][x] = Q.p[e][y];
 }
 
+// Zero-gradient fill at the non-periodic faces of the level's domain for a patch with
+// known position: ghost cell c (local) of a patch at level index lo takes the value of
+// the nearest in-domain cell (clamped along the axes where it lies outside the domain),
+// which is the patch's own interior or a ghost cell filled from a neighbour before.
+// Ghost cells inside the domain are left alone (neighbour copies or provided values).
+template <int DIM>
+__device__ __forceinline__ void domain_fill_item(const Geom& g, const Comp& Q, int ncomp, const int* lo,
+                                                 const int* dom, const int* dom_periodic, long x) {
+    int c[3], s[3];
+    c[0] = (int)(x % g.G[0]) - GHOST;
+    c[1] = (int)((x / g.G[0]) % g.G[1]) - GHOST;
+    c[2] = DIM == 3 ? (int)(x / ((long)g.G[0] * g.G[1])) - GHOST : 0;
+    bool physical = false;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        s[a] = c[a];
+        if (a >= DIM || dom_periodic[a]) continue;
+        const int G = lo[a] + c[a];
+        if (G < 0) { s[a] = -lo[a]; physical = true; }
+        else if (G >= dom[a]) { s[a] = dom[a] - 1 - lo[a]; physical = true; }
+    }
+    if (!physical) return;
+    const long y = cidx<DIM>(g, s[0], s[1], s[2]);
+    for (int e = 0; e < ncomp; e++) Q.p[e][x] = Q.p[e][y];
+}
+
 }  // namespace hmr

@@ -37,12 +37,22 @@ struct PatchWork {
     Scratch S;
     Comp Q[3];        // stage states (ghost box)
     Comp Qout;        // output of the substep
-    int periodic[3];  // ghost fill of a patch that spans the domain: periodic axes (else zero-gradient)
+    int periodic[3];  // own ghost fill per axis (hmr_fill_mode) when the level has no layout
+    int lo[3];        // first interior cell in the level's index space (layout set)
     long off_fill;    // prefix offsets of the item counts, per phase
     long off_cells;
     long off_sensor;
     long off_face[3];
     long off_update;
+};
+
+// One box of ghost cells of patch dst copied from the interior of patch src (possibly a
+// periodic image): dst-local start dlo, src-local start slo, extent ext; off = prefix
+// offset of its cells in the flat copy index space.
+struct GhostCopy {
+    int dst, src;
+    int dlo[3], slo[3], ext[3];
+    long off;
 };
 
 struct LevelArgs {
@@ -60,6 +70,14 @@ struct LevelArgs {
     unsigned int barrier_extra;      // diagnostic: arrivals that never come (0 in normal use)
     Redo redo;                       // faces handed from the fast to the exact form (count zeroed per launch)
     const double* dt_dev;            // when set, the time step is read from this device value instead of dt
+    // ghost exchange between the patches of the level (hmr_level_set_layout): copies from
+    // neighbours and periodic images, then zero-gradient at the domain's non-periodic faces
+    int exchange;
+    const GhostCopy* copies;         // device array
+    int ncopy;
+    long total_copy;
+    int dom[3];                      // domain extent in cells
+    int dom_periodic[3];
 };
 
 }  // namespace hmr

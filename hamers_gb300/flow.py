@@ -402,6 +402,18 @@ class BatchedLevel:
         L.check("hmr_level_substep", self._lib.hmr_level_substep(self.level, int(stage), float(dt),
                                                                  _stream_ptr(stream)))
 
+    def set_layout(self, lo, domain, periodic):
+        """Patch positions (first interior cell per patch, level index space), the domain's cells
+        per axis and its periodic axes: enables the ghost exchange between patches."""
+        dim = self.rec.flow_model.dim
+        flat = []
+        for p in range(self.npatch):
+            flat += list(lo[p][:dim]) + [0] * (3 - dim)
+        lo_a = (ctypes.c_int * len(flat))(*flat)
+        dom = (ctypes.c_int * 3)(*(list(domain) + [1] * (3 - len(domain))))
+        per = (ctypes.c_int * 3)(*(list(periodic) + [0] * (3 - len(periodic))))
+        L.check("hmr_level_set_layout", self._lib.hmr_level_set_layout(self.level, lo_a, dom, per))
+
     def set_periodic(self, patch, periodic):
         per = (ctypes.c_int * 3)(*(list(periodic) + [0] * (3 - len(periodic))))
         L.check("hmr_level_set_periodic", self._lib.hmr_level_set_periodic(self.level, int(patch), per))

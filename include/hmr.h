@@ -193,6 +193,15 @@ int hmr_fill_ghosts_vjp_patch(hmr_ctx* ctx, const hmr_patch_geometry* geom, doub
  * the intermediate stage buffers (slots 1, 2), the scratch and the captured step graph. */
 int hmr_level_create(hmr_ctx* ctx, int num_patches, const hmr_patch_geometry* geoms, hmr_level** out);
 int hmr_level_destroy(hmr_level* level);
+/* Places the level's patches in its index space and enables the device-resident ghost exchange
+ * (the same-level part of SAMRAI's fill schedule, RungeKuttaLevelIntegrator.cpp:1568,1701):
+ * before every substep the ghost cells of each patch are copied from the interiors of the
+ * patches (and of their periodic images) that cover them, then cells outside the domain along
+ * non-periodic axes take the nearest in-domain value (zero-gradient, the extrapolation boundary);
+ * ghost cells inside the domain covered by no patch of the level (a coarse-fine boundary) are
+ * left as the caller provides them.  lo: 3 ints per patch (first interior cell), domain: cells
+ * per axis, periodic: 0/1 per axis.  Boxes must lie in the domain and not overlap. */
+int hmr_level_set_layout(hmr_level* level, const int* lo, const int* domain, const int* periodic);
 /* Binds the caller's ghost-box arrays (ncomp device pointers) as slot 0 of a patch. */
 int hmr_level_bind_state(hmr_level* level, int patch, double* const* comps);
 /* Device pointers of the stage-`slot` state of a patch (slot 0: the bound arrays). */
