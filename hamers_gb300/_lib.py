@@ -27,6 +27,8 @@ HMR_FOUR_EQN_CONSERVATIVE = 1
 HMR_FIVE_EQN_ALLAIRE = 2
 HMR_WCNS5_JS_HLLC_HLL = 0
 HMR_WCNS6_LD_HLLC_HLL = 1
+HMR_WCNS5_Z_HLLC_HLL = 2
+HMR_WCNS6_CU_M2_HLLC_HLL = 3
 HMR_PRECISION_FAST = 0
 HMR_PRECISION_EXACT = 1
 
@@ -55,6 +57,9 @@ class Config(ctypes.Structure):
         ("constant_C", ctypes.c_double),
         ("constant_alpha_tau", ctypes.c_double),
         ("precision", ctypes.c_int),
+        ("constant_Chi", ctypes.c_double),
+        ("constant_epsilon", ctypes.c_double),
+        ("grid_dx", ctypes.c_double * 3),
     ]
 
 

@@ -2,8 +2,9 @@
 
 hmr_faces.cu is compiled once per arithmetic form -- the exact form
 (-DHMR_FAST=0 --fmad=false, the reference's operation order, bitwise equal to
-it) and the fast form (-DHMR_FAST=1) -- and flow model (-DHMR_MODEL=0/1/2), six
-translation units compiled in parallel.  The cell-data kernels are always exact.
+it) and the fast form (-DHMR_FAST=1) -- flow model (-DHMR_MODEL=0/1/2) and
+scheme set (-DHMR_SCHEME_SET=0: WCNS5-JS/WCNS6-LD, 1: WCNS5-Z/WCNS6-CU-M2),
+twelve translation units compiled in parallel.  The cell-data kernels are always exact.
 """
 import os
 import shutil
@@ -24,9 +25,10 @@ UNITS = [
     ("hmr_abi.cu", "hmr_abi.o", ["-DHMR_FAST=0", "--fmad=false"]),
     ("hmr_noalloc.cu", "hmr_noalloc.o", ["-DHMR_FAST=0", "--fmad=false"]),
 ] + [
-    ("hmr_faces.cu", "hmr_faces_%s_m%d.o" % (form, model),
-     ["-DHMR_FAST=%d" % fast, "--fmad=%s" % ("true" if fast else "false"), "-DHMR_MODEL=%d" % model])
-    for form, fast in (("exact", 0), ("fast", 1)) for model in (0, 1, 2)
+    ("hmr_faces.cu", "hmr_faces_%s_m%d_s%d.o" % (form, model, sset),
+     ["-DHMR_FAST=%d" % fast, "--fmad=%s" % ("true" if fast else "false"), "-DHMR_MODEL=%d" % model,
+      "-DHMR_SCHEME_SET=%d" % sset])
+    for form, fast in (("exact", 0), ("fast", 1)) for model in (0, 1, 2) for sset in (0, 1)
 ] + [
     ("hmr_vjp.cu", "hmr_vjp_m%d.o" % model, ["-DHMR_FAST=0", "--fmad=true", "-DHMR_MODEL=%d" % model])
     for model in (0, 1, 2)

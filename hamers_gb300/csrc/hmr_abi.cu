@@ -181,8 +181,11 @@ int hmr_config_default(hmr_config* cfg, int flow_model, int reconstructor, int d
     cfg->convective_flux_reconstructor = reconstructor;
     cfg->constant_p = 2;
     cfg->constant_q = 4;
-    cfg->constant_C = 1.0e9;
+    // WCNS6-CU-M2-HLLC-HLL.cpp:252-270; the other schemes' C is WCNS6-LD's
+    cfg->constant_C = reconstructor == HMR_WCNS6_CU_M2_HLLC_HLL ? 1000.0 : 1.0e9;
     cfg->constant_alpha_tau = 35.0;
+    cfg->constant_Chi = 1.0e8;
+    cfg->constant_epsilon = 1.0e-8;
     cfg->precision = HMR_PRECISION_FAST;
     return HMR_OK;
 }
@@ -192,12 +195,13 @@ int hmr_ctx_create(const hmr_config* cfg, hmr_ctx** out) {
     *out = nullptr;
     if (cfg->dim != 2 && cfg->dim != 3) return HMR_ERR_ARGUMENT;
     if (cfg->num_species < 1 || cfg->num_species > HMR_MAX_SPECIES) return HMR_ERR_ARGUMENT;
-    if (cfg->convective_flux_reconstructor != HMR_WCNS5_JS_HLLC_HLL &&
-        cfg->convective_flux_reconstructor != HMR_WCNS6_LD_HLLC_HLL)
-        return HMR_ERR_UNSUPPORTED;
+    if (!reconstructor_known(cfg->convective_flux_reconstructor)) return HMR_ERR_UNSUPPORTED;
     if (cfg->precision != HMR_PRECISION_FAST && cfg->precision != HMR_PRECISION_EXACT) return HMR_ERR_ARGUMENT;
-    if (cfg->constant_p < 1 || cfg->constant_p > 8 || cfg->constant_q < 1 || cfg->constant_q > 8)
-        return HMR_ERR_ARGUMENT;
+    {
+        Params probe;  // scheme constants in range (and, for WCNS6-CU-M2, the grid spacing set)
+        const int r = scheme_params(cfg, probe);
+        if (r) return r;
+    }
     int neq = 0, ncomp = 0;
     if (cfg->flow_model == HMR_SINGLE_SPECIES) {
         if (cfg->num_species != 1) return HMR_ERR_ARGUMENT;
@@ -230,10 +234,7 @@ int hmr_ctx_create(const hmr_config* cfg, hmr_ctx** out) {
     c->v.nsp = cfg->num_species;
     c->v.scheme = cfg->convective_flux_reconstructor;
     species_params(cfg->species_gamma, cfg->species_R, cfg->num_species, c->P);
-    c->P.p = cfg->constant_p;
-    c->P.q = cfg->constant_q;
-    c->P.C = cfg->constant_C;
-    c->P.alpha_tau = cfg->constant_alpha_tau;
+    scheme_params(cfg, c->P);
     c->precision = cfg->precision;
     c->neq = neq;
     c->ncomp = ncomp;

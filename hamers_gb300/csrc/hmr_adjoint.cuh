@@ -282,6 +282,152 @@ __device__ __forceinline__ void ld_pair_bwd(const double* U, const double* b, co
 }
 
 // ----------------------------------------------------------------------------
+// WCNS5-Z, one side: S[0..4] from the upwind side, b[0..2] its indicators.
+// w_k = u_k/sum u, u_k = d_k (1 + x_k^p), x_k = tau_5/(b_k + eps), tau_5 = |b_0 - b_2|.
+// ----------------------------------------------------------------------------
+__device__ __forceinline__ void z_side_bwd(int p, const double* S, const double* b, double obar, double* Sb) {
+    const double du[3] = {1.0/16.0, 5.0/8.0, 5.0/16.0};
+    const double tau_5 = fabs(sub_(b[0], b[2]));
+    double r[3], x[3], px1[3], ur[3], Us = 0.0;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        r[k] = double(1)/(b[k] + HMR_EPS);
+        x[k] = tau_5*r[k];
+        px1[k] = ipow0(x[k], p - 1);
+        ur[k] = du[k]*(1.0 + px1[k]*x[k]);
+        Us += ur[k];
+    }
+    const double iUs = double(1)/Us;
+    const double w[3] = {ur[0]*iUs, ur[1]*iUs, ur[2]*iUs};
+    const double q[3] = {3.0/8.0*S[0] - 10.0/8.0*S[1] + 15.0/8.0*S[2],
+                         -1.0/8.0*S[1] + 6.0/8.0*S[2] + 3.0/8.0*S[3],
+                         3.0/8.0*S[2] + 6.0/8.0*S[3] - 1.0/8.0*S[4]};
+    Sb[0] += obar*(3.0/8.0*w[0]);
+    Sb[1] += obar*(-10.0/8.0*w[0] - 1.0/8.0*w[1]);
+    Sb[2] += obar*(15.0/8.0*w[0] + 6.0/8.0*w[1] + 3.0/8.0*w[2]);
+    Sb[3] += obar*(3.0/8.0*w[1] + 6.0/8.0*w[2]);
+    Sb[4] += obar*(-1.0/8.0*w[2]);
+    const double out = w[0]*q[0] + w[1]*q[1] + w[2]*q[2];
+    double bb[3], taub = 0.0;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        // d out/d u_k = (q_k - out)/sum u
+        const double xb = obar*(q[k] - out)*iUs*du[k]*p*px1[k];
+        taub += xb*r[k];
+        bb[k] = -xb*tau_5*r[k]*r[k];
+    }
+    const double s5 = sgn_(b[0] - b[2]);
+    bb[0] += taub*s5;
+    bb[2] -= taub*s5;
+    js_betas_bwd(S, bb[0], bb[1], bb[2], Sb);
+}
+
+// Forward of both sides (the operations of z_pair<true>) keeping the indicators:
+// b[0..2] minus side, b[3..5] plus side.
+__device__ __forceinline__ void z_pair_keep(const double* U, int p, double& Um, double& Up, double* b) {
+    js_betas_x(U[0], U[1], U[2], U[3], U[4], b[0], b[1], b[2]);
+    Um = z_interp<true>(b[0], b[1], b[2], p, U[0], U[1], U[2], U[3], U[4]);
+    js_betas_x(U[5], U[4], U[3], U[2], U[1], b[3], b[4], b[5]);
+    Up = z_interp<true>(b[3], b[4], b[5], p, U[5], U[4], U[3], U[2], U[1]);
+}
+
+__device__ __forceinline__ void z_pair_bwd(const double* U, const double* b, int p, double Umb, double Upb,
+                                           double* Ub) {
+    double Sb[5] = {0, 0, 0, 0, 0};
+    z_side_bwd(p, U, b, Umb, Sb);
+#pragma unroll
+    for (int j = 0; j < 5; j++) Ub[j] += Sb[j];
+    const double R[5] = {U[5], U[4], U[3], U[2], U[1]};
+    double Rb[5] = {0, 0, 0, 0, 0};
+    z_side_bwd(p, R, b + 3, Upb, Rb);
+#pragma unroll
+    for (int j = 0; j < 5; j++) Ub[5 - j] += Rb[j];
+}
+
+// ----------------------------------------------------------------------------
+// WCNS6-CU-M2, one side: S[0..5] from the upwind side, b[0..3] its indicators,
+// ce = eps dx^2 and cx = Chi dx^2 of the face's axis.
+// w_k = o_k/sum o, o_k = dc_k y_k^q, y_k = C + tau_6 (beta_avg + cx)/((b_k + ce)(b_k + cx)),
+// beta_avg = (b_0 + b_2 + 6 b_1)/8, tau_6 = |b_3 - beta_avg|.
+// ----------------------------------------------------------------------------
+__device__ __forceinline__ void cu_side_bwd(const Params& P, double ce, double cx, const double* S, const double* b,
+                                            double obar, double* Sb) {
+    const double dc[4] = {1.0/32.0, 15.0/32.0, 15.0/32.0, 1.0/32.0};
+    const double beta_avg = mul_(double(1)/double(8), add_(add_(b[0], b[2]), mul_(double(6), b[1])));
+    const double tau_6 = fabs(sub_(b[3], beta_avg));
+    const double ax = beta_avg + cx;
+    double ek[4], xk[4], g[4], py1[4], orw[4], Os = 0.0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        ek[k] = double(1)/(b[k] + ce);
+        xk[k] = double(1)/(b[k] + cx);
+        g[k] = tau_6*ax*ek[k]*xk[k];
+        const double y = P.C + g[k];
+        py1[k] = ipow0(y, P.q - 1);
+        orw[k] = dc[k]*py1[k]*y;
+        Os += orw[k];
+    }
+    const double iOs = double(1)/Os;
+    double w[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) w[k] = orw[k]*iOs;
+    const double q[4] = {3.0/8.0*S[0] - 10.0/8.0*S[1] + 15.0/8.0*S[2],
+                         -1.0/8.0*S[1] + 6.0/8.0*S[2] + 3.0/8.0*S[3],
+                         3.0/8.0*S[2] + 6.0/8.0*S[3] - 1.0/8.0*S[4],
+                         15.0/8.0*S[3] - 10.0/8.0*S[4] + 3.0/8.0*S[5]};
+    Sb[0] += obar*(3.0/8.0*w[0]);
+    Sb[1] += obar*(-10.0/8.0*w[0] - 1.0/8.0*w[1]);
+    Sb[2] += obar*(15.0/8.0*w[0] + 6.0/8.0*w[1] + 3.0/8.0*w[2]);
+    Sb[3] += obar*(3.0/8.0*w[1] + 6.0/8.0*w[2] + 15.0/8.0*w[3]);
+    Sb[4] += obar*(-1.0/8.0*w[2] - 10.0/8.0*w[3]);
+    Sb[5] += obar*(3.0/8.0*w[3]);
+    const double out = w[0]*q[0] + w[1]*q[1] + w[2]*q[2] + w[3]*q[3];
+    double bb[4], tau6b = 0.0, axb = 0.0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const double yb = obar*(q[k] - out)*iOs*dc[k]*P.q*py1[k];
+        const double ex = ek[k]*xk[k];
+        tau6b += yb*ax*ex;
+        axb += yb*tau_6*ex;
+        bb[k] = -yb*g[k]*(ek[k] + xk[k]);
+    }
+    const double s6 = sgn_(b[3] - beta_avg);
+    bb[3] += tau6b*s6;
+    const double bavgb = axb - tau6b*s6;
+    bb[0] += bavgb/8.0;
+    bb[2] += bavgb/8.0;
+    bb[1] += bavgb*6.0/8.0;
+    js_betas_bwd(S, bb[0], bb[1], bb[2], Sb);
+    ld_beta3_bwd(S, bb[3], Sb);
+}
+
+// Forward of both sides (the operations of cu_pair<true, A>) keeping the
+// indicators: b[0..3] minus side, b[4..7] plus side.
+template <int A>
+__device__ __forceinline__ void cu_pair_keep(const double* U, const Params& P, double& Um, double& Up, double* b) {
+    js_betas_x(U[0], U[1], U[2], U[3], U[4], b[0], b[1], b[2]);
+    b[3] = ld_beta3(U[0], U[1], U[2], U[3], U[4], U[5]);
+    Um = cu_interp<true>(b, P, P.cu_e[A], P.cu_x[A], U[0], U[1], U[2], U[3], U[4], U[5]);
+    js_betas_x(U[5], U[4], U[3], U[2], U[1], b[4], b[5], b[6]);
+    b[7] = ld_beta3(U[5], U[4], U[3], U[2], U[1], U[0]);
+    Up = cu_interp<true>(b + 4, P, P.cu_e[A], P.cu_x[A], U[5], U[4], U[3], U[2], U[1], U[0]);
+}
+
+template <int A>
+__device__ __forceinline__ void cu_pair_bwd(const double* U, const double* b, const Params& P, double Umb,
+                                            double Upb, double* Ub) {
+    double Sb[6] = {0, 0, 0, 0, 0, 0};
+    cu_side_bwd(P, P.cu_e[A], P.cu_x[A], U, b, Umb, Sb);
+#pragma unroll
+    for (int j = 0; j < 6; j++) Ub[j] += Sb[j];
+    const double R[6] = {U[5], U[4], U[3], U[2], U[1], U[0]};
+    double Rb[6] = {0, 0, 0, 0, 0, 0};
+    cu_side_bwd(P, P.cu_e[A], P.cu_x[A], R, b + 4, Upb, Rb);
+#pragma unroll
+    for (int j = 0; j < 6; j++) Ub[5 - j] += Rb[j];
+}
+
+// ----------------------------------------------------------------------------
 // Thermodynamics.
 // ----------------------------------------------------------------------------
 // Mixture gamma of a face state or a cell and the adjoint of gamma pushed to
@@ -453,7 +599,6 @@ __device__ void riemann_bwd(const Params& P, const double* VL, const double* VR,
 #pragma unroll
     for (int e = 0; e < NEQ; e++) VK[e] = left ? VL[e] : VR[e];
     const double rhoK = left ? rhoL : rhoR;
-    const double epsK = left ? epsL : epsR;
     const double sK = left ? s_L : s_R;
     const double uK = left ? uL : uR;
     const double pK = left ? pL : pR;

@@ -1,7 +1,9 @@
-// Face and update kernels of one arithmetic form and one flow model.  Built
-// six times from this file: -DHMR_FAST=0 --fmad=false (namespace
-// hmr_exact_m<model>) and -DHMR_FAST=1 (namespace hmr_fast_m<model>), with
-// -DHMR_MODEL=0 (single species), 1 (four-equation) or 2 (five-equation).
+// Face and update kernels of one arithmetic form, one flow model and one
+// scheme set.  Built twelve times from this file: -DHMR_FAST=0 --fmad=false
+// (namespace hmr_exact_...) and -DHMR_FAST=1 (hmr_fast_...), with
+// -DHMR_MODEL=0 (single species), 1 (four-equation) or 2 (five-equation), and
+// -DHMR_SCHEME_SET=0 (WCNS5-JS, WCNS6-LD; namespace <form>_m<model>) or 1
+// (WCNS5-Z, WCNS6-CU-M2; namespace <form>_zc_m<model>).
 #include <cuda_runtime.h>
 
 #include "hmr_launch.h"
@@ -10,10 +12,18 @@
 #error "HMR_MODEL must be defined: 0 single species, 1 four-equation, 2 five-equation"
 #endif
 
+#ifndef HMR_SCHEME_SET
+#define HMR_SCHEME_SET 0
+#endif
+
 #define HMR_CAT2(a, b) a##b
 #define HMR_CAT(a, b) HMR_CAT2(a, b)
-#if HMR_FAST
+#if HMR_FAST && HMR_SCHEME_SET
+#define HMR_NS HMR_CAT(hmr_fast_zc_m, HMR_MODEL)
+#elif HMR_FAST
 #define HMR_NS HMR_CAT(hmr_fast_m, HMR_MODEL)
+#elif HMR_SCHEME_SET
+#define HMR_NS HMR_CAT(hmr_exact_zc_m, HMR_MODEL)
 #else
 #define HMR_NS HMR_CAT(hmr_exact_m, HMR_MODEL)
 #endif
@@ -27,17 +37,20 @@ struct VT {
     static constexpr int DIM = D, MODEL = M, NSP = N, SCHEME = S;
 };
 
-// Variants of this translation unit: 2D/3D x WCNS5-JS/WCNS6-LD of its model
-// (one species for the single-species model, two for the multi-species ones).
+// Variants of this translation unit: 2D/3D x the two schemes of its set, for
+// its model (one species for the single-species model, two for the
+// multi-species ones).
 template <class F>
 static int dispatch(const Variant& v, F f) {
     constexpr int M_ = HMR_MODEL;
     constexpr int N_ = M_ == SINGLE_SPECIES ? 1 : 2;
+    constexpr int S0 = HMR_SCHEME_SET ? WCNS5_Z : WCNS5_JS;
+    constexpr int S1 = HMR_SCHEME_SET ? WCNS6_CU_M2 : WCNS6_LD;
     if (v.model != M_ || v.nsp != N_) return -2;
-    if (v.dim == 2 && v.scheme == WCNS5_JS) return f(VT<2, M_, N_, WCNS5_JS>{});
-    if (v.dim == 2 && v.scheme == WCNS6_LD) return f(VT<2, M_, N_, WCNS6_LD>{});
-    if (v.dim == 3 && v.scheme == WCNS5_JS) return f(VT<3, M_, N_, WCNS5_JS>{});
-    if (v.dim == 3 && v.scheme == WCNS6_LD) return f(VT<3, M_, N_, WCNS6_LD>{});
+    if (v.dim == 2 && v.scheme == S0) return f(VT<2, M_, N_, S0>{});
+    if (v.dim == 2 && v.scheme == S1) return f(VT<2, M_, N_, S1>{});
+    if (v.dim == 3 && v.scheme == S0) return f(VT<3, M_, N_, S0>{});
+    if (v.dim == 3 && v.scheme == S1) return f(VT<3, M_, N_, S1>{});
     return -2;
 }
 

@@ -148,7 +148,9 @@ __device__ __forceinline__ bool face_eval(const Params& P, const FaceProj<DIM, M
 #pragma unroll
         for (int m = 0; m < 6; m++) U[m] = W[m][e];
         if constexpr (SCHEME == WCNS5_JS) js_pair<X>(U, P.p, Wm[e], Wp[e]);
-        else ld_pair<X>(U, P, Wm[e], Wp[e]);
+        else if constexpr (SCHEME == WCNS6_LD) ld_pair<X>(U, P, Wm[e], Wp[e]);
+        else if constexpr (SCHEME == WCNS5_Z) z_pair<X>(U, P.p, Wm[e], Wp[e]);
+        else cu_pair<X, A>(U, P, Wm[e], Wp[e]);
     }
     double VL[NEQ], VR[NEQ];
     prim_from_char<X, DIM, MODEL, NSP, A>(F, Wm, VL);

@@ -7,6 +7,7 @@
 
 #include <cuda_runtime.h>
 
+#include "hmr.h"
 #include "hmr_kernels.cuh"
 #include "hmr_vjp_items.cuh"
 
@@ -22,6 +23,35 @@ inline void species_params(const double* gamma, const double* R, int nsp, Params
         P.cp[s] = P.gamma[s]/(P.gamma[s] - double(1))*Rs;
         P.cv[s] = double(1)/(P.gamma[s] - double(1))*Rs;
     }
+}
+
+inline bool reconstructor_known(int r) {
+    return r == HMR_WCNS5_JS_HLLC_HLL || r == HMR_WCNS6_LD_HLLC_HLL || r == HMR_WCNS5_Z_HLLC_HLL ||
+           r == HMR_WCNS6_CU_M2_HLLC_HLL;
+}
+
+// Scheme constants of Params from a configuration whose reconstructor is known:
+// p, q, C, alpha_tau, and WCNS6-CU-M2's epsilon dx^2 and Chi dx^2 per axis, each
+// evaluated as the reference writes it (epsilon*dx*dx, left to right) from the
+// grid geometry's spacing.  Returns HMR_ERR_ARGUMENT for constants out of range.
+inline int scheme_params(const hmr_config* cfg, Params& P) {
+    if (cfg->constant_p < 1 || cfg->constant_p > 8 || cfg->constant_q < 1 || cfg->constant_q > 8)
+        return HMR_ERR_ARGUMENT;
+    P.p = cfg->constant_p;
+    P.q = cfg->constant_q;
+    P.C = cfg->constant_C;
+    P.alpha_tau = cfg->constant_alpha_tau;
+    for (int d = 0; d < 3; d++) P.cu_e[d] = P.cu_x[d] = 0.0;
+    if (cfg->convective_flux_reconstructor == HMR_WCNS6_CU_M2_HLLC_HLL) {
+        if (!(cfg->constant_Chi >= 0.0) || !(cfg->constant_epsilon >= 0.0)) return HMR_ERR_ARGUMENT;
+        for (int d = 0; d < cfg->dim && d < 3; d++) {
+            const double dx = cfg->grid_dx[d];
+            if (!(dx > 0.0)) return HMR_ERR_ARGUMENT;
+            P.cu_e[d] = cfg->constant_epsilon*dx*dx;
+            P.cu_x[d] = cfg->constant_Chi*dx*dx;
+        }
+    }
+    return HMR_OK;
 }
 
 struct Variant {
@@ -103,9 +133,10 @@ int launch_rk_stage(const hmr::Variant& v, const hmr::Geom& g, int ncoef, const 
                     cudaStream_t st);
 }
 
-// hmr_faces.cu is built once per arithmetic form and flow model (six
-// translation units compiled in parallel); each defines these launchers in
-// namespace <form>_m<model>.
+// hmr_faces.cu is built once per arithmetic form, flow model and scheme set
+// (twelve translation units compiled in parallel); each defines these launchers
+// in namespace <form>_m<model> (WCNS5-JS, WCNS6-LD) or <form>_zc_m<model>
+// (WCNS5-Z, WCNS6-CU-M2).
 #define HMR_DECLARE_FACE_LAUNCHERS(NS)                                                                       \
     namespace NS {                                                                                           \
     int launch_faces(const hmr::Variant& v, const hmr::Params& P, const hmr::Geom& g, const hmr::Scratch& S, \
@@ -123,6 +154,12 @@ HMR_DECLARE_FACE_LAUNCHERS(hmr_exact_m2)
 HMR_DECLARE_FACE_LAUNCHERS(hmr_fast_m0)
 HMR_DECLARE_FACE_LAUNCHERS(hmr_fast_m1)
 HMR_DECLARE_FACE_LAUNCHERS(hmr_fast_m2)
+HMR_DECLARE_FACE_LAUNCHERS(hmr_exact_zc_m0)
+HMR_DECLARE_FACE_LAUNCHERS(hmr_exact_zc_m1)
+HMR_DECLARE_FACE_LAUNCHERS(hmr_exact_zc_m2)
+HMR_DECLARE_FACE_LAUNCHERS(hmr_fast_zc_m0)
+HMR_DECLARE_FACE_LAUNCHERS(hmr_fast_zc_m1)
+HMR_DECLARE_FACE_LAUNCHERS(hmr_fast_zc_m2)
 
 // Per-form entry points: route to the translation unit of the variant's model.
 #define HMR_ROUTE(NS, FN, ...)                                            \
@@ -133,22 +170,30 @@ HMR_DECLARE_FACE_LAUNCHERS(hmr_fast_m2)
     default: return -2;                                                   \
     }
 
+// ... and to the translation unit of its scheme set.
+#define HMR_ROUTE_SCHEME(NS, FN, ...)                                     \
+    if (v.scheme == hmr::WCNS5_Z || v.scheme == hmr::WCNS6_CU_M2) {       \
+        HMR_ROUTE(NS##_zc, FN, __VA_ARGS__)                               \
+    } else {                                                              \
+        HMR_ROUTE(NS, FN, __VA_ARGS__)                                    \
+    }
+
 #define HMR_DEFINE_FACE_ROUTER(NS)                                                                             \
     namespace NS {                                                                                             \
     inline int launch_faces(const hmr::Variant& v, const hmr::Params& P, const hmr::Geom& g,                   \
                             const hmr::Scratch& S, hmr::Counters* cnt, const hmr::Redo& R, cudaStream_t st) {  \
-        HMR_ROUTE(NS, launch_faces, v, P, g, S, cnt, R, st)                                                    \
+        HMR_ROUTE_SCHEME(NS, launch_faces, v, P, g, S, cnt, R, st)                                                    \
     }                                                                                                          \
     inline int launch_update(const hmr::Variant& v, const hmr::Geom& g, const hmr::Scratch& S,                 \
                              const hmr::UpdateArgs& U, cudaStream_t st) {                                      \
-        HMR_ROUTE(NS, launch_update, v, g, S, U, st)                                                           \
+        HMR_ROUTE_SCHEME(NS, launch_update, v, g, S, U, st)                                                           \
     }                                                                                                          \
     inline int launch_level(const hmr::Variant& v, const hmr::Params& P, const hmr::LevelArgs& L, int blocks,  \
                             int threads, cudaStream_t st) {                                                    \
-        HMR_ROUTE(NS, launch_level, v, P, L, blocks, threads, st)                                              \
+        HMR_ROUTE_SCHEME(NS, launch_level, v, P, L, blocks, threads, st)                                              \
     }                                                                                                          \
     inline int level_max_blocks(const hmr::Variant& v, int threads, int* blocks) {                             \
-        HMR_ROUTE(NS, level_max_blocks, v, threads, blocks)                                                    \
+        HMR_ROUTE_SCHEME(NS, level_max_blocks, v, threads, blocks)                                                    \
     }                                                                                                          \
     }
 

@@ -68,12 +68,13 @@ extern "C" int hmr_rk_substep_patch_noalloc(const hmr_config* cfg, const hmr_pat
     if (!cfg || !pg || !alpha || !Q_int || !Q_out || stage < 0 || stage > 2) return HMR_ERR_ARGUMENT;
     const int dim = cfg->dim;
     if (dim != 2 && dim != 3) return HMR_ERR_ARGUMENT;
-    if (cfg->convective_flux_reconstructor != HMR_WCNS5_JS_HLLC_HLL &&
-        cfg->convective_flux_reconstructor != HMR_WCNS6_LD_HLLC_HLL)
-        return HMR_ERR_UNSUPPORTED;
+    if (!reconstructor_known(cfg->convective_flux_reconstructor)) return HMR_ERR_UNSUPPORTED;
     if (cfg->precision != HMR_PRECISION_FAST && cfg->precision != HMR_PRECISION_EXACT) return HMR_ERR_ARGUMENT;
-    if (cfg->constant_p < 1 || cfg->constant_p > 8 || cfg->constant_q < 1 || cfg->constant_q > 8)
-        return HMR_ERR_ARGUMENT;
+    {
+        Params probe;  // scheme constants in range (and, for WCNS6-CU-M2, the grid spacing set)
+        const int r = scheme_params(cfg, probe);
+        if (r) return r;
+    }
     int neq = 0, ncomp = 0;
     if (cfg->flow_model == HMR_SINGLE_SPECIES && cfg->num_species == 1) {
         neq = dim + 2;
@@ -132,10 +133,7 @@ extern "C" int hmr_rk_substep_patch_noalloc(const hmr_config* cfg, const hmr_pat
     v.scheme = cfg->convective_flux_reconstructor;
     Params P;
     species_params(cfg->species_gamma, cfg->species_R, cfg->num_species, P);
-    P.p = cfg->constant_p;
-    P.q = cfg->constant_q;
-    P.C = cfg->constant_C;
-    P.alpha_tau = cfg->constant_alpha_tau;
+    scheme_params(cfg, P);
 
     unsigned char* bytes = static_cast<unsigned char*>(base);
     double* p = reinterpret_cast<double*>(bytes + kHeaderBytes);

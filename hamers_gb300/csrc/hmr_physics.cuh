@@ -10,6 +10,8 @@
 // Formulas and the reference lines they follow:
 //   WCNS5-JS  src/flow/convective_flux_reconstructors/WCNS56/ConvectiveFluxReconstructorWCNS5-JS-HLLC-HLL.cpp:24-164
 //   WCNS6-LD  src/flow/convective_flux_reconstructors/WCNS56/ConvectiveFluxReconstructorWCNS6-LD-HLLC-HLL.cpp:24-319
+//   WCNS5-Z   src/flow/convective_flux_reconstructors/WCNS56/ConvectiveFluxReconstructorWCNS5-Z-HLLC-HLL.cpp:78-168
+//   WCNS6-CU-M2 src/flow/convective_flux_reconstructors/WCNS56/ConvectiveFluxReconstructorWCNS6-CU-M2-HLLC-HLL.cpp:112-228
 //   projection / characteristic transforms / bounds
 //             src/flow/flow_models/single-species/FlowModelBasicUtilitiesSingleSpecies.cpp:3013,4638,5882,7023
 //             src/flow/flow_models/five-eqn_Allaire/FlowModelBasicUtilitiesFiveEqnAllaire.cpp:5446,7474,8232,9201
@@ -31,7 +33,7 @@
 namespace hmr {
 
 enum { SINGLE_SPECIES = 0, FOUR_EQN_CONSERVATIVE = 1, FIVE_EQN_ALLAIRE = 2 };
-enum { WCNS5_JS = 0, WCNS6_LD = 1 };
+enum { WCNS5_JS = 0, WCNS6_LD = 1, WCNS5_Z = 2, WCNS6_CU_M2 = 3 };
 
 constexpr int MAX_SPECIES = 4;
 constexpr int MAX_COMP = 12;
@@ -44,6 +46,8 @@ struct Params {
     double cv[MAX_SPECIES];            // species c_v = 1/(gamma_i - 1)*R_i
     int p, q;                          // WCNS constants
     double C, alpha_tau;
+    double cu_e[3];                    // WCNS6-CU-M2 epsilon*dx*dx per axis (dx: the grid geometry's spacing)
+    double cu_x[3];                    // WCNS6-CU-M2 Chi*dx*dx per axis
 };
 
 template <int DIM, int MODEL, int NSP>
@@ -536,6 +540,113 @@ __device__ __forceinline__ void ld_pair(const double* U, const Params& P, double
     js_betas_x(U[5], U[4], U[3], U[2], U[1], b[0], b[1], b[2]);
     b[3] = ld_beta3(U[5], U[4], U[3], U[2], U[1], U[0]);
     Up = ld_interp<X>(b, sigma, P, U[5], U[4], U[3], U[2], U[1], U[0]);
+}
+
+// ----------------------------------------------------------------------------
+// WCNS5-Z (WCNS5-Z-HLLC-HLL.cpp:78-168): the WCNS5-JS indicators and stencil,
+// weights d_k (1 + (tau_5/(beta_k + eps))^p) with tau_5 = |beta_0 - beta_2|.
+// ----------------------------------------------------------------------------
+template <bool X>
+__device__ __forceinline__ double z_interp(double b0, double b1, double b2, int p,
+                                           double S0, double S1, double S2, double S3, double S4) {
+    const double tau_5 = fabs(sub_(b0, b2));
+    double w0, w1, w2;
+    if constexpr (X) {
+        w0 = mul_(double(1)/double(16), add_(double(1), ipow_<true>(tau_5/add_(b0, HMR_EPS), p)));
+        w1 = mul_(double(5)/double(8), add_(double(1), ipow_<true>(tau_5/add_(b1, HMR_EPS), p)));
+        w2 = mul_(double(5)/double(16), add_(double(1), ipow_<true>(tau_5/add_(b2, HMR_EPS), p)));
+        const double ws = add_(add_(w0, w1), w2);
+        w0 = w0/ws; w1 = w1/ws; w2 = w2/ws;
+        const double t0 = mul_(mul_(double(3)/double(8), w0), S0);
+        const double t1 = mul_(sub_(mul_(-double(10)/double(8), w0), mul_(double(1)/double(8), w1)), S1);
+        const double t2 = mul_(add_(add_(mul_(double(15)/double(8), w0), mul_(double(6)/double(8), w1)),
+                                    mul_(double(3)/double(8), w2)), S2);
+        const double t3 = mul_(add_(mul_(double(3)/double(8), w1), mul_(double(6)/double(8), w2)), S3);
+        const double t4 = mul_(mul_(double(1)/double(8), w2), S4);
+        return sub_(add_(add_(add_(t0, t1), t2), t3), t4);
+    } else {
+        // d_k (1 + T/E_k) with E_k = (beta_k + eps)^p, T = tau_5^p, over one common
+        // denominator: w_k = d_k (E_k + T) prod_{j!=k} E_j / sum_m (...).
+        const double T = ipow_<false>(tau_5, p);
+        const double e0 = ipow_<false>(b0 + HMR_EPS, p), e1 = ipow_<false>(b1 + HMR_EPS, p),
+                     e2 = ipow_<false>(b2 + HMR_EPS, p);
+        const double a0 = double(1)/double(16)*((e0 + T)*(e1*e2));
+        const double a1 = double(5)/double(8)*((e1 + T)*(e0*e2));
+        const double a2 = double(5)/double(16)*((e2 + T)*(e0*e1));
+        const double r = double(1)/(a0 + a1 + a2);
+        w0 = a0*r; w1 = a1*r; w2 = a2*r;
+        return double(3)/double(8)*w0*S0 +
+            (-double(10)/double(8)*w0 - double(1)/double(8)*w1)*S1 +
+            (double(15)/double(8)*w0 + double(6)/double(8)*w1 + double(3)/double(8)*w2)*S2 +
+            (double(3)/double(8)*w1 + double(6)/double(8)*w2)*S3 -
+            double(1)/double(8)*w2*S4;
+    }
+}
+
+template <bool X>
+__device__ __forceinline__ void z_pair(const double* U, int p, double& Um, double& Up) {
+    double b0, b1, b2;
+    js_betas_x(U[0], U[1], U[2], U[3], U[4], b0, b1, b2);
+    Um = z_interp<X>(b0, b1, b2, p, U[0], U[1], U[2], U[3], U[4]);
+    js_betas_x(U[5], U[4], U[3], U[2], U[1], b0, b1, b2);
+    Up = z_interp<X>(b0, b1, b2, p, U[5], U[4], U[3], U[2], U[1]);
+}
+
+// ----------------------------------------------------------------------------
+// WCNS6-CU-M2 (WCNS6-CU-M2-HLLC-HLL.cpp:112-228): the WCNS6-LD indicators and
+// stencil, weights d_k (C + tau_6/(beta_k + eps dx^2) (beta_avg + Chi dx^2)/(beta_k + Chi dx^2))^q
+// with beta_avg = (beta_0 + beta_2 + 6 beta_1)/8, tau_6 = |beta_3 - beta_avg|.
+// ce = eps dx^2 and cx = Chi dx^2 of the face's axis.
+// ----------------------------------------------------------------------------
+template <bool X>
+__device__ __forceinline__ double cu_interp(const double* b, const Params& P, double ce, double cx,
+                                            double S0, double S1, double S2, double S3, double S4, double S5) {
+    const double beta_avg = mul_(double(1)/double(8), add_(add_(b[0], b[2]), mul_(double(6), b[1])));
+    const double tau_6 = fabs(sub_(b[3], beta_avg));
+    double o0, o1, o2, o3;
+    if constexpr (X) {
+        const double ax = add_(beta_avg, cx);
+        o0 = mul_(double(1)/double(32), ipow_<true>(add_(P.C, mul_(tau_6/add_(b[0], ce), ax)/add_(b[0], cx)), P.q));
+        o1 = mul_(double(15)/double(32), ipow_<true>(add_(P.C, mul_(tau_6/add_(b[1], ce), ax)/add_(b[1], cx)), P.q));
+        o2 = mul_(double(15)/double(32), ipow_<true>(add_(P.C, mul_(tau_6/add_(b[2], ce), ax)/add_(b[2], cx)), P.q));
+        o3 = mul_(double(1)/double(32), ipow_<true>(add_(P.C, mul_(tau_6/add_(b[3], ce), ax)/add_(b[3], cx)), P.q));
+        const double os = add_(add_(add_(o0, o1), o2), o3);
+        o0 = o0/os; o1 = o1/os; o2 = o2/os; o3 = o3/os;
+        const double t0 = mul_(mul_(double(3)/double(8), o0), S0);
+        const double t1 = mul_(sub_(mul_(-double(10)/double(8), o0), mul_(double(1)/double(8), o1)), S1);
+        const double t2 = mul_(add_(add_(mul_(double(15)/double(8), o0), mul_(double(6)/double(8), o1)),
+                                    mul_(double(3)/double(8), o2)), S2);
+        const double t3 = mul_(add_(add_(mul_(double(3)/double(8), o1), mul_(double(6)/double(8), o2)),
+                                    mul_(double(15)/double(8), o3)), S3);
+        const double t4 = mul_(sub_(mul_(-double(1)/double(8), o2), mul_(double(10)/double(8), o3)), S4);
+        const double t5 = mul_(mul_(double(3)/double(8), o3), S5);
+        return add_(add_(add_(add_(add_(t0, t1), t2), t3), t4), t5);
+    } else {
+        const double g = tau_6*(beta_avg + cx);
+        o0 = double(1)/double(32)*ipow_<false>(P.C + g/((b[0] + ce)*(b[0] + cx)), P.q);
+        o1 = double(15)/double(32)*ipow_<false>(P.C + g/((b[1] + ce)*(b[1] + cx)), P.q);
+        o2 = double(15)/double(32)*ipow_<false>(P.C + g/((b[2] + ce)*(b[2] + cx)), P.q);
+        o3 = double(1)/double(32)*ipow_<false>(P.C + g/((b[3] + ce)*(b[3] + cx)), P.q);
+        const double ro = double(1)/(o0 + o1 + o2 + o3);
+        o0 *= ro; o1 *= ro; o2 *= ro; o3 *= ro;
+        return double(3)/double(8)*o0*S0 +
+            (-double(10)/double(8)*o0 - double(1)/double(8)*o1)*S1 +
+            (double(15)/double(8)*o0 + double(6)/double(8)*o1 + double(3)/double(8)*o2)*S2 +
+            (double(3)/double(8)*o1 + double(6)/double(8)*o2 + double(15)/double(8)*o3)*S3 +
+            (-double(1)/double(8)*o2 - double(10)/double(8)*o3)*S4 +
+            double(3)/double(8)*o3*S5;
+    }
+}
+
+template <bool X, int A>
+__device__ __forceinline__ void cu_pair(const double* U, const Params& P, double& Um, double& Up) {
+    double b[4];
+    js_betas_x(U[0], U[1], U[2], U[3], U[4], b[0], b[1], b[2]);
+    b[3] = ld_beta3(U[0], U[1], U[2], U[3], U[4], U[5]);
+    Um = cu_interp<X>(b, P, P.cu_e[A], P.cu_x[A], U[0], U[1], U[2], U[3], U[4], U[5]);
+    js_betas_x(U[5], U[4], U[3], U[2], U[1], b[0], b[1], b[2]);
+    b[3] = ld_beta3(U[5], U[4], U[3], U[2], U[1], U[0]);
+    Up = cu_interp<X>(b, P, P.cu_e[A], P.cu_x[A], U[5], U[4], U[3], U[2], U[1], U[0]);
 }
 
 // ----------------------------------------------------------------------------

@@ -34,8 +34,12 @@ static int dispatch(const Variant& v, F f) {
     if (v.model != M_ || v.nsp != N_) return -2;
     if (v.dim == 2 && v.scheme == WCNS5_JS) return f(VT<2, M_, N_, WCNS5_JS>{});
     if (v.dim == 2 && v.scheme == WCNS6_LD) return f(VT<2, M_, N_, WCNS6_LD>{});
+    if (v.dim == 2 && v.scheme == WCNS5_Z) return f(VT<2, M_, N_, WCNS5_Z>{});
+    if (v.dim == 2 && v.scheme == WCNS6_CU_M2) return f(VT<2, M_, N_, WCNS6_CU_M2>{});
     if (v.dim == 3 && v.scheme == WCNS5_JS) return f(VT<3, M_, N_, WCNS5_JS>{});
     if (v.dim == 3 && v.scheme == WCNS6_LD) return f(VT<3, M_, N_, WCNS6_LD>{});
+    if (v.dim == 3 && v.scheme == WCNS5_Z) return f(VT<3, M_, N_, WCNS5_Z>{});
+    if (v.dim == 3 && v.scheme == WCNS6_CU_M2) return f(VT<3, M_, N_, WCNS6_CU_M2>{});
     return -2;
 }
 

@@ -187,6 +187,13 @@ __device__ __forceinline__ void char_stencil(const Geom& g, const Scratch& S, co
     }
 }
 
+// Forward values kept per characteristic variable and face for the reverse pass:
+// the smoothness indicators of both sides (and WCNS6-LD's sigma).
+template <int SCHEME>
+__host__ __device__ constexpr int weno_kept() {
+    return SCHEME == WCNS5_JS || SCHEME == WCNS5_Z ? 6 : (SCHEME == WCNS6_LD ? 9 : 8);
+}
+
 // Item u = e*nf + t: forward WCNS interpolation of variable e at face t (exact
 // form), keeping the reconstructed values and the smoothness indicators.
 template <int DIM, int MODEL, int NSP, int SCHEME, int AX>
@@ -202,9 +209,11 @@ __device__ __forceinline__ void face_fwd_weno_item(const Params& P, const Geom& 
     load_proj<DIM, MODEL, NSP>(VA.Fp[AX], nf, t, F);
     double U[6], b[9], Wm, Wp;
     char_stencil<DIM, MODEL, NSP, AX>(g, S, F, xR, st, e, U);
-    constexpr int NB = SCHEME == WCNS5_JS ? 6 : 9;
+    constexpr int NB = weno_kept<SCHEME>();
     if constexpr (SCHEME == WCNS5_JS) js_pair_keep(U, P.p, Wm, Wp, b);
-    else ld_pair_keep(U, P, Wm, Wp, b);
+    else if constexpr (SCHEME == WCNS6_LD) ld_pair_keep(U, P, Wm, Wp, b);
+    else if constexpr (SCHEME == WCNS5_Z) z_pair_keep(U, P.p, Wm, Wp, b);
+    else cu_pair_keep<AX>(U, P, Wm, Wp, b);
     VA.Wv[AX][(long)(2 * e) * nf + t] = Wm;
     VA.Wv[AX][(long)(2 * e + 1) * nf + t] = Wp;
 #pragma unroll
@@ -327,12 +336,14 @@ __device__ __forceinline__ void face_bwd_weno_item(const Params& P, const Geom& 
     char_stencil<DIM, MODEL, NSP, AX>(g, S, F, xR, st, e, U);
     const double Wmb = VA.Wb[AX][(long)(2 * e) * nf + t];
     const double Wpb = VA.Wb[AX][(long)(2 * e + 1) * nf + t];
-    constexpr int NB = SCHEME == WCNS5_JS ? 6 : 9;
+    constexpr int NB = weno_kept<SCHEME>();
     double b[NB];
 #pragma unroll
     for (int q = 0; q < NB; q++) b[q] = VA.Kb[AX][(long)(NB * e + q) * nf + t];
     if constexpr (SCHEME == WCNS5_JS) js_pair_bwd(U, b, P.p, Wmb, Wpb, Ub);
-    else ld_pair_bwd(U, b, P, Wmb, Wpb, Ub);
+    else if constexpr (SCHEME == WCNS6_LD) ld_pair_bwd(U, b, P, Wmb, Wpb, Ub);
+    else if constexpr (SCHEME == WCNS5_Z) z_pair_bwd(U, b, P.p, Wmb, Wpb, Ub);
+    else cu_pair_bwd<AX>(U, b, P, Wmb, Wpb, Ub);
     double* Cb = VA.Cb[AX];
 #pragma unroll
     for (int m = 0; m < 6; m++) Cb[(long)(m * NEQ + e) * nf + t] = Ub[m];

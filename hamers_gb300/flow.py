@@ -33,6 +33,8 @@ _FLOW_MODELS = {
 _RECONSTRUCTORS = {
     "WCNS5_JS_HLLC_HLL": L.HMR_WCNS5_JS_HLLC_HLL,
     "WCNS6_LD_HLLC_HLL": L.HMR_WCNS6_LD_HLLC_HLL,
+    "WCNS5_Z_HLLC_HLL": L.HMR_WCNS5_Z_HLLC_HLL,
+    "WCNS6_CU_M2_HLLC_HLL": L.HMR_WCNS6_CU_M2_HLLC_HLL,
 }
 
 # SSPRK(3,3), RungeKuttaLevelIntegrator.cpp:3909-3927
@@ -96,14 +98,19 @@ def _comp_ptrs(t, ncomp):
 
 
 class ConvectiveFluxReconstructor:
-    """WCNS5-JS / WCNS6-LD + HLLC-HLL reconstructor behind the C ABI.
+    """WCNS5-JS / WCNS6-LD / WCNS5-Z / WCNS6-CU-M2 + HLLC-HLL reconstructor behind the C ABI.
 
     db keys follow the reference's input database: constant_p, constant_q,
-    constant_C, constant_alpha_tau (ConvectiveFluxReconstructorWCNS6-LD-HLLC-HLL.cpp:343-361).
+    constant_C, constant_alpha_tau (ConvectiveFluxReconstructorWCNS6-LD-HLLC-HLL.cpp:343-361),
+    constant_Chi, constant_epsilon (ConvectiveFluxReconstructorWCNS6-CU-M2-HLLC-HLL.cpp:252-270);
+    keys left out take the scheme's defaults.
+    grid_geometry: the grid geometry (an object with getDx(), or the spacing itself) of
+    the coarsest level, as the reference passes CartesianGridGeometry to the reconstructor;
+    WCNS6-CU-M2 scales its weights by that spacing and needs it, the others ignore it.
     precision: 'fast' (default, <= 1e-12 relative) or 'exact' (bitwise to the reference order).
     """
 
-    def __init__(self, name, flow_model, db=None, precision="fast"):
+    def __init__(self, name, flow_model, db=None, precision="fast", grid_geometry=None):
         if name not in _RECONSTRUCTORS:
             raise ValueError(f"unknown convective flux reconstructor {name!r}")
         db = db or {}
@@ -114,10 +121,16 @@ class ConvectiveFluxReconstructor:
         for s in range(flow_model.num_species):
             cfg.species_gamma[s] = flow_model.species_gamma[s]
             cfg.species_R[s] = flow_model.species_R[s]
-        cfg.constant_p = int(db.get("constant_p", 2))
-        cfg.constant_q = int(db.get("constant_q", 4))
-        cfg.constant_C = float(db.get("constant_C", 1.0e9))
-        cfg.constant_alpha_tau = float(db.get("constant_alpha_tau", 35.0))
+        for key, conv in (("constant_p", int), ("constant_q", int), ("constant_C", float),
+                          ("constant_alpha_tau", float), ("constant_Chi", float), ("constant_epsilon", float)):
+            if key in db:
+                setattr(cfg, key, conv(db[key]))
+        if grid_geometry is not None:
+            dx = grid_geometry.getDx() if hasattr(grid_geometry, "getDx") else grid_geometry
+            for d, v in enumerate(list(dx)[:3]):
+                cfg.grid_dx[d] = float(v)
+        elif name == "WCNS6_CU_M2_HLLC_HLL":
+            raise ValueError("WCNS6_CU_M2_HLLC_HLL needs grid_geometry (its weights use the grid spacing)")
         cfg.precision = L.HMR_PRECISION_EXACT if precision == "exact" else L.HMR_PRECISION_FAST
         self.flow_model = flow_model
         self.name = name

@@ -68,7 +68,9 @@ typedef enum {
  * (src/flow/convective_flux_reconstructors/ConvectiveFluxReconstructorManager.cpp:40-91). */
 typedef enum {
     HMR_WCNS5_JS_HLLC_HLL = 0,
-    HMR_WCNS6_LD_HLLC_HLL = 1
+    HMR_WCNS6_LD_HLLC_HLL = 1,
+    HMR_WCNS5_Z_HLLC_HLL = 2,
+    HMR_WCNS6_CU_M2_HLLC_HLL = 3
 } hmr_reconstructor;
 
 typedef enum {
@@ -83,11 +85,17 @@ typedef struct {
     double species_gamma[HMR_MAX_SPECIES];     /* Equation_of_state_mixing_rules.species_gamma */
     double species_R[HMR_MAX_SPECIES];         /* Equation_of_state_mixing_rules.species_R */
     int convective_flux_reconstructor;         /* hmr_reconstructor */
-    int constant_p;                            /* WCNS constant p (default 2) */
-    int constant_q;                            /* WCNS6-LD constant q (default 4) */
-    double constant_C;                         /* WCNS6-LD constant C (default 1e9) */
+    int constant_p;                            /* WCNS5-JS / WCNS5-Z / WCNS6-LD constant p (default 2) */
+    int constant_q;                            /* WCNS6-LD / WCNS6-CU-M2 constant q (default 4) */
+    double constant_C;                         /* WCNS6-LD constant C (default 1e9); WCNS6-CU-M2 C (default 1000) */
     double constant_alpha_tau;                 /* WCNS6-LD constant alpha_tau (default 35) */
     int precision;                             /* hmr_precision */
+    double constant_Chi;                       /* WCNS6-CU-M2 constant Chi (default 1e8) */
+    double constant_epsilon;                   /* WCNS6-CU-M2 constant epsilon (default 1e-8) */
+    double grid_dx[3];                         /* CartesianGridGeometry::getDx(), the coarsest level's spacing:
+                                                  WCNS6-CU-M2 scales its weights by it on every level
+                                                  (WCNS6-CU-M2-HLLC-HLL.cpp:367-368).  Required (> 0 on the
+                                                  used axes) for WCNS6-CU-M2, ignored by the other schemes. */
 } hmr_config;
 
 typedef struct {

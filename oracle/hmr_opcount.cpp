@@ -52,7 +52,8 @@ double hmro_count_ops(int model, int dim, int nsp, int scheme, const double* gam
     c.model = model; c.dim = dim; c.num_species = nsp; c.scheme = scheme;
     for (int i = 0; i < 8; i++) c.gamma[i] = i < nsp ? gamma[i] : 1.4;
     for (int i = 0; i < 8; i++) c.R[i] = 1.0;
-    c.p = 2; c.q = 4; c.C = 1.0e9; c.alpha_tau = 35.0;
+    c.p = 2; c.q = 4; c.C = 1.0e9; c.alpha_tau = 35.0; c.Chi = 1.0e8; c.epsilon = 1.0e-8;
+    for (int i = 0; i < 3; i++) c.grid_dx[i] = dx[i];
     const hmro::Box b = hmro::make_box(dim, n, 4);
     const int ncomp = hmro::num_comp(c), neq = hmro::num_eqn(c);
     std::vector<C> q((size_t)ncomp * b.ncell());

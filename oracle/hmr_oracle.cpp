@@ -12,33 +12,7 @@ using namespace hmro;
 
 extern "C" {
 
-struct hmro_config {
-    int model;
-    int dim;
-    int num_species;
-    int scheme;
-    double gamma[8];
-    double R[8];
-    int p;
-    int q;
-    double C;
-    double alpha_tau;
-};
-
-static Config to_cfg(const hmro_config* c) {
-    Config k;
-    k.model = c->model;
-    k.dim = c->dim;
-    k.num_species = c->num_species;
-    k.scheme = c->scheme;
-    for (int i = 0; i < 8; i++) k.gamma[i] = c->gamma[i];
-    for (int i = 0; i < 8; i++) k.R[i] = c->R[i];
-    k.p = c->p;
-    k.q = c->q;
-    k.C = c->C;
-    k.alpha_tau = c->alpha_tau;
-    return k;
-}
+static Config to_cfg(const hmro_config* c) { return hmro_to_config(c); }
 
 static long flux_len(const Config& c, const Box& b) {
     const int neq = num_eqn(c);

@@ -44,7 +44,9 @@ inline double s_fmax(double a, double b) { return std::fmax(a, b); }
 inline double s_val(double a) { return a; }
 
 enum { MODEL_SINGLE_SPECIES = 0, MODEL_FOUR_EQN_CONSERVATIVE = 1, MODEL_FIVE_EQN_ALLAIRE = 2 };
-enum { SCHEME_WCNS5_JS = 0, SCHEME_WCNS6_LD = 1 };
+// ConvectiveFluxReconstructorManager.cpp:40-91: WCNS5_JS_HLLC_HLL, WCNS6_LD_HLLC_HLL,
+// WCNS5_Z_HLLC_HLL, WCNS6_CU_M2_HLLC_HLL (all on the WCNS56 driver).
+enum { SCHEME_WCNS5_JS = 0, SCHEME_WCNS6_LD = 1, SCHEME_WCNS5_Z = 2, SCHEME_WCNS6_CU_M2 = 3 };
 
 struct Config {
     int model;
@@ -53,10 +55,14 @@ struct Config {
     int scheme;
     double gamma[8];     // species_gamma
     double R[8];         // species_R (four-equation model: species heat capacities)
-    int p;               // constant_p  (JS default 2, WCNS5-JS-HLLC-HLL.cpp:188-191; LD default 2)
-    int q;               // constant_q  (LD default 4, WCNS6-LD-HLLC-HLL.cpp:343-361)
-    double C;            // constant_C  (LD default 1e9)
+    int p;               // constant_p  (JS, Z default 2, WCNS5-JS-HLLC-HLL.cpp:188-191; LD default 2)
+    int q;               // constant_q  (LD, CU-M2 default 4, WCNS6-LD-HLLC-HLL.cpp:343-361)
+    double C;            // constant_C  (LD default 1e9; CU-M2 default 1000, WCNS6-CU-M2-HLLC-HLL.cpp:252-270)
     double alpha_tau;    // constant_alpha_tau (LD default 35)
+    double Chi;          // constant_Chi (CU-M2 default 1e8)
+    double epsilon;      // constant_epsilon (CU-M2 default 1e-8)
+    double grid_dx[3];   // CartesianGridGeometry::getDx(): the coarsest level's spacing, which
+                         // WCNS6-CU-M2 uses on every level (WCNS6-CU-M2-HLLC-HLL.cpp:367-368)
 };
 
 // Number of equations.  single: 2+dim (FlowModelSingleSpecies.cpp:29);
@@ -297,6 +303,101 @@ inline T ld_plus(const T* U, int p, int q, double C, double alpha_tau) {  // :23
     beta[3] = ld_beta3_tilde(U);
     T o0, o1, o2, o3;
     ld_weights(o0, o1, o2, o3, beta, sigma, p, q, C, alpha_tau);
+    return double(3)/double(8)*o0*U[5] +
+        (-double(10)/double(8)*o0 - double(1)/double(8)*o1)*U[4] +
+        (double(15)/double(8)*o0 + double(6)/double(8)*o1 + double(3)/double(8)*o2)*U[3] +
+        (double(3)/double(8)*o1 + double(6)/double(8)*o2 + double(15)/double(8)*o3)*U[2] +
+        (-double(1)/double(8)*o2 - double(10)/double(8)*o3)*U[1] +
+        double(3)/double(8)*o3*U[0];
+}
+
+// ---------------------------------------------------------------------------
+// WCNS5-Z local interpolation, ConvectiveFluxReconstructorWCNS5-Z-HLLC-HLL.cpp:78-168:
+// the WCNS5-JS indicators and 5-point stencil with the weights
+// d_k (1 + (tau_5/(beta_k + eps))^p), tau_5 = |beta_0 - beta_2|.
+// ---------------------------------------------------------------------------
+template <class T>
+inline void z_weights(T& w0, T& w1, T& w2, const T& b0, const T& b1, const T& b2, int p) {
+    T tau_5 = s_fabs(b0 - b2);
+    w0 = double(1)/double(16)*(double(1) + ipow_(tau_5/(b0 + EPS), p));
+    w1 = double(5)/double(8)*(double(1) + ipow_(tau_5/(b1 + EPS), p));
+    w2 = double(5)/double(16)*(double(1) + ipow_(tau_5/(b2 + EPS), p));
+    T ws = w0 + w1 + w2;
+    w0 = w0/ws; w1 = w1/ws; w2 = w2/ws;
+}
+
+template <class T>
+inline T z_minus(const T* U, int p) {  // :78-120
+    T b0, b1, b2, w0, w1, w2;
+    js_beta(b0, b1, b2, U);
+    z_weights(w0, w1, w2, b0, b1, b2, p);
+    return double(3)/double(8)*w0*U[0] +
+        (-double(10)/double(8)*w0 - double(1)/double(8)*w1)*U[1] +
+        (double(15)/double(8)*w0 + double(6)/double(8)*w1 +
+        double(3)/double(8)*w2)*U[2] +
+        (double(3)/double(8)*w1 + double(6)/double(8)*w2)*U[3] -
+        double(1)/double(8)*w2*U[4];
+}
+
+template <class T>
+inline T z_plus(const T* U, int p) {  // :126-168
+    T b0, b1, b2, w0, w1, w2;
+    js_beta_tilde(b0, b1, b2, U);
+    z_weights(w0, w1, w2, b0, b1, b2, p);
+    return double(3)/double(8)*w0*U[5] +
+        (-double(10)/double(8)*w0 - double(1)/double(8)*w1)*U[4] +
+        (double(15)/double(8)*w0 + double(6)/double(8)*w1 +
+        double(3)/double(8)*w2)*U[3] +
+        (double(3)/double(8)*w1 + double(6)/double(8)*w2)*U[2] -
+        double(1)/double(8)*w2*U[1];
+}
+
+// ---------------------------------------------------------------------------
+// WCNS6-CU-M2 local interpolation, ConvectiveFluxReconstructorWCNS6-CU-M2-HLLC-HLL.cpp:112-228:
+// the WCNS6-LD indicators and 6-point stencil with the weights
+//   d_k (C + tau_6/(beta_k + eps dx^2) (beta_avg + Chi dx^2)/(beta_k + Chi dx^2))^q,
+// beta_avg = (beta_0 + beta_2 + 6 beta_1)/8, tau_6 = |beta_3 - beta_avg|, and no
+// central-upwind switch.  dx is the grid geometry's spacing along the face normal.
+// ---------------------------------------------------------------------------
+template <class T>
+inline void cu_weights(T& o0, T& o1, T& o2, T& o3, const T* beta, int q, double C, double Chi,
+                       double epsilon, double dx) {
+    T beta_avg = double(1)/double(8)*(beta[0] + beta[2] + double(6)*beta[1]);  // 6*beta_1 in the reference: the same value
+    T tau_6 = s_fabs(beta[3] - beta_avg);
+    o0 = double(1)/double(32)*ipow_(C + tau_6/(beta[0] + epsilon*dx*dx)*
+        (beta_avg + Chi*dx*dx)/(beta[0] + Chi*dx*dx), q);
+    o1 = double(15)/double(32)*ipow_(C + tau_6/(beta[1] + epsilon*dx*dx)*
+        (beta_avg + Chi*dx*dx)/(beta[1] + Chi*dx*dx), q);
+    o2 = double(15)/double(32)*ipow_(C + tau_6/(beta[2] + epsilon*dx*dx)*
+        (beta_avg + Chi*dx*dx)/(beta[2] + Chi*dx*dx), q);
+    o3 = double(1)/double(32)*ipow_(C + tau_6/(beta[3] + epsilon*dx*dx)*
+        (beta_avg + Chi*dx*dx)/(beta[3] + Chi*dx*dx), q);
+    T os = o0 + o1 + o2 + o3;
+    o0 = o0/os; o1 = o1/os; o2 = o2/os; o3 = o3/os;
+}
+
+template <class T>
+inline T cu_minus(const T* U, int q, double C, double Chi, double epsilon, double dx) {  // :112-167
+    T beta[4];
+    js_beta(beta[0], beta[1], beta[2], U);
+    beta[3] = ld_beta3(U);
+    T o0, o1, o2, o3;
+    cu_weights(o0, o1, o2, o3, beta, q, C, Chi, epsilon, dx);
+    return double(3)/double(8)*o0*U[0] +
+        (-double(10)/double(8)*o0 - double(1)/double(8)*o1)*U[1] +
+        (double(15)/double(8)*o0 + double(6)/double(8)*o1 + double(3)/double(8)*o2)*U[2] +
+        (double(3)/double(8)*o1 + double(6)/double(8)*o2 + double(15)/double(8)*o3)*U[3] +
+        (-double(1)/double(8)*o2 - double(10)/double(8)*o3)*U[4] +
+        double(3)/double(8)*o3*U[5];
+}
+
+template <class T>
+inline T cu_plus(const T* U, int q, double C, double Chi, double epsilon, double dx) {  // :173-228
+    T beta[4];
+    js_beta_tilde(beta[0], beta[1], beta[2], U);
+    beta[3] = ld_beta3_tilde(U);
+    T o0, o1, o2, o3;
+    cu_weights(o0, o1, o2, o3, beta, q, C, Chi, epsilon, dx);
     return double(3)/double(8)*o0*U[5] +
         (-double(10)/double(8)*o0 - double(1)/double(8)*o1)*U[4] +
         (double(15)/double(8)*o0 + double(6)/double(8)*o1 + double(3)/double(8)*o2)*U[3] +
@@ -961,7 +1062,9 @@ void conv_flux_source(const Config& c, const int* n, const double* dx, double dt
             for (int e = 0; e < neq; e++) W[((size_t)m * neq + e) * nf + f] = Wc[e];
         }
 
-        // WENO interpolation (performWENOInterpolation: JS :235-737, LD :417-955).
+        // WENO interpolation (performWENOInterpolation: JS :235-737, LD :417-955,
+        // Z WCNS5-Z-HLLC-HLL.cpp:239-741, CU-M2 WCNS6-CU-M2-HLLC-HLL.cpp:326-891 with the
+        // grid geometry's spacing along this axis, :383,541,806).
         for (int e = 0; e < neq; e++)
         for (long f = 0; f < nf; f++) {
             T U[6];
@@ -969,9 +1072,15 @@ void conv_flux_source(const Config& c, const int* n, const double* dx, double dt
             if (c.scheme == SCHEME_WCNS5_JS) {
                 Wm[(size_t)e * nf + f] = js_minus(U, c.p);
                 Wp[(size_t)e * nf + f] = js_plus(U, c.p);
-            } else {
+            } else if (c.scheme == SCHEME_WCNS6_LD) {
                 Wm[(size_t)e * nf + f] = ld_minus(U, c.p, c.q, c.C, c.alpha_tau);
                 Wp[(size_t)e * nf + f] = ld_plus(U, c.p, c.q, c.C, c.alpha_tau);
+            } else if (c.scheme == SCHEME_WCNS5_Z) {
+                Wm[(size_t)e * nf + f] = z_minus(U, c.p);
+                Wp[(size_t)e * nf + f] = z_plus(U, c.p);
+            } else {
+                Wm[(size_t)e * nf + f] = cu_minus(U, c.q, c.C, c.Chi, c.epsilon, c.grid_dx[a]);
+                Wp[(size_t)e * nf + f] = cu_plus(U, c.q, c.C, c.Chi, c.epsilon, c.grid_dx[a]);
             }
         }
 
@@ -1196,3 +1305,41 @@ void fill_ghosts(const Config& c, const int* n, const int* periodic, T* const* Q
 }
 
 }  // namespace hmro
+
+// C view of Config taken by the entry points of the oracle libraries
+// (hmr_oracle.cpp, hmr_tangent.cpp); oracle.py's _Cfg mirrors it field by field.
+extern "C" {
+struct hmro_config {
+    int model;
+    int dim;
+    int num_species;
+    int scheme;
+    double gamma[8];
+    double R[8];
+    int p;
+    int q;
+    double C;
+    double alpha_tau;
+    double Chi;
+    double epsilon;
+    double grid_dx[3];
+};
+}
+
+inline hmro::Config hmro_to_config(const hmro_config* c) {
+    hmro::Config k;
+    k.model = c->model;
+    k.dim = c->dim;
+    k.num_species = c->num_species;
+    k.scheme = c->scheme;
+    for (int i = 0; i < 8; i++) k.gamma[i] = c->gamma[i];
+    for (int i = 0; i < 8; i++) k.R[i] = c->R[i];
+    k.p = c->p;
+    k.q = c->q;
+    k.C = c->C;
+    k.alpha_tau = c->alpha_tau;
+    k.Chi = c->Chi;
+    k.epsilon = c->epsilon;
+    for (int i = 0; i < 3; i++) k.grid_dx[i] = c->grid_dx[i];
+    return k;
+}

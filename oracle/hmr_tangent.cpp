@@ -64,40 +64,17 @@ inline double s_val(hmro_dual::D a) { return a.v; }
 
 extern "C" {
 
-struct hmro_config_t {
-    int model;
-    int dim;
-    int num_species;
-    int scheme;
-    double gamma[8];
-    double R[8];
-    int p;
-    int q;
-    double C;
-    double alpha_tau;
-};
-
 // Tangent of the fused substep: Q_out = sum_{n<=stage} alpha[n] Q_int[n]
 // + beta * (-div F(Q_int[stage]) + S(Q_int[stage])) (the forward of
 // hmr_rk_substep_patch).  Q_int / dQ_int hold stage+1 consecutive ghost-box
 // states (ncomp components each, ghosts of the last one filled); Q_out and
 // dQ_out receive the output state and its derivative along dQ_int (ghost box,
 // interior written).
-int hmro_tangent_substep(const hmro_config_t* cfg, const int* n, const double* dx, double dt, int stage,
+int hmro_tangent_substep(const hmro_config* cfg, const int* n, const double* dx, double dt, int stage,
                          const double* alpha, double beta, const double* Q_int, const double* dQ_int,
                          double* Q_out, double* dQ_out) {
     using hmro_dual::D;
-    hmro::Config c;
-    c.model = cfg->model;
-    c.dim = cfg->dim;
-    c.num_species = cfg->num_species;
-    c.scheme = cfg->scheme;
-    for (int i = 0; i < 8; i++) c.gamma[i] = cfg->gamma[i];
-    for (int i = 0; i < 8; i++) c.R[i] = cfg->R[i];
-    c.p = cfg->p;
-    c.q = cfg->q;
-    c.C = cfg->C;
-    c.alpha_tau = cfg->alpha_tau;
+    const hmro::Config c = hmro_to_config(cfg);
     const hmro::Box b = hmro::make_box(c.dim, n, 4);
     const int ncomp = hmro::num_comp(c), neq = hmro::num_eqn(c);
     const long nc = b.ncell();

@@ -24,6 +24,8 @@ MODEL_FOUR_EQN_CONSERVATIVE = 1
 MODEL_FIVE_EQN_ALLAIRE = 2
 SCHEME_WCNS5_JS = 0
 SCHEME_WCNS6_LD = 1
+SCHEME_WCNS5_Z = 2
+SCHEME_WCNS6_CU_M2 = 3
 GHOST = 4
 
 
@@ -31,7 +33,8 @@ class _Cfg(ctypes.Structure):
     _fields_ = [("model", ctypes.c_int), ("dim", ctypes.c_int), ("num_species", ctypes.c_int),
                 ("scheme", ctypes.c_int), ("gamma", ctypes.c_double * 8), ("R", ctypes.c_double * 8),
                 ("p", ctypes.c_int),
-                ("q", ctypes.c_int), ("C", ctypes.c_double), ("alpha_tau", ctypes.c_double)]
+                ("q", ctypes.c_int), ("C", ctypes.c_double), ("alpha_tau", ctypes.c_double),
+                ("Chi", ctypes.c_double), ("epsilon", ctypes.c_double), ("grid_dx", ctypes.c_double * 3)]
 
 
 def build():
@@ -84,23 +87,37 @@ def tangent_lib():
 
 
 class Config:
-    """Flow model + scheme selection (mirrors the reference's input keys)."""
+    """Flow model + scheme selection (mirrors the reference's input keys).
+
+    C defaults to the scheme's own default (1e9 for WCNS6-LD, 1000 for
+    WCNS6-CU-M2).  grid_dx is the grid geometry's (coarsest level's) spacing,
+    which WCNS6-CU-M2's weights use on every level; it is required for that
+    scheme and ignored by the others.
+    """
 
     def __init__(self, model, dim, species_gamma, scheme=SCHEME_WCNS5_JS,
-                 p=2, q=4, C=1.0e9, alpha_tau=35.0, species_R=None):
+                 p=2, q=4, C=None, alpha_tau=35.0, species_R=None, Chi=1.0e8, epsilon=1.0e-8,
+                 grid_dx=None):
         self.model = int(model)
         self.dim = int(dim)
         self.species_gamma = [float(g) for g in species_gamma]
         self.num_species = len(self.species_gamma)
         self.species_R = [float(r) for r in (species_R or [1.0] * self.num_species)]
         self.scheme = int(scheme)
+        if C is None:
+            C = 1000.0 if self.scheme == SCHEME_WCNS6_CU_M2 else 1.0e9
         self.p, self.q, self.C, self.alpha_tau = int(p), int(q), float(C), float(alpha_tau)
+        self.Chi, self.epsilon = float(Chi), float(epsilon)
+        self.grid_dx = None if grid_dx is None else [float(v) for v in grid_dx] + [1.0] * (3 - len(grid_dx))
 
     def c(self):
+        if self.scheme == SCHEME_WCNS6_CU_M2 and self.grid_dx is None:
+            raise ValueError("WCNS6-CU-M2 needs the grid geometry's spacing (grid_dx)")
         g = (ctypes.c_double * 8)(*(self.species_gamma + [0.0] * (8 - self.num_species)))
         r = (ctypes.c_double * 8)(*(self.species_R + [0.0] * (8 - self.num_species)))
+        gd = (ctypes.c_double * 3)(*(self.grid_dx or [0.0, 0.0, 0.0]))
         return _Cfg(self.model, self.dim, self.num_species, self.scheme, g, r, self.p, self.q,
-                    self.C, self.alpha_tau)
+                    self.C, self.alpha_tau, self.Chi, self.epsilon, gd)
 
     @property
     def neq(self):

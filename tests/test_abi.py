@@ -56,3 +56,24 @@ def test_null_arguments_are_rejected(lib):
     assert lib.hmr_ctx_destroy(None) == L.HMR_ERR_ARGUMENT
     assert lib.hmr_conv_flux_source_patch(None, None, None, 0.0, None, None, None) == L.HMR_ERR_ARGUMENT
     assert lib.hmr_level_destroy(None) == L.HMR_ERR_ARGUMENT
+
+
+def test_cu_m2_defaults_and_grid_spacing(lib):
+    """WCNS6-CU-M2 defaults (WCNS6-CU-M2-HLLC-HLL.cpp:252-270: q 4, C 1000, Chi 1e8, epsilon 1e-8);
+    its weights use the grid geometry's spacing, so a context without one is refused."""
+    cfg = L.Config()
+    assert lib.hmr_config_default(ctypes.byref(cfg), L.HMR_SINGLE_SPECIES, L.HMR_WCNS6_CU_M2_HLLC_HLL, 2, 1) == 0
+    assert (cfg.constant_q, cfg.constant_C, cfg.constant_Chi, cfg.constant_epsilon) == (4, 1000.0, 1.0e8, 1.0e-8)
+    ctx = ctypes.c_void_p()
+    assert lib.hmr_ctx_create(ctypes.byref(cfg), ctypes.byref(ctx)) == L.HMR_ERR_ARGUMENT
+    cfg.grid_dx[0], cfg.grid_dx[1] = 0.1, -0.1
+    assert lib.hmr_ctx_create(ctypes.byref(cfg), ctypes.byref(ctx)) == L.HMR_ERR_ARGUMENT
+
+
+def test_reconstructor_names_and_grid_geometry_requirement():
+    from hamers_gb300 import flow
+    fm = flow.FlowModel("SINGLE_SPECIES", 2, [1.4])
+    with pytest.raises(ValueError):
+        flow.ConvectiveFluxReconstructor("WCNS6_CU_M2_HLLC_HLL", fm)
+    with pytest.raises(ValueError):
+        flow.ConvectiveFluxReconstructor("WCNS6_TEST", fm)

@@ -2,10 +2,12 @@
 
 The reference's CI runs its convergence problems and asserts the final L2
 rate (tests/2D_convergence_test_single_species/convergence_test.py:8-16,281):
-rate > 4.8 for WCNS5_JS_HLLC_HLL and > 5.8 for WCNS6_LD_HLLC_HLL, on grids
+rate > 4.8 for WCNS5_JS_HLLC_HLL and WCNS5_Z_HLLC_HLL and > 5.8 for
+WCNS6_LD_HLLC_HLL (convergence_test.py:8-16), on grids
 N = 8, 16, 32, 64 with 8x8 patches, dt = 0.001*dx, 8*N/8 steps in 2D (N/8 in 3D).
 A periodic single level of 8x8 patches equals one periodic N x N patch, so the
-oracle runs one patch.
+oracle runs one patch.  WCNS6_CU_M2_HLLC_HLL is not in the reference's list;
+it is held to its formal sixth order with the WCNS6-LD threshold.
 """
 import math
 
@@ -15,7 +17,9 @@ import pytest
 from hamers_gb300 import problems as P
 from oracle import oracle as O
 
-EXPECTED = {O.SCHEME_WCNS5_JS: 4.8, O.SCHEME_WCNS6_LD: 5.8}
+EXPECTED = {O.SCHEME_WCNS5_JS: 4.8, O.SCHEME_WCNS6_LD: 5.8, O.SCHEME_WCNS5_Z: 4.8, O.SCHEME_WCNS6_CU_M2: 5.8}
+SCHEMES = [O.SCHEME_WCNS5_JS, O.SCHEME_WCNS6_LD, O.SCHEME_WCNS5_Z, O.SCHEME_WCNS6_CU_M2]
+SCHEME_IDS = ["js", "ld", "z", "cu"]
 
 
 def l2_errors(model, dim, scheme, levels):
@@ -23,7 +27,7 @@ def l2_errors(model, dim, scheme, levels):
     for N in levels:
         Q, dx, dt, nsteps, exact, gam = P.convergence_problem(model, dim, N)
         cfg = O.Config(model, dim, gam, scheme,
-                       species_R=P.FOUR_EQN_R if model == O.MODEL_FOUR_EQN_CONSERVATIVE else None)
+                       species_R=P.FOUR_EQN_R if model == O.MODEL_FOUR_EQN_CONSERVATIVE else None, grid_dx=dx)
         O.fill_ghosts(cfg, [N] * dim, [1] * dim, Q)
         O.rk3_advance(cfg, [N] * dim, dx, dt, [1] * dim, nsteps, Q)
         Qi = P.interior(Q, dim)
@@ -35,7 +39,7 @@ def l2_errors(model, dim, scheme, levels):
 
 @pytest.mark.parametrize("model", [O.MODEL_SINGLE_SPECIES, O.MODEL_FOUR_EQN_CONSERVATIVE, O.MODEL_FIVE_EQN_ALLAIRE],
                          ids=["single", "four", "five"])
-@pytest.mark.parametrize("scheme", [O.SCHEME_WCNS5_JS, O.SCHEME_WCNS6_LD], ids=["js", "ld"])
+@pytest.mark.parametrize("scheme", SCHEMES, ids=SCHEME_IDS)
 def test_convergence_2d(model, scheme):
     errs = l2_errors(model, 2, scheme, [8, 16, 32, 64])
     rate = math.log2(errs[-2] / errs[-1])
@@ -44,7 +48,8 @@ def test_convergence_2d(model, scheme):
 
 @pytest.mark.parametrize("model", [O.MODEL_SINGLE_SPECIES, O.MODEL_FOUR_EQN_CONSERVATIVE, O.MODEL_FIVE_EQN_ALLAIRE],
                          ids=["single", "four", "five"])
-def test_convergence_3d_js(model):
-    errs = l2_errors(model, 3, O.SCHEME_WCNS5_JS, [8, 16, 32])
+@pytest.mark.parametrize("scheme", [O.SCHEME_WCNS5_JS, O.SCHEME_WCNS5_Z], ids=["js", "z"])
+def test_convergence_3d(model, scheme):
+    errs = l2_errors(model, 3, scheme, [8, 16, 32])
     rate = math.log2(errs[-2] / errs[-1])
-    assert rate > EXPECTED[O.SCHEME_WCNS5_JS], (errs, rate)
+    assert rate > EXPECTED[scheme], (errs, rate)

@@ -19,19 +19,24 @@ CASES = [
     (O.MODEL_FIVE_EQN_ALLAIRE, 2, O.SCHEME_WCNS5_JS, [1.4, 1.67], None),
     (O.MODEL_FIVE_EQN_ALLAIRE, 2, O.SCHEME_WCNS6_LD, [1.4, 1.67], None),
     (O.MODEL_SINGLE_SPECIES, 3, O.SCHEME_WCNS5_JS, [1.4], None),
+    (O.MODEL_SINGLE_SPECIES, 2, O.SCHEME_WCNS5_Z, [1.4], None),
+    (O.MODEL_FIVE_EQN_ALLAIRE, 2, O.SCHEME_WCNS5_Z, [1.4, 1.67], None),
+    (O.MODEL_SINGLE_SPECIES, 2, O.SCHEME_WCNS6_CU_M2, [1.4], None),
+    (O.MODEL_FOUR_EQN_CONSERVATIVE, 2, O.SCHEME_WCNS6_CU_M2, P.FOUR_EQN_GAMMA, P.FOUR_EQN_R),
 ]
-IDS = ["%s-%dd-%s" % ({0: "single", 1: "four", 2: "five"}[m], d, "js" if s == 0 else "ld") for m, d, s, _, _ in CASES]
+SCHEME_IDS = {O.SCHEME_WCNS5_JS: "js", O.SCHEME_WCNS6_LD: "ld", O.SCHEME_WCNS5_Z: "z", O.SCHEME_WCNS6_CU_M2: "cu"}
+IDS = ["%s-%dd-%s" % ({0: "single", 1: "four", 2: "five"}[m], d, SCHEME_IDS[s]) for m, d, s, _, _ in CASES]
 
 
 @pytest.mark.parametrize("case", CASES, ids=IDS)
 def test_tangent_matches_central_differences(case):
     model, dim, scheme, gam, R = case
     n = (12, 10) if dim == 2 else (8, 7, 6)
-    cfg = O.Config(model, dim, gam, scheme, species_R=R)
+    dx = [0.1] * dim
+    cfg = O.Config(model, dim, gam, scheme, species_R=R, grid_dx=dx)
     Q = smooth_state(model, dim, n, seed=3, species_gamma=gam)
     rng = np.random.default_rng(0)
     v = rng.standard_normal(Q.shape) * np.abs(Q).mean(axis=(1, 2, 3), keepdims=True)
-    dx = [0.1] * dim
     dt = 1e-2
     _, dQ = O.tangent_substep(cfg, n, dx, dt, 0, [1.0], 1.0, [Q], [v])
     zero = np.zeros_like(v)
