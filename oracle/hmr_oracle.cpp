@@ -85,6 +85,52 @@ int hmro_rk_stage(const hmro_config* cfg, const int* n, const double* dx, int ns
     return 0;
 }
 
+// DiffusiveFluxReconstructorMidpoint::computeDiffusiveFluxOnPatch for one
+// single-species patch (flux overwritten, dt-scaled, same layout as the convective flux).
+int hmro_diff_flux(const hmro_config* cfg, const hmro_transport* tr, const int* n, const double* dx, double dt,
+                   const double* Q, double* flux) {
+    const Config c = to_cfg(cfg);
+    if (c.model != MODEL_SINGLE_SPECIES || (tr->order != 2 && tr->order != 4)) return -1;
+    const Box b = make_box(c.dim, n, 4);
+    const int ncomp = num_comp(c);
+    std::vector<const double*> q(ncomp);
+    for (int e = 0; e < ncomp; e++) q[e] = Q + (size_t)e * b.ncell();
+    std::vector<double*> f;
+    flux_ptrs(c, b, flux, f);
+    diff_flux<double>(c, hmro_to_transport(tr), n, dx, dt, q.data(), f.data());
+    return 0;
+}
+
+// NavierStokes::advanceSingleStepOnPatch: hmro_rk_stage with the diffusive
+// fluxes Fd_int (same blocks as F_int) entering the divergence.
+int hmro_rk_stage_ns(const hmro_config* cfg, const int* n, const double* dx, int nstages,
+                     const double* alpha, const double* beta, const double* gamma,
+                     const double* Q_int, const double* F_int, const double* Fd_int, const double* S_int,
+                     double* Q_out) {
+    const Config c = to_cfg(cfg);
+    const Box b = make_box(c.dim, n, 4);
+    const int ncomp = num_comp(c), neq = num_eqn(c);
+    const long nint = (long)b.n[0] * b.n[1] * b.n[2];
+    const long fl = flux_len(c, b);
+    std::vector<std::vector<const double*>> qi(nstages), fi(nstages), di(nstages), si(nstages);
+    std::vector<const double* const*> qp(nstages), fp(nstages), dp(nstages), sp(nstages);
+    for (int s = 0; s < nstages; s++) {
+        for (int e = 0; e < ncomp; e++) qi[s].push_back(Q_int + (size_t)s * ncomp * b.ncell() + (size_t)e * b.ncell());
+        std::vector<double*> f;
+        flux_ptrs(c, b, const_cast<double*>(F_int + (size_t)s * fl), f);
+        for (double* p : f) fi[s].push_back(p);
+        flux_ptrs(c, b, const_cast<double*>(Fd_int + (size_t)s * fl), f);
+        for (double* p : f) di[s].push_back(p);
+        for (int e = 0; e < neq; e++) si[s].push_back(S_int + (size_t)s * neq * nint + (size_t)e * nint);
+        qp[s] = qi[s].data(); fp[s] = fi[s].data(); dp[s] = di[s].data(); sp[s] = si[s].data();
+    }
+    std::vector<double*> qo(ncomp);
+    for (int e = 0; e < ncomp; e++) qo[e] = Q_out + (size_t)e * b.ncell();
+    rk_stage<double>(c, n, dx, nstages, alpha, beta, gamma, qp.data(), fp.data(), sp.data(),
+                     qo.data(), nullptr, nullptr, dp.data());
+    return 0;
+}
+
 int hmro_fill_ghosts(const hmro_config* cfg, const int* n, const int* periodic, double* Q) {
     const Config c = to_cfg(cfg);
     const Box b = make_box(c.dim, n, 4);
@@ -131,6 +177,34 @@ int hmro_rk3_advance(const hmro_config* cfg, const int* n, const double* dx, dou
     }
     if (stats) for (int i = 0; i < 3; i++) stats[i] = tot[i];
     (void)neq;
+    return 0;
+}
+
+// The same SSPRK3 loop for NavierStokes: convective + diffusive fluxes.
+int hmro_ns_rk3_advance(const hmro_config* cfg, const hmro_transport* tr, const int* n, const double* dx,
+                        double dt, const int* periodic, int nsteps, double* Q) {
+    const Config c = to_cfg(cfg);
+    const Box b = make_box(c.dim, n, 4);
+    const int ncomp = num_comp(c), neq = num_eqn(c);
+    const long nint = (long)b.n[0] * b.n[1] * b.n[2];
+    const long fl = flux_len(c, b);
+    const size_t qs = (size_t)ncomp * b.ncell();
+    std::vector<double> Qint(3 * qs), Fint(3 * fl), Dint(3 * fl), Sint(3 * (size_t)neq * nint), Qout(qs);
+    for (int step = 0; step < nsteps; step++) {
+        for (int sn = 0; sn < 3; sn++) {
+            std::copy(Q, Q + qs, Qint.begin() + sn * qs);
+            hmro_fill_ghosts(cfg, n, periodic, Qint.data() + sn * qs);
+            std::fill(Sint.begin() + sn * (size_t)neq * nint, Sint.begin() + (sn + 1) * (size_t)neq * nint, 0.0);
+            hmro_conv_flux_source(cfg, n, dx, dt, Qint.data() + sn * qs, Fint.data() + sn * fl,
+                                  Sint.data() + sn * (size_t)neq * nint, nullptr);
+            const int r = hmro_diff_flux(cfg, tr, n, dx, dt, Qint.data() + sn * qs, Dint.data() + sn * fl);
+            if (r) return r;
+            hmro_rk_stage_ns(cfg, n, dx, sn + 1, RK3_ALPHA[sn], RK3_BETA[sn], RK3_GAMMA[sn],
+                             Qint.data(), Fint.data(), Dint.data(), Sint.data(), Qout.data());
+            std::copy(Qout.begin(), Qout.end(), Q);
+        }
+        hmro_fill_ghosts(cfg, n, periodic, Q);
+    }
     return 0;
 }
 

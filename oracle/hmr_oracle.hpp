@@ -1213,7 +1213,8 @@ template <class T>
 void rk_stage(const Config& c, const int* n, const double* dx, int nstages,
               const double* alpha, const double* beta, const double* gamma,
               const T* const* const* Q_int, const T* const* const* F_int, const T* const* const* S_int,
-              T* const* Q_out, T* const* F_acc, T* const* S_acc) {
+              T* const* Q_out, T* const* F_acc, T* const* S_acc,
+              const T* const* const* Fd_int = nullptr) {
     const int dim = c.dim;
     const int neq = num_eqn(c);
     const int ncomp = num_comp(c);
@@ -1236,12 +1237,31 @@ void rk_stage(const Config& c, const int* n, const double* dx, int nstages,
                 const T* Fy = F_int[s][1 * neq + e];
                 const T* Fz = (dim == 3) ? F_int[s][2 * neq + e] : nullptr;
                 const T* S = S_int[s][e];
+                const T* Dx = Fd_int ? Fd_int[s][0 * neq + e] : nullptr;
+                const T* Dy = Fd_int ? Fd_int[s][1 * neq + e] : nullptr;
+                const T* Dz = (Fd_int && dim == 3) ? Fd_int[s][2 * neq + e] : nullptr;
                 for (int k = 0; k < b.n[2]; k++)
                 for (int j = 0; j < b.n[1]; j++)
                 for (int i = 0; i < b.n[0]; i++) {
                     const long x = b.cell(i, j, k);
                     const long is = interior_index(b, i, j, k);
-                    if (dim == 2) {
+                    const long xl = side_index(b, 0, i, j, k), xr = side_index(b, 0, i + 1, j, k);
+                    const long yl = side_index(b, 1, i, j, k), yr = side_index(b, 1, i, j + 1, k);
+                    if (Fd_int && dim == 2) {
+                        // NavierStokes::advanceSingleStepOnPatch (NavierStokes.cpp:1743-1749, 2D)
+                        Q_out[e][x] += beta[s]*
+                            (-(Fx[xr] - Fx[xl] + Dx[xr] - Dx[xl])/dx[0] -
+                              (Fy[yr] - Fy[yl] + Dy[yr] - Dy[yl])/dx[1] +
+                              S[is]);
+                    } else if (Fd_int) {
+                        // NavierStokes.cpp:2085-2092 (3D)
+                        const long zl = side_index(b, 2, i, j, k), zr = side_index(b, 2, i, j, k + 1);
+                        Q_out[e][x] += beta[s]*
+                            (-(Fx[xr] - Fx[xl] + Dx[xr] - Dx[xl])/dx[0] -
+                              (Fy[yr] - Fy[yl] + Dy[yr] - Dy[yl])/dx[1] -
+                              (Fz[zr] - Fz[zl] + Dz[zr] - Dz[zl])/dx[2] +
+                              S[is]);
+                    } else if (dim == 2) {
                         Q_out[e][x] += beta[s]*
                             (-(Fx[side_index(b, 0, i + 1, j, k)] - Fx[side_index(b, 0, i, j, k)])/dx[0] -
                               (Fy[side_index(b, 1, i, j + 1, k)] - Fy[side_index(b, 1, i, j, k)])/dx[1] +
@@ -1278,6 +1298,206 @@ void rk_stage(const Config& c, const int* n, const double* dx, int nstages,
                     const long x = b.cell(i, j, k);
                     ZN[x] -= Q_out[N + dim + 1 + si][x];
                 }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Navier-Stokes diffusive flux of a single-species patch,
+// DiffusiveFluxReconstructorMidpoint::computeDiffusiveFluxOnPatch
+//   src/flow/diffusive_flux_reconstructors/midpoint/DiffusiveFluxReconstructorMidpoint.cpp:38-2312
+// with the second-order (…MidpointSecondOrder.cpp) and fourth-order
+// (…MidpointFourthOrder.cpp) stencils, the single-species coefficient tables of
+//   src/flow/flow_models/single-species/FlowModelDiffusiveFluxUtilitiesSingleSpecies.cpp
+//   (derivative variables :654-1505, diffusivities at sides :2471-2799, their use :2800-3700),
+// constant shear and bulk viscosity and the Prandtl thermal conductivity
+// kappa = c_p mu/Pr (EquationOfThermalConductivityPrandtl.cpp:29-63), and the
+// temperature T = p/((gamma - 1) c_v rho) (EquationOfStateIdealGas.cpp:2157-2173).
+// ---------------------------------------------------------------------------
+struct Transport {
+    int order;          // 2 or 4: MIDPOINT_SECOND_ORDER / MIDPOINT_FOURTH_ORDER
+    double mu;          // Equation_of_shear_viscosity_mixing_rules.species_mu (CONSTANT)
+    double mu_v;        // Equation_of_bulk_viscosity_mixing_rules.species_mu_v (CONSTANT)
+    double c_p, Pr;     // Equation_of_thermal_conductivity_mixing_rules.species_c_p, species_Pr (PRANDTL)
+    double mu_kappa;    // ... and that model's own (constant) shear viscosity species_mu
+};
+
+// One term of a midpoint flux: equation e += D[k] * (derivative of variable v).
+// v: 0..dim-1 velocity components, 3 temperature.  Rows follow the reference's
+// per-equation order (first the derivatives along x, then y, then z).
+struct DiffTerm { int e, v, k; };
+
+// Terms of the flux normal to axis a differentiated along axis d.  The
+// reference's D_k at a side normal to a (computeSideDataOfDiffusiveFluxDiffusivities):
+//   D0 = -(4/3 mu + mu_v), D1 = 2/3 mu - mu_v, D2 = -mu,
+//   D3 = -u_a (4/3 mu + mu_v), D4 = u_a (2/3 mu - mu_v),
+//   D5, D6 = -u_t mu for the transverse velocities t in increasing axis order (3D),
+//   last = -kappa (D7 in 3D; D6 in 2D, where D5 = -u_t mu).
+inline int diff_terms(int dim, int a, int d, DiffTerm* out) {
+    static const DiffTerm T3[3][3][7] = {
+        {{{1, 0, 0}, {2, 1, 2}, {3, 2, 2}, {4, 0, 3}, {4, 1, 5}, {4, 2, 6}, {4, 3, 7}},
+         {{1, 1, 1}, {2, 0, 2}, {4, 0, 5}, {4, 1, 4}},
+         {{1, 2, 1}, {3, 0, 2}, {4, 0, 6}, {4, 2, 4}}},
+        {{{1, 1, 2}, {2, 0, 1}, {4, 0, 4}, {4, 1, 5}},
+         {{1, 0, 2}, {2, 1, 0}, {3, 2, 2}, {4, 0, 5}, {4, 1, 3}, {4, 2, 6}, {4, 3, 7}},
+         {{2, 2, 1}, {3, 1, 2}, {4, 1, 6}, {4, 2, 4}}},
+        {{{1, 2, 2}, {3, 0, 1}, {4, 0, 4}, {4, 2, 5}},
+         {{2, 2, 2}, {3, 1, 1}, {4, 1, 4}, {4, 2, 6}},
+         {{1, 0, 2}, {2, 1, 2}, {3, 2, 0}, {4, 0, 5}, {4, 1, 6}, {4, 2, 3}, {4, 3, 7}}}};
+    static const int N3[3][3] = {{7, 4, 4}, {4, 7, 4}, {4, 4, 7}};
+    static const DiffTerm T2[2][2][5] = {
+        {{{1, 0, 0}, {2, 1, 2}, {3, 0, 3}, {3, 1, 5}, {3, 3, 6}},
+         {{1, 1, 1}, {2, 0, 2}, {3, 0, 5}, {3, 1, 4}}},
+        {{{1, 1, 2}, {2, 0, 1}, {3, 0, 4}, {3, 1, 5}},
+         {{1, 0, 2}, {2, 1, 0}, {3, 0, 5}, {3, 1, 3}, {3, 3, 6}}}};
+    static const int N2[2][2] = {{5, 4}, {4, 5}};
+    const int nt = dim == 3 ? N3[a][d] : N2[a][d];
+    for (int t = 0; t < nt; t++) out[t] = dim == 3 ? T3[a][d][t] : T2[a][d][t];
+    return nt;
+}
+
+// Diffusivities D_k at one side normal to axis a from the side values of mu,
+// mu_v, kappa and the velocity (FlowModelDiffusiveFluxUtilitiesSingleSpecies.cpp:2471-2799).
+template <class T>
+inline void side_diffusivities(int dim, int a, const T& mu, const T& mu_v, const T& kappa, const T* u, T* D) {
+    D[0] = -(double(4)/double(3)*mu + mu_v);
+    D[1] = double(2)/double(3)*mu - mu_v;
+    D[2] = -mu;
+    D[3] = -u[a]*(double(4)/double(3)*mu + mu_v);
+    D[4] = u[a]*(double(2)/double(3)*mu - mu_v);
+    if (dim == 2) {
+        D[5] = -u[1 - a]*mu;
+        D[6] = -kappa;
+    } else {
+        const int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
+        D[5] = -u[t1]*mu;
+        D[6] = -u[t2]*mu;
+        D[7] = -kappa;
+    }
+}
+
+// Midpoint stencils (…MidpointSecondOrder.cpp / …MidpointFourthOrder.cpp):
+//   derivative at a midpoint   2nd: 1*(u_R - u_L)/dx             4th: (9/8 (u_R - u_L) - 1/24 (u_RR - u_LL))/dx
+//   derivative at a node       2nd: 1/2*(u_+1 - u_-1)/dx         4th: (2/3 (u_+1 - u_-1) - 1/12 (u_+2 - u_-2))/dx
+//   node -> midpoint value     2nd: 1/2*(u_R + u_L)              4th: 9/16 (u_R + u_L) - 1/16 (u_RR + u_LL)
+//   midpoint -> face flux      2nd: dt*1*F                        4th: dt*(13/12 F - 1/24 (F_-1 + F_+1))
+// each evaluated in the reference's operation order; dx_inv = 1/dx.
+template <class T>
+inline T mid_derivative(int order, const T& LL, const T& L, const T& R, const T& RR, double dx_inv) {
+    if (order == 2) return double(1)*(R - L)*dx_inv;
+    return (double(9)/double(8)*(R - L) + -double(1)/double(24)*(RR - LL))*dx_inv;
+}
+template <class T>
+inline T node_derivative(int order, const T& mm, const T& m, const T& p, const T& pp, double dx_inv) {
+    if (order == 2) return double(1)/double(2)*(p - m)*dx_inv;
+    return (double(2)/double(3)*(p - m) + -double(1)/double(12)*(pp - mm))*dx_inv;
+}
+template <class T>
+inline T mid_value(int order, const T& LL, const T& L, const T& R, const T& RR) {
+    if (order == 2) return double(1)/double(2)*(R + L);
+    return double(9)/double(16)*(R + L) + -double(1)/double(16)*(RR + LL);
+}
+
+// Cell fields the diffusive flux reads: velocity and temperature.
+template <class T>
+void diff_cell_fields(const Config& c, const Box& b, const Derived<T>& D, std::vector<T>& W) {
+    const int dim = c.dim;
+    const long nc = b.ncell();
+    W.assign((size_t)4 * nc, T(0.0));
+    const double cv = species_cv(c, 0);
+    for (long x = 0; x < nc; x++) {
+        for (int d = 0; d < dim; d++) W[(size_t)d * nc + x] = D.V[(size_t)(1 + d) * nc + x];
+        const T& rho = D.V[x];
+        const T& p = D.V[(size_t)(dim + 1) * nc + x];
+        W[(size_t)3 * nc + x] = p/((c.gamma[0] - double(1))*cv*rho);
+    }
+}
+
+// Midpoint flux (all equations) of the side normal to a between cells xL = x - e_a and x
+// (f = index along a of cell x): F_mid of …Midpoint.cpp:1420-1620 (x), analogues for y, z.
+template <class T>
+void diff_midpoint(const Config& c, const Transport& tr, const Box& b, const std::vector<T>& W, int a,
+                   int i, int j, int k, const double* dx, T* F) {
+    const int dim = c.dim, neq = num_eqn(c);
+    const long nc = b.ncell();
+    const int order = tr.order;
+    auto at = [&](int v, int ii, int jj, int kk) -> const T& { return W[(size_t)v * nc + b.cell(ii, jj, kk)]; };
+    auto sh = [&](int ax, int m, int& ii, int& jj, int& kk) {
+        ii = i; jj = j; kk = k;
+        if (ax == 0) ii += m; else if (ax == 1) jj += m; else kk += m;
+    };
+    // value of field v at the midpoint (cells f-2, f-1, f, f+1 along a)
+    auto mid = [&](auto&& cellval) {
+        int i0, j0, k0, i1, j1, k1, i2, j2, k2, i3, j3, k3;
+        sh(a, -2, i0, j0, k0); sh(a, -1, i1, j1, k1); sh(a, 0, i2, j2, k2); sh(a, 1, i3, j3, k3);
+        return mid_value(order, cellval(i0, j0, k0), cellval(i1, j1, k1), cellval(i2, j2, k2), cellval(i3, j3, k3));
+    };
+    // constant transport properties at cells, interpolated like every other side variable
+    const double kappa_c = tr.c_p*tr.mu_kappa/tr.Pr;
+    const T mu = mid([&](int, int, int) { return T(tr.mu); });
+    const T mu_v = mid([&](int, int, int) { return T(tr.mu_v); });
+    const T kappa = mid([&](int, int, int) { return T(kappa_c); });
+    T u[3] = {T(0.0), T(0.0), T(0.0)};
+    for (int d = 0; d < dim; d++) u[d] = mid([&](int ii, int jj, int kk) { return at(d, ii, jj, kk); });
+    T D[8];
+    side_diffusivities(dim, a, mu, mu_v, kappa, u, D);
+    for (int e = 0; e < neq; e++) F[e] = T(0.0);
+    for (int d = 0; d < dim; d++) {
+        DiffTerm terms[7];
+        const int nt = diff_terms(dim, a, d, terms);
+        const double dx_inv = double(1)/dx[d];
+        for (int t = 0; t < nt; t++) {
+            const int v = terms[t].v;
+            T g;
+            if (d == a) {
+                int i0, j0, k0, i1, j1, k1, i2, j2, k2, i3, j3, k3;
+                sh(a, -2, i0, j0, k0); sh(a, -1, i1, j1, k1); sh(a, 0, i2, j2, k2); sh(a, 1, i3, j3, k3);
+                g = mid_derivative(order, at(v, i0, j0, k0), at(v, i1, j1, k1), at(v, i2, j2, k2), at(v, i3, j3, k3),
+                                   dx_inv);
+            } else {
+                // derivative along d at the four cells, then to the midpoint along a
+                g = mid([&](int ii, int jj, int kk) {
+                    auto node = [&](int m) {
+                        int i4 = ii, j4 = jj, k4 = kk;
+                        if (d == 0) i4 += m; else if (d == 1) j4 += m; else k4 += m;
+                        return at(v, i4, j4, k4);
+                    };
+                    return node_derivative(order, node(-2), node(-1), node(1), node(2), dx_inv);
+                });
+            }
+            F[terms[t].e] += D[terms[t].k]*g;
+        }
+    }
+}
+
+// Diffusive flux of a patch: dim*neq side arrays (0 ghosts), overwritten.
+template <class T>
+void diff_flux(const Config& c, const Transport& tr, const int* n, const double* dx, double dt,
+               const T* const* Q, T* const* flux) {
+    const int dim = c.dim, neq = num_eqn(c);
+    const Box b = make_box(dim, n, 4);
+    Derived<T> D;
+    compute_derived(c, b, Q, D);
+    std::vector<T> W;
+    diff_cell_fields(c, b, D, W);
+    const double a_r = double(9)/double(8) + -double(1)/double(24), b_r = -double(1)/double(24);
+    T Fm[3][8], Fo[8];
+    for (int a = 0; a < dim; a++) {
+        const int e0 = b.n[0] + (a == 0), e1 = b.n[1] + (a == 1), e2 = b.n[2] + (a == 2);
+        for (int k = 0; k < e2; k++)
+        for (int j = 0; j < e1; j++)
+        for (int i = 0; i < e0; i++) {
+            const long f = side_index(b, a, i, j, k);
+            if (tr.order == 2) {
+                diff_midpoint(c, tr, b, W, a, i, j, k, dx, Fo);
+                for (int e = 0; e < neq; e++) flux[a * neq + e][f] = T(0.0) + dt*double(1)*Fo[e];
+            } else {
+                for (int m = -1; m <= 1; m++)
+                    diff_midpoint(c, tr, b, W, a, i + (a == 0 ? m : 0), j + (a == 1 ? m : 0), k + (a == 2 ? m : 0),
+                                  dx, Fm[m + 1]);
+                for (int e = 0; e < neq; e++)
+                    flux[a * neq + e][f] = T(0.0) + dt*(a_r*(Fm[1][e]) + b_r*(Fm[0][e] + Fm[2][e]));
+            }
         }
     }
 }
@@ -1324,6 +1544,25 @@ struct hmro_config {
     double epsilon;
     double grid_dx[3];
 };
+}
+
+// C view of Transport (oracle.py's _Transport mirrors it).
+extern "C" {
+struct hmro_transport {
+    int order;
+    double mu, mu_v, c_p, Pr, mu_kappa;
+};
+}
+
+inline hmro::Transport hmro_to_transport(const hmro_transport* t) {
+    hmro::Transport r;
+    r.order = t->order;
+    r.mu = t->mu;
+    r.mu_v = t->mu_v;
+    r.c_p = t->c_p;
+    r.Pr = t->Pr;
+    r.mu_kappa = t->mu_kappa;
+    return r;
 }
 
 inline hmro::Config hmro_to_config(const hmro_config* c) {

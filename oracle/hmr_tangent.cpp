@@ -70,9 +70,11 @@ extern "C" {
 // states (ncomp components each, ghosts of the last one filled); Q_out and
 // dQ_out receive the output state and its derivative along dQ_int (ghost box,
 // interior written).
+// With tr non-null the substep is NavierStokes's: the diffusive flux of
+// Q_int[stage] enters the divergence too.
 int hmro_tangent_substep(const hmro_config* cfg, const int* n, const double* dx, double dt, int stage,
                          const double* alpha, double beta, const double* Q_int, const double* dQ_int,
-                         double* Q_out, double* dQ_out) {
+                         double* Q_out, double* dQ_out, const hmro_transport* tr) {
     using hmro_dual::D;
     const hmro::Config c = hmro_to_config(cfg);
     const hmro::Box b = hmro::make_box(c.dim, n, 4);
@@ -98,20 +100,28 @@ int hmro_tangent_substep(const hmro_config* cfg, const int* n, const double* dx,
     std::vector<D*> sp;
     for (auto& s : src) sp.push_back(s.data());
     hmro::conv_flux_source<D>(c, n, dx, dt, qp[stage].data(), fp.data(), sp.data(), nullptr);
+    std::vector<std::vector<D>> dflux;
+    std::vector<D*> dfp;
+    if (tr) {
+        for (auto& f : flux) dflux.emplace_back(f.size());
+        for (auto& f : dflux) dfp.push_back(f.data());
+        hmro::diff_flux<D>(c, hmro_to_transport(tr), n, dx, dt, qp[stage].data(), dfp.data());
+    }
 
-    std::vector<const D* const*> qpp(nst), fpp(nst), spp(nst);
+    std::vector<const D* const*> qpp(nst), fpp(nst), spp(nst), dpp(nst);
     std::vector<double> betas(nst, 0.0), gammas(nst, 0.0);
     betas[stage] = beta;
     for (int s = 0; s < nst; s++) {
         qpp[s] = qp[s].data();
         fpp[s] = fp.data();
         spp[s] = sp.data();
+        dpp[s] = tr ? dfp.data() : nullptr;
     }
     std::vector<D> qo((size_t)ncomp * nc);
     std::vector<D*> qop(ncomp);
     for (int e = 0; e < ncomp; e++) qop[e] = qo.data() + (size_t)e * nc;
     hmro::rk_stage<D>(c, n, dx, nst, alpha, betas.data(), gammas.data(), qpp.data(), fpp.data(), spp.data(),
-                      qop.data(), nullptr, nullptr);
+                      qop.data(), nullptr, nullptr, tr ? dpp.data() : nullptr);
     for (size_t i = 0; i < qo.size(); i++) {
         Q_out[i] = qo[i].v;
         dQ_out[i] = qo[i].d;

@@ -37,6 +37,25 @@ class _Cfg(ctypes.Structure):
                 ("Chi", ctypes.c_double), ("epsilon", ctypes.c_double), ("grid_dx", ctypes.c_double * 3)]
 
 
+class _Transport(ctypes.Structure):
+    _fields_ = [("order", ctypes.c_int), ("mu", ctypes.c_double), ("mu_v", ctypes.c_double),
+                ("c_p", ctypes.c_double), ("Pr", ctypes.c_double), ("mu_kappa", ctypes.c_double)]
+
+
+class Transport:
+    """Navier-Stokes transport of a single-species patch: midpoint diffusive flux of
+    the given order (2 or 4), constant shear viscosity mu and bulk viscosity mu_v,
+    Prandtl thermal conductivity c_p*mu_kappa/Pr (mu_kappa defaults to mu)."""
+
+    def __init__(self, mu, c_p, Pr, mu_v=0.0, order=4, mu_kappa=None):
+        self.order = int(order)
+        self.mu, self.mu_v, self.c_p, self.Pr = float(mu), float(mu_v), float(c_p), float(Pr)
+        self.mu_kappa = float(mu if mu_kappa is None else mu_kappa)
+
+    def c(self):
+        return _Transport(self.order, self.mu, self.mu_v, self.c_p, self.Pr, self.mu_kappa)
+
+
 def build():
     """Compile the oracle library with its Makefile."""
     subprocess.check_call(["make", "-s", "-C", _HERE])
@@ -63,6 +82,10 @@ def lib():
         L.hmro_stage_threads.restype = ctypes.c_long
         L.hmro_spectral_radius.argtypes = [cp, ip, dp, dp]
         L.hmro_spectral_radius.restype = ctypes.c_double
+        tp = ctypes.POINTER(_Transport)
+        L.hmro_diff_flux.argtypes = [cp, tp, ip, dp, ctypes.c_double, dp, dp]
+        L.hmro_rk_stage_ns.argtypes = [cp, ip, dp, ctypes.c_int, dp, dp, dp, dp, dp, dp, dp, dp]
+        L.hmro_ns_rk3_advance.argtypes = [cp, tp, ip, dp, ctypes.c_double, ip, ctypes.c_int, dp]
         L.hmro_num_eqn.argtypes = [cp]
         L.hmro_num_comp.argtypes = [cp]
         _lib = L
@@ -81,7 +104,7 @@ def tangent_lib():
         dp = ctypes.POINTER(ctypes.c_double)
         ip = ctypes.POINTER(ctypes.c_int)
         L.hmro_tangent_substep.argtypes = [ctypes.POINTER(_Cfg), ip, dp, ctypes.c_double, ctypes.c_int, dp,
-                                           ctypes.c_double, dp, dp, dp, dp]
+                                           ctypes.c_double, dp, dp, dp, dp, ctypes.POINTER(_Transport)]
         _tan = L
     return _tan
 
@@ -233,11 +256,57 @@ def stage_threads(cfg, n, dx, dt, Q, nthreads):
                                     int(nthreads))
 
 
-def tangent_substep(cfg, n, dx, dt, stage, alpha, beta, Q_int, dQ_int):
+def _split_flux(cfg, n, flat):
+    out, off = [], 0
+    for s in flux_shapes(cfg, n):
+        m = int(np.prod(s))
+        out.append(flat[off:off + m].reshape(s))
+        off += m
+    return out
+
+
+def diff_flux(cfg, tr, n, dx, dt, Q):
+    """computeDiffusiveFluxOnPatch (single species): list of dt-scaled face fluxes per axis."""
+    Q = np.ascontiguousarray(Q, dtype=np.float64)
+    assert Q.shape == ghost_shape(cfg, n)
+    flat = np.zeros(sum(int(np.prod(s)) for s in flux_shapes(cfg, n)))
+    r = lib().hmro_diff_flux(ctypes.byref(cfg.c()), ctypes.byref(tr.c()), _ip(_n3(n)),
+                             _dv(list(dx) + [1.0] * (3 - len(dx))), float(dt), _dp(Q), _dp(flat))
+    if r != 0:
+        raise ValueError("the oracle's diffusive flux covers single-species patches, order 2 or 4")
+    return _split_flux(cfg, n, flat)
+
+
+def rk_stage_ns(cfg, n, dx, alpha, beta, gamma, Q_int, F_int, Fd_int, S_int):
+    """NavierStokes::advanceSingleStepOnPatch for one stage."""
+    ns = len(alpha)
+    Qi = np.ascontiguousarray(np.stack(Q_int), dtype=np.float64)
+    Fi = np.ascontiguousarray(np.stack([np.concatenate([f.ravel() for f in F]) for F in F_int]))
+    Di = np.ascontiguousarray(np.stack([np.concatenate([f.ravel() for f in F]) for F in Fd_int]))
+    Si = np.ascontiguousarray(np.stack(S_int), dtype=np.float64)
+    Qo = np.zeros(ghost_shape(cfg, n))
+    lib().hmro_rk_stage_ns(ctypes.byref(cfg.c()), _ip(_n3(n)), _dv(list(dx) + [1.0] * (3 - len(dx))), ns,
+                           _dv(alpha), _dv(beta), _dv(gamma), _dp(Qi), _dp(Fi), _dp(Di), _dp(Si), _dp(Qo))
+    return Qo
+
+
+def ns_rk3_advance(cfg, tr, n, dx, dt, periodic, nsteps, Q):
+    """nsteps SSPRK3 steps of the Navier-Stokes equations on one patch, in place."""
+    assert Q.flags["C_CONTIGUOUS"] and Q.dtype == np.float64
+    r = lib().hmro_ns_rk3_advance(ctypes.byref(cfg.c()), ctypes.byref(tr.c()), _ip(_n3(n)),
+                                  _dv(list(dx) + [1.0] * (3 - len(dx))), float(dt),
+                                  _ip(list(periodic) + [0] * (3 - len(periodic))), int(nsteps), _dp(Q))
+    if r != 0:
+        raise ValueError("the oracle's diffusive flux covers single-species patches, order 2 or 4")
+    return Q
+
+
+def tangent_substep(cfg, n, dx, dt, stage, alpha, beta, Q_int, dQ_int, transport=None):
     """Fused substep (hmr_rk_substep_patch's forward) and its tangent along dQ_int.
 
     Q_int, dQ_int: lists of stage+1 ghost-box states; returns (Q_out, dQ_out)
-    over the ghost box (interior written, ghosts zero)."""
+    over the ghost box (interior written, ghosts zero).  With a Transport the
+    substep is NavierStokes's (diffusive flux included)."""
     shape = ghost_shape(cfg, n)
     Qi = np.ascontiguousarray(np.stack([np.asarray(q, dtype=np.float64) for q in Q_int[:stage + 1]]))
     dQi = np.ascontiguousarray(np.stack([np.asarray(q, dtype=np.float64) for q in dQ_int[:stage + 1]]))
@@ -246,7 +315,8 @@ def tangent_substep(cfg, n, dx, dt, stage, alpha, beta, Q_int, dQ_int):
     dQo = np.zeros(shape)
     tangent_lib().hmro_tangent_substep(ctypes.byref(cfg.c()), _ip(_n3(n)), _dv(list(dx) + [1.0] * (3 - len(dx))),
                                        float(dt), int(stage), _dv(list(alpha)[:stage + 1]), float(beta),
-                                       _dp(Qi), _dp(dQi), _dp(Qo), _dp(dQo))
+                                       _dp(Qi), _dp(dQi), _dp(Qo), _dp(dQo),
+                                       ctypes.byref(transport.c()) if transport is not None else None)
     return Qo, dQo
 
 
