@@ -29,6 +29,9 @@ HMR_WCNS5_JS_HLLC_HLL = 0
 HMR_WCNS6_LD_HLLC_HLL = 1
 HMR_WCNS5_Z_HLLC_HLL = 2
 HMR_WCNS6_CU_M2_HLLC_HLL = 3
+HMR_DIFFUSIVE_NONE = 0
+HMR_MIDPOINT_SECOND_ORDER = 2
+HMR_MIDPOINT_FOURTH_ORDER = 4
 HMR_PRECISION_FAST = 0
 HMR_PRECISION_EXACT = 1
 
@@ -41,6 +44,7 @@ EXPORTS = [
     "hmr_level_substep", "hmr_level_step", "hmr_level_check", "hmr_level_barrier_diagnostic", "hmr_level_autotune",
     "hmr_rk_substep_patch_noalloc", "hmr_rk_substep_vjp_patch", "hmr_fill_ghosts_vjp_patch",
     "hmr_spectral_radius_patch", "hmr_level_step_cfl", "hmr_level_last_dt", "hmr_level_set_layout",
+    "hmr_diff_flux_patch", "hmr_rk_stage_ns_patch",
 ]
 
 
@@ -60,6 +64,12 @@ class Config(ctypes.Structure):
         ("constant_Chi", ctypes.c_double),
         ("constant_epsilon", ctypes.c_double),
         ("grid_dx", ctypes.c_double * 3),
+        ("diffusive_flux_reconstructor", ctypes.c_int),
+        ("species_mu", ctypes.c_double),
+        ("species_mu_v", ctypes.c_double),
+        ("species_c_p", ctypes.c_double),
+        ("species_Pr", ctypes.c_double),
+        ("species_mu_kappa", ctypes.c_double),
     ]
 
 
@@ -133,6 +143,9 @@ def load():
     L.hmr_level_step_cfl.argtypes = [vp, ctypes.c_double, vp]
     L.hmr_level_last_dt.argtypes = [vp, dp]
     L.hmr_level_set_layout.argtypes = [vp, ip, ip, ip]
+    L.hmr_diff_flux_patch.argtypes = [vp, gp, DPP, ctypes.c_double, DPP, vp]
+    L.hmr_rk_stage_ns_patch.argtypes = [vp, gp, ctypes.c_int, dp, dp, dp, DPPP, DPPP, DPPP, DPPP, DPP, DPP, DPP,
+                                        DPP, vp]
     for name in EXPORTS:
         getattr(L, name).restype = ctypes.c_int
     _lib = L

@@ -18,7 +18,9 @@ LIB = os.path.join(OUT, "libhmr_gb300.so")
 PEAK_LIB = os.path.join(OUT, "libhmr_peak.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", os.path.join(HERE, "..", "include")]
+# Host code keeps the reference's rounding too (aarch64 GCC would fuse multiply-adds).
+COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+          "-I", os.path.join(HERE, "..", "include")]
 
 UNITS = [
     ("hmr_cells.cu", "hmr_cells.o", ["-DHMR_FAST=0", "--fmad=false"]),
@@ -32,6 +34,9 @@ UNITS = [
 ] + [
     ("hmr_vjp.cu", "hmr_vjp_m%d.o" % model, ["-DHMR_FAST=0", "--fmad=true", "-DHMR_MODEL=%d" % model])
     for model in (0, 1, 2)
+] + [
+    ("hmr_diffusive.cu", "hmr_diffusive_%s.o" % form, ["-DHMR_FAST=%d" % fast, "--fmad=%s" % ("true" if fast else "false")])
+    for form, fast in (("exact", 0), ("fast", 1))
 ]
 
 

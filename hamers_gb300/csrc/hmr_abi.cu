@@ -94,6 +94,11 @@ static size_t scratch_doubles(const hmr_ctx* c, const Geom& g) {
     const long nc = ncell_of(g);
     size_t s = (size_t)(c->neq + 4) * nc;
     for (int a = 0; a < c->v.dim; a++) s += (size_t)(c->neq + 2) * nface_of(g, a);
+    if (c->P.dorder) {
+        // NavierStokes: temperature, node velocity gradient, midpoint diffusive fluxes
+        s += (size_t)(1 + c->v.dim * c->v.dim) * nc;
+        for (int a = 0; a < c->v.dim; a++) s += (size_t)c->neq * nface_of(g, a);
+    }
     return s + 64;
 }
 
@@ -121,6 +126,14 @@ static Scratch carve_scratch(const hmr_ctx* c, const Geom& g, double* base) {
             S.Fm[a] = nullptr;
             S.um[a] = nullptr;
         }
+    }
+    p += total_faces(c, g);   // queue of faces for the exact pass (face_launch)
+    S.Td = S.Gd = nullptr;
+    for (int a = 0; a < 3; a++) S.Fd[a] = nullptr;
+    if (c->P.dorder) {
+        S.Td = p; p += nc;
+        S.Gd = p; p += (size_t)c->v.dim * c->v.dim * nc;
+        for (int a = 0; a < c->v.dim; a++) { S.Fd[a] = p; p += (size_t)c->neq * nface_of(g, a); }
     }
     return S;
 }
@@ -150,6 +163,14 @@ static int face_launch(hmr_ctx* c, const Geom& g, const Scratch& S, cudaStream_t
 static int update_launch(hmr_ctx* c, const Geom& g, const Scratch& S, const UpdateArgs& U, cudaStream_t st) {
     if (c->precision == HMR_PRECISION_EXACT) return hmr_exact::launch_update(c->v, g, S, U, st);
     return hmr_fast::launch_update(c->v, g, S, U, st);
+}
+
+// NavierStokes: temperature and node gradient (always exact), then the midpoint diffusive fluxes.
+static int diff_launch(hmr_ctx* c, const Geom& g, const Scratch& S, cudaStream_t st) {
+    int r = hmr_cells::launch_diff_grad(c->v, c->P, g, S, st);
+    if (r) return r;
+    if (c->precision == HMR_PRECISION_EXACT) return hmr_diff_exact::launch_diff_mid(c->v, c->P, g, S, st);
+    return hmr_diff_fast::launch_diff_mid(c->v, c->P, g, S, st);
 }
 
 template <class C>
@@ -279,13 +300,18 @@ int hmr_read_counters(hmr_ctx* c, unsigned long long out[2], int reset) {
     return cuda_status(e);
 }
 
-// Cells + sensor + faces of one patch into the context scratch.
-static int patch_faces(hmr_ctx* c, const Geom& g, const Comp& Q, Scratch& S, cudaStream_t st) {
+// Cells + sensor + faces of one patch into the context scratch (and, with diff, the
+// midpoint diffusive fluxes).
+static int patch_faces(hmr_ctx* c, const Geom& g, const Comp& Q, Scratch& S, cudaStream_t st, bool diff = false) {
     int r = ensure_scratch(c, g);
     if (r) return r;
     S = carve_scratch(c, g, c->scratch);
     r = hmr_cells::launch_cells(c->v, c->P, g, Q, S, st);
     if (r) return r;
+    if (diff) {
+        r = diff_launch(c, g, S, st);
+        if (r) return r;
+    }
     r = hmr_cells::launch_sensor(c->v, g, S, st);
     if (r) return r;
     return face_launch(c, g, S, st);
@@ -331,12 +357,65 @@ int hmr_rk_substep_patch(hmr_ctx* c, const hmr_patch_geometry* pg, int stage, co
     U.dt = dt;
     for (int e = 0; e < 3 * MAX_COMP; e++) U.Fout.p[e] = nullptr;
     for (int e = 0; e < MAX_COMP; e++) U.Sout.p[e] = nullptr;
+    U.dorder = c->P.dorder;
     const Geom g = make_geom(c->v.dim, pg);
     cudaStream_t st = as_stream(stream);
     Scratch scr;
-    int r = patch_faces(c, g, U.Qint[stage], scr, st);
+    int r = patch_faces(c, g, U.Qint[stage], scr, st, c->P.dorder != 0);
     if (r) return r;
     return update_launch(c, g, scr, U, st);
+}
+
+int hmr_diff_flux_patch(hmr_ctx* c, const hmr_patch_geometry* pg, const double* const* Q, double dt,
+                        double* const* flux, void* stream) {
+    if (!c || !valid_geom(c->v.dim, pg)) return HMR_ERR_ARGUMENT;
+    if (!c->P.dorder) return HMR_ERR_UNSUPPORTED;
+    Comp q;
+    FluxComp F;
+    if (!load_comp(q, Q, c->ncomp)) return HMR_ERR_ARGUMENT;
+    if (!load_flux(F, flux, c->v.dim * c->neq)) return HMR_ERR_ARGUMENT;
+    const Geom g = make_geom(c->v.dim, pg);
+    cudaStream_t st = as_stream(stream);
+    int r = ensure_scratch(c, g);
+    if (r) return r;
+    const Scratch S = carve_scratch(c, g, c->scratch);
+    r = hmr_cells::launch_cells(c->v, c->P, g, q, S, st);
+    if (r) return r;
+    r = diff_launch(c, g, S, st);
+    if (r) return r;
+    if (c->precision == HMR_PRECISION_EXACT) return hmr_diff_exact::launch_diff_faces_out(c->v, c->P, g, S, dt, F, st);
+    return hmr_diff_fast::launch_diff_faces_out(c->v, c->P, g, S, dt, F, st);
+}
+
+int hmr_rk_stage_ns_patch(hmr_ctx* c, const hmr_patch_geometry* pg, int ncoef, const double* alpha,
+                          const double* beta, const double* gamma, const double* const* const* Q_int,
+                          const double* const* const* F_int, const double* const* const* Fd_int,
+                          const double* const* const* S_int, double* const* Q, double* const* flux_acc,
+                          double* const* diff_flux_acc, double* const* source_acc, void* stream) {
+    if (!c || !valid_geom(c->v.dim, pg) || ncoef < 1 || ncoef > 4 || !alpha || !beta) return HMR_ERR_ARGUMENT;
+    if (!c->P.dorder) return HMR_ERR_UNSUPPORTED;
+    if (!Q_int || !F_int || !Fd_int || !S_int) return HMR_ERR_ARGUMENT;
+    Comp Qi[4], Si[4], Qo, Sa;
+    FluxComp Fi[4], Di[4], Fa, Da;
+    for (int n = 0; n < ncoef; n++) {
+        if (!load_comp(Qi[n], Q_int[n], c->ncomp)) return HMR_ERR_ARGUMENT;
+        if (!load_flux(Fi[n], F_int[n], c->v.dim * c->neq)) return HMR_ERR_ARGUMENT;
+        if (!load_flux(Di[n], Fd_int[n], c->v.dim * c->neq)) return HMR_ERR_ARGUMENT;
+        if (!load_comp(Si[n], S_int[n], c->neq)) return HMR_ERR_ARGUMENT;
+    }
+    if (!load_comp(Qo, Q, c->ncomp)) return HMR_ERR_ARGUMENT;
+    const bool acc = flux_acc != nullptr || diff_flux_acc != nullptr || source_acc != nullptr;
+    if (acc) {
+        if (!gamma || !load_flux(Fa, flux_acc, c->v.dim * c->neq) ||
+            !load_flux(Da, diff_flux_acc, c->v.dim * c->neq) || !load_comp(Sa, source_acc, c->neq))
+            return HMR_ERR_ARGUMENT;
+    } else {
+        for (int e = 0; e < 3 * MAX_COMP; e++) Fa.p[e] = Da.p[e] = nullptr;
+        for (int e = 0; e < MAX_COMP; e++) Sa.p[e] = nullptr;
+    }
+    const Geom g = make_geom(c->v.dim, pg);
+    return hmr_cells::launch_rk_stage(c->v, g, ncoef, alpha, beta, acc ? gamma : nullptr, Qi, Fi, Si, Qo, Fa, Sa,
+                                      as_stream(stream), Di, acc ? &Da : nullptr);
 }
 
 int hmr_rk_stage_patch(hmr_ctx* c, const hmr_patch_geometry* pg, int ncoef, const double* alpha,
@@ -393,6 +472,12 @@ int hmr_rk_substep_vjp_patch(hmr_ctx* c, const hmr_patch_geometry* pg, int stage
                             (size_t)(9 * c->neq) + (size_t)(9 + 4 * c->v.nsp) + 1;
     size_t need = 0;
     for (int a = 0; a < c->v.dim; a++) need += per_face * nface_of(g, a);
+    // Navier-Stokes: midpoint adjoints, node-gradient and primitive-variable adjoints
+    const int nmb = c->v.dim + (c->v.dim + 1) + 2 * (c->v.dim - 1);
+    if (c->P.dorder) {
+        for (int a = 0; a < c->v.dim; a++) need += (size_t)nmb * nface_of(g, a);
+        need += (size_t)(c->v.dim * c->v.dim + c->neq) * ncell_of(g);
+    }
     need *= sizeof(double);
     if (need > c->vjp_bytes) {
         if (c->vjp) cudaFree(c->vjp);
@@ -415,9 +500,20 @@ int hmr_rk_substep_vjp_patch(hmr_ctx* c, const hmr_patch_geometry* pg, int stage
         A.Fp[a] = p; p += (size_t)(9 + 4 * c->v.nsp) * nf;
         A.okf[a] = reinterpret_cast<unsigned char*>(p); p += nf;   // one double per face reserved
     }
+    for (int a = 0; a < 3; a++) A.Mb[a] = nullptr;
+    A.Gdb = A.Dv = nullptr;
+    if (c->P.dorder) {
+        for (int a = 0; a < c->v.dim; a++) { A.Mb[a] = p; p += (size_t)nmb * nface_of(g, a); }
+        A.Gdb = p; p += (size_t)c->v.dim * c->v.dim * ncell_of(g);
+        A.Dv = p; p += (size_t)c->neq * ncell_of(g);
+    }
     if (beta != 0.0) {
         r = hmr_cells::launch_cells(c->v, c->P, g, A.Qs, S, st);
         if (r) return r;
+        if (c->P.dorder) {
+            r = hmr_cells::launch_diff_grad(c->v, c->P, g, S, st);
+            if (r) return r;
+        }
         r = hmr_cells::launch_sensor(c->v, g, S, st);
         if (r) return r;
     }
@@ -562,6 +658,7 @@ extern "C" {
 int hmr_level_create(hmr_ctx* c, int np, const hmr_patch_geometry* geoms, hmr_level** out) {
     if (!c || np < 1 || !geoms || !out) return HMR_ERR_ARGUMENT;
     *out = nullptr;
+    if (c->P.dorder) return HMR_ERR_UNSUPPORTED;   // the batched form covers the Euler equations
     for (int p = 0; p < np; p++)
         if (!valid_geom(c->v.dim, &geoms[p])) return HMR_ERR_ARGUMENT;
     hmr_level* lv = new (std::nothrow) hmr_level();

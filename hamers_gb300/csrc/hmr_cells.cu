@@ -4,6 +4,8 @@
 // combination of Euler::advanceSingleStepOnPatch (src/apps/Euler/Euler.cpp:1003-1680).
 #include <cuda_runtime.h>
 
+#include <cstring>
+
 #include "hmr_launch.h"
 
 namespace hmr_cells {
@@ -281,6 +283,9 @@ struct StageArgs {
     Comp Qout;
     FluxComp Facc;
     Comp Sacc;
+    int ns;              // NavierStokes: the diffusive fluxes Fd enter the divergence (and Fdacc)
+    FluxComp Fd[4];
+    FluxComp Fdacc;
 };
 
 template <int DIM, int MODEL, int NSP>
@@ -310,10 +315,24 @@ __global__ void __launch_bounds__(THREADS) rk_stage_kernel(Geom g, StageArgs A) 
                 for (int e = 0; e < NEQ; e++) {
                     const double* Fx = A.F[n].p[e];
                     const double* Fy = A.F[n].p[NEQ + e];
-                    double div = sub_(-(Fx[fx1] - Fx[fx0])/g.dx[0], (Fy[fy1] - Fy[fy0])/g.dx[1]);
-                    if (DIM == 3) {
-                        const double* Fz = A.F[n].p[2 * NEQ + e];
-                        div = sub_(div, (Fz[fz1] - Fz[fz0])/g.dx[2]);
+                    double div;
+                    if (A.ns) {
+                        // NavierStokes.cpp:1743-1749 (2D), 2085-2092 (3D)
+                        const double* Dx = A.Fd[n].p[e];
+                        const double* Dy = A.Fd[n].p[NEQ + e];
+                        div = -(Fx[fx1] - Fx[fx0] + Dx[fx1] - Dx[fx0])/g.dx[0] -
+                              (Fy[fy1] - Fy[fy0] + Dy[fy1] - Dy[fy0])/g.dx[1];
+                        if (DIM == 3) {
+                            const double* Fz = A.F[n].p[2 * NEQ + e];
+                            const double* Dz = A.Fd[n].p[2 * NEQ + e];
+                            div = div - (Fz[fz1] - Fz[fz0] + Dz[fz1] - Dz[fz0])/g.dx[2];
+                        }
+                    } else {
+                        div = sub_(-(Fx[fx1] - Fx[fx0])/g.dx[0], (Fy[fy1] - Fy[fy0])/g.dx[1]);
+                        if (DIM == 3) {
+                            const double* Fz = A.F[n].p[2 * NEQ + e];
+                            div = sub_(div, (Fz[fz1] - Fz[fz0])/g.dx[2]);
+                        }
                     }
                     q[e] = add_(q[e], mul_(A.beta[n], add_(div, A.S[n].p[e][t])));
                 }
@@ -341,6 +360,24 @@ __global__ void __launch_bounds__(THREADS) rk_stage_kernel(Geom g, StageArgs A) 
                     }
                     A.Sacc.p[e][t] = add_(A.Sacc.p[e][t], mul_(A.gamma[n], A.S[n].p[e][t]));
                 }
+                if (A.ns && A.Fdacc.p[0] != nullptr) {
+                    // NavierStokes.cpp:2170-2260: the diffusive fluxes are accumulated alike
+#pragma unroll
+                    for (int e = 0; e < NEQ; e++) {
+                        double* Fx = A.Fdacc.p[e];
+                        double* Fy = A.Fdacc.p[NEQ + e];
+                        Fx[fx0] = add_(Fx[fx0], mul_(A.gamma[n], A.Fd[n].p[e][fx0]));
+                        if (i == g.n[0] - 1) Fx[fx1] = add_(Fx[fx1], mul_(A.gamma[n], A.Fd[n].p[e][fx1]));
+                        Fy[fy0] = add_(Fy[fy0], mul_(A.gamma[n], A.Fd[n].p[NEQ + e][fy0]));
+                        if (j == g.n[1] - 1) Fy[fy1] = add_(Fy[fy1], mul_(A.gamma[n], A.Fd[n].p[NEQ + e][fy1]));
+                        if (DIM == 3) {
+                            double* Fz = A.Fdacc.p[2 * NEQ + e];
+                            Fz[fz0] = add_(Fz[fz0], mul_(A.gamma[n], A.Fd[n].p[2 * NEQ + e][fz0]));
+                            if (k == g.n[2] - 1)
+                                Fz[fz1] = add_(Fz[fz1], mul_(A.gamma[n], A.Fd[n].p[2 * NEQ + e][fz1]));
+                        }
+                    }
+                }
             }
         }
 #pragma unroll
@@ -348,11 +385,34 @@ __global__ void __launch_bounds__(THREADS) rk_stage_kernel(Geom g, StageArgs A) 
     }
 }
 
+template <int DIM, int ORD>
+__global__ void __launch_bounds__(THREADS) diff_grad_kernel(Params P, Geom g, Scratch S) {
+    const long nc = ncell_of(g);
+    for (long x = (long)blockIdx.x * blockDim.x + threadIdx.x; x < nc; x += (long)gridDim.x * blockDim.x)
+        diff_grad_item<DIM, ORD>(P, g, S, x);
+}
+
+int launch_diff_grad(const Variant& v, const Params& P, const Geom& g, const Scratch& S, cudaStream_t st) {
+    if (v.model != SINGLE_SPECIES || (P.dorder != 2 && P.dorder != 4)) return -2;
+    const int b = grid_for(ncell_of(g));
+    if (v.dim == 2 && P.dorder == 2) diff_grad_kernel<2, 2><<<b, THREADS, 0, st>>>(P, g, S);
+    else if (v.dim == 2) diff_grad_kernel<2, 4><<<b, THREADS, 0, st>>>(P, g, S);
+    else if (P.dorder == 2) diff_grad_kernel<3, 2><<<b, THREADS, 0, st>>>(P, g, S);
+    else diff_grad_kernel<3, 4><<<b, THREADS, 0, st>>>(P, g, S);
+    return (int)cudaPeekAtLastError();
+}
+
 int launch_rk_stage(const Variant& v, const Geom& g, int ncoef, const double* alpha, const double* beta,
                     const double* gamma, const Comp* Qint, const FluxComp* Fint, const Comp* Sint, const Comp& Qout,
-                    const FluxComp& Facc, const Comp& Sacc, cudaStream_t st) {
+                    const FluxComp& Facc, const Comp& Sacc, cudaStream_t st, const FluxComp* Fdint,
+                    const FluxComp* Fdacc) {
     if (ncoef < 1 || ncoef > 4) return -1;
+    if (Fdint && v.model != SINGLE_SPECIES) return -2;
     StageArgs A;
+    std::memset(&A, 0, sizeof(A));
+    A.ns = Fdint != nullptr;
+    for (int n = 0; Fdint && n < ncoef; n++) A.Fd[n] = Fdint[n];
+    if (Fdacc) A.Fdacc = *Fdacc;
     A.ncoef = ncoef;
     for (int n = 0; n < ncoef; n++) {
         A.alpha[n] = alpha[n];

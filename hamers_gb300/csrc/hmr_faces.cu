@@ -301,6 +301,7 @@ level_kernel(Params P, LevelArgs L) {
         U.Qout = w.Qout;
         U.Fout.p[0] = nullptr;   // flux/source outputs are not produced by the batched form
         U.Sout.p[0] = nullptr;
+        U.dorder = 0;            // the batched form advances the Euler equations
         update_item<DIM, MODEL, NSP>(w.g, w.S, U, t - w.off_update);
     }
 }

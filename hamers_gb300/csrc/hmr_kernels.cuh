@@ -46,6 +46,9 @@ struct Scratch {
     double* Omega;    // ncell
     double* Fm[3];    // NEQ x nface(a)
     double* um[3];    // nface(a) (five-equation model only)
+    double* Td;       // ncell: temperature (Navier-Stokes only)
+    double* Gd;       // DIM*DIM x ncell: node velocity gradient d_d u_c (Navier-Stokes only)
+    double* Fd[3];    // NEQ x nface(a): diffusive flux at the midpoints (Navier-Stokes only)
 };
 
 __host__ __device__ inline long ncell_of(const Geom& g) { return (long)g.G[0] * g.G[1] * g.G[2]; }
@@ -278,6 +281,12 @@ __device__ __forceinline__ void redo_push(const Redo& R, int axis, long item) {
 // ---------------------------------------------------------------------------
 // Phase 4: update of one interior cell.
 // ---------------------------------------------------------------------------
+}  // namespace hmr
+
+#include "hmr_diffusive.cuh"
+
+namespace hmr {
+
 struct UpdateArgs {
     Comp Qint[3];        // stage states Q_int[0..nst-1] (ghost box); Qint[nst-1] is the current one
     double alpha[3];
@@ -287,6 +296,7 @@ struct UpdateArgs {
     Comp Qout;           // ghost-box arrays; interior written
     FluxComp Fout;       // optional: dt-scaled face fluxes, SAMRAI side layout (dim*NEQ arrays)
     Comp Sout;           // optional: source (interior, NEQ arrays), accumulated
+    int dorder;          // 0: Euler; 2 or 4: NavierStokes, the midpoint diffusive fluxes in S.Fd enter
 };
 
 // Node (cell-centre) flux of component e in direction A.
@@ -404,14 +414,33 @@ __device__ __forceinline__ void update_item(const Geom& g, const Scratch& S, con
 
     if (U.Qout.p[0] == nullptr) return;   // flux/source only (computeConvectiveFluxAndSourceOnPatch)
 
-    // Euler::advanceSingleStepOnPatch (Euler.cpp:1188-1660): Q = 0, += alpha_n Q_n, += beta (div + S).
+    // NavierStokes: diffusive face fluxes of the current stage (single species).
+    double dl[3][NEQ], dr[3][NEQ];
+    bool ns = false;
+    if constexpr (MODEL == SINGLE_SPECIES) {
+        if (U.beta != 0.0 && U.dorder == 4) { diff_cell_faces<DIM, 4, NEQ>(g, S, U.dt, i, j, k, dl, dr); ns = true; }
+        else if (U.beta != 0.0 && U.dorder == 2) { diff_cell_faces<DIM, 2, NEQ>(g, S, U.dt, i, j, k, dl, dr); ns = true; }
+    }
+
+    // Euler::advanceSingleStepOnPatch (Euler.cpp:1188-1660): Q = 0, += alpha_n Q_n, += beta (div + S);
+    // NavierStokes::advanceSingleStepOnPatch (NavierStokes.cpp:1743-1749, 2085-2092) adds the
+    // diffusive fluxes to the divergence.
     double qn[NEQ];
 #pragma unroll
     for (int e = 0; e < NEQ; e++) {
         double acc = 0.0;
         for (int n = 0; n < U.nst; n++)
             if (U.alpha[n] != 0.0) acc += U.alpha[n]*U.Qint[n].p[e][x];
-        if (U.beta != 0.0) {
+        if (U.beta != 0.0 && ns) {
+            if constexpr (DIM == 2) {
+                acc += U.beta*(-(fr[0][e] - fl[0][e] + dr[0][e] - dl[0][e])/g.dx[0] -
+                               (fr[1][e] - fl[1][e] + dr[1][e] - dl[1][e])/g.dx[1] + (0.0 + src[e]));
+            } else {
+                acc += U.beta*(-(fr[0][e] - fl[0][e] + dr[0][e] - dl[0][e])/g.dx[0] -
+                               (fr[1][e] - fl[1][e] + dr[1][e] - dl[1][e])/g.dx[1] -
+                               (fr[2][e] - fl[2][e] + dr[2][e] - dl[2][e])/g.dx[2] + (0.0 + src[e]));
+            }
+        } else if (U.beta != 0.0) {
             if constexpr (DIM == 2) {
                 acc += U.beta*(-(fr[0][e] - fl[0][e])/g.dx[0] - (fr[1][e] - fl[1][e])/g.dx[1] + (0.0 + src[e]));
             } else {

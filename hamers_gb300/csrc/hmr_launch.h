@@ -30,10 +30,47 @@ inline bool reconstructor_known(int r) {
            r == HMR_WCNS6_CU_M2_HLLC_HLL;
 }
 
+// Node-to-midpoint interpolation of a cell value (…MidpointSecondOrder.cpp, …FourthOrder.cpp
+// interpolateDataFromNodeToMidpoint), in the reference's operation order; host code is built
+// with -ffp-contract=off so that the products are not fused into the sums.
+inline double host_mid_value(int order, double LL, double L, double R, double RR) {
+    if (order == 2) return double(1)/double(2)*(R + L);
+    return double(9)/double(16)*(R + L) + -double(1)/double(16)*(RR + LL);
+}
+
+// Navier-Stokes constants of Params (single species): the side values of the constant
+// transport properties, interpolated from cells as every side variable is, and the
+// combinations D0, D1 of FlowModelDiffusiveFluxUtilitiesSingleSpecies.cpp:2471-2799 use.
+inline int diffusive_params(const hmr_config* cfg, Params& P) {
+    const int order = cfg->diffusive_flux_reconstructor;
+    P.dorder = 0;
+    P.dS43 = P.dS23 = P.dmu = P.dkappa = P.dTc = 0.0;
+    if (order == HMR_DIFFUSIVE_NONE) return HMR_OK;
+    if (order != HMR_MIDPOINT_SECOND_ORDER && order != HMR_MIDPOINT_FOURTH_ORDER) return HMR_ERR_UNSUPPORTED;
+    if (cfg->flow_model != HMR_SINGLE_SPECIES) return HMR_ERR_UNSUPPORTED;
+    if (!(cfg->species_mu >= 0.0) || !(cfg->species_mu_v >= 0.0) || !(cfg->species_c_p >= 0.0) ||
+        !(cfg->species_Pr > 0.0) || !(cfg->species_mu_kappa >= 0.0) || !(cfg->species_gamma[0] > 1.0))
+        return HMR_ERR_ARGUMENT;
+    const double mu = cfg->species_mu, mu_v = cfg->species_mu_v;
+    const double kappa = cfg->species_c_p*cfg->species_mu_kappa/cfg->species_Pr;   // Prandtl.cpp:63
+    const double mu_s = host_mid_value(order, mu, mu, mu, mu);
+    const double mu_v_s = host_mid_value(order, mu_v, mu_v, mu_v, mu_v);
+    P.dorder = order;
+    P.dmu = mu_s;
+    P.dkappa = host_mid_value(order, kappa, kappa, kappa, kappa);
+    P.dS43 = double(4)/double(3)*mu_s + mu_v_s;
+    P.dS23 = double(2)/double(3)*mu_s - mu_v_s;
+    const double gamma = cfg->species_gamma[0];
+    const double c_v = double(1)/(gamma - double(1))*cfg->species_R[0];   // MixingRulesIdealGas.cpp:116-120
+    P.dTc = (gamma - double(1))*c_v;
+    return HMR_OK;
+}
+
 // Scheme constants of Params from a configuration whose reconstructor is known:
 // p, q, C, alpha_tau, and WCNS6-CU-M2's epsilon dx^2 and Chi dx^2 per axis, each
 // evaluated as the reference writes it (epsilon*dx*dx, left to right) from the
-// grid geometry's spacing.  Returns HMR_ERR_ARGUMENT for constants out of range.
+// grid geometry's spacing, and the Navier-Stokes constants.  Returns HMR_ERR_ARGUMENT for
+// constants out of range, HMR_ERR_UNSUPPORTED for a diffusive flux the context cannot compute.
 inline int scheme_params(const hmr_config* cfg, Params& P) {
     if (cfg->constant_p < 1 || cfg->constant_p > 8 || cfg->constant_q < 1 || cfg->constant_q > 8)
         return HMR_ERR_ARGUMENT;
@@ -51,7 +88,7 @@ inline int scheme_params(const hmr_config* cfg, Params& P) {
             P.cu_x[d] = cfg->constant_Chi*dx*dx;
         }
     }
-    return HMR_OK;
+    return diffusive_params(cfg, P);
 }
 
 struct Variant {
@@ -127,11 +164,28 @@ int launch_spectral_patch(const hmr::Variant& v, const hmr::Params& P, const hmr
 int launch_spectral_level(const hmr::Variant& v, const hmr::Params& P, const hmr::PatchWork* work, int npatch,
                           long total_interior, unsigned long long* d_max, cudaStream_t st);
 int launch_stable_dt(const unsigned long long* d_max, double cfl, double* d_dt, cudaStream_t st);
+// Euler / NavierStokes advanceSingleStepOnPatch; with Fdint (ncoef diffusive flux sets) the
+// NavierStokes form, and Fdacc (optional) accumulates them with gamma.
 int launch_rk_stage(const hmr::Variant& v, const hmr::Geom& g, int ncoef, const double* alpha,
                     const double* beta, const double* gamma, const hmr::Comp* Qint, const hmr::FluxComp* Fint,
                     const hmr::Comp* Sint, const hmr::Comp& Qout, const hmr::FluxComp& Facc, const hmr::Comp& Sacc,
-                    cudaStream_t st);
+                    cudaStream_t st, const hmr::FluxComp* Fdint = nullptr, const hmr::FluxComp* Fdacc = nullptr);
+// Navier-Stokes cell phase: temperature and node velocity gradient into S.Td, S.Gd.
+int launch_diff_grad(const hmr::Variant& v, const hmr::Params& P, const hmr::Geom& g, const hmr::Scratch& S,
+                     cudaStream_t st);
 }
+
+// hmr_diffusive.cu, built once per arithmetic form (namespaces hmr_diff_exact, hmr_diff_fast):
+// midpoint diffusive fluxes into S.Fd, and the dt-scaled face fluxes in SAMRAI side layout.
+#define HMR_DECLARE_DIFF_LAUNCHERS(NS)                                                                         \
+    namespace NS {                                                                                             \
+    int launch_diff_mid(const hmr::Variant& v, const hmr::Params& P, const hmr::Geom& g, const hmr::Scratch& S, \
+                        cudaStream_t st);                                                                      \
+    int launch_diff_faces_out(const hmr::Variant& v, const hmr::Params& P, const hmr::Geom& g,                 \
+                              const hmr::Scratch& S, double dt, const hmr::FluxComp& F, cudaStream_t st);      \
+    }
+HMR_DECLARE_DIFF_LAUNCHERS(hmr_diff_exact)
+HMR_DECLARE_DIFF_LAUNCHERS(hmr_diff_fast)
 
 // hmr_faces.cu is built once per arithmetic form, flow model and scheme set
 // (twelve translation units compiled in parallel); each defines these launchers

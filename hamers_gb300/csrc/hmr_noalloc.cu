@@ -69,6 +69,7 @@ extern "C" int hmr_rk_substep_patch_noalloc(const hmr_config* cfg, const hmr_pat
     const int dim = cfg->dim;
     if (dim != 2 && dim != 3) return HMR_ERR_ARGUMENT;
     if (!reconstructor_known(cfg->convective_flux_reconstructor)) return HMR_ERR_UNSUPPORTED;
+    if (cfg->diffusive_flux_reconstructor != HMR_DIFFUSIVE_NONE) return HMR_ERR_UNSUPPORTED;
     if (cfg->precision != HMR_PRECISION_FAST && cfg->precision != HMR_PRECISION_EXACT) return HMR_ERR_ARGUMENT;
     {
         Params probe;  // scheme constants in range (and, for WCNS6-CU-M2, the grid spacing set)
@@ -153,6 +154,8 @@ extern "C" int hmr_rk_substep_patch_noalloc(const hmr_config* cfg, const hmr_pat
             S.um[a] = nullptr;
         }
     }
+    S.Td = S.Gd = nullptr;   // Euler equations only
+    for (int a = 0; a < 3; a++) S.Fd[a] = nullptr;
     Redo R;
     R.list = reinterpret_cast<unsigned long long*>(p);
     R.count = reinterpret_cast<unsigned int*>(bytes);   // zeroed by the fast face launch before use

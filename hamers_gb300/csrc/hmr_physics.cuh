@@ -48,6 +48,10 @@ struct Params {
     double C, alpha_tau;
     double cu_e[3];                    // WCNS6-CU-M2 epsilon*dx*dx per axis (dx: the grid geometry's spacing)
     double cu_x[3];                    // WCNS6-CU-M2 Chi*dx*dx per axis
+    // Navier-Stokes (single species): side values of 4/3 mu + mu_v, 2/3 mu - mu_v, mu, kappa
+    // (constant cell values interpolated to the midpoints), and (gamma - 1) c_v for T.
+    int dorder;                        // 0 Euler; 2, 4 midpoint diffusive flux of that order
+    double dS43, dS23, dmu, dkappa, dTc;
 };
 
 template <int DIM, int MODEL, int NSP>

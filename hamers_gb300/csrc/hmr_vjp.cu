@@ -114,6 +114,39 @@ cell_bwd_kernel(Params P, Geom g, Scratch S, VjpArgs VA) {
         cell_bwd_item<DIM, MODEL, NSP>(P, g, S, VA, x);
 }
 
+template <int DIM, int ORD, int AX>
+__global__ void __launch_bounds__(VJP_THREADS)
+diff_mid_bwd_kernel(Params P, Geom g, Scratch S, VjpArgs VA) {
+    const long nf = nface_of(g, AX);
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < nf; t += (long)gridDim.x * blockDim.x)
+        diff_mid_bwd_item<DIM, ORD, AX>(P, g, S, VA, t);
+}
+
+template <int DIM, int ORD>
+__global__ void __launch_bounds__(VJP_THREADS) diff_gd_bwd_kernel(Geom g, VjpArgs VA) {
+    const long nc = ncell_of(g);
+    for (long x = (long)blockIdx.x * blockDim.x + threadIdx.x; x < nc; x += (long)gridDim.x * blockDim.x)
+        diff_gd_bwd_item<DIM, ORD>(g, VA, x);
+}
+
+template <int DIM, int ORD>
+__global__ void __launch_bounds__(VJP_THREADS) diff_cell_bwd_kernel(Params P, Geom g, Scratch S, VjpArgs VA) {
+    const long nc = ncell_of(g);
+    for (long x = (long)blockIdx.x * blockDim.x + threadIdx.x; x < nc; x += (long)gridDim.x * blockDim.x)
+        diff_cell_bwd_item<DIM, ORD>(P, g, S, VA, x);
+}
+
+// Navier-Stokes: the diffusive flux's share of the primitive-variable adjoints (into VA.Dv).
+template <int DIM, int ORD>
+static void launch_diff_bwd(const Params& P, const Geom& g, const Scratch& S, const VjpArgs& A, cudaStream_t st) {
+    diff_mid_bwd_kernel<DIM, ORD, 0><<<grid_for(nface_of(g, 0), VJP_THREADS), VJP_THREADS, 0, st>>>(P, g, S, A);
+    diff_mid_bwd_kernel<DIM, ORD, 1><<<grid_for(nface_of(g, 1), VJP_THREADS), VJP_THREADS, 0, st>>>(P, g, S, A);
+    if constexpr (DIM == 3)
+        diff_mid_bwd_kernel<DIM, ORD, 2><<<grid_for(nface_of(g, 2), VJP_THREADS), VJP_THREADS, 0, st>>>(P, g, S, A);
+    diff_gd_bwd_kernel<DIM, ORD><<<grid_for(ncell_of(g), VJP_THREADS), VJP_THREADS, 0, st>>>(g, A);
+    diff_cell_bwd_kernel<DIM, ORD><<<grid_for(ncell_of(g), VJP_THREADS), VJP_THREADS, 0, st>>>(P, g, S, A);
+}
+
 int launch_vjp(const Variant& v, const Params& P, const Geom& g, const Scratch& S, const VjpArgs& A,
                cudaStream_t st) {
     return dispatch(v, [&](auto t) {
@@ -122,6 +155,13 @@ int launch_vjp(const Variant& v, const Params& P, const Geom& g, const Scratch& 
             launch_face_axis<T, 0>(P, g, S, A, st);
             launch_face_axis<T, 1>(P, g, S, A, st);
             if constexpr (T::DIM == 3) launch_face_axis<T, 2>(P, g, S, A, st);
+        }
+        if constexpr (T::MODEL == SINGLE_SPECIES) {
+            if (A.beta != 0.0 && A.Dv != nullptr) {
+                if (P.dorder == 4) launch_diff_bwd<T::DIM, 4>(P, g, S, A, st);
+                else if (P.dorder == 2) launch_diff_bwd<T::DIM, 2>(P, g, S, A, st);
+                else return -2;
+            }
         }
         cell_bwd_kernel<T::DIM, T::MODEL, T::NSP>
             <<<grid_for(ncell_of(g), VJP_THREADS), VJP_THREADS, 0, st>>>(P, g, S, A);

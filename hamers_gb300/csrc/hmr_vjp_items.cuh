@@ -19,6 +19,8 @@
 //     accumulates into Qb_in[s]; adds alpha_n Qb_out into Qb_in[n].
 #pragma once
 
+#include <type_traits>
+
 #include "hmr_adjoint.cuh"
 
 namespace hmr {
@@ -38,6 +40,11 @@ struct VjpArgs {
     double* Kb[3];    // per axis: 9*NEQ x nface(a) forward smoothness indicators (and WCNS6-LD sigma)
     double* Fp[3];    // per axis: FaceLayout<NSP>::NFP x nface(a) projection factors and partial adjoints
     unsigned char* okf[3];   // per axis: nface(a) bounds flags
+    // Navier-Stokes (null for the Euler equations): per axis diff_nmb<DIM>() x nface(a) midpoint
+    // adjoints, DIM*DIM x ncell node-gradient adjoints, NEQ x ncell primitive-variable adjoints
+    double* Mb[3];
+    double* Gdb;
+    double* Dv;
 };
 
 // Adjoint of the pre-rewrite stage output (component e < NEQ) at a cell:
@@ -540,6 +547,10 @@ __device__ __forceinline__ void cell_bwd_item(const Params& P, const Geom& g, co
 #pragma unroll
         for (int e = 0; e < NEQ; e++) { V[e] = S.V[e * nc + x]; Vb[e] = 0.0; }
         double rb = 0.0, cb = 0.0;
+        if (VA.Dv != nullptr) {
+#pragma unroll
+            for (int e = 0; e < NEQ; e++) Vb[e] = VA.Dv[e * nc + x];
+        }
         cell_axis_bwd<DIM, MODEL, NSP, 0>(g, S, VA, i, j, k, x, Q, V, Vb, rb, cb, Qb);
         cell_axis_bwd<DIM, MODEL, NSP, 1>(g, S, VA, i, j, k, x, Q, V, Vb, rb, cb, Qb);
         if constexpr (DIM == 3) cell_axis_bwd<DIM, MODEL, NSP, 2>(g, S, VA, i, j, k, x, Q, V, Vb, rb, cb, Qb);
@@ -555,3 +566,5 @@ __device__ __forceinline__ void cell_bwd_item(const Params& P, const Geom& g, co
 }
 
 }  // namespace hmr
+
+#include "hmr_diffusive_vjp.cuh"

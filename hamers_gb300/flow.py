@@ -7,6 +7,10 @@ Names follow HAMeRS:
                                    (include/flow/convective_flux_reconstructors/ConvectiveFluxReconstructor.hpp:23-124)
   Euler                         -- the RungeKuttaPatchStrategy of src/apps/Euler/Euler.cpp
                                    (computeFluxesAndSourcesOnPatch :904, advanceSingleStepOnPatch :1003)
+  DiffusiveFluxReconstructor    -- DiffusiveFluxReconstructorMidpoint (second / fourth order)
+                                   (src/flow/diffusive_flux_reconstructors/midpoint/DiffusiveFluxReconstructorMidpoint.cpp:38)
+  NavierStokes                  -- the patch strategy of src/apps/Navier-Stokes/NavierStokes.cpp
+                                   (computeFluxesAndSourcesOnPatch :1104, advanceSingleStepOnPatch :1249)
   RungeKuttaLevelIntegrator     -- SSPRK3 stage loop (RungeKuttaLevelIntegrator.cpp:1672-1748)
   BatchedLevel                  -- all patches of a level per substep in one persistent kernel
 
@@ -37,6 +41,11 @@ _RECONSTRUCTORS = {
     "WCNS6_CU_M2_HLLC_HLL": L.HMR_WCNS6_CU_M2_HLLC_HLL,
 }
 
+_DIFFUSIVE = {
+    "MIDPOINT_SECOND_ORDER": L.HMR_MIDPOINT_SECOND_ORDER,
+    "MIDPOINT_FOURTH_ORDER": L.HMR_MIDPOINT_FOURTH_ORDER,
+}
+
 # SSPRK(3,3), RungeKuttaLevelIntegrator.cpp:3909-3927
 RK3_ALPHA = [[1.0], [3.0 / 4.0, 1.0 / 4.0], [1.0 / 3.0, 0.0, 2.0 / 3.0]]
 RK3_BETA = [[1.0], [0.0, 1.0 / 4.0], [0.0, 0.0, 2.0 / 3.0]]
@@ -50,9 +59,18 @@ def _stream_ptr(stream):
 
 
 class FlowModel:
-    """Flow model selection: 'SINGLE_SPECIES', 'FOUR_EQN_CONSERVATIVE' or 'FIVE_EQN_ALLAIRE', ideal gas."""
+    """Flow model selection: 'SINGLE_SPECIES', 'FOUR_EQN_CONSERVATIVE' or 'FIVE_EQN_ALLAIRE', ideal gas.
 
-    def __init__(self, flow_model, dim, species_gamma, species_R=None):
+    transport (Navier-Stokes, single species): the reference's mixing-rule keys
+      species_mu    Equation_of_shear_viscosity_mixing_rules (equation_of_shear_viscosity CONSTANT)
+      species_mu_v  Equation_of_bulk_viscosity_mixing_rules (CONSTANT; default 0)
+      species_c_p, species_Pr
+                    Equation_of_thermal_conductivity_mixing_rules (PRANDTL: kappa = c_p mu/Pr,
+                    with that block's own species_mu, given here as species_mu_kappa and
+                    defaulting to species_mu)
+    """
+
+    def __init__(self, flow_model, dim, species_gamma, species_R=None, transport=None):
         if flow_model not in _FLOW_MODELS:
             raise ValueError(f"unknown flow model {flow_model!r}")
         self.name = flow_model
@@ -61,6 +79,16 @@ class FlowModel:
         self.species_gamma = [float(g) for g in species_gamma]
         self.num_species = len(self.species_gamma)
         self.species_R = [float(r) for r in (species_R or [1.0] * self.num_species)]
+        self.transport = None
+        if transport is not None:
+            t = dict(transport)
+            self.transport = {
+                "species_mu": float(t["species_mu"]),
+                "species_mu_v": float(t.get("species_mu_v", 0.0)),
+                "species_c_p": float(t["species_c_p"]),
+                "species_Pr": float(t["species_Pr"]),
+                "species_mu_kappa": float(t.get("species_mu_kappa", t["species_mu"])),
+            }
 
     def getNumberOfEquations(self):
         if self.model == L.HMR_SINGLE_SPECIES:
@@ -110,9 +138,15 @@ class ConvectiveFluxReconstructor:
     precision: 'fast' (default, <= 1e-12 relative) or 'exact' (bitwise to the reference order).
     """
 
-    def __init__(self, name, flow_model, db=None, precision="fast", grid_geometry=None):
+    def __init__(self, name, flow_model, db=None, precision="fast", grid_geometry=None,
+                 diffusive_flux_reconstructor=None):
         if name not in _RECONSTRUCTORS:
             raise ValueError(f"unknown convective flux reconstructor {name!r}")
+        if diffusive_flux_reconstructor is not None:
+            if diffusive_flux_reconstructor not in _DIFFUSIVE:
+                raise ValueError(f"unknown diffusive flux reconstructor {diffusive_flux_reconstructor!r}")
+            if flow_model.transport is None:
+                raise ValueError("a diffusive flux reconstructor needs the flow model's transport properties")
         db = db or {}
         lib = L.load()
         cfg = L.Config()
@@ -131,6 +165,11 @@ class ConvectiveFluxReconstructor:
                 cfg.grid_dx[d] = float(v)
         elif name == "WCNS6_CU_M2_HLLC_HLL":
             raise ValueError("WCNS6_CU_M2_HLLC_HLL needs grid_geometry (its weights use the grid spacing)")
+        if diffusive_flux_reconstructor is not None:
+            cfg.diffusive_flux_reconstructor = _DIFFUSIVE[diffusive_flux_reconstructor]
+            for key, v in flow_model.transport.items():
+                setattr(cfg, key, v)
+        self.diffusive = diffusive_flux_reconstructor
         cfg.precision = L.HMR_PRECISION_EXACT if precision == "exact" else L.HMR_PRECISION_FAST
         self.flow_model = flow_model
         self.name = name
@@ -274,6 +313,74 @@ class Euler:
         per = (ctypes.c_int * 3)(*(list(periodic) + [0] * (3 - len(periodic))))
         L.check("hmr_fill_ghosts_vjp_patch", self._lib.hmr_fill_ghosts_vjp_patch(
             self.rec.ctx, ctypes.byref(g), q, per, _stream_ptr(stream)))
+
+
+class DiffusiveFluxReconstructor:
+    """MIDPOINT_SECOND_ORDER / MIDPOINT_FOURTH_ORDER diffusive flux behind the C ABI.
+
+    It runs in the context of a ConvectiveFluxReconstructor created with
+    diffusive_flux_reconstructor=<name> (one context holds the whole
+    Navier-Stokes configuration, so that the fused substep can use both)."""
+
+    def __init__(self, convective):
+        if convective.diffusive is None:
+            raise ValueError("the convective reconstructor was created without a diffusive flux reconstructor")
+        self.conv = convective
+        self.name = convective.diffusive
+        self._lib = convective._lib
+
+    def getDiffusiveFluxNumberOfGhostCells(self):
+        return 1 if self.name == "MIDPOINT_SECOND_ORDER" else 3
+
+    def computeDiffusiveFluxOnPatch(self, patch, diffusive_flux, dt, stream=None):
+        """dt-scaled diffusive face fluxes (overwritten), same layout as the convective flux."""
+        rec = self.conv
+        g = patch.geometry()
+        q, _k1 = L.ptr_array(_comp_ptrs(patch.data, rec.ncomp))
+        f, _k2 = L.ptr_array(sum((_comp_ptrs(t, rec.neq) for t in diffusive_flux[:rec.flow_model.dim]), []))
+        L.check("hmr_diff_flux_patch", self._lib.hmr_diff_flux_patch(
+            rec.ctx, ctypes.byref(g), q, float(dt), f, _stream_ptr(stream)))
+
+
+class NavierStokes(Euler):
+    """Patch strategy of src/apps/Navier-Stokes/NavierStokes.cpp: convective + diffusive fluxes.
+
+    The reconstructor's context carries the diffusive flux reconstructor; substep() is then
+    NavierStokes's fused stage and RungeKuttaLevelIntegrator advances the Navier-Stokes
+    equations."""
+
+    def __init__(self, reconstructor):
+        super().__init__(reconstructor)
+        self.diff = DiffusiveFluxReconstructor(reconstructor)
+
+    def computeFluxesAndSourcesOnPatch(self, patch, convective_flux, diffusive_flux, source, dt, stream=None):
+        source.zero_()   # NavierStokes.cpp:1112-1126
+        self.rec.computeConvectiveFluxAndSourceOnPatch(patch, convective_flux, source, dt, stream)
+        self.diff.computeDiffusiveFluxOnPatch(patch, diffusive_flux, dt, stream)
+
+    def advanceSingleStepOnPatch(self, patch, alpha, beta, gamma, Q_int, F_int, Fd_int, S_int,
+                                 flux_acc=None, diff_flux_acc=None, source_acc=None, stream=None):
+        """Q = sum alpha_n Q_int[n] + beta_n (-div (F_int[n] + Fd_int[n]) + S_int[n]) into patch.data."""
+        rec = self.rec
+        nc = len(alpha)
+        g = patch.geometry()
+        a = (ctypes.c_double * nc)(*alpha)
+        b = (ctypes.c_double * nc)(*beta)
+        c = (ctypes.c_double * nc)(*gamma)
+        qi, k1 = L.ptr_array2([_comp_ptrs(t, rec.ncomp) for t in Q_int])
+        fi, k2 = L.ptr_array2([sum((_comp_ptrs(f, rec.neq) for f in F), []) for F in F_int])
+        di, k3 = L.ptr_array2([sum((_comp_ptrs(f, rec.neq) for f in F), []) for F in Fd_int])
+        si, k4 = L.ptr_array2([_comp_ptrs(t, rec.neq) for t in S_int])
+        qo, k5 = L.ptr_array(_comp_ptrs(patch.data, rec.ncomp))
+        fa = da = sa = None
+        keep = []
+        if flux_acc is not None:
+            fa, k6 = L.ptr_array(sum((_comp_ptrs(f, rec.neq) for f in flux_acc), []))
+            da, k7 = L.ptr_array(sum((_comp_ptrs(f, rec.neq) for f in diff_flux_acc), []))
+            sa, k8 = L.ptr_array(_comp_ptrs(source_acc, rec.neq))
+            keep += [k6, k7, k8]
+        L.check("hmr_rk_stage_ns_patch", self._lib.hmr_rk_stage_ns_patch(
+            rec.ctx, ctypes.byref(g), nc, a, b, c, qi, fi, di, si, qo, fa, da, sa, _stream_ptr(stream)))
 
 
 class RungeKuttaLevelIntegrator:

@@ -73,6 +73,15 @@ typedef enum {
     HMR_WCNS6_CU_M2_HLLC_HLL = 3
 } hmr_reconstructor;
 
+/* NavierStokes diffusive_flux_reconstructor (DiffusiveFluxReconstructorManager.cpp):
+ * none (the Euler equations) or the midpoint reconstructors of the given order
+ * (DiffusiveFluxReconstructorMidpointSecondOrder / ...FourthOrder).  Single species only. */
+typedef enum {
+    HMR_DIFFUSIVE_NONE = 0,
+    HMR_MIDPOINT_SECOND_ORDER = 2,
+    HMR_MIDPOINT_FOURTH_ORDER = 4
+} hmr_diffusive;
+
 typedef enum {
     HMR_PRECISION_FAST = 0,   /* regrouped FP64 with FMA; <= 1e-12 relative to the reference */
     HMR_PRECISION_EXACT = 1   /* the reference's operation order, no FMA: bitwise equal to it */
@@ -96,6 +105,12 @@ typedef struct {
                                                   WCNS6-CU-M2 scales its weights by it on every level
                                                   (WCNS6-CU-M2-HLLC-HLL.cpp:367-368).  Required (> 0 on the
                                                   used axes) for WCNS6-CU-M2, ignored by the other schemes. */
+    int diffusive_flux_reconstructor;          /* hmr_diffusive; HMR_DIFFUSIVE_NONE by default */
+    double species_mu;                         /* Equation_of_shear_viscosity_mixing_rules (CONSTANT) */
+    double species_mu_v;                       /* Equation_of_bulk_viscosity_mixing_rules (CONSTANT) */
+    double species_c_p;                        /* Equation_of_thermal_conductivity_mixing_rules (PRANDTL): */
+    double species_Pr;                         /*   kappa = c_p*mu/Pr with that model's own constant */
+    double species_mu_kappa;                   /*   shear viscosity species_mu */
 } hmr_config;
 
 typedef struct {
@@ -144,10 +159,32 @@ int hmr_rk_stage_patch(hmr_ctx* ctx, const hmr_patch_geometry* geom, int num_coe
                        const double* const* const* S_int, double* const* Q,
                        double* const* flux_acc, double* const* source_acc, void* stream);
 
+/* DiffusiveFluxReconstructorMidpoint::computeDiffusiveFluxOnPatch
+ * (src/flow/diffusive_flux_reconstructors/midpoint/DiffusiveFluxReconstructorMidpoint.cpp:38-2312):
+ * dt-scaled diffusive face fluxes (overwritten; same layout as the convective flux) of one
+ * single-species patch whose ghost cells are filled.  Needs a context created with a
+ * diffusive_flux_reconstructor; HMR_ERR_UNSUPPORTED otherwise. */
+int hmr_diff_flux_patch(hmr_ctx* ctx, const hmr_patch_geometry* geom, const double* const* Q, double dt,
+                        double* const* flux, void* stream);
+
+/* NavierStokes::advanceSingleStepOnPatch (src/apps/Navier-Stokes/NavierStokes.cpp:1249-2330):
+ * hmr_rk_stage_patch with the diffusive fluxes Fd_int[n] entering the divergence,
+ *   Q = sum_n alpha[n] Q_int[n] + beta[n] * (-div (F_int[n] + Fd_int[n]) + S_int[n]),
+ * and diff_flux_acc += gamma[n] Fd_int[n] beside flux_acc and source_acc (all three optional
+ * together).  Single-species contexts with a diffusive_flux_reconstructor. */
+int hmr_rk_stage_ns_patch(hmr_ctx* ctx, const hmr_patch_geometry* geom, int num_coeffs,
+                          const double* alpha, const double* beta, const double* gamma,
+                          const double* const* const* Q_int, const double* const* const* F_int,
+                          const double* const* const* Fd_int, const double* const* const* S_int,
+                          double* const* Q, double* const* flux_acc, double* const* diff_flux_acc,
+                          double* const* source_acc, void* stream);
+
 /* Fused flux + stage update of stage `stage` of a Shu-Osher scheme whose flux weight is
  * non-zero only for the current stage (SSPRK3 is): computes the convective flux and source
  * of Q_int[stage] and writes Q_out = sum_n alpha[n] Q_int[n] + beta * (-div F + S) on the
- * interior.  Q_int has stage+1 states; Q_int[stage] must have its ghost cells filled. */
+ * interior.  Q_int has stage+1 states; Q_int[stage] must have its ghost cells filled.
+ * With a diffusive_flux_reconstructor in the context this is NavierStokes's stage: the
+ * diffusive flux of Q_int[stage] enters the divergence too. */
 int hmr_rk_substep_patch(hmr_ctx* ctx, const hmr_patch_geometry* geom, int stage, const double* alpha,
                          double beta, const double* const* const* Q_int, double dt, double* const* Q_out,
                          void* stream);

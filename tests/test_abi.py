@@ -77,3 +77,18 @@ def test_reconstructor_names_and_grid_geometry_requirement():
         flow.ConvectiveFluxReconstructor("WCNS6_CU_M2_HLLC_HLL", fm)
     with pytest.raises(ValueError):
         flow.ConvectiveFluxReconstructor("WCNS6_TEST", fm)
+
+
+def test_diffusive_flux_needs_single_species_and_valid_transport(lib):
+    cfg = L.Config()
+    lib.hmr_config_default(ctypes.byref(cfg), L.HMR_FIVE_EQN_ALLAIRE, L.HMR_WCNS5_JS_HLLC_HLL, 2, 2)
+    cfg.diffusive_flux_reconstructor = L.HMR_MIDPOINT_FOURTH_ORDER
+    cfg.species_mu, cfg.species_c_p, cfg.species_Pr, cfg.species_mu_kappa = 0.01, 1.0, 0.7, 0.01
+    ctx = ctypes.c_void_p()
+    assert lib.hmr_ctx_create(ctypes.byref(cfg), ctypes.byref(ctx)) == L.HMR_ERR_UNSUPPORTED
+    lib.hmr_config_default(ctypes.byref(cfg), L.HMR_SINGLE_SPECIES, L.HMR_WCNS5_JS_HLLC_HLL, 3, 1)
+    cfg.diffusive_flux_reconstructor = 6
+    assert lib.hmr_ctx_create(ctypes.byref(cfg), ctypes.byref(ctx)) == L.HMR_ERR_UNSUPPORTED
+    cfg.diffusive_flux_reconstructor = L.HMR_MIDPOINT_SECOND_ORDER
+    cfg.species_Pr = 0.0
+    assert lib.hmr_ctx_create(ctypes.byref(cfg), ctypes.byref(ctx)) == L.HMR_ERR_ARGUMENT
