@@ -63,6 +63,8 @@ def parse():
                     help="skip the batched-vs-per-patch measurement on uneven 3D patches")
     ap.add_argument("--no-peak", action="store_true", help="skip the FP64 peak microbenchmark")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint/forward cost measurement")
+    ap.add_argument("--c4", action="store_true",
+                    help="also time the 3D Navier-Stokes Taylor-Green workload and its adjoint (128^3, ~1 min)")
     ap.add_argument("--c5", action="store_true",
                     help="also run the 3-level 3D five-equation batched substep + amplitude adjoint")
     ap.add_argument("--uneven-patches", type=int, default=512)
@@ -387,6 +389,102 @@ def c5_level_and_adjoint(args, flow, base=128, reps=3):
             "grad_amplitudes_norm": float(grad.norm())}
 
 
+def c4_navier_stokes(args, flow, N=128, nsteps=100, every=10, fd_dirs=16, fd_steps=10):
+    """3D Navier-Stokes Taylor-Green vortex, 128^3 periodic on [0, 2 pi)^3 (Mach 0.1, Re 1600,
+    Pr 0.72, gamma 1.4), WCNS5-JS + HLLC-HLL with the fourth-order midpoint diffusive flux,
+    per-patch fused substeps: 100 SSPRK3 steps checkpointed every 10, then the reverse sweep
+    (recompute + substep VJPs) for the gradient of the final kinetic energy.  The gradient is
+    checked against central differences along 16 seeded directions (seed 3) over the first
+    checkpoint segment (10 steps) of the same problem."""
+    import torch
+    from hamers_gb300 import problems as P
+    Qnp, dx = P.taylor_green_3d(N)
+    tr = P.taylor_green_transport()
+    dt = P.taylor_green_dt(Qnp[:, 4:-4, 4:-4, 4:-4], dx, mu=tr["species_mu"], prandtl=tr["species_Pr"])
+    fm = flow.FlowModel("SINGLE_SPECIES", 3, [1.4], transport=tr)
+    rec = flow.ConvectiveFluxReconstructor("WCNS5_JS_HLLC_HLL", fm, precision=args.precision,
+                                           diffusive_flux_reconstructor="MIDPOINT_FOURTH_ORDER")
+    ns = flow.NavierStokes(rec)
+    n, per = [N] * 3, [1, 1, 1]
+    dV = dx[0] * dx[1] * dx[2]
+    Q0 = torch.from_numpy(Qnp).cuda()
+    stream = torch.cuda.current_stream()
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+
+    def kinetic_and_grad(Q):
+        rho = Q[0]
+        u = Q[1:4] / rho
+        G = torch.zeros_like(Q)
+        G[0, 4:-4, 4:-4, 4:-4] = (-0.5 * (u * u).sum(dim=0) * dV)[4:-4, 4:-4, 4:-4]
+        G[1:4, 4:-4, 4:-4, 4:-4] = (u * dV)[:, 4:-4, 4:-4, 4:-4]
+        J = 0.5 * float(((Q[1:4] * Q[1:4]).sum(dim=0) / rho)[4:-4, 4:-4, 4:-4].sum()) * dV
+        return J, G
+
+    # warm-up (graph-free per-patch path: fill + 4-5 kernels per substep)
+    Qw = Q0.clone()
+    flow.RungeKuttaLevelIntegrator(ns, flow.Patch(n, dx, Qw), per).advance(dt, nsteps=2)
+    torch.cuda.synchronize()
+    Q = Q0.clone()
+    integ = flow.RungeKuttaLevelIntegrator(ns, flow.Patch(n, dx, Q), per)
+    e[0].record(stream)
+    integ.advance(dt, nsteps=nsteps, checkpoint_every=every)
+    e[1].record(stream)
+    torch.cuda.synchronize()
+    t_fwd = e[0].elapsed_time(e[1])
+    J, G = kinetic_and_grad(Q)
+    e[2].record(stream)
+    grad = integ.adjoint(G)
+    e[3].record(stream)
+    torch.cuda.synchronize()
+    t_adj = e[2].elapsed_time(e[3])
+    cells = N ** 3
+    out = {"workload": "3D Navier-Stokes Taylor-Green vortex 128^3 periodic, Mach 0.1, Re 1600, Pr 0.72, "
+                       "WCNS5-JS + HLLC-HLL + 4th-order midpoint diffusive flux, 100 SSPRK3 steps, "
+                       "checkpoint every 10, gradient of the final kinetic energy",
+           "precision": args.precision, "dt": dt, "steps": nsteps,
+           "forward_ms": t_fwd, "forward_cell_updates_per_s": cells * 3 * nsteps / (t_fwd * 1e-3),
+           "adjoint_ms": t_adj, "adjoint_over_forward": t_adj / t_fwd,
+           "final_kinetic_energy": J}
+    # gradient check over the first checkpoint segment, at the vortex with smooth 0.05
+    # perturbations (the exact vortex sits on non-differentiable points of the flux: w = 0
+    # and mirror-symmetric faces), along 16 smooth random directions (seed 3)
+    Qp0 = torch.from_numpy(P.taylor_green_3d(N, perturb=0.05)[0]).cuda()
+    Qa = Qp0.clone()
+    seg = flow.RungeKuttaLevelIntegrator(ns, flow.Patch(n, dx, Qa), per)
+    seg.advance(dt, nsteps=fd_steps, checkpoint_every=fd_steps)
+    _, Gs = kinetic_and_grad(Qa)
+    gs = seg.adjoint(Gs)
+    rng = np.random.default_rng(3)
+    scale = Qp0[:, 4:-4, 4:-4, 4:-4].abs().mean(dim=(1, 2, 3))
+    ax = (torch.arange(N, dtype=torch.float64, device="cuda") + 0.5) * dx[0]
+    z, y, x = torch.meshgrid(ax, ax, ax, indexing="ij")
+    errs = []
+    for _ in range(fd_dirs):
+        v = torch.zeros_like(Qp0)
+        for q in range(5):
+            k = rng.integers(1, 4, size=(3, 3))
+            ph = rng.uniform(0, 2 * np.pi, 3)
+            a = rng.standard_normal(3)
+            v[q, 4:-4, 4:-4, 4:-4] = float(scale[q]) * sum(
+                float(a[m]) * torch.sin(int(k[m, 0]) * x + int(k[m, 1]) * y + int(k[m, 2]) * z + float(ph[m]))
+                for m in range(3))
+        ad = float((gs * v).sum())
+        e_h = []
+        for h in (1e-6, 1e-7):
+            Js = []
+            for sgn in (1.0, -1.0):
+                Qs = Qp0 + sgn * h * v
+                flow.RungeKuttaLevelIntegrator(ns, flow.Patch(n, dx, Qs), per).advance(dt, nsteps=fd_steps)
+                Js.append(kinetic_and_grad(Qs)[0])
+            e_h.append(abs((Js[0] - Js[1]) / (2 * h) - ad) / max(abs(ad), 1e-300))
+        errs.append(min(e_h))
+    out["fd_check"] = {"directions": fd_dirs, "steps": fd_steps, "h": [1e-6, 1e-7], "seed": 3,
+                       "base": "Taylor-Green vortex + smooth perturbations of amplitude 0.05",
+                       "max_rel_err": max(errs), "median_rel_err": float(np.median(errs))}
+    rec.close()
+    return out
+
+
 def cpu_baseline_oracle(Q, n, dx, dt, budget_s=15.0, threads=None):
     """Oracle stage throughput on the host cores on a bounded sample (rows of the patch)."""
     from oracle import oracle as O
@@ -608,6 +706,11 @@ def main():
             line["adjoint"] = adjoint_cost(args, flow, Qnp, n, dx, dt)
         except Exception as exc:  # report, never lose the headline line
             line["adjoint"] = {"error": str(exc)[:300]}
+    if args.c4:
+        try:
+            line["c4"] = c4_navier_stokes(args, flow)
+        except Exception as exc:  # report, never lose the headline line
+            line["c4"] = {"error": str(exc)[:300]}
     if args.c5:
         try:
             line["c5"] = c5_level_and_adjoint(args, flow)

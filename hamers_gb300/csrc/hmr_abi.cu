@@ -520,6 +520,74 @@ int hmr_rk_substep_vjp_patch(hmr_ctx* c, const hmr_patch_geometry* pg, int stage
     return hmr_vjp::launch_vjp(c->v, c->P, g, S, A, st);
 }
 
+int hmr_sync_fluxes_patch(hmr_ctx* c, const hmr_patch_geometry* pg, double* const* Q, const double* const* flux,
+                          const double* const* diff_flux, const double* const* source, void* stream) {
+    if (!c || !valid_geom(c->v.dim, pg)) return HMR_ERR_ARGUMENT;
+    if (diff_flux && !c->P.dorder) return HMR_ERR_UNSUPPORTED;
+    Comp q, S;
+    FluxComp F, D;
+    if (!load_comp(q, Q, c->ncomp) || !load_flux(F, flux, c->v.dim * c->neq) || !load_comp(S, source, c->neq))
+        return HMR_ERR_ARGUMENT;
+    if (diff_flux && !load_flux(D, diff_flux, c->v.dim * c->neq)) return HMR_ERR_ARGUMENT;
+    const Geom g = make_geom(c->v.dim, pg);
+    return hmr_cells::launch_sync(c->v, g, q, F, diff_flux ? &D : nullptr, S, as_stream(stream));
+}
+
+// Placement of a fine patch over a coarse patch; HMR_ERR_ARGUMENT unless the ratio is at
+// least 1 and the fine box is aligned with it.
+static int coarsen_args(const hmr_ctx* c, const hmr_patch_geometry* coarse, const int* coarse_lo,
+                        const hmr_patch_geometry* fine, const int* fine_lo, const int* ratio, CoarsenArgs& C) {
+    const int dim = c->v.dim;
+    if (!valid_geom(dim, coarse) || !valid_geom(dim, fine) || !coarse_lo || !fine_lo || !ratio)
+        return HMR_ERR_ARGUMENT;
+    std::memset(&C, 0, sizeof(C));
+    C.gc = make_geom(dim, coarse);
+    C.gf = make_geom(dim, fine);
+    for (int d = 0; d < 3; d++) {
+        if (d >= dim) {
+            C.r[d] = 1; C.clo[d] = C.flo[d] = 0; C.lo[d] = 0; C.hi[d] = 1;
+            continue;
+        }
+        if (ratio[d] < 1 || ratio[d] > 64) return HMR_ERR_ARGUMENT;
+        C.r[d] = ratio[d];
+        C.clo[d] = coarse_lo[d];
+        C.flo[d] = fine_lo[d];
+        const long flo = fine_lo[d], fhi = (long)fine_lo[d] + fine->n[d];
+        if (((flo % ratio[d]) + ratio[d]) % ratio[d] != 0 || ((fhi % ratio[d]) + ratio[d]) % ratio[d] != 0)
+            return HMR_ERR_ARGUMENT;
+        const long lo = std::max<long>(flo / ratio[d], coarse_lo[d]) - coarse_lo[d];
+        const long hi = std::min<long>(fhi / ratio[d], (long)coarse_lo[d] + coarse->n[d]) - coarse_lo[d];
+        C.lo[d] = (int)lo;
+        C.hi[d] = (int)std::max(hi, lo);
+    }
+    return HMR_OK;
+}
+
+int hmr_coarsen_patch(hmr_ctx* c, const hmr_patch_geometry* coarse, const int* coarse_lo,
+                      const hmr_patch_geometry* fine, const int* fine_lo, const int* ratio,
+                      const double* const* Q_fine, double* const* Q_coarse, void* stream) {
+    if (!c) return HMR_ERR_ARGUMENT;
+    CoarsenArgs C;
+    int r = coarsen_args(c, coarse, coarse_lo, fine, fine_lo, ratio, C);
+    if (r) return r;
+    Comp qf, qc;
+    if (!load_comp(qf, Q_fine, c->ncomp) || !load_comp(qc, Q_coarse, c->ncomp)) return HMR_ERR_ARGUMENT;
+    return hmr_cells::launch_coarsen_cells(c->v.dim, C, qf, qc, c->ncomp, as_stream(stream));
+}
+
+int hmr_coarsen_fluxsum_patch(hmr_ctx* c, const hmr_patch_geometry* coarse, const int* coarse_lo,
+                              const hmr_patch_geometry* fine, const int* fine_lo, const int* ratio,
+                              const double* const* fine_flux, double* const* coarse_flux, void* stream) {
+    if (!c) return HMR_ERR_ARGUMENT;
+    CoarsenArgs C;
+    int r = coarsen_args(c, coarse, coarse_lo, fine, fine_lo, ratio, C);
+    if (r) return r;
+    FluxComp ff, fc;
+    if (!load_flux(ff, fine_flux, c->v.dim * c->neq) || !load_flux(fc, coarse_flux, c->v.dim * c->neq))
+        return HMR_ERR_ARGUMENT;
+    return hmr_cells::launch_coarsen_fluxsum(c->v.dim, C, ff, fc, c->neq, as_stream(stream));
+}
+
 int hmr_spectral_radius_patch(hmr_ctx* c, const hmr_patch_geometry* pg, const double* const* Q, double* d_max,
                               void* stream) {
     if (!c || !valid_geom(c->v.dim, pg) || !d_max) return HMR_ERR_ARGUMENT;

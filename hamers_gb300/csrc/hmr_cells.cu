@@ -385,6 +385,171 @@ __global__ void __launch_bounds__(THREADS) rk_stage_kernel(Geom g, StageArgs A) 
     }
 }
 
+// ---------------------------------------------------------------------------
+// Refluxing.  synchronizeFluxes (Euler.cpp:1682-1943, NavierStokes.cpp:2425-2700):
+// Q += -div (F [+ Fd]) + S on the interior with the time-integrated fluxes, then the
+// five-equation last volume fraction 1 - sum.
+// ---------------------------------------------------------------------------
+struct SyncArgs {
+    Comp Q;
+    FluxComp F, Fd;
+    Comp S;
+    int ns;
+};
+
+template <int DIM, int MODEL, int NSP>
+__global__ void __launch_bounds__(THREADS) sync_kernel(Geom g, SyncArgs A) {
+    using M = Model<DIM, MODEL, NSP>;
+    constexpr int NEQ = M::NEQ;
+    const long nint = ninterior_of(g);
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < nint; t += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % g.n[0]);
+        const int j = (int)((t / g.n[0]) % g.n[1]);
+        const int k = DIM == 3 ? (int)(t / ((long)g.n[0] * g.n[1])) : 0;
+        const long x = cidx<DIM>(g, i, j, k);
+        const long fx0 = side_idx<DIM, 0>(g, i, j, k), fx1 = side_idx<DIM, 0>(g, i + 1, j, k);
+        const long fy0 = side_idx<DIM, 1>(g, i, j, k), fy1 = side_idx<DIM, 1>(g, i, j + 1, k);
+        long fz0 = 0, fz1 = 0;
+        if (DIM == 3) { fz0 = side_idx<DIM, 2>(g, i, j, k); fz1 = side_idx<DIM, 2>(g, i, j, k + 1); }
+        double q[NEQ];
+#pragma unroll
+        for (int e = 0; e < NEQ; e++) {
+            const double* Fx = A.F.p[e];
+            const double* Fy = A.F.p[NEQ + e];
+            double d;
+            if (A.ns) {
+                const double* Dx = A.Fd.p[e];
+                const double* Dy = A.Fd.p[NEQ + e];
+                d = -(Fx[fx1] - Fx[fx0] + Dx[fx1] - Dx[fx0])/g.dx[0] -
+                    (Fy[fy1] - Fy[fy0] + Dy[fy1] - Dy[fy0])/g.dx[1];
+                if (DIM == 3) {
+                    const double* Fz = A.F.p[2 * NEQ + e];
+                    const double* Dz = A.Fd.p[2 * NEQ + e];
+                    d = d - (Fz[fz1] - Fz[fz0] + Dz[fz1] - Dz[fz0])/g.dx[2];
+                }
+            } else {
+                d = -(Fx[fx1] - Fx[fx0])/g.dx[0] - (Fy[fy1] - Fy[fy0])/g.dx[1];
+                if (DIM == 3) {
+                    const double* Fz = A.F.p[2 * NEQ + e];
+                    d = d - (Fz[fz1] - Fz[fz0])/g.dx[2];
+                }
+            }
+            q[e] = A.Q.p[e][x] + (d + A.S.p[e][t]);
+            A.Q.p[e][x] = q[e];
+        }
+        if constexpr (MODEL == FIVE_EQN_ALLAIRE) {
+            double zl = 1.0;
+#pragma unroll
+            for (int s = 0; s < NSP - 1; s++) zl = zl - q[M::IZ + s];
+            A.Q.p[M::NCOMP - 1][x] = zl;
+        }
+    }
+}
+
+int launch_sync(const Variant& v, const Geom& g, const Comp& Q, const FluxComp& F, const FluxComp* Fd,
+                const Comp& S, cudaStream_t st) {
+    if (Fd && v.model != SINGLE_SPECIES) return -2;
+    SyncArgs A;
+    std::memset(&A, 0, sizeof(A));
+    A.Q = Q;
+    A.F = F;
+    A.S = S;
+    A.ns = Fd != nullptr;
+    if (Fd) A.Fd = *Fd;
+    return dispatch(v, [&](auto t) {
+        using T = decltype(t);
+        sync_kernel<T::DIM, T::MODEL, T::NSP><<<grid_for(ninterior_of(g)), THREADS, 0, st>>>(g, A);
+        return (int)cudaPeekAtLastError();
+    });
+}
+
+// Coarsening between a fine patch and a coarse patch of the next coarser level (SAMRAI's
+// CONSERVATIVE_COARSEN, restated: mean of the fine cells / faces, summed in fine index order
+// and multiplied once by 1/r^k).  Placement: first interior cell lo and size n of each patch in
+// its level's index space; the fine box is aligned with the ratio.
+template <int DIM>
+__global__ void __launch_bounds__(THREADS) coarsen_cells_kernel(CoarsenArgs C, Comp Qf, Comp Qc, int ncomp) {
+    const long e0 = C.hi[0] - C.lo[0], e1 = C.hi[1] - C.lo[1], e2 = C.hi[2] - C.lo[2];
+    const long ncov = e0 * e1 * e2;
+    const double w = double(1)/double(C.r[0] * C.r[1] * C.r[2]);
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < ncov * ncomp; t += (long)gridDim.x * blockDim.x) {
+        const int e = (int)(t / ncov);
+        const long u = t % ncov;
+        const int i = C.lo[0] + (int)(u % e0), j = C.lo[1] + (int)((u / e0) % e1), k = C.lo[2] + (int)(u / (e0 * e1));
+        const int fi = (i + C.clo[0]) * C.r[0] - C.flo[0];
+        const int fj = (j + C.clo[1]) * C.r[1] - C.flo[1];
+        const int fk = (k + C.clo[2]) * C.r[2] - C.flo[2];
+        double sum = 0.0;
+        for (int q2 = 0; q2 < C.r[2]; q2++)
+            for (int q1 = 0; q1 < C.r[1]; q1++)
+                for (int q0 = 0; q0 < C.r[0]; q0++) sum += Qf.p[e][cidx<DIM>(C.gf, fi + q0, fj + q1, fk + q2)];
+        Qc.p[e][cidx<DIM>(C.gc, i, j, k)] = sum*w;
+    }
+}
+
+// One outer side of the fine patch normal to axis A: each coarse face it covers takes the
+// mean of its fine faces.  ff, cf: face index along A in the fine and coarse patch.
+template <int DIM, int A>
+__global__ void __launch_bounds__(THREADS) coarsen_fluxsum_kernel(CoarsenArgs C, FluxComp Ff, FluxComp Fc, int neq,
+                                                                 int ff, int cf) {
+    const long e0 = A == 0 ? 1 : C.hi[0] - C.lo[0];
+    const long e1 = A == 1 ? 1 : C.hi[1] - C.lo[1];
+    const long e2 = A == 2 ? 1 : C.hi[2] - C.lo[2];
+    const long nfc = e0 * e1 * e2;
+    const int r0 = A == 0 ? 1 : C.r[0], r1 = A == 1 ? 1 : C.r[1], r2 = A == 2 ? 1 : C.r[2];
+    const double w = double(1)/double(r0 * r1 * r2);
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < nfc * neq; t += (long)gridDim.x * blockDim.x) {
+        const int e = (int)(t / nfc);
+        const long u = t % nfc;
+        int c[3] = {C.lo[0] + (int)(u % e0), C.lo[1] + (int)((u / e0) % e1), C.lo[2] + (int)(u / (e0 * e1))};
+        c[A] = cf;
+        int f0[3];
+#pragma unroll
+        for (int d = 0; d < 3; d++) f0[d] = (c[d] + C.clo[d]) * C.r[d] - C.flo[d];
+        f0[A] = ff;
+        double sum = 0.0;
+        for (int q2 = 0; q2 < r2; q2++)
+            for (int q1 = 0; q1 < r1; q1++)
+                for (int q0 = 0; q0 < r0; q0++)
+                    sum += Ff.p[A * neq + e][side_idx<DIM, A>(C.gf, f0[0] + q0, f0[1] + q1, f0[2] + q2)];
+        Fc.p[A * neq + e][side_idx<DIM, A>(C.gc, c[0], c[1], c[2])] = sum*w;
+    }
+}
+
+int launch_coarsen_cells(int dim, const CoarsenArgs& C, const Comp& Qf, const Comp& Qc, int ncomp, cudaStream_t st) {
+    const long ncov = (long)(C.hi[0] - C.lo[0]) * (C.hi[1] - C.lo[1]) * (C.hi[2] - C.lo[2]);
+    if (ncov <= 0) return 0;
+    if (dim == 2) coarsen_cells_kernel<2><<<grid_for(ncov * ncomp), THREADS, 0, st>>>(C, Qf, Qc, ncomp);
+    else coarsen_cells_kernel<3><<<grid_for(ncov * ncomp), THREADS, 0, st>>>(C, Qf, Qc, ncomp);
+    return (int)cudaPeekAtLastError();
+}
+
+template <int DIM, int A>
+static void fluxsum_sides(const CoarsenArgs& C, const FluxComp& Ff, const FluxComp& Fc, int neq, cudaStream_t st) {
+    long nfc = 1;
+    for (int d = 0; d < 3; d++) if (d != A) nfc *= C.hi[d] - C.lo[d];
+    if (nfc <= 0) return;
+    for (int side = 0; side < 2; side++) {
+        const int ff = side == 0 ? 0 : C.gf.n[A];
+        const int cf = (C.flo[A] + ff) / C.r[A] - C.clo[A];
+        if (cf < 0 || cf > C.gc.n[A]) continue;
+        coarsen_fluxsum_kernel<DIM, A><<<grid_for(nfc * neq), THREADS, 0, st>>>(C, Ff, Fc, neq, ff, cf);
+    }
+}
+
+int launch_coarsen_fluxsum(int dim, const CoarsenArgs& C, const FluxComp& Ff, const FluxComp& Fc, int neq,
+                           cudaStream_t st) {
+    if (dim == 2) {
+        fluxsum_sides<2, 0>(C, Ff, Fc, neq, st);
+        fluxsum_sides<2, 1>(C, Ff, Fc, neq, st);
+    } else {
+        fluxsum_sides<3, 0>(C, Ff, Fc, neq, st);
+        fluxsum_sides<3, 1>(C, Ff, Fc, neq, st);
+        fluxsum_sides<3, 2>(C, Ff, Fc, neq, st);
+    }
+    return (int)cudaPeekAtLastError();
+}
+
 template <int DIM, int ORD>
 __global__ void __launch_bounds__(THREADS) diff_grad_kernel(Params P, Geom g, Scratch S) {
     const long nc = ncell_of(g);

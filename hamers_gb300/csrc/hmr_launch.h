@@ -91,6 +91,14 @@ inline int scheme_params(const hmr_config* cfg, Params& P) {
     return diffusive_params(cfg, P);
 }
 
+// A fine patch over a coarse patch of the next coarser level: geometries, first interior
+// cells in the level index spaces, ratio, and the covered coarse cells [lo, hi) (local).
+struct CoarsenArgs {
+    Geom gc, gf;
+    int clo[3], flo[3], r[3];
+    int lo[3], hi[3];
+};
+
 struct Variant {
     int dim;
     int model;
@@ -170,6 +178,14 @@ int launch_rk_stage(const hmr::Variant& v, const hmr::Geom& g, int ncoef, const 
                     const double* beta, const double* gamma, const hmr::Comp* Qint, const hmr::FluxComp* Fint,
                     const hmr::Comp* Sint, const hmr::Comp& Qout, const hmr::FluxComp& Facc, const hmr::Comp& Sacc,
                     cudaStream_t st, const hmr::FluxComp* Fdint = nullptr, const hmr::FluxComp* Fdacc = nullptr);
+// Refluxing: synchronizeFluxes on a coarse patch (Fd for NavierStokes), and the coarsening
+// of a fine patch's interior / outer-side flux sums onto a coarse patch.
+int launch_sync(const hmr::Variant& v, const hmr::Geom& g, const hmr::Comp& Q, const hmr::FluxComp& F,
+                const hmr::FluxComp* Fd, const hmr::Comp& S, cudaStream_t st);
+int launch_coarsen_cells(int dim, const hmr::CoarsenArgs& C, const hmr::Comp& Qf, const hmr::Comp& Qc, int ncomp,
+                         cudaStream_t st);
+int launch_coarsen_fluxsum(int dim, const hmr::CoarsenArgs& C, const hmr::FluxComp& Ff, const hmr::FluxComp& Fc,
+                           int neq, cudaStream_t st);
 // Navier-Stokes cell phase: temperature and node velocity gradient into S.Td, S.Gd.
 int launch_diff_grad(const hmr::Variant& v, const hmr::Params& P, const hmr::Geom& g, const hmr::Scratch& S,
                      cudaStream_t st);

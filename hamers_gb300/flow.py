@@ -263,6 +263,20 @@ class Euler:
         L.check("hmr_rk_stage_patch", self._lib.hmr_rk_stage_patch(
             rec.ctx, ctypes.byref(g), nc, a, b, c, qi, fi, si, qo, fa, sa, _stream_ptr(stream)))
 
+    def synchronizeFluxes(self, patch, flux, source, stream=None, diffusive_flux=None):
+        """Euler::synchronizeFluxes (Euler.cpp:1682): the coarse step redone from the old state in
+        patch.data with the time-integrated (gamma-accumulated, reflux-corrected) fluxes."""
+        rec = self.rec
+        g = patch.geometry()
+        q, k1 = L.ptr_array(_comp_ptrs(patch.data, rec.ncomp))
+        f, k2 = L.ptr_array(sum((_comp_ptrs(t, rec.neq) for t in flux[:rec.flow_model.dim]), []))
+        d = None
+        if diffusive_flux is not None:
+            d, k3 = L.ptr_array(sum((_comp_ptrs(t, rec.neq) for t in diffusive_flux[:rec.flow_model.dim]), []))
+        s_, k4 = L.ptr_array(_comp_ptrs(source, rec.neq))
+        L.check("hmr_sync_fluxes_patch", self._lib.hmr_sync_fluxes_patch(
+            rec.ctx, ctypes.byref(g), q, f, d, s_, _stream_ptr(stream)))
+
     def fillGhosts(self, patch, periodic, stream=None):
         g = patch.geometry()
         q, _k = L.ptr_array(_comp_ptrs(patch.data, self.rec.ncomp))
@@ -381,6 +395,34 @@ class NavierStokes(Euler):
             keep += [k6, k7, k8]
         L.check("hmr_rk_stage_ns_patch", self._lib.hmr_rk_stage_ns_patch(
             rec.ctx, ctypes.byref(g), nc, a, b, c, qi, fi, di, si, qo, fa, da, sa, _stream_ptr(stream)))
+
+
+def _ivec(v):
+    return (ctypes.c_int * 3)(*(list(v) + [0] * (3 - len(v))))
+
+
+def coarsenFluxSum(reconstructor, coarse, coarse_lo, fine, fine_lo, ratio, fine_flux, coarse_flux, stream=None):
+    """Flux-sum coarsening of refluxing (RungeKuttaLevelIntegrator.cpp:2140-2160): on the outer
+    sides of the fine patch, coarse faces take the mean of the fine faces they cover."""
+    rec = reconstructor
+    dim = rec.flow_model.dim
+    gc, gf = coarse.geometry(), fine.geometry()
+    ff, k1 = L.ptr_array(sum((_comp_ptrs(t, rec.neq) for t in fine_flux[:dim]), []))
+    fc, k2 = L.ptr_array(sum((_comp_ptrs(t, rec.neq) for t in coarse_flux[:dim]), []))
+    L.check("hmr_coarsen_fluxsum_patch", rec._lib.hmr_coarsen_fluxsum_patch(
+        rec.ctx, ctypes.byref(gc), _ivec(coarse_lo), ctypes.byref(gf), _ivec(fine_lo), _ivec(list(ratio) + [1] * 3),
+        ff, fc, _stream_ptr(stream)))
+
+
+def coarsenPatch(reconstructor, coarse, coarse_lo, fine, fine_lo, ratio, stream=None):
+    """Coarsening of a fine patch's interior onto the coarse cells it covers (mean of the fine cells)."""
+    rec = reconstructor
+    gc, gf = coarse.geometry(), fine.geometry()
+    qf, k1 = L.ptr_array(_comp_ptrs(fine.data, rec.ncomp))
+    qc, k2 = L.ptr_array(_comp_ptrs(coarse.data, rec.ncomp))
+    L.check("hmr_coarsen_patch", rec._lib.hmr_coarsen_patch(
+        rec.ctx, ctypes.byref(gc), _ivec(coarse_lo), ctypes.byref(gf), _ivec(fine_lo), _ivec(list(ratio) + [1] * 3),
+        qf, qc, _stream_ptr(stream)))
 
 
 class RungeKuttaLevelIntegrator:

@@ -229,20 +229,53 @@ def shock_interface_2d(N=1024, seed=1, gammas=(1.4, 1.67), density_ratio=3.0, ma
     return np.ascontiguousarray(Q), dx, dt
 
 
-def taylor_green_3d(N=128, mach=0.1, gamma=1.4):
-    """3D Taylor-Green vortex on [0, 2 pi)^3 (rho = 1, p0 = 1/(gamma M^2))."""
+def taylor_green_3d(N=128, mach=0.1, gamma=1.4, perturb=0.0, seed=3):
+    """3D Taylor-Green vortex on [0, 2 pi)^3 (rho = 1, p0 = 1/(gamma M^2)).
+
+    perturb > 0 adds smooth periodic modes of that amplitude (seeded phases) to every
+    primitive variable.  The unperturbed vortex has w = 0 everywhere and mirror-symmetric
+    states across the faces on its symmetry planes: constant WCNS stencils (smoothness
+    indicators at HAMERS_EPSILON) and HLLC contact speeds of exactly zero, points where the
+    reference's flux is not differentiable at the scale of a finite-difference step; the
+    perturbed vortex is used where derivatives are checked by differences."""
     n = [N, N, N]
     dx = [2.0 * math.pi / N] * 3
     X = _grid(n, [0.0, 0.0, 0.0], dx, 3)
     x, y, z = X
-    u = np.sin(x) * np.cos(y) * np.cos(z)
-    v = -np.cos(x) * np.sin(y) * np.cos(z)
-    w = np.zeros_like(u)
+    ph = np.random.default_rng(seed).uniform(0.0, 2.0 * math.pi, 10) if perturb else np.zeros(10)
+    e = float(perturb)
+    u = np.sin(x) * np.cos(y) * np.cos(z) + e * np.sin(x + 2.0 * y + ph[0]) * np.cos(z + ph[1])
+    v = -np.cos(x) * np.sin(y) * np.cos(z) + e * np.cos(2.0 * x + ph[2]) * np.sin(y + z + ph[3])
+    w = e * np.sin(x + ph[4]) * np.cos(y + ph[5]) * np.sin(2.0 * z + ph[6])
     p0 = 1.0 / (gamma * mach * mach)
-    p = p0 + ((np.cos(2.0 * z) + 2.0) * (np.cos(2.0 * x) + np.cos(2.0 * y)) - 2.0) / 16.0
-    rho = np.ones_like(u)
+    p = p0 + ((np.cos(2.0 * z) + 2.0) * (np.cos(2.0 * x) + np.cos(2.0 * y)) - 2.0) / 16.0 + \
+        e * np.cos(x + y + z + ph[7])
+    rho = 1.0 + e * np.sin(x + ph[8]) * np.sin(y + z + ph[9])
     Q = single_species_state(rho, [u, v, w], p, gamma)
     return np.ascontiguousarray(Q), dx
+
+
+# Navier-Stokes Taylor-Green vortex at Re = 1600 (mu = 1/Re with the unit velocity and length
+# of taylor_green_3d), Pr = 0.72, constant viscosity, no bulk viscosity, R = 1 so that
+# c_p = gamma/(gamma - 1).  Keys are the reference's mixing-rule keys.
+def taylor_green_transport(reynolds=1600.0, prandtl=0.72, gamma=1.4):
+    return {"species_mu": 1.0 / reynolds, "species_mu_v": 0.0,
+            "species_c_p": gamma / (gamma - 1.0), "species_Pr": prandtl}
+
+
+def taylor_green_dt(Q, dx, gamma=1.4, cfl=0.4, mu=1.0 / 1600.0, prandtl=0.72):
+    """Time step of the initial Taylor-Green state: cfl over the larger of the convective
+    spectral radius max sum_d (|u_d| + c)/dx_d and the diffusive one 2 max(D)/dx^2 summed
+    over the axes, D = max(4/3 mu, gamma mu/Pr)/rho (held fixed over the run)."""
+    rho = Q[0]
+    u = [Q[1 + d] / rho for d in range(3)]
+    ke = 0.5 * rho * sum(v * v for v in u)
+    p = (gamma - 1.0) * (Q[4] - ke)
+    c = np.sqrt(gamma * p / rho)
+    conv = sum((np.abs(u[d]) + c) / dx[d] for d in range(3)).max()
+    D = max(4.0 / 3.0 * mu, gamma * mu / prandtl) / rho.min()
+    diff = 2.0 * D * sum(1.0 / (h * h) for h in dx)
+    return cfl / max(conv, diff)
 
 
 def blobs_patches_3d(num_patches=512, side_lo=16, side_hi=64, seed=2, nblobs=32, gamma=1.4):

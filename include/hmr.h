@@ -210,6 +210,32 @@ int hmr_fill_ghosts_patch(hmr_ctx* ctx, const hmr_patch_geometry* geom, double* 
 int hmr_spectral_radius_patch(hmr_ctx* ctx, const hmr_patch_geometry* geom, const double* const* Q,
                               double* d_max, void* stream);
 
+/* Refluxing (RungeKuttaLevelIntegrator.cpp:2120-2230, synchronising a coarse level with the
+ * finer one after its step).  Fluxes are the time-integrated ones that hmr_rk_stage_patch /
+ * hmr_rk_stage_ns_patch accumulate with gamma (keep accumulating the fine patch's over its
+ * time-refined steps).  A patch's placement is the level index of its first interior cell (lo)
+ * and its size; the fine box must be aligned with the refinement ratio.
+ *
+ * hmr_coarsen_fluxsum_patch: on the outer sides of the fine patch, every coarse face of
+ * coarse_flux that the side covers takes the mean of the fine faces of fine_flux within it
+ * (the flux-sum coarsening, :2140-2160).
+ * hmr_sync_fluxes_patch: Euler::synchronizeFluxes (src/apps/Euler/Euler.cpp:1682-1943) /
+ * NavierStokes::synchronizeFluxes (diff_flux non-null; NavierStokes.cpp:2425-2700): the coarse
+ * patch's step redone from its old state Q (ghost box, interior updated) with those fluxes,
+ * Q += -div (flux [+ diff_flux]) + source, then the five-equation last volume fraction.
+ * hmr_coarsen_patch: every coarse cell the fine patch covers takes the mean of its fine cells
+ * (the coarsening of fine interiors, :2190-2230).
+ * The two coarsenings are SAMRAI's CONSERVATIVE_COARSEN (volume / area weighted means). */
+int hmr_coarsen_fluxsum_patch(hmr_ctx* ctx, const hmr_patch_geometry* coarse, const int* coarse_lo,
+                              const hmr_patch_geometry* fine, const int* fine_lo, const int* ratio,
+                              const double* const* fine_flux, double* const* coarse_flux, void* stream);
+int hmr_sync_fluxes_patch(hmr_ctx* ctx, const hmr_patch_geometry* geom, double* const* Q,
+                          const double* const* flux, const double* const* diff_flux,
+                          const double* const* source, void* stream);
+int hmr_coarsen_patch(hmr_ctx* ctx, const hmr_patch_geometry* coarse, const int* coarse_lo,
+                      const hmr_patch_geometry* fine, const int* fine_lo, const int* ratio,
+                      const double* const* Q_fine, double* const* Q_coarse, void* stream);
+
 /* Adjoint (vector-Jacobian product) of hmr_rk_substep_patch.  No counterpart in the reference,
  * which has no derivative code.  For the adjoint Qbar_out of the substep's output (ghost-box
  * arrays; interior read) it accumulates into Qbar_int[n] (n = 0..stage, ghost boxes, caller

@@ -131,6 +131,49 @@ int hmro_rk_stage_ns(const hmro_config* cfg, const int* n, const double* dx, int
     return 0;
 }
 
+// Euler / NavierStokes synchronizeFluxes on one coarse patch (Fd null for Euler): Q (ghost
+// box, interior updated) += -div (F [+ Fd]) + S with the time-integrated fluxes.
+int hmro_sync_fluxes(const hmro_config* cfg, const int* n, const double* dx, const double* F,
+                     const double* Fd, const double* S, double* Q) {
+    const Config c = to_cfg(cfg);
+    const Box b = make_box(c.dim, n, 4);
+    const int ncomp = num_comp(c), neq = num_eqn(c);
+    const long nint = (long)b.n[0] * b.n[1] * b.n[2];
+    std::vector<double*> f, d, q(ncomp);
+    flux_ptrs(c, b, const_cast<double*>(F), f);
+    if (Fd) flux_ptrs(c, b, const_cast<double*>(Fd), d);
+    std::vector<const double*> fc(f.begin(), f.end()), dc(d.begin(), d.end()), sc(neq);
+    for (int e = 0; e < neq; e++) sc[e] = S + (size_t)e * nint;
+    for (int e = 0; e < ncomp; e++) q[e] = Q + (size_t)e * b.ncell();
+    sync_fluxes<double>(c, n, dx, fc.data(), Fd ? dc.data() : nullptr, sc.data(), q.data());
+    return 0;
+}
+
+// Flux-sum coarsening of one fine patch onto one coarse patch (flux arrays as hmro_conv_flux_source's).
+int hmro_coarsen_fluxsum(const hmro_config* cfg, const int* ratio, const int* cn, const int* clo, const int* fn,
+                         const int* flo, const double* Ff, double* Fc) {
+    const Config c = to_cfg(cfg);
+    std::vector<double*> ff, fc;
+    flux_ptrs(c, make_box(c.dim, fn, 4), const_cast<double*>(Ff), ff);
+    flux_ptrs(c, make_box(c.dim, cn, 4), Fc, fc);
+    std::vector<const double*> ffc(ff.begin(), ff.end());
+    coarsen_fluxsum(c, ratio, cn, clo, fn, flo, ffc.data(), fc.data());
+    return 0;
+}
+
+// Coarsening of a fine patch's interior onto the covered cells of a coarse patch (ghost boxes).
+int hmro_coarsen_cells(const hmro_config* cfg, const int* ratio, const int* cn, const int* clo, const int* fn,
+                       const int* flo, const double* Qf, double* Qc) {
+    const Config c = to_cfg(cfg);
+    const int ncomp = num_comp(c);
+    const Box cb = make_box(c.dim, cn, 4), fb = make_box(c.dim, fn, 4);
+    std::vector<const double*> qf(ncomp);
+    std::vector<double*> qc(ncomp);
+    for (int e = 0; e < ncomp; e++) { qf[e] = Qf + (size_t)e * fb.ncell(); qc[e] = Qc + (size_t)e * cb.ncell(); }
+    coarsen_cells(c, ratio, cn, clo, fn, flo, qf.data(), qc.data());
+    return 0;
+}
+
 int hmro_fill_ghosts(const hmro_config* cfg, const int* n, const int* periodic, double* Q) {
     const Config c = to_cfg(cfg);
     const Box b = make_box(c.dim, n, 4);

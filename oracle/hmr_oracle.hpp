@@ -1502,6 +1502,153 @@ void diff_flux(const Config& c, const Transport& tr, const int* n, const double*
     }
 }
 
+// ---------------------------------------------------------------------------
+// Refluxing (synchronisation of a coarse level with the finer one).
+//   sync_fluxes      Euler::synchronizeFluxes (src/apps/Euler/Euler.cpp:1682-1943) and
+//                    NavierStokes::synchronizeFluxes (NavierStokes.cpp:2425-2700): the coarse
+//                    step redone from its old state with the time-integrated fluxes,
+//                    Q += -div (F [+ Fd]) + S, then updateCellDataOfConservativeVariables.
+//   coarsen_fluxsum  the flux-sum coarsening of RungeKuttaLevelIntegrator.cpp:2140-2160: on the
+//                    outer sides of a fine patch each coarse face takes the mean of the r^(d-1)
+//                    fine faces it covers.
+//   coarsen_cells    the coarsening of fine interiors (RungeKuttaLevelIntegrator.cpp:2190-2230):
+//                    each covered coarse cell takes the mean of its r^d fine cells.
+// The two coarsening operators are SAMRAI's (CONSERVATIVE_COARSEN: area / volume weighted
+// averages), which is not in the reference's tree; the order of their sums here (fine index
+// order, then one multiplication by 1/r^k) is this restatement's own.
+// ---------------------------------------------------------------------------
+template <class T>
+void sync_fluxes(const Config& c, const int* n, const double* dx, const T* const* F, const T* const* Fd,
+                 const T* const* S, T* const* Q) {
+    const int dim = c.dim, neq = num_eqn(c);
+    const Box b = make_box(dim, n, 4);
+    for (int e = 0; e < neq; e++) {
+        for (int k = 0; k < b.n[2]; k++)
+        for (int j = 0; j < b.n[1]; j++)
+        for (int i = 0; i < b.n[0]; i++) {
+            const long x = b.cell(i, j, k);
+            const long is = interior_index(b, i, j, k);
+            const long xl = side_index(b, 0, i, j, k), xr = side_index(b, 0, i + 1, j, k);
+            const long yl = side_index(b, 1, i, j, k), yr = side_index(b, 1, i, j + 1, k);
+            const T* Fx = F[e];
+            const T* Fy = F[neq + e];
+            if (Fd) {
+                const T* Dx = Fd[e];
+                const T* Dy = Fd[neq + e];
+                if (dim == 2) {
+                    Q[e][x] += (-(Fx[xr] - Fx[xl] + Dx[xr] - Dx[xl])/dx[0] -
+                                 (Fy[yr] - Fy[yl] + Dy[yr] - Dy[yl])/dx[1] +
+                                 S[e][is]);
+                } else {
+                    const long zl = side_index(b, 2, i, j, k), zr = side_index(b, 2, i, j, k + 1);
+                    const T* Fz = F[2 * neq + e];
+                    const T* Dz = Fd[2 * neq + e];
+                    Q[e][x] += (-(Fx[xr] - Fx[xl] + Dx[xr] - Dx[xl])/dx[0] -
+                                 (Fy[yr] - Fy[yl] + Dy[yr] - Dy[yl])/dx[1] -
+                                 (Fz[zr] - Fz[zl] + Dz[zr] - Dz[zl])/dx[2] +
+                                 S[e][is]);
+                }
+            } else if (dim == 2) {
+                Q[e][x] += (-(Fx[xr] - Fx[xl])/dx[0] -
+                             (Fy[yr] - Fy[yl])/dx[1] +
+                             S[e][is]);
+            } else {
+                const long zl = side_index(b, 2, i, j, k), zr = side_index(b, 2, i, j, k + 1);
+                const T* Fz = F[2 * neq + e];
+                Q[e][x] += (-(Fx[xr] - Fx[xl])/dx[0] -
+                             (Fy[yr] - Fy[yl])/dx[1] -
+                             (Fz[zr] - Fz[zl])/dx[2] +
+                             S[e][is]);
+            }
+        }
+    }
+    if (c.model == MODEL_FIVE_EQN_ALLAIRE) {
+        // FlowModelFiveEqnAllaire::updateCellDataOfConservativeVariables
+        const int N = c.num_species;
+        for (int k = 0; k < b.n[2]; k++)
+        for (int j = 0; j < b.n[1]; j++)
+        for (int i = 0; i < b.n[0]; i++) {
+            const long x = b.cell(i, j, k);
+            Q[neq][x] = T(1.0);
+            for (int si = 0; si < N - 1; si++) Q[neq][x] -= Q[N + dim + 1 + si][x];
+        }
+    }
+}
+
+// Patch placement in a level's index space: first interior cell lo[3], interior size n[3].
+// The fine patch's box coarsened by ratio[3] must be aligned (lo and lo + n multiples of r).
+inline void coarsen_fluxsum(const Config& c, const int* ratio, const int* cn, const int* clo,
+                            const int* fn, const int* flo, const double* const* Ff, double* const* Fc) {
+    const int dim = c.dim, neq = num_eqn(c);
+    const Box cb = make_box(dim, cn, 4), fb = make_box(dim, fn, 4);
+    for (int a = 0; a < dim; a++) {
+        int area = 1;
+        for (int d = 0; d < dim; d++) if (d != a) area *= ratio[d];
+        const double w = double(1)/double(area);
+        for (int side = 0; side < 2; side++) {
+            const int ff = side == 0 ? 0 : fn[a];            // fine face index along a (local)
+            const int cf = (flo[a] + ff)/ratio[a] - clo[a];  // coarse face index along a (local)
+            if (cf < 0 || cf > cn[a]) continue;
+            int lo[3] = {0, 0, 0}, hi[3] = {1, 1, 1};
+            for (int d = 0; d < dim; d++) {
+                if (d == a) continue;
+                lo[d] = std::max(flo[d]/ratio[d], clo[d]) - clo[d];
+                hi[d] = std::min((flo[d] + fn[d])/ratio[d], clo[d] + cn[d]) - clo[d];
+            }
+            for (int e = 0; e < neq; e++)
+            for (int k = lo[2]; k < hi[2]; k++)
+            for (int j = lo[1]; j < hi[1]; j++)
+            for (int i = lo[0]; i < hi[0]; i++) {
+                const int cc[3] = {i, j, k};
+                int fi0[3];
+                for (int d = 0; d < 3; d++) fi0[d] = d < dim ? (cc[d] + clo[d])*ratio[d] - flo[d] : 0;
+                double sum = 0.0;
+                const int r1 = a == 1 ? 1 : (dim > 1 ? ratio[1] : 1);
+                const int r2 = (dim == 3 && a != 2) ? ratio[2] : 1;
+                const int r0 = a == 0 ? 1 : ratio[0];
+                for (int q2 = 0; q2 < r2; q2++)
+                for (int q1 = 0; q1 < r1; q1++)
+                for (int q0 = 0; q0 < r0; q0++) {
+                    int f[3] = {fi0[0] + q0, fi0[1] + q1, fi0[2] + q2};
+                    f[a] = ff;
+                    sum += Ff[a * neq + e][side_index(fb, a, f[0], f[1], f[2])];
+                }
+                int g[3] = {i, j, k};
+                g[a] = cf;
+                Fc[a * neq + e][side_index(cb, a, g[0], g[1], g[2])] = sum*w;
+            }
+        }
+    }
+}
+
+inline void coarsen_cells(const Config& c, const int* ratio, const int* cn, const int* clo,
+                          const int* fn, const int* flo, const double* const* Qf, double* const* Qc) {
+    const int dim = c.dim, ncomp = num_comp(c);
+    const Box cb = make_box(dim, cn, 4), fb = make_box(dim, fn, 4);
+    int vol = 1;
+    for (int d = 0; d < dim; d++) vol *= ratio[d];
+    const double w = double(1)/double(vol);
+    int lo[3] = {0, 0, 0}, hi[3] = {1, 1, 1};
+    for (int d = 0; d < dim; d++) {
+        lo[d] = std::max(flo[d]/ratio[d], clo[d]) - clo[d];
+        hi[d] = std::min((flo[d] + fn[d])/ratio[d], clo[d] + cn[d]) - clo[d];
+    }
+    const int r0 = ratio[0], r1 = dim > 1 ? ratio[1] : 1, r2 = dim > 2 ? ratio[2] : 1;
+    for (int e = 0; e < ncomp; e++)
+    for (int k = lo[2]; k < hi[2]; k++)
+    for (int j = lo[1]; j < hi[1]; j++)
+    for (int i = lo[0]; i < hi[0]; i++) {
+        const int fi = (i + clo[0])*r0 - flo[0];
+        const int fj = dim > 1 ? (j + clo[1])*r1 - flo[1] : 0;
+        const int fk = dim > 2 ? (k + clo[2])*r2 - flo[2] : 0;
+        double sum = 0.0;
+        for (int q2 = 0; q2 < r2; q2++)
+        for (int q1 = 0; q1 < r1; q1++)
+        for (int q0 = 0; q0 < r0; q0++) sum += Qf[e][fb.cell(fi + q0, fj + q1, fk + q2)];
+        Qc[e][cb.cell(i, j, k)] = sum*w;
+    }
+}
+
 // Ghost fill of one patch: periodic along the axes with periodic[a] != 0,
 // zero-gradient (copy of the nearest interior cell) elsewhere.  On one level
 // with one patch this is what SAMRAI's periodic shift and the

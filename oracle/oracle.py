@@ -86,6 +86,9 @@ def lib():
         L.hmro_diff_flux.argtypes = [cp, tp, ip, dp, ctypes.c_double, dp, dp]
         L.hmro_rk_stage_ns.argtypes = [cp, ip, dp, ctypes.c_int, dp, dp, dp, dp, dp, dp, dp, dp]
         L.hmro_ns_rk3_advance.argtypes = [cp, tp, ip, dp, ctypes.c_double, ip, ctypes.c_int, dp]
+        L.hmro_sync_fluxes.argtypes = [cp, ip, dp, dp, dp, dp, dp]
+        L.hmro_coarsen_fluxsum.argtypes = [cp, ip, ip, ip, ip, ip, dp, dp]
+        L.hmro_coarsen_cells.argtypes = [cp, ip, ip, ip, ip, ip, dp, dp]
         L.hmro_num_eqn.argtypes = [cp]
         L.hmro_num_comp.argtypes = [cp]
         _lib = L
@@ -299,6 +302,41 @@ def ns_rk3_advance(cfg, tr, n, dx, dt, periodic, nsteps, Q):
     if r != 0:
         raise ValueError("the oracle's diffusive flux covers single-species patches, order 2 or 4")
     return Q
+
+
+def _flat(F):
+    return np.ascontiguousarray(np.concatenate([np.asarray(f, dtype=np.float64).ravel() for f in F]))
+
+
+def sync_fluxes(cfg, n, dx, F, S, Q, Fd=None):
+    """synchronizeFluxes on one coarse patch: Q (ghost box, in place) += -div (F [+ Fd]) + S."""
+    assert Q.flags["C_CONTIGUOUS"] and Q.dtype == np.float64
+    fd = _flat(Fd) if Fd is not None else None
+    lib().hmro_sync_fluxes(ctypes.byref(cfg.c()), _ip(_n3(n)), _dv(list(dx) + [1.0] * (3 - len(dx))),
+                           _dp(_flat(F)), _dp(fd) if fd is not None else None,
+                           _dp(np.ascontiguousarray(S, dtype=np.float64)), _dp(Q))
+    return Q
+
+
+def coarsen_fluxsum(cfg, ratio, cn, clo, fn, flo, Ff, Fc):
+    """Flux-sum coarsening of a fine patch (at flo, size fn) onto a coarse patch (clo, cn); Fc in place."""
+    flat = _flat(Fc)
+    lib().hmro_coarsen_fluxsum(ctypes.byref(cfg.c()), _ip(_n3(ratio)), _ip(_n3(cn)), _ip(list(clo) + [0] * (3 - len(clo))),
+                               _ip(_n3(fn)), _ip(list(flo) + [0] * (3 - len(flo))), _dp(_flat(Ff)), _dp(flat))
+    off = 0
+    for f in Fc:
+        f.ravel()[:] = flat[off:off + f.size]
+        off += f.size
+    return Fc
+
+
+def coarsen_cells(cfg, ratio, cn, clo, fn, flo, Qf, Qc):
+    """Coarsen a fine patch's interior onto the covered cells of a coarse patch (Qc in place)."""
+    assert Qc.flags["C_CONTIGUOUS"] and Qc.dtype == np.float64
+    lib().hmro_coarsen_cells(ctypes.byref(cfg.c()), _ip(_n3(ratio)), _ip(_n3(cn)), _ip(list(clo) + [0] * (3 - len(clo))),
+                             _ip(_n3(fn)), _ip(list(flo) + [0] * (3 - len(flo))),
+                             _dp(np.ascontiguousarray(Qf, dtype=np.float64)), _dp(Qc))
+    return Qc
 
 
 def tangent_substep(cfg, n, dx, dt, stage, alpha, beta, Q_int, dQ_int, transport=None):
