@@ -45,7 +45,7 @@ EXPORTS = [
     "hmr_rk_substep_patch_noalloc", "hmr_rk_substep_vjp_patch", "hmr_fill_ghosts_vjp_patch",
     "hmr_spectral_radius_patch", "hmr_level_step_cfl", "hmr_level_last_dt", "hmr_level_set_layout",
     "hmr_diff_flux_patch", "hmr_rk_stage_ns_patch", "hmr_coarsen_fluxsum_patch", "hmr_sync_fluxes_patch",
-    "hmr_coarsen_patch",
+    "hmr_coarsen_patch", "hmr_refine_ghosts_patch",
 ]
 
 
@@ -148,6 +148,7 @@ def load():
     L.hmr_coarsen_fluxsum_patch.argtypes = [vp, gp, ip, gp, ip, ip, DPP, DPP, vp]
     L.hmr_sync_fluxes_patch.argtypes = [vp, gp, DPP, DPP, DPP, DPP, vp]
     L.hmr_coarsen_patch.argtypes = [vp, gp, ip, gp, ip, ip, DPP, DPP, vp]
+    L.hmr_refine_ghosts_patch.argtypes = [vp, gp, ip, gp, ip, ip, DPP, DPP, ctypes.c_double, DPP, vp]
     L.hmr_rk_stage_ns_patch.argtypes = [vp, gp, ctypes.c_int, dp, dp, dp, DPPP, DPPP, DPPP, DPPP, DPP, DPP, DPP,
                                         DPP, vp]
     for name in EXPORTS:

@@ -563,6 +563,21 @@ static int coarsen_args(const hmr_ctx* c, const hmr_patch_geometry* coarse, cons
     return HMR_OK;
 }
 
+int hmr_refine_ghosts_patch(hmr_ctx* c, const hmr_patch_geometry* fine, const int* fine_lo,
+                            const hmr_patch_geometry* coarse, const int* coarse_lo, const int* ratio,
+                            const double* const* Q_coarse_old, const double* const* Q_coarse_new, double theta,
+                            double* const* Q_fine, void* stream) {
+    if (!c || !(theta >= 0.0 && theta <= 1.0)) return HMR_ERR_ARGUMENT;
+    CoarsenArgs C;
+    int r = coarsen_args(c, coarse, coarse_lo, fine, fine_lo, ratio, C);
+    if (r) return r;
+    Comp qo, qn, qf;
+    if (!load_comp(qo, Q_coarse_old, c->ncomp) || !load_comp(qn, Q_coarse_new, c->ncomp) ||
+        !load_comp(qf, Q_fine, c->ncomp))
+        return HMR_ERR_ARGUMENT;
+    return hmr_cells::launch_refine_ghosts(c->v.dim, C, qo, qn, theta, qf, c->ncomp, as_stream(stream));
+}
+
 int hmr_coarsen_patch(hmr_ctx* c, const hmr_patch_geometry* coarse, const int* coarse_lo,
                       const hmr_patch_geometry* fine, const int* fine_lo, const int* ratio,
                       const double* const* Q_fine, double* const* Q_coarse, void* stream) {

@@ -550,6 +550,61 @@ int launch_coarsen_fluxsum(int dim, const CoarsenArgs& C, const FluxComp& Ff, co
     return (int)cudaPeekAtLastError();
 }
 
+// Coarse-fine ghost cells of a fine patch: linear time interpolation of the coarse state,
+// (1 - theta) old + theta new, then conservative linear refinement with monotonised-central
+// slopes per coarse cell (SAMRAI's LINEAR_TIME_INTERPOLATE and CONSERVATIVE_LINEAR_REFINE,
+// registered at FlowModelSingleSpecies.cpp:578-597; restated).  Item: a fine ghost-box cell.
+__device__ __forceinline__ double mc_slope(double dm, double dp) {
+    if (!(dm*dp > 0.0)) return 0.0;
+    const double d = double(1)/double(2)*(dm + dp);
+    const double b = double(2)*fmin(fabs(dm), fabs(dp));
+    return fabs(d) < b ? d : (d > 0.0 ? b : -b);
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(THREADS) refine_ghosts_kernel(CoarsenArgs C, Comp Qo, Comp Qn, double theta,
+                                                               Comp Qf, int ncomp) {
+    const long nfc = ncell_of(C.gf);
+    for (long x = (long)blockIdx.x * blockDim.x + threadIdx.x; x < nfc; x += (long)gridDim.x * blockDim.x) {
+        const int f[3] = {(int)(x % C.gf.G[0]) - GHOST, (int)((x / C.gf.G[0]) % C.gf.G[1]) - GHOST,
+                          DIM == 3 ? (int)(x / ((long)C.gf.G[0] * C.gf.G[1])) - GHOST : 0};
+        bool inside = true, covered = true;
+        int c[3] = {0, 0, 0}, lev[3] = {0, 0, 0};
+#pragma unroll
+        for (int d = 0; d < DIM; d++) {
+            if (f[d] < 0 || f[d] >= C.gf.n[d]) inside = false;
+            lev[d] = C.flo[d] + f[d];
+            const int cl = lev[d] >= 0 ? lev[d] / C.r[d] : -((-lev[d] + C.r[d] - 1) / C.r[d]);
+            c[d] = cl - C.clo[d];
+            if (c[d] < 0 || c[d] >= C.gc.n[d]) covered = false;
+        }
+        if (inside || !covered) continue;
+        const long xc = cidx<DIM>(C.gc, c[0], c[1], c[2]);
+        for (int e = 0; e < ncomp; e++) {
+            const double* o = Qo.p[e];
+            const double* nw = Qn.p[e];
+            auto q = [&](long y) { return (double(1) - theta)*o[y] + theta*nw[y]; };
+            const double q0 = q(xc);
+            double v = q0;
+#pragma unroll
+            for (int d = 0; d < DIM; d++) {
+                const long st = d == 0 ? 1 : (d == 1 ? (long)C.gc.G[0] : (long)C.gc.G[0] * C.gc.G[1]);
+                const double s = mc_slope(q0 - q(xc - st), q(xc + st) - q0);
+                const double off = (double(lev[d]) + 0.5)/double(C.r[d]) - (double(c[d] + C.clo[d]) + 0.5);
+                v += s*off;
+            }
+            Qf.p[e][x] = v;
+        }
+    }
+}
+
+int launch_refine_ghosts(int dim, const CoarsenArgs& C, const Comp& Qo, const Comp& Qn, double theta,
+                         const Comp& Qf, int ncomp, cudaStream_t st) {
+    if (dim == 2) refine_ghosts_kernel<2><<<grid_for(ncell_of(C.gf)), THREADS, 0, st>>>(C, Qo, Qn, theta, Qf, ncomp);
+    else refine_ghosts_kernel<3><<<grid_for(ncell_of(C.gf)), THREADS, 0, st>>>(C, Qo, Qn, theta, Qf, ncomp);
+    return (int)cudaPeekAtLastError();
+}
+
 template <int DIM, int ORD>
 __global__ void __launch_bounds__(THREADS) diff_grad_kernel(Params P, Geom g, Scratch S) {
     const long nc = ncell_of(g);

@@ -186,6 +186,9 @@ int launch_coarsen_cells(int dim, const hmr::CoarsenArgs& C, const hmr::Comp& Qf
                          cudaStream_t st);
 int launch_coarsen_fluxsum(int dim, const hmr::CoarsenArgs& C, const hmr::FluxComp& Ff, const hmr::FluxComp& Fc,
                            int neq, cudaStream_t st);
+// Coarse-fine ghost cells of a fine patch from a coarse patch (time fraction theta).
+int launch_refine_ghosts(int dim, const hmr::CoarsenArgs& C, const hmr::Comp& Qo, const hmr::Comp& Qn, double theta,
+                         const hmr::Comp& Qf, int ncomp, cudaStream_t st);
 // Navier-Stokes cell phase: temperature and node velocity gradient into S.Td, S.Gd.
 int launch_diff_grad(const hmr::Variant& v, const hmr::Params& P, const hmr::Geom& g, const hmr::Scratch& S,
                      cudaStream_t st);

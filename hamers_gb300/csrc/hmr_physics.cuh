@@ -504,10 +504,12 @@ __device__ __forceinline__ double ld_interp(const double* b, double sigma, const
         const double t5 = mul_(mul_(double(3)/double(8), o3), S5);
         return add_(add_(add_(add_(add_(t0, t1), t2), t3), t4), t5);
     } else {
-        const double r0 = double(1)/(b[0] + HMR_EPS);
-        const double r1 = double(1)/(b[1] + HMR_EPS);
-        const double r2 = double(1)/(b[2] + HMR_EPS);
-        const double r3 = double(1)/(b[3] + HMR_EPS);
+        // the four 1/(beta_k + eps) from one division: 1/e_k = (prod_{j!=k} e_j)/(prod_j e_j)
+        // (e_k in [1e-15, 1e77) keeps the product of four in range)
+        const double e0 = b[0] + HMR_EPS, e1 = b[1] + HMR_EPS, e2 = b[2] + HMR_EPS, e3 = b[3] + HMR_EPS;
+        const double e01 = e0*e1, e23 = e2*e3;
+        const double rp = double(1)/(e01*e23);
+        const double r0 = rp*(e1*e23), r1 = rp*(e0*e23), r2 = rp*(e01*e3), r3 = rp*(e01*e2);
         u0 = double(1)/double(16)*(double(1) + ipow_<false>(tau_5*r0, P.p));
         u1 = double(5)/double(8)*(double(1) + ipow_<false>(tau_5*r1, P.p));
         u2 = double(5)/double(16)*(double(1) + ipow_<false>(tau_5*r2, P.p));
@@ -626,11 +628,16 @@ __device__ __forceinline__ double cu_interp(const double* b, const Params& P, do
         const double t5 = mul_(mul_(double(3)/double(8), o3), S5);
         return add_(add_(add_(add_(add_(t0, t1), t2), t3), t4), t5);
     } else {
+        // g/d_k with d_k = (beta_k + eps dx^2)(beta_k + Chi dx^2), the four from one division
         const double g = tau_6*(beta_avg + cx);
-        o0 = double(1)/double(32)*ipow_<false>(P.C + g/((b[0] + ce)*(b[0] + cx)), P.q);
-        o1 = double(15)/double(32)*ipow_<false>(P.C + g/((b[1] + ce)*(b[1] + cx)), P.q);
-        o2 = double(15)/double(32)*ipow_<false>(P.C + g/((b[2] + ce)*(b[2] + cx)), P.q);
-        o3 = double(1)/double(32)*ipow_<false>(P.C + g/((b[3] + ce)*(b[3] + cx)), P.q);
+        const double d0 = (b[0] + ce)*(b[0] + cx), d1 = (b[1] + ce)*(b[1] + cx);
+        const double d2 = (b[2] + ce)*(b[2] + cx), d3 = (b[3] + ce)*(b[3] + cx);
+        const double d01 = d0*d1, d23 = d2*d3;
+        const double gp = g/(d01*d23);
+        o0 = double(1)/double(32)*ipow_<false>(P.C + gp*(d1*d23), P.q);
+        o1 = double(15)/double(32)*ipow_<false>(P.C + gp*(d0*d23), P.q);
+        o2 = double(15)/double(32)*ipow_<false>(P.C + gp*(d01*d3), P.q);
+        o3 = double(1)/double(32)*ipow_<false>(P.C + gp*(d01*d2), P.q);
         const double ro = double(1)/(o0 + o1 + o2 + o3);
         o0 *= ro; o1 *= ro; o2 *= ro; o3 *= ro;
         return double(3)/double(8)*o0*S0 +

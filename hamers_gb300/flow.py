@@ -397,8 +397,8 @@ class NavierStokes(Euler):
             rec.ctx, ctypes.byref(g), nc, a, b, c, qi, fi, di, si, qo, fa, da, sa, _stream_ptr(stream)))
 
 
-def _ivec(v):
-    return (ctypes.c_int * 3)(*(list(v) + [0] * (3 - len(v))))
+def _ivec(v, fill=0):
+    return (ctypes.c_int * 3)(*((list(v) + [fill] * 3)[:3]))
 
 
 def coarsenFluxSum(reconstructor, coarse, coarse_lo, fine, fine_lo, ratio, fine_flux, coarse_flux, stream=None):
@@ -410,8 +410,22 @@ def coarsenFluxSum(reconstructor, coarse, coarse_lo, fine, fine_lo, ratio, fine_
     ff, k1 = L.ptr_array(sum((_comp_ptrs(t, rec.neq) for t in fine_flux[:dim]), []))
     fc, k2 = L.ptr_array(sum((_comp_ptrs(t, rec.neq) for t in coarse_flux[:dim]), []))
     L.check("hmr_coarsen_fluxsum_patch", rec._lib.hmr_coarsen_fluxsum_patch(
-        rec.ctx, ctypes.byref(gc), _ivec(coarse_lo), ctypes.byref(gf), _ivec(fine_lo), _ivec(list(ratio) + [1] * 3),
+        rec.ctx, ctypes.byref(gc), _ivec(coarse_lo), ctypes.byref(gf), _ivec(fine_lo), _ivec(ratio, 1),
         ff, fc, _stream_ptr(stream)))
+
+
+def refineGhosts(reconstructor, fine, fine_lo, coarse, coarse_lo, ratio, coarse_old, coarse_new, theta,
+                 stream=None):
+    """Coarse-fine ghost cells of the fine patch from the coarse patch's states at the old and new
+    time (coarse_old / coarse_new: ghost-box tensors, ghosts filled) at time fraction theta."""
+    rec = reconstructor
+    gf, gc = fine.geometry(), coarse.geometry()
+    qo, k1 = L.ptr_array(_comp_ptrs(coarse_old, rec.ncomp))
+    qn, k2 = L.ptr_array(_comp_ptrs(coarse_new, rec.ncomp))
+    qf, k3 = L.ptr_array(_comp_ptrs(fine.data, rec.ncomp))
+    L.check("hmr_refine_ghosts_patch", rec._lib.hmr_refine_ghosts_patch(
+        rec.ctx, ctypes.byref(gf), _ivec(fine_lo), ctypes.byref(gc), _ivec(coarse_lo), _ivec(ratio, 1),
+        qo, qn, float(theta), qf, _stream_ptr(stream)))
 
 
 def coarsenPatch(reconstructor, coarse, coarse_lo, fine, fine_lo, ratio, stream=None):
@@ -421,7 +435,7 @@ def coarsenPatch(reconstructor, coarse, coarse_lo, fine, fine_lo, ratio, stream=
     qf, k1 = L.ptr_array(_comp_ptrs(fine.data, rec.ncomp))
     qc, k2 = L.ptr_array(_comp_ptrs(coarse.data, rec.ncomp))
     L.check("hmr_coarsen_patch", rec._lib.hmr_coarsen_patch(
-        rec.ctx, ctypes.byref(gc), _ivec(coarse_lo), ctypes.byref(gf), _ivec(fine_lo), _ivec(list(ratio) + [1] * 3),
+        rec.ctx, ctypes.byref(gc), _ivec(coarse_lo), ctypes.byref(gf), _ivec(fine_lo), _ivec(ratio, 1),
         qf, qc, _stream_ptr(stream)))
 
 

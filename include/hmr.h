@@ -236,6 +236,19 @@ int hmr_coarsen_patch(hmr_ctx* ctx, const hmr_patch_geometry* coarse, const int*
                       const hmr_patch_geometry* fine, const int* fine_lo, const int* ratio,
                       const double* const* Q_fine, double* const* Q_coarse, void* stream);
 
+/* Coarse-fine ghost cells of a fine patch: the part of the fill schedule that interpolates
+ * from the next coarser level (RungeKuttaLevelIntegrator.cpp:1568,1701; operators registered at
+ * src/flow/flow_models/single-species/FlowModelSingleSpecies.cpp:578-597).  The coarse state at
+ * the fine time is (1 - theta) Q_coarse_old + theta Q_coarse_new; every ghost cell of Q_fine
+ * whose coarse cell lies in the coarse patch's interior takes the conservative linear
+ * refinement of it (monotonised-central slopes per coarse cell: the fine values average back
+ * to the coarse value).  The coarse patch's ghost cells must be filled.  Same-level neighbour
+ * copies overwrite these values afterwards where a neighbour exists. */
+int hmr_refine_ghosts_patch(hmr_ctx* ctx, const hmr_patch_geometry* fine, const int* fine_lo,
+                            const hmr_patch_geometry* coarse, const int* coarse_lo, const int* ratio,
+                            const double* const* Q_coarse_old, const double* const* Q_coarse_new, double theta,
+                            double* const* Q_fine, void* stream);
+
 /* Adjoint (vector-Jacobian product) of hmr_rk_substep_patch.  No counterpart in the reference,
  * which has no derivative code.  For the adjoint Qbar_out of the substep's output (ghost-box
  * arrays; interior read) it accumulates into Qbar_int[n] (n = 0..stage, ghost boxes, caller

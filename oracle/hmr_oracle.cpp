@@ -174,6 +174,23 @@ int hmro_coarsen_cells(const hmro_config* cfg, const int* ratio, const int* cn, 
     return 0;
 }
 
+// Coarse-fine ghost cells of a fine patch from a coarse patch at the time fraction theta.
+int hmro_refine_ghosts(const hmro_config* cfg, const int* ratio, const int* fn, const int* flo, const int* cn,
+                       const int* clo, const double* Qc_old, const double* Qc_new, double theta, double* Qf) {
+    const Config c = to_cfg(cfg);
+    const int ncomp = num_comp(c);
+    const Box cb = make_box(c.dim, cn, 4), fb = make_box(c.dim, fn, 4);
+    std::vector<const double*> qo(ncomp), qn(ncomp);
+    std::vector<double*> qf(ncomp);
+    for (int e = 0; e < ncomp; e++) {
+        qo[e] = Qc_old + (size_t)e * cb.ncell();
+        qn[e] = Qc_new + (size_t)e * cb.ncell();
+        qf[e] = Qf + (size_t)e * fb.ncell();
+    }
+    refine_ghosts(c, ratio, fn, flo, cn, clo, qo.data(), qn.data(), theta, qf.data());
+    return 0;
+}
+
 int hmro_fill_ghosts(const hmro_config* cfg, const int* n, const int* periodic, double* Q) {
     const Config c = to_cfg(cfg);
     const Box b = make_box(c.dim, n, 4);

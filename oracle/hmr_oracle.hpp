@@ -1649,6 +1649,67 @@ inline void coarsen_cells(const Config& c, const int* ratio, const int* cn, cons
     }
 }
 
+// ---------------------------------------------------------------------------
+// Coarse-fine ghost cells of a fine patch (the fill schedule's interpolation from the next
+// coarser level, RungeKuttaLevelIntegrator.cpp:1568,1701 with the operators registered at
+// FlowModelSingleSpecies.cpp:578-597): the coarse state at the fine time,
+//   Q_c = (1 - theta) Q_c,old + theta Q_c,new
+// (linear time interpolation), then conservative linear refinement: in a coarse cell C,
+//   q_f = Q_c(C) + sum_d s_d(C) ((f_d + 1/2)/r_d - (C_d + 1/2)),
+// with the monotonised-central slope per coarse cell width
+//   s_d = sign(D) min(|D|, 2 min(|D-|, |D+|)) if D- D+ > 0 else 0,  D = (D- + D+)/2,
+//   D- = Q_c(C) - Q_c(C - e_d),  D+ = Q_c(C + e_d) - Q_c(C).
+// The mean of the fine values over a coarse cell is the coarse value.  Both operators are
+// SAMRAI's (LINEAR_TIME_INTERPOLATE, CONSERVATIVE_LINEAR_REFINE), outside the reference's
+// tree; this is a restatement of the published method, not a copy.  Every fine ghost cell
+// whose coarse cell lies inside the coarse patch's interior is written (the coarse patch's
+// ghost cells must be filled: the slopes read one coarse cell beyond).
+// ---------------------------------------------------------------------------
+inline double mc_slope(double dm, double dp) {
+    if (!(dm*dp > 0.0)) return 0.0;
+    const double d = double(1)/double(2)*(dm + dp);
+    const double b = double(2)*std::min(std::fabs(dm), std::fabs(dp));
+    return std::fabs(d) < b ? d : (d > 0.0 ? b : -b);
+}
+
+inline void refine_ghosts(const Config& c, const int* ratio, const int* fn, const int* flo, const int* cn,
+                          const int* clo, const double* const* Qc_old, const double* const* Qc_new, double theta,
+                          double* const* Qf) {
+    const int dim = c.dim, ncomp = num_comp(c);
+    const Box fb = make_box(dim, fn, 4), cb = make_box(dim, cn, 4);
+    for (int k = -fb.g[2]; k < fb.n[2] + fb.g[2]; k++)
+    for (int j = -fb.g[1]; j < fb.n[1] + fb.g[1]; j++)
+    for (int i = -fb.g[0]; i < fb.n[0] + fb.g[0]; i++) {
+        const int f[3] = {i, j, k};
+        bool inside = true, covered = true;
+        int C[3] = {0, 0, 0};
+        for (int d = 0; d < dim; d++) {
+            if (f[d] < 0 || f[d] >= fn[d]) inside = false;
+            const int lev = flo[d] + f[d];
+            const int cl = (lev >= 0 ? lev/ratio[d] : -((-lev + ratio[d] - 1)/ratio[d]));
+            C[d] = cl - clo[d];
+            if (C[d] < 0 || C[d] >= cn[d]) covered = false;
+        }
+        if (inside || !covered) continue;
+        for (int e = 0; e < ncomp; e++) {
+            auto q = [&](int di, int dj, int dk) {
+                const long x = cb.cell(C[0] + di, C[1] + dj, C[2] + dk);
+                return (double(1) - theta)*Qc_old[e][x] + theta*Qc_new[e][x];
+            };
+            const double q0 = q(0, 0, 0);
+            double v = q0;
+            for (int d = 0; d < dim; d++) {
+                const int o[3] = {d == 0, d == 1, d == 2};
+                const double s = mc_slope(q0 - q(-o[0], -o[1], -o[2]), q(o[0], o[1], o[2]) - q0);
+                const int lev = flo[d] + f[d];
+                const double off = (double(lev) + 0.5)/double(ratio[d]) - (double(C[d] + clo[d]) + 0.5);
+                v += s*off;
+            }
+            Qf[e][fb.cell(i, j, k)] = v;
+        }
+    }
+}
+
 // Ghost fill of one patch: periodic along the axes with periodic[a] != 0,
 // zero-gradient (copy of the nearest interior cell) elsewhere.  On one level
 // with one patch this is what SAMRAI's periodic shift and the

@@ -89,6 +89,7 @@ def lib():
         L.hmro_sync_fluxes.argtypes = [cp, ip, dp, dp, dp, dp, dp]
         L.hmro_coarsen_fluxsum.argtypes = [cp, ip, ip, ip, ip, ip, dp, dp]
         L.hmro_coarsen_cells.argtypes = [cp, ip, ip, ip, ip, ip, dp, dp]
+        L.hmro_refine_ghosts.argtypes = [cp, ip, ip, ip, ip, ip, dp, dp, ctypes.c_double, dp]
         L.hmro_num_eqn.argtypes = [cp]
         L.hmro_num_comp.argtypes = [cp]
         _lib = L
@@ -337,6 +338,17 @@ def coarsen_cells(cfg, ratio, cn, clo, fn, flo, Qf, Qc):
                              _ip(_n3(fn)), _ip(list(flo) + [0] * (3 - len(flo))),
                              _dp(np.ascontiguousarray(Qf, dtype=np.float64)), _dp(Qc))
     return Qc
+
+
+def refine_ghosts(cfg, ratio, fn, flo, cn, clo, Qc_old, Qc_new, theta, Qf):
+    """Coarse-fine ghost cells of the fine patch (flo, fn) from the coarse patch (clo, cn)
+    at time fraction theta (linear time interpolation, conservative linear refinement); Qf in place."""
+    assert Qf.flags["C_CONTIGUOUS"] and Qf.dtype == np.float64
+    lib().hmro_refine_ghosts(ctypes.byref(cfg.c()), _ip(_n3(ratio)), _ip(_n3(fn)), _ip(list(flo) + [0] * (3 - len(flo))),
+                             _ip(_n3(cn)), _ip(list(clo) + [0] * (3 - len(clo))),
+                             _dp(np.ascontiguousarray(Qc_old, dtype=np.float64)),
+                             _dp(np.ascontiguousarray(Qc_new, dtype=np.float64)), float(theta), _dp(Qf))
+    return Qf
 
 
 def tangent_substep(cfg, n, dx, dt, stage, alpha, beta, Q_int, dQ_int, transport=None):
