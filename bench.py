@@ -63,6 +63,9 @@ def parse():
                     help="skip the batched-vs-per-patch measurement on uneven 3D patches")
     ap.add_argument("--no-peak", action="store_true", help="skip the FP64 peak microbenchmark")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint/forward cost measurement")
+    ap.add_argument("--c4-only", action="store_true",
+                    help="time only the C4 forward (Navier-Stokes Taylor-Green 128^3) for --steps steps after "
+                         "--warmup steps and print its line (used for the C4 launch list)")
     ap.add_argument("--c4", action="store_true",
                     help="also time the 3D Navier-Stokes Taylor-Green workload and its adjoint (128^3, ~1 min)")
     ap.add_argument("--c5", action="store_true",
@@ -485,6 +488,35 @@ def c4_navier_stokes(args, flow, N=128, nsteps=100, every=10, fd_dirs=16, fd_ste
     return out
 
 
+def c4_forward_only(args, flow, N=128):
+    """The C4 forward alone: --warmup then --steps SSPRK3 steps of the Navier-Stokes
+    Taylor-Green vortex (per-patch fused substeps), device-timed."""
+    import torch
+    from hamers_gb300 import problems as P
+    Qnp, dx = P.taylor_green_3d(N)
+    tr = P.taylor_green_transport()
+    dt = P.taylor_green_dt(Qnp[:, 4:-4, 4:-4, 4:-4], dx, mu=tr["species_mu"], prandtl=tr["species_Pr"])
+    fm = flow.FlowModel("SINGLE_SPECIES", 3, [1.4], transport=tr)
+    rec = flow.ConvectiveFluxReconstructor("WCNS5_JS_HLLC_HLL", fm, precision=args.precision,
+                                           diffusive_flux_reconstructor="MIDPOINT_FOURTH_ORDER")
+    ns = flow.NavierStokes(rec)
+    Q = torch.from_numpy(Qnp).cuda()
+    integ = flow.RungeKuttaLevelIntegrator(ns, flow.Patch([N] * 3, dx, Q), [1, 1, 1])
+    integ.advance(dt, nsteps=args.warmup)
+    torch.cuda.synchronize()
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    stream = torch.cuda.current_stream()
+    e[0].record(stream)
+    integ.advance(dt, nsteps=args.steps)
+    e[1].record(stream)
+    torch.cuda.synchronize()
+    ms = e[0].elapsed_time(e[1])
+    rec.close()
+    return {"workload": "3D Navier-Stokes Taylor-Green vortex 128^3 (C4 forward only)", "precision": args.precision,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / max(args.steps, 1),
+            "cell_updates_per_s": N ** 3 * 3 * args.steps / (ms * 1e-3)}
+
+
 def cpu_baseline_oracle(Q, n, dx, dt, budget_s=15.0, threads=None):
     """Oracle stage throughput on the host cores on a bounded sample (rows of the patch)."""
     from oracle import oracle as O
@@ -599,6 +631,10 @@ def main():
     from hamers_gb300 import build as B
     B.build()
     from hamers_gb300 import flow
+    if args.c4_only:
+        if rank == 0:
+            print(json.dumps({"c4_forward": c4_forward_only(args, flow)}), flush=True)
+        return
 
     n = args.n
     Qnp, dx, dt = workload(n)
