@@ -254,6 +254,7 @@ int hmr_ctx_create(const hmr_config* cfg, hmr_ctx** out) {
     c->v.model = cfg->flow_model;
     c->v.nsp = cfg->num_species;
     c->v.scheme = cfg->convective_flux_reconstructor;
+    c->v.dorder = cfg->diffusive_flux_reconstructor;
     species_params(cfg->species_gamma, cfg->species_R, cfg->num_species, c->P);
     scheme_params(cfg, c->P);
     c->precision = cfg->precision;
@@ -741,7 +742,6 @@ extern "C" {
 int hmr_level_create(hmr_ctx* c, int np, const hmr_patch_geometry* geoms, hmr_level** out) {
     if (!c || np < 1 || !geoms || !out) return HMR_ERR_ARGUMENT;
     *out = nullptr;
-    if (c->P.dorder) return HMR_ERR_UNSUPPORTED;   // the batched form covers the Euler equations
     for (int p = 0; p < np; p++)
         if (!valid_geom(c->v.dim, &geoms[p])) return HMR_ERR_ARGUMENT;
     hmr_level* lv = new (std::nothrow) hmr_level();

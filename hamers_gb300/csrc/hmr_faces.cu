@@ -6,6 +6,8 @@
 // (WCNS5-Z, WCNS6-CU-M2; namespace <form>_zc_m<model>).
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "hmr_launch.h"
 
 #ifndef HMR_MODEL
@@ -191,7 +193,9 @@ __device__ __forceinline__ int find_patch(const PatchWork* W, int np, long t, Of
 
 constexpr int LEVEL_MAX_THREADS = 256;
 
-template <int DIM, int MODEL, int NSP, int SCHEME>
+// DORD: 0 for the Euler equations, 2 or 4 for NavierStokes with that diffusive order (single
+// species); a separate instantiation, so that the Euler kernel keeps its registers.
+template <int DIM, int MODEL, int NSP, int SCHEME, int DORD>
 __global__ void __launch_bounds__(LEVEL_MAX_THREADS)
 level_kernel(Params P, LevelArgs L) {
     const long stride = (long)gridDim.x * blockDim.x;
@@ -246,7 +250,31 @@ level_kernel(Params P, LevelArgs L) {
         const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_sensor; });
         sensor_item<DIM, MODEL, NSP>(W[p].g, W[p].S, t - W[p].off_sensor);
     }
+    if constexpr (DORD != 0) {
+        // NavierStokes: temperature and node velocity gradient (needs the cell data only)
+        for (long t = t0; t < L.total_cells; t += stride) {
+            const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_cells; });
+            diff_grad_item<DIM, DORD>(P, W[p].g, W[p].S, t - W[p].off_cells);
+        }
+    }
     HMR_BARRIER();
+    if constexpr (DORD != 0) {
+        // NavierStokes: midpoint diffusive fluxes (needs the node gradient), beside the faces
+        for (long t = t0; t < L.total_face[0]; t += stride) {
+            const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_face[0]; });
+            diff_mid_item<DIM, DORD, 0>(P, W[p].g, W[p].S, t - W[p].off_face[0]);
+        }
+        for (long t = t0; t < L.total_face[1]; t += stride) {
+            const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_face[1]; });
+            diff_mid_item<DIM, DORD, 1>(P, W[p].g, W[p].S, t - W[p].off_face[1]);
+        }
+        if constexpr (DIM == 3) {
+            for (long t = t0; t < L.total_face[2]; t += stride) {
+                const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_face[2]; });
+                diff_mid_item<DIM, DORD, 2>(P, W[p].g, W[p].S, t - W[p].off_face[2]);
+            }
+        }
+    }
     constexpr bool X = !HMR_FAST;
     for (long t = t0; t < L.total_face[0]; t += stride) {
         const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_face[0]; });
@@ -301,23 +329,39 @@ level_kernel(Params P, LevelArgs L) {
         U.Qout = w.Qout;
         U.Fout.p[0] = nullptr;   // flux/source outputs are not produced by the batched form
         U.Sout.p[0] = nullptr;
-        U.dorder = 0;            // the batched form advances the Euler equations
+        U.dorder = DORD;
         update_item<DIM, MODEL, NSP>(w.g, w.S, U, t - w.off_update);
     }
+}
+
+// The level kernel instantiation of a variant: the diffusive order selects the NavierStokes one.
+template <class T, class F>
+static int with_dorder(const Variant& v, F f) {
+    if constexpr (T::MODEL == SINGLE_SPECIES) {
+        if (v.dorder == 4) return f(std::integral_constant<int, 4>{});
+        if (v.dorder == 2) return f(std::integral_constant<int, 2>{});
+    }
+    if (v.dorder != 0) return -2;
+    return f(std::integral_constant<int, 0>{});
+}
+
+template <class T, int DORD>
+static int level_max_blocks_of(int threads, int* blocks) {
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, level_kernel<T::DIM, T::MODEL, T::NSP, T::SCHEME, DORD>, threads, 0);
+    if (e != cudaSuccess) return (int)e;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    *blocks = per_sm * sms;
+    return 0;
 }
 
 int level_max_blocks(const Variant& v, int threads, int* blocks) {
     return dispatch(v, [&](auto t) {
         using T = decltype(t);
-        int per_sm = 0;
-        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &per_sm, level_kernel<T::DIM, T::MODEL, T::NSP, T::SCHEME>, threads, 0);
-        if (e != cudaSuccess) return (int)e;
-        int dev = 0, sms = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        *blocks = per_sm * sms;
-        return 0;
+        return with_dorder<T>(v, [&](auto d) { return level_max_blocks_of<T, decltype(d)::value>(threads, blocks); });
     });
 }
 
@@ -325,17 +369,20 @@ int launch_level(const Variant& v, const Params& P, const LevelArgs& L, int bloc
                  cudaStream_t st) {
     return dispatch(v, [&](auto t) {
         using T = decltype(t);
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(blocks);
-        cfg.blockDim = dim3(threads);
-        cfg.dynamicSmemBytes = 0;
-        cfg.stream = st;
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeCooperative;
-        attr[0].val.cooperative = 1;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
-        return (int)cudaLaunchKernelEx(&cfg, level_kernel<T::DIM, T::MODEL, T::NSP, T::SCHEME>, P, L);
+        return with_dorder<T>(v, [&](auto d) {
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(blocks);
+            cfg.blockDim = dim3(threads);
+            cfg.dynamicSmemBytes = 0;
+            cfg.stream = st;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeCooperative;
+            attr[0].val.cooperative = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            return (int)cudaLaunchKernelEx(&cfg, level_kernel<T::DIM, T::MODEL, T::NSP, T::SCHEME, decltype(d)::value>,
+                                           P, L);
+        });
     });
 }
 

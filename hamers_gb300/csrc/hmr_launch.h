@@ -104,6 +104,7 @@ struct Variant {
     int model;
     int nsp;
     int scheme;
+    int dorder = 0;   // NavierStokes midpoint diffusive flux order (0: Euler)
 };
 
 // One entry of the batched worklist: a patch with its stage states.

@@ -165,3 +165,49 @@ def test_navier_stokes_vjp_dot_product(cuda, case, stage):
         _, JVe = O.tangent_substep(cfg, n, dx, dt, stage, alpha, beta, Qs, V)
         assert abs(float(np.sum(W * JVe)) - rhs) > 10 * TOL_DOT[label] * scale
     ns.rec.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", [CASES[0], CASES[2]], ids=[IDS[0], IDS[2]])
+@pytest.mark.parametrize("precision", ["exact", "fast"])
+def test_batched_level_navier_stokes(cuda, case, precision):
+    """Uneven patches of one level in the persistent kernel with the diffusive phases: exact
+    form bitwise to the oracle's NavierStokes steps per patch, fast form within 1e-9."""
+    import torch
+    from hamers_gb300 import flow
+    dim, order, _ = case
+    rng = np.random.default_rng(23)
+    if dim == 2:
+        sizes = [(int(rng.integers(6, 26)), int(rng.integers(6, 26))) for _ in range(4)]
+    else:
+        sizes = [tuple(int(rng.integers(5, 12)) for _ in range(3)) for _ in range(3)]
+    cfg = O.Config(O.MODEL_SINGLE_SPECIES, dim, [1.4])
+    ns = make(dim, order, precision)
+    dt = 1.0e-3
+    geoms, tens, expect = [], [], []
+    for p, n in enumerate(sizes):
+        dx = [1.0 / v for v in n]
+        Q = smooth_state(O.MODEL_SINGLE_SPECIES, dim, n, seed=40 + p, species_gamma=[1.4])
+        Qo = Q.copy()
+        O.fill_ghosts(cfg, n, [1] * dim, Qo)
+        O.ns_rk3_advance(cfg, transport(order), n, dx, dt, [1] * dim, 2, Qo)
+        geoms.append((list(n), dx))
+        tens.append(torch.from_numpy(Q).cuda())
+        expect.append(Qo)
+    lv = flow.BatchedLevel(ns.rec, geoms)
+    for p, Q in enumerate(tens):
+        lv.bind(p, Q)
+        lv.set_periodic(p, [1] * dim)
+    for _ in range(2):
+        lv.step(dt)
+    torch.cuda.synchronize()
+    lv.check()
+    sl = (slice(None),) + tuple(slice(4, -4) if a < dim else slice(None) for a in (2, 1, 0))
+    for Q, Qo in zip(tens, expect):
+        got = Q.cpu().numpy()[sl]
+        if precision == "exact":
+            assert np.array_equal(got, Qo[sl]), np.abs(got - Qo[sl]).max()
+        else:
+            assert rel_err(got, Qo[sl]) <= 1e-9
+    lv.close()
+    ns.rec.close()
