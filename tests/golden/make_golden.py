@@ -2,10 +2,12 @@
 
 The reference ships no golden flux vectors (its tests pin only the order of
 accuracy), so these fixtures freeze the oracle's output on small seeded inputs:
-for each of the 12 variants (model x dimension x scheme), the dt-scaled face
-fluxes, the source and the face counters of computeConvectiveFluxAndSourceOnPatch
-on a smooth and a shock state, and the interior state after one SSPRK3 step with
-periodic ghost fill.  The inputs are regenerated from their seeds (tests/helpers.py).
+for each of the 24 variants (model x dimension x scheme: WCNS5-JS, WCNS6-LD, WCNS5-Z,
+WCNS6-CU-M2), the dt-scaled face fluxes, the source and the face counters of
+computeConvectiveFluxAndSourceOnPatch on a smooth and a shock state, and the interior
+state after one SSPRK3 step with periodic ghost fill; and for the Navier-Stokes path
+(single species, 2D/3D, second and fourth order) the diffusive face fluxes and one
+NavierStokes SSPRK3 step.  The inputs are regenerated from their seeds (tests/helpers.py).
 
     python tests/golden/make_golden.py      # rewrites tests/golden/convective_fixtures.npz
 """
@@ -32,11 +34,27 @@ SIZES = {2: (8, 6), 3: (4, 4, 4)}
 DT = 1.3e-3
 
 
+SCHEMES = ((O.SCHEME_WCNS5_JS, "js"), (O.SCHEME_WCNS6_LD, "ld"), (O.SCHEME_WCNS5_Z, "z"),
+           (O.SCHEME_WCNS6_CU_M2, "cu"))
+NS_TRANSPORT = dict(mu=0.02, c_p=3.5, Pr=0.72, mu_v=0.005)
+
+
 def cases():
     for model, mname, gam, R in MODELS:
         for dim in (2, 3):
-            for scheme, sname in ((O.SCHEME_WCNS5_JS, "js"), (O.SCHEME_WCNS6_LD, "ld")):
+            for scheme, sname in SCHEMES:
                 yield model, mname, gam, R, dim, scheme, sname
+
+
+def ns_cases():
+    for dim in (2, 3):
+        for order in (2, 4):
+            yield dim, order
+
+
+def ns_transport(order):
+    t = NS_TRANSPORT
+    return O.Transport(t["mu"], t["c_p"], t["Pr"], mu_v=t["mu_v"], order=order)
 
 
 def inputs(model, dim, gam, label):
@@ -48,11 +66,11 @@ def inputs(model, dim, gam, label):
 def compute():
     out = {}
     for model, mname, gam, R, dim, scheme, sname in cases():
-        cfg = O.Config(model, dim, gam, scheme, species_R=R)
         for label in ("smooth", "shock"):
             key = f"{mname}_{dim}d_{sname}_{label}"
             n, Q = inputs(model, dim, gam, label)
             dx = [1.0 / v for v in n]
+            cfg = O.Config(model, dim, gam, scheme, species_R=R, grid_dx=dx)
             F, S, st = O.conv_flux_source(cfg, n, dx, DT, Q)
             for a, f in enumerate(F):
                 out[f"{key}_flux{a}"] = f
@@ -61,6 +79,19 @@ def compute():
             Qs = Q.copy()
             O.fill_ghosts(cfg, n, [1] * dim, Qs)
             O.rk3_advance(cfg, n, dx, DT, [1] * dim, 1, Qs)
+            sl = (slice(None),) + tuple(slice(4, -4) if d < dim else slice(None) for d in (2, 1, 0))
+            out[f"{key}_rk3"] = np.ascontiguousarray(Qs[sl])
+    for dim, order in ns_cases():
+        cfg = O.Config(O.MODEL_SINGLE_SPECIES, dim, [1.4])
+        for label in ("smooth", "shock"):
+            key = f"ns_{dim}d_o{order}_{label}"
+            n, Q = inputs(O.MODEL_SINGLE_SPECIES, dim, [1.4], label)
+            dx = [1.0 / v for v in n]
+            for a, f in enumerate(O.diff_flux(cfg, ns_transport(order), n, dx, DT, Q)):
+                out[f"{key}_dflux{a}"] = f
+            Qs = Q.copy()
+            O.fill_ghosts(cfg, n, [1] * dim, Qs)
+            O.ns_rk3_advance(cfg, ns_transport(order), n, dx, DT, [1] * dim, 1, Qs)
             sl = (slice(None),) + tuple(slice(4, -4) if d < dim else slice(None) for d in (2, 1, 0))
             out[f"{key}_rk3"] = np.ascontiguousarray(Qs[sl])
     return out

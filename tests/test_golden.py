@@ -1,7 +1,7 @@
 """Golden fixtures of the convective path (tests/golden/convective_fixtures.npz).
 
-The fixtures freeze the oracle's output on small seeded inputs for all 12
-variants (see tests/golden/make_golden.py).  The CPU test checks that the
+The fixtures freeze the oracle's output on small seeded inputs for all 24
+convective variants and the Navier-Stokes path (see tests/golden/make_golden.py).  The CPU test checks that the
 oracle still reproduces them bit for bit (x86 and Arm alike: the oracle is
 built with -ffp-contract=off and uses only correctly rounded operations); the
 GPU test checks the exact form of the CUDA path against the stored values
@@ -39,8 +39,9 @@ def test_exact_form_matches_golden_fixtures(cuda, golden, case):
     model, mname, gam, R, dim, scheme, sname = case
     names = {0: "SINGLE_SPECIES", 1: "FOUR_EQN_CONSERVATIVE", 2: "FIVE_EQN_ALLAIRE"}
     fm = flow.FlowModel(names[model], dim, gam, species_R=R)
-    rec = flow.ConvectiveFluxReconstructor("WCNS5_JS_HLLC_HLL" if scheme == 0 else "WCNS6_LD_HLLC_HLL", fm,
-                                           precision="exact")
+    rname = {0: "WCNS5_JS_HLLC_HLL", 1: "WCNS6_LD_HLLC_HLL", 2: "WCNS5_Z_HLLC_HLL", 3: "WCNS6_CU_M2_HLLC_HLL"}[scheme]
+    n0, _ = G.inputs(model, dim, gam, "smooth")
+    rec = flow.ConvectiveFluxReconstructor(rname, fm, precision="exact", grid_geometry=[1.0 / v for v in n0])
     for label in ("smooth", "shock"):
         key = f"{mname}_{dim}d_{sname}_{label}"
         n, Q = G.inputs(model, dim, gam, label)
@@ -60,3 +61,37 @@ def test_exact_form_matches_golden_fixtures(cuda, golden, case):
         torch.cuda.synchronize()
         sl = (slice(None),) + tuple(slice(4, -4) if d < dim else slice(None) for d in (2, 1, 0))
         assert np.array_equal(Qs.cpu().numpy()[sl], golden[f"{key}_rk3"]), f"{key} rk3"
+
+
+NS_CASES = list(G.ns_cases())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", NS_CASES, ids=["%dd-o%d" % c for c in NS_CASES])
+def test_navier_stokes_matches_golden_fixtures(cuda, golden, case):
+    import torch
+    from hamers_gb300 import flow
+    dim, order = case
+    t = G.NS_TRANSPORT
+    fm = flow.FlowModel("SINGLE_SPECIES", dim, [1.4], transport={
+        "species_mu": t["mu"], "species_mu_v": t["mu_v"], "species_c_p": t["c_p"], "species_Pr": t["Pr"]})
+    rec = flow.ConvectiveFluxReconstructor("WCNS5_JS_HLLC_HLL", fm, precision="exact",
+                                           diffusive_flux_reconstructor="MIDPOINT_FOURTH_ORDER" if order == 4
+                                           else "MIDPOINT_SECOND_ORDER")
+    ns = flow.NavierStokes(rec)
+    for label in ("smooth", "shock"):
+        key = f"ns_{dim}d_o{order}_{label}"
+        n, Q = G.inputs(0, dim, [1.4], label)
+        dx = [1.0 / v for v in n]
+        patch = flow.Patch(n, dx, torch.from_numpy(Q).cuda())
+        F = rec.allocateFlux(patch)
+        ns.diff.computeDiffusiveFluxOnPatch(patch, F, G.DT)
+        torch.cuda.synchronize()
+        for a in range(dim):
+            assert np.array_equal(F[a].cpu().numpy(), golden[f"{key}_dflux{a}"]), f"{key} flux {a}"
+        Qs = torch.from_numpy(Q).cuda()
+        flow.RungeKuttaLevelIntegrator(ns, flow.Patch(n, dx, Qs), [1] * dim).advance(G.DT, nsteps=1)
+        torch.cuda.synchronize()
+        sl = (slice(None),) + tuple(slice(4, -4) if d < dim else slice(None) for d in (2, 1, 0))
+        assert np.array_equal(Qs.cpu().numpy()[sl], golden[f"{key}_rk3"]), f"{key} rk3"
+    rec.close()
