@@ -447,6 +447,10 @@ def c4_navier_stokes(args, flow, N=128, nsteps=100, every=10, fd_dirs=16, fd_ste
            "precision": args.precision, "dt": dt, "steps": nsteps,
            "forward_ms": t_fwd, "forward_cell_updates_per_s": cells * 3 * nsteps / (t_fwd * 1e-3),
            "adjoint_ms": t_adj, "adjoint_over_forward": t_adj / t_fwd,
+           "vjp_over_forward_est": (t_adj - t_fwd) / t_fwd,
+           "note": "adjoint = the whole reverse sweep: each segment's forward recomputed from its checkpoint "
+                   "(about one forward) plus the substep and ghost-fill VJPs; vjp_over_forward_est subtracts "
+                   "one forward",
            "final_kinetic_energy": J}
     # gradient with respect to the initial velocity: for u -> u + du at fixed rho and p,
     # d(rho u) = rho du and dE = rho u.du, so dJ/du = rho (dJ/d(rho u) + u dJ/dE)

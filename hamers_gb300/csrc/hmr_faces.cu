@@ -196,7 +196,7 @@ constexpr int LEVEL_MAX_THREADS = 256;
 // DORD: 0 for the Euler equations, 2 or 4 for NavierStokes with that diffusive order (single
 // species); a separate instantiation, so that the Euler kernel keeps its registers.
 template <int DIM, int MODEL, int NSP, int SCHEME, int DORD>
-__global__ void __launch_bounds__(LEVEL_MAX_THREADS)
+__global__ void __launch_bounds__(LEVEL_MAX_THREADS, 1)
 level_kernel(Params P, LevelArgs L) {
     const long stride = (long)gridDim.x * blockDim.x;
     const long t0 = (long)blockIdx.x * blockDim.x + threadIdx.x;
