@@ -988,9 +988,9 @@ static int level_capture_cfl(hmr_level* lv, double cfl) {
     if (r == HMR_OK) {
         r = cuda_status(cudaMemsetAsync(lv->d_srmax, 0, sizeof(unsigned long long), cs));
         if (r == HMR_OK)
-            r = hmr_cells::launch_spectral_level(c->v, c->P, lv->d_work, lv->npatch, lv->L.total_update,
+            r = hmr_cells::launch_spectral_level(c->v, c->P, lv->d_work, lv->npatch, lv->L.total_cells,
                                                  lv->d_srmax, cs);
-        if (r == HMR_OK) r = hmr_cells::launch_stable_dt(lv->d_srmax, cfl, lv->d_dt, cs);
+        if (r == HMR_OK) r = hmr_cells::launch_stable_dt(lv->d_srmax, cfl, lv->d_dt, cs, c->P.dorder != 0);
         for (int stage = 0; stage < 3 && r == HMR_OK; stage++) {
             r = cuda_status(cudaMemsetAsync(lv->d_barrier, 0, 2 * sizeof(unsigned int), cs));
             if (r != HMR_OK) break;

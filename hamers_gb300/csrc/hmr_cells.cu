@@ -186,6 +186,19 @@ __device__ __forceinline__ double spectral_cell(const Params& P, const Geom& g, 
     double s = add_(fabs(V[M::IU]), cs)/g.dx[0];
 #pragma unroll
     for (int d = 1; d < DIM; d++) s = add_(s, add_(fabs(V[M::IU + d]), cs)/g.dx[d]);
+    if constexpr (MODEL == SINGLE_SPECIES) {
+        if (P.dorder != 0) {
+            // NavierStokes.cpp:1074-1078: 2 max_d(D/dx_d^2), D = max(mu/rho, mu_v/rho, kappa/(rho c_p))
+            // (FlowModelSingleSpecies.cpp:4569-4573); the patch value is the max of both radii
+            const double r = V[0];
+            double Dm = fmax(P.cmu/r, P.cmu_v/r);
+            Dm = fmax(Dm, P.ckappa/mul_(r, P.cp[0]));
+            double q = Dm/mul_(g.dx[0], g.dx[0]);
+            if constexpr (DIM == 2) q = fmax(q, Dm/mul_(g.dx[1], g.dx[1]));
+            else q = fmax(q, fmax(Dm/mul_(g.dx[1], g.dx[1]), Dm/mul_(g.dx[2], g.dx[2])));
+            s = fmax(s, mul_(double(2), q));
+        }
+    }
     return s;
 }
 
@@ -205,15 +218,13 @@ __device__ __forceinline__ void block_max_to(double v, unsigned long long* d_max
     }
 }
 
+// Item: a cell of the ghost box (the reference's loops cover the ghost cells too).
 template <int DIM, int MODEL, int NSP>
 __global__ void __launch_bounds__(THREADS) spectral_patch_kernel(Params P, Geom g, Comp Q, unsigned long long* d_max) {
-    const long n = ninterior_of(g);
+    const long n = ncell_of(g);
     double m = 0.0;
-    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
-        const int i = (int)(t % g.n[0]), j = (int)((t / g.n[0]) % g.n[1]);
-        const int k = DIM == 3 ? (int)(t / ((long)g.n[0] * g.n[1])) : 0;
-        m = fmax(m, spectral_cell<DIM, MODEL, NSP>(P, g, Q, cidx<DIM>(g, i, j, k)));
-    }
+    for (long x = (long)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (long)gridDim.x * blockDim.x)
+        m = fmax(m, spectral_cell<DIM, MODEL, NSP>(P, g, Q, x));
     block_max_to(m, d_max);
 }
 
@@ -225,28 +236,26 @@ __global__ void __launch_bounds__(THREADS) spectral_level_kernel(Params P, const
         int lo = 0, hi = np - 1;
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
-            if (W[mid].off_update <= t) lo = mid;
+            if (W[mid].off_cells <= t) lo = mid;
             else hi = mid - 1;
         }
-        const Geom& g = W[lo].g;
-        const long u = t - W[lo].off_update;
-        const int i = (int)(u % g.n[0]), j = (int)((u / g.n[0]) % g.n[1]);
-        const int k = DIM == 3 ? (int)(u / ((long)g.n[0] * g.n[1])) : 0;
-        m = fmax(m, spectral_cell<DIM, MODEL, NSP>(P, g, W[lo].Q[0], cidx<DIM>(g, i, j, k)));
+        m = fmax(m, spectral_cell<DIM, MODEL, NSP>(P, W[lo].g, W[lo].Q[0], t - W[lo].off_cells));
     }
     block_max_to(m, d_max);
 }
 
-__global__ void stable_dt_kernel(const unsigned long long* d_max, double cfl, double* d_dt) {
+// Euler: dt = (1/max)*cfl (Euler.cpp:729, 881; RungeKuttaLevelIntegrator.cpp:1914-1916);
+// NavierStokes: dt = (1/(max + eps))*cfl (NavierStokes.cpp:893, 1085).
+__global__ void stable_dt_kernel(const unsigned long long* d_max, double cfl, double* d_dt, int ns) {
     const double m = __longlong_as_double((long long)*d_max);
-    *d_dt = mul_(double(1)/m, cfl);
+    *d_dt = mul_(ns ? double(1)/add_(m, HMR_EPS) : double(1)/m, cfl);
 }
 
 int launch_spectral_patch(const Variant& v, const Params& P, const Geom& g, const Comp& Q,
                           unsigned long long* d_max, cudaStream_t st) {
     return dispatch(v, [&](auto t) {
         using T = decltype(t);
-        int blocks = grid_for(ninterior_of(g));
+        int blocks = grid_for(ncell_of(g));
         if (blocks > 4096) blocks = 4096;
         spectral_patch_kernel<T::DIM, T::MODEL, T::NSP><<<blocks, THREADS, 0, st>>>(P, g, Q, d_max);
         return (int)cudaPeekAtLastError();
@@ -264,8 +273,8 @@ int launch_spectral_level(const Variant& v, const Params& P, const PatchWork* wo
     });
 }
 
-int launch_stable_dt(const unsigned long long* d_max, double cfl, double* d_dt, cudaStream_t st) {
-    stable_dt_kernel<<<1, 1, 0, st>>>(d_max, cfl, d_dt);
+int launch_stable_dt(const unsigned long long* d_max, double cfl, double* d_dt, cudaStream_t st, bool ns) {
+    stable_dt_kernel<<<1, 1, 0, st>>>(d_max, cfl, d_dt, ns ? 1 : 0);
     return (int)cudaPeekAtLastError();
 }
 

@@ -45,6 +45,7 @@ inline int diffusive_params(const hmr_config* cfg, Params& P) {
     const int order = cfg->diffusive_flux_reconstructor;
     P.dorder = 0;
     P.dS43 = P.dS23 = P.dmu = P.dkappa = P.dTc = 0.0;
+    P.cmu = P.cmu_v = P.ckappa = 0.0;
     if (order == HMR_DIFFUSIVE_NONE) return HMR_OK;
     if (order != HMR_MIDPOINT_SECOND_ORDER && order != HMR_MIDPOINT_FOURTH_ORDER) return HMR_ERR_UNSUPPORTED;
     if (cfg->flow_model != HMR_SINGLE_SPECIES) return HMR_ERR_UNSUPPORTED;
@@ -56,6 +57,9 @@ inline int diffusive_params(const hmr_config* cfg, Params& P) {
     const double mu_s = host_mid_value(order, mu, mu, mu, mu);
     const double mu_v_s = host_mid_value(order, mu_v, mu_v, mu_v, mu_v);
     P.dorder = order;
+    P.cmu = mu;
+    P.cmu_v = mu_v;
+    P.ckappa = kappa;
     P.dmu = mu_s;
     P.dkappa = host_mid_value(order, kappa, kappa, kappa, kappa);
     P.dS43 = double(4)/double(3)*mu_s + mu_v_s;
@@ -165,14 +169,15 @@ int launch_sensor(const hmr::Variant& v, const hmr::Geom& g, const hmr::Scratch&
 int launch_fill(int dim, const hmr::Geom& g, const hmr::Comp& Q, int ncomp, const int* periodic, cudaStream_t st);
 int launch_fill_vjp(int dim, const hmr::Geom& g, const hmr::Comp& Qb, int ncomp, const int* periodic,
                     cudaStream_t st);
-// Stable time step (Euler::computeSpectralRadiusesAndStableDtOnPatch): running max over interior
-// cells of sum_d (|u_d| + c)/dx_d into *d_max (bits of a non-negative double), per patch or over a
-// level's worklist (slot-0 states), and dt = (1/max)*cfl.
+// Stable time step (Euler::computeSpectralRadiusesAndStableDtOnPatch): running max over the
+// ghost-box cells of sum_d (|u_d| + c)/dx_d (NavierStokes: and of the diffusive radius) into
+// *d_max (bits of a non-negative double), per patch or over a level's worklist (slot-0 states),
+// and dt = (1/max)*cfl (NavierStokes: (1/(max + eps))*cfl).
 int launch_spectral_patch(const hmr::Variant& v, const hmr::Params& P, const hmr::Geom& g, const hmr::Comp& Q,
                           unsigned long long* d_max, cudaStream_t st);
 int launch_spectral_level(const hmr::Variant& v, const hmr::Params& P, const hmr::PatchWork* work, int npatch,
                           long total_interior, unsigned long long* d_max, cudaStream_t st);
-int launch_stable_dt(const unsigned long long* d_max, double cfl, double* d_dt, cudaStream_t st);
+int launch_stable_dt(const unsigned long long* d_max, double cfl, double* d_dt, cudaStream_t st, bool ns = false);
 // Euler / NavierStokes advanceSingleStepOnPatch; with Fdint (ncoef diffusive flux sets) the
 // NavierStokes form, and Fdacc (optional) accumulates them with gamma.
 int launch_rk_stage(const hmr::Variant& v, const hmr::Geom& g, int ncoef, const double* alpha,

@@ -52,6 +52,7 @@ struct Params {
     // (constant cell values interpolated to the midpoints), and (gamma - 1) c_v for T.
     int dorder;                        // 0 Euler; 2, 4 midpoint diffusive flux of that order
     double dS43, dS23, dmu, dkappa, dTc;
+    double cmu, cmu_v, ckappa;         // the cell values of mu, mu_v, kappa (stable time step)
 };
 
 template <int DIM, int MODEL, int NSP>

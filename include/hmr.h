@@ -203,10 +203,14 @@ int hmr_fill_ghosts_patch(hmr_ctx* ctx, const hmr_patch_geometry* geom, double* 
                           const int* periodic, void* stream);
 
 /* Stable time step of a patch (Euler::computeSpectralRadiusesAndStableDtOnPatch,
- * src/apps/Euler/Euler.cpp:489-900): the maximum over interior cells of
- * sum_d (|u_d| + c)/dx_d is max-reduced into *d_max (a device double holding a non-negative
- * value: 0.0 to start, or a previous patch's value for a running maximum over a level).
- * The level's time step is then (1/max)*CFL (RungeKuttaLevelIntegrator.cpp:1846-1916). */
+ * src/apps/Euler/Euler.cpp:489-900): the maximum over the cells of the ghost box (the
+ * reference's loops include the ghost cells) of sum_d (|u_d| + c)/dx_d is max-reduced into
+ * *d_max (a device double holding a non-negative value: 0.0 to start, or a previous patch's
+ * value for a running maximum over a level).  The level's time step is then (1/max)*CFL
+ * (RungeKuttaLevelIntegrator.cpp:1846-1916).  With a diffusive_flux_reconstructor this is
+ * NavierStokes's (NavierStokes.cpp:595-1100): the maximum also covers the diffusive radius
+ * 2 max_d(D/dx_d^2), D = max(mu/rho, mu_v/rho, kappa/(rho c_p)), and the time step is
+ * (1/(max + 1e-15))*CFL. */
 int hmr_spectral_radius_patch(hmr_ctx* ctx, const hmr_patch_geometry* geom, const double* const* Q,
                               double* d_max, void* stream);
 
@@ -303,8 +307,9 @@ int hmr_level_substep(hmr_level* level, int stage, double dt, void* stream);
 int hmr_level_step(hmr_level* level, double dt, void* stream);
 /* Synchronises and reports whether a barrier of a persistent kernel gave up
  * (HMR_ERR_BARRIER, flag cleared) since the last check. */
-/* One SSPRK3 step whose time step is computed on the device from the slot-0 states,
- * dt = (1/max spectral radius)*cfl over every patch of the level, inside the same captured
+/* One SSPRK3 step whose time step is computed on the device from the slot-0 states (ghost
+ * boxes as they stand), dt = (1/max spectral radius)*cfl over every patch of the level
+ * (NavierStokes: as hmr_spectral_radius_patch describes), inside the same captured
  * graph as the three substeps: no host synchronisation per step.  The graph is cached for
  * the cfl value. */
 int hmr_level_step_cfl(hmr_level* level, double cfl, void* stream);

@@ -269,9 +269,15 @@ int hmro_ns_rk3_advance(const hmro_config* cfg, const hmro_transport* tr, const 
 }
 
 // Euler::computeSpectralRadiusesAndStableDtOnPatch (Euler.cpp:489-900) for one
-// patch: max over interior cells of sum_d (|u_d| + c)/dx_d (max wave speed
-// |u_d| + c, FlowModelSingleSpecies.cpp:3959 and the other models' analogues).
-double hmro_spectral_radius(const hmro_config* cfg, const int* n, const double* dx, const double* Q) {
+// patch: max over the cells of the ghost box (the reference's loops run from
+// -num_ghosts to n + num_ghosts, Euler.cpp:699-736, 841-880) of sum_d (|u_d| + c)/dx_d (max
+// wave speed |u_d| + c, FlowModelSingleSpecies.cpp:3959 and the other models'
+// analogues); the stable dt is 1/max.  With tr non-null, NavierStokes's
+// (NavierStokes.cpp:595-1100, diffusive radius :884, :1074, dt :893, :1085): the max also
+// covers 2 max_d(D/dx_d^2) with D = max(mu/rho, mu_v/rho, kappa/(rho c_p))
+// (FlowModelSingleSpecies.cpp:4569-4573), and the stable dt is 1/(max + eps).
+double hmro_spectral_radius_ns(const hmro_config* cfg, const hmro_transport* tr, const int* n, const double* dx,
+                               const double* Q) {
     const Config c = to_cfg(cfg);
     const Box b = make_box(c.dim, n, 4);
     const int ncomp = num_comp(c);
@@ -281,16 +287,28 @@ double hmro_spectral_radius(const hmro_config* cfg, const int* n, const double* 
     compute_derived(c, b, q.data(), D);
     const int iu = vel_index(c);
     const long nc = b.ncell();
-    double m = 0.0;
-    for (int k = 0; k < b.n[2]; k++)
-    for (int j = 0; j < b.n[1]; j++)
-    for (int i = 0; i < b.n[0]; i++) {
-        const long x = b.cell(i, j, k);
+    double m = 0.0, md = 0.0;
+    for (long x = 0; x < nc; x++) {
         double s = (std::fabs(D.V[(size_t)iu * nc + x]) + D.cs[x])/dx[0];
         for (int d = 1; d < c.dim; d++) s = s + (std::fabs(D.V[(size_t)(iu + d) * nc + x]) + D.cs[x])/dx[d];
         m = std::fmax(m, s);
+        if (tr) {
+            const double rho = D.V[x];
+            const double c_p = c.gamma[0]/(c.gamma[0] - double(1))*c.R[0];
+            const double kappa = tr->c_p*tr->mu_kappa/tr->Pr;
+            double Dm = std::fmax(tr->mu/rho, tr->mu_v/rho);
+            Dm = std::fmax(Dm, kappa/(rho*c_p));
+            double r = Dm/(dx[0]*dx[0]);
+            if (c.dim == 2) r = std::fmax(r, Dm/(dx[1]*dx[1]));
+            else r = std::fmax(r, std::fmax(Dm/(dx[1]*dx[1]), Dm/(dx[2]*dx[2])));
+            md = std::fmax(md, double(2)*r);
+        }
     }
-    return m;
+    return tr ? std::fmax(md, m) : m;
+}
+
+double hmro_spectral_radius(const hmro_config* cfg, const int* n, const double* dx, const double* Q) {
+    return hmro_spectral_radius_ns(cfg, nullptr, n, dx, Q);
 }
 
 // CPU baseline: the patch is split along its slowest axis into nthreads

@@ -82,6 +82,8 @@ def lib():
         L.hmro_stage_threads.restype = ctypes.c_long
         L.hmro_spectral_radius.argtypes = [cp, ip, dp, dp]
         L.hmro_spectral_radius.restype = ctypes.c_double
+        L.hmro_spectral_radius_ns.argtypes = [cp, ctypes.POINTER(_Transport), ip, dp, dp]
+        L.hmro_spectral_radius_ns.restype = ctypes.c_double
         tp = ctypes.POINTER(_Transport)
         L.hmro_diff_flux.argtypes = [cp, tp, ip, dp, ctypes.c_double, dp, dp]
         L.hmro_rk_stage_ns.argtypes = [cp, ip, dp, ctypes.c_int, dp, dp, dp, dp, dp, dp, dp, dp]
@@ -370,8 +372,12 @@ def tangent_substep(cfg, n, dx, dt, stage, alpha, beta, Q_int, dQ_int, transport
     return Qo, dQo
 
 
-def spectral_radius(cfg, n, dx, Q):
-    """Max over interior cells of sum_d (|u_d| + c)/dx_d (the stable dt is (1/that)*CFL)."""
+def spectral_radius(cfg, n, dx, Q, transport=None):
+    """Max over the ghost box of sum_d (|u_d| + c)/dx_d (the stable dt is (1/that)*CFL); with a
+    Transport, NavierStokes's max of that and the diffusive radius (dt = (1/(that + eps))*CFL)."""
     Q = np.ascontiguousarray(Q, dtype=np.float64)
+    if transport is not None:
+        return lib().hmro_spectral_radius_ns(ctypes.byref(cfg.c()), ctypes.byref(transport.c()), _ip(_n3(n)),
+                                             _dv(list(dx) + [1.0] * (3 - len(dx))), _dp(Q))
     return lib().hmro_spectral_radius(ctypes.byref(cfg.c()), _ip(_n3(n)), _dv(list(dx) + [1.0] * (3 - len(dx))),
                                       _dp(Q))

@@ -211,3 +211,33 @@ def test_batched_level_navier_stokes(cuda, case, precision):
             assert rel_err(got, Qo[sl]) <= 1e-9
     lv.close()
     ns.rec.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", [CASES[0], CASES[2]], ids=[IDS[0], IDS[2]])
+def test_navier_stokes_stable_dt(cuda, case):
+    """NavierStokes::computeSpectralRadiusesAndStableDtOnPatch: the acoustic and diffusive radii
+    over the ghost box, bitwise; and the level's on-device dt = (1/(max + eps))*cfl."""
+    import torch
+    from hamers_gb300 import flow
+    dim, order, n = case
+    cfg = O.Config(O.MODEL_SINGLE_SPECIES, dim, [1.4])
+    ns = make(dim, order, "exact")
+    # a viscous case: the diffusive radius dominates on the finer axis
+    dx = [1.0 / v for v in n]
+    dx[0] *= 1e-3
+    Q = smooth_state(O.MODEL_SINGLE_SPECIES, dim, n, seed=17, species_gamma=[1.4])
+    want = O.spectral_radius(cfg, n, dx, Q, transport=transport(order))
+    assert want > O.spectral_radius(cfg, n, dx, Q)
+    got = ns.spectralRadius(flow.Patch(n, dx, torch.from_numpy(Q).cuda()))
+    assert got == want
+    lv = flow.BatchedLevel(ns.rec, [(list(n), dx)])
+    Qg = torch.from_numpy(Q).cuda()
+    lv.bind(0, Qg)
+    lv.set_periodic(0, [1] * dim)
+    lv.step_cfl(0.4)
+    torch.cuda.synchronize()
+    lv.check()
+    assert lv.last_dt() == (1.0 / (want + 1e-15)) * 0.4
+    lv.close()
+    ns.rec.close()
