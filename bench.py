@@ -48,6 +48,10 @@ ALG_FP64_OPS_PER_CELL = 6140.0
 ALG_BYTES_PER_CELL = 8 * NEQ * (2 + 3 + 3) / 3.0
 
 
+# DRAM traffic of one level_kernel launch of the default workload, bytes (ncu capture).
+LEVEL_KERNEL_TRAFFIC_BYTES = 412389632 + 249082624
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -739,9 +743,13 @@ def main():
                 "d2h_bytes_per_step": state_bytes},
         "gpu_launches": 3 * launches_per_substep * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved_gbs / hbm, "traffic": None,
-                     "note": f"peak {peak_kind}; algorithmic {ALG_BYTES_PER_CELL:.1f} B/cell-update; "
-                             "the kernel is FP64-pipe bound, see fp64"},
+                     "frac": achieved_gbs / hbm,
+                     # ncu dram__bytes_read.sum + dram__bytes_write.sum of one level_kernel launch
+                     # of this workload (profiles/level_kernel_dram_c2_five_eqn_ld_1024.md)
+                     "traffic": LEVEL_KERNEL_TRAFFIC_BYTES if (n == 1024 and args.form == "batched") else None,
+                     "note": f"peak {peak_kind}; algorithmic {ALG_BYTES_PER_CELL:.1f} B/cell-update; traffic: ncu "
+                             "DRAM bytes of one launch (scratch round trips of the persistent kernel's "
+                             "phases); the kernel is FP64-pipe bound, see fp64"},
         "fp64": {"achieved": ALG_FP64_OPS_PER_CELL * n * n / (avg_sub_ms * 1e-3) / 1e12,
                  "peak": fp64, "unit": "TFLOP/s", "frac": (ALG_FP64_OPS_PER_CELL * n * n / (avg_sub_ms * 1e-3)
                                                          / 1e12 / fp64) if fp64 else None,

@@ -475,13 +475,17 @@ __device__ __forceinline__ double ld_interp(const double* b, double sigma, const
     const double tau_6 = fabs(sub_(b[3], beta_avg));
     const double R_tau = tau_6/add_(beta_avg, HMR_EPS);
     const bool blend = R_tau > P.alpha_tau;
-    double u0, u1, u2, o0, o1, o2, o3;
+    double u0 = 0.0, u1 = 0.0, u2 = 0.0, o0, o1, o2, o3;
+    // The upwind weights u_k only enter when the switch blends (their value is not used
+    // otherwise, so skipping them changes no result).
     if constexpr (X) {
-        u0 = mul_(double(1)/double(16), add_(double(1), ipow_<true>(tau_5/add_(b[0], HMR_EPS), P.p)));
-        u1 = mul_(double(5)/double(8), add_(double(1), ipow_<true>(tau_5/add_(b[1], HMR_EPS), P.p)));
-        u2 = mul_(double(5)/double(16), add_(double(1), ipow_<true>(tau_5/add_(b[2], HMR_EPS), P.p)));
-        const double us = add_(add_(u0, u1), u2);
-        u0 = u0/us; u1 = u1/us; u2 = u2/us;
+        if (blend) {
+            u0 = mul_(double(1)/double(16), add_(double(1), ipow_<true>(tau_5/add_(b[0], HMR_EPS), P.p)));
+            u1 = mul_(double(5)/double(8), add_(double(1), ipow_<true>(tau_5/add_(b[1], HMR_EPS), P.p)));
+            u2 = mul_(double(5)/double(16), add_(double(1), ipow_<true>(tau_5/add_(b[2], HMR_EPS), P.p)));
+            const double us = add_(add_(u0, u1), u2);
+            u0 = u0/us; u1 = u1/us; u2 = u2/us;
+        }
         o0 = mul_(double(1)/double(32), add_(P.C, ipow_<true>(tau_6/add_(b[0], HMR_EPS), P.q)));
         o1 = mul_(double(15)/double(32), add_(P.C, ipow_<true>(tau_6/add_(b[1], HMR_EPS), P.q)));
         o2 = mul_(double(15)/double(32), add_(P.C, ipow_<true>(tau_6/add_(b[2], HMR_EPS), P.q)));
@@ -511,11 +515,13 @@ __device__ __forceinline__ double ld_interp(const double* b, double sigma, const
         const double e01 = e0*e1, e23 = e2*e3;
         const double rp = double(1)/(e01*e23);
         const double r0 = rp*(e1*e23), r1 = rp*(e0*e23), r2 = rp*(e01*e3), r3 = rp*(e01*e2);
-        u0 = double(1)/double(16)*(double(1) + ipow_<false>(tau_5*r0, P.p));
-        u1 = double(5)/double(8)*(double(1) + ipow_<false>(tau_5*r1, P.p));
-        u2 = double(5)/double(16)*(double(1) + ipow_<false>(tau_5*r2, P.p));
-        const double ru = double(1)/(u0 + u1 + u2);
-        u0 *= ru; u1 *= ru; u2 *= ru;
+        if (blend) {
+            u0 = double(1)/double(16)*(double(1) + ipow_<false>(tau_5*r0, P.p));
+            u1 = double(5)/double(8)*(double(1) + ipow_<false>(tau_5*r1, P.p));
+            u2 = double(5)/double(16)*(double(1) + ipow_<false>(tau_5*r2, P.p));
+            const double ru = double(1)/(u0 + u1 + u2);
+            u0 *= ru; u1 *= ru; u2 *= ru;
+        }
         o0 = double(1)/double(32)*(P.C + ipow_<false>(tau_6*r0, P.q));
         o1 = double(15)/double(32)*(P.C + ipow_<false>(tau_6*r1, P.q));
         o2 = double(15)/double(32)*(P.C + ipow_<false>(tau_6*r2, P.q));
