@@ -161,16 +161,19 @@ __device__ __forceinline__ void ld_side_bwd(const Params& P, double sigma, const
     // weights, with reciprocals (derivative values only)
     const double du[3] = {1.0/16.0, 5.0/8.0, 5.0/16.0};
     const double dc[4] = {1.0/32.0, 15.0/32.0, 15.0/32.0, 1.0/32.0};
-    double r[4], xu[3], xo[4], pu1[3], po1[4], ur[3], orw[4];
+    double r[4], xu[3] = {0, 0, 0}, xo[4], pu1[3] = {0, 0, 0}, po1[4], ur[3] = {0, 0, 0}, orw[4];
 #pragma unroll
     for (int k = 0; k < 4; k++) r[k] = double(1)/(b[k] + HMR_EPS);
-    double Us = 0.0, Os = 0.0;
+    double Us = 1.0, Os = 0.0;
+    if (blend) {   // the upwind weights only enter where the switch blends
+        Us = 0.0;
 #pragma unroll
-    for (int k = 0; k < 3; k++) {
-        xu[k] = tau_5*r[k];
-        pu1[k] = ipow0(xu[k], P.p - 1);
-        ur[k] = du[k]*(1.0 + pu1[k]*xu[k]);
-        Us += ur[k];
+        for (int k = 0; k < 3; k++) {
+            xu[k] = tau_5*r[k];
+            pu1[k] = ipow0(xu[k], P.p - 1);
+            ur[k] = du[k]*(1.0 + pu1[k]*xu[k]);
+            Us += ur[k];
+        }
     }
 #pragma unroll
     for (int k = 0; k < 4; k++) {
@@ -179,7 +182,7 @@ __device__ __forceinline__ void ld_side_bwd(const Params& P, double sigma, const
         orw[k] = dc[k]*(P.C + po1[k]*xo[k]);
         Os += orw[k];
     }
-    const double iUs = double(1)/Us, iOs = double(1)/Os;
+    const double iUs = blend ? double(1)/Us : 0.0, iOs = double(1)/Os;
     double u[3], o[4], of[4];
 #pragma unroll
     for (int k = 0; k < 3; k++) u[k] = ur[k]*iUs;
@@ -258,10 +261,11 @@ __device__ __forceinline__ void ld_pair_keep(const double* U, const Params& P, d
     const double sigma = ld_sigma(U);
     js_betas_x(U[0], U[1], U[2], U[3], U[4], b[0], b[1], b[2]);
     b[3] = ld_beta3(U[0], U[1], U[2], U[3], U[4], U[5]);
-    Um = ld_interp<true>(b, sigma, P, U[0], U[1], U[2], U[3], U[4], U[5]);
+    double sg = sigma;
+    Um = ld_interp<true>(b, U, sg, P, U[0], U[1], U[2], U[3], U[4], U[5]);
     js_betas_x(U[5], U[4], U[3], U[2], U[1], b[4], b[5], b[6]);
     b[7] = ld_beta3(U[5], U[4], U[3], U[2], U[1], U[0]);
-    Up = ld_interp<true>(b + 4, sigma, P, U[5], U[4], U[3], U[2], U[1], U[0]);
+    Up = ld_interp<true>(b + 4, U, sg, P, U[5], U[4], U[3], U[2], U[1], U[0]);
     b[8] = sigma;
 }
 

@@ -467,7 +467,9 @@ __device__ __forceinline__ double ld_beta3(double S0, double S1, double S2, doub
 // WCNS6-LD weights and midpoint value (WCNS6-LD-HLLC-HLL.cpp:158-222), stencil S0..S5 from
 // the upwind side; b[0..3] are that side's smoothness indicators.
 template <bool X>
-__device__ __forceinline__ double ld_interp(const double* b, double sigma, const Params& P,
+// sigma: the pair's ld_sigma(U), or negative until a side needs it (computed on first use:
+// it only enters where the switch blends).
+__device__ __forceinline__ double ld_interp(const double* b, const double* U, double& sigma, const Params& P,
                                             double S0, double S1, double S2, double S3, double S4, double S5) {
     // Decision inputs are always exact: tau_5, tau_6, beta_avg, R_tau.
     const double tau_5 = fabs(sub_(b[0], b[2]));
@@ -493,6 +495,7 @@ __device__ __forceinline__ double ld_interp(const double* b, double sigma, const
         const double os = add_(add_(add_(o0, o1), o2), o3);
         o0 = o0/os; o1 = o1/os; o2 = o2/os; o3 = o3/os;
         if (blend) {
+            if (sigma < 0.0) sigma = ld_sigma(U);
             const double ms = sub_(double(1), sigma);
             o0 = add_(mul_(sigma, u0), mul_(ms, o0));
             o1 = add_(mul_(sigma, u1), mul_(ms, o1));
@@ -529,6 +532,7 @@ __device__ __forceinline__ double ld_interp(const double* b, double sigma, const
         const double ro = double(1)/(o0 + o1 + o2 + o3);
         o0 *= ro; o1 *= ro; o2 *= ro; o3 *= ro;
         if (blend) {
+            if (sigma < 0.0) sigma = ld_sigma(U);
             o0 = sigma*u0 + (double(1) - sigma)*o0;
             o1 = sigma*u1 + (double(1) - sigma)*o1;
             o2 = sigma*u2 + (double(1) - sigma)*o2;
@@ -545,14 +549,14 @@ __device__ __forceinline__ double ld_interp(const double* b, double sigma, const
 
 template <bool X>
 __device__ __forceinline__ void ld_pair(const double* U, const Params& P, double& Um, double& Up) {
-    const double sigma = ld_sigma(U);
+    double sigma = -1.0;   // ld_sigma(U), computed if a side blends
     double b[4];
     js_betas_x(U[0], U[1], U[2], U[3], U[4], b[0], b[1], b[2]);
     b[3] = ld_beta3(U[0], U[1], U[2], U[3], U[4], U[5]);
-    Um = ld_interp<X>(b, sigma, P, U[0], U[1], U[2], U[3], U[4], U[5]);
+    Um = ld_interp<X>(b, U, sigma, P, U[0], U[1], U[2], U[3], U[4], U[5]);
     js_betas_x(U[5], U[4], U[3], U[2], U[1], b[0], b[1], b[2]);
     b[3] = ld_beta3(U[5], U[4], U[3], U[2], U[1], U[0]);
-    Up = ld_interp<X>(b, sigma, P, U[5], U[4], U[3], U[2], U[1], U[0]);
+    Up = ld_interp<X>(b, U, sigma, P, U[5], U[4], U[3], U[2], U[1], U[0]);
 }
 
 // ----------------------------------------------------------------------------
