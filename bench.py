@@ -328,6 +328,7 @@ def c5_level_and_adjoint(args, flow, base=128, reps=3):
     for p, Q in enumerate(states):
         lv.bind(p, Q)
         lv.set_periodic(p, [2, 2, 2])
+    tuned = lv.autotune(dt)   # substep 0 reads the bound state and writes the level's own output
     stream = torch.cuda.current_stream()
     e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
     lv.substep(0, dt)
@@ -392,6 +393,7 @@ def c5_level_and_adjoint(args, flow, base=128, reps=3):
             "batched_substep_ms": t_batched, "batched_cell_updates_per_s": cells / (t_batched * 1e-3),
             "per_patch_substep_ms": t_patch, "per_patch_cell_updates_per_s": cells / (t_patch * 1e-3),
             "batched_over_per_patch": t_patch / t_batched,
+            "launch_shape": {"threads": tuned[0], "blocks_per_sm": tuned[1]},
             "adjoint_substep_ms": t_adj, "adjoint_over_batched_forward": t_adj / t_batched,
             "grad_amplitudes_norm": float(grad.norm())}
 

@@ -5,7 +5,12 @@
 // operation order (the X = true forms of hmr_physics.cuh), so that every
 // discrete choice -- bounds check and first-order fallback, shock sensor,
 // HLLC side, WCNS6-LD tau switch, min/max branches -- is the one the forward
-// substep takes, and then propagates adjoints along that branch.
+// substep takes, and then propagates adjoints along that branch.  The one
+// exception is the WCNS weighting of faces the HLLC (not HLLC-HLL) flux takes:
+// it is recomputed in the regrouped form (X = false), within rounding of the
+// reference's, from the reference's own smoothness indicators, so the WCNS
+// decisions are the forward's and the Riemann decisions differ only where a
+// reconstructed state sits within rounding of a threshold.
 // Conventions at non-smooth points (shared with the CPU tangent of the oracle):
 //   |x|        : sign(x), 0 at x = 0
 //   fmin(a, b) : adjoint to a if a < b, else to b
@@ -28,6 +33,21 @@ __device__ __forceinline__ double ipow0(double b, int e) {
     double r = 1.0;
     for (int i = 0; i < e; i++) r *= b;
     return r;
+}
+
+// Reciprocals 1/e_k of three or four positive values from one division,
+// 1/e_k = (prod_{j!=k} e_j)/(prod_j e_j): the reverse sides take them for the
+// derivative values only (e_k = beta_k + eps in [1e-15, 1e77) keeps the products in range).
+__device__ __forceinline__ void recip3(double e0, double e1, double e2, double* r) {
+    const double e12 = e1*e2;
+    const double rp = double(1)/(e0*e12);
+    r[0] = rp*e12; r[1] = rp*(e0*e2); r[2] = rp*(e0*e1);
+}
+
+__device__ __forceinline__ void recip4(double e0, double e1, double e2, double e3, double* r) {
+    const double e01 = e0*e1, e23 = e2*e3;
+    const double rp = double(1)/(e01*e23);
+    r[0] = rp*(e1*e23); r[1] = rp*(e0*e23); r[2] = rp*(e01*e3); r[3] = rp*(e01*e2);
 }
 
 // ----------------------------------------------------------------------------
@@ -76,7 +96,9 @@ __device__ __forceinline__ void ld_beta3_bwd(const double* S, double bb3, double
 __device__ __forceinline__ void js_side_bwd(int p, const double* S, double b0, double b1, double b2, double obar,
                                             double* Sb) {
     // alpha_k = d_k/(b_k + eps)^p, w_k = alpha_k/sum alpha (reciprocals: derivative values only)
-    const double r0 = double(1)/(b0 + HMR_EPS), r1 = double(1)/(b1 + HMR_EPS), r2 = double(1)/(b2 + HMR_EPS);
+    double rr[3];
+    recip3(b0 + HMR_EPS, b1 + HMR_EPS, b2 + HMR_EPS, rr);
+    const double r0 = rr[0], r1 = rr[1], r2 = rr[2];
     const double a0 = (double(1)/double(16))*ipow0(r0, p);
     const double a1 = (double(5)/double(8))*ipow0(r1, p);
     const double a2 = (double(5)/double(16))*ipow0(r2, p);
@@ -98,13 +120,14 @@ __device__ __forceinline__ void js_side_bwd(int p, const double* S, double b0, d
     js_betas_bwd(S, bb0, bb1, bb2, Sb);
 }
 
-// Forward of both sides (the operations of js_pair<true>) keeping the smoothness
+// Forward of both sides (the operations of js_pair<X>) keeping the smoothness
 // indicators: b[0..2] of the minus side, b[3..5] of the plus side.
+template <bool X>
 __device__ __forceinline__ void js_pair_keep(const double* U, int p, double& Um, double& Up, double* b) {
     js_betas_x(U[0], U[1], U[2], U[3], U[4], b[0], b[1], b[2]);
-    Um = js_interp<true>(b[0], b[1], b[2], p, U[0], U[1], U[2], U[3], U[4]);
+    Um = js_interp<X>(b[0], b[1], b[2], p, U[0], U[1], U[2], U[3], U[4]);
     js_betas_x(U[5], U[4], U[3], U[2], U[1], b[3], b[4], b[5]);
-    Up = js_interp<true>(b[3], b[4], b[5], p, U[5], U[4], U[3], U[2], U[1]);
+    Up = js_interp<X>(b[3], b[4], b[5], p, U[5], U[4], U[3], U[2], U[1]);
 }
 
 // Both sides of one characteristic variable: U[0..5] at cells face-3..face+2,
@@ -152,18 +175,16 @@ __device__ __forceinline__ void ld_sigma_bwd(const double* U, double sigb, doubl
 // One side: S[0..5] from the upwind side.  Accumulates Sb and the adjoint of sigma.
 __device__ __forceinline__ void ld_side_bwd(const Params& P, double sigma, const double* S, const double* b,
                                             double obar, double* Sb, double& sigb) {
-    // decision inputs, exactly as in ld_interp<true>
+    // decision inputs, exactly as in ld_interp
     const double tau_5 = fabs(sub_(b[0], b[2]));
     const double beta_avg = mul_(double(1)/double(8), add_(add_(b[0], b[2]), mul_(double(6), b[1])));
     const double tau_6 = fabs(sub_(b[3], beta_avg));
-    const double R_tau = tau_6/add_(beta_avg, HMR_EPS);
-    const bool blend = R_tau > P.alpha_tau;
+    const bool blend = ld_switch(tau_6, beta_avg, P.alpha_tau);
     // weights, with reciprocals (derivative values only)
     const double du[3] = {1.0/16.0, 5.0/8.0, 5.0/16.0};
     const double dc[4] = {1.0/32.0, 15.0/32.0, 15.0/32.0, 1.0/32.0};
     double r[4], xu[3] = {0, 0, 0}, xo[4], pu1[3] = {0, 0, 0}, po1[4], ur[3] = {0, 0, 0}, orw[4];
-#pragma unroll
-    for (int k = 0; k < 4; k++) r[k] = double(1)/(b[k] + HMR_EPS);
+    recip4(b[0] + HMR_EPS, b[1] + HMR_EPS, b[2] + HMR_EPS, b[3] + HMR_EPS, r);
     double Us = 1.0, Os = 0.0;
     if (blend) {   // the upwind weights only enter where the switch blends
         Us = 0.0;
@@ -255,18 +276,19 @@ __device__ __forceinline__ void ld_side_bwd(const Params& P, double sigma, const
     ld_beta3_bwd(S, bb[3], Sb);
 }
 
-// Forward of both sides (the operations of ld_pair<true>) keeping the smoothness
-// indicators b[0..3] (minus side), b[4..7] (plus side) and sigma (b[8]).
+// Forward of both sides (the operations of ld_pair<X>) keeping the smoothness
+// indicators b[0..3] (minus side), b[4..7] (plus side) and sigma (b[8]; negative
+// where neither side blends, since sigma then enters nothing).
+template <bool X>
 __device__ __forceinline__ void ld_pair_keep(const double* U, const Params& P, double& Um, double& Up, double* b) {
-    const double sigma = ld_sigma(U);
+    double sg = -1.0;
     js_betas_x(U[0], U[1], U[2], U[3], U[4], b[0], b[1], b[2]);
     b[3] = ld_beta3(U[0], U[1], U[2], U[3], U[4], U[5]);
-    double sg = sigma;
-    Um = ld_interp<true>(b, U, sg, P, U[0], U[1], U[2], U[3], U[4], U[5]);
+    Um = ld_interp<X>(b, U, sg, P, U[0], U[1], U[2], U[3], U[4], U[5]);
     js_betas_x(U[5], U[4], U[3], U[2], U[1], b[4], b[5], b[6]);
     b[7] = ld_beta3(U[5], U[4], U[3], U[2], U[1], U[0]);
-    Up = ld_interp<true>(b + 4, U, sg, P, U[5], U[4], U[3], U[2], U[1], U[0]);
-    b[8] = sigma;
+    Up = ld_interp<X>(b + 4, U, sg, P, U[5], U[4], U[3], U[2], U[1], U[0]);
+    b[8] = sg;
 }
 
 __device__ __forceinline__ void ld_pair_bwd(const double* U, const double* b, const Params& P, double Umb,
@@ -282,7 +304,7 @@ __device__ __forceinline__ void ld_pair_bwd(const double* U, const double* b, co
     ld_side_bwd(P, sigma, R, b + 4, Upb, Rb, sigb);
 #pragma unroll
     for (int j = 0; j < 6; j++) Ub[5 - j] += Rb[j];
-    ld_sigma_bwd(U, sigb, Ub);
+    if (sigma >= 0.0) ld_sigma_bwd(U, sigb, Ub);
 }
 
 // ----------------------------------------------------------------------------
@@ -293,9 +315,9 @@ __device__ __forceinline__ void z_side_bwd(int p, const double* S, const double*
     const double du[3] = {1.0/16.0, 5.0/8.0, 5.0/16.0};
     const double tau_5 = fabs(sub_(b[0], b[2]));
     double r[3], x[3], px1[3], ur[3], Us = 0.0;
+    recip3(b[0] + HMR_EPS, b[1] + HMR_EPS, b[2] + HMR_EPS, r);
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-        r[k] = double(1)/(b[k] + HMR_EPS);
         x[k] = tau_5*r[k];
         px1[k] = ipow0(x[k], p - 1);
         ur[k] = du[k]*(1.0 + px1[k]*x[k]);
@@ -326,13 +348,14 @@ __device__ __forceinline__ void z_side_bwd(int p, const double* S, const double*
     js_betas_bwd(S, bb[0], bb[1], bb[2], Sb);
 }
 
-// Forward of both sides (the operations of z_pair<true>) keeping the indicators:
+// Forward of both sides (the operations of z_pair<X>) keeping the indicators:
 // b[0..2] minus side, b[3..5] plus side.
+template <bool X>
 __device__ __forceinline__ void z_pair_keep(const double* U, int p, double& Um, double& Up, double* b) {
     js_betas_x(U[0], U[1], U[2], U[3], U[4], b[0], b[1], b[2]);
-    Um = z_interp<true>(b[0], b[1], b[2], p, U[0], U[1], U[2], U[3], U[4]);
+    Um = z_interp<X>(b[0], b[1], b[2], p, U[0], U[1], U[2], U[3], U[4]);
     js_betas_x(U[5], U[4], U[3], U[2], U[1], b[3], b[4], b[5]);
-    Up = z_interp<true>(b[3], b[4], b[5], p, U[5], U[4], U[3], U[2], U[1]);
+    Up = z_interp<X>(b[3], b[4], b[5], p, U[5], U[4], U[3], U[2], U[1]);
 }
 
 __device__ __forceinline__ void z_pair_bwd(const double* U, const double* b, int p, double Umb, double Upb,
@@ -361,10 +384,10 @@ __device__ __forceinline__ void cu_side_bwd(const Params& P, double ce, double c
     const double tau_6 = fabs(sub_(b[3], beta_avg));
     const double ax = beta_avg + cx;
     double ek[4], xk[4], g[4], py1[4], orw[4], Os = 0.0;
+    recip4(b[0] + ce, b[1] + ce, b[2] + ce, b[3] + ce, ek);
+    recip4(b[0] + cx, b[1] + cx, b[2] + cx, b[3] + cx, xk);
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-        ek[k] = double(1)/(b[k] + ce);
-        xk[k] = double(1)/(b[k] + cx);
         g[k] = tau_6*ax*ek[k]*xk[k];
         const double y = P.C + g[k];
         py1[k] = ipow0(y, P.q - 1);
@@ -405,16 +428,16 @@ __device__ __forceinline__ void cu_side_bwd(const Params& P, double ce, double c
     ld_beta3_bwd(S, bb[3], Sb);
 }
 
-// Forward of both sides (the operations of cu_pair<true, A>) keeping the
+// Forward of both sides (the operations of cu_pair<X, A>) keeping the
 // indicators: b[0..3] minus side, b[4..7] plus side.
-template <int A>
+template <bool X, int A>
 __device__ __forceinline__ void cu_pair_keep(const double* U, const Params& P, double& Um, double& Up, double* b) {
     js_betas_x(U[0], U[1], U[2], U[3], U[4], b[0], b[1], b[2]);
     b[3] = ld_beta3(U[0], U[1], U[2], U[3], U[4], U[5]);
-    Um = cu_interp<true>(b, P, P.cu_e[A], P.cu_x[A], U[0], U[1], U[2], U[3], U[4], U[5]);
+    Um = cu_interp<X>(b, P, P.cu_e[A], P.cu_x[A], U[0], U[1], U[2], U[3], U[4], U[5]);
     js_betas_x(U[5], U[4], U[3], U[2], U[1], b[4], b[5], b[6]);
     b[7] = ld_beta3(U[5], U[4], U[3], U[2], U[1], U[0]);
-    Up = cu_interp<true>(b + 4, P, P.cu_e[A], P.cu_x[A], U[5], U[4], U[3], U[2], U[1], U[0]);
+    Up = cu_interp<X>(b + 4, P, P.cu_e[A], P.cu_x[A], U[5], U[4], U[3], U[2], U[1], U[0]);
 }
 
 template <int A>

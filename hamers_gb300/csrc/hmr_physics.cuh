@@ -293,6 +293,13 @@ __device__ __forceinline__ void char_from_prim(const FaceProj<DIM, MODEL, NSP>& 
 // ----------------------------------------------------------------------------
 template <bool X>
 __device__ __forceinline__ double ipow_(double b, int e) {
+    if constexpr (!X) {   // the reconstructors' default exponents, by squaring
+        if (e == 2) return b*b;
+        if (e == 4) {
+            const double b2 = b*b;
+            return b2*b2;
+        }
+    }
     double r = b;
     for (int i = 1; i < e; i++) r = X ? mul_(r, b) : r*b;
     return r;
@@ -464,6 +471,22 @@ __device__ __forceinline__ double ld_beta3(double S0, double S1, double S2, doub
     return mul_(double(1)/double(232243200), add_(add_(add_(add_(add_(t0, t1), t2), t3), t4), t5));
 }
 
+// WCNS6-LD's tau switch, R_tau = tau_6/(beta_avg + eps) > alpha_tau, decided without
+// the division where the product m = alpha_tau (beta_avg + eps) is far from tau_6.  With
+// u = 2^-53: tau_6 > m (1 + 1e-14) puts the exact quotient above alpha_tau (1 + 4u), so its
+// rounding exceeds alpha_tau; tau_6 < m (1 - 1e-14) puts it below alpha_tau, so its rounding
+// does not exceed it.  Between the two, for NaN, and outside the normal range the quotient
+// is formed as the reference forms it.  The decision is the reference's bit for bit.
+__device__ __forceinline__ bool ld_switch(double tau_6, double beta_avg, double alpha) {
+    const double d = add_(beta_avg, HMR_EPS);
+    const double m = mul_(alpha, d);
+    if (alpha > 1.0e-280 && m > 1.0e-280 && m < 1.0e280) {
+        if (tau_6 > mul_(m, 1.0 + 1.0e-14)) return true;
+        if (tau_6 < mul_(m, 1.0 - 1.0e-14)) return false;
+    }
+    return tau_6/d > alpha;
+}
+
 // WCNS6-LD weights and midpoint value (WCNS6-LD-HLLC-HLL.cpp:158-222), stencil S0..S5 from
 // the upwind side; b[0..3] are that side's smoothness indicators.
 template <bool X>
@@ -471,12 +494,12 @@ template <bool X>
 // it only enters where the switch blends).
 __device__ __forceinline__ double ld_interp(const double* b, const double* U, double& sigma, const Params& P,
                                             double S0, double S1, double S2, double S3, double S4, double S5) {
-    // Decision inputs are always exact: tau_5, tau_6, beta_avg, R_tau.
+    // Decision inputs are always exact (tau_5, tau_6, beta_avg), and the tau switch is the
+    // reference's decision in both forms.
     const double tau_5 = fabs(sub_(b[0], b[2]));
     const double beta_avg = mul_(double(1)/double(8), add_(add_(b[0], b[2]), mul_(double(6), b[1])));
     const double tau_6 = fabs(sub_(b[3], beta_avg));
-    const double R_tau = tau_6/add_(beta_avg, HMR_EPS);
-    const bool blend = R_tau > P.alpha_tau;
+    const bool blend = X ? tau_6/add_(beta_avg, HMR_EPS) > P.alpha_tau : ld_switch(tau_6, beta_avg, P.alpha_tau);
     double u0 = 0.0, u1 = 0.0, u2 = 0.0, o0, o1, o2, o3;
     // The upwind weights u_k only enter when the switch blends (their value is not used
     // otherwise, so skipping them changes no result).

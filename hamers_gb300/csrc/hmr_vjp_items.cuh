@@ -201,8 +201,11 @@ __host__ __device__ constexpr int weno_kept() {
     return SCHEME == WCNS5_JS || SCHEME == WCNS5_Z ? 6 : (SCHEME == WCNS6_LD ? 9 : 8);
 }
 
-// Item u = e*nf + t: forward WCNS interpolation of variable e at face t (exact
-// form), keeping the reconstructed values and the smoothness indicators.
+// Item u = e*nf + t: forward WCNS interpolation of variable e at face t, keeping
+// the reconstructed values and the smoothness indicators.  The indicators and
+// every WCNS decision are the reference's bits in both forms; the weighting is the
+// exact form on HLLC-HLL faces (whose blending weight amplifies rounding) and the
+// regrouped form elsewhere.
 template <int DIM, int MODEL, int NSP, int SCHEME, int AX>
 __device__ __forceinline__ void face_fwd_weno_item(const Params& P, const Geom& g, const Scratch& S,
                                                    const VjpArgs& VA, long u) {
@@ -217,10 +220,20 @@ __device__ __forceinline__ void face_fwd_weno_item(const Params& P, const Geom& 
     double U[6], b[9], Wm, Wp;
     char_stencil<DIM, MODEL, NSP, AX>(g, S, F, xR, st, e, U);
     constexpr int NB = weno_kept<SCHEME>();
-    if constexpr (SCHEME == WCNS5_JS) js_pair_keep(U, P.p, Wm, Wp, b);
-    else if constexpr (SCHEME == WCNS6_LD) ld_pair_keep(U, P, Wm, Wp, b);
-    else if constexpr (SCHEME == WCNS5_Z) z_pair_keep(U, P.p, Wm, Wp, b);
-    else cu_pair_keep<AX>(U, P, Wm, Wp, b);
+    const long xL = xR - st;
+    const double theta_avg = 0.5*(S.theta[xL] + S.theta[xR]);
+    const double Omega_avg = 0.5*(S.Omega[xL] + S.Omega[xR]);
+    if (-theta_avg/(fabs(theta_avg) + Omega_avg + HMR_EPS) > 0.65) {
+        if constexpr (SCHEME == WCNS5_JS) js_pair_keep<true>(U, P.p, Wm, Wp, b);
+        else if constexpr (SCHEME == WCNS6_LD) ld_pair_keep<true>(U, P, Wm, Wp, b);
+        else if constexpr (SCHEME == WCNS5_Z) z_pair_keep<true>(U, P.p, Wm, Wp, b);
+        else cu_pair_keep<true, AX>(U, P, Wm, Wp, b);
+    } else {
+        if constexpr (SCHEME == WCNS5_JS) js_pair_keep<false>(U, P.p, Wm, Wp, b);
+        else if constexpr (SCHEME == WCNS6_LD) ld_pair_keep<false>(U, P, Wm, Wp, b);
+        else if constexpr (SCHEME == WCNS5_Z) z_pair_keep<false>(U, P.p, Wm, Wp, b);
+        else cu_pair_keep<false, AX>(U, P, Wm, Wp, b);
+    }
     VA.Wv[AX][(long)(2 * e) * nf + t] = Wm;
     VA.Wv[AX][(long)(2 * e + 1) * nf + t] = Wp;
 #pragma unroll
