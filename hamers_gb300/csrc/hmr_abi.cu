@@ -1068,13 +1068,13 @@ int hmr_level_autotune(hmr_level* lv, double dt, int* threads_out, int* bpsm_out
     int dev = 0, sms = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int cand_threads[3] = {64, 128, 256};
+    const int cand_threads[2] = {64, 128};   // the level kernel's launch bound is 128 threads
     float best = 1e30f;
     int best_t = lv->threads, best_b = lv->blocks;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    for (int ti = 0; ti < 3; ti++) {
+    for (int ti = 0; ti < 2; ti++) {
         const int t = cand_threads[ti];
         int maxb = 0;
         if (level_max_blocks(lv, t, &maxb) || maxb < 1) continue;

@@ -191,12 +191,20 @@ __device__ __forceinline__ int find_patch(const PatchWork* W, int np, long t, Of
     return lo;
 }
 
-constexpr int LEVEL_MAX_THREADS = 256;
+// 128 threads per block at most, with registers for three such blocks per SM (at most 170 per
+// thread) in the fast form, as the per-patch face kernels use; the exact form's face item, the
+// 3D multi-species models and the 3D NavierStokes phases need more registers and keep two
+// blocks per SM.
+constexpr int LEVEL_MAX_THREADS = 128;
+template <int DIM, int MODEL, int DORD>
+constexpr int level_min_blocks() {
+    return HMR_FAST && (DIM == 2 || (MODEL == SINGLE_SPECIES && DORD == 0)) ? 3 : 2;
+}
 
 // DORD: 0 for the Euler equations, 2 or 4 for NavierStokes with that diffusive order (single
 // species); a separate instantiation, so that the Euler kernel keeps its registers.
 template <int DIM, int MODEL, int NSP, int SCHEME, int DORD>
-__global__ void __launch_bounds__(LEVEL_MAX_THREADS, 1)
+__global__ void __launch_bounds__(LEVEL_MAX_THREADS, level_min_blocks<DIM, MODEL, DORD>())
 level_kernel(Params P, LevelArgs L) {
     const long stride = (long)gridDim.x * blockDim.x;
     const long t0 = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -330,7 +338,7 @@ level_kernel(Params P, LevelArgs L) {
         U.Fout.p[0] = nullptr;   // flux/source outputs are not produced by the batched form
         U.Sout.p[0] = nullptr;
         U.dorder = DORD;
-        update_item<DIM, MODEL, NSP>(w.g, w.S, U, t - w.off_update);
+        update_item<DIM, MODEL, NSP, true>(w.g, w.S, U, t - w.off_update);
     }
 }
 

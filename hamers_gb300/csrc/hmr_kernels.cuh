@@ -378,7 +378,10 @@ __device__ __forceinline__ void axis_terms(const Geom& g, const Scratch& S, cons
     }
 }
 
-template <int DIM, int MODEL, int NSP>
+// LOCAL: U is a per-item local copy (batched form); its stage arrays are then selected with
+// constant indices only, since a runtime index into it would put it in local memory.  A
+// kernel-parameter U (per-patch launches) is indexed directly.
+template <int DIM, int MODEL, int NSP, bool LOCAL = false>
 __device__ __forceinline__ void update_item(const Geom& g, const Scratch& S, const UpdateArgs& U, long t) {
     using M = Model<DIM, MODEL, NSP>;
     constexpr int NEQ = M::NEQ;
@@ -387,7 +390,13 @@ __device__ __forceinline__ void update_item(const Geom& g, const Scratch& S, con
     const int k = DIM == 3 ? (int)(t / ((long)g.n[0] * g.n[1])) : 0;
     const long nc = ncell_of(g);
     const long x = cidx<DIM>(g, i, j, k);
-    const Comp& Q = U.Qint[U.nst - 1];
+    Comp Qsel;
+    if constexpr (LOCAL) {
+#pragma unroll
+        for (int e = 0; e < M::NCOMP; e++)
+            Qsel.p[e] = U.nst == 1 ? U.Qint[0].p[e] : (U.nst == 2 ? U.Qint[1].p[e] : U.Qint[2].p[e]);
+    }
+    const Comp& Q = LOCAL ? Qsel : U.Qint[U.nst - 1];
 
     double fl[3][NEQ], fr[3][NEQ], us[3];
     axis_terms<DIM, MODEL, NSP, 0>(g, S, Q, U, i, j, k, x, nc, fl[0], fr[0], us[0]);
@@ -429,8 +438,14 @@ __device__ __forceinline__ void update_item(const Geom& g, const Scratch& S, con
 #pragma unroll
     for (int e = 0; e < NEQ; e++) {
         double acc = 0.0;
-        for (int n = 0; n < U.nst; n++)
-            if (U.alpha[n] != 0.0) acc += U.alpha[n]*U.Qint[n].p[e][x];
+        if constexpr (LOCAL) {
+#pragma unroll
+            for (int n = 0; n < 3; n++)
+                if (n < U.nst && U.alpha[n] != 0.0) acc += U.alpha[n]*U.Qint[n].p[e][x];
+        } else {
+            for (int n = 0; n < U.nst; n++)
+                if (U.alpha[n] != 0.0) acc += U.alpha[n]*U.Qint[n].p[e][x];
+        }
         if (U.beta != 0.0 && ns) {
             if constexpr (DIM == 2) {
                 acc += U.beta*(-(fr[0][e] - fl[0][e] + dr[0][e] - dl[0][e])/g.dx[0] -

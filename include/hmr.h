@@ -319,7 +319,7 @@ int hmr_level_check(hmr_level* level);
 /* Diagnostic: bound every barrier wait by timeout_ns and, with extra_arrivals = 1, make the
  * first barrier unreachable so that the give-up path can be tested.  Use (0, 2e9) to restore. */
 int hmr_level_barrier_diagnostic(hmr_level* level, unsigned int extra_arrivals, unsigned long long timeout_ns);
-/* Autotuner: times the persistent kernel of this level at 64/128/256 threads per block and
+/* Autotuner: times the persistent kernel of this level at 64 and 128 threads per block and
  * every resident block count per SM, keeps the fastest.  Returns the chosen shape. */
 int hmr_level_autotune(hmr_level* level, double dt, int* threads_out, int* blocks_per_sm_out, void* stream);
 

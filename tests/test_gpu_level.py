@@ -102,7 +102,7 @@ def test_autotuned_level_is_unchanged(cuda):
             lv.set_periodic(p, periodic[p])
         if tune:
             shape = lv.autotune(dt)
-            assert shape[0] in (64, 128, 256) and shape[1] >= 1
+            assert shape[0] in (64, 128) and shape[1] >= 1
             for p, Q in enumerate(states):
                 Q.copy_(torch.from_numpy(Q0[p]))
         lv.step(dt)
