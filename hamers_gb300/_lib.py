@@ -41,7 +41,7 @@ EXPORTS = [
     "hmr_num_ghosts", "hmr_ctx_reserve", "hmr_read_counters", "hmr_conv_flux_source_patch",
     "hmr_rk_stage_patch", "hmr_rk_substep_patch", "hmr_fill_ghosts_patch", "hmr_level_create",
     "hmr_level_destroy", "hmr_level_bind_state", "hmr_level_set_periodic", "hmr_level_state",
-    "hmr_level_substep", "hmr_level_step", "hmr_level_check", "hmr_level_barrier_diagnostic", "hmr_level_autotune",
+    "hmr_level_substep", "hmr_level_step", "hmr_level_check", "hmr_level_barrier_diagnostic", "hmr_level_autotune", "hmr_level_set_launch",
     "hmr_rk_substep_patch_noalloc", "hmr_rk_substep_vjp_patch", "hmr_fill_ghosts_vjp_patch",
     "hmr_spectral_radius_patch", "hmr_level_step_cfl", "hmr_level_last_dt", "hmr_level_set_layout",
     "hmr_diff_flux_patch", "hmr_rk_stage_ns_patch", "hmr_coarsen_fluxsum_patch", "hmr_sync_fluxes_patch",
@@ -135,6 +135,7 @@ def load():
     L.hmr_level_barrier_diagnostic.argtypes = [vp, ctypes.c_uint, ctypes.c_ulonglong]
     L.hmr_level_step.argtypes = [vp, ctypes.c_double, vp]
     L.hmr_level_autotune.argtypes = [vp, ctypes.c_double, ip, ip, vp]
+    L.hmr_level_set_launch.argtypes = [vp, ctypes.c_int, ctypes.c_int]
     L.hmr_rk_substep_patch_noalloc.argtypes = [cfgp, gp, ctypes.c_int, dp, ctypes.c_double, DPPP,
                                                ctypes.c_double, DPP, vp]
     L.hmr_rk_substep_vjp_patch.argtypes = [vp, gp, ctypes.c_int, dp, ctypes.c_double, DPPP, ctypes.c_double,

@@ -27,6 +27,8 @@ struct hmr_ctx {
     size_t vjp_bytes = 0;
 };
 
+constexpr int LEVEL_COUNTERS = 8;   // barrier arrivals, redo-queue length, six phase-chunk counters
+
 struct hmr_level {
     hmr_ctx* ctx;
     int npatch;
@@ -37,7 +39,7 @@ struct hmr_level {
     double* d_scratch = nullptr;
     std::vector<size_t> state_off;     // per patch, in doubles
     LevelArgs L = {};
-    unsigned int* d_barrier = nullptr;   // [0] barrier arrivals, [1] redo-queue length
+    unsigned int* d_barrier = nullptr;   // [0] barrier arrivals, [1] redo-queue length, [2..7] phase chunks
     int* d_status = nullptr;
     unsigned long long* d_redo = nullptr;
     long redo_cap = 0;
@@ -666,6 +668,7 @@ static LevelArgs stage_args(hmr_level* lv, int stage, double dt) {
     L.status = lv->d_status;
     L.redo.list = lv->d_redo;
     L.redo.count = lv->d_barrier + 1;
+    L.chunk = lv->d_barrier + 2;
     L.redo.cap = (unsigned long long)lv->redo_cap;
     return L;
 }
@@ -673,7 +676,7 @@ static LevelArgs stage_args(hmr_level* lv, int stage, double dt) {
 // Barrier reset + persistent kernel of one substep, enqueued on st.
 static int level_enqueue(hmr_level* lv, int stage, double dt, int threads, int blocks, cudaStream_t st) {
     hmr_ctx* c = lv->ctx;
-    cudaError_t e = cudaMemsetAsync(lv->d_barrier, 0, 2 * sizeof(unsigned int), st);
+    cudaError_t e = cudaMemsetAsync(lv->d_barrier, 0, LEVEL_COUNTERS * sizeof(unsigned int), st);
     if (e != cudaSuccess) return cuda_status(e);
     const LevelArgs L = stage_args(lv, stage, dt);
     if (c->precision == HMR_PRECISION_EXACT) return hmr_exact::launch_level(c->v, c->P, L, blocks, threads, st);
@@ -784,7 +787,7 @@ int hmr_level_create(hmr_ctx* c, int np, const hmr_patch_geometry* geoms, hmr_le
     if (e == cudaSuccess) e = cudaMemset(lv->d_state, 0, state_tot * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&lv->d_scratch, scratch_tot * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&lv->d_work, (size_t)3 * np * sizeof(PatchWork));
-    if (e == cudaSuccess) e = cudaMalloc(&lv->d_barrier, 2 * sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMalloc(&lv->d_barrier, LEVEL_COUNTERS * sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMalloc(&lv->d_status, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(lv->d_status, 0, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&lv->d_srmax, sizeof(unsigned long long));
@@ -992,7 +995,7 @@ static int level_capture_cfl(hmr_level* lv, double cfl) {
                                                  lv->d_srmax, cs);
         if (r == HMR_OK) r = hmr_cells::launch_stable_dt(lv->d_srmax, cfl, lv->d_dt, cs, c->P.dorder != 0);
         for (int stage = 0; stage < 3 && r == HMR_OK; stage++) {
-            r = cuda_status(cudaMemsetAsync(lv->d_barrier, 0, 2 * sizeof(unsigned int), cs));
+            r = cuda_status(cudaMemsetAsync(lv->d_barrier, 0, LEVEL_COUNTERS * sizeof(unsigned int), cs));
             if (r != HMR_OK) break;
             LevelArgs L = stage_args(lv, stage, 0.0);
             L.dt_dev = lv->d_dt;
@@ -1054,6 +1057,20 @@ int hmr_level_barrier_diagnostic(hmr_level* lv, unsigned int extra_arrivals, uns
     lv->L.barrier_extra = extra_arrivals;
     lv->L.timeout_ns = timeout_ns;
     level_drop_graphs(lv);
+    return HMR_OK;
+}
+
+int hmr_level_set_launch(hmr_level* lv, int threads, int blocks_per_sm) {
+    if (!lv || (threads != 64 && threads != 128) || blocks_per_sm < 1) return HMR_ERR_ARGUMENT;
+    int dev = 0, sms = 1, maxb = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int r = level_max_blocks(lv, threads, &maxb);
+    if (r) return r;
+    if (blocks_per_sm * sms > maxb) return HMR_ERR_ARGUMENT;   // more than can be resident
+    if (threads != lv->threads || blocks_per_sm * sms != lv->blocks) level_drop_graphs(lv);
+    lv->threads = threads;
+    lv->blocks = blocks_per_sm * sms;
     return HMR_OK;
 }
 

@@ -195,6 +195,29 @@ __device__ __forceinline__ int find_patch(const PatchWork* W, int np, long t, Of
 // thread) in the fast form, as the per-patch face kernels use; the exact form's face item, the
 // 3D multi-species models and the 3D NavierStokes phases need more registers and keep two
 // blocks per SM.
+// Items [0, total) of a phase, handed out in chunks of one block's width from a counter, in
+// order: blocks that finish early take the next chunk (the order and balancing of one block
+// per chunk launched on its own), and the chunks in flight stay within a narrow band of the
+// index space, so that neighbouring stencil rows meet in L2 (a fixed grid-stride assignment
+// lets fast and slow blocks drift apart over the phase).
+template <class F>
+__device__ __forceinline__ void level_chunks(unsigned int* counter, long total, F f) {
+    __shared__ unsigned int s_chunk;
+    const long nchunk = (total + blockDim.x - 1) / blockDim.x;
+    while (true) {
+        __syncthreads();   // every thread has read the previous chunk
+        if (threadIdx.x == 0) s_chunk = atomicAdd(counter, 1u);
+        __syncthreads();
+        const long c = s_chunk;
+        if (c >= nchunk) break;
+        const long t = c * blockDim.x + threadIdx.x;
+        if (t < total) f(t);
+    }
+}
+
+// Chunk counters of LevelArgs::chunk.
+enum { CHUNK_FACE0 = 0, CHUNK_CELLS = 3, CHUNK_SENSOR = 4, CHUNK_UPDATE = 5 };
+
 constexpr int LEVEL_MAX_THREADS = 128;
 template <int DIM, int MODEL, int DORD>
 constexpr int level_min_blocks() {
@@ -249,15 +272,15 @@ level_kernel(Params P, LevelArgs L) {
         }
     }
     HMR_BARRIER();
-    for (long t = t0; t < L.total_cells; t += stride) {
+    level_chunks(L.chunk + CHUNK_CELLS, L.total_cells, [&](long t) {
         const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_cells; });
         cells_item<DIM, MODEL, NSP>(P, W[p].g, W[p].Q[L.nst - 1], W[p].S, t - W[p].off_cells);
-    }
+    });
     HMR_BARRIER();
-    for (long t = t0; t < L.total_sensor; t += stride) {
+    level_chunks(L.chunk + CHUNK_SENSOR, L.total_sensor, [&](long t) {
         const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_sensor; });
         sensor_item<DIM, MODEL, NSP>(W[p].g, W[p].S, t - W[p].off_sensor);
-    }
+    });
     if constexpr (DORD != 0) {
         // NavierStokes: temperature and node velocity gradient (needs the cell data only)
         for (long t = t0; t < L.total_cells; t += stride) {
@@ -284,22 +307,22 @@ level_kernel(Params P, LevelArgs L) {
         }
     }
     constexpr bool X = !HMR_FAST;
-    for (long t = t0; t < L.total_face[0]; t += stride) {
+    level_chunks(L.chunk + CHUNK_FACE0, L.total_face[0], [&](long t) {
         const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_face[0]; });
         if (face_item<X, DIM, MODEL, NSP, SCHEME, 0>(P, W[p].g, W[p].S, t - W[p].off_face[0], nullptr))
             redo_push(L.redo, 0, t);
-    }
-    for (long t = t0; t < L.total_face[1]; t += stride) {
+    });
+    level_chunks(L.chunk + CHUNK_FACE0 + 1, L.total_face[1], [&](long t) {
         const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_face[1]; });
         if (face_item<X, DIM, MODEL, NSP, SCHEME, 1>(P, W[p].g, W[p].S, t - W[p].off_face[1], nullptr))
             redo_push(L.redo, 1, t);
-    }
+    });
     if constexpr (DIM == 3) {
-        for (long t = t0; t < L.total_face[2]; t += stride) {
+        level_chunks(L.chunk + CHUNK_FACE0 + 2, L.total_face[2], [&](long t) {
             const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_face[2]; });
             if (face_item<X, DIM, MODEL, NSP, SCHEME, 2>(P, W[p].g, W[p].S, t - W[p].off_face[2], nullptr))
                 redo_push(L.redo, 2, t);
-        }
+        });
     }
 #if HMR_FAST
     HMR_BARRIER();
@@ -325,7 +348,7 @@ level_kernel(Params P, LevelArgs L) {
 #endif
     HMR_BARRIER();
 #undef HMR_BARRIER
-    for (long t = t0; t < L.total_update; t += stride) {
+    level_chunks(L.chunk + CHUNK_UPDATE, L.total_update, [&](long t) {
         const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_update; });
         const PatchWork& w = W[p];
         UpdateArgs U;
@@ -339,7 +362,7 @@ level_kernel(Params P, LevelArgs L) {
         U.Sout.p[0] = nullptr;
         U.dorder = DORD;
         update_item<DIM, MODEL, NSP, true>(w.g, w.S, U, t - w.off_update);
-    }
+    });
 }
 
 // The level kernel instantiation of a variant: the diffusive order selects the NavierStokes one.

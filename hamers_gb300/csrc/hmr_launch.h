@@ -149,6 +149,7 @@ struct LevelArgs {
     unsigned long long timeout_ns;   // bound of every barrier wait
     unsigned int barrier_extra;      // diagnostic: arrivals that never come (0 in normal use)
     Redo redo;                       // faces handed from the fast to the exact form (count zeroed per launch)
+    unsigned int* chunk;             // counters of the chunks each phase has handed out (zeroed per launch)
     const double* dt_dev;            // when set, the time step is read from this device value instead of dt
     // ghost exchange between the patches of the level (hmr_level_set_layout): copies from
     // neighbours and periodic images, then zero-gradient at the domain's non-periodic faces

@@ -615,6 +615,9 @@ class BatchedLevel:
     def step(self, dt, stream=None):
         L.check("hmr_level_step", self._lib.hmr_level_step(self.level, float(dt), _stream_ptr(stream)))
 
+    def set_launch(self, threads, blocks_per_sm):
+        L.check("hmr_level_set_launch", self._lib.hmr_level_set_launch(self.level, int(threads), int(blocks_per_sm)))
+
     def autotune(self, dt, stream=None):
         t = ctypes.c_int()
         b = ctypes.c_int()

@@ -319,6 +319,9 @@ int hmr_level_check(hmr_level* level);
 /* Diagnostic: bound every barrier wait by timeout_ns and, with extra_arrivals = 1, make the
  * first barrier unreachable so that the give-up path can be tested.  Use (0, 2e9) to restore. */
 int hmr_level_barrier_diagnostic(hmr_level* level, unsigned int extra_arrivals, unsigned long long timeout_ns);
+/* Launch shape of the persistent kernel: 64 or 128 threads per block and 1..(resident
+ * maximum) blocks per SM; HMR_ERR_ARGUMENT for a shape that cannot be resident at once. */
+int hmr_level_set_launch(hmr_level* level, int threads, int blocks_per_sm);
 /* Autotuner: times the persistent kernel of this level at 64 and 128 threads per block and
  * every resident block count per SM, keeps the fastest.  Returns the chosen shape. */
 int hmr_level_autotune(hmr_level* level, double dt, int* threads_out, int* blocks_per_sm_out, void* stream);
