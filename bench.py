@@ -49,7 +49,7 @@ ALG_BYTES_PER_CELL = 8 * NEQ * (2 + 3 + 3) / 3.0
 
 
 # DRAM traffic of one level_kernel launch of the default workload, bytes (ncu capture).
-LEVEL_KERNEL_TRAFFIC_BYTES = 412389632 + 249082624
+LEVEL_KERNEL_TRAFFIC_BYTES = 413476608 + 248229120
 
 
 def parse():
@@ -747,7 +747,7 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
                      "frac": achieved_gbs / hbm,
                      # ncu dram__bytes_read.sum + dram__bytes_write.sum of one level_kernel launch
-                     # of this workload (profiles/level_kernel_dram_c2_five_eqn_ld_1024.md)
+                     # of this workload at the autotuned shape
                      "traffic": LEVEL_KERNEL_TRAFFIC_BYTES if (n == 1024 and args.form == "batched") else None,
                      "note": f"peak {peak_kind}; algorithmic {ALG_BYTES_PER_CELL:.1f} B/cell-update; traffic: ncu "
                              "DRAM bytes of one launch (scratch round trips of the persistent kernel's "
