@@ -84,6 +84,42 @@ def test_batched_level_matches_oracle(cuda, variant, precision):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["exact", "fast"])
+def test_launch_shape_leaves_results_unchanged(cuda, precision):
+    """Every resident launch shape gives the same bits (phase items are handed out in chunks
+    from counters, and each item's arithmetic does not depend on which block runs it); shapes
+    that cannot be resident are rejected before any launch."""
+    import torch
+    from hamers_gb300 import flow
+    model, dim, scheme, _, gam = VARIANTS[5]
+    rec = make(model, dim, scheme, gam, precision)
+    sizes, periodic = _patches(dim, 13)
+    dt = 1.0e-3
+    Q0 = [smooth_state(model, dim, n, seed=80 + p, species_gamma=gam) for p, n in enumerate(sizes)]
+    lv = flow.BatchedLevel(rec, [(list(n), [1.0 / v for v in n]) for n in sizes])
+    states = [torch.from_numpy(q).cuda() for q in Q0]
+    for p, Q in enumerate(states):
+        lv.bind(p, Q)
+        lv.set_periodic(p, periodic[p])
+    for bad in ((256, 1), (96, 1), (64, 0), (128, 1000)):
+        with pytest.raises(RuntimeError):
+            lv.set_launch(*bad)
+    results = []
+    for shape in ((64, 1), (128, 1), (128, 2), (64, 3)):
+        lv.set_launch(*shape)
+        for p, Q in enumerate(states):
+            Q.copy_(torch.from_numpy(Q0[p]))
+        lv.step(dt)
+        torch.cuda.synchronize()
+        lv.check()
+        results.append([Q.cpu().numpy() for Q in states])
+    lv.close()
+    for other in results[1:]:
+        for a, b in zip(results[0], other):
+            assert np.array_equal(a, b)
+
+
+@pytest.mark.gpu
 def test_autotuned_level_is_unchanged(cuda):
     """The autotuner only changes the launch shape: results stay bitwise equal (exact form)."""
     import torch
