@@ -434,6 +434,13 @@ __device__ __forceinline__ void update_item(const Geom& g, const Scratch& S, con
     // Euler::advanceSingleStepOnPatch (Euler.cpp:1188-1660): Q = 0, += alpha_n Q_n, += beta (div + S);
     // NavierStokes::advanceSingleStepOnPatch (NavierStokes.cpp:1743-1749, 2085-2092) adds the
     // diffusive fluxes to the divergence.
+    // x/dx: the reference's division in the exact form, a product with the reciprocal in the fast one.
+    double rdx[3] = {0.0, 0.0, 0.0};
+    if constexpr (HMR_FAST != 0) {
+#pragma unroll
+        for (int a = 0; a < DIM; a++) rdx[a] = double(1)/g.dx[a];
+    }
+    auto ddx = [&](double v, int a) { return HMR_FAST != 0 ? v*rdx[a] : v/g.dx[a]; };
     double qn[NEQ];
 #pragma unroll
     for (int e = 0; e < NEQ; e++) {
@@ -448,19 +455,19 @@ __device__ __forceinline__ void update_item(const Geom& g, const Scratch& S, con
         }
         if (U.beta != 0.0 && ns) {
             if constexpr (DIM == 2) {
-                acc += U.beta*(-(fr[0][e] - fl[0][e] + dr[0][e] - dl[0][e])/g.dx[0] -
-                               (fr[1][e] - fl[1][e] + dr[1][e] - dl[1][e])/g.dx[1] + (0.0 + src[e]));
+                acc += U.beta*(-ddx(fr[0][e] - fl[0][e] + dr[0][e] - dl[0][e], 0) -
+                               ddx(fr[1][e] - fl[1][e] + dr[1][e] - dl[1][e], 1) + (0.0 + src[e]));
             } else {
-                acc += U.beta*(-(fr[0][e] - fl[0][e] + dr[0][e] - dl[0][e])/g.dx[0] -
-                               (fr[1][e] - fl[1][e] + dr[1][e] - dl[1][e])/g.dx[1] -
-                               (fr[2][e] - fl[2][e] + dr[2][e] - dl[2][e])/g.dx[2] + (0.0 + src[e]));
+                acc += U.beta*(-ddx(fr[0][e] - fl[0][e] + dr[0][e] - dl[0][e], 0) -
+                               ddx(fr[1][e] - fl[1][e] + dr[1][e] - dl[1][e], 1) -
+                               ddx(fr[2][e] - fl[2][e] + dr[2][e] - dl[2][e], 2) + (0.0 + src[e]));
             }
         } else if (U.beta != 0.0) {
             if constexpr (DIM == 2) {
-                acc += U.beta*(-(fr[0][e] - fl[0][e])/g.dx[0] - (fr[1][e] - fl[1][e])/g.dx[1] + (0.0 + src[e]));
+                acc += U.beta*(-ddx(fr[0][e] - fl[0][e], 0) - ddx(fr[1][e] - fl[1][e], 1) + (0.0 + src[e]));
             } else {
-                acc += U.beta*(-(fr[0][e] - fl[0][e])/g.dx[0] - (fr[1][e] - fl[1][e])/g.dx[1] -
-                               (fr[2][e] - fl[2][e])/g.dx[2] + (0.0 + src[e]));
+                acc += U.beta*(-ddx(fr[0][e] - fl[0][e], 0) - ddx(fr[1][e] - fl[1][e], 1) -
+                               ddx(fr[2][e] - fl[2][e], 2) + (0.0 + src[e]));
             }
         }
         qn[e] = acc;
