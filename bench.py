@@ -395,6 +395,8 @@ def c5_level_and_adjoint(args, flow, base=128, reps=3):
             "batched_over_per_patch": t_patch / t_batched,
             "launch_shape": {"threads": tuned[0], "blocks_per_sm": tuned[1]},
             "adjoint_substep_ms": t_adj, "adjoint_over_batched_forward": t_adj / t_batched,
+            # the adjoint runs patch by patch: the same form's forward is the per-patch one
+            "adjoint_over_per_patch_forward": t_adj / t_patch,
             "grad_amplitudes_norm": float(grad.norm())}
 
 
