@@ -746,8 +746,8 @@ def main():
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": state_bytes,
                 "d2h_bytes_per_step": state_bytes,
                 "note": "every step copies the initial state in from pinned host memory and the result out, "
-                        "so each timed step starts from the initial condition; the device-timed loop "
-                        "advances the state, whose later steps hand more faces to the exact form"},
+                        "so each timed step starts from the initial condition, while the device-timed "
+                        "loop advances the state (the work of a step depends on the state)"},
         "gpu_launches": 3 * launches_per_substep * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
                      "frac": achieved_gbs / hbm,
