@@ -27,7 +27,7 @@ struct hmr_ctx {
     size_t vjp_bytes = 0;
 };
 
-constexpr int LEVEL_COUNTERS = 8;   // barrier arrivals, redo-queue length, six phase-chunk counters
+constexpr int LEVEL_COUNTERS = 9;   // barrier arrivals, redo-queue length, seven phase-chunk counters
 
 struct hmr_level {
     hmr_ctx* ctx;
@@ -39,7 +39,7 @@ struct hmr_level {
     double* d_scratch = nullptr;
     std::vector<size_t> state_off;     // per patch, in doubles
     LevelArgs L = {};
-    unsigned int* d_barrier = nullptr;   // [0] barrier arrivals, [1] redo-queue length, [2..7] phase chunks
+    unsigned int* d_barrier = nullptr;   // [0] barrier arrivals, [1] redo-queue length, [2..8] phase chunks
     int* d_status = nullptr;
     unsigned long long* d_redo = nullptr;
     long redo_cap = 0;

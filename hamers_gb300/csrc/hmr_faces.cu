@@ -138,8 +138,9 @@ int launch_update(const Variant& v, const Geom& g, const Scratch& S, const Updat
 // ---------------------------------------------------------------------------
 // Batched form: one persistent kernel per RK substep over every patch of a
 // level.  Phases are separated by a grid barrier; inside a phase the items of
-// all patches form one flat index space that the resident blocks stride over,
-// so small and large patches share the SMs evenly.
+// all patches form one flat index space that the resident blocks take in
+// block-wide chunks (the small ghost phases: a grid-stride loop), so small and
+// large patches share the SMs evenly.
 // ---------------------------------------------------------------------------
 
 // Grid barrier on a monotonically increasing arrival counter.  Barrier number
@@ -216,7 +217,7 @@ __device__ __forceinline__ void level_chunks(unsigned int* counter, long total, 
 }
 
 // Chunk counters of LevelArgs::chunk.
-enum { CHUNK_FACE0 = 0, CHUNK_CELLS = 3, CHUNK_SENSOR = 4, CHUNK_UPDATE = 5 };
+enum { CHUNK_FACE0 = 0, CHUNK_CELLS = 3, CHUNK_SENSOR = 4, CHUNK_UPDATE = 5, CHUNK_REDO = 6 };
 
 constexpr int LEVEL_MAX_THREADS = 128;
 template <int DIM, int MODEL, int DORD>
@@ -329,7 +330,7 @@ level_kernel(Params P, LevelArgs L) {
     {
         // Exact recomputation of the faces the fast form handed back.
         const unsigned long long nredo = min((unsigned long long)*((volatile unsigned int*)L.redo.count), L.redo.cap);
-        for (unsigned long long r = (unsigned long long)t0; r < nredo; r += (unsigned long long)stride) {
+        level_chunks(L.chunk + CHUNK_REDO, (long)nredo, [&](long r) {
             const unsigned long long v = L.redo.list[r];
             const int a = (int)(v >> 56);
             const long t = (long)(v & ((1ull << 56) - 1));
@@ -343,7 +344,7 @@ level_kernel(Params P, LevelArgs L) {
                 const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_face[2]; });
                 face_item<true, DIM, MODEL, NSP, SCHEME, 2>(P, W[p].g, W[p].S, t - W[p].off_face[2], nullptr);
             }
-        }
+        });
     }
 #endif
     HMR_BARRIER();
