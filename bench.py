@@ -588,7 +588,10 @@ def run_reference(args):
     n = args.n
     threads = os.cpu_count() or 1
     cfg = O.Config(O.MODEL_FIVE_EQN_ALLAIRE, 2, [1.4, 1.67], O.SCHEME_WCNS6_LD)
-    rows = max(threads, 32)
+    # The whole patch per substep (about 0.1 s on 16 Grace cores), so that every thread's
+    # sub-patch is tall enough for its 4-row ghost halo not to dominate; fewer rows only for
+    # runs of more than 200 steps, to keep the arm within a few minutes.
+    rows = min(n, max(16 * threads, (n * 200) // max(args.steps, 1)))
     G = 4
     sub = Q[:, :, : rows + 2 * G, :].copy()
     for _ in range(max(0, min(args.warmup, 1))):
