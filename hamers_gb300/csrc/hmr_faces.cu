@@ -192,10 +192,6 @@ __device__ __forceinline__ int find_patch(const PatchWork* W, int np, long t, Of
     return lo;
 }
 
-// 128 threads per block at most, with registers for three such blocks per SM (at most 170 per
-// thread) in the fast form, as the per-patch face kernels use; the exact form's face item, the
-// 3D multi-species models and the 3D NavierStokes phases need more registers and keep two
-// blocks per SM.
 // Items [0, total) of a phase, handed out in chunks of one block's width from a counter, in
 // order: blocks that finish early take the next chunk (the order and balancing of one block
 // per chunk launched on its own), and the chunks in flight stay within a narrow band of the
@@ -219,6 +215,10 @@ __device__ __forceinline__ void level_chunks(unsigned int* counter, long total, 
 // Chunk counters of LevelArgs::chunk.
 enum { CHUNK_FACE0 = 0, CHUNK_CELLS = 3, CHUNK_SENSOR = 4, CHUNK_UPDATE = 5, CHUNK_REDO = 6 };
 
+// 128 threads per block at most, with registers for three such blocks per SM (at most 170 per
+// thread) in the fast form, as the per-patch face kernels use; the exact form's face item, the
+// 3D multi-species models and the 3D NavierStokes phases need more registers and keep two
+// blocks per SM.
 constexpr int LEVEL_MAX_THREADS = 128;
 template <int DIM, int MODEL, int DORD>
 constexpr int level_min_blocks() {
