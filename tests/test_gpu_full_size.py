@@ -1,0 +1,139 @@
+"""The default benchmark workload at its full size: 2D five-equation Allaire, 1024 x 1024,
+WCNS6-LD + HLLC-HLL, a Mach 1.5 shock on a perturbed interface (seed 1).
+
+* one flux/source call against the oracle on the whole patch (exact form bitwise, fast form
+  within 1e-12; a flux component whose values on the whole axis are below 1e-6 of the axis's
+  largest component -- the y-fluxes of mass and energy of a state with v = 0, the x-flux of a
+  species held at volume fraction 1e-8 -- is measured against that largest component, since
+  its own values are rounding noise of the other components' scale);
+* the batched persistent kernel against the per-patch kernels over one SSPRK3 step: the same
+  bits in either arithmetic form (every face and cell is computed by the same item code);
+* conservation: with periodic ghosts on both axes, one SSPRK3 step leaves the totals of the
+  conserved components (partial densities, momentum, energy) unchanged to rounding, because
+  every face flux enters its two cells with opposite signs.
+"""
+import numpy as np
+import pytest
+
+from hamers_gb300 import problems as P
+from oracle import oracle as O
+from tests.helpers import rel_err
+
+N = 1024
+GAMMA = [1.4, 1.67]
+NCONS = 5          # Z_1 rho_1, Z_2 rho_2, rho u, rho v, E (the volume fractions are advected)
+G = 4
+
+
+@pytest.fixture(scope="module")
+def c2():
+    Q, dx, dt = P.shock_interface_2d(N=N, seed=1)
+    return np.ascontiguousarray(Q), list(dx), float(dt)
+
+
+def _axis_err(a, b):
+    """max |a-b| / max(|b|, s_e), s_e = the component's max |b|, or the axis's largest
+    component max where that is more than 1e6 times the component's own."""
+    scales = [float(np.abs(b[e]).max()) for e in range(b.shape[0])]
+    top = max(scales)
+    worst = 0.0
+    for e in range(b.shape[0]):
+        s_e = scales[e] if scales[e] >= 1e-6 * top else top
+        worst = max(worst, float((np.abs(a[e] - b[e]) / np.maximum(np.abs(b[e]), s_e)).max()))
+    return worst
+
+
+def _rec(precision):
+    from hamers_gb300 import flow
+    fm = flow.FlowModel("FIVE_EQN_ALLAIRE", 2, GAMMA)
+    return flow.ConvectiveFluxReconstructor("WCNS6_LD_HLLC_HLL", fm, precision=precision)
+
+
+@pytest.mark.gpu
+def test_full_size_flux_matches_oracle(cuda, c2):
+    import torch
+    from hamers_gb300 import flow
+    Q, dx, dt = c2
+    cfg = O.Config(O.MODEL_FIVE_EQN_ALLAIRE, 2, GAMMA, O.SCHEME_WCNS6_LD)
+    Fo, So, _ = O.conv_flux_source(cfg, [N, N], dx, dt, Q)
+    for precision in ("exact", "fast"):
+        rec = _rec(precision)
+        patch = flow.Patch([N, N], dx, torch.from_numpy(Q).cuda())
+        F = rec.allocateFlux(patch)
+        S = rec.allocateSource(patch)
+        rec.computeConvectiveFluxAndSourceOnPatch(patch, F, S, dt)
+        torch.cuda.synchronize()
+        Fg = [f.cpu().numpy() for f in F]
+        Sg = S.cpu().numpy()
+        rec.close()
+        for a in range(2):
+            if precision == "exact":
+                assert np.array_equal(Fg[a], Fo[a]), f"flux axis {a}"
+            else:
+                assert _axis_err(Fg[a], Fo[a]) <= 1e-12, f"flux axis {a}"
+        if precision == "exact":
+            assert np.array_equal(Sg, So)
+        else:
+            assert rel_err(Sg[-1:], So[-1:]) <= 1e-12
+
+
+def _per_patch_step(rec, Q0, dx, dt, periodic):
+    import torch
+    from hamers_gb300 import flow
+    eu = flow.Euler(rec)
+    Qs = [torch.from_numpy(Q0).cuda(), torch.empty(Q0.shape, dtype=torch.float64, device="cuda"),
+          torch.empty(Q0.shape, dtype=torch.float64, device="cuda")]
+    views = [flow.Patch([N, N], dx, q) for q in Qs]
+    for s in range(3):
+        eu.fillGhosts(views[s], periodic)
+        eu.substep(views[s], s, Qs[:s + 1], dt, Qs[0] if s == 2 else Qs[s + 1])
+    torch.cuda.synchronize()
+    return Qs[0].cpu().numpy()
+
+
+def _batched_step(rec, Q0, dx, dt, periodic):
+    import torch
+    from hamers_gb300 import flow
+    Q = torch.from_numpy(Q0).cuda()
+    lv = flow.BatchedLevel(rec, [([N, N], dx)])
+    lv.bind(0, Q)
+    lv.set_periodic(0, periodic)
+    lv.step(dt)
+    torch.cuda.synchronize()
+    lv.check()
+    out = Q.cpu().numpy()
+    lv.close()
+    return out
+
+
+def _interior(Q):
+    return Q[:, 0, G:-G, G:-G]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["exact", "fast"])
+def test_full_size_batched_equals_per_patch(cuda, c2, precision):
+    Q, dx, dt = c2
+    rec = _rec(precision)
+    a = _per_patch_step(rec, Q, dx, dt, [0, 1])
+    b = _batched_step(rec, Q, dx, dt, [0, 1])
+    rec.close()
+    assert np.array_equal(_interior(a), _interior(b))
+
+
+@pytest.mark.gpu
+def test_full_size_periodic_step_conserves_totals(cuda, c2):
+    Q, dx, dt = c2
+    rec = _rec("fast")
+    out = _batched_step(rec, Q, dx, dt, [1, 1])
+    rec.close()
+    before, after = _interior(Q), _interior(out)
+    assert np.isfinite(after).all()
+    mom = float(np.sum(np.abs(before[2])) + np.sum(np.abs(before[3])))   # v = 0 initially
+    for e in range(NCONS):
+        t0 = np.sum(before[e], dtype=np.float64)
+        t1 = np.sum(after[e], dtype=np.float64)
+        scale = mom if e in (2, 3) else float(np.sum(np.abs(before[e])))
+        assert abs(t1 - t0) <= 1e-12 * scale, (e, t0, t1)
+    # the step did change the state (the shock and the interface moved)
+    assert not np.array_equal(before, after)
