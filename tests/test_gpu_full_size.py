@@ -1,5 +1,5 @@
-"""The default benchmark workload at its full size: 2D five-equation Allaire, 1024 x 1024,
-WCNS6-LD + HLLC-HLL, a Mach 1.5 shock on a perturbed interface (seed 1).
+"""The benchmark workloads at their full sizes.  First the default one: 2D five-equation
+Allaire, 1024 x 1024, WCNS6-LD + HLLC-HLL, a Mach 1.5 shock on a perturbed interface (seed 1):
 
 * one flux/source call against the oracle on the whole patch (exact form bitwise, fast form
   within 1e-12; a flux component whose values on the whole axis are below 1e-6 of the axis's
@@ -11,6 +11,9 @@ WCNS6-LD + HLLC-HLL, a Mach 1.5 shock on a perturbed interface (seed 1).
 * conservation: with periodic ghosts on both axes, one SSPRK3 step leaves the totals of the
   conserved components (partial densities, momentum, energy) unchanged to rounding, because
   every face flux enters its two cells with opposite signs.
+
+Then the uneven-patch workload (3D single species, 512 patches, 45 M cells): batched against
+per-patch, bit for bit.
 """
 import numpy as np
 import pytest
@@ -137,3 +140,39 @@ def test_full_size_periodic_step_conserves_totals(cuda, c2):
         assert abs(t1 - t0) <= 1e-12 * scale, (e, t0, t1)
     # the step did change the state (the shock and the interface moved)
     assert not np.array_equal(before, after)
+
+
+@pytest.mark.gpu
+def test_full_size_uneven_level_batched_equals_per_patch(cuda):
+    """The uneven-patch workload at its full size (3D single species WCNS5-JS, 512 cubic
+    patches of side 16-64 on 2 levels, 45 M cells, fast form): one SSPRK3 step of the batched
+    level gives the same bits as the per-patch kernels, patch by patch (each patch's own
+    zero-gradient ghosts in both forms)."""
+    import torch
+    from hamers_gb300 import flow
+    patches = P.blobs_patches_3d_device(num_patches=512)
+    fm = flow.FlowModel("SINGLE_SPECIES", 3, [1.4])
+    rec = flow.ConvectiveFluxReconstructor("WCNS5_JS_HLLC_HLL", fm, precision="fast")
+    dt = 0.2 * min(dx[0] for _, dx, _ in patches) / 2.5
+    Q0 = [Q.clone() for _, _, Q in patches]
+    lv = flow.BatchedLevel(rec, [(n, dx) for n, dx, _ in patches])
+    for i, (_, _, Q) in enumerate(patches):
+        lv.bind(i, Q)
+    lv.step(dt)
+    torch.cuda.synchronize()
+    lv.check()
+    lv.close()
+    batched = [Q.clone() for _, _, Q in patches]
+    eu = flow.Euler(rec)
+    for (n, dx, Q), q0 in zip(patches, Q0):
+        Q.copy_(q0)
+        Qs = [Q, torch.empty_like(Q), torch.empty_like(Q)]
+        views = [flow.Patch(n, dx, q) for q in Qs]
+        for s in range(3):
+            eu.fillGhosts(views[s], [0, 0, 0])
+            eu.substep(views[s], s, Qs[:s + 1], dt, Qs[0] if s == 2 else Qs[s + 1])
+    torch.cuda.synchronize()
+    rec.close()
+    for (n, _, Q), b in zip(patches, batched):
+        inner = (slice(None),) + tuple(slice(G, G + v) for v in (n[2], n[1], n[0]))
+        assert torch.equal(Q[inner], b[inner]), n
