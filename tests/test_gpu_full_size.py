@@ -12,8 +12,8 @@ Allaire, 1024 x 1024, WCNS6-LD + HLLC-HLL, a Mach 1.5 shock on a perturbed inter
   conserved components (partial densities, momentum, energy) unchanged to rounding, because
   every face flux enters its two cells with opposite signs.
 
-Then the uneven-patch workload (3D single species, 512 patches, 45 M cells): batched against
-per-patch, bit for bit.
+Then the uneven-patch workload (3D single species, 512 patches, 45 M cells) and the 3-level
+workload (3D five-equation, 474 patches, 35.5 M cells): batched against per-patch, bit for bit.
 """
 import numpy as np
 import pytest
@@ -176,3 +176,38 @@ def test_full_size_uneven_level_batched_equals_per_patch(cuda):
     for (n, _, Q), b in zip(patches, batched):
         inner = (slice(None),) + tuple(slice(G, G + v) for v in (n[2], n[1], n[0]))
         assert torch.equal(Q[inner], b[inner]), n
+
+
+@pytest.mark.gpu
+def test_full_size_amr_substep_batched_equals_per_patch(cuda):
+    """The 3-level workload at its full size (3D five-equation shock on a perturbed interface,
+    474 uneven patches, 35.5 M cells, WCNS6-LD, fast form, ghosts from the analytic initial
+    state): the first RK substep of the batched level (slot 1 of every patch) gives the same bits
+    as the per-patch kernels."""
+    import torch
+    from hamers_gb300 import flow
+    layout = P.amr_layout_3d(base=128, seed=4)
+    amps, waves, phases = P.shock_interface_3d_modes(64, seed=4)
+    a = torch.tensor(amps, dtype=torch.float64, device="cuda")
+    finest = min(dx[0] for _, _, _, dx in layout)
+    fm = flow.FlowModel("FIVE_EQN_ALLAIRE", 3, [1.4, 1.09])
+    rec = flow.ConvectiveFluxReconstructor("WCNS6_LD_HLLC_HLL", fm, precision="fast")
+    states = [P.shock_interface_3d_patch(lo, n, dx, a, waves, phases, finest) for _, lo, n, dx in layout]
+    dt = 0.4 * finest / (3.0 * 3.0)
+    lv = flow.BatchedLevel(rec, [(n, dx) for _, _, n, dx in layout])
+    for p, Q in enumerate(states):
+        lv.bind(p, Q)
+        lv.set_periodic(p, [2, 2, 2])
+    lv.substep(0, dt)
+    torch.cuda.synchronize()
+    lv.check()
+    eu = flow.Euler(rec)
+    out = None
+    for p, ((_, _, n, dx), Q) in enumerate(zip(layout, states)):
+        if out is None or out.shape != Q.shape:
+            out = torch.empty_like(Q)
+        eu.substep(flow.Patch(n, dx, Q), 0, [Q], dt, out)
+        inner = (slice(None),) + tuple(slice(G, G + v) for v in (n[2], n[1], n[0]))
+        assert torch.equal(out[inner], lv.state(p, 1)[inner]), (p, n)
+    lv.close()
+    rec.close()
