@@ -13,7 +13,8 @@ Allaire, 1024 x 1024, WCNS6-LD + HLLC-HLL, a Mach 1.5 shock on a perturbed inter
   every face flux enters its two cells with opposite signs.
 
 Then the uneven-patch workload (3D single species, 512 patches, 45 M cells) and the 3-level
-workload (3D five-equation, 474 patches, 35.5 M cells): batched against per-patch, bit for bit.
+workload (3D five-equation, 474 patches, 35.5 M cells): batched against per-patch, bit for bit;
+and the Navier-Stokes Taylor-Green vortex at 128^3: conservation over ten steps.
 """
 import numpy as np
 import pytest
@@ -211,3 +212,36 @@ def test_full_size_amr_substep_batched_equals_per_patch(cuda):
         assert torch.equal(out[inner], lv.state(p, 1)[inner]), (p, n)
     lv.close()
     rec.close()
+
+
+@pytest.mark.gpu
+def test_full_size_navier_stokes_step_conserves_totals(cuda):
+    """The Navier-Stokes workload at its full size (Taylor-Green vortex 128^3, periodic, Mach 0.1,
+    Re 1600, WCNS5-JS + HLLC-HLL + fourth-order midpoint diffusive flux, fast form): ten SSPRK3
+    steps keep the totals of mass, momentum and energy to rounding (convective and diffusive
+    face fluxes both enter their two cells with opposite signs), and the kinetic energy decays."""
+    import torch
+    from hamers_gb300 import flow
+    N3 = 128
+    Qnp, dx = P.taylor_green_3d(N3)
+    tr = P.taylor_green_transport()
+    dt = P.taylor_green_dt(Qnp[:, 4:-4, 4:-4, 4:-4], dx, mu=tr["species_mu"], prandtl=tr["species_Pr"])
+    fm = flow.FlowModel("SINGLE_SPECIES", 3, [1.4], transport=tr)
+    rec = flow.ConvectiveFluxReconstructor("WCNS5_JS_HLLC_HLL", fm, precision="fast",
+                                           diffusive_flux_reconstructor="MIDPOINT_FOURTH_ORDER")
+    Q = torch.from_numpy(np.ascontiguousarray(Qnp)).cuda()
+    integ = flow.RungeKuttaLevelIntegrator(flow.NavierStokes(rec), flow.Patch([N3] * 3, dx, Q), [1, 1, 1])
+    integ.advance(dt, nsteps=10)
+    torch.cuda.synchronize()
+    out = Q.cpu().numpy()
+    rec.close()
+    inner = (slice(None),) + (slice(G, -G),) * 3
+    before, after = Qnp[inner], out[inner]
+    assert np.isfinite(after).all()
+    mom = float(sum(np.sum(np.abs(before[1 + d])) for d in range(3)))
+    for e in range(5):
+        scale = mom if 1 <= e <= 3 else float(np.sum(np.abs(before[e])))
+        assert abs(np.sum(after[e]) - np.sum(before[e])) <= 1e-12 * scale, e
+    ke0 = 0.5 * np.sum((before[1] ** 2 + before[2] ** 2 + before[3] ** 2) / before[0])
+    ke1 = 0.5 * np.sum((after[1] ** 2 + after[2] ** 2 + after[3] ** 2) / after[0])
+    assert ke1 < ke0
