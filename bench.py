@@ -21,6 +21,7 @@ import argparse
 import ctypes
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -573,9 +574,18 @@ def cpu_baseline_oracle(Q, n, dx, dt, budget_s=15.0, threads=None):
         el = time.perf_counter() - t0
         total_cells += cells
         total_time += el
+    # one core, as one MPI rank of the reference advances its patch: a band of 128 rows
+    rows1 = min(128, n)
+    sub = Q[:, :, : rows1 + 2 * G, :].copy()
+    t0 = time.perf_counter()
+    cells1 = O.stage_threads(cfg, [n, rows1], dx, dt, sub, 1)
+    el1 = time.perf_counter() - t0
     return {"value": total_cells / total_time, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{best[0]} x {n} rows of the patch, one RK stage per call, "
-                      f"{threads} std::threads (one sub-patch each), {total_time:.1f} s of CPU work"}
+                      f"{threads} std::threads (one sub-patch each), {total_time:.1f} s of CPU work",
+            "host": f"{platform.machine()}, {os.cpu_count()} hardware threads",
+            "one_core": {"value": cells1 / el1, "unit": UNIT,
+                         "sample": f"{rows1} x {n} rows, one RK stage, one thread, {el1:.1f} s"}}
 
 
 def run_reference(args):
