@@ -181,6 +181,60 @@ def flux_shapes(cfg, n):
     return out
 
 
+_REF_DIR = os.path.join(_HERE, "_ref")
+_REF_LIB_PATH = os.path.join(_REF_DIR, "libhmr_ref.so")
+_REF_SRC = os.environ.get("HMR_REFERENCE_SRC", "/root/reference")
+_ref_lib = None
+
+
+def ref_available():
+    """True when the reference's own translation units are built (oracle/_ref/libhmr_ref.so)
+    or can be built here (the reference sources are present)."""
+    return os.path.exists(_REF_LIB_PATH) or os.path.isdir(os.path.join(_REF_SRC, "src"))
+
+
+def ref_lib():
+    """The reference's hot path compiled from its own sources (refshim/Makefile): the checker
+    of this oracle.  Builds it on first use when the reference sources are present."""
+    global _ref_lib
+    if _ref_lib is None:
+        if os.path.isdir(os.path.join(_REF_SRC, "src")):
+            subprocess.check_call(["make", "-s", "-j", str(os.cpu_count() or 1), "-C",
+                                   os.path.join(_HERE, "refshim"), "REF=" + _REF_SRC])
+        L = ctypes.CDLL(_REF_LIB_PATH)
+        dp = ctypes.POINTER(ctypes.c_double)
+        ip = ctypes.POINTER(ctypes.c_int)
+        L.hmrref_conv_flux_source.argtypes = [ctypes.POINTER(_Cfg), ip, dp, ctypes.c_double, dp, dp, dp]
+        L.hmrref_conv_flux_source.restype = ctypes.c_int
+        L.hmrref_last_error.restype = ctypes.c_char_p
+        _ref_lib = L
+    return _ref_lib
+
+
+def ref_conv_flux_source(cfg, n, dx, dt, Q, source=None):
+    """The reference's ConvectiveFluxReconstructorWCNS56::computeConvectiveFluxAndSourceOnPatch on
+    one patch, same arguments and results as conv_flux_source (without the face statistics)."""
+    n3 = _n3(n)
+    Q = np.ascontiguousarray(Q, dtype=np.float64)
+    assert Q.shape == ghost_shape(cfg, n)
+    shapes = flux_shapes(cfg, n)
+    flat = np.zeros(sum(int(np.prod(s)) for s in shapes))
+    if source is None:
+        source = np.zeros((cfg.neq, n3[2], n3[1], n3[0]))
+    source = np.ascontiguousarray(source, dtype=np.float64)
+    L = ref_lib()
+    rc = L.hmrref_conv_flux_source(ctypes.byref(cfg.c()), _ip(n3), _dv(list(dx) + [1.0] * (3 - len(dx))),
+                                   float(dt), _dp(Q), _dp(flat), _dp(source))
+    if rc != 0:
+        raise RuntimeError("reference: " + L.hmrref_last_error().decode())
+    out, off = [], 0
+    for s in shapes:
+        m = int(np.prod(s))
+        out.append(flat[off:off + m].reshape(s))
+        off += m
+    return out, source
+
+
 def _dp(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
 

@@ -1,15 +1,22 @@
-"""Generates the golden fixtures of the convective path from the CPU oracle.
+"""Generates the golden fixtures of the convective path.
 
-The reference ships no golden flux vectors (its tests pin only the order of
-accuracy), so these fixtures freeze the oracle's output on small seeded inputs:
-for each of the 24 variants (model x dimension x scheme: WCNS5-JS, WCNS6-LD, WCNS5-Z,
-WCNS6-CU-M2), the dt-scaled face fluxes, the source and the face counters of
-computeConvectiveFluxAndSourceOnPatch on a smooth and a shock state, and the interior
-state after one SSPRK3 step with periodic ghost fill; and for the Navier-Stokes path
-(single species, 2D/3D, second and fourth order) the diffusive face fluxes and one
-NavierStokes SSPRK3 step.  The inputs are regenerated from their seeds (tests/helpers.py).
+The reference ships no golden flux vectors (its tests pin only the order of accuracy), so these
+fixtures are made here on small seeded inputs.  For each of the 24 variants (model x dimension x
+scheme: WCNS5-JS, WCNS6-LD, WCNS5-Z, WCNS6-CU-M2):
+
+  * the dt-scaled face fluxes and the source of computeConvectiveFluxAndSourceOnPatch on a
+    smooth, a shock and a rough (fallback-heavy) state come from the REFERENCE'S OWN CODE --
+    its translation units compiled by oracle/refshim/Makefile into oracle/_ref/libhmr_ref.so;
+  * the fallback and HLLC-HLL face counters (the reference does not count them) and the interior
+    state after one SSPRK3 step with periodic ghost fill (smooth and shock states; the RK stage
+    of Euler::advanceSingleStepOnPatch is not among the compiled units) come from the oracle.
+
+For the Navier-Stokes path (single species, 2D/3D, second and fourth order) the diffusive face
+fluxes and one NavierStokes SSPRK3 step come from the oracle.  The inputs are regenerated from
+their seeds (tests/helpers.py, tests/test_ref_oracle.py).
 
     python tests/golden/make_golden.py      # rewrites tests/golden/convective_fixtures.npz
+                                            # (needs the reference sources for the fluxes)
 """
 import os
 import sys
@@ -23,7 +30,7 @@ if ROOT not in sys.path:
 
 from hamers_gb300 import problems as P  # noqa: E402
 from oracle import oracle as O  # noqa: E402
-from tests.helpers import shock_state, smooth_state  # noqa: E402
+from tests.helpers import rough_state, shock_state, smooth_state  # noqa: E402
 
 OUT = os.path.join(HERE, "convective_fixtures.npz")
 
@@ -57,25 +64,34 @@ def ns_transport(order):
     return O.Transport(t["mu"], t["c_p"], t["Pr"], mu_v=t["mu_v"], order=order)
 
 
+LABELS = ("smooth", "shock", "rough")
+
+
 def inputs(model, dim, gam, label):
     n = SIZES[dim]
-    gen = smooth_state if label == "smooth" else shock_state
+    gen = {"smooth": smooth_state, "shock": shock_state, "rough": rough_state}[label]
     return n, gen(model, dim, n, seed=7, species_gamma=gam)
 
 
-def compute():
+def compute(fluxes_from="reference"):
+    """All fixtures; the convective fluxes and sources from the reference's compiled code
+    (fluxes_from="reference") or from the oracle ("oracle")."""
     out = {}
     for model, mname, gam, R, dim, scheme, sname in cases():
-        for label in ("smooth", "shock"):
+        for label in LABELS:
             key = f"{mname}_{dim}d_{sname}_{label}"
             n, Q = inputs(model, dim, gam, label)
             dx = [1.0 / v for v in n]
             cfg = O.Config(model, dim, gam, scheme, species_R=R, grid_dx=dx)
             F, S, st = O.conv_flux_source(cfg, n, dx, DT, Q)
+            if fluxes_from == "reference":
+                F, S = O.ref_conv_flux_source(cfg, n, dx, DT, Q)
             for a, f in enumerate(F):
                 out[f"{key}_flux{a}"] = f
             out[f"{key}_source"] = S
             out[f"{key}_counters"] = np.array(st[1:], dtype=np.int64)
+            if label == "rough":
+                continue   # no time step: the rough state's sound speeds are far above this dt's CFL bound
             Qs = Q.copy()
             O.fill_ghosts(cfg, n, [1] * dim, Qs)
             O.rk3_advance(cfg, n, dx, DT, [1] * dim, 1, Qs)

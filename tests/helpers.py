@@ -68,6 +68,25 @@ def shock_state(model, dim, n, seed=0, species_gamma=None):
                                                  tuple(species_gamma or [1.4, 1.67])))
 
 
+def rough_state(model, dim, n, seed=0, species_gamma=None):
+    """Cell-by-cell random data: density and pressure log-uniform over six decades, velocity
+    U[-2, 2], mass or volume fraction U[0, 1].  Reconstructed states of many faces leave their
+    bounds, which sends those faces to the first-order fallback."""
+    rng = np.random.default_rng(seed)
+    nn = list(n) + [1] * (3 - len(n))
+    shape = tuple(nn[d] + 8 if d < dim else 1 for d in (2, 1, 0))
+    logu = lambda: np.exp(rng.uniform(np.log(1e-6), 0.0, shape))
+    rho, p = logu(), logu()
+    vel = [rng.uniform(-2.0, 2.0, shape) for _ in range(dim)]
+    if model == O.MODEL_SINGLE_SPECIES:
+        return np.ascontiguousarray(P.single_species_state(rho, vel, p, (species_gamma or [1.4])[0]))
+    frac = np.clip(rng.uniform(0.0, 1.0, shape), 1e-8, 1 - 1e-8)
+    if model == O.MODEL_FOUR_EQN_CONSERVATIVE:
+        return np.ascontiguousarray(P.four_eqn_state([rho * frac, rho * (1.0 - frac)], vel, p,
+                                                     species_gamma or P.FOUR_EQN_GAMMA, P.FOUR_EQN_R))
+    return np.ascontiguousarray(P.five_eqn_state(frac, rho, 3.0, vel, p, tuple(species_gamma or [1.4, 1.67])))
+
+
 def rel_err(a, b):
     """max |a-b| / max(|b|, component scale), component scale = max |b| of that component."""
     a = np.asarray(a, dtype=np.float64)

@@ -1,0 +1,102 @@
+"""The oracle restatement against the reference's own code.
+
+oracle/refshim/Makefile compiles the reference's hot-path translation units unmodified and in
+place -- the WCNS56 driver and its WCNS5-JS / WCNS6-LD / WCNS5-Z / WCNS6-CU-M2 reconstructors
+(src/flow/convective_flux_reconstructors/WCNS56/), the three flow models with their basic
+utilities and HLLC / HLLC-HLL Riemann solvers (src/flow/flow_models/), the ideal-gas equation of
+state and mixing rules (src/util/mixing_rules/), and the first-order derivative of the shock
+sensor (src/util/derivatives/) -- against a stand-in for the SAMRAI API, into
+oracle/_ref/libhmr_ref.so.  These tests run ConvectiveFluxReconstructorWCNS56::
+computeConvectiveFluxAndSourceOnPatch from that library and the oracle's restatement on the
+same inputs and require every face flux and source value to be bitwise equal.  They need the
+reference sources (or a library built from them) and skip without them.
+"""
+import numpy as np
+import pytest
+
+from hamers_gb300 import problems as P
+from oracle import oracle as O
+from tests.helpers import noisy_shock_state, rough_state, shock_state, smooth_state, vortex_state
+
+pytestmark = pytest.mark.skipif(not O.ref_available(), reason="reference sources not present")
+
+MODELS = [(O.MODEL_SINGLE_SPECIES, "single", [1.4], None),
+          (O.MODEL_FOUR_EQN_CONSERVATIVE, "four", list(P.FOUR_EQN_GAMMA), list(P.FOUR_EQN_R)),
+          (O.MODEL_FIVE_EQN_ALLAIRE, "five", [1.4, 1.67], None)]
+SCHEMES = [(O.SCHEME_WCNS5_JS, "js"), (O.SCHEME_WCNS6_LD, "ld"), (O.SCHEME_WCNS5_Z, "z"),
+           (O.SCHEME_WCNS6_CU_M2, "cu")]
+CASES = [(m, mn, g, r, d, s, sn) for (m, mn, g, r) in MODELS for d in (2, 3) for (s, sn) in SCHEMES]
+IDS = ["%s-%dd-%s" % (c[1], c[4], c[6]) for c in CASES]
+
+
+STATES = {"smooth": smooth_state, "shock": shock_state, "noisy": noisy_shock_state, "rough": rough_state}
+
+
+def run_both(model, dim, gam, R, scheme, n, Q, dt=1.3e-3):
+    dx = [1.0 / v for v in n]
+    cfg = O.Config(model, dim, gam, scheme, species_R=R, grid_dx=dx)
+    fo, so, stats = O.conv_flux_source(cfg, n, dx, dt, Q)
+    fr, sr = O.ref_conv_flux_source(cfg, n, dx, dt, Q)
+    return fo, so, fr, sr, stats
+
+
+@pytest.mark.parametrize("case", CASES, ids=IDS)
+def test_oracle_is_bitwise_the_reference(case):
+    model, _, gam, R, dim, scheme, _ = case
+    n = [13, 11] if dim == 2 else [9, 8, 7]
+    for label, gen in STATES.items():
+        Q = gen(model, dim, n, seed=3, species_gamma=gam)
+        fo, so, fr, sr, _ = run_both(model, dim, gam, R, scheme, n, Q)
+        for a in range(dim):
+            assert np.array_equal(fo[a], fr[a]), f"{label}: face flux of axis {a}"
+        assert np.array_equal(so, sr), f"{label}: source"
+
+
+def test_the_comparison_exercises_every_branch():
+    """The states above reach the first-order fallback and the HLLC-HLL faces in every model."""
+    for model, _, gam, R in MODELS:
+        seen = [0, 0]
+        for label in ("shock", "noisy", "rough"):
+            n = [13, 11]
+            Q = STATES[label](model, 2, n, seed=3, species_gamma=gam)
+            _, _, _, _, stats = run_both(model, 2, gam, R, O.SCHEME_WCNS6_LD, n, Q)
+            seen[0] += stats[1]
+            seen[1] += stats[2]
+        assert seen[0] > 0, f"model {model}: no fallback face"
+        assert seen[1] > 0, f"model {model}: no HLLC-HLL face"
+
+
+def test_default_workload_band_is_bitwise_the_reference():
+    """The benchmark's 2D five-equation shock/interface problem (WCNS6-LD) at 96^2, whose
+    Mach 1.5 shock and tanh interface hit the fallback and HLLC-HLL faces."""
+    Q, dx, dt = P.shock_interface_2d(N=96, seed=1)
+    cfg = O.Config(O.MODEL_FIVE_EQN_ALLAIRE, 2, [1.4, 1.67], O.SCHEME_WCNS6_LD)
+    fo, so, stats = O.conv_flux_source(cfg, [96, 96], dx, dt, Q)
+    fr, sr = O.ref_conv_flux_source(cfg, [96, 96], dx, dt, Q)
+    assert stats[1] > 0 and stats[2] > 0
+    for a in range(2):
+        assert np.array_equal(fo[a], fr[a])
+    assert np.array_equal(so, sr)
+
+
+def test_source_is_accumulated_like_the_reference():
+    """The source argument is added to (Euler.cpp zeroes it before the call), in both."""
+    model, gam = O.MODEL_FIVE_EQN_ALLAIRE, [1.4, 1.67]
+    n = [10, 9]
+    dx = [0.1, 1.0 / 9]
+    Q = smooth_state(model, 2, n, seed=4, species_gamma=gam)
+    cfg = O.Config(model, 2, gam, O.SCHEME_WCNS5_JS)
+    s0 = np.random.default_rng(1).standard_normal((cfg.neq, 1, 9, 10))
+    _, so, _ = O.conv_flux_source(cfg, n, dx, 1e-3, Q, source=s0.copy())
+    _, sr = O.ref_conv_flux_source(cfg, n, dx, 1e-3, Q, source=s0.copy())
+    assert np.array_equal(so, sr) and not np.array_equal(so, s0)
+
+
+def test_vortex_state_is_bitwise_the_reference():
+    """The smooth periodic state of the finite-difference checks."""
+    for model, _, gam, R in MODELS:
+        for dim in (2, 3):
+            n = [12, 10] if dim == 2 else [8, 6, 6]
+            Q = vortex_state(model, dim, n, seed=2, species_gamma=gam)
+            fo, so, fr, sr, _ = run_both(model, dim, gam, R, O.SCHEME_WCNS6_LD, n, Q)
+            assert all(np.array_equal(a, b) for a, b in zip(fo, fr)) and np.array_equal(so, sr)
