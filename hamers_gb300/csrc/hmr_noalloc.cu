@@ -6,7 +6,8 @@
 // HMR_NOALLOC_SCRATCH_BYTES.  Every GPU that loads the library holds that
 // array until the process exits.  Host code must not use the array's name as
 // a device address: the address is obtained with cudaGetSymbolAddress once
-// per device (with that device current) and cached.
+// per device and CUDA context (with that device current) and cached.
+#include <cuda.h>            // CUcontext and the driver's function types only; libcuda is not linked
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -26,9 +27,48 @@ constexpr int kMaxDevices = 64;
 __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 std::mutex g_mu;
-void* g_addr[kMaxDevices] = {};
 
-// Device address of the scratch array on the current device (resolved once).
+// A symbol's device address belongs to the CUDA context that loaded the module, not to the
+// device: after cudaDeviceReset, or under a driver-API context of the host's own, the array
+// has another address.  Each cached address therefore carries the id of the context it was
+// resolved in (cuCtxGetId: unique for the life of the process) and is resolved again when
+// the current context's id differs.
+struct Slot {
+    void* addr = nullptr;
+    unsigned long long ctx_id = 0;
+};
+Slot g_slot[kMaxDevices];
+
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+
+// Id of the current context, or 0 when none is current or the driver cannot say.
+unsigned long long current_context_id() {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static bool looked_up = false;
+    if (!looked_up) {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<CtxGetIdFn>(f);
+        cudaGetLastError();
+        looked_up = true;
+    }
+    if (!get_current || !get_id) return 0;
+    CUcontext ctx = nullptr;
+    if (get_current(&ctx) != CUDA_SUCCESS || ctx == nullptr) return 0;
+    unsigned long long id = 0;
+    if (get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+// Device address of the scratch array in the current device's current context.
 int scratch_address(void** out) {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
@@ -38,13 +78,21 @@ int scratch_address(void** out) {
     }
     if (dev < 0 || dev >= kMaxDevices) return HMR_ERR_UNSUPPORTED;
     std::lock_guard<std::mutex> lock(g_mu);
-    if (g_addr[dev] == nullptr) {
+    Slot& s = g_slot[dev];
+    unsigned long long id = current_context_id();
+    // id 0: no context is current yet (the symbol lookup below creates the primary one) or
+    // the driver cannot name it; either way the address is resolved now, not reused.
+    if (s.addr == nullptr || id == 0 || id != s.ctx_id) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || p == nullptr) return e != cudaSuccess ? (int)e : HMR_ERR_STATE;
-        g_addr[dev] = p;
+        if (e != cudaSuccess || p == nullptr) {
+            cudaGetLastError();
+            return e != cudaSuccess ? (int)e : HMR_ERR_STATE;
+        }
+        s.addr = p;
+        s.ctx_id = current_context_id();
     }
-    *out = g_addr[dev];
+    *out = s.addr;
     return HMR_OK;
 }
 
@@ -94,16 +142,22 @@ extern "C" int hmr_rk_substep_patch_noalloc(const hmr_config* cfg, const hmr_pat
         if (cfg->flow_model == HMR_FOUR_EQN_CONSERVATIVE && !(cfg->species_R[s] > 0.0)) return HMR_ERR_ARGUMENT;
     }
 
+    // The allocating entry points' geometry bounds (at most 2^20 cells per axis, fewer than
+    // 2^40 ghost-box cells), so that no size below can overflow.
     Geom g;
+    long ghost_cells = 1;
     for (int d = 0; d < 3; d++) {
-        if (d < dim && (pg->n[d] < 1 || !(pg->dx[d] > 0.0))) return HMR_ERR_ARGUMENT;
+        if (d < dim && (pg->n[d] < 1 || pg->n[d] > (1 << 20) || !(pg->dx[d] > 0.0))) return HMR_ERR_ARGUMENT;
         g.n[d] = d < dim ? pg->n[d] : 1;
         g.G[d] = d < dim ? g.n[d] + 2 * GHOST : 1;
         g.dx[d] = d < dim ? pg->dx[d] : 1.0;
+        ghost_cells *= g.G[d];
     }
+    if (ghost_cells >= (1L << 40)) return HMR_ERR_ARGUMENT;
 
     // Scratch layout and the size check, before touching the device.
     const long nc = ncell_of(g);
+    if ((size_t)nc > kScratchBytes / sizeof(double)) return HMR_ERR_CAPACITY;
     size_t need = (size_t)(neq + 4) * nc;            // V, rho, cs, theta, Omega
     size_t nfaces = 0;
     for (int a = 0; a < dim; a++) {

@@ -108,3 +108,9 @@ def test_noalloc_rejects_a_patch_larger_than_its_scratch(cuda):
     rc = lib.hmr_rk_substep_patch_noalloc(ctypes.byref(cfg), ctypes.byref(g), 0, alpha, 1.0,
                                           ctypes.cast(outer, L.DPPP), 1.0e-3, inner, None)
     assert rc == L.HMR_ERR_CAPACITY
+    # A geometry whose sizes would overflow the scratch arithmetic is refused as an argument
+    # error, before any size is computed from it.
+    g = geometry([2**31 - 4, 16], [1.0e-9, 1.0 / 16])
+    rc = lib.hmr_rk_substep_patch_noalloc(ctypes.byref(cfg), ctypes.byref(g), 0, alpha, 1.0,
+                                          ctypes.cast(outer, L.DPPP), 1.0e-3, inner, None)
+    assert rc == L.HMR_ERR_ARGUMENT
