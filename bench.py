@@ -9,7 +9,8 @@ form (one persistent kernel per substep, each substep a captured CUDA graph).
 
   value   device-timed cell-updates/s with the state resident in HBM
   e2e     the same through the public API (hamers_gb300.flow.BatchedLevel)
-          with the state copied host->device (pinned) and back every step
+          with the state copied host->device (pinned) and back every step,
+          advancing the same trajectory as the device-timed loop
 Working set per step (~0.5 GB of state and scratch) exceeds L2 (129 MB).
 
 --impl reference times the reference algorithm on the host cores: the CPU
@@ -41,12 +42,45 @@ NEQ, NCOMP = 6, 7
 # Algorithmic FP64 operations per cell-update of this workload (add, sub, mul,
 # div, sqrt, fabs, fmin, fmax counted 1 each), counted by running the oracle
 # on an operation-counting scalar type (oracle/hmr_opcount.cpp) on this
-# problem at 128x128.
-ALG_FP64_OPS_PER_CELL = 6140.0
+# problem at its full size, 1024x1024 (oracle/opcount_workloads.py).
+ALG_FP64_OPS_PER_CELL = 6006.0
 # Algorithmic HBM bytes per cell-update: SSPRK3 stage 0 reads Q^n and writes
 # Q^(1) (2*8*neq B), stages 1 and 2 read Q^n, Q^(k) and write Q^(k+1)
 # (3*8*neq B); averaged over the three substeps.
 ALG_BYTES_PER_CELL = 8 * NEQ * (2 + 3 + 3) / 3.0
+
+
+# Algorithmic FP64 operations per cell-update of the other workloads, counted the same way
+# over every patch of each workload (oracle/opcount_workloads.py).
+ALG_FP64_OPS_C1 = 1886.4      # 2D single species WCNS5-JS, one 256^2 patch
+ALG_FP64_OPS_C3 = None        # 3D single species WCNS5-JS, 512 uneven cubic patches
+ALG_FP64_OPS_C5 = None        # 3D five-equation WCNS6-LD, 3-level layout of uneven patches
+
+
+def alg_bytes(neq, stages=(0, 1, 2)):
+    """Algorithmic HBM bytes per cell-update, averaged over the given SSPRK3 stages: stage 0
+    reads Q^n and writes Q^(1); stages 1 and 2 read two states and write one."""
+    return sum(8 * neq * (2 if s == 0 else 3) for s in stages) / len(stages)
+
+
+def bench_config(n):
+    """The workload both arms time (identical in the GPU and the reference arm's lines)."""
+    return {"workload": WORKLOAD, "cells": n * n, "substeps_per_step": 3,
+            "l2": "working set per step ~0.5 GB > 129 MB L2 (no flush)", "parallelism": "replicas"}
+
+
+def roofline_fracs(cell_updates_per_s, ops_per_cell, bytes_per_cell, fp64_peak, hbm_peak):
+    """FP64 (algorithmic ops against the measured DFMA peak) and HBM (algorithmic bytes against
+    the measured copy bandwidth) fractions of a cell-update rate."""
+    out = {}
+    if ops_per_cell:
+        tf = ops_per_cell * cell_updates_per_s / 1e12
+        out["fp64"] = {"achieved": tf, "peak": fp64_peak, "unit": "TFLOP/s", "ops_per_cell_update": ops_per_cell,
+                       "frac": tf / fp64_peak if fp64_peak else None}
+    gbs = bytes_per_cell * cell_updates_per_s / 1e9
+    out["hbm"] = {"achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "bytes_per_cell_update": bytes_per_cell,
+                  "frac": gbs / hbm_peak}
+    return out
 
 
 # DRAM traffic of one level_kernel launch of the default workload, bytes (ncu capture).
@@ -73,8 +107,10 @@ def parse():
                          "--warmup steps and print its line (used for the C4 launch list)")
     ap.add_argument("--c4", action="store_true",
                     help="also time the 3D Navier-Stokes Taylor-Green workload and its adjoint (128^3, ~1 min)")
-    ap.add_argument("--c5", action="store_true",
-                    help="also run the 3-level 3D five-equation batched substep + amplitude adjoint")
+    ap.add_argument("--no-c5", action="store_true",
+                    help="skip the 3-level 3D five-equation batched substep + amplitude adjoint")
+    ap.add_argument("--no-c1", action="store_true",
+                    help="skip the 2D single-species 256^2 per-patch workload")
     ap.add_argument("--uneven-patches", type=int, default=512)
     return ap.parse_args()
 
@@ -239,7 +275,11 @@ def uneven_batched_vs_patch(args, flow):
             "per_patch_cell_updates_per_s": cu / (t_patch * 1e-3),
             "batched_over_per_patch": t_patch / t_batched,
             "batched_ms_per_step": t_batched, "per_patch_ms_per_step": t_patch,
-            "launch_shape": {"threads": tuned[0], "blocks_per_sm": tuned[1]}}
+            "launch_shape": {"threads": tuned[0], "blocks_per_sm": tuned[1]},
+            "batched_roofline": roofline_fracs(cu / (t_batched * 1e-3), ALG_FP64_OPS_C3, alg_bytes(5),
+                                               args.fp64_peak, args.hbm_peak),
+            "per_patch_roofline": roofline_fracs(cu / (t_patch * 1e-3), ALG_FP64_OPS_C3, alg_bytes(5),
+                                                 args.fp64_peak, args.hbm_peak)}
 
 
 def adjoint_cost(args, flow, Qnp, n, dx, dt, reps=3):
@@ -395,6 +435,10 @@ def c5_level_and_adjoint(args, flow, base=128, reps=3):
             "per_patch_substep_ms": t_patch, "per_patch_cell_updates_per_s": cells / (t_patch * 1e-3),
             "batched_over_per_patch": t_patch / t_batched,
             "launch_shape": {"threads": tuned[0], "blocks_per_sm": tuned[1]},
+            "batched_roofline": roofline_fracs(cells / (t_batched * 1e-3), ALG_FP64_OPS_C5, alg_bytes(7, (0,)),
+                                               args.fp64_peak, args.hbm_peak),
+            "per_patch_roofline": roofline_fracs(cells / (t_patch * 1e-3), ALG_FP64_OPS_C5, alg_bytes(7, (0,)),
+                                                 args.fp64_peak, args.hbm_peak),
             "adjoint_substep_ms": t_adj, "adjoint_over_batched_forward": t_adj / t_batched,
             # the adjoint runs patch by patch: the same form's forward is the per-patch one
             "adjoint_over_per_patch_forward": t_adj / t_patch,
@@ -541,6 +585,37 @@ def c4_forward_only(args, flow, N=128):
             "cell_updates_per_s": N ** 3 * 3 * args.steps / (ms * 1e-3)}
 
 
+def c1_per_patch(args, flow, N=256, steps=20):
+    """2D single species density wave (gamma 1.4, rho = 1 + 0.2 sin(2 pi (x + y)), u = v = 1,
+    p = 1, periodic), one 256^2 patch, WCNS5-JS + HLLC-HLL, SSPRK3 at CFL 0.4: the per-patch
+    drop-in form (periodic ghost fill + fused substep per stage), device-timed over `steps`
+    steps after 3 warm-up steps."""
+    import torch
+    from hamers_gb300 import problems as P
+    Qnp, dx, dt = P.density_wave_2d(N)
+    fm = flow.FlowModel("SINGLE_SPECIES", 2, [1.4])
+    rec = flow.ConvectiveFluxReconstructor("WCNS5_JS_HLLC_HLL", fm, precision=args.precision)
+    drv = PatchDriver(flow, rec, N, dx, torch.from_numpy(Qnp).cuda(), [1, 1])
+    for _ in range(3):
+        drv.step(dt)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    e[0].record(stream)
+    for _ in range(steps):
+        drv.step(dt)
+    e[1].record(stream)
+    torch.cuda.synchronize()
+    ms = e[0].elapsed_time(e[1]) / steps
+    rec.close()
+    rate = N * N * 3 / (ms * 1e-3)
+    return {"workload": "2D single species density wave 256x256, WCNS5-JS + HLLC-HLL, periodic, SSPRK3 at CFL 0.4",
+            "form": "per-patch (ghost fill + fused substep per stage)", "precision": args.precision,
+            "cells": N * N, "steps": steps, "ms_per_step": ms, "cell_updates_per_s": rate,
+            "roofline": roofline_fracs(rate, ALG_FP64_OPS_C1, alg_bytes(4), args.fp64_peak, args.hbm_peak),
+            "l2": "working set 2.4 MB fits in L2: HBM fraction is an upper bound on DRAM use"}
+
+
 def cpu_baseline_oracle(Q, n, dx, dt, budget_s=15.0, threads=None):
     """Oracle stage throughput on the host cores on a bounded sample (rows of the patch)."""
     from oracle import oracle as O
@@ -616,11 +691,10 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": WORKLOAD + f" (sample: {rows} rows x {n})",
-                                            "cells": n * rows, "substeps_per_step": 3},
+            "data": "synthetic", "config": bench_config(n),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{rows} x {n} rows of the {n}x{n} patch per substep, "
-                                       f"{threads} std::threads (one sub-patch each)"},
+                             "sample": f"{rows} x {n} rows of the {n}x{n} patch per substep "
+                                       f"({n * rows} cells), {threads} std::threads (one sub-patch each)"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -667,6 +741,9 @@ def main():
     from hamers_gb300 import build as B
     B.build()
     from hamers_gb300 import flow
+    peaks, peak_kind = measured_peaks()
+    args.hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    args.fp64_peak = None if args.no_peak else fp64_peak_tflops()
     if args.c4_only:
         if rank == 0:
             print(json.dumps({"c4_forward": c4_forward_only(args, flow)}), flush=True)
@@ -713,54 +790,58 @@ def main():
         torch.cuda.synchronize()
         t_host = time.perf_counter() - t_host0
     lv.check()
+    Q_device_loop = Q.clone()
     step_ms = [ev[k][0].elapsed_time(ev[k][3]) for k in range(args.steps)]
     sub_ms = [ev[k][s].elapsed_time(ev[k][s + 1]) for k in range(args.steps) for s in range(3)]
     total_ms = ev[0][0].elapsed_time(ev[-1][3])
     cells_per_step = n * n * 3
     total_ms, value = replica_throughput(total_ms, cells_per_step, args.steps, world, "cuda")
 
-    # End-to-end through the public API: pinned host state in, step, state out.
-    host_in = Q0.cpu().pin_memory()
-    host_out = torch.empty_like(host_in).pin_memory()
+    # End-to-end through the public API: every step copies the host state in (pinned), advances
+    # it and copies the result out, and the next step starts from that result, so the timed
+    # steps follow the device-timed loop's trajectory from the same initial state.
+    host = [Q0.cpu().pin_memory(), torch.empty_like(Q0, device="cpu").pin_memory()]
     for _ in range(2):
-        Q.copy_(host_in, non_blocking=True)
+        Q.copy_(host[0], non_blocking=True)
         lv.step(dt)
-        host_out.copy_(Q, non_blocking=True)
+        host[1].copy_(Q, non_blocking=True)
     torch.cuda.synchronize()
+    host[0].copy_(Q0.cpu())
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for _ in range(args.steps):
-        Q.copy_(host_in, non_blocking=True)
+    for k in range(args.steps):
+        src, dst = host[k % 2], host[(k + 1) % 2]
+        Q.copy_(src, non_blocking=True)
         lv.step(dt)
-        host_out.copy_(Q, non_blocking=True)
+        dst.copy_(Q, non_blocking=True)
     e1.record(stream)
     torch.cuda.synchronize()
     lv.check()
     e2e_ms = e0.elapsed_time(e1)
+    e2e_same = bool(torch.equal(host[args.steps % 2], Q_device_loop.cpu()))
     e2e_value = world * cells_per_step * args.steps / (e2e_ms * 1e-3)
     state_bytes = Q.numel() * 8
 
-    peaks, peak_kind = measured_peaks()
-    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    hbm = args.hbm_peak
     avg_sub_ms = sum(sub_ms) / len(sub_ms)
     achieved_gbs = ALG_BYTES_PER_CELL * n * n / (avg_sub_ms * 1e-3) / 1e9
-    fp64 = None if args.no_peak else fp64_peak_tflops()
+    fp64 = args.fp64_peak
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "cells": n * n, "substeps_per_step": 3,
-                   "form": ("batched persistent kernel, one CUDA graph per substep" if args.form == "batched"
-                            else "per-patch kernels (fill, cells, sensor, faces x/y, update) per substep"),
-                   "precision": args.precision,
-                   "launch_shape": {"threads": tuned[0], "blocks_per_sm": tuned[1]},
-                   "l2": "working set per step ~0.5 GB > 129 MB L2 (no flush)", "parallelism": "replicas"},
+        "config": bench_config(n),
+        "form": {"form": ("batched persistent kernel, one CUDA graph per substep" if args.form == "batched"
+                          else "per-patch kernels (fill, cells, sensor, faces x/y, update) per substep"),
+                 "precision": args.precision,
+                 "launch_shape": {"threads": tuned[0], "blocks_per_sm": tuned[1]}},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": state_bytes,
                 "d2h_bytes_per_step": state_bytes,
-                "note": "every step copies the initial state in from pinned host memory and the result out, "
-                        "so each timed step starts from the initial condition, while the device-timed "
-                        "loop advances the state (the work of a step depends on the state)"},
+                "note": "every step copies the host state in from pinned memory, advances it and copies the "
+                        "result out; the next step starts from that result, so the steps follow the "
+                        "device-timed loop's trajectory from the same initial state",
+                "same_final_state_as_device_loop": e2e_same},
         "gpu_launches": 3 * launches_per_substep * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
                      "frac": achieved_gbs / hbm,
@@ -790,7 +871,12 @@ def main():
             line["c4"] = c4_navier_stokes(args, flow)
         except Exception as exc:  # report, never lose the headline line
             line["c4"] = {"error": str(exc)[:300]}
-    if args.c5:
+    if not args.no_c1:
+        try:
+            line["c1"] = c1_per_patch(args, flow)
+        except Exception as exc:  # report, never lose the headline line
+            line["c1"] = {"error": str(exc)[:300]}
+    if not args.no_c5:
         try:
             line["c5"] = c5_level_and_adjoint(args, flow)
         except Exception as exc:  # report, never lose the headline line

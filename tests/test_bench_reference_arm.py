@@ -28,3 +28,7 @@ def test_reference_arm_prints_the_contract_line():
     assert d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert d["config"]["cells"] == 64 * 64   # the whole patch per substep
+    # the reference arm's config is the GPU arm's, key for key
+    sys.path.insert(0, ROOT)
+    import bench
+    assert d["config"] == bench.bench_config(64)
