@@ -53,8 +53,8 @@ ALG_BYTES_PER_CELL = 8 * NEQ * (2 + 3 + 3) / 3.0
 # Algorithmic FP64 operations per cell-update of the other workloads, counted the same way
 # over every patch of each workload (oracle/opcount_workloads.py).
 ALG_FP64_OPS_C1 = 1886.4      # 2D single species WCNS5-JS, one 256^2 patch
-ALG_FP64_OPS_C3 = None        # 3D single species WCNS5-JS, 512 uneven cubic patches
-ALG_FP64_OPS_C5 = None        # 3D five-equation WCNS6-LD, 3-level layout of uneven patches
+ALG_FP64_OPS_C3 = 3583.1      # 3D single species WCNS5-JS, 512 uneven cubic patches
+ALG_FP64_OPS_C5 = 11061.9     # 3D five-equation WCNS6-LD, 3-level layout of 474 uneven patches
 
 
 def alg_bytes(neq, stages=(0, 1, 2)):
