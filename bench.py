@@ -112,6 +112,10 @@ def parse():
     ap.add_argument("--no-c1", action="store_true",
                     help="skip the 2D single-species 256^2 per-patch workload")
     ap.add_argument("--uneven-patches", type=int, default=512)
+    ap.add_argument("--per-patch-busy", action="store_true",
+                    help="also record the per-patch form's kernel-busy share of one uneven-patch step")
+    ap.add_argument("--uneven-only", action="store_true",
+                    help="run only the uneven-patch batched-vs-per-patch measurement and print it")
     return ap.parse_args()
 
 
@@ -267,6 +271,7 @@ def uneven_batched_vs_patch(args, flow):
     e[1].record(stream)
     torch.cuda.synchronize()
     t_patch = e[0].elapsed_time(e[1]) / reps
+    busy = per_patch_busy_share(step_patches) if args.per_patch_busy else None
     rec.close()
     cu = 3 * cells
     return {"workload": f"3D single species WCNS5-JS + HLLC-HLL, {len(patches)} uneven cubic patches "
@@ -276,10 +281,40 @@ def uneven_batched_vs_patch(args, flow):
             "batched_over_per_patch": t_patch / t_batched,
             "batched_ms_per_step": t_batched, "per_patch_ms_per_step": t_patch,
             "launch_shape": {"threads": tuned[0], "blocks_per_sm": tuned[1]},
+            "per_patch_busy": busy,
             "batched_roofline": roofline_fracs(cu / (t_batched * 1e-3), ALG_FP64_OPS_C3, alg_bytes(5),
                                                args.fp64_peak, args.hbm_peak),
             "per_patch_roofline": roofline_fracs(cu / (t_patch * 1e-3), ALG_FP64_OPS_C3, alg_bytes(5),
                                                  args.fp64_peak, args.hbm_peak)}
+
+
+def per_patch_busy_share(step):
+    """How much of one per-patch step's span the GPU spends in kernels: the step runs once
+    under torch.profiler (CUDA activity records, no kernel replay), and the union of the kernel
+    intervals is compared with the span from the first kernel's start to the last one's end."""
+    import torch
+    from torch.profiler import ProfilerActivity, profile
+    torch.cuda.synchronize()
+    with profile(activities=[ProfilerActivity.CUDA]) as prof:
+        step()
+        torch.cuda.synchronize()
+    spans = sorted((ev.time_range.start, ev.time_range.end) for ev in prof.events()
+                   if ev.device_type == torch.autograd.DeviceType.CUDA and ev.time_range.end > ev.time_range.start)
+    if not spans:
+        return None
+    busy, cur_s, cur_e = 0.0, spans[0][0], spans[0][1]
+    for a, b in spans[1:]:
+        if a > cur_e:
+            busy += cur_e - cur_s
+            cur_s, cur_e = a, b
+        else:
+            cur_e = max(cur_e, b)
+    busy += cur_e - cur_s
+    span = max(b for _, b in spans) - spans[0][0]
+    return {"launches": len(spans), "kernel_busy_ms": busy * 1e-3, "span_ms": span * 1e-3,
+            "busy_share": busy / span if span > 0 else None,
+            "note": "one per-patch step under torch.profiler (CUDA activity records): union of kernel "
+                    "intervals against the span from the first kernel start to the last kernel end"}
 
 
 def adjoint_cost(args, flow, Qnp, n, dx, dt, reps=3):
@@ -747,6 +782,10 @@ def main():
     if args.c4_only:
         if rank == 0:
             print(json.dumps({"c4_forward": c4_forward_only(args, flow)}), flush=True)
+        return
+    if args.uneven_only:
+        if rank == 0:
+            print(json.dumps({"batched_vs_per_patch": uneven_batched_vs_patch(args, flow)}), flush=True)
         return
 
     n = args.n
