@@ -298,10 +298,16 @@ def per_patch_busy_share(step):
     with profile(activities=[ProfilerActivity.CUDA]) as prof:
         step()
         torch.cuda.synchronize()
-    spans = sorted((ev.time_range.start, ev.time_range.end) for ev in prof.events()
-                   if ev.device_type == torch.autograd.DeviceType.CUDA and ev.time_range.end > ev.time_range.start)
+    # raw activity records: kernels launched through the C ABI have no torch operator, so they
+    # appear there (device type CUDA) rather than among the profiler's operator events
+    spans = []
+    for ev in prof.profiler.kineto_results.events():
+        if ev.device_type() == torch.autograd.DeviceType.CUDA and ev.duration_ns() > 0:
+            t0 = ev.start_ns() * 1e-3
+            spans.append((t0, t0 + ev.duration_ns() * 1e-3))
+    spans.sort()
     if not spans:
-        return None
+        return {"error": "no CUDA activity records"}
     busy, cur_s, cur_e = 0.0, spans[0][0], spans[0][1]
     for a, b in spans[1:]:
         if a > cur_e:

@@ -82,8 +82,10 @@ def build(force=False, verbose=False, extra=()):
             failed.append(" ".join(cmd))
     if failed:
         raise RuntimeError("nvcc failed:\n" + "\n".join(failed))
+    # measurement and self-check utilities: the FP64 peak and the integer-pipe FP64 check
     peak = [exe] + ARCH + ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
-                           os.path.join(CSRC, "hmr_peak.cu"), "-o", PEAK_LIB + ".tmp"]
+                           os.path.join(CSRC, "hmr_peak.cu"), os.path.join(CSRC, "hmr_emu_check.cu"),
+                           "-o", PEAK_LIB + ".tmp"]
     subprocess.check_call(peak)
     os.replace(PEAK_LIB + ".tmp", PEAK_LIB)
     tmp = LIB + ".tmp"

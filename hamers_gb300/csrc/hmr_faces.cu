@@ -222,7 +222,11 @@ enum { CHUNK_FACE0 = 0, CHUNK_CELLS = 3, CHUNK_SENSOR = 4, CHUNK_UPDATE = 5, CHU
 constexpr int LEVEL_MAX_THREADS = 128;
 template <int DIM, int MODEL, int DORD>
 constexpr int level_min_blocks() {
+#ifdef HMR_LEVEL_MIN_BLOCKS
+    return HMR_LEVEL_MIN_BLOCKS;
+#else
     return HMR_FAST && (DIM == 2 || (MODEL == SINGLE_SPECIES && DORD == 0)) ? 3 : 2;
+#endif
 }
 
 // DORD: 0 for the Euler equations, 2 or 4 for NavierStokes with that diffusive order (single

@@ -30,6 +30,8 @@
 
 #define HMR_EPS 1.0e-15  // HAMERS_EPSILON
 
+#include "hmr_emu64.cuh"
+
 namespace hmr {
 
 enum { SINGLE_SPECIES = 0, FOUR_EQN_CONSERVATIVE = 1, FIVE_EQN_ALLAIRE = 2 };
@@ -85,6 +87,36 @@ __device__ __forceinline__ double ipow_d(double b, int e) {
 __device__ __forceinline__ double mul_(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double add_(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double sub_(double a, double b) { return __dsub_rn(a, b); }
+
+// The same explicitly rounded operations on the native FP64 pipe or emulated on the integer
+// pipes (hmr_emu64.cuh): identical result bits, different hardware.  E is a mask: bit 0
+// emulates the multiplications, bit 1 the additions and subtractions.  An emulated
+// multiplication costs about 24 ALU and 20 IMAD warp instructions, less pipe time than the 64
+// cycles a native one holds the FP64 pipe; an emulated addition costs about 49 ALU
+// instructions, more.  The smoothness indicators -- about half of a face's FP64 operations --
+// take E per side from HMR_EMU_BETA (bits 0-1 the minus side, bits 2-3 the plus side), so that
+// the integer pipes carry part of the work the narrow FP64 pipe would otherwise serialise.
+template <int E>
+__device__ __forceinline__ double mulx(double a, double b) {
+    if constexpr ((E & 1) != 0) return emu_dmul(a, b);
+    else return __dmul_rn(a, b);
+}
+template <int E>
+__device__ __forceinline__ double addx(double a, double b) {
+    if constexpr ((E & 2) != 0) return emu_dadd(a, b);
+    else return __dadd_rn(a, b);
+}
+template <int E>
+__device__ __forceinline__ double subx(double a, double b) {
+    if constexpr ((E & 2) != 0) return emu_dsub(a, b);
+    else return __dsub_rn(a, b);
+}
+
+#ifndef HMR_EMU_BETA
+#define HMR_EMU_BETA 0
+#endif
+constexpr int EMU_BETA_M = HMR_EMU_BETA & 3;         // minus-side indicators
+constexpr int EMU_BETA_P = (HMR_EMU_BETA >> 2) & 3;  // plus-side indicators
 
 template <int NSP>
 __device__ __forceinline__ double gamma_all_x(const Params& P, const double* Z) {
@@ -369,24 +401,26 @@ __device__ __forceinline__ void prim_from_char(const FaceProj<DIM, MODEL, NSP>& 
 // upwind side (U[0..4] for the minus side, U[5..1] for the plus side), every
 // product explicitly rounded: see the note above char_from_prim.  WCNS6-LD's
 // tau-switch (R_tau > alpha_tau) is a discrete decision on these values.
+template <int E = 0>
 __device__ __forceinline__ double lin3x(double c0, double a0, double c1, double a1, double c2, double a2) {
-    return add_(sub_(mul_(c0, a0), mul_(c1, a1)), mul_(c2, a2));
+    return addx<E>(subx<E>(mulx<E>(c0, a0), mulx<E>(c1, a1)), mulx<E>(c2, a2));
 }
 
+template <int E = 0>
 __device__ __forceinline__ void js_betas_x(double S0, double S1, double S2, double S3, double S4,
                                            double& b0, double& b1, double& b2) {
     // b0 = 1/3*(S0*(4*S0 - 19*S1 + 11*S2) + S1*(25*S1 - 31*S2) + 10*S2*S2)
-    b0 = mul_(double(1)/double(3), add_(add_(mul_(S0, lin3x(4.0, S0, 19.0, S1, 11.0, S2)),
-                                            mul_(S1, sub_(mul_(25.0, S1), mul_(31.0, S2)))),
-                                       mul_(mul_(10.0, S2), S2)));
+    b0 = mulx<E>(double(1)/double(3), addx<E>(addx<E>(mulx<E>(S0, lin3x<E>(4.0, S0, 19.0, S1, 11.0, S2)),
+                                            mulx<E>(S1, subx<E>(mulx<E>(25.0, S1), mulx<E>(31.0, S2)))),
+                                       mulx<E>(mulx<E>(10.0, S2), S2)));
     // b1 = 1/3*(S1*(4*S1 - 13*S2 + 5*S3) + 13*S2*(S2 - S3) + 4*S3*S3)
-    b1 = mul_(double(1)/double(3), add_(add_(mul_(S1, lin3x(4.0, S1, 13.0, S2, 5.0, S3)),
-                                            mul_(mul_(13.0, S2), sub_(S2, S3))),
-                                       mul_(mul_(4.0, S3), S3)));
+    b1 = mulx<E>(double(1)/double(3), addx<E>(addx<E>(mulx<E>(S1, lin3x<E>(4.0, S1, 13.0, S2, 5.0, S3)),
+                                            mulx<E>(mulx<E>(13.0, S2), subx<E>(S2, S3))),
+                                       mulx<E>(mulx<E>(4.0, S3), S3)));
     // b2 = 1/3*(S2*(10*S2 - 31*S3 + 11*S4) + S3*(25*S3 - 19*S4) + 4*S4*S4)
-    b2 = mul_(double(1)/double(3), add_(add_(mul_(S2, lin3x(10.0, S2, 31.0, S3, 11.0, S4)),
-                                            mul_(S3, sub_(mul_(25.0, S3), mul_(19.0, S4)))),
-                                       mul_(mul_(4.0, S4), S4)));
+    b2 = mulx<E>(double(1)/double(3), addx<E>(addx<E>(mulx<E>(S2, lin3x<E>(10.0, S2, 31.0, S3, 11.0, S4)),
+                                            mulx<E>(S3, subx<E>(mulx<E>(25.0, S3), mulx<E>(19.0, S4)))),
+                                       mulx<E>(mulx<E>(4.0, S4), S4)));
 }
 
 // Weighted 5-point midpoint value from the stencil S0..S4 (upwind first).
@@ -429,9 +463,9 @@ __device__ __forceinline__ double js_interp(double b0, double b1, double b2, int
 template <bool X>
 __device__ __forceinline__ void js_pair(const double* U, int p, double& Um, double& Up) {
     double b0, b1, b2;
-    js_betas_x(U[0], U[1], U[2], U[3], U[4], b0, b1, b2);
+    js_betas_x<EMU_BETA_M>(U[0], U[1], U[2], U[3], U[4], b0, b1, b2);
     Um = js_interp<X>(b0, b1, b2, p, U[0], U[1], U[2], U[3], U[4]);
-    js_betas_x(U[5], U[4], U[3], U[2], U[1], b0, b1, b2);
+    js_betas_x<EMU_BETA_P>(U[5], U[4], U[3], U[2], U[1], b0, b1, b2);
     Up = js_interp<X>(b0, b1, b2, p, U[5], U[4], U[3], U[2], U[1]);
 }
 
@@ -449,26 +483,27 @@ __device__ __forceinline__ double ld_sigma(const double* U) {  // WCNS6-LD-HLLC-
 
 // beta_3 with the stencil ordered from the upwind side (S0..S5), every
 // product explicitly rounded (see js_betas_x).  WCNS6-LD-HLLC-HLL.cpp:70-83.
+template <int E = 0>
 __device__ __forceinline__ double ld_beta3(double S0, double S1, double S2, double S3, double S4, double S5) {
     // S0*(525910327*S0 - 4562164630*S1 + 7799501420*S2 - 6610694540*S3 + 2794296070*S4 - 472758974*S5)
-    const double t0 = mul_(S0, sub_(add_(sub_(add_(sub_(mul_(525910327.0, S0), mul_(4562164630.0, S1)),
-                                                  mul_(7799501420.0, S2)), mul_(6610694540.0, S3)),
-                                        mul_(2794296070.0, S4)), mul_(472758974.0, S5)));
+    const double t0 = mulx<E>(S0, subx<E>(addx<E>(subx<E>(addx<E>(subx<E>(mulx<E>(525910327.0, S0), mulx<E>(4562164630.0, S1)),
+                                                  mulx<E>(7799501420.0, S2)), mulx<E>(6610694540.0, S3)),
+                                        mulx<E>(2794296070.0, S4)), mulx<E>(472758974.0, S5)));
     // 5*S1*(2146987907*S1 - 7722406988*S2 + 6763559276*S3 - 2926461814*S4 + 503766638*S5)
-    const double t1 = mul_(mul_(5.0, S1), add_(sub_(add_(sub_(mul_(2146987907.0, S1), mul_(7722406988.0, S2)),
-                                                        mul_(6763559276.0, S3)), mul_(2926461814.0, S4)),
-                                              mul_(503766638.0, S5)));
+    const double t1 = mulx<E>(mulx<E>(5.0, S1), addx<E>(subx<E>(addx<E>(subx<E>(mulx<E>(2146987907.0, S1), mulx<E>(7722406988.0, S2)),
+                                                        mulx<E>(6763559276.0, S3)), mulx<E>(2926461814.0, S4)),
+                                              mulx<E>(503766638.0, S5)));
     // 20*S2*(1833221603*S2 - 3358664662*S3 + 1495974539*S4 - 263126407*S5)
-    const double t2 = mul_(mul_(20.0, S2), sub_(add_(sub_(mul_(1833221603.0, S2), mul_(3358664662.0, S3)),
-                                                    mul_(1495974539.0, S4)), mul_(263126407.0, S5)));
+    const double t2 = mulx<E>(mulx<E>(20.0, S2), subx<E>(addx<E>(subx<E>(mulx<E>(1833221603.0, S2), mulx<E>(3358664662.0, S3)),
+                                                    mulx<E>(1495974539.0, S4)), mulx<E>(263126407.0, S5)));
     // 20*S3*(1607794163*S3 - 1486026707*S4 + 268747951*S5)
-    const double t3 = mul_(mul_(20.0, S3), add_(sub_(mul_(1607794163.0, S3), mul_(1486026707.0, S4)),
-                                               mul_(268747951.0, S5)));
+    const double t3 = mulx<E>(mulx<E>(20.0, S3), addx<E>(subx<E>(mulx<E>(1607794163.0, S3), mulx<E>(1486026707.0, S4)),
+                                               mulx<E>(268747951.0, S5)));
     // 5*S4*(1432381427*S4 - 536951582*S5)
-    const double t4 = mul_(mul_(5.0, S4), sub_(mul_(1432381427.0, S4), mul_(536951582.0, S5)));
+    const double t4 = mulx<E>(mulx<E>(5.0, S4), subx<E>(mulx<E>(1432381427.0, S4), mulx<E>(536951582.0, S5)));
     // 263126407*S5*S5
-    const double t5 = mul_(mul_(263126407.0, S5), S5);
-    return mul_(double(1)/double(232243200), add_(add_(add_(add_(add_(t0, t1), t2), t3), t4), t5));
+    const double t5 = mulx<E>(mulx<E>(263126407.0, S5), S5);
+    return mulx<E>(double(1)/double(232243200), addx<E>(addx<E>(addx<E>(addx<E>(addx<E>(t0, t1), t2), t3), t4), t5));
 }
 
 // WCNS6-LD's tau switch, R_tau = tau_6/(beta_avg + eps) > alpha_tau, decided without
@@ -574,11 +609,11 @@ template <bool X>
 __device__ __forceinline__ void ld_pair(const double* U, const Params& P, double& Um, double& Up) {
     double sigma = -1.0;   // ld_sigma(U), computed if a side blends
     double b[4];
-    js_betas_x(U[0], U[1], U[2], U[3], U[4], b[0], b[1], b[2]);
-    b[3] = ld_beta3(U[0], U[1], U[2], U[3], U[4], U[5]);
+    js_betas_x<EMU_BETA_M>(U[0], U[1], U[2], U[3], U[4], b[0], b[1], b[2]);
+    b[3] = ld_beta3<EMU_BETA_M>(U[0], U[1], U[2], U[3], U[4], U[5]);
     Um = ld_interp<X>(b, U, sigma, P, U[0], U[1], U[2], U[3], U[4], U[5]);
-    js_betas_x(U[5], U[4], U[3], U[2], U[1], b[0], b[1], b[2]);
-    b[3] = ld_beta3(U[5], U[4], U[3], U[2], U[1], U[0]);
+    js_betas_x<EMU_BETA_P>(U[5], U[4], U[3], U[2], U[1], b[0], b[1], b[2]);
+    b[3] = ld_beta3<EMU_BETA_P>(U[5], U[4], U[3], U[2], U[1], U[0]);
     Up = ld_interp<X>(b, U, sigma, P, U[5], U[4], U[3], U[2], U[1], U[0]);
 }
 
@@ -626,9 +661,9 @@ __device__ __forceinline__ double z_interp(double b0, double b1, double b2, int 
 template <bool X>
 __device__ __forceinline__ void z_pair(const double* U, int p, double& Um, double& Up) {
     double b0, b1, b2;
-    js_betas_x(U[0], U[1], U[2], U[3], U[4], b0, b1, b2);
+    js_betas_x<EMU_BETA_M>(U[0], U[1], U[2], U[3], U[4], b0, b1, b2);
     Um = z_interp<X>(b0, b1, b2, p, U[0], U[1], U[2], U[3], U[4]);
-    js_betas_x(U[5], U[4], U[3], U[2], U[1], b0, b1, b2);
+    js_betas_x<EMU_BETA_P>(U[5], U[4], U[3], U[2], U[1], b0, b1, b2);
     Up = z_interp<X>(b0, b1, b2, p, U[5], U[4], U[3], U[2], U[1]);
 }
 
@@ -686,11 +721,11 @@ __device__ __forceinline__ double cu_interp(const double* b, const Params& P, do
 template <bool X, int A>
 __device__ __forceinline__ void cu_pair(const double* U, const Params& P, double& Um, double& Up) {
     double b[4];
-    js_betas_x(U[0], U[1], U[2], U[3], U[4], b[0], b[1], b[2]);
-    b[3] = ld_beta3(U[0], U[1], U[2], U[3], U[4], U[5]);
+    js_betas_x<EMU_BETA_M>(U[0], U[1], U[2], U[3], U[4], b[0], b[1], b[2]);
+    b[3] = ld_beta3<EMU_BETA_M>(U[0], U[1], U[2], U[3], U[4], U[5]);
     Um = cu_interp<X>(b, P, P.cu_e[A], P.cu_x[A], U[0], U[1], U[2], U[3], U[4], U[5]);
-    js_betas_x(U[5], U[4], U[3], U[2], U[1], b[0], b[1], b[2]);
-    b[3] = ld_beta3(U[5], U[4], U[3], U[2], U[1], U[0]);
+    js_betas_x<EMU_BETA_P>(U[5], U[4], U[3], U[2], U[1], b[0], b[1], b[2]);
+    b[3] = ld_beta3<EMU_BETA_P>(U[5], U[4], U[3], U[2], U[1], U[0]);
     Up = cu_interp<X>(b, P, P.cu_e[A], P.cu_x[A], U[5], U[4], U[3], U[2], U[1], U[0]);
 }
 
