@@ -69,13 +69,18 @@ def shock_state(model, dim, n, seed=0, species_gamma=None):
 
 
 def rough_state(model, dim, n, seed=0, species_gamma=None):
-    """Cell-by-cell random data: density and pressure log-uniform over six decades, velocity
-    U[-2, 2], mass or volume fraction U[0, 1].  Reconstructed states of many faces leave their
-    bounds, which sends those faces to the first-order fallback."""
+    """Cell-by-cell random data: density and pressure log-uniform over six decades (a uniform
+    significand in [1, 2) times 2^-k, k = 0..19), velocity U[-2, 2], mass or volume fraction
+    U[0, 1].  Reconstructed states of many faces leave their bounds, which sends those faces to
+    the first-order fallback.  Only exact operations build the values (no exp or log, whose
+    vectorised implementations differ between machines), so every machine makes the same bits."""
     rng = np.random.default_rng(seed)
     nn = list(n) + [1] * (3 - len(n))
     shape = tuple(nn[d] + 8 if d < dim else 1 for d in (2, 1, 0))
-    logu = lambda: np.exp(rng.uniform(np.log(1e-6), 0.0, shape))
+
+    def logu():
+        return np.ldexp(rng.uniform(1.0, 2.0, shape), -rng.integers(0, 20, shape))
+
     rho, p = logu(), logu()
     vel = [rng.uniform(-2.0, 2.0, shape) for _ in range(dim)]
     if model == O.MODEL_SINGLE_SPECIES:
