@@ -45,7 +45,8 @@ EXPORTS = [
     "hmr_rk_substep_patch_noalloc", "hmr_rk_substep_vjp_patch", "hmr_fill_ghosts_vjp_patch",
     "hmr_spectral_radius_patch", "hmr_level_step_cfl", "hmr_level_last_dt", "hmr_level_set_layout",
     "hmr_diff_flux_patch", "hmr_rk_stage_ns_patch", "hmr_coarsen_fluxsum_patch", "hmr_sync_fluxes_patch",
-    "hmr_coarsen_patch", "hmr_refine_ghosts_patch",
+    "hmr_coarsen_patch", "hmr_refine_ghosts_patch", "hmr_level_substep_vjp",
+    "hmr_level_set_vjp_budget", "hmr_level_set_work_split", "hmr_level_work_split",
 ]
 
 
@@ -141,6 +142,10 @@ def load():
     L.hmr_rk_substep_vjp_patch.argtypes = [vp, gp, ctypes.c_int, dp, ctypes.c_double, DPPP, ctypes.c_double,
                                            DPP, DPPP, vp]
     L.hmr_fill_ghosts_vjp_patch.argtypes = [vp, gp, DPP, ip, vp]
+    L.hmr_level_substep_vjp.argtypes = [vp, ctypes.c_int, ctypes.c_double, DPPP, ctypes.POINTER(DPPP), vp]
+    L.hmr_level_set_vjp_budget.argtypes = [vp, ctypes.c_ulonglong]
+    L.hmr_level_set_work_split.argtypes = [vp, ctypes.c_int, ctypes.c_int]
+    L.hmr_level_work_split.argtypes = [vp, ip, ip]
     L.hmr_spectral_radius_patch.argtypes = [vp, gp, DPP, dp, vp]
     L.hmr_level_step_cfl.argtypes = [vp, ctypes.c_double, vp]
     L.hmr_level_last_dt.argtypes = [vp, dp]
@@ -164,6 +169,15 @@ def ptr_array(ptrs):
     for i, p in enumerate(ptrs):
         arr[i] = ctypes.cast(ctypes.c_void_p(int(p)), ctypes.POINTER(ctypes.c_double))
     return ctypes.cast(arr, DPP), arr
+
+
+def ptr_array3(lists):
+    """double* const* const* const* from a list of lists of pointer lists."""
+    inner = [ptr_array2(p) for p in lists]
+    outer = (DPPP * len(inner))()
+    for i, (pp, _) in enumerate(inner):
+        outer[i] = pp
+    return ctypes.cast(outer, ctypes.POINTER(DPPP)), (outer, inner)
 
 
 def ptr_array2(lists):

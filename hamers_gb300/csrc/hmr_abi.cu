@@ -63,6 +63,11 @@ struct hmr_level {
     double* d_dt = nullptr;
     cudaGraphExec_t cfl_graph = nullptr;
     double cfl_graph_cfl = 0.0;
+    // batched substep VJP: per-face reverse buffers of one group of patches, and the records
+    double* d_vjp = nullptr;
+    size_t vjp_bytes = 0;
+    size_t vjp_budget = 0;             // 0: a quarter of the free device memory at the first call
+    VjpWork* d_vjpwork = nullptr;
 };
 
 static int cuda_status(cudaError_t e) { return e == cudaSuccess ? HMR_OK : (int)e; }
@@ -482,6 +487,8 @@ int hmr_rk_substep_vjp_patch(hmr_ctx* c, const hmr_patch_geometry* pg, int stage
         need += (size_t)(c->v.dim * c->v.dim + c->neq) * ncell_of(g);
     }
     need *= sizeof(double);
+    const size_t rec_bytes = (sizeof(VjpWork) + 255) / 256 * 256;   // the one-patch record, first
+    need += rec_bytes;
     if (need > c->vjp_bytes) {
         if (c->vjp) cudaFree(c->vjp);
         c->vjp = nullptr;
@@ -490,7 +497,8 @@ int hmr_rk_substep_vjp_patch(hmr_ctx* c, const hmr_patch_geometry* pg, int stage
         if (e != cudaSuccess) return cuda_status(e);
         c->vjp_bytes = need;
     }
-    double* p = c->vjp;
+    VjpWork* d_rec = reinterpret_cast<VjpWork*>(c->vjp);
+    double* p = reinterpret_cast<double*>(reinterpret_cast<unsigned char*>(c->vjp) + rec_bytes);
     for (int a = 0; a < 3; a++) {
         A.Cb[a] = A.Wb[a] = A.Wv[a] = A.Kb[a] = A.Fp[a] = nullptr;
         A.okf[a] = nullptr;
@@ -520,7 +528,7 @@ int hmr_rk_substep_vjp_patch(hmr_ctx* c, const hmr_patch_geometry* pg, int stage
         r = hmr_cells::launch_sensor(c->v, g, S, st);
         if (r) return r;
     }
-    return hmr_vjp::launch_vjp(c->v, c->P, g, S, A, st);
+    return hmr_vjp::launch_vjp(c->v, c->P, g, S, A, d_rec, st);
 }
 
 int hmr_sync_fluxes_patch(hmr_ctx* c, const hmr_patch_geometry* pg, double* const* Q, const double* const* flux,
@@ -817,6 +825,8 @@ int hmr_level_create(hmr_ctx* c, int np, const hmr_patch_geometry* geoms, hmr_le
     lv->L.total_update = off_update;
     lv->L.timeout_ns = 2000000000ull;
     lv->L.barrier_extra = 0;
+    lv->L.chunk_mult = 1;
+    lv->L.split_mode = 0;
     lv->threads = 128;
     int r = level_max_blocks(lv, lv->threads, &lv->blocks);
     if (r || lv->blocks < 1) {
@@ -839,6 +849,8 @@ int hmr_level_destroy(hmr_level* lv) {
     if (lv->d_srmax) cudaFree(lv->d_srmax);
     if (lv->d_copies) cudaFree(lv->d_copies);
     if (lv->d_dt) cudaFree(lv->d_dt);
+    if (lv->d_vjp) cudaFree(lv->d_vjp);
+    if (lv->d_vjpwork) cudaFree(lv->d_vjpwork);
     delete lv;
     return HMR_OK;
 }
@@ -950,6 +962,135 @@ int hmr_level_set_layout(hmr_level* lv, const int* lo, const int* domain, const 
 int hmr_level_state(hmr_level* lv, int p, int slot, double** comps_out) {
     if (!lv || p < 0 || p >= lv->npatch || slot < 0 || slot > 2 || !comps_out) return HMR_ERR_ARGUMENT;
     for (int e = 0; e < lv->ctx->ncomp; e++) comps_out[e] = lv->work[p].Q[slot].p[e];
+    return HMR_OK;
+}
+
+// Doubles of the per-face reverse buffers of one patch's substep VJP (Euler equations): per face
+// the contributions (6 neq + 2), reconstructed-value adjoints (2 neq) and values (2 neq),
+// smoothness indicators (9 neq), projection factors and their partial adjoints (9 + 4 nsp) and
+// the bounds flag (one double reserved).
+static size_t vjp_face_doubles(const hmr_ctx* c) {
+    return (size_t)(6 * c->neq + 2) + (size_t)(2 * c->neq) + (size_t)(2 * c->neq) + (size_t)(9 * c->neq) +
+           (size_t)(9 + 4 * c->v.nsp) + 1;
+}
+
+int hmr_level_set_vjp_budget(hmr_level* lv, unsigned long long bytes) {
+    if (!lv) return HMR_ERR_ARGUMENT;
+    lv->vjp_budget = (size_t)bytes;
+    return HMR_OK;
+}
+
+int hmr_level_substep_vjp(hmr_level* lv, int stage, double dt, const double* const* const* Qbar_out,
+                          double* const* const* const* Qbar_int, void* stream) {
+    if (!lv || stage < 0 || stage > 2 || !Qbar_out || !Qbar_int) return HMR_ERR_ARGUMENT;
+    hmr_ctx* c = lv->ctx;
+    if (c->P.dorder != 0) return HMR_ERR_UNSUPPORTED;
+    if (lv->bound != lv->npatch) return HMR_ERR_STATE;
+    const int np = lv->npatch;
+    const double beta = RK3_BETA[stage];
+    const size_t per_face = vjp_face_doubles(c);
+    // per-patch buffer sizes (doubles, rounded to 32 for alignment)
+    std::vector<size_t> need(np);
+    size_t largest = 0, total = 0;
+    for (int p = 0; p < np; p++) {
+        size_t n = 0;
+        for (int a = 0; a < c->v.dim; a++) n += per_face * nface_of(lv->geoms[p], a);
+        need[p] = (n + 31) / 32 * 32;
+        largest = std::max(largest, need[p]);
+        total += need[p];
+    }
+    if (lv->vjp_budget == 0) {
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+            cudaGetLastError();
+            free_b = (size_t)1 << 32;
+        }
+        lv->vjp_budget = free_b / 4;
+    }
+    const size_t cap = std::max(largest, std::min(total, lv->vjp_budget / sizeof(double)));
+    if (cap * sizeof(double) > lv->vjp_bytes) {
+        if (lv->d_vjp) cudaFree(lv->d_vjp);
+        lv->d_vjp = nullptr;
+        lv->vjp_bytes = 0;
+        cudaError_t e = cudaMalloc(&lv->d_vjp, cap * sizeof(double));
+        if (e != cudaSuccess) return cuda_status(e);
+        lv->vjp_bytes = cap * sizeof(double);
+    }
+    if (!lv->d_vjpwork) {
+        cudaError_t e = cudaMalloc(&lv->d_vjpwork, (size_t)np * sizeof(VjpWork));
+        if (e != cudaSuccess) return cuda_status(e);
+    }
+    // records: each patch's buffers at its offset inside its group's share of d_vjp, prefix
+    // offsets of its items relative to the first patch of its group
+    std::vector<VjpWork> work(np);
+    std::vector<int> group_first;
+    std::vector<std::array<long, VJP_NPH * 3>> group_totals;
+    size_t used = 0;
+    std::array<long, VJP_NPH * 3> acc{};
+    for (int p = 0; p < np; p++) {
+        if (p == 0 || used + need[p] > cap) {
+            if (p > 0) group_totals.push_back(acc);
+            group_first.push_back(p);
+            used = 0;
+            acc.fill(0);
+        }
+        VjpWork& w = work[p];
+        std::memset(&w, 0, sizeof(w));
+        const Geom& g = lv->geoms[p];
+        w.g = g;
+        w.S = lv->work[p].S;
+        VjpArgs& A = w.A;
+        A.Qs = lv->work[p].Q[stage];
+        if (!Qbar_out[p] || !load_comp(A.Qbo, Qbar_out[p], c->ncomp) || !Qbar_int[p]) return HMR_ERR_ARGUMENT;
+        for (int st = 0; st <= stage; st++)
+            if (!load_comp(A.Qbi[st], Qbar_int[p][st], c->ncomp)) return HMR_ERR_ARGUMENT;
+        for (int st = 0; st < 3; st++) A.alpha[st] = st <= stage ? RK3_ALPHA[stage][st] : 0.0;
+        A.nst = stage + 1;
+        A.beta = beta;
+        A.dt = dt;
+        double* q = lv->d_vjp + used;
+        for (int a = 0; a < c->v.dim; a++) {
+            const long nf = nface_of(g, a);
+            A.Cb[a] = q; q += (size_t)(6 * c->neq + 2) * nf;
+            A.Wb[a] = q; q += (size_t)(2 * c->neq) * nf;
+            A.Wv[a] = q; q += (size_t)(2 * c->neq) * nf;
+            A.Kb[a] = q; q += (size_t)(9 * c->neq) * nf;
+            A.Fp[a] = q; q += (size_t)(9 + 4 * c->v.nsp) * nf;
+            A.okf[a] = reinterpret_cast<unsigned char*>(q); q += nf;
+        }
+        used += need[p];
+        long items[VJP_NPH * 3];
+        vjp_item_counts(c->v, g, items);
+        for (int k = 0; k < VJP_NPH * 3; k++) {
+            w.off[k] = acc[k];
+            acc[k] += items[k];
+        }
+    }
+    group_totals.push_back(acc);
+    if (lv->dirty) {
+        int r = level_upload(lv);
+        if (r) return r;
+    }
+    cudaStream_t st = as_stream(stream);
+    if (beta != 0.0) {
+        // the forward values the reverse sweep starts from: cell data and sensor of slot `stage`
+        // (the exact-form cell unit, as the forward computes them)
+        int r = hmr_cells::launch_cells_level(c->v, c->P, lv->d_work, np, lv->L.total_cells, stage, st);
+        if (r) return r;
+        r = hmr_cells::launch_sensor_level(c->v, lv->d_work, np, lv->L.total_sensor, st);
+        if (r) return r;
+    }
+    cudaError_t e = cudaMemcpyAsync(lv->d_vjpwork, work.data(), (size_t)np * sizeof(VjpWork),
+                                    cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_status(e);
+    const size_t ng = group_first.size();
+    for (size_t k = 0; k < ng; k++) {
+        const int first = group_first[k];
+        const int count = (k + 1 < ng ? group_first[k + 1] : np) - first;
+        const int r = hmr_vjp::launch_vjp_level(c->v, c->P, lv->d_vjpwork + first, count, group_totals[k].data(),
+                                                beta != 0.0, st);
+        if (r) return r;
+    }
     return HMR_OK;
 }
 
@@ -1074,6 +1215,22 @@ int hmr_level_set_launch(hmr_level* lv, int threads, int blocks_per_sm) {
     return HMR_OK;
 }
 
+int hmr_level_set_work_split(hmr_level* lv, int chunk_blocks, int mode) {
+    if (!lv || (chunk_blocks != 1 && chunk_blocks != 2 && chunk_blocks != 4) || mode < 0 || mode > 1)
+        return HMR_ERR_ARGUMENT;
+    if (chunk_blocks != lv->L.chunk_mult || mode != lv->L.split_mode) level_drop_graphs(lv);
+    lv->L.chunk_mult = chunk_blocks;
+    lv->L.split_mode = mode;
+    return HMR_OK;
+}
+
+int hmr_level_work_split(hmr_level* lv, int* chunk_blocks, int* mode) {
+    if (!lv || !chunk_blocks || !mode) return HMR_ERR_ARGUMENT;
+    *chunk_blocks = lv->L.chunk_mult;
+    *mode = lv->L.split_mode;
+    return HMR_OK;
+}
+
 int hmr_level_autotune(hmr_level* lv, double dt, int* threads_out, int* bpsm_out, void* stream) {
     if (!lv) return HMR_ERR_ARGUMENT;
     if (lv->bound != lv->npatch) return HMR_ERR_STATE;
@@ -1086,6 +1243,10 @@ int hmr_level_autotune(hmr_level* lv, double dt, int* threads_out, int* bpsm_out
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int cand_threads[2] = {64, 128};   // the level kernel's launch bound is 128 threads
+    // launch shapes first, with one-block chunks for every phase
+    const int mult0 = lv->L.chunk_mult, mode0 = lv->L.split_mode;
+    lv->L.chunk_mult = 1;
+    lv->L.split_mode = 0;
     float best = 1e30f;
     int best_t = lv->threads, best_b = lv->blocks;
     cudaEvent_t e0, e1;
@@ -1112,9 +1273,31 @@ int hmr_level_autotune(hmr_level* lv, double dt, int* threads_out, int* bpsm_out
             }
         }
     }
+    // then the work splitting at the chosen shape: chunk width (1, 2, 4 block widths) and the
+    // hand-out of the cell-wise phases (chunks or grid stride)
+    int best_m = 1, best_s = 0;
+    const int splits[4][2] = {{1, 0}, {2, 0}, {4, 0}, {1, 1}};
+    for (int k = 0; k < 4; k++) {
+        lv->L.chunk_mult = splits[k][0];
+        lv->L.split_mode = splits[k][1];
+        if (level_enqueue(lv, 0, dt, best_t, best_b, st)) continue;
+        cudaEventRecord(e0, st);
+        for (int rep = 0; rep < 2; rep++) level_enqueue(lv, 0, dt, best_t, best_b, st);
+        cudaEventRecord(e1, st);
+        if (cudaEventSynchronize(e1) != cudaSuccess) continue;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (k == 0 || ms < best) {
+            best = ms;
+            best_m = splits[k][0];
+            best_s = splits[k][1];
+        }
+    }
+    lv->L.chunk_mult = best_m;
+    lv->L.split_mode = best_s;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    if (best_t != lv->threads || best_b != lv->blocks) level_drop_graphs(lv);
+    if (best_t != lv->threads || best_b != lv->blocks || best_m != mult0 || best_s != mode0) level_drop_graphs(lv);
     lv->threads = best_t;
     lv->blocks = best_b;
     if (threads_out) *threads_out = best_t;

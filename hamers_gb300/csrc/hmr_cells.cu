@@ -273,6 +273,51 @@ int launch_spectral_level(const Variant& v, const Params& P, const PatchWork* wo
     });
 }
 
+template <int DIM, int MODEL, int NSP>
+__global__ void __launch_bounds__(THREADS)
+cells_level_kernel(Params P, const PatchWork* W, int np, long total, int slot) {
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        int lo = 0, hi = np - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (W[mid].off_cells <= t) lo = mid;
+            else hi = mid - 1;
+        }
+        cells_item<DIM, MODEL, NSP>(P, W[lo].g, W[lo].Q[slot], W[lo].S, t - W[lo].off_cells);
+    }
+}
+
+template <int DIM, int MODEL, int NSP>
+__global__ void __launch_bounds__(THREADS) sensor_level_kernel(const PatchWork* W, int np, long total) {
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        int lo = 0, hi = np - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (W[mid].off_sensor <= t) lo = mid;
+            else hi = mid - 1;
+        }
+        sensor_item<DIM, MODEL, NSP>(W[lo].g, W[lo].S, t - W[lo].off_sensor);
+    }
+}
+
+int launch_cells_level(const Variant& v, const Params& P, const PatchWork* work, int npatch, long total, int slot,
+                       cudaStream_t st) {
+    if (slot < 0 || slot > 2) return -1;
+    return dispatch(v, [&](auto t) {
+        using T = decltype(t);
+        cells_level_kernel<T::DIM, T::MODEL, T::NSP><<<grid_for(total), THREADS, 0, st>>>(P, work, npatch, total, slot);
+        return (int)cudaPeekAtLastError();
+    });
+}
+
+int launch_sensor_level(const Variant& v, const PatchWork* work, int npatch, long total, cudaStream_t st) {
+    return dispatch(v, [&](auto t) {
+        using T = decltype(t);
+        sensor_level_kernel<T::DIM, T::MODEL, T::NSP><<<grid_for(total), THREADS, 0, st>>>(work, npatch, total);
+        return (int)cudaPeekAtLastError();
+    });
+}
+
 int launch_stable_dt(const unsigned long long* d_max, double cfl, double* d_dt, cudaStream_t st, bool ns) {
     stable_dt_kernel<<<1, 1, 0, st>>>(d_max, cfl, d_dt, ns ? 1 : 0);
     return (int)cudaPeekAtLastError();

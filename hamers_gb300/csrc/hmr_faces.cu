@@ -197,18 +197,35 @@ __device__ __forceinline__ int find_patch(const PatchWork* W, int np, long t, Of
 // per chunk launched on its own), and the chunks in flight stay within a narrow band of the
 // index space, so that neighbouring stencil rows meet in L2 (a fixed grid-stride assignment
 // lets fast and slow blocks drift apart over the phase).
+// A chunk is `mult` block widths (work-splitting knob of the autotuner); a block takes its
+// items in block-wide rows.
 template <class F>
-__device__ __forceinline__ void level_chunks(unsigned int* counter, long total, F f) {
+__device__ __forceinline__ void level_chunks(unsigned int* counter, long total, int mult, F f) {
     __shared__ unsigned int s_chunk;
-    const long nchunk = (total + blockDim.x - 1) / blockDim.x;
+    const long width = (long)blockDim.x * mult;
+    const long nchunk = (total + width - 1) / width;
     while (true) {
         __syncthreads();   // every thread has read the previous chunk
         if (threadIdx.x == 0) s_chunk = atomicAdd(counter, 1u);
         __syncthreads();
         const long c = s_chunk;
         if (c >= nchunk) break;
-        const long t = c * blockDim.x + threadIdx.x;
-        if (t < total) f(t);
+        for (int r = 0; r < mult; r++) {
+            const long t = c * width + (long)r * blockDim.x + threadIdx.x;
+            if (t < total) f(t);
+        }
+    }
+}
+
+// The cell-wise phases (cell data, sensor, update), handed out in chunks or -- the other
+// work-splitting mode -- by a fixed grid-stride assignment.
+template <class F>
+__device__ __forceinline__ void level_cell_items(unsigned int* counter, long total, const LevelArgs& L, F f) {
+    if (L.split_mode == 1) {
+        const long stride = (long)gridDim.x * blockDim.x;
+        for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) f(t);
+    } else {
+        level_chunks(counter, total, L.chunk_mult, f);
     }
 }
 
@@ -277,12 +294,12 @@ level_kernel(Params P, LevelArgs L) {
         }
     }
     HMR_BARRIER();
-    level_chunks(L.chunk + CHUNK_CELLS, L.total_cells, [&](long t) {
+    level_cell_items(L.chunk + CHUNK_CELLS, L.total_cells, L, [&](long t) {
         const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_cells; });
         cells_item<DIM, MODEL, NSP>(P, W[p].g, W[p].Q[L.nst - 1], W[p].S, t - W[p].off_cells);
     });
     HMR_BARRIER();
-    level_chunks(L.chunk + CHUNK_SENSOR, L.total_sensor, [&](long t) {
+    level_cell_items(L.chunk + CHUNK_SENSOR, L.total_sensor, L, [&](long t) {
         const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_sensor; });
         sensor_item<DIM, MODEL, NSP>(W[p].g, W[p].S, t - W[p].off_sensor);
     });
@@ -312,18 +329,18 @@ level_kernel(Params P, LevelArgs L) {
         }
     }
     constexpr bool X = !HMR_FAST;
-    level_chunks(L.chunk + CHUNK_FACE0, L.total_face[0], [&](long t) {
+    level_chunks(L.chunk + CHUNK_FACE0, L.total_face[0], L.chunk_mult, [&](long t) {
         const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_face[0]; });
         if (face_item<X, DIM, MODEL, NSP, SCHEME, 0>(P, W[p].g, W[p].S, t - W[p].off_face[0], nullptr))
             redo_push(L.redo, 0, t);
     });
-    level_chunks(L.chunk + CHUNK_FACE0 + 1, L.total_face[1], [&](long t) {
+    level_chunks(L.chunk + CHUNK_FACE0 + 1, L.total_face[1], L.chunk_mult, [&](long t) {
         const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_face[1]; });
         if (face_item<X, DIM, MODEL, NSP, SCHEME, 1>(P, W[p].g, W[p].S, t - W[p].off_face[1], nullptr))
             redo_push(L.redo, 1, t);
     });
     if constexpr (DIM == 3) {
-        level_chunks(L.chunk + CHUNK_FACE0 + 2, L.total_face[2], [&](long t) {
+        level_chunks(L.chunk + CHUNK_FACE0 + 2, L.total_face[2], L.chunk_mult, [&](long t) {
             const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_face[2]; });
             if (face_item<X, DIM, MODEL, NSP, SCHEME, 2>(P, W[p].g, W[p].S, t - W[p].off_face[2], nullptr))
                 redo_push(L.redo, 2, t);
@@ -334,7 +351,7 @@ level_kernel(Params P, LevelArgs L) {
     {
         // Exact recomputation of the faces the fast form handed back.
         const unsigned long long nredo = min((unsigned long long)*((volatile unsigned int*)L.redo.count), L.redo.cap);
-        level_chunks(L.chunk + CHUNK_REDO, (long)nredo, [&](long r) {
+        level_chunks(L.chunk + CHUNK_REDO, (long)nredo, L.chunk_mult, [&](long r) {
             const unsigned long long v = L.redo.list[r];
             const int a = (int)(v >> 56);
             const long t = (long)(v & ((1ull << 56) - 1));
@@ -353,7 +370,7 @@ level_kernel(Params P, LevelArgs L) {
 #endif
     HMR_BARRIER();
 #undef HMR_BARRIER
-    level_chunks(L.chunk + CHUNK_UPDATE, L.total_update, [&](long t) {
+    level_cell_items(L.chunk + CHUNK_UPDATE, L.total_update, L, [&](long t) {
         const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_update; });
         const PatchWork& w = W[p];
         UpdateArgs U;

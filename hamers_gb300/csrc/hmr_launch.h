@@ -111,6 +111,26 @@ struct Variant {
     int dorder = 0;   // NavierStokes midpoint diffusive flux order (0: Euler)
 };
 
+inline int variant_neq(const Variant& v) {
+    if (v.model == SINGLE_SPECIES) return v.dim + 2;
+    if (v.model == FOUR_EQN_CONSERVATIVE) return v.nsp + v.dim + 1;
+    return v.dim + 2 * v.nsp;
+}
+
+// Items of each phase of one patch's substep VJP (VjpWork phases; face phases per axis).
+inline void vjp_item_counts(const Variant& v, const Geom& g, long* n) {
+    for (int k = 0; k < VJP_NPH * 3; k++) n[k] = 0;
+    const int neq = variant_neq(v);
+    for (int a = 0; a < v.dim; a++) {
+        const long nf = nface_of(g, a);
+        n[VJP_PH_PROJ * 3 + a] = n[VJP_PH_RIEM * 3 + a] = n[VJP_PH_CHAR * 3 + a] = nf;
+        n[VJP_PH_FWD * 3 + a] = n[VJP_PH_BWDW * 3 + a] = nf * neq;
+        if (v.dorder) n[VJP_PH_DMID * 3 + a] = nf;
+    }
+    if (v.dorder) n[VJP_PH_DGD * 3] = n[VJP_PH_DCELL * 3] = ncell_of(g);
+    n[VJP_PH_CELLB * 3] = ncell_of(g);
+}
+
 // One entry of the batched worklist: a patch with its stage states.
 struct PatchWork {
     Geom g;
@@ -159,6 +179,10 @@ struct LevelArgs {
     long total_copy;
     int dom[3];                      // domain extent in cells
     int dom_periodic[3];
+    // work splitting (autotuned; results do not depend on it): phase chunks of chunk_mult
+    // block widths; split_mode 1 hands the cell-wise phases out by a fixed grid stride
+    int chunk_mult;
+    int split_mode;
 };
 
 }  // namespace hmr
@@ -178,6 +202,12 @@ int launch_spectral_patch(const hmr::Variant& v, const hmr::Params& P, const hmr
                           unsigned long long* d_max, cudaStream_t st);
 int launch_spectral_level(const hmr::Variant& v, const hmr::Params& P, const hmr::PatchWork* work, int npatch,
                           long total_interior, unsigned long long* d_max, cudaStream_t st);
+// Cell data (from each patch's stage-`slot` state) and sensor of every patch of a worklist, one
+// launch each over the flat cell / sensor item spaces (PatchWork offsets).
+int launch_cells_level(const hmr::Variant& v, const hmr::Params& P, const hmr::PatchWork* work, int npatch,
+                       long total_cells, int slot, cudaStream_t st);
+int launch_sensor_level(const hmr::Variant& v, const hmr::PatchWork* work, int npatch, long total_sensor,
+                        cudaStream_t st);
 int launch_stable_dt(const unsigned long long* d_max, double cfl, double* d_dt, cudaStream_t st, bool ns = false);
 // Euler / NavierStokes advanceSingleStepOnPatch; with Fdint (ncoef diffusive flux sets) the
 // NavierStokes form, and Fdacc (optional) accumulates them with gamma.
@@ -284,15 +314,24 @@ HMR_DEFINE_FACE_ROUTER(hmr_fast)
 #define HMR_DECLARE_VJP_LAUNCHER(NS)                                                                           \
     namespace NS {                                                                                             \
     int launch_vjp(const hmr::Variant& v, const hmr::Params& P, const hmr::Geom& g, const hmr::Scratch& S,     \
-                   const hmr::VjpArgs& A, cudaStream_t st);                                                    \
+                   const hmr::VjpArgs& A, hmr::VjpWork* d_rec, cudaStream_t st);                               \
+    int launch_vjp_level(const hmr::Variant& v, const hmr::Params& P, const hmr::VjpWork* W, int np,           \
+                         const long* totals, bool flux_terms, cudaStream_t st);                                \
     }
 HMR_DECLARE_VJP_LAUNCHER(hmr_vjp_m0)
 HMR_DECLARE_VJP_LAUNCHER(hmr_vjp_m1)
 HMR_DECLARE_VJP_LAUNCHER(hmr_vjp_m2)
 
 namespace hmr_vjp {
+// d_rec: device space for one VjpWork record (the per-patch form is a group of one patch).
 inline int launch_vjp(const hmr::Variant& v, const hmr::Params& P, const hmr::Geom& g, const hmr::Scratch& S,
-                      const hmr::VjpArgs& A, cudaStream_t st) {
-    HMR_ROUTE(hmr_vjp, launch_vjp, v, P, g, S, A, st)
+                      const hmr::VjpArgs& A, hmr::VjpWork* d_rec, cudaStream_t st) {
+    HMR_ROUTE(hmr_vjp, launch_vjp, v, P, g, S, A, d_rec, st)
+}
+// The substep VJP of a group of patches (device array W of np records; totals[PH * 3 + axis]
+// items per phase); flux_terms false (beta == 0) runs only the cell gather.
+inline int launch_vjp_level(const hmr::Variant& v, const hmr::Params& P, const hmr::VjpWork* W, int np,
+                            const long* totals, bool flux_terms, cudaStream_t st) {
+    HMR_ROUTE(hmr_vjp, launch_vjp_level, v, P, W, np, totals, flux_terms, st)
 }
 }

@@ -52,121 +52,110 @@ static inline int grid_for(long items, int threads) {
     return (int)b;
 }
 
-template <int DIM, int MODEL, int NSP, int AX>
+// ---------------------------------------------------------------------------
+// One launch per phase over the flat item space of a group of patches (device records W,
+// patch by binary search over the prefix offsets).  The per-patch form runs the same kernels
+// on a one-patch group, so that a patch's result is bitwise the same in both forms: the
+// reverse arithmetic is FMA-contracted, and contraction is decided per kernel, so only the
+// same kernels give the same bits.
+// ---------------------------------------------------------------------------
+template <int PH, int AX>
+__device__ __forceinline__ int vjp_find(const VjpWork* W, int np, long t) {
+    int lo = 0, hi = np - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (W[mid].off[PH * 3 + AX] <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int DIM, int MODEL, int NSP, int SCHEME, int ORD, int PH, int AX>
 __global__ void __launch_bounds__(VJP_THREADS)
-face_proj_kernel(Geom g, Scratch S, VjpArgs VA) {
-    const long nf = nface_of(g, AX);
-    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < nf; t += (long)gridDim.x * blockDim.x)
-        face_proj_item<DIM, MODEL, NSP, AX>(g, S, VA, t);
+level_vjp_kernel(Params P, const VjpWork* W, int np, long total) {
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const int p = vjp_find<PH, AX>(W, np, t);
+        const VjpWork& w = W[p];
+        const long u = t - w.off[PH * 3 + AX];
+        if constexpr (PH == VJP_PH_PROJ) face_proj_item<DIM, MODEL, NSP, AX>(w.g, w.S, w.A, u);
+        else if constexpr (PH == VJP_PH_FWD) face_fwd_weno_item<DIM, MODEL, NSP, SCHEME, AX>(P, w.g, w.S, w.A, u);
+        else if constexpr (PH == VJP_PH_RIEM) face_bwd_riemann_item<DIM, MODEL, NSP, SCHEME, AX>(P, w.g, w.S, w.A, u);
+        else if constexpr (PH == VJP_PH_BWDW) face_bwd_weno_item<DIM, MODEL, NSP, SCHEME, AX>(P, w.g, w.S, w.A, u);
+        else if constexpr (PH == VJP_PH_CHAR) face_bwd_char_item<DIM, MODEL, NSP, AX>(w.g, w.S, w.A, u);
+        else if constexpr (PH == VJP_PH_DMID) diff_mid_bwd_item<DIM, ORD, AX>(P, w.g, w.S, w.A, u);
+        else if constexpr (PH == VJP_PH_DGD) diff_gd_bwd_item<DIM, ORD>(w.g, w.A, u);
+        else if constexpr (PH == VJP_PH_DCELL) diff_cell_bwd_item<DIM, ORD>(P, w.g, w.S, w.A, u);
+        else cell_bwd_item<DIM, MODEL, NSP>(P, w.g, w.S, w.A, u);
+    }
 }
 
-template <int DIM, int MODEL, int NSP, int SCHEME, int AX>
-__global__ void __launch_bounds__(VJP_THREADS)
-face_fwd_weno_kernel(Params P, Geom g, Scratch S, VjpArgs VA) {
-    const long n = nface_of(g, AX) * Model<DIM, MODEL, NSP>::NEQ;
-    for (long u = (long)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (long)gridDim.x * blockDim.x)
-        face_fwd_weno_item<DIM, MODEL, NSP, SCHEME, AX>(P, g, S, VA, u);
+template <class T, int ORD, int PH, int AX>
+static void launch_phase(const Params& P, const VjpWork* W, int np, const long* totals, cudaStream_t st) {
+    const long n = totals[PH * 3 + AX];
+    if (n <= 0) return;
+    level_vjp_kernel<T::DIM, T::MODEL, T::NSP, T::SCHEME, ORD, PH, AX>
+        <<<grid_for(n, VJP_THREADS), VJP_THREADS, 0, st>>>(P, W, np, n);
 }
 
-template <int DIM, int MODEL, int NSP, int SCHEME, int AX>
-__global__ void __launch_bounds__(VJP_THREADS)
-face_bwd_riemann_kernel(Params P, Geom g, Scratch S, VjpArgs VA) {
-    const long nf = nface_of(g, AX);
-    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < nf; t += (long)gridDim.x * blockDim.x)
-        face_bwd_riemann_item<DIM, MODEL, NSP, SCHEME, AX>(P, g, S, VA, t);
-}
-
-template <int DIM, int MODEL, int NSP, int SCHEME, int AX>
-__global__ void __launch_bounds__(VJP_THREADS)
-face_bwd_weno_kernel(Params P, Geom g, Scratch S, VjpArgs VA) {
-    const long n = nface_of(g, AX) * Model<DIM, MODEL, NSP>::NEQ;
-    for (long u = (long)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (long)gridDim.x * blockDim.x)
-        face_bwd_weno_item<DIM, MODEL, NSP, SCHEME, AX>(P, g, S, VA, u);
-}
-
-template <int DIM, int MODEL, int NSP, int AX>
-__global__ void __launch_bounds__(VJP_THREADS)
-face_bwd_char_kernel(Geom g, Scratch S, VjpArgs VA) {
-    const long nf = nface_of(g, AX);
-    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < nf; t += (long)gridDim.x * blockDim.x)
-        face_bwd_char_item<DIM, MODEL, NSP, AX>(g, S, VA, t);
-}
-
-template <class T, int AX>
-static void launch_face_axis(const Params& P, const Geom& g, const Scratch& S, const VjpArgs& A, cudaStream_t st) {
-    const long nf = nface_of(g, AX);
-    constexpr int NEQ = Model<T::DIM, T::MODEL, T::NSP>::NEQ;
-    face_proj_kernel<T::DIM, T::MODEL, T::NSP, AX><<<grid_for(nf, VJP_THREADS), VJP_THREADS, 0, st>>>(g, S, A);
-    face_fwd_weno_kernel<T::DIM, T::MODEL, T::NSP, T::SCHEME, AX>
-        <<<grid_for(nf * NEQ, VJP_THREADS), VJP_THREADS, 0, st>>>(P, g, S, A);
-    face_bwd_riemann_kernel<T::DIM, T::MODEL, T::NSP, T::SCHEME, AX>
-        <<<grid_for(nf, VJP_THREADS), VJP_THREADS, 0, st>>>(P, g, S, A);
-    face_bwd_weno_kernel<T::DIM, T::MODEL, T::NSP, T::SCHEME, AX>
-        <<<grid_for(nf * NEQ, VJP_THREADS), VJP_THREADS, 0, st>>>(P, g, S, A);
-    face_bwd_char_kernel<T::DIM, T::MODEL, T::NSP, AX><<<grid_for(nf, VJP_THREADS), VJP_THREADS, 0, st>>>(g, S, A);
-}
-
-template <int DIM, int MODEL, int NSP>
-__global__ void __launch_bounds__(VJP_THREADS)
-cell_bwd_kernel(Params P, Geom g, Scratch S, VjpArgs VA) {
-    const long nc = ncell_of(g);
-    for (long x = (long)blockIdx.x * blockDim.x + threadIdx.x; x < nc; x += (long)gridDim.x * blockDim.x)
-        cell_bwd_item<DIM, MODEL, NSP>(P, g, S, VA, x);
-}
-
-template <int DIM, int ORD, int AX>
-__global__ void __launch_bounds__(VJP_THREADS)
-diff_mid_bwd_kernel(Params P, Geom g, Scratch S, VjpArgs VA) {
-    const long nf = nface_of(g, AX);
-    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < nf; t += (long)gridDim.x * blockDim.x)
-        diff_mid_bwd_item<DIM, ORD, AX>(P, g, S, VA, t);
-}
-
-template <int DIM, int ORD>
-__global__ void __launch_bounds__(VJP_THREADS) diff_gd_bwd_kernel(Geom g, VjpArgs VA) {
-    const long nc = ncell_of(g);
-    for (long x = (long)blockIdx.x * blockDim.x + threadIdx.x; x < nc; x += (long)gridDim.x * blockDim.x)
-        diff_gd_bwd_item<DIM, ORD>(g, VA, x);
-}
-
-template <int DIM, int ORD>
-__global__ void __launch_bounds__(VJP_THREADS) diff_cell_bwd_kernel(Params P, Geom g, Scratch S, VjpArgs VA) {
-    const long nc = ncell_of(g);
-    for (long x = (long)blockIdx.x * blockDim.x + threadIdx.x; x < nc; x += (long)gridDim.x * blockDim.x)
-        diff_cell_bwd_item<DIM, ORD>(P, g, S, VA, x);
+template <class T, int ORD, int AX>
+static void launch_axis(const Params& P, const VjpWork* W, int np, const long* totals, cudaStream_t st) {
+    launch_phase<T, ORD, VJP_PH_PROJ, AX>(P, W, np, totals, st);
+    launch_phase<T, ORD, VJP_PH_FWD, AX>(P, W, np, totals, st);
+    launch_phase<T, ORD, VJP_PH_RIEM, AX>(P, W, np, totals, st);
+    launch_phase<T, ORD, VJP_PH_BWDW, AX>(P, W, np, totals, st);
+    launch_phase<T, ORD, VJP_PH_CHAR, AX>(P, W, np, totals, st);
 }
 
 // Navier-Stokes: the diffusive flux's share of the primitive-variable adjoints (into VA.Dv).
-template <int DIM, int ORD>
-static void launch_diff_bwd(const Params& P, const Geom& g, const Scratch& S, const VjpArgs& A, cudaStream_t st) {
-    diff_mid_bwd_kernel<DIM, ORD, 0><<<grid_for(nface_of(g, 0), VJP_THREADS), VJP_THREADS, 0, st>>>(P, g, S, A);
-    diff_mid_bwd_kernel<DIM, ORD, 1><<<grid_for(nface_of(g, 1), VJP_THREADS), VJP_THREADS, 0, st>>>(P, g, S, A);
-    if constexpr (DIM == 3)
-        diff_mid_bwd_kernel<DIM, ORD, 2><<<grid_for(nface_of(g, 2), VJP_THREADS), VJP_THREADS, 0, st>>>(P, g, S, A);
-    diff_gd_bwd_kernel<DIM, ORD><<<grid_for(ncell_of(g), VJP_THREADS), VJP_THREADS, 0, st>>>(g, A);
-    diff_cell_bwd_kernel<DIM, ORD><<<grid_for(ncell_of(g), VJP_THREADS), VJP_THREADS, 0, st>>>(P, g, S, A);
+template <class T, int ORD>
+static void launch_diff(const Params& P, const VjpWork* W, int np, const long* totals, cudaStream_t st) {
+    launch_phase<T, ORD, VJP_PH_DMID, 0>(P, W, np, totals, st);
+    launch_phase<T, ORD, VJP_PH_DMID, 1>(P, W, np, totals, st);
+    if constexpr (T::DIM == 3) launch_phase<T, ORD, VJP_PH_DMID, 2>(P, W, np, totals, st);
+    launch_phase<T, ORD, VJP_PH_DGD, 0>(P, W, np, totals, st);
+    launch_phase<T, ORD, VJP_PH_DCELL, 0>(P, W, np, totals, st);
 }
 
-int launch_vjp(const Variant& v, const Params& P, const Geom& g, const Scratch& S, const VjpArgs& A,
-               cudaStream_t st) {
+template <class T, int ORD>
+static int launch_group(const Params& P, const VjpWork* W, int np, const long* totals, bool flux_terms,
+                        cudaStream_t st) {
+    if (flux_terms) {
+        launch_axis<T, ORD, 0>(P, W, np, totals, st);
+        launch_axis<T, ORD, 1>(P, W, np, totals, st);
+        if constexpr (T::DIM == 3) launch_axis<T, ORD, 2>(P, W, np, totals, st);
+        if constexpr (ORD != 0) launch_diff<T, ORD>(P, W, np, totals, st);
+    }
+    launch_phase<T, ORD, VJP_PH_CELLB, 0>(P, W, np, totals, st);
+    return (int)cudaPeekAtLastError();
+}
+
+int launch_vjp_level(const Variant& v, const Params& P, const VjpWork* W, int np, const long* totals,
+                     bool flux_terms, cudaStream_t st) {
     return dispatch(v, [&](auto t) {
         using T = decltype(t);
-        if (A.beta != 0.0) {
-            launch_face_axis<T, 0>(P, g, S, A, st);
-            launch_face_axis<T, 1>(P, g, S, A, st);
-            if constexpr (T::DIM == 3) launch_face_axis<T, 2>(P, g, S, A, st);
-        }
         if constexpr (T::MODEL == SINGLE_SPECIES) {
-            if (A.beta != 0.0 && A.Dv != nullptr) {
-                if (P.dorder == 4) launch_diff_bwd<T::DIM, 4>(P, g, S, A, st);
-                else if (P.dorder == 2) launch_diff_bwd<T::DIM, 2>(P, g, S, A, st);
-                else return -2;
-            }
+            if (P.dorder == 4) return launch_group<T, 4>(P, W, np, totals, flux_terms, st);
+            if (P.dorder == 2) return launch_group<T, 2>(P, W, np, totals, flux_terms, st);
         }
-        cell_bwd_kernel<T::DIM, T::MODEL, T::NSP>
-            <<<grid_for(ncell_of(g), VJP_THREADS), VJP_THREADS, 0, st>>>(P, g, S, A);
-        return (int)cudaPeekAtLastError();
+        if (P.dorder != 0) return -2;
+        return launch_group<T, 0>(P, W, np, totals, flux_terms, st);
     });
+}
+
+// The one-patch record, written on the device (a kernel argument, so nothing waits on the host).
+__global__ void store_record_kernel(VjpWork w, VjpWork* dst) { *dst = w; }
+
+int launch_vjp(const Variant& v, const Params& P, const Geom& g, const Scratch& S, const VjpArgs& A,
+               VjpWork* d_rec, cudaStream_t st) {
+    VjpWork w;
+    w.g = g;
+    w.S = S;
+    w.A = A;
+    long totals[VJP_NPH * 3];
+    for (int k = 0; k < VJP_NPH * 3; k++) w.off[k] = 0;
+    vjp_item_counts(v, g, totals);
+    store_record_kernel<<<1, 1, 0, st>>>(w, d_rec);
+    return launch_vjp_level(v, P, d_rec, 1, totals, A.beta != 0.0, st);
 }
 
 }  // namespace HMR_NS

@@ -47,6 +47,22 @@ struct VjpArgs {
     double* Dv;
 };
 
+// One patch of a group whose substep VJPs run together, one launch per phase over the flat
+// item space of all the group's patches (the per-patch form is a group of one).
+// off[PH * 3 + axis] is the patch's prefix offset in the item space of phase PH (phases over
+// cells use axis 0).  Phases: projection factors, WCNS forward keeping the smoothness
+// indicators, Riemann reverse, WCNS reverse, projection reverse (per face axis); for
+// NavierStokes the midpoint (per axis), node-gradient and cell reverses of the diffusive flux;
+// the cell gather.
+enum { VJP_PH_PROJ = 0, VJP_PH_FWD, VJP_PH_RIEM, VJP_PH_BWDW, VJP_PH_CHAR, VJP_PH_DMID, VJP_PH_DGD,
+       VJP_PH_DCELL, VJP_PH_CELLB, VJP_NPH };
+struct VjpWork {
+    Geom g;
+    Scratch S;
+    VjpArgs A;
+    long off[VJP_NPH * 3];
+};
+
 // Adjoint of the pre-rewrite stage output (component e < NEQ) at a cell:
 // Qb_out, with the five-equation last volume fraction's adjoint moved onto
 // the others (Z_N = 1 - sum Z_k, only written when beta != 0).

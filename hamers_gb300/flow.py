@@ -578,6 +578,17 @@ class BatchedLevel:
         L.check("hmr_level_substep", self._lib.hmr_level_substep(self.level, int(stage), float(dt),
                                                                  _stream_ptr(stream)))
 
+    def substepVJP(self, stage, dt, Qbar_out, Qbar_int, stream=None):
+        """Adjoint of substep(stage, dt) over every patch, batched: for each patch p accumulates
+        into Qbar_int[p][n] (n <= stage, ghost-box tensors) the vector-Jacobian product of
+        Qbar_out[p] with the substep at the level's stage states (as the forward left them).
+        Bitwise the per-patch Euler.substepVJP of each patch."""
+        nc = self.rec.ncomp
+        qb, k1 = L.ptr_array2([_comp_ptrs(t, nc) for t in Qbar_out])
+        qbi, k2 = L.ptr_array3([[_comp_ptrs(t, nc) for t in slots[:stage + 1]] for slots in Qbar_int])
+        L.check("hmr_level_substep_vjp", self._lib.hmr_level_substep_vjp(
+            self.level, int(stage), float(dt), qb, qbi, _stream_ptr(stream)))
+
     def set_layout(self, lo, domain, periodic):
         """Patch positions (first interior cell per patch, level index space), the domain's cells
         per axis and its periodic axes: enables the ghost exchange between patches."""
@@ -617,6 +628,16 @@ class BatchedLevel:
 
     def set_launch(self, threads, blocks_per_sm):
         L.check("hmr_level_set_launch", self._lib.hmr_level_set_launch(self.level, int(threads), int(blocks_per_sm)))
+
+    def set_work_split(self, chunk_blocks, mode=0):
+        """Chunks of chunk_blocks (1, 2, 4) block widths per phase; mode 1: grid-stride hand-out
+        of the cell-wise phases."""
+        L.check("hmr_level_set_work_split", self._lib.hmr_level_set_work_split(self.level, int(chunk_blocks), int(mode)))
+
+    def work_split(self):
+        m, s_ = ctypes.c_int(), ctypes.c_int()
+        L.check("hmr_level_work_split", self._lib.hmr_level_work_split(self.level, ctypes.byref(m), ctypes.byref(s_)))
+        return m.value, s_.value
 
     def autotune(self, dt, stream=None):
         t = ctypes.c_int()

@@ -305,6 +305,23 @@ int hmr_level_set_periodic(hmr_level* level, int patch, const int* periodic);
 int hmr_level_substep(hmr_level* level, int stage, double dt, void* stream);
 /* One SSPRK3 step: the three substep graphs in order. */
 int hmr_level_step(hmr_level* level, double dt, void* stream);
+/* Vector-Jacobian product of hmr_level_substep over every patch of the level, batched (no
+ * counterpart in the reference: its adjoint form, like hmr_rk_substep_vjp_patch's).  For each
+ * patch p it adds to Qbar_int[p][n] (n = 0..stage; ncomp ghost-box arrays each) the product of
+ * Qbar_out[p] (ncomp ghost-box arrays; interior read) with the Jacobian of substep `stage` at
+ * the level's stage states, as they stand after the forward substep (slot `stage` ghost-filled);
+ * the ghost fill's own adjoint is the caller's, as for the per-patch form.  Results are bitwise
+ * those of hmr_rk_substep_vjp_patch on each patch.  The patches run together, one launch per
+ * phase over the flat item space of a group of patches whose per-face reverse buffers (about
+ * 1.2 KB per face) fit a quarter of the device memory free at the first call; the buffers
+ * stay with the level.  The Euler equations only (HMR_ERR_UNSUPPORTED for a NavierStokes
+ * context); HMR_ERR_STATE until every patch's slot 0 is bound. */
+int hmr_level_substep_vjp(hmr_level* level, int stage, double dt, const double* const* const* Qbar_out,
+                          double* const* const* const* Qbar_int, void* stream);
+/* Memory budget of hmr_level_substep_vjp's per-face reverse buffers, in bytes (0: a quarter of
+ * the device memory free at the next call).  The largest patch always gets its buffers; a
+ * smaller budget splits the level into more groups of patches. */
+int hmr_level_set_vjp_budget(hmr_level* level, unsigned long long bytes);
 /* Synchronises and reports whether a barrier of a persistent kernel gave up
  * (HMR_ERR_BARRIER, flag cleared) since the last check. */
 /* One SSPRK3 step whose time step is computed on the device from the slot-0 states (ghost
@@ -322,8 +339,15 @@ int hmr_level_barrier_diagnostic(hmr_level* level, unsigned int extra_arrivals, 
 /* Launch shape of the persistent kernel: 64 or 128 threads per block and 1..(resident
  * maximum) blocks per SM; HMR_ERR_ARGUMENT for a shape that cannot be resident at once. */
 int hmr_level_set_launch(hmr_level* level, int threads, int blocks_per_sm);
+/* Work splitting of the persistent kernel: every phase's items are handed out in chunks of
+ * chunk_blocks (1, 2 or 4) block widths taken from a counter in order; mode 1 hands the
+ * cell-wise phases (cell data, sensor, update) out by a fixed grid stride instead.  Results do
+ * not depend on either. */
+int hmr_level_set_work_split(hmr_level* level, int chunk_blocks, int mode);
+int hmr_level_work_split(hmr_level* level, int* chunk_blocks, int* mode);
 /* Autotuner: times the persistent kernel of this level at 64 and 128 threads per block and
- * every resident block count per SM, keeps the fastest.  Returns the chosen shape. */
+ * every resident block count per SM, then the work splittings at the fastest shape, and keeps
+ * the fastest.  Returns the chosen shape (hmr_level_work_split gives the chosen splitting). */
 int hmr_level_autotune(hmr_level* level, double dt, int* threads_out, int* blocks_per_sm_out, void* stream);
 
 /* Fixed device scratch of hmr_rk_substep_patch_noalloc: 32 MiB, held on every GPU that loads

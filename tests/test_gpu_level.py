@@ -86,9 +86,10 @@ def test_batched_level_matches_oracle(cuda, variant, precision):
 @pytest.mark.gpu
 @pytest.mark.parametrize("precision", ["exact", "fast"])
 def test_launch_shape_leaves_results_unchanged(cuda, precision):
-    """Every resident launch shape gives the same bits (phase items are handed out in chunks
-    from counters, and each item's arithmetic does not depend on which block runs it); shapes
-    that cannot be resident are rejected before any launch."""
+    """Every resident launch shape and work splitting gives the same bits (phase items are
+    handed out in chunks from counters or by grid stride, and each item's arithmetic does not
+    depend on which block runs it); shapes that cannot be resident, and unknown splittings, are
+    rejected before any launch."""
     import torch
     from hamers_gb300 import flow
     model, dim, scheme, _, gam = VARIANTS[5]
@@ -104,9 +105,17 @@ def test_launch_shape_leaves_results_unchanged(cuda, precision):
     for bad in ((256, 1), (96, 1), (64, 0), (128, 1000)):
         with pytest.raises(RuntimeError):
             lv.set_launch(*bad)
+    for bad in ((3, 0), (0, 0), (1, 2), (2, -1)):
+        with pytest.raises(RuntimeError):
+            lv.set_work_split(*bad)
     results = []
-    for shape in ((64, 1), (128, 1), (128, 2), (64, 3)):
+    # launch shapes and work splittings (chunk widths of 1, 2, 4 blocks; grid-stride hand-out
+    # of the cell-wise phases)
+    for shape, split in (((64, 1), (1, 0)), ((128, 1), (1, 0)), ((128, 2), (1, 0)), ((64, 3), (1, 0)),
+                         ((128, 2), (2, 0)), ((64, 2), (4, 0)), ((128, 1), (1, 1)), ((64, 3), (4, 1))):
         lv.set_launch(*shape)
+        lv.set_work_split(*split)
+        assert lv.work_split() == split
         for p, Q in enumerate(states):
             Q.copy_(torch.from_numpy(Q0[p]))
         lv.step(dt)
