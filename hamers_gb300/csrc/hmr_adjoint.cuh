@@ -120,13 +120,23 @@ __device__ __forceinline__ void js_side_bwd(int p, const double* S, double b0, d
     js_betas_bwd(S, bb0, bb1, bb2, Sb);
 }
 
+// The adjoint's forward recomputation of the smoothness indicators runs one (face, variable)
+// item per thread at high occupancy, where integer-pipe multiplications (hmr_emu64.cuh) can run
+// beside the native FP64 pipe; HMR_EMU_BETA_VJP takes the mask encoding of HMR_EMU_BETA.  The
+// result bits are the same either way.
+#ifndef HMR_EMU_BETA_VJP
+#define HMR_EMU_BETA_VJP 0
+#endif
+constexpr int EMU_VJP_M = HMR_EMU_BETA_VJP & 3;
+constexpr int EMU_VJP_P = (HMR_EMU_BETA_VJP >> 2) & 3;
+
 // Forward of both sides (the operations of js_pair<X>) keeping the smoothness
 // indicators: b[0..2] of the minus side, b[3..5] of the plus side.
 template <bool X>
 __device__ __forceinline__ void js_pair_keep(const double* U, int p, double& Um, double& Up, double* b) {
-    js_betas_x(U[0], U[1], U[2], U[3], U[4], b[0], b[1], b[2]);
+    js_betas_x<EMU_VJP_M>(U[0], U[1], U[2], U[3], U[4], b[0], b[1], b[2]);
     Um = js_interp<X>(b[0], b[1], b[2], p, U[0], U[1], U[2], U[3], U[4]);
-    js_betas_x(U[5], U[4], U[3], U[2], U[1], b[3], b[4], b[5]);
+    js_betas_x<EMU_VJP_P>(U[5], U[4], U[3], U[2], U[1], b[3], b[4], b[5]);
     Up = js_interp<X>(b[3], b[4], b[5], p, U[5], U[4], U[3], U[2], U[1]);
 }
 
@@ -282,11 +292,11 @@ __device__ __forceinline__ void ld_side_bwd(const Params& P, double sigma, const
 template <bool X>
 __device__ __forceinline__ void ld_pair_keep(const double* U, const Params& P, double& Um, double& Up, double* b) {
     double sg = -1.0;
-    js_betas_x(U[0], U[1], U[2], U[3], U[4], b[0], b[1], b[2]);
-    b[3] = ld_beta3(U[0], U[1], U[2], U[3], U[4], U[5]);
+    js_betas_x<EMU_VJP_M>(U[0], U[1], U[2], U[3], U[4], b[0], b[1], b[2]);
+    b[3] = ld_beta3<EMU_VJP_M>(U[0], U[1], U[2], U[3], U[4], U[5]);
     Um = ld_interp<X>(b, U, sg, P, U[0], U[1], U[2], U[3], U[4], U[5]);
-    js_betas_x(U[5], U[4], U[3], U[2], U[1], b[4], b[5], b[6]);
-    b[7] = ld_beta3(U[5], U[4], U[3], U[2], U[1], U[0]);
+    js_betas_x<EMU_VJP_P>(U[5], U[4], U[3], U[2], U[1], b[4], b[5], b[6]);
+    b[7] = ld_beta3<EMU_VJP_P>(U[5], U[4], U[3], U[2], U[1], U[0]);
     Up = ld_interp<X>(b + 4, U, sg, P, U[5], U[4], U[3], U[2], U[1], U[0]);
     b[8] = sg;
 }
@@ -352,9 +362,9 @@ __device__ __forceinline__ void z_side_bwd(int p, const double* S, const double*
 // b[0..2] minus side, b[3..5] plus side.
 template <bool X>
 __device__ __forceinline__ void z_pair_keep(const double* U, int p, double& Um, double& Up, double* b) {
-    js_betas_x(U[0], U[1], U[2], U[3], U[4], b[0], b[1], b[2]);
+    js_betas_x<EMU_VJP_M>(U[0], U[1], U[2], U[3], U[4], b[0], b[1], b[2]);
     Um = z_interp<X>(b[0], b[1], b[2], p, U[0], U[1], U[2], U[3], U[4]);
-    js_betas_x(U[5], U[4], U[3], U[2], U[1], b[3], b[4], b[5]);
+    js_betas_x<EMU_VJP_P>(U[5], U[4], U[3], U[2], U[1], b[3], b[4], b[5]);
     Up = z_interp<X>(b[3], b[4], b[5], p, U[5], U[4], U[3], U[2], U[1]);
 }
 
@@ -432,11 +442,11 @@ __device__ __forceinline__ void cu_side_bwd(const Params& P, double ce, double c
 // indicators: b[0..3] minus side, b[4..7] plus side.
 template <bool X, int A>
 __device__ __forceinline__ void cu_pair_keep(const double* U, const Params& P, double& Um, double& Up, double* b) {
-    js_betas_x(U[0], U[1], U[2], U[3], U[4], b[0], b[1], b[2]);
-    b[3] = ld_beta3(U[0], U[1], U[2], U[3], U[4], U[5]);
+    js_betas_x<EMU_VJP_M>(U[0], U[1], U[2], U[3], U[4], b[0], b[1], b[2]);
+    b[3] = ld_beta3<EMU_VJP_M>(U[0], U[1], U[2], U[3], U[4], U[5]);
     Um = cu_interp<X>(b, P, P.cu_e[A], P.cu_x[A], U[0], U[1], U[2], U[3], U[4], U[5]);
-    js_betas_x(U[5], U[4], U[3], U[2], U[1], b[4], b[5], b[6]);
-    b[7] = ld_beta3(U[5], U[4], U[3], U[2], U[1], U[0]);
+    js_betas_x<EMU_VJP_P>(U[5], U[4], U[3], U[2], U[1], b[4], b[5], b[6]);
+    b[7] = ld_beta3<EMU_VJP_P>(U[5], U[4], U[3], U[2], U[1], U[0]);
     Up = cu_interp<X>(b + 4, P, P.cu_e[A], P.cu_x[A], U[5], U[4], U[3], U[2], U[1], U[0]);
 }
 
