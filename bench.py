@@ -113,7 +113,8 @@ def parse():
                     help="skip the 2D single-species 256^2 per-patch workload")
     ap.add_argument("--uneven-patches", type=int, default=512)
     ap.add_argument("--per-patch-busy", action="store_true",
-                    help="also record the per-patch form's kernel-busy share of one uneven-patch step")
+                    help="run one extra per-patch uneven-patch step inside an NVTX range (per_patch_step) for "
+                         "an ncu launch list of exactly that step")
     ap.add_argument("--uneven-only", action="store_true",
                     help="run only the uneven-patch batched-vs-per-patch measurement and print it")
     return ap.parse_args()
@@ -271,7 +272,8 @@ def uneven_batched_vs_patch(args, flow):
     e[1].record(stream)
     torch.cuda.synchronize()
     t_patch = e[0].elapsed_time(e[1]) / reps
-    busy = per_patch_busy_share(step_patches) if args.per_patch_busy else None
+    if args.per_patch_busy:
+        mark_per_patch_step(step_patches)
     rec.close()
     cu = 3 * cells
     return {"workload": f"3D single species WCNS5-JS + HLLC-HLL, {len(patches)} uneven cubic patches "
@@ -281,46 +283,23 @@ def uneven_batched_vs_patch(args, flow):
             "batched_over_per_patch": t_patch / t_batched,
             "batched_ms_per_step": t_batched, "per_patch_ms_per_step": t_patch,
             "launch_shape": {"threads": tuned[0], "blocks_per_sm": tuned[1]},
-            "per_patch_busy": busy,
             "batched_roofline": roofline_fracs(cu / (t_batched * 1e-3), ALG_FP64_OPS_C3, alg_bytes(5),
                                                args.fp64_peak, args.hbm_peak),
             "per_patch_roofline": roofline_fracs(cu / (t_patch * 1e-3), ALG_FP64_OPS_C3, alg_bytes(5),
                                                  args.fp64_peak, args.hbm_peak)}
 
 
-def per_patch_busy_share(step):
-    """How much of one per-patch step's span the GPU spends in kernels: the step runs once
-    under torch.profiler (CUDA activity records, no kernel replay), and the union of the kernel
-    intervals is compared with the span from the first kernel's start to the last one's end."""
+def mark_per_patch_step(step):
+    """Runs one more per-patch step inside an NVTX range named per_patch_step, so that a launch
+    list (ncu --nvtx --nvtx-include per_patch_step/) holds exactly that step's kernels; their
+    summed device time against the step's device-timed wall time gives the share of the step the
+    GPU spends in kernels."""
     import torch
-    from torch.profiler import ProfilerActivity, profile
     torch.cuda.synchronize()
-    with profile(activities=[ProfilerActivity.CUDA]) as prof:
-        step()
-        torch.cuda.synchronize()
-    # raw activity records: kernels launched through the C ABI have no torch operator, so they
-    # appear there (device type CUDA) rather than among the profiler's operator events
-    spans = []
-    for ev in prof.profiler.kineto_results.events():
-        if ev.device_type() == torch.autograd.DeviceType.CUDA and ev.duration_ns() > 0:
-            t0 = ev.start_ns() * 1e-3
-            spans.append((t0, t0 + ev.duration_ns() * 1e-3))
-    spans.sort()
-    if not spans:
-        return {"error": "no CUDA activity records"}
-    busy, cur_s, cur_e = 0.0, spans[0][0], spans[0][1]
-    for a, b in spans[1:]:
-        if a > cur_e:
-            busy += cur_e - cur_s
-            cur_s, cur_e = a, b
-        else:
-            cur_e = max(cur_e, b)
-    busy += cur_e - cur_s
-    span = max(b for _, b in spans) - spans[0][0]
-    return {"launches": len(spans), "kernel_busy_ms": busy * 1e-3, "span_ms": span * 1e-3,
-            "busy_share": busy / span if span > 0 else None,
-            "note": "one per-patch step under torch.profiler (CUDA activity records): union of kernel "
-                    "intervals against the span from the first kernel start to the last kernel end"}
+    torch.cuda.nvtx.range_push("per_patch_step")
+    step()
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
 
 
 def adjoint_cost(args, flow, Qnp, n, dx, dt, reps=3):
@@ -461,6 +440,24 @@ def c5_level_and_adjoint(args, flow, base=128, reps=3):
     e[1].record(stream)
     torch.cuda.synchronize()
     t_adj = e[0].elapsed_time(e[1]) / reps
+    # the same adjoint batched over the level (hmr_level_substep_vjp), at the stage state the
+    # level's forward substep leaves (slot 0: the bound states, ghosts provided)
+    bars_b = [[torch.zeros_like(Q)] for Q in states]
+
+    def reverse_batched():
+        for b in bars_b:
+            b[0].zero_()
+        lv.substepVJP(0, dt, W, bars_b)
+
+    reverse_batched()
+    torch.cuda.synchronize()
+    e[0].record(stream)
+    for _ in range(reps):
+        reverse_batched()
+    e[1].record(stream)
+    torch.cuda.synchronize()
+    t_adj_b = e[0].elapsed_time(e[1]) / reps
+    same_bits = all(torch.equal(b[0], q) for b, q in zip(bars_b, bars))
     a_req = a.clone().requires_grad_(True)
     grad = torch.zeros_like(a)
     for (_, lo, n, dx), b in zip(layout, bars):
@@ -480,9 +477,10 @@ def c5_level_and_adjoint(args, flow, base=128, reps=3):
                                                args.fp64_peak, args.hbm_peak),
             "per_patch_roofline": roofline_fracs(cells / (t_patch * 1e-3), ALG_FP64_OPS_C5, alg_bytes(7, (0,)),
                                                  args.fp64_peak, args.hbm_peak),
-            "adjoint_substep_ms": t_adj, "adjoint_over_batched_forward": t_adj / t_batched,
-            # the adjoint runs patch by patch: the same form's forward is the per-patch one
-            "adjoint_over_per_patch_forward": t_adj / t_patch,
+            "adjoint_per_patch_substep_ms": t_adj, "adjoint_batched_substep_ms": t_adj_b,
+            "adjoint_batched_over_batched_forward": t_adj_b / t_batched,
+            "adjoint_per_patch_over_per_patch_forward": t_adj / t_patch,
+            "adjoint_batched_equals_per_patch": same_bits,
             "grad_amplitudes_norm": float(grad.norm())}
 
 

@@ -6,15 +6,19 @@
 
 namespace hmro_count {
 inline unsigned long long g_ops = 0;
+inline int g_phase = 0;
+inline unsigned long long g_phase_ops[16] = {};
+// every counted operation is also charged to the oracle's current sub-phase (HMRO_PHASE)
+inline void tick() { g_ops++; g_phase_ops[g_phase]++; }
 struct C {
     double v;
     C() : v(0.0) {}
     C(double x) : v(x) {}
 };
-inline C operator+(C a, C b) { g_ops++; return C(a.v + b.v); }
-inline C operator-(C a, C b) { g_ops++; return C(a.v - b.v); }
-inline C operator*(C a, C b) { g_ops++; return C(a.v * b.v); }
-inline C operator/(C a, C b) { g_ops++; return C(a.v / b.v); }
+inline C operator+(C a, C b) { tick(); return C(a.v + b.v); }
+inline C operator-(C a, C b) { tick(); return C(a.v - b.v); }
+inline C operator*(C a, C b) { tick(); return C(a.v * b.v); }
+inline C operator/(C a, C b) { tick(); return C(a.v / b.v); }
 inline C operator-(C a) { return C(-a.v); }
 inline C operator+(C a, double b) { return a + C(b); }
 inline C operator-(C a, double b) { return a - C(b); }
@@ -30,13 +34,14 @@ inline C& operator*=(C& a, C b) { a = a * b; return a; }
 }  // namespace hmro_count
 
 namespace hmro {
-inline hmro_count::C s_sqrt(hmro_count::C a) { hmro_count::g_ops++; return hmro_count::C(std::sqrt(a.v)); }
-inline hmro_count::C s_fabs(hmro_count::C a) { hmro_count::g_ops++; return hmro_count::C(std::fabs(a.v)); }
-inline hmro_count::C s_fmin(hmro_count::C a, hmro_count::C b) { hmro_count::g_ops++; return hmro_count::C(std::fmin(a.v, b.v)); }
-inline hmro_count::C s_fmax(hmro_count::C a, hmro_count::C b) { hmro_count::g_ops++; return hmro_count::C(std::fmax(a.v, b.v)); }
+inline hmro_count::C s_sqrt(hmro_count::C a) { hmro_count::tick(); return hmro_count::C(std::sqrt(a.v)); }
+inline hmro_count::C s_fabs(hmro_count::C a) { hmro_count::tick(); return hmro_count::C(std::fabs(a.v)); }
+inline hmro_count::C s_fmin(hmro_count::C a, hmro_count::C b) { hmro_count::tick(); return hmro_count::C(std::fmin(a.v, b.v)); }
+inline hmro_count::C s_fmax(hmro_count::C a, hmro_count::C b) { hmro_count::tick(); return hmro_count::C(std::fmax(a.v, b.v)); }
 inline double s_val(hmro_count::C a) { return a.v; }
 }  // namespace hmro
 
+#define HMRO_PHASE(k) (hmro_count::g_phase = (k))
 #include "hmr_oracle.hpp"
 
 #include <vector>
@@ -73,6 +78,7 @@ double hmro_count_ops(int model, int dim, int nsp, int scheme, const double* gam
     for (auto& s : src) sp.push_back(s.data());
     hmro::g_minimal_hll = true;
     hmro_count::g_ops = 0;
+    for (int k = 0; k < 16; k++) hmro_count::g_phase_ops[k] = 0;
     hmro::conv_flux_source<C>(c, n, dx, 1.0e-3, qp.data(), fp.data(), sp.data(), nullptr);
     // stage update: Q = 1*Q + 1*(div + S)
     std::vector<C> qo((size_t)ncomp * b.ncell());
@@ -82,9 +88,19 @@ double hmro_count_ops(int model, int dim, int nsp, int scheme, const double* gam
     const C* const* fi[1] = {fp.data()};
     const C* const* si[1] = {sp.data()};
     const double one = 1.0, zero = 0.0;
+    hmro_count::g_phase = hmro::HMRO_PH_STAGE;
     hmro::rk_stage<C>(c, n, dx, 1, &one, &one, &zero, qi, fi, si, qop.data(), nullptr, nullptr);
     hmro::g_minimal_hll = false;
     return (double)hmro_count::g_ops / (double)nint;
+}
+
+// Operations per interior cell of the last hmro_count_ops call, by sub-phase (HMRO_NPH values:
+// cell data, sensor, projection factors, characteristic variables, smoothness indicators,
+// weights and interpolation, inverse projection, bounds, Riemann, flux formula, source, stage).
+void hmro_count_phases(const int* n, int dim, double* out) {
+    long nint = 1;
+    for (int d = 0; d < dim; d++) nint *= n[d];
+    for (int k = 0; k < hmro::HMRO_NPH; k++) out[k] = (double)hmro_count::g_phase_ops[k] / (double)nint;
 }
 
 }  // extern "C"

@@ -43,6 +43,14 @@ inline double s_fmin(double a, double b) { return std::fmin(a, b); }
 inline double s_fmax(double a, double b) { return std::fmax(a, b); }
 inline double s_val(double a) { return a; }
 
+// Sub-phase markers for the operation counter (hmr_opcount.cpp defines HMRO_PHASE to attribute
+// every counted operation to the current sub-phase); no-ops otherwise.
+enum { HMRO_PH_CELLS = 0, HMRO_PH_SENSOR, HMRO_PH_PROJ, HMRO_PH_CHAR, HMRO_PH_BETA, HMRO_PH_WEIGHTS,
+       HMRO_PH_INV, HMRO_PH_BOUNDS, HMRO_PH_RIEMANN, HMRO_PH_FLUX, HMRO_PH_SOURCE, HMRO_PH_STAGE, HMRO_NPH };
+#ifndef HMRO_PHASE
+#define HMRO_PHASE(k) ((void)0)
+#endif
+
 enum { MODEL_SINGLE_SPECIES = 0, MODEL_FOUR_EQN_CONSERVATIVE = 1, MODEL_FIVE_EQN_ALLAIRE = 2 };
 // ConvectiveFluxReconstructorManager.cpp:40-91: WCNS5_JS_HLLC_HLL, WCNS6_LD_HLLC_HLL,
 // WCNS5_Z_HLLC_HLL, WCNS6_CU_M2_HLLC_HLL (all on the WCNS56 driver).
@@ -171,7 +179,9 @@ inline void js_beta_tilde(T& b0, T& b1, T& b2, const T* U) {  // :51-72
 template <class T>
 inline T js_minus(const T* U, int p) {  // :78-117
     T b0, b1, b2;
+    HMRO_PHASE(HMRO_PH_BETA);
     js_beta(b0, b1, b2, U);
+    HMRO_PHASE(HMRO_PH_WEIGHTS);
     T w0 = double(1.0)/double(16)/ipow_(b0 + EPS, p);
     T w1 = double(5.0)/double(8)/ipow_(b1 + EPS, p);
     T w2 = double(5.0)/double(16)/ipow_(b2 + EPS, p);
@@ -187,7 +197,9 @@ inline T js_minus(const T* U, int p) {  // :78-117
 template <class T>
 inline T js_plus(const T* U, int p) {  // :123-164
     T b0, b1, b2;
+    HMRO_PHASE(HMRO_PH_BETA);
     js_beta_tilde(b0, b1, b2, U);
+    HMRO_PHASE(HMRO_PH_WEIGHTS);
     T w0 = double(1)/double(16)/ipow_(b0 + EPS, p);
     T w1 = double(5)/double(8)/ipow_(b1 + EPS, p);
     T w2 = double(5)/double(16)/ipow_(b2 + EPS, p);
@@ -281,10 +293,13 @@ inline void ld_weights(T& o0, T& o1, T& o2, T& o3, const T* beta, const T& sigma
 
 template <class T>
 inline T ld_minus(const T* U, int p, int q, double C, double alpha_tau) {  // :139-222
+    HMRO_PHASE(HMRO_PH_WEIGHTS);
     T sigma = ld_sigma(U);
     T beta[4];
+    HMRO_PHASE(HMRO_PH_BETA);
     js_beta(beta[0], beta[1], beta[2], U);
     beta[3] = ld_beta3(U);
+    HMRO_PHASE(HMRO_PH_WEIGHTS);
     T o0, o1, o2, o3;
     ld_weights(o0, o1, o2, o3, beta, sigma, p, q, C, alpha_tau);
     return double(3)/double(8)*o0*U[0] +
@@ -297,10 +312,13 @@ inline T ld_minus(const T* U, int p, int q, double C, double alpha_tau) {  // :1
 
 template <class T>
 inline T ld_plus(const T* U, int p, int q, double C, double alpha_tau) {  // :238-319
+    HMRO_PHASE(HMRO_PH_WEIGHTS);
     T sigma = ld_sigma(U);
     T beta[4];
+    HMRO_PHASE(HMRO_PH_BETA);
     js_beta_tilde(beta[0], beta[1], beta[2], U);
     beta[3] = ld_beta3_tilde(U);
+    HMRO_PHASE(HMRO_PH_WEIGHTS);
     T o0, o1, o2, o3;
     ld_weights(o0, o1, o2, o3, beta, sigma, p, q, C, alpha_tau);
     return double(3)/double(8)*o0*U[5] +
@@ -329,7 +347,9 @@ inline void z_weights(T& w0, T& w1, T& w2, const T& b0, const T& b1, const T& b2
 template <class T>
 inline T z_minus(const T* U, int p) {  // :78-120
     T b0, b1, b2, w0, w1, w2;
+    HMRO_PHASE(HMRO_PH_BETA);
     js_beta(b0, b1, b2, U);
+    HMRO_PHASE(HMRO_PH_WEIGHTS);
     z_weights(w0, w1, w2, b0, b1, b2, p);
     return double(3)/double(8)*w0*U[0] +
         (-double(10)/double(8)*w0 - double(1)/double(8)*w1)*U[1] +
@@ -342,7 +362,9 @@ inline T z_minus(const T* U, int p) {  // :78-120
 template <class T>
 inline T z_plus(const T* U, int p) {  // :126-168
     T b0, b1, b2, w0, w1, w2;
+    HMRO_PHASE(HMRO_PH_BETA);
     js_beta_tilde(b0, b1, b2, U);
+    HMRO_PHASE(HMRO_PH_WEIGHTS);
     z_weights(w0, w1, w2, b0, b1, b2, p);
     return double(3)/double(8)*w0*U[5] +
         (-double(10)/double(8)*w0 - double(1)/double(8)*w1)*U[4] +
@@ -379,8 +401,10 @@ inline void cu_weights(T& o0, T& o1, T& o2, T& o3, const T* beta, int q, double 
 template <class T>
 inline T cu_minus(const T* U, int q, double C, double Chi, double epsilon, double dx) {  // :112-167
     T beta[4];
+    HMRO_PHASE(HMRO_PH_BETA);
     js_beta(beta[0], beta[1], beta[2], U);
     beta[3] = ld_beta3(U);
+    HMRO_PHASE(HMRO_PH_WEIGHTS);
     T o0, o1, o2, o3;
     cu_weights(o0, o1, o2, o3, beta, q, C, Chi, epsilon, dx);
     return double(3)/double(8)*o0*U[0] +
@@ -394,8 +418,10 @@ inline T cu_minus(const T* U, int q, double C, double Chi, double epsilon, doubl
 template <class T>
 inline T cu_plus(const T* U, int q, double C, double Chi, double epsilon, double dx) {  // :173-228
     T beta[4];
+    HMRO_PHASE(HMRO_PH_BETA);
     js_beta_tilde(beta[0], beta[1], beta[2], U);
     beta[3] = ld_beta3_tilde(U);
+    HMRO_PHASE(HMRO_PH_WEIGHTS);
     T o0, o1, o2, o3;
     cu_weights(o0, o1, o2, o3, beta, q, C, Chi, epsilon, dx);
     return double(3)/double(8)*o0*U[5] +
@@ -966,7 +992,9 @@ void conv_flux_source(const Config& c, const int* n, const double* dx, double dt
     const Box b = make_box(dim, n, 4);
     const long nc = b.ncell();
     Derived<T> D;
+    HMRO_PHASE(HMRO_PH_CELLS);
     compute_derived(c, b, Q, D);
+    HMRO_PHASE(HMRO_PH_SENSOR);
     const int iu = vel_index(c);
     const bool five = (c.model == MODEL_FIVE_EQN_ALLAIRE);
     const bool multi = (c.model != MODEL_SINGLE_SPECIES);
@@ -1024,6 +1052,7 @@ void conv_flux_source(const Config& c, const int* n, const double* dx, double dt
         umid[a].assign(nf, T(0.0));
         const int off[3] = {a == 0, a == 1, a == 2};
 
+        HMRO_PHASE(HMRO_PH_PROJ);
         // Projection variables (SIMPLE averaging).
         //  single: FlowModelBasicUtilitiesSingleSpecies.cpp:4638-5134
         //  five:   FlowModelBasicUtilitiesFiveEqnAllaire.cpp:7474-8207
@@ -1046,6 +1075,7 @@ void conv_flux_source(const Config& c, const int* n, const double* dx, double dt
             }
         }
 
+        HMRO_PHASE(HMRO_PH_CHAR);
         // Characteristic variables for the six offsets m-3, m = 0..5
         // (WCNS56-HLLC-HLL.cpp:886-893).
         for (int m = 0; m < 6; m++)
@@ -1084,6 +1114,7 @@ void conv_flux_source(const Config& c, const int* n, const double* dx, double dt
             }
         }
 
+        HMRO_PHASE(HMRO_PH_INV);
         // Back to primitive variables, bounds check, first-order fallback
         // (WCNS56-HLLC-HLL.cpp:908-1032).
         for (long f = 0; f < nf; f++) {
@@ -1096,6 +1127,7 @@ void conv_flux_source(const Config& c, const int* n, const double* dx, double dt
             prim_from_char(c, a, pr, wc, vc);
             for (int e = 0; e < neq; e++) Vp[(size_t)e * nf + f] = vc[e];
         }
+        HMRO_PHASE(HMRO_PH_BOUNDS);
         for (long f = 0; f < nf; f++) {
             T vc[16];
             for (int e = 0; e < neq; e++) vc[e] = Vm[(size_t)e * nf + f];
@@ -1118,6 +1150,7 @@ void conv_flux_source(const Config& c, const int* n, const double* dx, double dt
             }
         }
 
+        HMRO_PHASE(HMRO_PH_RIEMANN);
         // Riemann fluxes, Ducros-like sensor and selection (:1038-1194).
         for (int k = fs.lo[2]; k < fs.lo[2] + fs.ext[2]; k++)
         for (int j = fs.lo[1]; j < fs.lo[1] + fs.ext[1]; j++)
@@ -1141,6 +1174,7 @@ void conv_flux_source(const Config& c, const int* n, const double* dx, double dt
             cnt_faces++;
         }
 
+        HMRO_PHASE(HMRO_PH_FLUX);
         // Flux reconstruction, :1200-1282 (3D :2370-2480).
         for (int e = 0; e < neq; e++) {
             T* Fout = flux[a * neq + e];
@@ -1162,6 +1196,7 @@ void conv_flux_source(const Config& c, const int* n, const double* dx, double dt
         }
     }
 
+    HMRO_PHASE(HMRO_PH_SOURCE);
     // Advective source (five-eqn volume fractions), :1288-1369 (3D :2623).
     if (five) {
         for (int si = 0; si < N - 1; si++) {

@@ -8,6 +8,7 @@ initial state, and divides the summed operations of one RK stage by the summed
 interior cells:
 
   python oracle/opcount_workloads.py            # all workloads, a few minutes on 8 cores
+  python oracle/opcount_workloads.py --phases   # the default workload's count by sub-phase
 
   density_wave_256     2D single species, WCNS5-JS, one 256^2 patch
   shock_interface_1024 2D five-equation, WCNS6-LD, one 1024^2 patch
@@ -73,7 +74,42 @@ def shock_interface_3lv():
         yield (2, 3, 2, 1, [1.4, 1.09], n, dx, Q)
 
 
+PHASES = ["cell data", "sensor", "projection factors", "characteristic variables", "smoothness indicators",
+          "weights + interpolation", "inverse projection", "bounds check", "Riemann (HLLC / HLLC-HLL)",
+          "flux formula", "advective source", "stage update"]
+
+
+def phases(model, dim, nsp, scheme, gam, n, dx, Q):
+    """Algorithmic FP64 operations per cell-update of one patch, by sub-phase."""
+    L = ctypes.CDLL(LIB)
+    L.hmro_count_ops.restype = ctypes.c_double
+    dp = ctypes.POINTER(ctypes.c_double)
+    Q = np.ascontiguousarray(Q, dtype=np.float64)
+    g = (ctypes.c_double * 8)(*(list(gam) + [1.4] * (8 - len(gam))))
+    nn = (ctypes.c_int * 3)(*(list(n) + [1] * (3 - len(n))))
+    d = (ctypes.c_double * 3)(*(list(dx) + [1.0] * (3 - len(dx))))
+    total = L.hmro_count_ops(model, dim, nsp, scheme, g, nn, d, Q.ctypes.data_as(dp))
+    out = (ctypes.c_double * len(PHASES))()
+    L.hmro_count_phases(nn, dim, out)
+    return total, list(out)
+
+
+def phase_table():
+    """The default workload (2D five-equation WCNS6-LD, counted at 256^2 of its problem)."""
+    from hamers_gb300 import problems as P
+    Q, dx, _ = P.shock_interface_2d(N=256, seed=1)
+    total, ph = phases(2, 2, 2, 1, [1.4, 1.67], [256, 256], dx, Q)
+    print("| sub-phase | FP64 ops per cell-update | share |")
+    print("|---|---|---|")
+    for name, v in zip(PHASES, ph):
+        print(f"| {name} | {v:.1f} | {100 * v / total:.1f} % |")
+    print(f"| total | {total:.1f} | |")
+
+
 def main():
+    if sys.argv[1:] == ["--phases"]:
+        phase_table()
+        return
     if not os.path.exists(LIB):
         import subprocess
         subprocess.check_call(["make", "-s", "-C", HERE])
