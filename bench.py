@@ -232,6 +232,7 @@ def uneven_batched_vs_patch(args, flow):
     for i, (_, _, Q) in enumerate(patches):
         lv.bind(i, Q)
     tuned = lv.autotune(dt)
+    split = lv.work_split()
     for i, (_, _, Q) in enumerate(patches):
         Q.copy_(Q0[i])
     lv.step(dt)
@@ -283,6 +284,7 @@ def uneven_batched_vs_patch(args, flow):
             "batched_over_per_patch": t_patch / t_batched,
             "batched_ms_per_step": t_batched, "per_patch_ms_per_step": t_patch,
             "launch_shape": {"threads": tuned[0], "blocks_per_sm": tuned[1]},
+            "work_split": {"chunk_blocks": split[0], "cell_phases": "grid-stride" if split[1] else "chunks"},
             "batched_roofline": roofline_fracs(cu / (t_batched * 1e-3), ALG_FP64_OPS_C3, alg_bytes(5),
                                                args.fp64_peak, args.hbm_peak),
             "per_patch_roofline": roofline_fracs(cu / (t_patch * 1e-3), ALG_FP64_OPS_C3, alg_bytes(5),
@@ -390,6 +392,7 @@ def c5_level_and_adjoint(args, flow, base=128, reps=3):
         lv.bind(p, Q)
         lv.set_periodic(p, [2, 2, 2])
     tuned = lv.autotune(dt)   # substep 0 reads the bound state and writes the level's own output
+    split = lv.work_split()
     stream = torch.cuda.current_stream()
     e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
     lv.substep(0, dt)
@@ -473,6 +476,7 @@ def c5_level_and_adjoint(args, flow, base=128, reps=3):
             "per_patch_substep_ms": t_patch, "per_patch_cell_updates_per_s": cells / (t_patch * 1e-3),
             "batched_over_per_patch": t_patch / t_batched,
             "launch_shape": {"threads": tuned[0], "blocks_per_sm": tuned[1]},
+            "work_split": {"chunk_blocks": split[0], "cell_phases": "grid-stride" if split[1] else "chunks"},
             "batched_roofline": roofline_fracs(cells / (t_batched * 1e-3), ALG_FP64_OPS_C5, alg_bytes(7, (0,)),
                                                args.fp64_peak, args.hbm_peak),
             "per_patch_roofline": roofline_fracs(cells / (t_patch * 1e-3), ALG_FP64_OPS_C5, alg_bytes(7, (0,)),
@@ -804,10 +808,12 @@ def main():
         lv.bind(0, Q)
         lv.set_periodic(0, [0, 1])
         tuned = lv.autotune(dt)
+        split = lv.work_split()
         launches_per_substep = 1
     else:
         lv = PatchDriver(flow, rec, n, dx, Q, [0, 1])
         tuned = (128, None)
+        split = None
         launches_per_substep = 6
     Q.copy_(Q0)
 
@@ -878,7 +884,9 @@ def main():
         "form": {"form": ("batched persistent kernel, one CUDA graph per substep" if args.form == "batched"
                           else "per-patch kernels (fill, cells, sensor, faces x/y, update) per substep"),
                  "precision": args.precision,
-                 "launch_shape": {"threads": tuned[0], "blocks_per_sm": tuned[1]}},
+                 "launch_shape": {"threads": tuned[0], "blocks_per_sm": tuned[1]},
+                 "work_split": None if split is None else {"chunk_blocks": split[0],
+                                                           "cell_phases": "grid-stride" if split[1] else "chunks"}},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": state_bytes,
                 "d2h_bytes_per_step": state_bytes,
                 "note": "every step copies the host state in from pinned memory, advances it and copies the "
