@@ -32,13 +32,14 @@ HMR_WCNS6_CU_M2_HLLC_HLL = 3
 HMR_DIFFUSIVE_NONE = 0
 HMR_MIDPOINT_SECOND_ORDER = 2
 HMR_MIDPOINT_FOURTH_ORDER = 4
+HMR_MIDPOINT_SIXTH_ORDER = 6
 HMR_PRECISION_FAST = 0
 HMR_PRECISION_EXACT = 1
 
 # Every symbol include/hmr.h declares.
 EXPORTS = [
     "hmr_config_default", "hmr_ctx_create", "hmr_ctx_destroy", "hmr_num_equations", "hmr_num_components",
-    "hmr_num_ghosts", "hmr_ctx_reserve", "hmr_read_counters", "hmr_conv_flux_source_patch",
+    "hmr_num_ghosts", "hmr_num_patch_ghosts", "hmr_ctx_reserve", "hmr_read_counters", "hmr_conv_flux_source_patch",
     "hmr_rk_stage_patch", "hmr_rk_substep_patch", "hmr_fill_ghosts_patch", "hmr_level_create",
     "hmr_level_destroy", "hmr_level_bind_state", "hmr_level_set_periodic", "hmr_level_state",
     "hmr_level_substep", "hmr_level_step", "hmr_level_check", "hmr_level_barrier_diagnostic", "hmr_level_autotune", "hmr_level_set_launch",
@@ -120,6 +121,7 @@ def load():
     L.hmr_num_equations.argtypes = [vp]
     L.hmr_num_components.argtypes = [vp]
     L.hmr_num_ghosts.argtypes = [vp]
+    L.hmr_num_patch_ghosts.argtypes = [vp]
     L.hmr_ctx_reserve.argtypes = [vp, gp]
     L.hmr_read_counters.argtypes = [vp, ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_int]
     L.hmr_conv_flux_source_patch.argtypes = [vp, gp, DPP, ctypes.c_double, DPP, DPP, vp]

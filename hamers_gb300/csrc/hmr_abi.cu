@@ -74,14 +74,38 @@ static int cuda_status(cudaError_t e) { return e == cudaSuccess ? HMR_OK : (int)
 
 static inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
-static Geom make_geom(int dim, const hmr_patch_geometry* pg) {
+// Ghost width of a context's patch arrays: the larger of the convective (4) and diffusive
+// widths, as NavierStokes.cpp:317-349 sizes them; the sixth-order midpoint diffusive flux
+// needs 5 (DiffusiveFluxReconstructorMidpointSixthOrder.cpp:22), the others at most 3.
+static int patch_ghosts(const Variant& v) { return v.dorder == HMR_MIDPOINT_SIXTH_ORDER ? 5 : GHOST; }
+
+// Half-width of the diffusive midpoint set (faces -W .. n + W): 2 at sixth order, else 1.
+static int diff_half_width(const Variant& v) { return v.dorder == HMR_MIDPOINT_SIXTH_ORDER ? 2 : 1; }
+
+static Geom make_geom(int dim, const hmr_patch_geometry* pg, int gh) {
     Geom g;
+    g.gh = gh;
     for (int d = 0; d < 3; d++) {
         g.n[d] = d < dim ? pg->n[d] : 1;
-        g.G[d] = d < dim ? g.n[d] + 2 * GHOST : 1;
+        g.G[d] = d < dim ? g.n[d] + 2 * gh : 1;
         g.dx[d] = d < dim ? pg->dx[d] : 1.0;
     }
     return g;
+}
+
+// First momentum component of the conserved variables: single species (rho, rho u, E) 1;
+// four- and five-equation models (partial densities first) the number of species.
+static int momentum0(const Variant& v) { return v.model == SINGLE_SPECIES ? 1 : v.nsp; }
+
+// Fill modes of a patch's axes (hmr_fill_mode); a reflecting wall mirrors its gh ghost cells,
+// so the patch needs at least that many along the axis.
+static bool valid_fill_modes(int dim, const hmr_patch_geometry* pg, const int* mode, int gh) {
+    if (!mode) return false;
+    for (int a = 0; a < dim; a++) {
+        if (mode[a] < HMR_FILL_ZERO_GRADIENT || mode[a] > HMR_FILL_REFLECT) return false;
+        if (mode[a] == HMR_FILL_REFLECT && pg->n[a] < gh) return false;
+    }
+    return true;
 }
 
 static bool valid_geom(int dim, const hmr_patch_geometry* pg) {
@@ -91,7 +115,7 @@ static bool valid_geom(int dim, const hmr_patch_geometry* pg) {
         if (!(pg->dx[d] > 0.0)) return false;
     }
     long cells = 1;
-    for (int d = 0; d < dim; d++) cells *= (long)pg->n[d] + 2 * GHOST;
+    for (int d = 0; d < dim; d++) cells *= (long)pg->n[d] + 2 * GHOST_MAX;
     return cells < (1L << 40);
 }
 
@@ -104,7 +128,7 @@ static size_t scratch_doubles(const hmr_ctx* c, const Geom& g) {
     if (c->P.dorder) {
         // NavierStokes: temperature, node velocity gradient, midpoint diffusive fluxes
         s += (size_t)(1 + c->v.dim * c->v.dim) * nc;
-        for (int a = 0; a < c->v.dim; a++) s += (size_t)c->neq * nface_of(g, a);
+        for (int a = 0; a < c->v.dim; a++) s += (size_t)c->neq * nface_w(g, a, diff_half_width(c->v));
     }
     return s + 64;
 }
@@ -140,7 +164,7 @@ static Scratch carve_scratch(const hmr_ctx* c, const Geom& g, double* base) {
     if (c->P.dorder) {
         S.Td = p; p += nc;
         S.Gd = p; p += (size_t)c->v.dim * c->v.dim * nc;
-        for (int a = 0; a < c->v.dim; a++) { S.Fd[a] = p; p += (size_t)c->neq * nface_of(g, a); }
+        for (int a = 0; a < c->v.dim; a++) { S.Fd[a] = p; p += (size_t)c->neq * nface_w(g, a, diff_half_width(c->v)); }
     }
     return S;
 }
@@ -291,10 +315,11 @@ int hmr_ctx_destroy(hmr_ctx* c) {
 int hmr_num_equations(const hmr_ctx* c) { return c ? c->neq : HMR_ERR_ARGUMENT; }
 int hmr_num_components(const hmr_ctx* c) { return c ? c->ncomp : HMR_ERR_ARGUMENT; }
 int hmr_num_ghosts(const hmr_ctx* c) { return c ? GHOST : HMR_ERR_ARGUMENT; }
+int hmr_num_patch_ghosts(const hmr_ctx* c) { return c ? patch_ghosts(c->v) : HMR_ERR_ARGUMENT; }
 
 int hmr_ctx_reserve(hmr_ctx* c, const hmr_patch_geometry* pg) {
     if (!c || !valid_geom(c->v.dim, pg)) return HMR_ERR_ARGUMENT;
-    return ensure_scratch(c, make_geom(c->v.dim, pg));
+    return ensure_scratch(c, make_geom(c->v.dim, pg, patch_ghosts(c->v)));
 }
 
 int hmr_read_counters(hmr_ctx* c, unsigned long long out[2], int reset) {
@@ -333,7 +358,7 @@ int hmr_conv_flux_source_patch(hmr_ctx* c, const hmr_patch_geometry* pg, const d
     if (!load_comp(q, Q, c->ncomp)) return HMR_ERR_ARGUMENT;
     if (!load_flux(F, flux, c->v.dim * c->neq)) return HMR_ERR_ARGUMENT;
     if (!load_comp(S, source, c->neq)) return HMR_ERR_ARGUMENT;
-    const Geom g = make_geom(c->v.dim, pg);
+    const Geom g = make_geom(c->v.dim, pg, patch_ghosts(c->v));
     cudaStream_t st = as_stream(stream);
     Scratch scr;
     int r = patch_faces(c, g, q, scr, st);
@@ -366,7 +391,7 @@ int hmr_rk_substep_patch(hmr_ctx* c, const hmr_patch_geometry* pg, int stage, co
     for (int e = 0; e < 3 * MAX_COMP; e++) U.Fout.p[e] = nullptr;
     for (int e = 0; e < MAX_COMP; e++) U.Sout.p[e] = nullptr;
     U.dorder = c->P.dorder;
-    const Geom g = make_geom(c->v.dim, pg);
+    const Geom g = make_geom(c->v.dim, pg, patch_ghosts(c->v));
     cudaStream_t st = as_stream(stream);
     Scratch scr;
     int r = patch_faces(c, g, U.Qint[stage], scr, st, c->P.dorder != 0);
@@ -382,7 +407,7 @@ int hmr_diff_flux_patch(hmr_ctx* c, const hmr_patch_geometry* pg, const double* 
     FluxComp F;
     if (!load_comp(q, Q, c->ncomp)) return HMR_ERR_ARGUMENT;
     if (!load_flux(F, flux, c->v.dim * c->neq)) return HMR_ERR_ARGUMENT;
-    const Geom g = make_geom(c->v.dim, pg);
+    const Geom g = make_geom(c->v.dim, pg, patch_ghosts(c->v));
     cudaStream_t st = as_stream(stream);
     int r = ensure_scratch(c, g);
     if (r) return r;
@@ -421,7 +446,7 @@ int hmr_rk_stage_ns_patch(hmr_ctx* c, const hmr_patch_geometry* pg, int ncoef, c
         for (int e = 0; e < 3 * MAX_COMP; e++) Fa.p[e] = Da.p[e] = nullptr;
         for (int e = 0; e < MAX_COMP; e++) Sa.p[e] = nullptr;
     }
-    const Geom g = make_geom(c->v.dim, pg);
+    const Geom g = make_geom(c->v.dim, pg, patch_ghosts(c->v));
     return hmr_cells::launch_rk_stage(c->v, g, ncoef, alpha, beta, acc ? gamma : nullptr, Qi, Fi, Si, Qo, Fa, Sa,
                                       as_stream(stream), Di, acc ? &Da : nullptr);
 }
@@ -448,7 +473,7 @@ int hmr_rk_stage_patch(hmr_ctx* c, const hmr_patch_geometry* pg, int ncoef, cons
         for (int e = 0; e < 3 * MAX_COMP; e++) Fa.p[e] = nullptr;
         for (int e = 0; e < MAX_COMP; e++) Sa.p[e] = nullptr;
     }
-    const Geom g = make_geom(c->v.dim, pg);
+    const Geom g = make_geom(c->v.dim, pg, patch_ghosts(c->v));
     return hmr_cells::launch_rk_stage(c->v, g, ncoef, alpha, beta, acc ? gamma : nullptr, Qi, Fi, Si, Qo, Fa, Sa,
                                       as_stream(stream));
 }
@@ -458,6 +483,7 @@ int hmr_rk_substep_vjp_patch(hmr_ctx* c, const hmr_patch_geometry* pg, int stage
                              const double* const* Qbar_out, double* const* const* Qbar_int, void* stream) {
     if (!c || !valid_geom(c->v.dim, pg) || !alpha || !Q_int || !Qbar_out || !Qbar_int || stage < 0 || stage > 2)
         return HMR_ERR_ARGUMENT;
+    if (c->P.dorder == HMR_MIDPOINT_SIXTH_ORDER) return HMR_ERR_UNSUPPORTED;   // reverse stencils: orders 2, 4
     VjpArgs A;
     std::memset(&A, 0, sizeof(A));
     if (!load_comp(A.Qs, Q_int[stage], c->ncomp)) return HMR_ERR_ARGUMENT;
@@ -468,7 +494,7 @@ int hmr_rk_substep_vjp_patch(hmr_ctx* c, const hmr_patch_geometry* pg, int stage
     A.nst = stage + 1;
     A.beta = beta;
     A.dt = dt;
-    const Geom g = make_geom(c->v.dim, pg);
+    const Geom g = make_geom(c->v.dim, pg, patch_ghosts(c->v));
     cudaStream_t st = as_stream(stream);
     int r = ensure_scratch(c, g);
     if (r) return r;
@@ -540,7 +566,7 @@ int hmr_sync_fluxes_patch(hmr_ctx* c, const hmr_patch_geometry* pg, double* cons
     if (!load_comp(q, Q, c->ncomp) || !load_flux(F, flux, c->v.dim * c->neq) || !load_comp(S, source, c->neq))
         return HMR_ERR_ARGUMENT;
     if (diff_flux && !load_flux(D, diff_flux, c->v.dim * c->neq)) return HMR_ERR_ARGUMENT;
-    const Geom g = make_geom(c->v.dim, pg);
+    const Geom g = make_geom(c->v.dim, pg, patch_ghosts(c->v));
     return hmr_cells::launch_sync(c->v, g, q, F, diff_flux ? &D : nullptr, S, as_stream(stream));
 }
 
@@ -552,8 +578,8 @@ static int coarsen_args(const hmr_ctx* c, const hmr_patch_geometry* coarse, cons
     if (!valid_geom(dim, coarse) || !valid_geom(dim, fine) || !coarse_lo || !fine_lo || !ratio)
         return HMR_ERR_ARGUMENT;
     std::memset(&C, 0, sizeof(C));
-    C.gc = make_geom(dim, coarse);
-    C.gf = make_geom(dim, fine);
+    C.gc = make_geom(dim, coarse, patch_ghosts(c->v));
+    C.gf = make_geom(dim, fine, patch_ghosts(c->v));
     for (int d = 0; d < 3; d++) {
         if (d >= dim) {
             C.r[d] = 1; C.clo[d] = C.flo[d] = 0; C.lo[d] = 0; C.hi[d] = 1;
@@ -619,27 +645,27 @@ int hmr_spectral_radius_patch(hmr_ctx* c, const hmr_patch_geometry* pg, const do
     if (!c || !valid_geom(c->v.dim, pg) || !d_max) return HMR_ERR_ARGUMENT;
     Comp q;
     if (!load_comp(q, Q, c->ncomp)) return HMR_ERR_ARGUMENT;
-    const Geom g = make_geom(c->v.dim, pg);
+    const Geom g = make_geom(c->v.dim, pg, patch_ghosts(c->v));
     return hmr_cells::launch_spectral_patch(c->v, c->P, g, q, reinterpret_cast<unsigned long long*>(d_max),
                                             as_stream(stream));
 }
 
 int hmr_fill_ghosts_vjp_patch(hmr_ctx* c, const hmr_patch_geometry* pg, double* const* Qbar, const int* periodic,
                               void* stream) {
-    if (!c || !valid_geom(c->v.dim, pg)) return HMR_ERR_ARGUMENT;
+    if (!c || !valid_geom(c->v.dim, pg) || !valid_fill_modes(c->v.dim, pg, periodic, patch_ghosts(c->v))) return HMR_ERR_ARGUMENT;
     Comp q;
     if (!load_comp(q, Qbar, c->ncomp)) return HMR_ERR_ARGUMENT;
-    const Geom g = make_geom(c->v.dim, pg);
-    return hmr_cells::launch_fill_vjp(c->v.dim, g, q, c->ncomp, periodic, as_stream(stream));
+    const Geom g = make_geom(c->v.dim, pg, patch_ghosts(c->v));
+    return hmr_cells::launch_fill_vjp(c->v.dim, g, q, c->ncomp, periodic, momentum0(c->v), as_stream(stream));
 }
 
 int hmr_fill_ghosts_patch(hmr_ctx* c, const hmr_patch_geometry* pg, double* const* Q, const int* periodic,
                           void* stream) {
-    if (!c || !valid_geom(c->v.dim, pg)) return HMR_ERR_ARGUMENT;
+    if (!c || !valid_geom(c->v.dim, pg) || !valid_fill_modes(c->v.dim, pg, periodic, patch_ghosts(c->v))) return HMR_ERR_ARGUMENT;
     Comp q;
     if (!load_comp(q, Q, c->ncomp)) return HMR_ERR_ARGUMENT;
-    const Geom g = make_geom(c->v.dim, pg);
-    return hmr_cells::launch_fill(c->v.dim, g, q, c->ncomp, periodic, as_stream(stream));
+    const Geom g = make_geom(c->v.dim, pg, patch_ghosts(c->v));
+    return hmr_cells::launch_fill(c->v.dim, g, q, c->ncomp, periodic, momentum0(c->v), as_stream(stream));
 }
 
 }  // extern "C"
@@ -753,6 +779,7 @@ extern "C" {
 int hmr_level_create(hmr_ctx* c, int np, const hmr_patch_geometry* geoms, hmr_level** out) {
     if (!c || np < 1 || !geoms || !out) return HMR_ERR_ARGUMENT;
     *out = nullptr;
+    if (patch_ghosts(c->v) != GHOST) return HMR_ERR_UNSUPPORTED;   // levels carry 4 ghost cells
     for (int p = 0; p < np; p++)
         if (!valid_geom(c->v.dim, &geoms[p])) return HMR_ERR_ARGUMENT;
     hmr_level* lv = new (std::nothrow) hmr_level();
@@ -764,7 +791,7 @@ int hmr_level_create(hmr_ctx* c, int np, const hmr_patch_geometry* geoms, hmr_le
     long off_fill = 0, off_cells = 0, off_sensor = 0, off_face[3] = {0, 0, 0}, off_update = 0;
     lv->work.resize(np);
     for (int p = 0; p < np; p++) {
-        const Geom g = make_geom(c->v.dim, &geoms[p]);
+        const Geom g = make_geom(c->v.dim, &geoms[p], GHOST);
         lv->geoms.push_back(g);
         lv->state_off.push_back(state_tot);
         state_tot += (size_t)2 * c->ncomp * ncell_of(g);
@@ -827,6 +854,7 @@ int hmr_level_create(hmr_ctx* c, int np, const hmr_patch_geometry* geoms, hmr_le
     lv->L.barrier_extra = 0;
     lv->L.chunk_mult = 1;
     lv->L.split_mode = 0;
+    lv->L.mom0 = momentum0(c->v);
     lv->threads = 128;
     int r = level_max_blocks(lv, lv->threads, &lv->blocks);
     if (r || lv->blocks < 1) {
@@ -868,7 +896,10 @@ int hmr_level_bind_state(hmr_level* lv, int p, double* const* comps) {
 int hmr_level_set_periodic(hmr_level* lv, int p, const int* periodic) {
     if (!lv || p < 0 || p >= lv->npatch || !periodic) return HMR_ERR_ARGUMENT;
     for (int a = 0; a < 3; a++) {
-        if (a < lv->ctx->v.dim && (periodic[a] < 0 || periodic[a] > 2)) return HMR_ERR_ARGUMENT;
+        if (a < lv->ctx->v.dim && (periodic[a] < HMR_FILL_ZERO_GRADIENT || periodic[a] > HMR_FILL_REFLECT))
+            return HMR_ERR_ARGUMENT;
+        if (a < lv->ctx->v.dim && periodic[a] == HMR_FILL_REFLECT && lv->geoms[p].n[a] < GHOST)
+            return HMR_ERR_ARGUMENT;
         lv->work[p].periodic[a] = a < lv->ctx->v.dim ? periodic[a] : 0;
     }
     lv->dirty = true;
@@ -880,7 +911,10 @@ int hmr_level_set_layout(hmr_level* lv, const int* lo, const int* domain, const 
     const int dim = lv->ctx->v.dim;
     int dom[3] = {1, 1, 1}, per[3] = {0, 0, 0};
     for (int a = 0; a < dim; a++) {
-        if (domain[a] < 1 || periodic[a] < 0 || periodic[a] > 1) return HMR_ERR_ARGUMENT;
+        if (domain[a] < 1 || (periodic[a] != 0 && periodic[a] != 1 && periodic[a] != HMR_FILL_REFLECT))
+            return HMR_ERR_ARGUMENT;
+        // the mirror images of a reflecting wall's ghost cells lie in the domain
+        if (periodic[a] == HMR_FILL_REFLECT && domain[a] < GHOST) return HMR_ERR_ARGUMENT;
         dom[a] = domain[a];
         per[a] = periodic[a];
     }
@@ -906,7 +940,7 @@ int hmr_level_set_layout(hmr_level* lv, const int* lo, const int* domain, const 
     long total = 0;
     int kmax[3] = {0, 0, 0};
     for (int a = 0; a < dim; a++)
-        if (per[a]) kmax[a] = (GHOST + dom[a] - 1) / dom[a];
+        if (per[a] == 1) kmax[a] = (GHOST + dom[a] - 1) / dom[a];
     for (int p = 0; p < np; p++) {
         int glo[3], ghi[3];
         for (int a = 0; a < 3; a++) {

@@ -62,10 +62,10 @@ struct Periodic {
 };
 
 template <int DIM>
-__global__ void __launch_bounds__(THREADS) fill_kernel(Geom g, Comp Q, int ncomp, Periodic per) {
+__global__ void __launch_bounds__(THREADS) fill_kernel(Geom g, Comp Q, int ncomp, Periodic per, int mom0) {
     const long n = ncell_of(g);
     for (long x = (long)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (long)gridDim.x * blockDim.x)
-        fill_item<DIM>(g, Q, ncomp, per.p, x);
+        fill_item<DIM>(g, Q, ncomp, per.p, x, mom0);
 }
 
 int launch_cells(const Variant& v, const Params& P, const Geom& g, const Comp& Q, const Scratch& S,
@@ -86,11 +86,11 @@ int launch_sensor(const Variant& v, const Geom& g, const Scratch& S, cudaStream_
     });
 }
 
-int launch_fill(int dim, const Geom& g, const Comp& Q, int ncomp, const int* periodic, cudaStream_t st) {
+int launch_fill(int dim, const Geom& g, const Comp& Q, int ncomp, const int* periodic, int mom0, cudaStream_t st) {
     Periodic per;
     for (int a = 0; a < 3; a++) per.p[a] = periodic ? periodic[a] : 0;
-    if (dim == 2) fill_kernel<2><<<grid_for(ncell_of(g)), THREADS, 0, st>>>(g, Q, ncomp, per);
-    else fill_kernel<3><<<grid_for(ncell_of(g)), THREADS, 0, st>>>(g, Q, ncomp, per);
+    if (dim == 2) fill_kernel<2><<<grid_for(ncell_of(g)), THREADS, 0, st>>>(g, Q, ncomp, per, mom0);
+    else fill_kernel<3><<<grid_for(ncell_of(g)), THREADS, 0, st>>>(g, Q, ncomp, per, mom0);
     return (int)cudaPeekAtLastError();
 }
 
@@ -101,11 +101,13 @@ int launch_fill(int dim, const Geom& g, const Comp& Q, int ncomp, const int* per
 __device__ __forceinline__ int fill_src(int v, int n, int periodic) {
     if (v >= 0 && v < n) return v;
     if (periodic == 1) return ((v % n) + n) % n;
+    if (periodic == 3) return v < 0 ? -v - 1 : 2 * n - 1 - v;
     return v < 0 ? 0 : n - 1;
 }
 
 template <int DIM>
-__global__ void __launch_bounds__(THREADS) fill_vjp_gather_kernel(Geom g, Comp Qb, int ncomp, Periodic per) {
+__global__ void __launch_bounds__(THREADS) fill_vjp_gather_kernel(Geom g, Comp Qb, int ncomp, Periodic per,
+                                                                  int mom0) {
     const long n = ninterior_of(g);
     for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
         const int c[3] = {(int)(t % g.n[0]), (int)((t / g.n[0]) % g.n[1]),
@@ -116,7 +118,7 @@ __global__ void __launch_bounds__(THREADS) fill_vjp_gather_kernel(Geom g, Comp Q
             pre[a][0] = c[a];
             np[a] = 1;
             if (a >= DIM || per.p[a] == 2) continue;   // provided ghosts are not copies of this cell
-            for (int v = -GHOST; v < g.n[a] + GHOST; v++) {
+            for (int v = -g.gh; v < g.n[a] + g.gh; v++) {
                 if (v >= 0 && v < g.n[a]) continue;
                 if (fill_src(v, g.n[a], per.p[a]) == c[a] && np[a] < 9) pre[a][np[a]++] = v;
             }
@@ -128,7 +130,11 @@ __global__ void __launch_bounds__(THREADS) fill_vjp_gather_kernel(Geom g, Comp Q
                 for (int a1 = 0; a1 < np[1]; a1++)
                     for (int a0 = 0; a0 < np[0]; a0++) {
                         if (a0 == 0 && a1 == 0 && a2 == 0) continue;
-                        acc += Qb.p[e][cidx<DIM>(g, pre[0][a0], pre[1][a1], pre[2][a2])];
+                        const double v = Qb.p[e][cidx<DIM>(g, pre[0][a0], pre[1][a1], pre[2][a2])];
+                        // a reflecting wall negated the normal momentum of the copy
+                        const bool flip = (per.p[0] == 3 && a0 > 0 && e == mom0) != (per.p[1] == 3 && a1 > 0 && e == mom0 + 1) !=
+                                          (DIM == 3 && per.p[2] == 3 && a2 > 0 && e == mom0 + 2);
+                        acc += flip ? -v : v;
                     }
             if (acc != 0.0) Qb.p[e][y] += acc;
         }
@@ -139,8 +145,8 @@ template <int DIM>
 __global__ void __launch_bounds__(THREADS) fill_vjp_clear_kernel(Geom g, Comp Qb, int ncomp, Periodic per) {
     const long n = ncell_of(g);
     for (long x = (long)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (long)gridDim.x * blockDim.x) {
-        const int c[3] = {(int)(x % g.G[0]) - GHOST, (int)((x / g.G[0]) % g.G[1]) - GHOST,
-                          DIM == 3 ? (int)(x / ((long)g.G[0] * g.G[1])) - GHOST : 0};
+        const int c[3] = {(int)(x % g.G[0]) - g.gh, (int)((x / g.G[0]) % g.G[1]) - g.gh,
+                          DIM == 3 ? (int)(x / ((long)g.G[0] * g.G[1])) - g.gh : 0};
         bool inside = true, provided = false;
         for (int a = 0; a < DIM; a++) {
             if (c[a] < 0 || c[a] >= g.n[a]) {
@@ -154,14 +160,15 @@ __global__ void __launch_bounds__(THREADS) fill_vjp_clear_kernel(Geom g, Comp Qb
     }
 }
 
-int launch_fill_vjp(int dim, const Geom& g, const Comp& Qb, int ncomp, const int* periodic, cudaStream_t st) {
+int launch_fill_vjp(int dim, const Geom& g, const Comp& Qb, int ncomp, const int* periodic, int mom0,
+                    cudaStream_t st) {
     Periodic per;
     for (int a = 0; a < 3; a++) per.p[a] = periodic ? periodic[a] : 0;
     if (dim == 2) {
-        fill_vjp_gather_kernel<2><<<grid_for(ninterior_of(g)), THREADS, 0, st>>>(g, Qb, ncomp, per);
+        fill_vjp_gather_kernel<2><<<grid_for(ninterior_of(g)), THREADS, 0, st>>>(g, Qb, ncomp, per, mom0);
         fill_vjp_clear_kernel<2><<<grid_for(ncell_of(g)), THREADS, 0, st>>>(g, Qb, ncomp, per);
     } else {
-        fill_vjp_gather_kernel<3><<<grid_for(ninterior_of(g)), THREADS, 0, st>>>(g, Qb, ncomp, per);
+        fill_vjp_gather_kernel<3><<<grid_for(ninterior_of(g)), THREADS, 0, st>>>(g, Qb, ncomp, per, mom0);
         fill_vjp_clear_kernel<3><<<grid_for(ncell_of(g)), THREADS, 0, st>>>(g, Qb, ncomp, per);
     }
     return (int)cudaPeekAtLastError();
@@ -620,8 +627,8 @@ __global__ void __launch_bounds__(THREADS) refine_ghosts_kernel(CoarsenArgs C, C
                                                                Comp Qf, int ncomp) {
     const long nfc = ncell_of(C.gf);
     for (long x = (long)blockIdx.x * blockDim.x + threadIdx.x; x < nfc; x += (long)gridDim.x * blockDim.x) {
-        const int f[3] = {(int)(x % C.gf.G[0]) - GHOST, (int)((x / C.gf.G[0]) % C.gf.G[1]) - GHOST,
-                          DIM == 3 ? (int)(x / ((long)C.gf.G[0] * C.gf.G[1])) - GHOST : 0};
+        const int f[3] = {(int)(x % C.gf.G[0]) - C.gf.gh, (int)((x / C.gf.G[0]) % C.gf.G[1]) - C.gf.gh,
+                          DIM == 3 ? (int)(x / ((long)C.gf.G[0] * C.gf.G[1])) - C.gf.gh : 0};
         bool inside = true, covered = true;
         int c[3] = {0, 0, 0}, lev[3] = {0, 0, 0};
 #pragma unroll
@@ -667,12 +674,14 @@ __global__ void __launch_bounds__(THREADS) diff_grad_kernel(Params P, Geom g, Sc
 }
 
 int launch_diff_grad(const Variant& v, const Params& P, const Geom& g, const Scratch& S, cudaStream_t st) {
-    if (v.model != SINGLE_SPECIES || (P.dorder != 2 && P.dorder != 4)) return -2;
+    if (v.model != SINGLE_SPECIES || (P.dorder != 2 && P.dorder != 4 && P.dorder != 6)) return -2;
     const int b = grid_for(ncell_of(g));
     if (v.dim == 2 && P.dorder == 2) diff_grad_kernel<2, 2><<<b, THREADS, 0, st>>>(P, g, S);
-    else if (v.dim == 2) diff_grad_kernel<2, 4><<<b, THREADS, 0, st>>>(P, g, S);
+    else if (v.dim == 2 && P.dorder == 4) diff_grad_kernel<2, 4><<<b, THREADS, 0, st>>>(P, g, S);
+    else if (v.dim == 2) diff_grad_kernel<2, 6><<<b, THREADS, 0, st>>>(P, g, S);
     else if (P.dorder == 2) diff_grad_kernel<3, 2><<<b, THREADS, 0, st>>>(P, g, S);
-    else diff_grad_kernel<3, 4><<<b, THREADS, 0, st>>>(P, g, S);
+    else if (P.dorder == 4) diff_grad_kernel<3, 4><<<b, THREADS, 0, st>>>(P, g, S);
+    else diff_grad_kernel<3, 6><<<b, THREADS, 0, st>>>(P, g, S);
     return (int)cudaPeekAtLastError();
 }
 

@@ -27,7 +27,7 @@ static inline int grid_for(long items) {
 
 template <int DIM, int ORD, int A>
 __global__ void __launch_bounds__(DIFF_THREADS) diff_mid_kernel(Params P, Geom g, Scratch S) {
-    const long nf = nface_of(g, A);
+    const long nf = nface_w(g, A, diff_w<ORD>());
     for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < nf; t += (long)gridDim.x * blockDim.x)
         diff_mid_item<DIM, ORD, A>(P, g, S, t);
 }
@@ -41,7 +41,7 @@ __global__ void __launch_bounds__(DIFF_THREADS) diff_out_kernel(Geom g, Scratch 
     const long fst = A == 0 ? 1 : (A == 1 ? (long)g.n[0] : (long)g.n[0] * g.n[1]);
     for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < nout; t += (long)gridDim.x * blockDim.x) {
         const int i = (int)(t % e0), j = (int)((t / e0) % e1), k = DIM == 3 ? (int)(t / ((long)e0 * e1)) : 0;
-        const long f = fidx<A>(g, i, j, k);
+        const long f = dfidx<A, diff_w<ORD>()>(g, i, j, k);
 #pragma unroll
         for (int e = 0; e < NEQ; e++) F.p[A * NEQ + e][t] = diff_face<ORD, A>(g, S, dt, f, fst, e);
     }
@@ -49,9 +49,11 @@ __global__ void __launch_bounds__(DIFF_THREADS) diff_out_kernel(Geom g, Scratch 
 
 template <int DIM, int ORD>
 static void mid_axes(const Params& P, const Geom& g, const Scratch& S, cudaStream_t st) {
-    diff_mid_kernel<DIM, ORD, 0><<<grid_for(nface_of(g, 0)), DIFF_THREADS, 0, st>>>(P, g, S);
-    diff_mid_kernel<DIM, ORD, 1><<<grid_for(nface_of(g, 1)), DIFF_THREADS, 0, st>>>(P, g, S);
-    if constexpr (DIM == 3) diff_mid_kernel<DIM, ORD, 2><<<grid_for(nface_of(g, 2)), DIFF_THREADS, 0, st>>>(P, g, S);
+    constexpr int W = diff_w<ORD>();
+    diff_mid_kernel<DIM, ORD, 0><<<grid_for(nface_w(g, 0, W)), DIFF_THREADS, 0, st>>>(P, g, S);
+    diff_mid_kernel<DIM, ORD, 1><<<grid_for(nface_w(g, 1, W)), DIFF_THREADS, 0, st>>>(P, g, S);
+    if constexpr (DIM == 3)
+        diff_mid_kernel<DIM, ORD, 2><<<grid_for(nface_w(g, 2, W)), DIFF_THREADS, 0, st>>>(P, g, S);
 }
 
 template <int DIM, int ORD>
@@ -67,21 +69,32 @@ static void out_axes(const Geom& g, const Scratch& S, double dt, const FluxComp&
 }
 
 int launch_diff_mid(const Variant& v, const Params& P, const Geom& g, const Scratch& S, cudaStream_t st) {
-    if (v.model != SINGLE_SPECIES || (P.dorder != 2 && P.dorder != 4)) return -2;
-    if (v.dim == 2 && P.dorder == 2) mid_axes<2, 2>(P, g, S, st);
-    else if (v.dim == 2) mid_axes<2, 4>(P, g, S, st);
-    else if (P.dorder == 2) mid_axes<3, 2>(P, g, S, st);
-    else mid_axes<3, 4>(P, g, S, st);
+    if (v.model != SINGLE_SPECIES || (P.dorder != 2 && P.dorder != 4 && P.dorder != 6)) return -2;
+    if (P.dorder == 6 && g.gh < 5) return -2;
+    if (v.dim == 2) {
+        if (P.dorder == 2) mid_axes<2, 2>(P, g, S, st);
+        else if (P.dorder == 4) mid_axes<2, 4>(P, g, S, st);
+        else mid_axes<2, 6>(P, g, S, st);
+    } else {
+        if (P.dorder == 2) mid_axes<3, 2>(P, g, S, st);
+        else if (P.dorder == 4) mid_axes<3, 4>(P, g, S, st);
+        else mid_axes<3, 6>(P, g, S, st);
+    }
     return (int)cudaPeekAtLastError();
 }
 
 int launch_diff_faces_out(const Variant& v, const Params& P, const Geom& g, const Scratch& S, double dt,
                           const FluxComp& F, cudaStream_t st) {
-    if (v.model != SINGLE_SPECIES || (P.dorder != 2 && P.dorder != 4)) return -2;
-    if (v.dim == 2 && P.dorder == 2) out_axes<2, 2>(g, S, dt, F, st);
-    else if (v.dim == 2) out_axes<2, 4>(g, S, dt, F, st);
-    else if (P.dorder == 2) out_axes<3, 2>(g, S, dt, F, st);
-    else out_axes<3, 4>(g, S, dt, F, st);
+    if (v.model != SINGLE_SPECIES || (P.dorder != 2 && P.dorder != 4 && P.dorder != 6)) return -2;
+    if (v.dim == 2) {
+        if (P.dorder == 2) out_axes<2, 2>(g, S, dt, F, st);
+        else if (P.dorder == 4) out_axes<2, 4>(g, S, dt, F, st);
+        else out_axes<2, 6>(g, S, dt, F, st);
+    } else {
+        if (P.dorder == 2) out_axes<3, 2>(g, S, dt, F, st);
+        else if (P.dorder == 4) out_axes<3, 4>(g, S, dt, F, st);
+        else out_axes<3, 6>(g, S, dt, F, st);
+    }
     return (int)cudaPeekAtLastError();
 }
 

@@ -161,9 +161,9 @@ __device__ __forceinline__ void diff_mid_bwd_item(const Params& P, const Geom& g
 // Cell coordinates (interior origin) of ghost-box cell x.
 template <int DIM>
 __device__ __forceinline__ void diff_cell_coords(const Geom& g, long x, int (&c)[3]) {
-    c[0] = (int)(x % g.G[0]) - GHOST;
-    c[1] = (int)((x / g.G[0]) % g.G[1]) - GHOST;
-    c[2] = DIM == 3 ? (int)(x / ((long)g.G[0] * g.G[1])) - GHOST : 0;
+    c[0] = (int)(x % g.G[0]) - g.gh;
+    c[1] = (int)((x / g.G[0]) % g.G[1]) - g.gh;
+    c[2] = DIM == 3 ? (int)(x / ((long)g.G[0] * g.G[1])) - g.gh : 0;
 }
 
 // Adjoint of the node gradient Gd_{d,c} at cell x: the midpoints of every axis A != d
@@ -235,7 +235,7 @@ __device__ __forceinline__ void diff_cell_bwd_item(const Params& P, const Geom& 
 #pragma unroll
     for (int d = 0; d < DIM; d++) {
         const long st = d == 0 ? 1 : (d == 1 ? (long)g.G[0] : (long)g.G[0] * g.G[1]);
-        const int cd = c[d] + GHOST;
+        const int cd = c[d] + g.gh;
         const double dxi = double(1)/g.dx[d];
 #pragma unroll
         for (int l = -2; l <= 2; l++) {

@@ -285,12 +285,13 @@ level_kernel(Params P, LevelArgs L) {
         HMR_BARRIER();
         for (long t = t0; t < L.total_fill; t += stride) {
             const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_fill; });
-            domain_fill_item<DIM>(W[p].g, W[p].Q[sl], L.ncomp, W[p].lo, L.dom, L.dom_periodic, t - W[p].off_fill);
+            domain_fill_item<DIM>(W[p].g, W[p].Q[sl], L.ncomp, W[p].lo, L.dom, L.dom_periodic, t - W[p].off_fill,
+                                  L.mom0);
         }
     } else {
         for (long t = t0; t < L.total_fill; t += stride) {
             const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_fill; });
-            fill_item<DIM>(W[p].g, W[p].Q[L.nst - 1], L.ncomp, W[p].periodic, t - W[p].off_fill);
+            fill_item<DIM>(W[p].g, W[p].Q[L.nst - 1], L.ncomp, W[p].periodic, t - W[p].off_fill, L.mom0);
         }
     }
     HMR_BARRIER();

@@ -20,12 +20,16 @@
 
 namespace hmr {
 
+// Ghost width of the WCNS56 stencils (ConvectiveFluxReconstructorWCNS56-HLLC-HLL.cpp:22); a patch's
+// arrays carry GHOST cells, or 5 with the sixth-order midpoint diffusive flux (Geom::gh).
 constexpr int GHOST = 4;
+constexpr int GHOST_MAX = 5;
 
 struct Geom {
     int n[3];       // interior cells (1 on unused axes)
-    int G[3];       // ghost-box extents
+    int G[3];       // ghost-box extents, n + 2 gh
     double dx[3];
+    int gh = GHOST; // ghost cells per side
 };
 
 struct Comp {
@@ -58,11 +62,17 @@ __host__ __device__ inline long nface_of(const Geom& g, int a) {
     return r;
 }
 __host__ __device__ inline long ninterior_of(const Geom& g) { return (long)g.n[0] * g.n[1] * g.n[2]; }
+// Midpoint set of the diffusive flux along a: faces -W .. n_a + W (W = 1, or 2 at sixth order).
+__host__ __device__ inline long nface_w(const Geom& g, int a, int W) {
+    long r = 1;
+    for (int d = 0; d < 3; d++) r *= (d == a) ? (g.n[d] + 1 + 2 * W) : g.n[d];
+    return r;
+}
 
 template <int DIM>
 __device__ __forceinline__ long cidx(const Geom& g, int i, int j, int k) {
-    const int gz = DIM == 3 ? GHOST : 0;
-    return (long)(i + GHOST) + (long)(j + GHOST) * g.G[0] + (long)(k + gz) * g.G[0] * g.G[1];
+    const int gz = DIM == 3 ? g.gh : 0;
+    return (long)(i + g.gh) + (long)(j + g.gh) * g.G[0] + (long)(k + gz) * g.G[0] * g.G[1];
 }
 
 template <int A>
@@ -70,6 +80,13 @@ __device__ __forceinline__ long fidx(const Geom& g, int i, int j, int k) {
     const int e0 = g.n[0] + (A == 0 ? 3 : 0);
     const int e1 = g.n[1] + (A == 1 ? 3 : 0);
     return (long)(i + (A == 0)) + (long)(j + (A == 1)) * e0 + (long)(k + (A == 2)) * e0 * e1;
+}
+// Index in the diffusive midpoint set of half-width W (W = 1 is fidx).
+template <int A, int W>
+__device__ __forceinline__ long dfidx(const Geom& g, int i, int j, int k) {
+    const int e0 = g.n[0] + (A == 0 ? 1 + 2 * W : 0);
+    const int e1 = g.n[1] + (A == 1 ? 1 + 2 * W : 0);
+    return (long)(i + (A == 0 ? W : 0)) + (long)(j + (A == 1 ? W : 0)) * e0 + (long)(k + (A == 2 ? W : 0)) * e0 * e1;
 }
 
 // Counters reported by the face phase.
@@ -296,7 +313,7 @@ struct UpdateArgs {
     Comp Qout;           // ghost-box arrays; interior written
     FluxComp Fout;       // optional: dt-scaled face fluxes, SAMRAI side layout (dim*NEQ arrays)
     Comp Sout;           // optional: source (interior, NEQ arrays), accumulated
-    int dorder;          // 0: Euler; 2 or 4: NavierStokes, the midpoint diffusive fluxes in S.Fd enter
+    int dorder;          // 0: Euler; 2, 4 or 6: NavierStokes, the midpoint diffusive fluxes in S.Fd enter
 };
 
 // Node (cell-centre) flux of component e in direction A.
@@ -427,7 +444,8 @@ __device__ __forceinline__ void update_item(const Geom& g, const Scratch& S, con
     double dl[3][NEQ], dr[3][NEQ];
     bool ns = false;
     if constexpr (MODEL == SINGLE_SPECIES) {
-        if (U.beta != 0.0 && U.dorder == 4) { diff_cell_faces<DIM, 4, NEQ>(g, S, U.dt, i, j, k, dl, dr); ns = true; }
+        if (U.beta != 0.0 && U.dorder == 6) { diff_cell_faces<DIM, 6, NEQ>(g, S, U.dt, i, j, k, dl, dr); ns = true; }
+        else if (U.beta != 0.0 && U.dorder == 4) { diff_cell_faces<DIM, 4, NEQ>(g, S, U.dt, i, j, k, dl, dr); ns = true; }
         else if (U.beta != 0.0 && U.dorder == 2) { diff_cell_faces<DIM, 2, NEQ>(g, S, U.dt, i, j, k, dl, dr); ns = true; }
     }
 
@@ -491,13 +509,15 @@ __device__ __forceinline__ void update_item(const Geom& g, const Scratch& S, con
 // items skip).
 // ---------------------------------------------------------------------------
 template <int DIM>
-__device__ __forceinline__ void fill_item(const Geom& g, const Comp& Q, int ncomp, const int* periodic, long x) {
+__device__ __forceinline__ void fill_item(const Geom& g, const Comp& Q, int ncomp, const int* periodic, long x,
+                                          int mom0) {
     int c[3];
-    c[0] = (int)(x % g.G[0]) - GHOST;
-    c[1] = (int)((x / g.G[0]) % g.G[1]) - GHOST;
-    c[2] = DIM == 3 ? (int)(x / ((long)g.G[0] * g.G[1])) - GHOST : 0;
+    c[0] = (int)(x % g.G[0]) - g.gh;
+    c[1] = (int)((x / g.G[0]) % g.G[1]) - g.gh;
+    c[2] = DIM == 3 ? (int)(x / ((long)g.G[0] * g.G[1])) - g.gh : 0;
     bool inside = true;
     int s[3];
+    int flip = -1, flip2 = -1, flip3 = -1;   // momentum components negated by reflecting walls
 #pragma unroll
     for (int a = 0; a < 3; a++) {
         s[a] = c[a];
@@ -505,39 +525,66 @@ __device__ __forceinline__ void fill_item(const Geom& g, const Comp& Q, int ncom
         if (c[a] < 0 || c[a] >= g.n[a]) {
             if (periodic[a] == 2) return;
             inside = false;
-            if (periodic[a] == 1) s[a] = ((c[a] % g.n[a]) + g.n[a]) % g.n[a];
-            else s[a] = c[a] < 0 ? 0 : g.n[a] - 1;
+            if (periodic[a] == 1) {
+                s[a] = ((c[a] % g.n[a]) + g.n[a]) % g.n[a];
+            } else if (periodic[a] == 3) {
+                // reflecting wall: mirror image across the boundary face
+                // (BasicCartesianBoundaryUtilities2.cpp:349-440), normal momentum negated
+                s[a] = c[a] < 0 ? -c[a] - 1 : 2 * g.n[a] - 1 - c[a];
+                if (flip < 0) flip = mom0 + a;
+                else if (flip2 < 0) flip2 = mom0 + a;
+                else flip3 = mom0 + a;
+            } else {
+                s[a] = c[a] < 0 ? 0 : g.n[a] - 1;
+            }
         }
     }
     if (inside) return;
     const long y = cidx<DIM>(g, s[0], s[1], s[2]);
-    for (int e = 0; e < ncomp; e++) Q.p[e][x] = Q.p[e][y];
+    for (int e = 0; e < ncomp; e++) {
+        const double v = Q.p[e][y];
+        Q.p[e][x] = (e == flip || e == flip2 || e == flip3) ? -v : v;
+    }
 }
 
-// Zero-gradient fill at the non-periodic faces of the level's domain for a patch with
-// known position: ghost cell c (local) of a patch at level index lo takes the value of
-// the nearest in-domain cell (clamped along the axes where it lies outside the domain),
-// which is the patch's own interior or a ghost cell filled from a neighbour before.
-// Ghost cells inside the domain are left alone (neighbour copies or provided values).
+// Physical boundaries of the level's domain for a patch with known position: ghost cell c
+// (local) of a patch at level index lo, outside the domain along an axis, takes the value of
+// the nearest in-domain cell (zero-gradient, dom_periodic 0) or of its mirror image across the
+// domain face with the normal momentum negated (reflecting wall, dom_periodic 3) -- the patch's
+// own interior or a ghost cell filled from a neighbour before.  Ghost cells inside the domain
+// are left alone (neighbour copies or provided values).
 template <int DIM>
 __device__ __forceinline__ void domain_fill_item(const Geom& g, const Comp& Q, int ncomp, const int* lo,
-                                                 const int* dom, const int* dom_periodic, long x) {
+                                                 const int* dom, const int* dom_periodic, long x, int mom0) {
     int c[3], s[3];
-    c[0] = (int)(x % g.G[0]) - GHOST;
-    c[1] = (int)((x / g.G[0]) % g.G[1]) - GHOST;
-    c[2] = DIM == 3 ? (int)(x / ((long)g.G[0] * g.G[1])) - GHOST : 0;
+    c[0] = (int)(x % g.G[0]) - g.gh;
+    c[1] = (int)((x / g.G[0]) % g.G[1]) - g.gh;
+    c[2] = DIM == 3 ? (int)(x / ((long)g.G[0] * g.G[1])) - g.gh : 0;
     bool physical = false;
+    int flip = -1, flip2 = -1, flip3 = -1;
 #pragma unroll
     for (int a = 0; a < 3; a++) {
         s[a] = c[a];
-        if (a >= DIM || dom_periodic[a]) continue;
+        if (a >= DIM || dom_periodic[a] == 1) continue;
         const int G = lo[a] + c[a];
-        if (G < 0) { s[a] = -lo[a]; physical = true; }
-        else if (G >= dom[a]) { s[a] = dom[a] - 1 - lo[a]; physical = true; }
+        if (G >= 0 && G < dom[a]) continue;
+        physical = true;
+        if (dom_periodic[a] == 3) {
+            // reflecting wall: mirror image across the domain face, in the level's index space
+            s[a] = (G < 0 ? -G - 1 : 2 * dom[a] - 1 - G) - lo[a];
+            if (flip < 0) flip = mom0 + a;
+            else if (flip2 < 0) flip2 = mom0 + a;
+            else flip3 = mom0 + a;
+        } else {
+            s[a] = G < 0 ? -lo[a] : dom[a] - 1 - lo[a];
+        }
     }
     if (!physical) return;
     const long y = cidx<DIM>(g, s[0], s[1], s[2]);
-    for (int e = 0; e < ncomp; e++) Q.p[e][x] = Q.p[e][y];
+    for (int e = 0; e < ncomp; e++) {
+        const double v = Q.p[e][y];
+        Q.p[e][x] = (e == flip || e == flip2 || e == flip3) ? -v : v;
+    }
 }
 
 }  // namespace hmr

@@ -37,6 +37,10 @@ inline double host_mid_value(int order, double LL, double L, double R, double RR
     if (order == 2) return double(1)/double(2)*(R + L);
     return double(9)/double(16)*(R + L) + -double(1)/double(16)*(RR + LL);
 }
+// The sixth-order node -> midpoint value of a constant (…MidpointSixthOrder.cpp:962-1000).
+inline double host_mid_value6(double v) {
+    return (double(75)/double(128)*(v + v) + -double(25)/double(256)*(v + v) + double(3)/double(256)*(v + v));
+}
 
 // Navier-Stokes constants of Params (single species): the side values of the constant
 // transport properties, interpolated from cells as every side variable is, and the
@@ -47,21 +51,24 @@ inline int diffusive_params(const hmr_config* cfg, Params& P) {
     P.dS43 = P.dS23 = P.dmu = P.dkappa = P.dTc = 0.0;
     P.cmu = P.cmu_v = P.ckappa = 0.0;
     if (order == HMR_DIFFUSIVE_NONE) return HMR_OK;
-    if (order != HMR_MIDPOINT_SECOND_ORDER && order != HMR_MIDPOINT_FOURTH_ORDER) return HMR_ERR_UNSUPPORTED;
+    if (order != HMR_MIDPOINT_SECOND_ORDER && order != HMR_MIDPOINT_FOURTH_ORDER &&
+        order != HMR_MIDPOINT_SIXTH_ORDER)
+        return HMR_ERR_UNSUPPORTED;
     if (cfg->flow_model != HMR_SINGLE_SPECIES) return HMR_ERR_UNSUPPORTED;
     if (!(cfg->species_mu >= 0.0) || !(cfg->species_mu_v >= 0.0) || !(cfg->species_c_p >= 0.0) ||
         !(cfg->species_Pr > 0.0) || !(cfg->species_mu_kappa >= 0.0) || !(cfg->species_gamma[0] > 1.0))
         return HMR_ERR_ARGUMENT;
     const double mu = cfg->species_mu, mu_v = cfg->species_mu_v;
     const double kappa = cfg->species_c_p*cfg->species_mu_kappa/cfg->species_Pr;   // Prandtl.cpp:63
-    const double mu_s = host_mid_value(order, mu, mu, mu, mu);
-    const double mu_v_s = host_mid_value(order, mu_v, mu_v, mu_v, mu_v);
+    auto side = [order](double v) { return order == 6 ? host_mid_value6(v) : host_mid_value(order, v, v, v, v); };
+    const double mu_s = side(mu);
+    const double mu_v_s = side(mu_v);
     P.dorder = order;
     P.cmu = mu;
     P.cmu_v = mu_v;
     P.ckappa = kappa;
     P.dmu = mu_s;
-    P.dkappa = host_mid_value(order, kappa, kappa, kappa, kappa);
+    P.dkappa = side(kappa);
     P.dS43 = double(4)/double(3)*mu_s + mu_v_s;
     P.dS23 = double(2)/double(3)*mu_s - mu_v_s;
     const double gamma = cfg->species_gamma[0];
@@ -178,7 +185,8 @@ struct LevelArgs {
     int ncopy;
     long total_copy;
     int dom[3];                      // domain extent in cells
-    int dom_periodic[3];
+    int dom_periodic[3];             // per axis: 1 periodic, 0 zero-gradient or 3 reflecting wall faces
+    int mom0;                        // first momentum component (the normal one flips at a reflecting wall)
     // work splitting (autotuned; results do not depend on it): phase chunks of chunk_mult
     // block widths; split_mode 1 hands the cell-wise phases out by a fixed grid stride
     int chunk_mult;
@@ -191,8 +199,11 @@ namespace hmr_cells {
 int launch_cells(const hmr::Variant& v, const hmr::Params& P, const hmr::Geom& g, const hmr::Comp& Q,
                  const hmr::Scratch& S, cudaStream_t st);
 int launch_sensor(const hmr::Variant& v, const hmr::Geom& g, const hmr::Scratch& S, cudaStream_t st);
-int launch_fill(int dim, const hmr::Geom& g, const hmr::Comp& Q, int ncomp, const int* periodic, cudaStream_t st);
-int launch_fill_vjp(int dim, const hmr::Geom& g, const hmr::Comp& Qb, int ncomp, const int* periodic,
+// Ghost fill of one patch per axis (hmr_fill_mode); mom0: the first momentum component, whose
+// normal one a reflecting wall negates.
+int launch_fill(int dim, const hmr::Geom& g, const hmr::Comp& Q, int ncomp, const int* periodic, int mom0,
+                cudaStream_t st);
+int launch_fill_vjp(int dim, const hmr::Geom& g, const hmr::Comp& Qb, int ncomp, const int* periodic, int mom0,
                     cudaStream_t st);
 // Stable time step (Euler::computeSpectralRadiusesAndStableDtOnPatch): running max over the
 // ghost-box cells of sum_d (|u_d| + c)/dx_d (NavierStokes: and of the diffusive radius) into

@@ -556,9 +556,9 @@ __device__ __forceinline__ void cell_bwd_item(const Params& P, const Geom& g, co
     constexpr int NCOMP = M::NCOMP;
     const long nc = ncell_of(g);
     {
-        const int i = (int)(x % g.G[0]) - GHOST;
-        const int j = (int)((x / g.G[0]) % g.G[1]) - GHOST;
-        const int k = DIM == 3 ? (int)(x / ((long)g.G[0] * g.G[1])) - GHOST : 0;
+        const int i = (int)(x % g.G[0]) - g.gh;
+        const int j = (int)((x / g.G[0]) % g.G[1]) - g.gh;
+        const int k = DIM == 3 ? (int)(x / ((long)g.G[0] * g.G[1])) - g.gh : 0;
         const bool interior = i >= 0 && i < g.n[0] && j >= 0 && j < g.n[1] && (DIM == 2 || (k >= 0 && k < g.n[2]));
         // alpha terms (interior; equations only: the stored last volume fraction is not an input of the update)
         if (interior) {

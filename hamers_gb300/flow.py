@@ -7,7 +7,7 @@ Names follow HAMeRS:
                                    (include/flow/convective_flux_reconstructors/ConvectiveFluxReconstructor.hpp:23-124)
   Euler                         -- the RungeKuttaPatchStrategy of src/apps/Euler/Euler.cpp
                                    (computeFluxesAndSourcesOnPatch :904, advanceSingleStepOnPatch :1003)
-  DiffusiveFluxReconstructor    -- DiffusiveFluxReconstructorMidpoint (second / fourth order)
+  DiffusiveFluxReconstructor    -- DiffusiveFluxReconstructorMidpoint (second / fourth / sixth order)
                                    (src/flow/diffusive_flux_reconstructors/midpoint/DiffusiveFluxReconstructorMidpoint.cpp:38)
   NavierStokes                  -- the patch strategy of src/apps/Navier-Stokes/NavierStokes.cpp
                                    (computeFluxesAndSourcesOnPatch :1104, advanceSingleStepOnPatch :1249)
@@ -15,7 +15,8 @@ Names follow HAMeRS:
   BatchedLevel                  -- all patches of a level per substep in one persistent kernel
 
 Patch data are torch tensors on the CUDA device in SAMRAI layout:
-conserved variables (ncomp, G2, G1, G0) over the ghost box (ghost width 4),
+conserved variables (ncomp, G2, G1, G0) over the ghost box (ghost width 4; 5 with the
+sixth-order diffusive flux, getPatchNumberOfGhostCells()),
 face fluxes [axis] -> (neq, ...) and sources (neq, n2, n1, n0).  torch is used
 for device memory and streams only; every computation runs in libhmr_gb300.so.
 Errors from the library raise HmrError (argument errors are raised before any
@@ -44,10 +45,14 @@ _RECONSTRUCTORS = {
 _DIFFUSIVE = {
     "MIDPOINT_SECOND_ORDER": L.HMR_MIDPOINT_SECOND_ORDER,
     "MIDPOINT_FOURTH_ORDER": L.HMR_MIDPOINT_FOURTH_ORDER,
+    "MIDPOINT_SIXTH_ORDER": L.HMR_MIDPOINT_SIXTH_ORDER,
 }
 
 # SSPRK(3,3), RungeKuttaLevelIntegrator.cpp:3909-3927
 RK3_ALPHA = [[1.0], [3.0 / 4.0, 1.0 / 4.0], [1.0 / 3.0, 0.0, 2.0 / 3.0]]
+
+# ghost-fill mode per axis (hmr_fill_mode of include/hmr.h)
+FILL_ZERO_GRADIENT, FILL_PERIODIC, FILL_PROVIDED, FILL_REFLECT = 0, 1, 2, 3
 RK3_BETA = [[1.0], [0.0, 1.0 / 4.0], [0.0, 0.0, 2.0 / 3.0]]
 RK3_GAMMA = [[1.0 / 6.0], [0.0, 1.0 / 6.0], [0.0, 0.0, 2.0 / 3.0]]
 
@@ -195,6 +200,11 @@ class ConvectiveFluxReconstructor:
     def getConvectiveFluxNumberOfGhostCells(self):
         return self._lib.hmr_num_ghosts(self.ctx)
 
+    def getPatchNumberOfGhostCells(self):
+        """Ghost width of the patch arrays this context reads: 4, or 5 with the sixth-order
+        diffusive flux (NavierStokes.cpp:317-349 takes the larger of the two widths)."""
+        return self._lib.hmr_num_patch_ghosts(self.ctx)
+
     def allocateFlux(self, patch):
         dim = self.flow_model.dim
         n3 = list(patch.n) + [1] * (3 - len(patch.n))
@@ -278,6 +288,9 @@ class Euler:
             rec.ctx, ctypes.byref(g), q, f, d, s_, _stream_ptr(stream)))
 
     def fillGhosts(self, patch, periodic, stream=None):
+        """Ghost fill of one patch, mode per axis: FILL_ZERO_GRADIENT (0, the extrapolation
+        boundary), FILL_PERIODIC (1), FILL_PROVIDED (2, left as supplied) or FILL_REFLECT (3, a
+        slip wall: mirror image with the normal momentum negated; needs >= 4 cells on the axis)."""
         g = patch.geometry()
         q, _k = L.ptr_array(_comp_ptrs(patch.data, self.rec.ncomp))
         per = (ctypes.c_int * 3)(*(list(periodic) + [0] * (3 - len(periodic))))
@@ -330,7 +343,9 @@ class Euler:
 
 
 class DiffusiveFluxReconstructor:
-    """MIDPOINT_SECOND_ORDER / MIDPOINT_FOURTH_ORDER diffusive flux behind the C ABI.
+    """MIDPOINT_SECOND_ORDER / _FOURTH_ORDER / _SIXTH_ORDER diffusive flux behind the C ABI.
+    With the sixth order every patch array of the context carries 5 ghost cells
+    (ConvectiveFluxReconstructor.getPatchNumberOfGhostCells).
 
     It runs in the context of a ConvectiveFluxReconstructor created with
     diffusive_flux_reconstructor=<name> (one context holds the whole
@@ -344,7 +359,7 @@ class DiffusiveFluxReconstructor:
         self._lib = convective._lib
 
     def getDiffusiveFluxNumberOfGhostCells(self):
-        return 1 if self.name == "MIDPOINT_SECOND_ORDER" else 3
+        return {"MIDPOINT_SECOND_ORDER": 1, "MIDPOINT_FOURTH_ORDER": 3, "MIDPOINT_SIXTH_ORDER": 5}[self.name]
 
     def computeDiffusiveFluxOnPatch(self, patch, diffusive_flux, dt, stream=None):
         """dt-scaled diffusive face fluxes (overwritten), same layout as the convective flux."""
@@ -591,7 +606,8 @@ class BatchedLevel:
 
     def set_layout(self, lo, domain, periodic):
         """Patch positions (first interior cell per patch, level index space), the domain's cells
-        per axis and its periodic axes: enables the ghost exchange between patches."""
+        per axis and its boundary per axis (FILL_PERIODIC, FILL_ZERO_GRADIENT or FILL_REFLECT
+        walls): enables the ghost exchange between patches."""
         dim = self.rec.flow_model.dim
         flat = []
         for p in range(self.npatch):

@@ -17,7 +17,8 @@
  * Conventions (identical to SAMRAI's pdat layout used by the reference):
  *   - every array is FP64 in device memory, x fastest, then y, then z;
  *   - a patch's conserved variables are CellData on the ghost box (interior
- *     grown by hmr_num_ghosts() = 4 cells), one array per component, in the
+ *     grown by hmr_num_patch_ghosts() = 4 cells, 5 with the sixth-order diffusive
+ *     flux), one array per component, in the
  *     flow model's order:
  *       single species          : rho, rho*u_k (dim), E
  *       five-equation (Allaire) : Z_i*rho_i (N), rho*u_k (dim), E, Z_i (N; the
@@ -75,11 +76,15 @@ typedef enum {
 
 /* NavierStokes diffusive_flux_reconstructor (DiffusiveFluxReconstructorManager.cpp):
  * none (the Euler equations) or the midpoint reconstructors of the given order
- * (DiffusiveFluxReconstructorMidpointSecondOrder / ...FourthOrder).  Single species only. */
+ * (DiffusiveFluxReconstructorMidpointSecondOrder / ...FourthOrder / ...SixthOrder).  Single
+ * species only.  The sixth order reads 5 ghost cells, so a context with it takes patch arrays
+ * of ghost width 5 everywhere (hmr_num_patch_ghosts), runs per patch (no hmr_level) and has
+ * no substep VJP (HMR_ERR_UNSUPPORTED). */
 typedef enum {
     HMR_DIFFUSIVE_NONE = 0,
     HMR_MIDPOINT_SECOND_ORDER = 2,
-    HMR_MIDPOINT_FOURTH_ORDER = 4
+    HMR_MIDPOINT_FOURTH_ORDER = 4,
+    HMR_MIDPOINT_SIXTH_ORDER = 6
 } hmr_diffusive;
 
 typedef enum {
@@ -135,6 +140,10 @@ int hmr_num_equations(const hmr_ctx* ctx);
 int hmr_num_components(const hmr_ctx* ctx);
 /* ConvectiveFluxReconstructor::getConvectiveFluxNumberOfGhostCells (ConvectiveFluxReconstructor.hpp:46-50). */
 int hmr_num_ghosts(const hmr_ctx* ctx);
+/* Ghost width of the patch arrays every entry point of this context reads and writes: the larger
+ * of the convective and diffusive widths (NavierStokes.cpp:317-349), 4, or 5 with
+ * HMR_MIDPOINT_SIXTH_ORDER. */
+int hmr_num_patch_ghosts(const hmr_ctx* ctx);
 /* Pre-sizes the context's scratch for patches up to this geometry (needed before stream capture). */
 int hmr_ctx_reserve(hmr_ctx* ctx, const hmr_patch_geometry* geom);
 /* Face counters accumulated by the flux entry points since the last reset:
@@ -193,7 +202,12 @@ int hmr_rk_substep_patch(hmr_ctx* ctx, const hmr_patch_geometry* geom, int stage
 typedef enum {
     HMR_FILL_ZERO_GRADIENT = 0,   /* copy of the nearest interior cell (extrapolation boundary) */
     HMR_FILL_PERIODIC = 1,        /* periodic image within the patch */
-    HMR_FILL_PROVIDED = 2         /* ghost cells supplied by the caller are left untouched */
+    HMR_FILL_PROVIDED = 2,        /* ghost cells supplied by the caller are left untouched */
+    HMR_FILL_REFLECT = 3          /* reflecting (slip) wall: mirror image across the boundary face with the
+                                     normal momentum negated -- the reference's REFLECT condition
+                                     (BasicCartesianBoundaryUtilities2.cpp:349-440 with the scalar/vector
+                                     split of EulerBoundaryConditions.cpp:205-297); needs >= 4 cells along
+                                     the axis */
 } hmr_fill_mode;
 
 /* Single-patch ghost fill, mode per axis (hmr_fill_mode; any other non-zero value of older callers
@@ -270,8 +284,9 @@ int hmr_rk_substep_vjp_patch(hmr_ctx* ctx, const hmr_patch_geometry* geom, int s
                              const double* const* Qbar_out, double* const* const* Qbar_int, void* stream);
 
 /* Adjoint of hmr_fill_ghosts_patch: adds the adjoint of every filled ghost cell to the interior
- * cell it is copied from and zeroes it; ghost cells along HMR_FILL_PROVIDED axes keep their
- * adjoints (they belong to whatever supplied the values).  No counterpart in the reference. */
+ * cell it is copied from (negated for the normal momentum at a reflecting wall) and zeroes it;
+ * ghost cells along HMR_FILL_PROVIDED axes keep their adjoints (they belong to whatever supplied
+ * the values).  No counterpart in the reference. */
 int hmr_fill_ghosts_vjp_patch(hmr_ctx* ctx, const hmr_patch_geometry* geom, double* const* Qbar,
                               const int* periodic, void* stream);
 
@@ -285,10 +300,12 @@ int hmr_level_destroy(hmr_level* level);
  * (the same-level part of SAMRAI's fill schedule, RungeKuttaLevelIntegrator.cpp:1568,1701):
  * before every substep the ghost cells of each patch are copied from the interiors of the
  * patches (and of their periodic images) that cover them, then cells outside the domain along
- * non-periodic axes take the nearest in-domain value (zero-gradient, the extrapolation boundary);
- * ghost cells inside the domain covered by no patch of the level (a coarse-fine boundary) are
- * left as the caller provides them.  lo: 3 ints per patch (first interior cell), domain: cells
- * per axis, periodic: 0/1 per axis.  Boxes must lie in the domain and not overlap. */
+ * non-periodic axes take the nearest in-domain value (zero-gradient, the extrapolation boundary)
+ * or, at reflecting walls, the mirror image across the domain face with the normal momentum
+ * negated; ghost cells inside the domain covered by no patch of the level (a coarse-fine
+ * boundary) are left as the caller provides them.  lo: 3 ints per patch (first interior cell),
+ * domain: cells per axis, periodic per axis: 1 periodic, 0 zero-gradient faces,
+ * HMR_FILL_REFLECT reflecting walls.  Boxes must lie in the domain and not overlap. */
 int hmr_level_set_layout(hmr_level* level, const int* lo, const int* domain, const int* periodic);
 /* Binds the caller's ghost-box arrays (ncomp device pointers) as slot 0 of a patch. */
 int hmr_level_bind_state(hmr_level* level, int patch, double* const* comps);

@@ -39,7 +39,7 @@ int hmro_num_comp(const hmro_config* cfg) { return num_comp(to_cfg(cfg)); }
 int hmro_conv_flux_source(const hmro_config* cfg, const int* n, const double* dx, double dt,
                           const double* Q, double* flux, double* source, long* stats) {
     const Config c = to_cfg(cfg);
-    const Box b = make_box(c.dim, n, 4);
+    const Box b = make_box(c.dim, n, c.ghosts);
     const int ncomp = num_comp(c), neq = num_eqn(c);
     std::vector<const double*> q(ncomp);
     for (int e = 0; e < ncomp; e++) q[e] = Q + (size_t)e * b.ncell();
@@ -61,7 +61,7 @@ int hmro_rk_stage(const hmro_config* cfg, const int* n, const double* dx, int ns
                   const double* Q_int, const double* F_int, const double* S_int,
                   double* Q_out, double* F_acc, double* S_acc) {
     const Config c = to_cfg(cfg);
-    const Box b = make_box(c.dim, n, 4);
+    const Box b = make_box(c.dim, n, c.ghosts);
     const int ncomp = num_comp(c), neq = num_eqn(c);
     const long nint = (long)b.n[0] * b.n[1] * b.n[2];
     const long fl = flux_len(c, b);
@@ -90,8 +90,9 @@ int hmro_rk_stage(const hmro_config* cfg, const int* n, const double* dx, int ns
 int hmro_diff_flux(const hmro_config* cfg, const hmro_transport* tr, const int* n, const double* dx, double dt,
                    const double* Q, double* flux) {
     const Config c = to_cfg(cfg);
-    if (c.model != MODEL_SINGLE_SPECIES || (tr->order != 2 && tr->order != 4)) return -1;
-    const Box b = make_box(c.dim, n, 4);
+    if (c.model != MODEL_SINGLE_SPECIES || (tr->order != 2 && tr->order != 4 && tr->order != 6)) return -1;
+    if (tr->order == 6 && c.ghosts < 5) return -1;
+    const Box b = make_box(c.dim, n, c.ghosts);
     const int ncomp = num_comp(c);
     std::vector<const double*> q(ncomp);
     for (int e = 0; e < ncomp; e++) q[e] = Q + (size_t)e * b.ncell();
@@ -108,7 +109,7 @@ int hmro_rk_stage_ns(const hmro_config* cfg, const int* n, const double* dx, int
                      const double* Q_int, const double* F_int, const double* Fd_int, const double* S_int,
                      double* Q_out) {
     const Config c = to_cfg(cfg);
-    const Box b = make_box(c.dim, n, 4);
+    const Box b = make_box(c.dim, n, c.ghosts);
     const int ncomp = num_comp(c), neq = num_eqn(c);
     const long nint = (long)b.n[0] * b.n[1] * b.n[2];
     const long fl = flux_len(c, b);
@@ -136,7 +137,7 @@ int hmro_rk_stage_ns(const hmro_config* cfg, const int* n, const double* dx, int
 int hmro_sync_fluxes(const hmro_config* cfg, const int* n, const double* dx, const double* F,
                      const double* Fd, const double* S, double* Q) {
     const Config c = to_cfg(cfg);
-    const Box b = make_box(c.dim, n, 4);
+    const Box b = make_box(c.dim, n, c.ghosts);
     const int ncomp = num_comp(c), neq = num_eqn(c);
     const long nint = (long)b.n[0] * b.n[1] * b.n[2];
     std::vector<double*> f, d, q(ncomp);
@@ -154,8 +155,8 @@ int hmro_coarsen_fluxsum(const hmro_config* cfg, const int* ratio, const int* cn
                          const int* flo, const double* Ff, double* Fc) {
     const Config c = to_cfg(cfg);
     std::vector<double*> ff, fc;
-    flux_ptrs(c, make_box(c.dim, fn, 4), const_cast<double*>(Ff), ff);
-    flux_ptrs(c, make_box(c.dim, cn, 4), Fc, fc);
+    flux_ptrs(c, make_box(c.dim, fn, c.ghosts), const_cast<double*>(Ff), ff);
+    flux_ptrs(c, make_box(c.dim, cn, c.ghosts), Fc, fc);
     std::vector<const double*> ffc(ff.begin(), ff.end());
     coarsen_fluxsum(c, ratio, cn, clo, fn, flo, ffc.data(), fc.data());
     return 0;
@@ -166,7 +167,7 @@ int hmro_coarsen_cells(const hmro_config* cfg, const int* ratio, const int* cn, 
                        const int* flo, const double* Qf, double* Qc) {
     const Config c = to_cfg(cfg);
     const int ncomp = num_comp(c);
-    const Box cb = make_box(c.dim, cn, 4), fb = make_box(c.dim, fn, 4);
+    const Box cb = make_box(c.dim, cn, c.ghosts), fb = make_box(c.dim, fn, c.ghosts);
     std::vector<const double*> qf(ncomp);
     std::vector<double*> qc(ncomp);
     for (int e = 0; e < ncomp; e++) { qf[e] = Qf + (size_t)e * fb.ncell(); qc[e] = Qc + (size_t)e * cb.ncell(); }
@@ -179,7 +180,7 @@ int hmro_refine_ghosts(const hmro_config* cfg, const int* ratio, const int* fn, 
                        const int* clo, const double* Qc_old, const double* Qc_new, double theta, double* Qf) {
     const Config c = to_cfg(cfg);
     const int ncomp = num_comp(c);
-    const Box cb = make_box(c.dim, cn, 4), fb = make_box(c.dim, fn, 4);
+    const Box cb = make_box(c.dim, cn, c.ghosts), fb = make_box(c.dim, fn, c.ghosts);
     std::vector<const double*> qo(ncomp), qn(ncomp);
     std::vector<double*> qf(ncomp);
     for (int e = 0; e < ncomp; e++) {
@@ -193,7 +194,7 @@ int hmro_refine_ghosts(const hmro_config* cfg, const int* ratio, const int* fn, 
 
 int hmro_fill_ghosts(const hmro_config* cfg, const int* n, const int* periodic, double* Q) {
     const Config c = to_cfg(cfg);
-    const Box b = make_box(c.dim, n, 4);
+    const Box b = make_box(c.dim, n, c.ghosts);
     std::vector<double*> q(num_comp(c));
     for (int e = 0; e < num_comp(c); e++) q[e] = Q + (size_t)e * b.ncell();
     fill_ghosts<double>(c, n, periodic, q.data());
@@ -212,7 +213,7 @@ static const double RK3_GAMMA[3][3] = {{1.0/6.0, 0, 0}, {0.0, 1.0/6.0, 0}, {0.0,
 int hmro_rk3_advance(const hmro_config* cfg, const int* n, const double* dx, double dt,
                      const int* periodic, int nsteps, double* Q, long* stats) {
     const Config c = to_cfg(cfg);
-    const Box b = make_box(c.dim, n, 4);
+    const Box b = make_box(c.dim, n, c.ghosts);
     const int ncomp = num_comp(c), neq = num_eqn(c);
     const long nint = (long)b.n[0] * b.n[1] * b.n[2];
     const long fl = flux_len(c, b);
@@ -244,7 +245,7 @@ int hmro_rk3_advance(const hmro_config* cfg, const int* n, const double* dx, dou
 int hmro_ns_rk3_advance(const hmro_config* cfg, const hmro_transport* tr, const int* n, const double* dx,
                         double dt, const int* periodic, int nsteps, double* Q) {
     const Config c = to_cfg(cfg);
-    const Box b = make_box(c.dim, n, 4);
+    const Box b = make_box(c.dim, n, c.ghosts);
     const int ncomp = num_comp(c), neq = num_eqn(c);
     const long nint = (long)b.n[0] * b.n[1] * b.n[2];
     const long fl = flux_len(c, b);
@@ -279,7 +280,7 @@ int hmro_ns_rk3_advance(const hmro_config* cfg, const hmro_transport* tr, const 
 double hmro_spectral_radius_ns(const hmro_config* cfg, const hmro_transport* tr, const int* n, const double* dx,
                                const double* Q) {
     const Config c = to_cfg(cfg);
-    const Box b = make_box(c.dim, n, 4);
+    const Box b = make_box(c.dim, n, c.ghosts);
     const int ncomp = num_comp(c);
     std::vector<const double*> q(ncomp);
     for (int e = 0; e < ncomp; e++) q[e] = Q + (size_t)e * b.ncell();
@@ -323,7 +324,7 @@ long hmro_stage_threads(const hmro_config* cfg, const int* n, const double* dx, 
     const int slow = dim - 1;
     if (nthreads < 1) nthreads = 1;
     if (nthreads > n[slow]) nthreads = n[slow];
-    const Box b = make_box(dim, n, 4);
+    const Box b = make_box(dim, n, c.ghosts);
     const int ncomp = num_comp(c), neq = num_eqn(c);
     std::vector<std::thread> th;
     for (int t = 0; t < nthreads; t++) {
@@ -332,7 +333,7 @@ long hmro_stage_threads(const hmro_config* cfg, const int* n, const double* dx, 
             const int hi = (int)((long)n[slow] * (t + 1) / nthreads);
             int sn[3] = {n[0], n[1], dim == 3 ? n[2] : 1};
             sn[slow] = hi - lo;
-            const Box sb = make_box(dim, sn, 4);
+            const Box sb = make_box(dim, sn, c.ghosts);
             std::vector<double> sq((size_t)ncomp * sb.ncell());
             for (int e = 0; e < ncomp; e++)
                 for (int k = -sb.g[2]; k < sb.n[2] + sb.g[2]; k++)

@@ -71,6 +71,8 @@ struct Config {
     double epsilon;      // constant_epsilon (CU-M2 default 1e-8)
     double grid_dx[3];   // CartesianGridGeometry::getDx(): the coarsest level's spacing, which
                          // WCNS6-CU-M2 uses on every level (WCNS6-CU-M2-HLLC-HLL.cpp:367-368)
+    int ghosts = 4;      // ghost width of the patch arrays: 4 (WCNS56-HLLC-HLL.cpp:22), or 5 with
+                         // the sixth-order diffusive flux (DiffusiveFluxReconstructorMidpointSixthOrder.cpp:22)
 };
 
 // Number of equations.  single: 2+dim (FlowModelSingleSpecies.cpp:29);
@@ -989,7 +991,7 @@ void conv_flux_source(const Config& c, const int* n, const double* dx, double dt
                       const T* const* Q, T* const* flux, T* const* source, Stats* stats) {
     const int dim = c.dim;
     const int neq = num_eqn(c);
-    const Box b = make_box(dim, n, 4);
+    const Box b = make_box(dim, n, c.ghosts);
     const long nc = b.ncell();
     Derived<T> D;
     HMRO_PHASE(HMRO_PH_CELLS);
@@ -1253,7 +1255,7 @@ void rk_stage(const Config& c, const int* n, const double* dx, int nstages,
     const int dim = c.dim;
     const int neq = num_eqn(c);
     const int ncomp = num_comp(c);
-    const Box b = make_box(dim, n, 4);
+    const Box b = make_box(dim, n, c.ghosts);
     for (int e = 0; e < ncomp; e++)
         for (long x = 0; x < b.ncell(); x++) Q_out[e][x] = T(0.0);
     for (int s = 0; s < nstages; s++) {
@@ -1350,7 +1352,7 @@ void rk_stage(const Config& c, const int* n, const double* dx, int nstages,
 // temperature T = p/((gamma - 1) c_v rho) (EquationOfStateIdealGas.cpp:2157-2173).
 // ---------------------------------------------------------------------------
 struct Transport {
-    int order;          // 2 or 4: MIDPOINT_SECOND_ORDER / MIDPOINT_FOURTH_ORDER
+    int order;          // 2, 4 or 6: MIDPOINT_SECOND_ORDER / _FOURTH_ORDER / _SIXTH_ORDER (5 ghosts)
     double mu;          // Equation_of_shear_viscosity_mixing_rules.species_mu (CONSTANT)
     double mu_v;        // Equation_of_bulk_viscosity_mixing_rules.species_mu_v (CONSTANT)
     double c_p, Pr;     // Equation_of_thermal_conductivity_mixing_rules.species_c_p, species_Pr (PRANDTL)
@@ -1432,6 +1434,25 @@ inline T mid_value(int order, const T& LL, const T& L, const T& R, const T& RR) 
     if (order == 2) return double(1)/double(2)*(R + L);
     return double(9)/double(16)*(R + L) + -double(1)/double(16)*(RR + LL);
 }
+// Sixth order (…MidpointSixthOrder.cpp): midpoint derivative :80-117 (75/64, -25/384, 3/640),
+// node derivative :521-558 (3/4, -3/20, 1/60), node -> midpoint value :962-1000
+// (75/128, -25/256, 3/256); v[0..5] are the cells at offsets -3..2 (midpoint stencils) or
+// -3, -2, -1, 1, 2, 3 (node stencil).
+template <class T>
+inline T mid_derivative6(const T* v, double dx_inv) {
+    const double a = double(75)/double(64), b = -double(25)/double(384), c = double(3)/double(640);
+    return (a*(v[3] - v[2]) + b*(v[4] - v[1]) + c*(v[5] - v[0]))*dx_inv;
+}
+template <class T>
+inline T node_derivative6(const T* v, double dx_inv) {
+    const double a = double(3)/double(4), b = -double(3)/double(20), c = double(1)/double(60);
+    return (a*(v[3] - v[2]) + b*(v[4] - v[1]) + c*(v[5] - v[0]))*dx_inv;
+}
+template <class T>
+inline T mid_value6(const T* v) {
+    const double a = double(75)/double(128), b = -double(25)/double(256), c = double(3)/double(256);
+    return (a*(v[3] + v[2]) + b*(v[4] + v[1]) + c*(v[5] + v[0]));
+}
 
 // Cell fields the diffusive flux reads: velocity and temperature.
 template <class T>
@@ -1461,8 +1482,17 @@ void diff_midpoint(const Config& c, const Transport& tr, const Box& b, const std
         ii = i; jj = j; kk = k;
         if (ax == 0) ii += m; else if (ax == 1) jj += m; else kk += m;
     };
-    // value of field v at the midpoint (cells f-2, f-1, f, f+1 along a)
+    // value of field v at the midpoint (cells f-2, f-1, f, f+1 along a; f-3 .. f+2 at sixth order)
     auto mid = [&](auto&& cellval) {
+        if (order == 6) {
+            T v6[6];
+            for (int m = -3; m <= 2; m++) {
+                int ii, jj, kk;
+                sh(a, m, ii, jj, kk);
+                v6[m + 3] = cellval(ii, jj, kk);
+            }
+            return mid_value6(v6);
+        }
         int i0, j0, k0, i1, j1, k1, i2, j2, k2, i3, j3, k3;
         sh(a, -2, i0, j0, k0); sh(a, -1, i1, j1, k1); sh(a, 0, i2, j2, k2); sh(a, 1, i3, j3, k3);
         return mid_value(order, cellval(i0, j0, k0), cellval(i1, j1, k1), cellval(i2, j2, k2), cellval(i3, j3, k3));
@@ -1484,7 +1514,15 @@ void diff_midpoint(const Config& c, const Transport& tr, const Box& b, const std
         for (int t = 0; t < nt; t++) {
             const int v = terms[t].v;
             T g;
-            if (d == a) {
+            if (d == a && order == 6) {
+                T v6[6];
+                for (int m = -3; m <= 2; m++) {
+                    int ii, jj, kk;
+                    sh(a, m, ii, jj, kk);
+                    v6[m + 3] = at(v, ii, jj, kk);
+                }
+                g = mid_derivative6(v6, dx_inv);
+            } else if (d == a) {
                 int i0, j0, k0, i1, j1, k1, i2, j2, k2, i3, j3, k3;
                 sh(a, -2, i0, j0, k0); sh(a, -1, i1, j1, k1); sh(a, 0, i2, j2, k2); sh(a, 1, i3, j3, k3);
                 g = mid_derivative(order, at(v, i0, j0, k0), at(v, i1, j1, k1), at(v, i2, j2, k2), at(v, i3, j3, k3),
@@ -1497,6 +1535,10 @@ void diff_midpoint(const Config& c, const Transport& tr, const Box& b, const std
                         if (d == 0) i4 += m; else if (d == 1) j4 += m; else k4 += m;
                         return at(v, i4, j4, k4);
                     };
+                    if (order == 6) {
+                        const T v6[6] = {node(-3), node(-2), node(-1), node(1), node(2), node(3)};
+                        return node_derivative6(v6, dx_inv);
+                    }
                     return node_derivative(order, node(-2), node(-1), node(1), node(2), dx_inv);
                 });
             }
@@ -1510,13 +1552,16 @@ template <class T>
 void diff_flux(const Config& c, const Transport& tr, const int* n, const double* dx, double dt,
                const T* const* Q, T* const* flux) {
     const int dim = c.dim, neq = num_eqn(c);
-    const Box b = make_box(dim, n, 4);
+    const Box b = make_box(dim, n, c.ghosts);
     Derived<T> D;
     compute_derived(c, b, Q, D);
     std::vector<T> W;
     diff_cell_fields(c, b, D, W);
     const double a_r = double(9)/double(8) + -double(1)/double(24), b_r = -double(1)/double(24);
-    T Fm[3][8], Fo[8];
+    // sixth order (…MidpointSixthOrder.cpp:1400-1440): a_m + b_m + c_m, b_m + c_m, c_m
+    const double a6 = double(75)/double(64), b6 = -double(25)/double(384), c6 = double(3)/double(640);
+    const double a_r6 = a6 + b6 + c6, b_r6 = b6 + c6, c_r6 = c6;
+    T Fm[5][8], Fo[8];
     for (int a = 0; a < dim; a++) {
         const int e0 = b.n[0] + (a == 0), e1 = b.n[1] + (a == 1), e2 = b.n[2] + (a == 2);
         for (int k = 0; k < e2; k++)
@@ -1526,6 +1571,13 @@ void diff_flux(const Config& c, const Transport& tr, const int* n, const double*
             if (tr.order == 2) {
                 diff_midpoint(c, tr, b, W, a, i, j, k, dx, Fo);
                 for (int e = 0; e < neq; e++) flux[a * neq + e][f] = T(0.0) + dt*double(1)*Fo[e];
+            } else if (tr.order == 6) {
+                for (int m = -2; m <= 2; m++)
+                    diff_midpoint(c, tr, b, W, a, i + (a == 0 ? m : 0), j + (a == 1 ? m : 0), k + (a == 2 ? m : 0),
+                                  dx, Fm[m + 2]);
+                for (int e = 0; e < neq; e++)
+                    flux[a * neq + e][f] = T(0.0) + dt*(a_r6*(Fm[2][e]) + b_r6*(Fm[1][e] + Fm[3][e]) +
+                                                        c_r6*(Fm[0][e] + Fm[4][e]));
             } else {
                 for (int m = -1; m <= 1; m++)
                     diff_midpoint(c, tr, b, W, a, i + (a == 0 ? m : 0), j + (a == 1 ? m : 0), k + (a == 2 ? m : 0),
@@ -1556,7 +1608,7 @@ template <class T>
 void sync_fluxes(const Config& c, const int* n, const double* dx, const T* const* F, const T* const* Fd,
                  const T* const* S, T* const* Q) {
     const int dim = c.dim, neq = num_eqn(c);
-    const Box b = make_box(dim, n, 4);
+    const Box b = make_box(dim, n, c.ghosts);
     for (int e = 0; e < neq; e++) {
         for (int k = 0; k < b.n[2]; k++)
         for (int j = 0; j < b.n[1]; j++)
@@ -1615,7 +1667,7 @@ void sync_fluxes(const Config& c, const int* n, const double* dx, const T* const
 inline void coarsen_fluxsum(const Config& c, const int* ratio, const int* cn, const int* clo,
                             const int* fn, const int* flo, const double* const* Ff, double* const* Fc) {
     const int dim = c.dim, neq = num_eqn(c);
-    const Box cb = make_box(dim, cn, 4), fb = make_box(dim, fn, 4);
+    const Box cb = make_box(dim, cn, c.ghosts), fb = make_box(dim, fn, c.ghosts);
     for (int a = 0; a < dim; a++) {
         int area = 1;
         for (int d = 0; d < dim; d++) if (d != a) area *= ratio[d];
@@ -1659,7 +1711,7 @@ inline void coarsen_fluxsum(const Config& c, const int* ratio, const int* cn, co
 inline void coarsen_cells(const Config& c, const int* ratio, const int* cn, const int* clo,
                           const int* fn, const int* flo, const double* const* Qf, double* const* Qc) {
     const int dim = c.dim, ncomp = num_comp(c);
-    const Box cb = make_box(dim, cn, 4), fb = make_box(dim, fn, 4);
+    const Box cb = make_box(dim, cn, c.ghosts), fb = make_box(dim, fn, c.ghosts);
     int vol = 1;
     for (int d = 0; d < dim; d++) vol *= ratio[d];
     const double w = double(1)/double(vol);
@@ -1711,7 +1763,7 @@ inline void refine_ghosts(const Config& c, const int* ratio, const int* fn, cons
                           const int* clo, const double* const* Qc_old, const double* const* Qc_new, double theta,
                           double* const* Qf) {
     const int dim = c.dim, ncomp = num_comp(c);
-    const Box fb = make_box(dim, fn, 4), cb = make_box(dim, cn, 4);
+    const Box fb = make_box(dim, fn, c.ghosts), cb = make_box(dim, cn, c.ghosts);
     for (int k = -fb.g[2]; k < fb.n[2] + fb.g[2]; k++)
     for (int j = -fb.g[1]; j < fb.n[1] + fb.g[1]; j++)
     for (int i = -fb.g[0]; i < fb.n[0] + fb.g[0]; i++) {
@@ -1745,17 +1797,21 @@ inline void refine_ghosts(const Config& c, const int* ratio, const int* fn, cons
     }
 }
 
-// Ghost fill of one patch: periodic along the axes with periodic[a] != 0,
-// zero-gradient (copy of the nearest interior cell) elsewhere.  On one level
-// with one patch this is what SAMRAI's periodic shift and the
-// extrapolation boundary condition produce.
+// Ghost fill of one patch.  On one level with one patch this is what SAMRAI's periodic shift
+// and the reference's boundary conditions produce.  Per axis: mode 0 zero-gradient (nearest
+// interior cell, the extrapolation condition), 1 periodic,
+// 3 reflecting wall -- the mirror image across the boundary face, the momentum component normal
+// to it negated (BasicCartesianBoundaryUtilities2.cpp:349-395 REFLECT for the momentum vector,
+// :397-440 SYMMETRY for the scalars, as EulerBoundaryConditions.cpp:205-297 assigns them).
 template <class T>
 void fill_ghosts(const Config& c, const int* n, const int* periodic, T* const* Q) {
-    const Box b = make_box(c.dim, n, 4);
+    const Box b = make_box(c.dim, n, c.ghosts);
     const int ncomp = num_comp(c);
+    const int mom0 = vel_index(c);
     auto src = [&](int v, int a) {
         if (v >= 0 && v < b.n[a]) return v;
-        if (periodic[a]) return ((v % b.n[a]) + b.n[a]) % b.n[a];
+        if (periodic[a] == 1) return ((v % b.n[a]) + b.n[a]) % b.n[a];
+        if (periodic[a] == 3) return v < 0 ? -v - 1 : 2 * b.n[a] - 1 - v;
         return v < 0 ? 0 : b.n[a] - 1;
     };
     for (int e = 0; e < ncomp; e++)
@@ -1763,7 +1819,12 @@ void fill_ghosts(const Config& c, const int* n, const int* periodic, T* const* Q
         for (int j = -b.g[1]; j < b.n[1] + b.g[1]; j++)
         for (int i = -b.g[0]; i < b.n[0] + b.g[0]; i++) {
             if (i >= 0 && i < b.n[0] && j >= 0 && j < b.n[1] && k >= 0 && k < b.n[2]) continue;
-            Q[e][b.cell(i, j, k)] = Q[e][b.cell(src(i, 0), src(j, 1), c.dim == 3 ? src(k, 2) : 0)];
+            const int ijk[3] = {i, j, k};
+            bool flip = false;
+            for (int a = 0; a < c.dim; a++)
+                if (periodic[a] == 3 && (ijk[a] < 0 || ijk[a] >= b.n[a]) && e == mom0 + a) flip = !flip;
+            const T v = Q[e][b.cell(src(i, 0), src(j, 1), c.dim == 3 ? src(k, 2) : 0)];
+            Q[e][b.cell(i, j, k)] = flip ? -v : v;
         }
 }
 
@@ -1786,6 +1847,7 @@ struct hmro_config {
     double Chi;
     double epsilon;
     double grid_dx[3];
+    int ghosts;          // 0 means 4
 };
 }
 
@@ -1823,5 +1885,6 @@ inline hmro::Config hmro_to_config(const hmro_config* c) {
     k.Chi = c->Chi;
     k.epsilon = c->epsilon;
     for (int i = 0; i < 3; i++) k.grid_dx[i] = c->grid_dx[i];
+    k.ghosts = c->ghosts > 0 ? c->ghosts : 4;
     return k;
 }

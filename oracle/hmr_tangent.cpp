@@ -77,7 +77,7 @@ int hmro_tangent_substep(const hmro_config* cfg, const int* n, const double* dx,
                          double* Q_out, double* dQ_out, const hmro_transport* tr) {
     using hmro_dual::D;
     const hmro::Config c = hmro_to_config(cfg);
-    const hmro::Box b = hmro::make_box(c.dim, n, 4);
+    const hmro::Box b = hmro::make_box(c.dim, n, c.ghosts);
     const int ncomp = hmro::num_comp(c), neq = hmro::num_eqn(c);
     const long nc = b.ncell();
     const long nint = (long)b.n[0] * b.n[1] * b.n[2];

@@ -34,7 +34,8 @@ class _Cfg(ctypes.Structure):
                 ("scheme", ctypes.c_int), ("gamma", ctypes.c_double * 8), ("R", ctypes.c_double * 8),
                 ("p", ctypes.c_int),
                 ("q", ctypes.c_int), ("C", ctypes.c_double), ("alpha_tau", ctypes.c_double),
-                ("Chi", ctypes.c_double), ("epsilon", ctypes.c_double), ("grid_dx", ctypes.c_double * 3)]
+                ("Chi", ctypes.c_double), ("epsilon", ctypes.c_double), ("grid_dx", ctypes.c_double * 3),
+                ("ghosts", ctypes.c_int)]
 
 
 class _Transport(ctypes.Structure):
@@ -44,7 +45,7 @@ class _Transport(ctypes.Structure):
 
 class Transport:
     """Navier-Stokes transport of a single-species patch: midpoint diffusive flux of
-    the given order (2 or 4), constant shear viscosity mu and bulk viscosity mu_v,
+    the given order (2, 4, or 6 with a Config of ghosts=5), constant shear viscosity mu and bulk viscosity mu_v,
     Prandtl thermal conductivity c_p*mu_kappa/Pr (mu_kappa defaults to mu)."""
 
     def __init__(self, mu, c_p, Pr, mu_v=0.0, order=4, mu_kappa=None):
@@ -126,8 +127,9 @@ class Config:
 
     def __init__(self, model, dim, species_gamma, scheme=SCHEME_WCNS5_JS,
                  p=2, q=4, C=None, alpha_tau=35.0, species_R=None, Chi=1.0e8, epsilon=1.0e-8,
-                 grid_dx=None):
+                 grid_dx=None, ghosts=GHOST):
         self.model = int(model)
+        self.ghosts = int(ghosts)
         self.dim = int(dim)
         self.species_gamma = [float(g) for g in species_gamma]
         self.num_species = len(self.species_gamma)
@@ -146,7 +148,7 @@ class Config:
         r = (ctypes.c_double * 8)(*(self.species_R + [0.0] * (8 - self.num_species)))
         gd = (ctypes.c_double * 3)(*(self.grid_dx or [0.0, 0.0, 0.0]))
         return _Cfg(self.model, self.dim, self.num_species, self.scheme, g, r, self.p, self.q,
-                    self.C, self.alpha_tau, self.Chi, self.epsilon, gd)
+                    self.C, self.alpha_tau, self.Chi, self.epsilon, gd, self.ghosts)
 
     @property
     def neq(self):
@@ -166,9 +168,10 @@ def _n3(n):
     return n + [1] * (3 - len(n))
 
 
-def ghost_shape(cfg, n):
+def ghost_shape(cfg, n, ghosts=None):
     n3 = _n3(n)
-    G = [n3[d] + 2 * GHOST if d < cfg.dim else 1 for d in range(3)]
+    ghosts = cfg.ghosts if ghosts is None else ghosts
+    G = [n3[d] + 2 * ghosts if d < cfg.dim else 1 for d in range(3)]
     return (cfg.ncomp, G[2], G[1], G[0])
 
 
@@ -207,6 +210,9 @@ def ref_lib():
         L.hmrref_conv_flux_source.argtypes = [ctypes.POINTER(_Cfg), ip, dp, ctypes.c_double, dp, dp, dp]
         L.hmrref_conv_flux_source.restype = ctypes.c_int
         L.hmrref_last_error.restype = ctypes.c_char_p
+        L.hmrref_diff_flux.argtypes = [ctypes.POINTER(_Cfg), ctypes.POINTER(_Transport), ip, ctypes.c_int, dp,
+                                       ctypes.c_double, dp, dp]
+        L.hmrref_diff_flux.restype = ctypes.c_int
         _ref_lib = L
     return _ref_lib
 
@@ -292,6 +298,7 @@ def rk_stage(cfg, n, dx, alpha, beta, gamma, Q_int, F_int, S_int, F_acc=None, S_
 
 
 def fill_ghosts(cfg, n, periodic, Q):
+    """Ghost fill, mode per axis: 0 zero-gradient, 1 periodic, 3 reflecting wall."""
     assert Q.flags["C_CONTIGUOUS"] and Q.dtype == np.float64
     lib().hmro_fill_ghosts(ctypes.byref(cfg.c()), _ip(_n3(n)), _ip(list(periodic) + [0] * (3 - len(periodic))),
                            _dp(Q))
@@ -325,6 +332,21 @@ def _split_flux(cfg, n, flat):
     return out
 
 
+def ref_diff_flux(cfg, tr, n, dx, dt, Q, ghosts=4):
+    """The reference's DiffusiveFluxReconstructorMidpoint::computeDiffusiveFluxOnPatch (single
+    species) on one patch whose conservative variables carry `ghosts` ghost cells per side."""
+    n3 = _n3(n)
+    Q = np.ascontiguousarray(Q, dtype=np.float64)
+    assert Q.shape == ghost_shape(cfg, n, ghosts)
+    flat = np.zeros(sum(int(np.prod(s)) for s in flux_shapes(cfg, n)))
+    L = ref_lib()
+    rc = L.hmrref_diff_flux(ctypes.byref(cfg.c()), ctypes.byref(tr.c()), _ip(n3), int(ghosts),
+                            _dv(list(dx) + [1.0] * (3 - len(dx))), float(dt), _dp(Q), _dp(flat))
+    if rc != 0:
+        raise RuntimeError("reference: " + L.hmrref_last_error().decode())
+    return _split_flux(cfg, n, flat)
+
+
 def diff_flux(cfg, tr, n, dx, dt, Q):
     """computeDiffusiveFluxOnPatch (single species): list of dt-scaled face fluxes per axis."""
     Q = np.ascontiguousarray(Q, dtype=np.float64)
@@ -333,7 +355,7 @@ def diff_flux(cfg, tr, n, dx, dt, Q):
     r = lib().hmro_diff_flux(ctypes.byref(cfg.c()), ctypes.byref(tr.c()), _ip(_n3(n)),
                              _dv(list(dx) + [1.0] * (3 - len(dx))), float(dt), _dp(Q), _dp(flat))
     if r != 0:
-        raise ValueError("the oracle's diffusive flux covers single-species patches, order 2 or 4")
+        raise ValueError("the oracle's diffusive flux covers single-species patches, order 2 or 4 (or 6 with ghosts=5)")
     return _split_flux(cfg, n, flat)
 
 
@@ -357,7 +379,7 @@ def ns_rk3_advance(cfg, tr, n, dx, dt, periodic, nsteps, Q):
                                   _dv(list(dx) + [1.0] * (3 - len(dx))), float(dt),
                                   _ip(list(periodic) + [0] * (3 - len(periodic))), int(nsteps), _dp(Q))
     if r != 0:
-        raise ValueError("the oracle's diffusive flux covers single-species patches, order 2 or 4")
+        raise ValueError("the oracle's diffusive flux covers single-species patches, order 2 or 4 (or 6 with ghosts=5)")
     return Q
 
 

@@ -56,6 +56,7 @@ struct hmrref_config {
 };
 
 const char* hmrref_last_error() { return g_last_error.c_str(); }
+void hmrref_set_error(const char* what) { g_last_error = what; }
 
 int hmrref_conv_flux_source(const hmrref_config* cfg, const int* n, const double* dx, double dt, const double* Q,
                             double* flux, double* source) {

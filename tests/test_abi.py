@@ -89,7 +89,9 @@ def test_diffusive_flux_needs_single_species_and_valid_transport(lib):
     ctx = ctypes.c_void_p()
     assert lib.hmr_ctx_create(ctypes.byref(cfg), ctypes.byref(ctx)) == L.HMR_ERR_UNSUPPORTED
     lib.hmr_config_default(ctypes.byref(cfg), L.HMR_SINGLE_SPECIES, L.HMR_WCNS5_JS_HLLC_HLL, 3, 1)
-    cfg.diffusive_flux_reconstructor = 6
+    cfg.diffusive_flux_reconstructor = 8
+    assert lib.hmr_ctx_create(ctypes.byref(cfg), ctypes.byref(ctx)) == L.HMR_ERR_UNSUPPORTED
+    cfg.diffusive_flux_reconstructor = 3
     assert lib.hmr_ctx_create(ctypes.byref(cfg), ctypes.byref(ctx)) == L.HMR_ERR_UNSUPPORTED
     cfg.diffusive_flux_reconstructor = L.HMR_MIDPOINT_SECOND_ORDER
     cfg.species_Pr = 0.0

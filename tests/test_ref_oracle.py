@@ -100,3 +100,51 @@ def test_vortex_state_is_bitwise_the_reference():
             Q = vortex_state(model, dim, n, seed=2, species_gamma=gam)
             fo, so, fr, sr, _ = run_both(model, dim, gam, R, O.SCHEME_WCNS6_LD, n, Q)
             assert all(np.array_equal(a, b) for a, b in zip(fo, fr)) and np.array_equal(so, sr)
+
+
+# ---------------------------------------------------------------------------
+# Navier-Stokes: DiffusiveFluxReconstructorMidpointSecondOrder / FourthOrder / SixthOrder
+# (src/flow/diffusive_flux_reconstructors/midpoint/) with FlowModelSingleSpecies's diffusive
+# utilities, compiled from the reference's sources into the same library.
+# ---------------------------------------------------------------------------
+DIFF_CASES = [(d, o) for d in (2, 3) for o in (2, 4, 6)]
+
+
+def _wider(gen, dim, n, extra, seed):
+    """A state generated on n grown by `extra` cells per side: ghost width 4 + extra around n."""
+    return gen(O.MODEL_SINGLE_SPECIES, dim, [v + 2 * extra for v in n], seed=seed, species_gamma=[1.4])
+
+
+@pytest.mark.parametrize("dim,order", DIFF_CASES, ids=["%dd-o%d" % c for c in DIFF_CASES])
+def test_oracle_diffusive_flux_is_bitwise_the_reference(dim, order):
+    gh = 5 if order == 6 else 4
+    n = [13, 11] if dim == 2 else [8, 7, 6]
+    dx = [0.1, 0.07, 0.13][:dim]
+    cfg = O.Config(O.MODEL_SINGLE_SPECIES, dim, [1.4], species_R=[287.0], ghosts=gh)
+    tr = O.Transport(0.05, 1004.5, 0.72, mu_v=0.01, order=order, mu_kappa=0.07)
+    for label, gen in (("smooth", smooth_state), ("shock", shock_state), ("rough", rough_state)):
+        Q = _wider(gen, dim, n, gh - 4, seed=5)
+        fo = O.diff_flux(cfg, tr, n, dx, 1.1e-3, Q)
+        fr = O.ref_diff_flux(cfg, tr, n, dx, 1.1e-3, Q, ghosts=gh)
+        for a in range(dim):
+            assert np.array_equal(fo[a], fr[a]), f"{label}: diffusive flux of axis {a}"
+            assert np.any(fo[a] != 0.0)
+
+
+def test_oracle_wider_ghost_box_changes_nothing_else():
+    """The convective flux and the second/fourth-order diffusive flux read at most 4 ghost cells:
+    on a 5-ghost box they equal the 4-ghost results."""
+    for dim, n in ((2, [13, 11]), (3, [8, 7, 6])):
+        Q5 = _wider(shock_state, dim, n, 1, seed=8)
+        inner = (slice(None),) + tuple(slice(1, -1) if a < dim else slice(None) for a in (2, 1, 0))
+        Q4 = np.ascontiguousarray(Q5[inner])
+        c5 = O.Config(O.MODEL_SINGLE_SPECIES, dim, [1.4], species_R=[287.0], ghosts=5)
+        c4 = O.Config(O.MODEL_SINGLE_SPECIES, dim, [1.4], species_R=[287.0])
+        f5, s5, _ = O.conv_flux_source(c5, n, [0.1] * dim, 1e-3, Q5)
+        f4, s4, _ = O.conv_flux_source(c4, n, [0.1] * dim, 1e-3, Q4)
+        assert all(np.array_equal(a, b) for a, b in zip(f5, f4)) and np.array_equal(s5, s4)
+        for order in (2, 4):
+            tr = O.Transport(0.05, 1004.5, 0.72, mu_v=0.01, order=order)
+            d5 = O.diff_flux(c5, tr, n, [0.1] * dim, 1e-3, Q5)
+            d4 = O.diff_flux(c4, tr, n, [0.1] * dim, 1e-3, Q4)
+            assert all(np.array_equal(a, b) for a, b in zip(d5, d4))
