@@ -382,8 +382,7 @@ int hmr_level_autotune(hmr_level* level, double dt, int* threads_out, int* block
  *     is queued: square/cubic patches fit up to 453^2 (2D single species), 397^2 (2D five-equation),
  *     48^3 (3D single species) and 44^3 (3D five-equation) cells.
  *   - The first call on a device resolves the array's device address (cudaGetSymbolAddress with
- *     that device current) and caches it; make that first call before any stream capture.  The
- *     address belongs to the CUDA context: after cudaDeviceReset, or when another context is
+ *     that device current) and caches it.  The address belongs to the CUDA context: after cudaDeviceReset, or when another context is
  *     current on the device, the next call resolves it again (and is again a first call).
  *   - Allocates nothing: no cudaMalloc, cudaFree or allocating library call.  The face counters
  *     of hmr_read_counters are not updated.

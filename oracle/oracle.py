@@ -213,6 +213,8 @@ def ref_lib():
         L.hmrref_diff_flux.argtypes = [ctypes.POINTER(_Cfg), ctypes.POINTER(_Transport), ip, ctypes.c_int, dp,
                                        ctypes.c_double, dp, dp]
         L.hmrref_diff_flux.restype = ctypes.c_int
+        L.hmrref_fill_boundaries.argtypes = [ctypes.POINTER(_Cfg), ip, ip, ctypes.c_int, dp]
+        L.hmrref_fill_boundaries.restype = ctypes.c_int
         _ref_lib = L
     return _ref_lib
 
@@ -330,6 +332,20 @@ def _split_flux(cfg, n, flat):
         out.append(flat[off:off + m].reshape(s))
         off += m
     return out
+
+
+def ref_fill_boundaries(cfg, n, mode, Q, corner_axis=0):
+    """The reference's physical-boundary fill (EulerBoundaryConditions with
+    BasicCartesianBoundaryUtilities2/3) of one patch covering the domain, in place: mode per
+    axis 0 (FLOW) or 3 (REFLECT); corner_axis picks the axis of the X/Y/Z-prefixed corner
+    conditions."""
+    assert Q.flags["C_CONTIGUOUS"] and Q.dtype == np.float64 and Q.shape == ghost_shape(cfg, n)
+    L = ref_lib()
+    rc = L.hmrref_fill_boundaries(ctypes.byref(cfg.c()), _ip(_n3(n)), _ip(list(mode) + [0] * (3 - len(mode))),
+                                  int(corner_axis), _dp(Q))
+    if rc != 0:
+        raise RuntimeError("reference: " + L.hmrref_last_error().decode())
+    return Q
 
 
 def ref_diff_flux(cfg, tr, n, dx, dt, Q, ghosts=4):

@@ -486,13 +486,26 @@ public:
     virtual ~PatchGeometry() {}
 };
 
-// Types that appear only in declarations of services this build does not provide
-// (physical boundaries, hierarchies, levels).
+// A boundary box: the one-cell-thick box of ghost cells beside a patch side, edge or corner
+// that lies on the physical boundary, with its codimension (SAMRAI's boundary type) and its
+// location index (the BDRY_LOC / NODE_BDRY_LOC_2D / EDGE_BDRY_LOC_3D / NODE_BDRY_LOC_3D
+// numbering of CartesianBoundaryDefines.hpp).
 class BoundaryBox {
 public:
-    int getBoundaryType() const { return 0; }
-    int getLocationIndex() const { return 0; }
+    BoundaryBox() : box_(tbox::Dimension(1)) {}
+    BoundaryBox(const Box& box, int type, int loc) : box_(box), type_(type), loc_(loc) {}
+    const Box& getBox() const { return box_; }
+    int getBoundaryType() const { return type_; }
+    int getLocationIndex() const { return loc_; }
+
+private:
+    Box box_;
+    int type_ = 0;
+    int loc_ = 0;
 };
+
+// Types that appear only in declarations of services this build does not provide
+// (hierarchies, levels).
 class PatchHierarchy {};
 class PatchLevel {};
 
@@ -718,15 +731,35 @@ public:
     }
     const double* getDx() const { return dx_; }
     const double* getXLower() const { return xlo_; }
-    // A patch of this build touches no physical boundary: boundary fills find nothing to do.
-    std::vector<hier::BoundaryBox> getCodimensionBoundaries(int) const { return {}; }
-    hier::Box getBoundaryFillBox(const hier::BoundaryBox&, const hier::Box& b, const hier::IntVector&) const {
-        return hier::Box::getEmptyBox(b.getDim());
+    // Boundary boxes of the patch by codimension (1..3); none unless a caller sets them, so a
+    // patch touches no physical boundary by default.
+    void setCodimensionBoundaries(int codim, const std::vector<hier::BoundaryBox>& boxes) { bdry_[codim] = boxes; }
+    std::vector<hier::BoundaryBox> getCodimensionBoundaries(int codim) const {
+        return codim >= 1 && codim <= 3 ? bdry_[codim] : std::vector<hier::BoundaryBox>();
+    }
+    // The ghost cells a boundary box stands for: along each axis on which the box lies
+    // outside the patch, the `gcw` cells beyond that side; along the others the box's own
+    // extent.  Empty where gcw is 0 along an outward axis.
+    hier::Box getBoundaryFillBox(const hier::BoundaryBox& bb, const hier::Box& b, const hier::IntVector& gcw) const {
+        hier::Box f = bb.getBox();
+        for (int d = 0; d < b.getDim().getValue(); d++) {
+            if (f.upper(d) < b.lower(d)) {
+                if (gcw[d] <= 0) return hier::Box::getEmptyBox(b.getDim());
+                f.lower()[d] = b.lower(d) - gcw[d];
+                f.upper()[d] = b.lower(d) - 1;
+            } else if (f.lower(d) > b.upper(d)) {
+                if (gcw[d] <= 0) return hier::Box::getEmptyBox(b.getDim());
+                f.lower()[d] = b.upper(d) + 1;
+                f.upper()[d] = b.upper(d) + gcw[d];
+            }
+        }
+        return f;
     }
 
 private:
     double dx_[3];
     double xlo_[3];
+    std::vector<hier::BoundaryBox> bdry_[4];
 };
 
 }  // namespace geom

@@ -148,3 +148,28 @@ def test_oracle_wider_ghost_box_changes_nothing_else():
             d5 = O.diff_flux(c5, tr, n, [0.1] * dim, 1e-3, Q5)
             d4 = O.diff_flux(c4, tr, n, [0.1] * dim, 1e-3, Q4)
             assert all(np.array_equal(a, b) for a, b in zip(d5, d4))
+
+
+# ---------------------------------------------------------------------------
+# Physical boundaries: the reference's EulerBoundaryConditions split (SCALAR variables SYMMETRY,
+# the momentum REFLECT, at REFLECT walls) over its BasicCartesianBoundaryUtilities2 / 3
+# (src/util/basic_boundary_conditions/), compiled into the same library, on a patch covering
+# the domain with FLOW or REFLECT on every side.
+# ---------------------------------------------------------------------------
+BC_MODES = {2: ([3, 3], [0, 0], [3, 0], [0, 3]), 3: ([3, 3, 3], [0, 0, 0], [3, 0, 3], [0, 3, 0], [3, 3, 0])}
+
+
+@pytest.mark.parametrize("model,mn,gam,R", MODELS, ids=[m[1] for m in MODELS])
+@pytest.mark.parametrize("dim", [2, 3])
+def test_oracle_ghost_fill_is_bitwise_the_reference(model, mn, gam, R, dim):
+    n = [9, 7] if dim == 2 else [6, 5, 7]
+    cfg = O.Config(model, dim, gam, O.SCHEME_WCNS5_JS, species_R=R)
+    for mode in BC_MODES[dim]:
+        for corner_axis in range(dim):   # every choice of the corners' X/Y/Z-prefixed condition
+            Q = smooth_state(model, dim, n, seed=3, species_gamma=gam)
+            Qo = Q.copy()
+            O.fill_ghosts(cfg, n, mode, Qo)
+            Qr = Q.copy()
+            O.ref_fill_boundaries(cfg, n, mode, Qr, corner_axis)
+            assert not np.array_equal(Qr, Q)
+            assert np.array_equal(Qo, Qr), (mode, corner_axis)
