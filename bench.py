@@ -106,7 +106,9 @@ def parse():
                     help="time only the C4 forward (Navier-Stokes Taylor-Green 128^3) for --steps steps after "
                          "--warmup steps and print its line (used for the C4 launch list)")
     ap.add_argument("--c4", action="store_true",
-                    help="also time the 3D Navier-Stokes Taylor-Green workload and its adjoint (128^3, ~1 min)")
+                    help="check the 3D Navier-Stokes Taylor-Green gradient along 16 directions (default 4)")
+    ap.add_argument("--no-c4", action="store_true",
+                    help="skip the 3D Navier-Stokes Taylor-Green workload (128^3) and its adjoint")
     ap.add_argument("--no-c5", action="store_true",
                     help="skip the 3-level 3D five-equation batched substep + amplitude adjoint")
     ap.add_argument("--no-c1", action="store_true",
@@ -917,9 +919,9 @@ def main():
             line["adjoint"] = adjoint_cost(args, flow, Qnp, n, dx, dt)
         except Exception as exc:  # report, never lose the headline line
             line["adjoint"] = {"error": str(exc)[:300]}
-    if args.c4:
+    if not args.no_c4:
         try:
-            line["c4"] = c4_navier_stokes(args, flow)
+            line["c4"] = c4_navier_stokes(args, flow, fd_dirs=16 if args.c4 else 4)
         except Exception as exc:  # report, never lose the headline line
             line["c4"] = {"error": str(exc)[:300]}
     if not args.no_c1:

@@ -3,7 +3,7 @@ diffusive flux): the gradient of the final kinetic energy J = 1/2 sum rho |u|^2 
 respect to the initial state, by the checkpointed reverse sweep (100 SSPRK3 steps,
 checkpoint every 10), against central differences of the forward along 16 seeded
 directions of the initial velocity (seed 3; smooth random modes, density and pressure held).  Run on a 32^3 grid so that the 32 forward runs
-of the differences stay short; the 128^3 workload is timed by bench.py --c4.
+of the differences stay short; the 128^3 workload is timed by bench.py (its default run).
 
 The base point is the vortex with smooth perturbations of amplitude 0.05: the exact vortex
 has w = 0 and mirror-symmetric face states on its symmetry planes, where the reference's
