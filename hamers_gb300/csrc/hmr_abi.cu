@@ -779,7 +779,6 @@ extern "C" {
 int hmr_level_create(hmr_ctx* c, int np, const hmr_patch_geometry* geoms, hmr_level** out) {
     if (!c || np < 1 || !geoms || !out) return HMR_ERR_ARGUMENT;
     *out = nullptr;
-    if (patch_ghosts(c->v) != GHOST) return HMR_ERR_UNSUPPORTED;   // levels carry 4 ghost cells
     for (int p = 0; p < np; p++)
         if (!valid_geom(c->v.dim, &geoms[p])) return HMR_ERR_ARGUMENT;
     hmr_level* lv = new (std::nothrow) hmr_level();
@@ -788,10 +787,11 @@ int hmr_level_create(hmr_ctx* c, int np, const hmr_patch_geometry* geoms, hmr_le
     lv->npatch = np;
     size_t state_tot = 0, scratch_tot = 0;
     std::vector<size_t> scr_off(np);
-    long off_fill = 0, off_cells = 0, off_sensor = 0, off_face[3] = {0, 0, 0}, off_update = 0;
+    long off_fill = 0, off_cells = 0, off_sensor = 0, off_face[3] = {0, 0, 0}, off_dface[3] = {0, 0, 0};
+    long off_update = 0;
     lv->work.resize(np);
     for (int p = 0; p < np; p++) {
-        const Geom g = make_geom(c->v.dim, &geoms[p], GHOST);
+        const Geom g = make_geom(c->v.dim, &geoms[p], patch_ghosts(c->v));
         lv->geoms.push_back(g);
         lv->state_off.push_back(state_tot);
         state_tot += (size_t)2 * c->ncomp * ncell_of(g);
@@ -811,7 +811,11 @@ int hmr_level_create(hmr_ctx* c, int np, const hmr_patch_geometry* geoms, hmr_le
         off_sensor += (long)(g.n[0] + 4) * (g.n[1] + 4) * (c->v.dim == 3 ? g.n[2] + 4 : 1);
         for (int a = 0; a < 3; a++) {
             w.off_face[a] = off_face[a];
-            if (a < c->v.dim) off_face[a] += nface_of(g, a);
+            w.off_dface[a] = off_dface[a];
+            if (a < c->v.dim) {
+                off_face[a] += nface_of(g, a);
+                off_dface[a] += nface_w(g, a, diff_half_width(c->v));
+            }
         }
         w.off_update = off_update;
         off_update += ninterior_of(g);
@@ -848,7 +852,10 @@ int hmr_level_create(hmr_ctx* c, int np, const hmr_patch_geometry* geoms, hmr_le
     lv->L.total_fill = off_fill;
     lv->L.total_cells = off_cells;
     lv->L.total_sensor = off_sensor;
-    for (int a = 0; a < 3; a++) lv->L.total_face[a] = off_face[a];
+    for (int a = 0; a < 3; a++) {
+        lv->L.total_face[a] = off_face[a];
+        lv->L.total_dface[a] = off_dface[a];
+    }
     lv->L.total_update = off_update;
     lv->L.timeout_ns = 2000000000ull;
     lv->L.barrier_extra = 0;
@@ -898,7 +905,7 @@ int hmr_level_set_periodic(hmr_level* lv, int p, const int* periodic) {
     for (int a = 0; a < 3; a++) {
         if (a < lv->ctx->v.dim && (periodic[a] < HMR_FILL_ZERO_GRADIENT || periodic[a] > HMR_FILL_REFLECT))
             return HMR_ERR_ARGUMENT;
-        if (a < lv->ctx->v.dim && periodic[a] == HMR_FILL_REFLECT && lv->geoms[p].n[a] < GHOST)
+        if (a < lv->ctx->v.dim && periodic[a] == HMR_FILL_REFLECT && lv->geoms[p].n[a] < lv->geoms[p].gh)
             return HMR_ERR_ARGUMENT;
         lv->work[p].periodic[a] = a < lv->ctx->v.dim ? periodic[a] : 0;
     }
@@ -909,12 +916,13 @@ int hmr_level_set_periodic(hmr_level* lv, int p, const int* periodic) {
 int hmr_level_set_layout(hmr_level* lv, const int* lo, const int* domain, const int* periodic) {
     if (!lv || !lo || !domain || !periodic) return HMR_ERR_ARGUMENT;
     const int dim = lv->ctx->v.dim;
+    const int gh = patch_ghosts(lv->ctx->v);
     int dom[3] = {1, 1, 1}, per[3] = {0, 0, 0};
     for (int a = 0; a < dim; a++) {
         if (domain[a] < 1 || (periodic[a] != 0 && periodic[a] != 1 && periodic[a] != HMR_FILL_REFLECT))
             return HMR_ERR_ARGUMENT;
         // the mirror images of a reflecting wall's ghost cells lie in the domain
-        if (periodic[a] == HMR_FILL_REFLECT && domain[a] < GHOST) return HMR_ERR_ARGUMENT;
+        if (periodic[a] == HMR_FILL_REFLECT && domain[a] < gh) return HMR_ERR_ARGUMENT;
         dom[a] = domain[a];
         per[a] = periodic[a];
     }
@@ -940,12 +948,12 @@ int hmr_level_set_layout(hmr_level* lv, const int* lo, const int* domain, const 
     long total = 0;
     int kmax[3] = {0, 0, 0};
     for (int a = 0; a < dim; a++)
-        if (per[a] == 1) kmax[a] = (GHOST + dom[a] - 1) / dom[a];
+        if (per[a] == 1) kmax[a] = (gh + dom[a] - 1) / dom[a];
     for (int p = 0; p < np; p++) {
         int glo[3], ghi[3];
         for (int a = 0; a < 3; a++) {
-            glo[a] = a < dim ? blo[p][a] - GHOST : 0;
-            ghi[a] = a < dim ? bhi[p][a] + GHOST : 1;
+            glo[a] = a < dim ? blo[p][a] - gh : 0;
+            ghi[a] = a < dim ? bhi[p][a] + gh : 1;
         }
         for (int q = 0; q < np; q++)
             for (int k0 = -kmax[0]; k0 <= kmax[0]; k0++)

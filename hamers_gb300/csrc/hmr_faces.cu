@@ -246,8 +246,9 @@ constexpr int level_min_blocks() {
 #endif
 }
 
-// DORD: 0 for the Euler equations, 2 or 4 for NavierStokes with that diffusive order (single
-// species); a separate instantiation, so that the Euler kernel keeps its registers.
+// DORD: 0 for the Euler equations, 2, 4 or 6 for NavierStokes with that diffusive order (single
+// species; the sixth order on 5-ghost patch arrays); a separate instantiation, so that the
+// Euler kernel keeps its registers.
 template <int DIM, int MODEL, int NSP, int SCHEME, int DORD>
 __global__ void __launch_bounds__(LEVEL_MAX_THREADS, level_min_blocks<DIM, MODEL, DORD>())
 level_kernel(Params P, LevelArgs L) {
@@ -314,18 +315,18 @@ level_kernel(Params P, LevelArgs L) {
     HMR_BARRIER();
     if constexpr (DORD != 0) {
         // NavierStokes: midpoint diffusive fluxes (needs the node gradient), beside the faces
-        for (long t = t0; t < L.total_face[0]; t += stride) {
-            const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_face[0]; });
-            diff_mid_item<DIM, DORD, 0>(P, W[p].g, W[p].S, t - W[p].off_face[0]);
+        for (long t = t0; t < L.total_dface[0]; t += stride) {
+            const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_dface[0]; });
+            diff_mid_item<DIM, DORD, 0>(P, W[p].g, W[p].S, t - W[p].off_dface[0]);
         }
-        for (long t = t0; t < L.total_face[1]; t += stride) {
-            const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_face[1]; });
-            diff_mid_item<DIM, DORD, 1>(P, W[p].g, W[p].S, t - W[p].off_face[1]);
+        for (long t = t0; t < L.total_dface[1]; t += stride) {
+            const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_dface[1]; });
+            diff_mid_item<DIM, DORD, 1>(P, W[p].g, W[p].S, t - W[p].off_dface[1]);
         }
         if constexpr (DIM == 3) {
-            for (long t = t0; t < L.total_face[2]; t += stride) {
-                const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_face[2]; });
-                diff_mid_item<DIM, DORD, 2>(P, W[p].g, W[p].S, t - W[p].off_face[2]);
+            for (long t = t0; t < L.total_dface[2]; t += stride) {
+                const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_dface[2]; });
+                diff_mid_item<DIM, DORD, 2>(P, W[p].g, W[p].S, t - W[p].off_dface[2]);
             }
         }
     }
@@ -394,6 +395,7 @@ static int with_dorder(const Variant& v, F f) {
     if constexpr (T::MODEL == SINGLE_SPECIES) {
         if (v.dorder == 4) return f(std::integral_constant<int, 4>{});
         if (v.dorder == 2) return f(std::integral_constant<int, 2>{});
+        if (v.dorder == 6) return f(std::integral_constant<int, 6>{});
     }
     if (v.dorder != 0) return -2;
     return f(std::integral_constant<int, 0>{});

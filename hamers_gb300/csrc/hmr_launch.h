@@ -150,6 +150,7 @@ struct PatchWork {
     long off_cells;
     long off_sensor;
     long off_face[3];
+    long off_dface[3];   // diffusive midpoints (faces -W .. n + W; W = 2 at sixth order, else 1)
     long off_update;
 };
 
@@ -167,6 +168,7 @@ struct LevelArgs {
     int npatch;
     int ncomp;
     long total_fill, total_cells, total_sensor, total_face[3], total_update;
+    long total_dface[3];
     double alpha[3];
     int nst;
     double beta;

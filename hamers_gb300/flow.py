@@ -551,7 +551,8 @@ class BatchedLevel:
             for d in range(3):
                 arr[i].n[d] = nn[d] if d < dim else 1
                 arr[i].dx[d] = dx[d] if d < dim else 1.0
-            G = [nn[d] + 2 * GHOST if d < dim else 1 for d in range(3)]
+            gh = reconstructor.getPatchNumberOfGhostCells()
+            G = [nn[d] + 2 * gh if d < dim else 1 for d in range(3)]
             self.shapes.append((reconstructor.ncomp, G[2], G[1], G[0]))
         lv = ctypes.c_void_p()
         L.check("hmr_level_create", self._lib.hmr_level_create(reconstructor.ctx, n, arr, ctypes.byref(lv)))

@@ -245,3 +245,47 @@ def test_full_size_navier_stokes_step_conserves_totals(cuda):
     ke0 = 0.5 * np.sum((before[1] ** 2 + before[2] ** 2 + before[3] ** 2) / before[0])
     ke1 = 0.5 * np.sum((after[1] ** 2 + after[2] ** 2 + after[3] ** 2) / after[0])
     assert ke1 < ke0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["exact", "fast"])
+def test_c1_full_size_every_substep_matches_oracle(cuda, precision):
+    """The 2D single-species workload at its full size (256^2 density wave, WCNS5-JS + HLLC-HLL,
+    periodic, one SSPRK3 step at CFL 0.4): the flux and source of every substep's input state
+    against the oracle's (exact form bitwise, fast form within 1e-12 per axis), the stage states
+    advanced by the oracle; then the whole step through the per-patch integrator against the
+    oracle's step."""
+    import torch
+    from hamers_gb300 import flow
+    from tests.test_gpu_parity import gpu_flux
+    n = [256, 256]
+    Q, dx, dt = P.density_wave_2d(256)
+    cfg = O.Config(O.MODEL_SINGLE_SPECIES, 2, [1.4], O.SCHEME_WCNS5_JS)
+    fm = flow.FlowModel("SINGLE_SPECIES", 2, [1.4])
+    rec = flow.ConvectiveFluxReconstructor("WCNS5_JS_HLLC_HLL", fm, precision=precision)
+    per = [1, 1]
+    X = np.ascontiguousarray(Q.copy())
+    O.fill_ghosts(cfg, n, per, X)
+    Qint, Fint, Sint = [X], [], []
+    for s in range(3):
+        Fo, So, _ = O.conv_flux_source(cfg, n, dx, dt, Qint[s])
+        Fg, Sg = gpu_flux(rec, n, dx, dt, Qint[s])
+        for a in range(2):
+            if precision == "exact":
+                assert np.array_equal(Fg[a], Fo[a]), f"substep {s} axis {a}"
+            else:
+                assert _axis_err(Fg[a], Fo[a]) <= 1e-12, f"substep {s} axis {a}: {_axis_err(Fg[a], Fo[a]):.3e}"
+        Fint.append(Fo)
+        Sint.append(So)
+        Xn = O.rk_stage(cfg, n, dx, flow.RK3_ALPHA[s], flow.RK3_BETA[s], flow.RK3_GAMMA[s], Qint, Fint, Sint)
+        O.fill_ghosts(cfg, n, per, Xn)
+        Qint.append(Xn)
+    Qg = torch.from_numpy(Q.copy()).cuda()
+    flow.RungeKuttaLevelIntegrator(flow.Euler(rec), flow.Patch(n, dx, Qg), per).advance(dt, nsteps=1)
+    got = Qg.cpu().numpy()[:, :, G:-G, G:-G]
+    want = Qint[3][:, :, G:-G, G:-G]
+    if precision == "exact":
+        assert np.array_equal(got, want)
+    else:
+        assert rel_err(got, want) <= 1e-12
+    rec.close()

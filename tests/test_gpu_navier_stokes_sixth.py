@@ -5,7 +5,9 @@ sixth order is bitwise the reference's own code (tests/test_ref_oracle.py).
 Exact form bitwise (diffusive face fluxes, the general NavierStokes stage, SSPRK3 steps of the
 fused substep, the spectral radius over the 5-ghost box, reflecting and periodic ghost fills);
 fast form within 1e-12 per flux and 1e-9 over two steps.  A sixth-order context reads and writes
-5-ghost patch arrays everywhere, has no batched level and no substep VJP.
+5-ghost patch arrays everywhere, the batched level's included (uneven patches with their own
+fills, and a tiled domain with the device ghost exchange, against the oracle); it has no
+substep VJP.
 """
 import numpy as np
 import pytest
@@ -189,15 +191,116 @@ def test_sixth_order_spectral_radius_and_fills(cuda, case):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["exact", "fast"])
+@pytest.mark.parametrize("case", CASES, ids=IDS)
+def test_sixth_order_batched_level(cuda, case, precision):
+    """Uneven patches of one level in the persistent kernel (5-ghost arrays, each patch with its
+    own periodic or reflecting fill): exact form bitwise to the oracle's NavierStokes steps per
+    patch, fast form within 1e-9."""
+    import torch
+    from hamers_gb300 import flow
+    dim, _ = case
+    rng = np.random.default_rng(29)
+    if dim == 2:
+        sizes = [(int(rng.integers(6, 26)), int(rng.integers(6, 26))) for _ in range(4)]
+    else:
+        sizes = [tuple(int(rng.integers(5, 12)) for _ in range(3)) for _ in range(3)]
+    cfg = cfg_of(dim)
+    ns = make(dim, precision)
+    dt = 1.0e-3
+    geoms, tens, expect, pers = [], [], [], []
+    for p, n in enumerate(sizes):
+        dx = [1.0 / v for v in n]
+        per = [3 if (p + a) % 2 else 1 for a in range(dim)]
+        Q = state(smooth_state, dim, n, 40 + p)
+        Qo = Q.copy()
+        O.fill_ghosts(cfg, n, per, Qo)
+        O.ns_rk3_advance(cfg, transport(), n, dx, dt, per, 2, Qo)
+        geoms.append((list(n), dx))
+        tens.append(torch.from_numpy(Q).cuda())
+        expect.append(Qo)
+        pers.append(per)
+    lv = flow.BatchedLevel(ns.rec, geoms)
+    for p, Q in enumerate(tens):
+        assert tuple(Q.shape) == lv.shapes[p]
+        lv.bind(p, Q)
+        lv.set_periodic(p, pers[p])
+    for _ in range(2):
+        lv.step(dt)
+    torch.cuda.synchronize()
+    lv.check()
+    sl = interior(dim)
+    for Q, Qo in zip(tens, expect):
+        got = Q.cpu().numpy()[sl]
+        if precision == "exact":
+            assert np.array_equal(got, Qo[sl]), np.abs(got - Qo[sl]).max()
+        else:
+            assert rel_err(got, Qo[sl]) <= 1e-9
+    lv.close()
+    ns.rec.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", [(2, (36, 30), (1, 3)), (3, (15, 13, 12), (3, 1, 1))], ids=["2d", "3d"])
+def test_sixth_order_tiled_level_equals_one_patch(cuda, case):
+    """A domain tiled by uneven patches (down to two cells wide), advanced by the batched
+    substeps with the device ghost exchange over 5-cell halos, equals the oracle's single patch
+    covering the domain, bitwise (exact form)."""
+    import torch
+    from hamers_gb300 import flow
+    from tests.test_gpu_exchange import _tile
+    dim, domain, periodic = case
+    cfg = cfg_of(dim)
+    dx = [1.0 / v for v in domain]
+    dt, nsteps = 1.0e-3, 2
+    Qfull = state(shock_state, dim, domain, 31)
+    Qo = Qfull.copy()
+    O.fill_ghosts(cfg, domain, list(periodic), Qo)
+    O.ns_rk3_advance(cfg, transport(), domain, dx, dt, list(periodic), nsteps, Qo)
+    rng = np.random.default_rng(9)
+    segs = [_tile(domain[a], rng, 2, 13 if dim == 2 else 7) for a in range(dim)]
+    starts = [np.concatenate([[0], np.cumsum(s)[:-1]]).astype(int) for s in segs]
+    boxes = []
+    for idx in np.ndindex(*[len(s) for s in segs]):
+        boxes.append(([int(starts[a][idx[a]]) for a in range(dim)], [int(segs[a][idx[a]]) for a in range(dim)]))
+
+    def block(Q, lo, n):
+        sl = [slice(None)]
+        for a in (2, 1, 0):
+            sl.append(slice(lo[a] + GH, lo[a] + GH + n[a]) if a < dim else slice(None))
+        return Q[tuple(sl)]
+
+    inner = interior(dim)
+    states = []
+    for lo, n in boxes:
+        Q = np.zeros((Qfull.shape[0],) + tuple(n[a] + 2 * GH if a < dim else 1 for a in (2, 1, 0)))
+        Q[inner] = block(Qfull, lo, n)
+        states.append(torch.from_numpy(Q).cuda())
+    ns = make(dim, "exact")
+    lv = flow.BatchedLevel(ns.rec, [(n, dx) for _, n in boxes])
+    for p, Q in enumerate(states):
+        lv.bind(p, Q)
+    lv.set_layout([lo for lo, _ in boxes], list(domain), list(periodic))
+    for _ in range(nsteps):
+        lv.step(dt)
+    torch.cuda.synchronize()
+    lv.check()
+    for (lo, n), Q in zip(boxes, states):
+        got = Q.cpu().numpy()[inner]
+        ref = block(Qo, lo, n)
+        assert np.array_equal(got, ref), f"patch at {lo}: max diff {np.abs(got - ref).max()}"
+    lv.close()
+    ns.rec.close()
+
+
+@pytest.mark.gpu
 def test_sixth_order_unsupported_forms(cuda):
-    """No batched level (levels carry 4 ghost cells) and no substep VJP at sixth order."""
+    """No substep VJP at sixth order (its reverse stencils are the second- and fourth-order ones)."""
     import torch
     from hamers_gb300 import flow
     from hamers_gb300 import _lib as L
     ns = make(2, "exact")
     n = (12, 10)
-    with pytest.raises(L.HmrError):
-        flow.BatchedLevel(ns.rec, [(list(n), [0.1, 0.1])])
     Q = torch.from_numpy(state(smooth_state, 2, n, 3)).cuda()
     with pytest.raises(L.HmrError):
         ns.substepVJP(flow.Patch(n, [0.1, 0.1], Q), 0, [Q], 1e-3, torch.zeros_like(Q), [torch.zeros_like(Q)])
