@@ -483,7 +483,6 @@ int hmr_rk_substep_vjp_patch(hmr_ctx* c, const hmr_patch_geometry* pg, int stage
                              const double* const* Qbar_out, double* const* const* Qbar_int, void* stream) {
     if (!c || !valid_geom(c->v.dim, pg) || !alpha || !Q_int || !Qbar_out || !Qbar_int || stage < 0 || stage > 2)
         return HMR_ERR_ARGUMENT;
-    if (c->P.dorder == HMR_MIDPOINT_SIXTH_ORDER) return HMR_ERR_UNSUPPORTED;   // reverse stencils: orders 2, 4
     VjpArgs A;
     std::memset(&A, 0, sizeof(A));
     if (!load_comp(A.Qs, Q_int[stage], c->ncomp)) return HMR_ERR_ARGUMENT;
@@ -509,7 +508,7 @@ int hmr_rk_substep_vjp_patch(hmr_ctx* c, const hmr_patch_geometry* pg, int stage
     // Navier-Stokes: midpoint adjoints, node-gradient and primitive-variable adjoints
     const int nmb = c->v.dim + (c->v.dim + 1) + 2 * (c->v.dim - 1);
     if (c->P.dorder) {
-        for (int a = 0; a < c->v.dim; a++) need += (size_t)nmb * nface_of(g, a);
+        for (int a = 0; a < c->v.dim; a++) need += (size_t)nmb * nface_w(g, a, diff_half_width(c->v));
         need += (size_t)(c->v.dim * c->v.dim + c->neq) * ncell_of(g);
     }
     need *= sizeof(double);
@@ -540,7 +539,10 @@ int hmr_rk_substep_vjp_patch(hmr_ctx* c, const hmr_patch_geometry* pg, int stage
     for (int a = 0; a < 3; a++) A.Mb[a] = nullptr;
     A.Gdb = A.Dv = nullptr;
     if (c->P.dorder) {
-        for (int a = 0; a < c->v.dim; a++) { A.Mb[a] = p; p += (size_t)nmb * nface_of(g, a); }
+        for (int a = 0; a < c->v.dim; a++) {
+            A.Mb[a] = p;
+            p += (size_t)nmb * nface_w(g, a, diff_half_width(c->v));
+        }
         A.Gdb = p; p += (size_t)c->v.dim * c->v.dim * ncell_of(g);
         A.Dv = p; p += (size_t)c->neq * ncell_of(g);
     }

@@ -4,7 +4,8 @@
 //   cells       T = p/((gamma - 1) c_v rho), node gradient Gd_{d,c} = stencil_d(u_c)
 //   midpoints   F_mid = sum_terms D_k(u_mid) * g,  g a normal derivative of u_c or T,
 //               or a transverse node gradient interpolated to the midpoint
-//   faces       F_face = dt*(a_r F_mid + b_r (F_mid(-1) + F_mid(+1)))   (fourth order)
+//   faces       F_face = dt*(a_r F_mid + b_r (F_mid(-1) + F_mid(+1)))   (fourth order;
+//               + c_r (F_mid(-2) + F_mid(+2)) at sixth order)
 //   update      Q_out += beta*(-(F_face,R - F_face,L)/dx)
 // The reverse pass gathers, so that every sum has a fixed order:
 //   diff_mid_bwd_item  (midpoints)  adjoints of the side velocities, normal derivatives
@@ -30,38 +31,51 @@ __device__ __forceinline__ int diff_tslot(int dim, int d, int c) {
     return dim + (dim + 1) + 2 * rank + (c == A ? 0 : 1);
 }
 
-// Face-set index (index along A from -1 to n_A + 1, interior elsewhere) of the midpoint at
-// coordinate f along A and the transverse coordinates of (i, j, k); -1 if outside.
-template <int DIM, int A>
+// Midpoint-set index (index along A from -W to n_A + W, interior elsewhere; W = diff_w<ORD>)
+// of the midpoint at coordinate f along A and the transverse coordinates of (i, j, k); -1 if
+// outside.
+template <int DIM, int A, int W>
 __device__ __forceinline__ long diff_face_set_index(const Geom& g, int i, int j, int k, int f) {
     int c[3] = {i, j, k};
     c[A] = f;
-    if (f < -1 || f > g.n[A] + 1) return -1;
+    if (f < -W || f > g.n[A] + W) return -1;
 #pragma unroll
     for (int b = 0; b < DIM; b++)
         if (b != A && (c[b] < 0 || c[b] >= g.n[b])) return -1;
-    const long e0 = g.n[0] + (A == 0 ? 3 : 0);
-    const long e1 = g.n[1] + (A == 1 ? 3 : 0);
-    return (long)(c[0] + (A == 0)) + (long)(c[1] + (A == 1)) * e0 + (DIM == 3 ? (long)(c[2] + (A == 2)) * e0 * e1 : 0);
+    const long e0 = g.n[0] + (A == 0 ? 1 + 2 * W : 0);
+    const long e1 = g.n[1] + (A == 1 ? 1 + 2 * W : 0);
+    return (long)(c[0] + (A == 0 ? W : 0)) + (long)(c[1] + (A == 1 ? W : 0)) * e0 +
+           (DIM == 3 ? (long)(c[2] + (A == 2 ? W : 0)) * e0 * e1 : 0);
 }
 
-// Weights of the four cells xs[m] = x_f + (m - 2) e_A of a midpoint: interpolation and
-// normal derivative (without 1/dx).
+// Stencil half-width of the midpoint stencils: cells xs[m] = x_f + (m - H) e_A, m = 0 .. 2H-1
+// (the second order reads the inner two of four).
+template <int ORD>
+__host__ __device__ constexpr int diff_h() { return ORD == 6 ? 3 : 2; }
+
+// Weights of the cells xs[m] of a midpoint: interpolation and normal derivative (without 1/dx).
 template <int ORD>
 __device__ __forceinline__ double dw_value(int m) {
     if constexpr (ORD == 2) return (m == 1 || m == 2) ? 0.5 : 0.0;
-    else return (m == 1 || m == 2) ? 9.0/16.0 : -1.0/16.0;
+    else if constexpr (ORD == 4) return (m == 1 || m == 2) ? 9.0/16.0 : -1.0/16.0;
+    else return (m == 2 || m == 3) ? 75.0/128.0 : ((m == 1 || m == 4) ? -25.0/256.0 : 3.0/256.0);
 }
 template <int ORD>
 __device__ __forceinline__ double dw_deriv(int m) {
     if constexpr (ORD == 2) return m == 1 ? -1.0 : (m == 2 ? 1.0 : 0.0);
-    else return m == 0 ? 1.0/24.0 : (m == 1 ? -9.0/8.0 : (m == 2 ? 9.0/8.0 : -1.0/24.0));
+    else if constexpr (ORD == 4) return m == 0 ? 1.0/24.0 : (m == 1 ? -9.0/8.0 : (m == 2 ? 9.0/8.0 : -1.0/24.0));
+    else return m == 0 ? -3.0/640.0 : m == 1 ? 25.0/384.0 : m == 2 ? -75.0/64.0 :
+                m == 3 ? 75.0/64.0 : m == 4 ? -25.0/384.0 : 3.0/640.0;
 }
-// Weight of u(y + l e_d) in the node gradient at y (l = -2, -1, 1, 2; without 1/dx).
+// Weight of u(y + l e_d) in the node gradient at y (l = -H .. H, l != 0; without 1/dx).
 template <int ORD>
 __device__ __forceinline__ double dw_node(int l) {
     if constexpr (ORD == 2) return l == 1 ? 0.5 : (l == -1 ? -0.5 : 0.0);
-    else return l == 1 ? 2.0/3.0 : (l == -1 ? -2.0/3.0 : (l == 2 ? -1.0/12.0 : 1.0/12.0));
+    else if constexpr (ORD == 4) return l == 1 ? 2.0/3.0 : (l == -1 ? -2.0/3.0 : (l == 2 ? -1.0/12.0 : 1.0/12.0));
+    else {
+        const double w = (l == 1 || l == -1) ? 3.0/4.0 : ((l == 2 || l == -2) ? -3.0/20.0 : 1.0/60.0);
+        return l > 0 ? w : -w;
+    }
 }
 
 template <int DIM, int ORD, int A>
@@ -69,10 +83,16 @@ __device__ __forceinline__ void diff_mid_bwd_item(const Params& P, const Geom& g
                                                   const VjpArgs& VA, long t) {
     constexpr int NEQ = DIM + 2;
     constexpr int NMB = diff_nmb<DIM>();
-    const long nf = nface_of(g, A);
-    int i, j, k;
-    long xR, st;
-    face_coords<DIM, A>(g, t, i, j, k, xR, st);
+    constexpr int W = diff_w<ORD>();
+    constexpr int H = diff_h<ORD>();
+    const long nf = nface_w(g, A, W);
+    const int e0 = g.n[0] + (A == 0 ? 1 + 2 * W : 0);
+    const int e1 = g.n[1] + (A == 1 ? 1 + 2 * W : 0);
+    const int i = (int)(t % e0) - (A == 0 ? W : 0);
+    const int j = (int)((t / e0) % e1) - (A == 1 ? W : 0);
+    const int k = DIM == 3 ? (int)(t / ((long)e0 * e1)) - (A == 2 ? W : 0) : 0;
+    const long xR = cidx<DIM>(g, i, j, k);
+    const long st = A == 0 ? 1 : (A == 1 ? (long)g.G[0] : (long)g.G[0] * g.G[1]);
     const int ia = A == 0 ? i : (A == 1 ? j : k);
     // adjoint of F_mid from the face fluxes that read it
     double Fmb[NEQ];
@@ -82,10 +102,17 @@ __device__ __forceinline__ void diff_mid_bwd_item(const Params& P, const Geom& g
         const double c0 = Fface_bar<DIM, SINGLE_SPECIES, 1, A>(g, VA, i, j, k, ia, e);
         if constexpr (ORD == 2) {
             Fmb[e] = VA.dt*c0;
-        } else {
+        } else if constexpr (ORD == 4) {
             const double cm = Fface_bar<DIM, SINGLE_SPECIES, 1, A>(g, VA, i, j, k, ia - 1, e);
             const double cp = Fface_bar<DIM, SINGLE_SPECIES, 1, A>(g, VA, i, j, k, ia + 1, e);
             Fmb[e] = VA.dt*(13.0/12.0*c0 - 1.0/24.0*(cm + cp));
+        } else {
+            const double cm = Fface_bar<DIM, SINGLE_SPECIES, 1, A>(g, VA, i, j, k, ia - 1, e);
+            const double cp = Fface_bar<DIM, SINGLE_SPECIES, 1, A>(g, VA, i, j, k, ia + 1, e);
+            const double cmm = Fface_bar<DIM, SINGLE_SPECIES, 1, A>(g, VA, i, j, k, ia - 2, e);
+            const double cpp = Fface_bar<DIM, SINGLE_SPECIES, 1, A>(g, VA, i, j, k, ia + 2, e);
+            const double a_m = 75.0/64.0, b_m = -25.0/384.0, c_m = 3.0/640.0;
+            Fmb[e] = VA.dt*((a_m + b_m + c_m)*c0 + (b_m + c_m)*(cm + cp) + c_m*(cmm + cpp));
         }
         any = any || Fmb[e] != 0.0;
     }
@@ -97,30 +124,39 @@ __device__ __forceinline__ void diff_mid_bwd_item(const Params& P, const Geom& g
     }
     // forward values (as diff_mid_item)
     const long nc = ncell_of(g);
-    const long xs[4] = {xR - 2 * st, xR - st, xR, xR + st};
+    constexpr int O = ORD == 2 ? 1 : 0;
+    long xs[2 * H];
+#pragma unroll
+    for (int m = 0; m < 2 * H; m++) xs[m] = xR + (m - H) * st;
+    auto gather = [&](const double* f, double* v) {
+#pragma unroll
+        for (int m = 0; m < 2 * H; m++) v[m] = f[xs[m]];
+    };
     const double* V = S.V;
+    double v[2 * H];
     double um[3] = {0.0, 0.0, 0.0};
 #pragma unroll
     for (int c = 0; c < DIM; c++) {
-        const double* u = V + (1 + c) * nc;
-        um[c] = dmid_value<ORD>(u[xs[0]], u[xs[1]], u[xs[2]], u[xs[3]]);
+        gather(V + (1 + c) * nc, v);
+        um[c] = dmid_value<ORD>(v + O);
     }
     double gr[3][4] = {{0.0, 0.0, 0.0, 0.0}, {0.0, 0.0, 0.0, 0.0}, {0.0, 0.0, 0.0, 0.0}};
     const double dxa_inv = double(1)/g.dx[A];
 #pragma unroll
     for (int c = 0; c < DIM; c++) {
-        const double* u = V + (1 + c) * nc;
-        gr[A][c] = dmid_derivative<ORD>(u[xs[0]], u[xs[1]], u[xs[2]], u[xs[3]], dxa_inv);
+        gather(V + (1 + c) * nc, v);
+        gr[A][c] = dmid_derivative<ORD>(v + O, dxa_inv);
     }
-    gr[A][3] = dmid_derivative<ORD>(S.Td[xs[0]], S.Td[xs[1]], S.Td[xs[2]], S.Td[xs[3]], dxa_inv);
+    gather(S.Td, v);
+    gr[A][3] = dmid_derivative<ORD>(v + O, dxa_inv);
 #pragma unroll
     for (int d = 0; d < DIM; d++) {
         if (d == A) continue;
 #pragma unroll
         for (int c = 0; c < DIM; c++) {
             if (c != A && c != d) continue;
-            const double* G = S.Gd + (long)(d * DIM + c) * nc;
-            gr[d][c] = dmid_value<ORD>(G[xs[0]], G[xs[1]], G[xs[2]], G[xs[3]]);
+            gather(S.Gd + (long)(d * DIM + c) * nc, v);
+            gr[d][c] = dmid_value<ORD>(v + O);
         }
     }
     double Dk[8];
@@ -178,13 +214,15 @@ __device__ __forceinline__ void diff_gd_bwd_item(const Geom& g, const VjpArgs& V
     for (int d = 0; d < DIM; d++)
 #pragma unroll
         for (int q = 0; q < DIM; q++) Gb[d][q] = 0.0;
+    constexpr int W = diff_w<ORD>();
+    constexpr int H = diff_h<ORD>();
     auto axis = [&](auto AC) {
         constexpr int A = decltype(AC)::value;
-        const long nf = nface_of(g, A);
+        const long nf = nface_w(g, A, W);
         const double* Mb = VA.Mb[A];
 #pragma unroll
-        for (int m = 0; m < 4; m++) {
-            const long t = diff_face_set_index<DIM, A>(g, c[0], c[1], c[2], c[A] + 2 - m);
+        for (int m = 0; m < 2 * H; m++) {
+            const long t = diff_face_set_index<DIM, A, W>(g, c[0], c[1], c[2], c[A] + H - m);
             if (t < 0) continue;
             const double w = dw_value<ORD>(m);
 #pragma unroll
@@ -214,14 +252,16 @@ __device__ __forceinline__ void diff_cell_bwd_item(const Params& P, const Geom& 
     int c[3];
     diff_cell_coords<DIM>(g, x, c);
     double ub[3] = {0.0, 0.0, 0.0}, Tb = 0.0;
+    constexpr int W = diff_w<ORD>();
+    constexpr int H = diff_h<ORD>();
     auto axis = [&](auto AC) {
         constexpr int A = decltype(AC)::value;
-        const long nf = nface_of(g, A);
+        const long nf = nface_w(g, A, W);
         const double* Mb = VA.Mb[A];
         const double dxi = double(1)/g.dx[A];
 #pragma unroll
-        for (int m = 0; m < 4; m++) {
-            const long t = diff_face_set_index<DIM, A>(g, c[0], c[1], c[2], c[A] + 2 - m);
+        for (int m = 0; m < 2 * H; m++) {
+            const long t = diff_face_set_index<DIM, A, W>(g, c[0], c[1], c[2], c[A] + H - m);
             if (t < 0) continue;
             const double wv = dw_value<ORD>(m), wd = dw_deriv<ORD>(m)*dxi;
 #pragma unroll
@@ -238,7 +278,7 @@ __device__ __forceinline__ void diff_cell_bwd_item(const Params& P, const Geom& 
         const int cd = c[d] + g.gh;
         const double dxi = double(1)/g.dx[d];
 #pragma unroll
-        for (int l = -2; l <= 2; l++) {
+        for (int l = -H; l <= H; l++) {
             if (l == 0 || cd - l < 0 || cd - l >= g.G[d]) continue;
             const long y = x - l * st;
             const double w = dw_node<ORD>(l)*dxi;

@@ -132,7 +132,7 @@ inline void vjp_item_counts(const Variant& v, const Geom& g, long* n) {
         const long nf = nface_of(g, a);
         n[VJP_PH_PROJ * 3 + a] = n[VJP_PH_RIEM * 3 + a] = n[VJP_PH_CHAR * 3 + a] = nf;
         n[VJP_PH_FWD * 3 + a] = n[VJP_PH_BWDW * 3 + a] = nf * neq;
-        if (v.dorder) n[VJP_PH_DMID * 3 + a] = nf;
+        if (v.dorder) n[VJP_PH_DMID * 3 + a] = nface_w(g, a, v.dorder == 6 ? 2 : 1);
     }
     if (v.dorder) n[VJP_PH_DGD * 3] = n[VJP_PH_DCELL * 3] = ncell_of(g);
     n[VJP_PH_CELLB * 3] = ncell_of(g);

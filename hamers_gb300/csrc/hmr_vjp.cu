@@ -116,16 +116,18 @@ static void launch_diff(const Params& P, const VjpWork* W, int np, const long* t
     launch_phase<T, ORD, VJP_PH_DCELL, 0>(P, W, np, totals, st);
 }
 
+// The convective and cell phases do not depend on the diffusive order: one instantiation
+// (ORD 0) serves the Euler and every Navier-Stokes order.
 template <class T, int ORD>
 static int launch_group(const Params& P, const VjpWork* W, int np, const long* totals, bool flux_terms,
                         cudaStream_t st) {
     if (flux_terms) {
-        launch_axis<T, ORD, 0>(P, W, np, totals, st);
-        launch_axis<T, ORD, 1>(P, W, np, totals, st);
-        if constexpr (T::DIM == 3) launch_axis<T, ORD, 2>(P, W, np, totals, st);
+        launch_axis<T, 0, 0>(P, W, np, totals, st);
+        launch_axis<T, 0, 1>(P, W, np, totals, st);
+        if constexpr (T::DIM == 3) launch_axis<T, 0, 2>(P, W, np, totals, st);
         if constexpr (ORD != 0) launch_diff<T, ORD>(P, W, np, totals, st);
     }
-    launch_phase<T, ORD, VJP_PH_CELLB, 0>(P, W, np, totals, st);
+    launch_phase<T, 0, VJP_PH_CELLB, 0>(P, W, np, totals, st);
     return (int)cudaPeekAtLastError();
 }
 
@@ -136,6 +138,7 @@ int launch_vjp_level(const Variant& v, const Params& P, const VjpWork* W, int np
         if constexpr (T::MODEL == SINGLE_SPECIES) {
             if (P.dorder == 4) return launch_group<T, 4>(P, W, np, totals, flux_terms, st);
             if (P.dorder == 2) return launch_group<T, 2>(P, W, np, totals, flux_terms, st);
+            if (P.dorder == 6) return launch_group<T, 6>(P, W, np, totals, flux_terms, st);
         }
         if (P.dorder != 0) return -2;
         return launch_group<T, 0>(P, W, np, totals, flux_terms, st);

@@ -78,8 +78,7 @@ typedef enum {
  * none (the Euler equations) or the midpoint reconstructors of the given order
  * (DiffusiveFluxReconstructorMidpointSecondOrder / ...FourthOrder / ...SixthOrder).  Single
  * species only.  The sixth order reads 5 ghost cells, so a context with it takes patch arrays
- * of ghost width 5 everywhere (hmr_num_patch_ghosts, the level's bound states included) and has
- * no substep VJP (HMR_ERR_UNSUPPORTED). */
+ * of ghost width 5 everywhere (hmr_num_patch_ghosts, the level's bound states included). */
 typedef enum {
     HMR_DIFFUSIVE_NONE = 0,
     HMR_MIDPOINT_SECOND_ORDER = 2,

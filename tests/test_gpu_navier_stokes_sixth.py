@@ -6,8 +6,8 @@ Exact form bitwise (diffusive face fluxes, the general NavierStokes stage, SSPRK
 fused substep, the spectral radius over the 5-ghost box, reflecting and periodic ghost fills);
 fast form within 1e-12 per flux and 1e-9 over two steps.  A sixth-order context reads and writes
 5-ghost patch arrays everywhere, the batched level's included (uneven patches with their own
-fills, and a tiled domain with the device ghost exchange, against the oracle); it has no
-substep VJP.
+fills, and a tiled domain with the device ghost exchange, against the oracle), and the
+substep VJP against the oracle's tangent.
 """
 import numpy as np
 import pytest
@@ -294,14 +294,41 @@ def test_sixth_order_tiled_level_equals_one_patch(cuda, case):
 
 
 @pytest.mark.gpu
-def test_sixth_order_unsupported_forms(cuda):
-    """No substep VJP at sixth order (its reverse stencils are the second- and fourth-order ones)."""
+@pytest.mark.parametrize("stage", [0, 2])
+@pytest.mark.parametrize("case", CASES, ids=IDS)
+def test_sixth_order_vjp_dot_product(cuda, case, stage):
+    """The substep adjoint with the sixth-order diffusive flux (5-ghost arrays) against the
+    oracle's dual-number tangent, <W, J V> = <J^T W, V>, in the tolerances of the Euler
+    adjoint; and the diffusive part is in it (the fourth-order tangent differs)."""
     import torch
     from hamers_gb300 import flow
-    from hamers_gb300 import _lib as L
-    ns = make(2, "exact")
-    n = (12, 10)
-    Q = torch.from_numpy(state(smooth_state, 2, n, 3)).cuda()
-    with pytest.raises(L.HmrError):
-        ns.substepVJP(flow.Patch(n, [0.1, 0.1], Q), 0, [Q], 1e-3, torch.zeros_like(Q), [torch.zeros_like(Q)])
+    from tests.helpers import noisy_shock_state
+    from tests.test_gpu_adjoint import SSP, TOL_DOT, _directions
+    dim, n = case
+    cfg = cfg_of(dim)
+    ns = make(dim, "exact")
+    dx = [1.0 / v for v in n]
+    dt = 1.5e-3
+    alpha, beta = SSP[stage]
+    rng = np.random.default_rng(500 + stage)
+    mask = np.zeros((1,) + state(smooth_state, dim, n, 0).shape[1:], dtype=bool)
+    mask[interior(dim)] = True
+    tr4 = O.Transport(TRANSPORT["species_mu"], TRANSPORT["species_c_p"], TRANSPORT["species_Pr"],
+                      mu_v=TRANSPORT["species_mu_v"], order=4)
+    for label, gen in (("smooth", smooth_state), ("shock", noisy_shock_state)):
+        Qs = [state(gen, dim, n, 60 + k) for k in range(stage + 1)]
+        O.fill_ghosts(cfg, n, [1] * dim, Qs[stage])
+        V = [_directions(q, rng) for q in Qs]
+        W = rng.standard_normal(Qs[0].shape) * mask
+        _, JV = O.tangent_substep(cfg, n, dx, dt, stage, alpha, beta, Qs, V, transport=transport())
+        lhs = float(np.sum(W * JV))
+        scale = float(np.sum(np.abs(W * JV)))
+        tQ = [torch.from_numpy(q).cuda() for q in Qs]
+        tB = [torch.zeros_like(t) for t in tQ]
+        ns.substepVJP(flow.Patch(n, dx, tQ[stage]), stage, tQ, dt, torch.from_numpy(W).cuda(), tB)
+        torch.cuda.synchronize()
+        rhs = float(sum(np.sum(b.cpu().numpy() * v) for b, v in zip(tB, V)))
+        assert abs(lhs - rhs) <= TOL_DOT[label] * scale, f"{label}: {lhs:.16e} vs {rhs:.16e} scale {scale:.3e}"
+        _, JV4 = O.tangent_substep(cfg, n, dx, dt, stage, alpha, beta, Qs, V, transport=tr4)
+        assert abs(float(np.sum(W * JV4)) - rhs) > 10 * TOL_DOT[label] * scale
     ns.rec.close()
