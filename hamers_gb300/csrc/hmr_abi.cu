@@ -1028,17 +1028,22 @@ int hmr_level_substep_vjp(hmr_level* lv, int stage, double dt, const double* con
                           double* const* const* const* Qbar_int, void* stream) {
     if (!lv || stage < 0 || stage > 2 || !Qbar_out || !Qbar_int) return HMR_ERR_ARGUMENT;
     hmr_ctx* c = lv->ctx;
-    if (c->P.dorder != 0) return HMR_ERR_UNSUPPORTED;
     if (lv->bound != lv->npatch) return HMR_ERR_STATE;
     const int np = lv->npatch;
     const double beta = RK3_BETA[stage];
     const size_t per_face = vjp_face_doubles(c);
+    // Navier-Stokes: midpoint adjoints, node-gradient and primitive-variable adjoints
+    const int nmb = c->v.dim + (c->v.dim + 1) + 2 * (c->v.dim - 1);
     // per-patch buffer sizes (doubles, rounded to 32 for alignment)
     std::vector<size_t> need(np);
     size_t largest = 0, total = 0;
     for (int p = 0; p < np; p++) {
         size_t n = 0;
         for (int a = 0; a < c->v.dim; a++) n += per_face * nface_of(lv->geoms[p], a);
+        if (c->P.dorder) {
+            for (int a = 0; a < c->v.dim; a++) n += (size_t)nmb * nface_w(lv->geoms[p], a, diff_half_width(c->v));
+            n += (size_t)(c->v.dim * c->v.dim + c->neq) * ncell_of(lv->geoms[p]);
+        }
         need[p] = (n + 31) / 32 * 32;
         largest = std::max(largest, need[p]);
         total += need[p];
@@ -1102,6 +1107,14 @@ int hmr_level_substep_vjp(hmr_level* lv, int stage, double dt, const double* con
             A.Fp[a] = q; q += (size_t)(9 + 4 * c->v.nsp) * nf;
             A.okf[a] = reinterpret_cast<unsigned char*>(q); q += nf;
         }
+        if (c->P.dorder) {
+            for (int a = 0; a < c->v.dim; a++) {
+                A.Mb[a] = q;
+                q += (size_t)nmb * nface_w(g, a, diff_half_width(c->v));
+            }
+            A.Gdb = q; q += (size_t)c->v.dim * c->v.dim * ncell_of(g);
+            A.Dv = q; q += (size_t)c->neq * ncell_of(g);
+        }
         used += need[p];
         long items[VJP_NPH * 3];
         vjp_item_counts(c->v, g, items);
@@ -1121,6 +1134,10 @@ int hmr_level_substep_vjp(hmr_level* lv, int stage, double dt, const double* con
         // (the exact-form cell unit, as the forward computes them)
         int r = hmr_cells::launch_cells_level(c->v, c->P, lv->d_work, np, lv->L.total_cells, stage, st);
         if (r) return r;
+        if (c->P.dorder) {
+            r = hmr_cells::launch_diff_grad_level(c->v, c->P, lv->d_work, np, lv->L.total_cells, st);
+            if (r) return r;
+        }
         r = hmr_cells::launch_sensor_level(c->v, lv->d_work, np, lv->L.total_sensor, st);
         if (r) return r;
     }

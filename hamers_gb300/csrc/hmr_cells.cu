@@ -673,6 +673,33 @@ __global__ void __launch_bounds__(THREADS) diff_grad_kernel(Params P, Geom g, Sc
         diff_grad_item<DIM, ORD>(P, g, S, x);
 }
 
+// The same over the patches of a level (their PatchWork records; cells numbered as off_cells).
+template <int DIM, int ORD>
+__global__ void __launch_bounds__(THREADS) diff_grad_level_kernel(Params P, const PatchWork* W, int np, long total) {
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        int lo = 0, hi = np - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (W[mid].off_cells <= t) lo = mid;
+            else hi = mid - 1;
+        }
+        diff_grad_item<DIM, ORD>(P, W[lo].g, W[lo].S, t - W[lo].off_cells);
+    }
+}
+
+int launch_diff_grad_level(const Variant& v, const Params& P, const PatchWork* work, int npatch, long total,
+                           cudaStream_t st) {
+    if (v.model != SINGLE_SPECIES || (P.dorder != 2 && P.dorder != 4 && P.dorder != 6)) return -2;
+    const int b = grid_for(total);
+    if (v.dim == 2 && P.dorder == 2) diff_grad_level_kernel<2, 2><<<b, THREADS, 0, st>>>(P, work, npatch, total);
+    else if (v.dim == 2 && P.dorder == 4) diff_grad_level_kernel<2, 4><<<b, THREADS, 0, st>>>(P, work, npatch, total);
+    else if (v.dim == 2) diff_grad_level_kernel<2, 6><<<b, THREADS, 0, st>>>(P, work, npatch, total);
+    else if (P.dorder == 2) diff_grad_level_kernel<3, 2><<<b, THREADS, 0, st>>>(P, work, npatch, total);
+    else if (P.dorder == 4) diff_grad_level_kernel<3, 4><<<b, THREADS, 0, st>>>(P, work, npatch, total);
+    else diff_grad_level_kernel<3, 6><<<b, THREADS, 0, st>>>(P, work, npatch, total);
+    return (int)cudaPeekAtLastError();
+}
+
 int launch_diff_grad(const Variant& v, const Params& P, const Geom& g, const Scratch& S, cudaStream_t st) {
     if (v.model != SINGLE_SPECIES || (P.dorder != 2 && P.dorder != 4 && P.dorder != 6)) return -2;
     const int b = grid_for(ncell_of(g));

@@ -221,6 +221,10 @@ int launch_cells_level(const hmr::Variant& v, const hmr::Params& P, const hmr::P
                        long total_cells, int slot, cudaStream_t st);
 int launch_sensor_level(const hmr::Variant& v, const hmr::PatchWork* work, int npatch, long total_sensor,
                         cudaStream_t st);
+// Temperature and node velocity gradient of the stage of every patch of a level (NavierStokes;
+// after launch_cells_level).
+int launch_diff_grad_level(const hmr::Variant& v, const hmr::Params& P, const hmr::PatchWork* work, int npatch,
+                           long total, cudaStream_t st);
 int launch_stable_dt(const unsigned long long* d_max, double cfl, double* d_dt, cudaStream_t st, bool ns = false);
 // Euler / NavierStokes advanceSingleStepOnPatch; with Fdint (ncoef diffusive flux sets) the
 // NavierStokes form, and Fdacc (optional) accumulates them with gamma.

@@ -140,7 +140,9 @@ class ConvectiveFluxReconstructor:
     grid_geometry: the grid geometry (an object with getDx(), or the spacing itself) of
     the coarsest level, as the reference passes CartesianGridGeometry to the reconstructor;
     WCNS6-CU-M2 scales its weights by that spacing and needs it, the others ignore it.
-    precision: 'fast' (default, <= 1e-12 relative) or 'exact' (bitwise to the reference order).
+    precision: 'fast' (default, <= 1e-12 relative; <= 2e-15 c/|u_n| for the flux components
+    proportional to a normal velocity below 1e-3 of the sound speed) or 'exact' (bitwise to the
+    reference order).
     """
 
     def __init__(self, name, flow_model, db=None, precision="fast", grid_geometry=None,

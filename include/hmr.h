@@ -87,7 +87,9 @@ typedef enum {
 } hmr_diffusive;
 
 typedef enum {
-    HMR_PRECISION_FAST = 0,   /* regrouped FP64 with FMA; <= 1e-12 relative to the reference */
+    HMR_PRECISION_FAST = 0,   /* regrouped FP64 with FMA; <= 1e-12 relative to the reference per flux
+                                 component (<= 2e-15 c/|u_n| for the components proportional to a
+                                 normal velocity u_n below 1e-3 of the sound speed c) */
     HMR_PRECISION_EXACT = 1   /* the reference's operation order, no FMA: bitwise equal to it */
 } hmr_precision;
 
@@ -330,8 +332,8 @@ int hmr_level_step(hmr_level* level, double dt, void* stream);
  * those of hmr_rk_substep_vjp_patch on each patch.  The patches run together, one launch per
  * phase over the flat item space of a group of patches whose per-face reverse buffers (about
  * 1.2 KB per face) fit a quarter of the device memory free at the first call; the buffers
- * stay with the level.  The Euler equations only (HMR_ERR_UNSUPPORTED for a NavierStokes
- * context); HMR_ERR_STATE until every patch's slot 0 is bound. */
+ * stay with the level.  With a diffusive_flux_reconstructor the diffusive flux's reverse is
+ * included, as in the per-patch form.  HMR_ERR_STATE until every patch's slot 0 is bound. */
 int hmr_level_substep_vjp(hmr_level* level, int stage, double dt, const double* const* const* Qbar_out,
                           double* const* const* const* Qbar_int, void* stream);
 /* Memory budget of hmr_level_substep_vjp's per-face reverse buffers, in bytes (0: a quarter of

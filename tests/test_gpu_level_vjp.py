@@ -14,19 +14,33 @@ from tests.test_gpu_parity import IDS, VARIANTS, make
 
 CASES = [VARIANTS[i] for i in (1, 2, 5, 7, 9)]
 CASE_IDS = [IDS[i] for i in (1, 2, 5, 7, 9)]
+NS_TRANSPORT = dict(species_mu=0.02, species_mu_v=0.005, species_c_p=3.5, species_Pr=0.72)
 
 
-def _run(variant, budget=None):
+def _run(variant, budget=None, diffusive=None):
+    """Batched and per-patch VJPs of the three substeps; diffusive: None (Euler) or the
+    NavierStokes midpoint order (single species)."""
     import torch
     from hamers_gb300 import flow
     model, dim, scheme, _, gam = variant
-    rec = make(model, dim, scheme, gam, "fast")
+    if diffusive is None:
+        rec = make(model, dim, scheme, gam, "fast")
+        eu = flow.Euler(rec)
+    else:
+        fm = flow.FlowModel("SINGLE_SPECIES", dim, gam, transport=NS_TRANSPORT)
+        rec = flow.ConvectiveFluxReconstructor(
+            "WCNS5_JS_HLLC_HLL", fm, precision="fast",
+            diffusive_flux_reconstructor={2: "MIDPOINT_SECOND_ORDER", 4: "MIDPOINT_FOURTH_ORDER",
+                                          6: "MIDPOINT_SIXTH_ORDER"}[diffusive])
+        eu = flow.NavierStokes(rec)
+    grow = rec.getPatchNumberOfGhostCells() - 4
     sizes, periodic = _patches(dim, 11)
     dt = 1.0e-3
     geoms, states = [], []
     for p, n in enumerate(sizes):
         gen = noisy_shock_state if p % 2 else smooth_state
-        states.append(torch.from_numpy(gen(model, dim, n, seed=60 + p, species_gamma=gam)).cuda())
+        Q = gen(model, dim, [v + 2 * grow for v in n], seed=60 + p, species_gamma=gam)
+        states.append(torch.from_numpy(Q).cuda())
         geoms.append((list(n), [1.0 / v for v in n]))
     lv = flow.BatchedLevel(rec, geoms)
     if budget is not None:
@@ -34,7 +48,6 @@ def _run(variant, budget=None):
     for p, Q in enumerate(states):
         lv.bind(p, Q)
         lv.set_periodic(p, periodic[p])
-    eu = flow.Euler(rec)
     gen = torch.Generator(device="cuda")
     gen.manual_seed(5)
     out = []
@@ -79,3 +92,16 @@ def test_batched_vjp_in_groups_of_patches(cuda):
         for b, q in zip(batched, per_patch):
             for s in range(stage + 1):
                 assert np.array_equal(b[s].cpu().numpy(), q[s].cpu().numpy())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("order", [2, 4, 6])
+@pytest.mark.parametrize("variant", [VARIANTS[0], VARIANTS[2]], ids=[IDS[0], IDS[2]])
+def test_batched_navier_stokes_vjp_equals_per_patch_vjp(cuda, variant, order):
+    """NavierStokes contexts (single species, midpoint diffusive flux of each order; 5-ghost
+    arrays at sixth order): the batched VJP is bitwise the per-patch one."""
+    for stage, (batched, per_patch) in enumerate(_run(variant, diffusive=order)):
+        for p, (b, q) in enumerate(zip(batched, per_patch)):
+            for s in range(stage + 1):
+                x, y = b[s].cpu().numpy(), q[s].cpu().numpy()
+                assert np.array_equal(x, y), f"stage {stage} patch {p} slot {s}: max diff {np.abs(x - y).max()}"
