@@ -130,6 +130,19 @@ def _comp_ptrs(t, ncomp):
     return [t[e].data_ptr() for e in range(ncomp)]
 
 
+def _state_ptrs(rec, n, t):
+    """Component pointers of a conserved-variable array over the ghost box of a patch of n
+    interior cells; the library reads and writes the whole box, so its extent is checked
+    against the context's ghost width (4, or 5 with the sixth-order diffusive flux)."""
+    dim = rec.flow_model.dim
+    gh = rec.ghosts
+    want = tuple(int(n[a]) + 2 * gh if a < dim else 1 for a in (2, 1, 0))
+    if tuple(t.shape[1:]) != want:
+        raise ValueError(f"patch array of shape {tuple(t.shape)}: expected (ncomp,) + {want} "
+                         f"(interior {list(n)[:dim]} with {gh} ghost cells per side)")
+    return _comp_ptrs(t, rec.ncomp)
+
+
 class ConvectiveFluxReconstructor:
     """WCNS5-JS / WCNS6-LD / WCNS5-Z / WCNS6-CU-M2 + HLLC-HLL reconstructor behind the C ABI.
 
@@ -187,6 +200,7 @@ class ConvectiveFluxReconstructor:
         self.ctx = ctx
         self.neq = lib.hmr_num_equations(ctx)
         self.ncomp = lib.hmr_num_components(ctx)
+        self.ghosts = lib.hmr_num_patch_ghosts(ctx)
 
     def close(self):
         if self.ctx:
@@ -227,7 +241,7 @@ class ConvectiveFluxReconstructor:
     def computeConvectiveFluxAndSourceOnPatch(self, patch, convective_flux, source, dt, stream=None):
         """dt-scaled face fluxes (overwritten) and advective source (+=)."""
         g = patch.geometry()
-        q, _k1 = L.ptr_array(_comp_ptrs(patch.data, self.ncomp))
+        q, _k1 = L.ptr_array(_state_ptrs(self, patch.n, patch.data))
         fptrs = []
         for a in range(self.flow_model.dim):
             fptrs += _comp_ptrs(convective_flux[a], self.neq)
@@ -262,10 +276,10 @@ class Euler:
         a = (ctypes.c_double * nc)(*alpha)
         b = (ctypes.c_double * nc)(*beta)
         c = (ctypes.c_double * nc)(*gamma)
-        qi, k1 = L.ptr_array2([_comp_ptrs(t, rec.ncomp) for t in Q_int])
+        qi, k1 = L.ptr_array2([_state_ptrs(rec, patch.n, t) for t in Q_int])
         fi, k2 = L.ptr_array2([sum((_comp_ptrs(f, rec.neq) for f in F), []) for F in F_int])
         si, k3 = L.ptr_array2([_comp_ptrs(t, rec.neq) for t in S_int])
-        qo, k4 = L.ptr_array(_comp_ptrs(patch.data, rec.ncomp))
+        qo, k4 = L.ptr_array(_state_ptrs(rec, patch.n, patch.data))
         fa = sa = None
         keep = []
         if flux_acc is not None:
@@ -280,7 +294,7 @@ class Euler:
         patch.data with the time-integrated (gamma-accumulated, reflux-corrected) fluxes."""
         rec = self.rec
         g = patch.geometry()
-        q, k1 = L.ptr_array(_comp_ptrs(patch.data, rec.ncomp))
+        q, k1 = L.ptr_array(_state_ptrs(rec, patch.n, patch.data))
         f, k2 = L.ptr_array(sum((_comp_ptrs(t, rec.neq) for t in flux[:rec.flow_model.dim]), []))
         d = None
         if diffusive_flux is not None:
@@ -294,7 +308,7 @@ class Euler:
         boundary), FILL_PERIODIC (1), FILL_PROVIDED (2, left as supplied) or FILL_REFLECT (3, a
         slip wall: mirror image with the normal momentum negated; needs >= 4 cells on the axis)."""
         g = patch.geometry()
-        q, _k = L.ptr_array(_comp_ptrs(patch.data, self.rec.ncomp))
+        q, _k = L.ptr_array(_state_ptrs(self.rec, patch.n, patch.data))
         per = (ctypes.c_int * 3)(*(list(periodic) + [0] * (3 - len(periodic))))
         L.check("hmr_fill_ghosts_patch", self._lib.hmr_fill_ghosts_patch(
             self.rec.ctx, ctypes.byref(g), q, per, _stream_ptr(stream)))
@@ -304,8 +318,8 @@ class Euler:
         rec = self.rec
         g = patch.geometry()
         alpha = (ctypes.c_double * 3)(*(RK3_ALPHA[stage] + [0.0] * (2 - stage)))
-        qi, k1 = L.ptr_array2([_comp_ptrs(t, rec.ncomp) for t in Q_int[:stage + 1]])
-        qo, k2 = L.ptr_array(_comp_ptrs(out, rec.ncomp))
+        qi, k1 = L.ptr_array2([_state_ptrs(rec, patch.n, t) for t in Q_int[:stage + 1]])
+        qo, k2 = L.ptr_array(_state_ptrs(rec, patch.n, out))
         L.check("hmr_rk_substep_patch", self._lib.hmr_rk_substep_patch(
             rec.ctx, ctypes.byref(g), int(stage), alpha, RK3_BETA[stage][stage], qi, float(dt), qo,
             _stream_ptr(stream)))
@@ -317,9 +331,9 @@ class Euler:
         rec = self.rec
         g = patch.geometry()
         alpha = (ctypes.c_double * 3)(*(RK3_ALPHA[stage] + [0.0] * (2 - stage)))
-        qi, k1 = L.ptr_array2([_comp_ptrs(t, rec.ncomp) for t in Q_int[:stage + 1]])
-        qb, k2 = L.ptr_array(_comp_ptrs(Qbar_out, rec.ncomp))
-        qbi, k3 = L.ptr_array2([_comp_ptrs(t, rec.ncomp) for t in Qbar_int[:stage + 1]])
+        qi, k1 = L.ptr_array2([_state_ptrs(rec, patch.n, t) for t in Q_int[:stage + 1]])
+        qb, k2 = L.ptr_array(_state_ptrs(rec, patch.n, Qbar_out))
+        qbi, k3 = L.ptr_array2([_state_ptrs(rec, patch.n, t) for t in Qbar_int[:stage + 1]])
         L.check("hmr_rk_substep_vjp_patch", self._lib.hmr_rk_substep_vjp_patch(
             rec.ctx, ctypes.byref(g), int(stage), alpha, RK3_BETA[stage][stage], qi, float(dt), qb, qbi,
             _stream_ptr(stream)))
@@ -328,7 +342,7 @@ class Euler:
         """Max over the interior of sum_d (|u_d| + c)/dx_d (Euler::computeSpectralRadiusesAndStableDtOnPatch);
         max-reduced into the device scalar `out` if given (running max), else returned (synchronises)."""
         g = patch.geometry()
-        q, _k = L.ptr_array(_comp_ptrs(patch.data, self.rec.ncomp))
+        q, _k = L.ptr_array(_state_ptrs(self.rec, patch.n, patch.data))
         dst = out if out is not None else torch.zeros(1, dtype=torch.float64, device=patch.data.device)
         L.check("hmr_spectral_radius_patch", self._lib.hmr_spectral_radius_patch(
             self.rec.ctx, ctypes.byref(g), q, ctypes.cast(ctypes.c_void_p(dst.data_ptr()), ctypes.POINTER(ctypes.c_double)),
@@ -338,7 +352,7 @@ class Euler:
     def fillGhostsVJP(self, patch, periodic, stream=None):
         """Adjoint of fillGhosts() applied to the adjoint array patch.data."""
         g = patch.geometry()
-        q, _k = L.ptr_array(_comp_ptrs(patch.data, self.rec.ncomp))
+        q, _k = L.ptr_array(_state_ptrs(self.rec, patch.n, patch.data))
         per = (ctypes.c_int * 3)(*(list(periodic) + [0] * (3 - len(periodic))))
         L.check("hmr_fill_ghosts_vjp_patch", self._lib.hmr_fill_ghosts_vjp_patch(
             self.rec.ctx, ctypes.byref(g), q, per, _stream_ptr(stream)))
@@ -367,7 +381,7 @@ class DiffusiveFluxReconstructor:
         """dt-scaled diffusive face fluxes (overwritten), same layout as the convective flux."""
         rec = self.conv
         g = patch.geometry()
-        q, _k1 = L.ptr_array(_comp_ptrs(patch.data, rec.ncomp))
+        q, _k1 = L.ptr_array(_state_ptrs(rec, patch.n, patch.data))
         f, _k2 = L.ptr_array(sum((_comp_ptrs(t, rec.neq) for t in diffusive_flux[:rec.flow_model.dim]), []))
         L.check("hmr_diff_flux_patch", self._lib.hmr_diff_flux_patch(
             rec.ctx, ctypes.byref(g), q, float(dt), f, _stream_ptr(stream)))
@@ -398,11 +412,11 @@ class NavierStokes(Euler):
         a = (ctypes.c_double * nc)(*alpha)
         b = (ctypes.c_double * nc)(*beta)
         c = (ctypes.c_double * nc)(*gamma)
-        qi, k1 = L.ptr_array2([_comp_ptrs(t, rec.ncomp) for t in Q_int])
+        qi, k1 = L.ptr_array2([_state_ptrs(rec, patch.n, t) for t in Q_int])
         fi, k2 = L.ptr_array2([sum((_comp_ptrs(f, rec.neq) for f in F), []) for F in F_int])
         di, k3 = L.ptr_array2([sum((_comp_ptrs(f, rec.neq) for f in F), []) for F in Fd_int])
         si, k4 = L.ptr_array2([_comp_ptrs(t, rec.neq) for t in S_int])
-        qo, k5 = L.ptr_array(_comp_ptrs(patch.data, rec.ncomp))
+        qo, k5 = L.ptr_array(_state_ptrs(rec, patch.n, patch.data))
         fa = da = sa = None
         keep = []
         if flux_acc is not None:
@@ -437,9 +451,9 @@ def refineGhosts(reconstructor, fine, fine_lo, coarse, coarse_lo, ratio, coarse_
     time (coarse_old / coarse_new: ghost-box tensors, ghosts filled) at time fraction theta."""
     rec = reconstructor
     gf, gc = fine.geometry(), coarse.geometry()
-    qo, k1 = L.ptr_array(_comp_ptrs(coarse_old, rec.ncomp))
-    qn, k2 = L.ptr_array(_comp_ptrs(coarse_new, rec.ncomp))
-    qf, k3 = L.ptr_array(_comp_ptrs(fine.data, rec.ncomp))
+    qo, k1 = L.ptr_array(_state_ptrs(rec, coarse.n, coarse_old))
+    qn, k2 = L.ptr_array(_state_ptrs(rec, coarse.n, coarse_new))
+    qf, k3 = L.ptr_array(_state_ptrs(rec, fine.n, fine.data))
     L.check("hmr_refine_ghosts_patch", rec._lib.hmr_refine_ghosts_patch(
         rec.ctx, ctypes.byref(gf), _ivec(fine_lo), ctypes.byref(gc), _ivec(coarse_lo), _ivec(ratio, 1),
         qo, qn, float(theta), qf, _stream_ptr(stream)))
@@ -449,8 +463,8 @@ def coarsenPatch(reconstructor, coarse, coarse_lo, fine, fine_lo, ratio, stream=
     """Coarsening of a fine patch's interior onto the coarse cells it covers (mean of the fine cells)."""
     rec = reconstructor
     gc, gf = coarse.geometry(), fine.geometry()
-    qf, k1 = L.ptr_array(_comp_ptrs(fine.data, rec.ncomp))
-    qc, k2 = L.ptr_array(_comp_ptrs(coarse.data, rec.ncomp))
+    qf, k1 = L.ptr_array(_state_ptrs(rec, fine.n, fine.data))
+    qc, k2 = L.ptr_array(_state_ptrs(rec, coarse.n, coarse.data))
     L.check("hmr_coarsen_patch", rec._lib.hmr_coarsen_patch(
         rec.ctx, ctypes.byref(gc), _ivec(coarse_lo), ctypes.byref(gf), _ivec(fine_lo), _ivec(ratio, 1),
         qf, qc, _stream_ptr(stream)))

@@ -332,3 +332,22 @@ def test_sixth_order_vjp_dot_product(cuda, case, stage):
         _, JV4 = O.tangent_substep(cfg, n, dx, dt, stage, alpha, beta, Qs, V, transport=tr4)
         assert abs(float(np.sum(W * JV4)) - rhs) > 10 * TOL_DOT[label] * scale
     ns.rec.close()
+
+
+@pytest.mark.gpu
+def test_patch_arrays_must_match_the_ghost_width(cuda):
+    """The library reads and writes the whole ghost box, so the Python layer refuses an array
+    whose extent is not the context's ghost box (4-ghost arrays on a sixth-order context)."""
+    import torch
+    from hamers_gb300 import flow
+    ns = make(2, "exact")
+    n = (12, 10)
+    Q4 = torch.from_numpy(smooth_state(O.MODEL_SINGLE_SPECIES, 2, n, seed=3, species_gamma=[1.4])).cuda()
+    patch = flow.Patch(n, [0.1, 0.1], Q4)
+    with pytest.raises(ValueError):
+        ns.diff.computeDiffusiveFluxOnPatch(patch, ns.rec.allocateFlux(patch), 1e-3)
+    with pytest.raises(ValueError):
+        ns.fillGhosts(patch, [1, 1])
+    Q5 = torch.from_numpy(state(smooth_state, 2, n, 3)).cuda()
+    ns.fillGhosts(flow.Patch(n, [0.1, 0.1], Q5), [1, 1])
+    ns.rec.close()
