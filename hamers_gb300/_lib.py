@@ -46,7 +46,7 @@ EXPORTS = [
     "hmr_rk_substep_patch_noalloc", "hmr_rk_substep_vjp_patch", "hmr_fill_ghosts_vjp_patch",
     "hmr_spectral_radius_patch", "hmr_level_step_cfl", "hmr_level_last_dt", "hmr_level_set_layout",
     "hmr_diff_flux_patch", "hmr_rk_stage_ns_patch", "hmr_coarsen_fluxsum_patch", "hmr_sync_fluxes_patch",
-    "hmr_coarsen_patch", "hmr_refine_ghosts_patch", "hmr_level_substep_vjp",
+    "hmr_coarsen_patch", "hmr_refine_ghosts_patch", "hmr_level_substep_vjp", "hmr_level_fill_vjp",
     "hmr_level_set_vjp_budget", "hmr_level_set_work_split", "hmr_level_work_split",
 ]
 
@@ -145,6 +145,7 @@ def load():
                                            DPP, DPPP, vp]
     L.hmr_fill_ghosts_vjp_patch.argtypes = [vp, gp, DPP, ip, vp]
     L.hmr_level_substep_vjp.argtypes = [vp, ctypes.c_int, ctypes.c_double, DPPP, ctypes.POINTER(DPPP), vp]
+    L.hmr_level_fill_vjp.argtypes = [vp, DPPP, vp]
     L.hmr_level_set_vjp_budget.argtypes = [vp, ctypes.c_ulonglong]
     L.hmr_level_set_work_split.argtypes = [vp, ctypes.c_int, ctypes.c_int]
     L.hmr_level_work_split.argtypes = [vp, ip, ip]

@@ -68,6 +68,7 @@ struct hmr_level {
     size_t vjp_bytes = 0;
     size_t vjp_budget = 0;             // 0: a quarter of the free device memory at the first call
     VjpWork* d_vjpwork = nullptr;
+    hmr_cells::LevelFillVjpPatch* d_fillvjp = nullptr;   // records of the ghost fill's adjoint
 };
 
 static int cuda_status(cudaError_t e) { return e == cudaSuccess ? HMR_OK : (int)e; }
@@ -888,6 +889,7 @@ int hmr_level_destroy(hmr_level* lv) {
     if (lv->d_dt) cudaFree(lv->d_dt);
     if (lv->d_vjp) cudaFree(lv->d_vjp);
     if (lv->d_vjpwork) cudaFree(lv->d_vjpwork);
+    if (lv->d_fillvjp) cudaFree(lv->d_fillvjp);
     delete lv;
     return HMR_OK;
 }
@@ -1022,6 +1024,43 @@ int hmr_level_set_vjp_budget(hmr_level* lv, unsigned long long bytes) {
     if (!lv) return HMR_ERR_ARGUMENT;
     lv->vjp_budget = (size_t)bytes;
     return HMR_OK;
+}
+
+int hmr_level_fill_vjp(hmr_level* lv, double* const* const* Qbar, void* stream) {
+    if (!lv || !Qbar) return HMR_ERR_ARGUMENT;
+    hmr_ctx* c = lv->ctx;
+    const int np = lv->npatch;
+    const int mom0 = momentum0(c->v);
+    cudaStream_t st = as_stream(stream);
+    std::vector<Comp> qb(np);
+    for (int p = 0; p < np; p++)
+        if (!Qbar[p] || !load_comp(qb[p], Qbar[p], c->ncomp)) return HMR_ERR_ARGUMENT;
+    if (!lv->exchange) {
+        // each patch's own fill (hmr_level_set_periodic modes)
+        for (int p = 0; p < np; p++) {
+            int r = hmr_cells::launch_fill_vjp(c->v.dim, lv->geoms[p], qb[p], c->ncomp, lv->work[p].periodic, mom0, st);
+            if (r) return r;
+        }
+        return HMR_OK;
+    }
+    std::vector<hmr_cells::LevelFillVjpPatch> rec(np);
+    long total = 0;
+    for (int p = 0; p < np; p++) {
+        rec[p].g = lv->geoms[p];
+        rec[p].Qb = qb[p];
+        for (int a = 0; a < 3; a++) rec[p].lo[a] = lv->work[p].lo[a];
+        rec[p].off = total;
+        total += ncell_of(lv->geoms[p]);
+    }
+    if (!lv->d_fillvjp) {
+        cudaError_t e = cudaMalloc(&lv->d_fillvjp, (size_t)np * sizeof(hmr_cells::LevelFillVjpPatch));
+        if (e != cudaSuccess) return cuda_status(e);
+    }
+    cudaError_t e = cudaMemcpyAsync(lv->d_fillvjp, rec.data(), (size_t)np * sizeof(hmr_cells::LevelFillVjpPatch),
+                                    cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_status(e);
+    return hmr_cells::launch_level_fill_vjp(c->v.dim, lv->d_fillvjp, np, total, lv->d_copies, lv->ncopy,
+                                            lv->total_copy, c->ncomp, lv->dom, lv->dom_periodic, mom0, st);
 }
 
 int hmr_level_substep_vjp(hmr_level* lv, int stage, double dt, const double* const* const* Qbar_out,

@@ -742,4 +742,101 @@ int launch_rk_stage(const Variant& v, const Geom& g, int ncoef, const double* al
     });
 }
 
+// ---------------------------------------------------------------------------
+// Adjoint of a level's ghost fill with a layout (see launch_level_fill_vjp).
+// ---------------------------------------------------------------------------
+struct DomainArgs {
+    int dom[3], per[3];
+};
+
+template <int DIM>
+__global__ void __launch_bounds__(THREADS) level_domain_vjp_kernel(const LevelFillVjpPatch* W, int np, long total,
+                                                                   int ncomp, DomainArgs D, int mom0) {
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        int lo = 0, hi = np - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (W[mid].off <= t) lo = mid;
+            else hi = mid - 1;
+        }
+        const LevelFillVjpPatch& w = W[lo];
+        const Geom& g = w.g;
+        const long x = t - w.off;
+        int c[3], s[3];
+        c[0] = (int)(x % g.G[0]) - g.gh;
+        c[1] = (int)((x / g.G[0]) % g.G[1]) - g.gh;
+        c[2] = DIM == 3 ? (int)(x / ((long)g.G[0] * g.G[1])) - g.gh : 0;
+        bool physical = false;
+        int flip[3] = {-1, -1, -1};
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            s[a] = c[a];
+            if (a >= DIM || D.per[a] == 1) continue;
+            const int G = w.lo[a] + c[a];
+            if (G >= 0 && G < D.dom[a]) continue;
+            physical = true;
+            if (D.per[a] == 3) {
+                s[a] = (G < 0 ? -G - 1 : 2 * D.dom[a] - 1 - G) - w.lo[a];
+                flip[a] = mom0 + a;
+            } else {
+                s[a] = G < 0 ? -w.lo[a] : D.dom[a] - 1 - w.lo[a];
+            }
+        }
+        if (!physical) continue;
+        const long y = cidx<DIM>(g, s[0], s[1], s[2]);
+        for (int e = 0; e < ncomp; e++) {
+            const double v = w.Qb.p[e][x];
+            if (v != 0.0) atomicAdd(&w.Qb.p[e][y], (e == flip[0] || e == flip[1] || e == flip[2]) ? -v : v);
+            w.Qb.p[e][x] = 0.0;
+        }
+    }
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(THREADS) level_exchange_vjp_kernel(const LevelFillVjpPatch* W,
+                                                                     const GhostCopy* copies, int ncopy, long total,
+                                                                     int ncomp) {
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        int lo = 0, hi = ncopy - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (copies[mid].off <= t) lo = mid;
+            else hi = mid - 1;
+        }
+        const GhostCopy& cp = copies[lo];
+        const long u = t - cp.off;
+        const int a0 = (int)(u % cp.ext[0]);
+        const int a1 = (int)((u / cp.ext[0]) % cp.ext[1]);
+        const int a2 = (int)(u / ((long)cp.ext[0] * cp.ext[1]));
+        const LevelFillVjpPatch& wd = W[cp.dst];
+        const LevelFillVjpPatch& ws = W[cp.src];
+        const long xd = cidx<DIM>(wd.g, cp.dlo[0] + a0, cp.dlo[1] + a1, cp.dlo[2] + a2);
+        const long xs = cidx<DIM>(ws.g, cp.slo[0] + a0, cp.slo[1] + a1, cp.slo[2] + a2);
+        for (int e = 0; e < ncomp; e++) {
+            const double v = wd.Qb.p[e][xd];
+            wd.Qb.p[e][xd] = 0.0;
+            if (v != 0.0) atomicAdd(&ws.Qb.p[e][xs], v);
+        }
+    }
+}
+
+int launch_level_fill_vjp(int dim, const LevelFillVjpPatch* d_patches, int npatch, long total_cells,
+                          const GhostCopy* d_copies, int ncopy, long total_copy, int ncomp, const int* dom,
+                          const int* dom_periodic, int mom0, cudaStream_t st) {
+    DomainArgs D;
+    for (int a = 0; a < 3; a++) {
+        D.dom[a] = dom[a];
+        D.per[a] = dom_periodic[a];
+    }
+    if (dim == 2) level_domain_vjp_kernel<2><<<grid_for(total_cells), THREADS, 0, st>>>(d_patches, npatch, total_cells, ncomp, D, mom0);
+    else level_domain_vjp_kernel<3><<<grid_for(total_cells), THREADS, 0, st>>>(d_patches, npatch, total_cells, ncomp, D, mom0);
+    if (ncopy > 0 && total_copy > 0) {
+        if (dim == 2)
+            level_exchange_vjp_kernel<2><<<grid_for(total_copy), THREADS, 0, st>>>(d_patches, d_copies, ncopy, total_copy, ncomp);
+        else
+            level_exchange_vjp_kernel<3><<<grid_for(total_copy), THREADS, 0, st>>>(d_patches, d_copies, ncopy, total_copy, ncomp);
+    }
+    return (int)cudaPeekAtLastError();
+}
+
 }  // namespace hmr_cells

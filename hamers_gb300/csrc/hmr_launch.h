@@ -207,6 +207,20 @@ int launch_fill(int dim, const hmr::Geom& g, const hmr::Comp& Q, int ncomp, cons
                 cudaStream_t st);
 int launch_fill_vjp(int dim, const hmr::Geom& g, const hmr::Comp& Qb, int ncomp, const int* periodic, int mom0,
                     cudaStream_t st);
+// Adjoint of the level's ghost fill with a layout (the exchange between patches, then the domain's
+// physical faces): the physical ghost cells first add their adjoints to the in-domain cells they
+// were copied from (negated normal momentum at reflecting walls), then the exchanged ghost cells
+// to the patch interiors they were copied from; both are zeroed.  Ghost cells no copy wrote keep
+// theirs.  Sums of several ghost cells into one source cell are atomic.
+struct LevelFillVjpPatch {
+    hmr::Geom g;
+    hmr::Comp Qb;   // adjoint arrays of the patch (ghost box)
+    int lo[3];      // first interior cell in the level's index space
+    long off;       // prefix offset of its ghost-box cells
+};
+int launch_level_fill_vjp(int dim, const LevelFillVjpPatch* d_patches, int npatch, long total_cells,
+                          const hmr::GhostCopy* d_copies, int ncopy, long total_copy, int ncomp, const int* dom,
+                          const int* dom_periodic, int mom0, cudaStream_t st);
 // Stable time step (Euler::computeSpectralRadiusesAndStableDtOnPatch): running max over the
 // ghost-box cells of sum_d (|u_d| + c)/dx_d (NavierStokes: and of the diffusive radius) into
 // *d_max (bits of a non-negative double), per patch or over a level's worklist (slot-0 states),

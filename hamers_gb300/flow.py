@@ -574,6 +574,8 @@ class BatchedLevel:
         L.check("hmr_level_create", self._lib.hmr_level_create(reconstructor.ctx, n, arr, ctypes.byref(lv)))
         self.level = lv
         self.npatch = n
+        self._bound = {}
+        self._record = None
 
     def close(self):
         if self.level:
@@ -592,6 +594,16 @@ class BatchedLevel:
             raise ValueError(f"patch {patch}: expected shape {self.shapes[patch]}, got {tuple(data.shape)}")
         q, _k = L.ptr_array(_comp_ptrs(data, self.rec.ncomp))
         L.check("hmr_level_bind_state", self._lib.hmr_level_bind_state(self.level, int(patch), q))
+        self._bound[patch] = data
+
+    def _slot_views(self, patch, slot):
+        """Writable tensor views, one per component, of a patch's stage-`slot` state."""
+        return [torch.as_tensor(_DeviceArray(ptr, self.shapes[patch][1:]), device="cuda")
+                for ptr in self.state_pointers(patch, slot)]
+
+    def _load_slot(self, patch, slot, data):
+        for e, v in enumerate(self._slot_views(patch, slot)):
+            v.copy_(data[e])
 
     def state_pointers(self, patch, slot=0):
         arr = (ctypes.POINTER(ctypes.c_double) * self.rec.ncomp)()
@@ -620,6 +632,66 @@ class BatchedLevel:
         qbi, k2 = L.ptr_array3([[_comp_ptrs(t, nc) for t in slots[:stage + 1]] for slots in Qbar_int])
         L.check("hmr_level_substep_vjp", self._lib.hmr_level_substep_vjp(
             self.level, int(stage), float(dt), qb, qbi, _stream_ptr(stream)))
+
+    def fillGhostsVJP(self, Qbar, stream=None):
+        """Adjoint of the level's ghost fill (the exchange with the layout's physical faces, or
+        each patch's own fill) applied to the adjoint tensors Qbar[p] (ghost boxes)."""
+        nc = self.rec.ncomp
+        qb, k1 = L.ptr_array2([_comp_ptrs(t, nc) for t in Qbar])
+        L.check("hmr_level_fill_vjp", self._lib.hmr_level_fill_vjp(self.level, qb, _stream_ptr(stream)))
+
+    def advance(self, dt, nsteps=1, stream=None, checkpoint_every=0):
+        """nsteps level steps; with checkpoint_every=K the bound states are recorded every K
+        steps for adjoint()."""
+        if checkpoint_every:
+            self._record = {"dt": dt, "nsteps": nsteps,
+                            "ckpt": {0: [self._bound[p].clone() for p in range(self.npatch)]}}
+        for step in range(nsteps):
+            self.step(dt, stream)
+            if checkpoint_every and (step + 1) % checkpoint_every == 0 and step + 1 < nsteps:
+                self._record["ckpt"][step + 1] = [self._bound[p].clone() for p in range(self.npatch)]
+
+    def adjoint(self, Qbar, stream=None):
+        """Reverse sweep of the last recorded advance over the whole level: Qbar[p], the adjoint
+        of patch p's final state (ghost box, interior read); returns the adjoints of the initial
+        states (ghost boxes, the filled ghosts zero).  Each checkpoint segment is recomputed
+        keeping every step's ghost-filled stage states, which are loaded back into the level's
+        slots for the batched substep VJPs.  Overwrites the bound states."""
+        rec = self._record
+        if rec is None:
+            raise RuntimeError("adjoint() needs a preceding advance(..., checkpoint_every=K)")
+        np_, dt = self.npatch, rec["dt"]
+        Xb = [q.clone() for q in Qbar]
+        starts = sorted(rec["ckpt"])
+        ends = starts[1:] + [rec["nsteps"]]
+        for s0, s1 in reversed(list(zip(starts, ends))):
+            for p in range(np_):
+                self._bound[p].copy_(rec["ckpt"][s0][p])
+            saved = []
+            for _ in range(s0, s1):
+                self.substep(0, dt, stream)
+                X0 = [self._bound[p].clone() for p in range(np_)]
+                self.substep(1, dt, stream)
+                X1 = [torch.stack(self._slot_views(p, 1)).clone() for p in range(np_)]
+                self.substep(2, dt, stream)
+                X2 = [torch.stack(self._slot_views(p, 2)).clone() for p in range(np_)]
+                saved.append((X0, X1, X2))
+            for X0, X1, X2 in reversed(saved):
+                for p in range(np_):
+                    self._bound[p].copy_(X0[p])
+                    self._load_slot(p, 1, X1[p])
+                    self._load_slot(p, 2, X2[p])
+                Xn = [torch.zeros_like(x) for x in Xb]
+                B1 = [torch.zeros_like(x) for x in Xb]
+                B2 = [torch.zeros_like(x) for x in Xb]
+                self.substepVJP(2, dt, Xb, [[Xn[p], B1[p], B2[p]] for p in range(np_)], stream)
+                self.fillGhostsVJP(B2, stream)
+                self.substepVJP(1, dt, B2, [[Xn[p], B1[p]] for p in range(np_)], stream)
+                self.fillGhostsVJP(B1, stream)
+                self.substepVJP(0, dt, B1, [[Xn[p]] for p in range(np_)], stream)
+                self.fillGhostsVJP(Xn, stream)
+                Xb = Xn
+        return Xb
 
     def set_layout(self, lo, domain, periodic):
         """Patch positions (first interior cell per patch, level index space), the domain's cells

@@ -336,6 +336,16 @@ int hmr_level_step(hmr_level* level, double dt, void* stream);
  * included, as in the per-patch form.  HMR_ERR_STATE until every patch's slot 0 is bound. */
 int hmr_level_substep_vjp(hmr_level* level, int stage, double dt, const double* const* const* Qbar_out,
                           double* const* const* const* Qbar_int, void* stream);
+/* Adjoint of the level's ghost fill (the fill at the start of every substep): Qbar[p] (ncomp
+ * ghost-box arrays per patch) hold the adjoints of the filled state; every ghost cell the fill
+ * wrote adds its adjoint to the cell it was copied from -- for a level with a layout, first the
+ * physical faces' ghost cells (zero-gradient or mirror images, the normal momentum negated at
+ * reflecting walls) into in-domain cells, then the exchanged ghost cells into the interiors of
+ * the patches (and periodic images) they came from; without a layout, each patch's own fill as
+ * hmr_fill_ghosts_vjp_patch -- and is zeroed.  Ghost cells no copy wrote keep their adjoints.
+ * Several ghost cells summing into one cell add atomically, so the last bits of such sums may
+ * vary between runs.  No counterpart in the reference. */
+int hmr_level_fill_vjp(hmr_level* level, double* const* const* Qbar, void* stream);
 /* Memory budget of hmr_level_substep_vjp's per-face reverse buffers, in bytes (0: a quarter of
  * the device memory free at the next call).  The largest patch always gets its buffers; a
  * smaller budget splits the level into more groups of patches. */
