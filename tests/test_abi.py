@@ -58,6 +58,7 @@ def test_null_arguments_are_rejected(lib):
     assert lib.hmr_level_destroy(None) == L.HMR_ERR_ARGUMENT
     assert lib.hmr_level_set_launch(None, 128, 1) == L.HMR_ERR_ARGUMENT
     assert lib.hmr_level_autotune(None, 1e-3, None, None, None) == L.HMR_ERR_ARGUMENT
+    assert lib.hmr_level_fill_vjp(None, None, None) == L.HMR_ERR_ARGUMENT
 
 
 def test_cu_m2_defaults_and_grid_spacing(lib):
