@@ -47,7 +47,7 @@ EXPORTS = [
     "hmr_spectral_radius_patch", "hmr_level_step_cfl", "hmr_level_last_dt", "hmr_level_set_layout",
     "hmr_diff_flux_patch", "hmr_rk_stage_ns_patch", "hmr_coarsen_fluxsum_patch", "hmr_sync_fluxes_patch",
     "hmr_coarsen_patch", "hmr_refine_ghosts_patch", "hmr_level_substep_vjp", "hmr_level_fill_vjp",
-    "hmr_level_set_vjp_budget", "hmr_level_set_work_split", "hmr_level_work_split",
+    "hmr_level_set_vjp_budget", "hmr_level_set_work_split", "hmr_level_work_split", "hmr_set_dirichlet_values",
 ]
 
 
@@ -146,6 +146,7 @@ def load():
     L.hmr_fill_ghosts_vjp_patch.argtypes = [vp, gp, DPP, ip, vp]
     L.hmr_level_substep_vjp.argtypes = [vp, ctypes.c_int, ctypes.c_double, DPPP, ctypes.POINTER(DPPP), vp]
     L.hmr_level_fill_vjp.argtypes = [vp, DPPP, vp]
+    L.hmr_set_dirichlet_values.argtypes = [vp, ctypes.c_int, ctypes.c_int, dp]
     L.hmr_level_set_vjp_budget.argtypes = [vp, ctypes.c_ulonglong]
     L.hmr_level_set_work_split.argtypes = [vp, ctypes.c_int, ctypes.c_int]
     L.hmr_level_work_split.argtypes = [vp, ip, ip]

@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <array>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -25,6 +26,8 @@ struct hmr_ctx {
     unsigned int* redo_count = nullptr;
     double* vjp = nullptr;             // face contributions of the substep adjoint
     size_t vjp_bytes = 0;
+    double* d_bvals = nullptr;         // Dirichlet values per side (2 axis + high) x ncomp, on the device
+    double h_bvals[6 * MAX_COMP] = {};  // and their host copy
 };
 
 constexpr int LEVEL_COUNTERS = 9;   // barrier arrivals, redo-queue length, seven phase-chunk counters
@@ -103,7 +106,7 @@ static int momentum0(const Variant& v) { return v.model == SINGLE_SPECIES ? 1 : 
 static bool valid_fill_modes(int dim, const hmr_patch_geometry* pg, const int* mode, int gh) {
     if (!mode) return false;
     for (int a = 0; a < dim; a++) {
-        if (mode[a] < HMR_FILL_ZERO_GRADIENT || mode[a] > HMR_FILL_REFLECT) return false;
+        if (mode[a] < HMR_FILL_ZERO_GRADIENT || mode[a] > HMR_FILL_DIRICHLET) return false;
         if (mode[a] == HMR_FILL_REFLECT && pg->n[a] < gh) return false;
     }
     return true;
@@ -295,8 +298,10 @@ int hmr_ctx_create(const hmr_config* cfg, hmr_ctx** out) {
     cudaError_t e = cudaMalloc(&c->counters, sizeof(Counters));
     if (e == cudaSuccess) e = cudaMemset(c->counters, 0, sizeof(Counters));
     if (e == cudaSuccess) e = cudaMalloc(&c->redo_count, sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_bvals, sizeof(c->h_bvals));
+    if (e == cudaSuccess) e = cudaMemset(c->d_bvals, 0, sizeof(c->h_bvals));
     if (e != cudaSuccess) {
-        delete c;
+        hmr_ctx_destroy(c);
         return cuda_status(e);
     }
     *out = c;
@@ -309,8 +314,17 @@ int hmr_ctx_destroy(hmr_ctx* c) {
     if (c->counters) cudaFree(c->counters);
     if (c->redo_count) cudaFree(c->redo_count);
     if (c->vjp) cudaFree(c->vjp);
+    if (c->d_bvals) cudaFree(c->d_bvals);
     delete c;
     return HMR_OK;
+}
+
+int hmr_set_dirichlet_values(hmr_ctx* c, int axis, int side, const double* values) {
+    if (!c || axis < 0 || axis >= c->v.dim || (side != 0 && side != 1) || !values) return HMR_ERR_ARGUMENT;
+    for (int e = 0; e < c->ncomp; e++)
+        if (!std::isfinite(values[e])) return HMR_ERR_ARGUMENT;
+    std::memcpy(c->h_bvals + (2 * axis + side) * c->ncomp, values, sizeof(double) * (size_t)c->ncomp);
+    return cuda_status(cudaMemcpy(c->d_bvals, c->h_bvals, sizeof(c->h_bvals), cudaMemcpyHostToDevice));
 }
 
 int hmr_num_equations(const hmr_ctx* c) { return c ? c->neq : HMR_ERR_ARGUMENT; }
@@ -668,7 +682,8 @@ int hmr_fill_ghosts_patch(hmr_ctx* c, const hmr_patch_geometry* pg, double* cons
     Comp q;
     if (!load_comp(q, Q, c->ncomp)) return HMR_ERR_ARGUMENT;
     const Geom g = make_geom(c->v.dim, pg, patch_ghosts(c->v));
-    return hmr_cells::launch_fill(c->v.dim, g, q, c->ncomp, periodic, momentum0(c->v), as_stream(stream));
+    return hmr_cells::launch_fill(c->v.dim, g, q, c->ncomp, periodic, momentum0(c->v), c->d_bvals,
+                                  as_stream(stream));
 }
 
 }  // extern "C"
@@ -865,6 +880,7 @@ int hmr_level_create(hmr_ctx* c, int np, const hmr_patch_geometry* geoms, hmr_le
     lv->L.chunk_mult = 1;
     lv->L.split_mode = 0;
     lv->L.mom0 = momentum0(c->v);
+    lv->L.bvals = c->d_bvals;
     lv->threads = 128;
     int r = level_max_blocks(lv, lv->threads, &lv->blocks);
     if (r || lv->blocks < 1) {
@@ -907,7 +923,7 @@ int hmr_level_bind_state(hmr_level* lv, int p, double* const* comps) {
 int hmr_level_set_periodic(hmr_level* lv, int p, const int* periodic) {
     if (!lv || p < 0 || p >= lv->npatch || !periodic) return HMR_ERR_ARGUMENT;
     for (int a = 0; a < 3; a++) {
-        if (a < lv->ctx->v.dim && (periodic[a] < HMR_FILL_ZERO_GRADIENT || periodic[a] > HMR_FILL_REFLECT))
+        if (a < lv->ctx->v.dim && (periodic[a] < HMR_FILL_ZERO_GRADIENT || periodic[a] > HMR_FILL_DIRICHLET))
             return HMR_ERR_ARGUMENT;
         if (a < lv->ctx->v.dim && periodic[a] == HMR_FILL_REFLECT && lv->geoms[p].n[a] < lv->geoms[p].gh)
             return HMR_ERR_ARGUMENT;
@@ -923,7 +939,8 @@ int hmr_level_set_layout(hmr_level* lv, const int* lo, const int* domain, const 
     const int gh = patch_ghosts(lv->ctx->v);
     int dom[3] = {1, 1, 1}, per[3] = {0, 0, 0};
     for (int a = 0; a < dim; a++) {
-        if (domain[a] < 1 || (periodic[a] != 0 && periodic[a] != 1 && periodic[a] != HMR_FILL_REFLECT))
+        if (domain[a] < 1 || (periodic[a] != 0 && periodic[a] != 1 && periodic[a] != HMR_FILL_REFLECT &&
+                              periodic[a] != HMR_FILL_DIRICHLET))
             return HMR_ERR_ARGUMENT;
         // the mirror images of a reflecting wall's ghost cells lie in the domain
         if (periodic[a] == HMR_FILL_REFLECT && domain[a] < gh) return HMR_ERR_ARGUMENT;

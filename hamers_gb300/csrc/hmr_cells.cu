@@ -62,10 +62,11 @@ struct Periodic {
 };
 
 template <int DIM>
-__global__ void __launch_bounds__(THREADS) fill_kernel(Geom g, Comp Q, int ncomp, Periodic per, int mom0) {
+__global__ void __launch_bounds__(THREADS) fill_kernel(Geom g, Comp Q, int ncomp, Periodic per, int mom0,
+                                                       const double* bv) {
     const long n = ncell_of(g);
     for (long x = (long)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (long)gridDim.x * blockDim.x)
-        fill_item<DIM>(g, Q, ncomp, per.p, x, mom0);
+        fill_item<DIM>(g, Q, ncomp, per.p, x, mom0, bv);
 }
 
 int launch_cells(const Variant& v, const Params& P, const Geom& g, const Comp& Q, const Scratch& S,
@@ -86,18 +87,20 @@ int launch_sensor(const Variant& v, const Geom& g, const Scratch& S, cudaStream_
     });
 }
 
-int launch_fill(int dim, const Geom& g, const Comp& Q, int ncomp, const int* periodic, int mom0, cudaStream_t st) {
+int launch_fill(int dim, const Geom& g, const Comp& Q, int ncomp, const int* periodic, int mom0, const double* bv,
+                cudaStream_t st) {
     Periodic per;
     for (int a = 0; a < 3; a++) per.p[a] = periodic ? periodic[a] : 0;
-    if (dim == 2) fill_kernel<2><<<grid_for(ncell_of(g)), THREADS, 0, st>>>(g, Q, ncomp, per, mom0);
-    else fill_kernel<3><<<grid_for(ncell_of(g)), THREADS, 0, st>>>(g, Q, ncomp, per, mom0);
+    if (dim == 2) fill_kernel<2><<<grid_for(ncell_of(g)), THREADS, 0, st>>>(g, Q, ncomp, per, mom0, bv);
+    else fill_kernel<3><<<grid_for(ncell_of(g)), THREADS, 0, st>>>(g, Q, ncomp, per, mom0, bv);
     return (int)cudaPeekAtLastError();
 }
 
 // Adjoint of the single-patch ghost fill: every ghost cell's adjoint is added
 // to the interior cell it was copied from (a gather per interior cell over the
 // ghost cells of its preimage, so no two threads write one cell), then the
-// ghost adjoints are cleared.
+// ghost adjoints are cleared.  Ghost cells beyond a Dirichlet side are copies of
+// no cell (their adjoints are cleared only).
 __device__ __forceinline__ int fill_src(int v, int n, int periodic) {
     if (v >= 0 && v < n) return v;
     if (periodic == 1) return ((v % n) + n) % n;
@@ -117,7 +120,7 @@ __global__ void __launch_bounds__(THREADS) fill_vjp_gather_kernel(Geom g, Comp Q
         for (int a = 0; a < 3; a++) {
             pre[a][0] = c[a];
             np[a] = 1;
-            if (a >= DIM || per.p[a] == 2) continue;   // provided ghosts are not copies of this cell
+            if (a >= DIM || per.p[a] == 2 || per.p[a] == 4) continue;   // provided or Dirichlet: no copies
             for (int v = -g.gh; v < g.n[a] + g.gh; v++) {
                 if (v >= 0 && v < g.n[a]) continue;
                 if (fill_src(v, g.n[a], per.p[a]) == c[a] && np[a] < 9) pre[a][np[a]++] = v;
@@ -766,7 +769,7 @@ __global__ void __launch_bounds__(THREADS) level_domain_vjp_kernel(const LevelFi
         c[0] = (int)(x % g.G[0]) - g.gh;
         c[1] = (int)((x / g.G[0]) % g.G[1]) - g.gh;
         c[2] = DIM == 3 ? (int)(x / ((long)g.G[0] * g.G[1])) - g.gh : 0;
-        bool physical = false;
+        bool physical = false, dirichlet = false;
         int flip[3] = {-1, -1, -1};
 #pragma unroll
         for (int a = 0; a < 3; a++) {
@@ -775,7 +778,9 @@ __global__ void __launch_bounds__(THREADS) level_domain_vjp_kernel(const LevelFi
             const int G = w.lo[a] + c[a];
             if (G >= 0 && G < D.dom[a]) continue;
             physical = true;
-            if (D.per[a] == 3) {
+            if (D.per[a] == 4) {
+                dirichlet = true;   // a constant: its adjoint reaches no cell
+            } else if (D.per[a] == 3) {
                 s[a] = (G < 0 ? -G - 1 : 2 * D.dom[a] - 1 - G) - w.lo[a];
                 flip[a] = mom0 + a;
             } else {
@@ -783,6 +788,10 @@ __global__ void __launch_bounds__(THREADS) level_domain_vjp_kernel(const LevelFi
             }
         }
         if (!physical) continue;
+        if (dirichlet) {
+            for (int e = 0; e < ncomp; e++) w.Qb.p[e][x] = 0.0;
+            continue;
+        }
         const long y = cidx<DIM>(g, s[0], s[1], s[2]);
         for (int e = 0; e < ncomp; e++) {
             const double v = w.Qb.p[e][x];

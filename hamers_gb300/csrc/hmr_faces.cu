@@ -287,12 +287,12 @@ level_kernel(Params P, LevelArgs L) {
         for (long t = t0; t < L.total_fill; t += stride) {
             const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_fill; });
             domain_fill_item<DIM>(W[p].g, W[p].Q[sl], L.ncomp, W[p].lo, L.dom, L.dom_periodic, t - W[p].off_fill,
-                                  L.mom0);
+                                  L.mom0, L.bvals);
         }
     } else {
         for (long t = t0; t < L.total_fill; t += stride) {
             const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_fill; });
-            fill_item<DIM>(W[p].g, W[p].Q[L.nst - 1], L.ncomp, W[p].periodic, t - W[p].off_fill, L.mom0);
+            fill_item<DIM>(W[p].g, W[p].Q[L.nst - 1], L.ncomp, W[p].periodic, t - W[p].off_fill, L.mom0, L.bvals);
         }
     }
     HMR_BARRIER();

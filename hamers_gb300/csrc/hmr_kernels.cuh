@@ -505,12 +505,17 @@ __device__ __forceinline__ void update_item(const Geom& g, const Scratch& S, con
 // ---------------------------------------------------------------------------
 // Ghost fill of a single patch, per axis: mode 0 zero-gradient, 1 periodic,
 // 2 provided by the caller (left untouched: neighbour copies, coarse-fine
-// interpolation or analytic values).  item over the ghost box (interior
-// items skip).
+// interpolation or analytic values), 3 reflecting wall, 4 Dirichlet (the
+// side's constant values bv[(2 axis + side) ncomp + e],
+// BasicCartesianBoundaryUtilities2.cpp:150-165).  A ghost cell beyond a
+// Dirichlet side takes that side's values -- beyond two Dirichlet sides, those
+// of the lower axis (the reference's corner conditions XDIRICHLET / YDIRICHLET
+// name the axis whose values a corner takes, :679-710) -- unless it lies beyond
+// a provided side.  item over the ghost box (interior items skip).
 // ---------------------------------------------------------------------------
 template <int DIM>
 __device__ __forceinline__ void fill_item(const Geom& g, const Comp& Q, int ncomp, const int* periodic, long x,
-                                          int mom0) {
+                                          int mom0, const double* bv) {
     int c[3];
     c[0] = (int)(x % g.G[0]) - g.gh;
     c[1] = (int)((x / g.G[0]) % g.G[1]) - g.gh;
@@ -518,6 +523,7 @@ __device__ __forceinline__ void fill_item(const Geom& g, const Comp& Q, int ncom
     bool inside = true;
     int s[3];
     int flip = -1, flip2 = -1, flip3 = -1;   // momentum components negated by reflecting walls
+    int dside = -1;                          // Dirichlet side (2 axis + high) whose values the cell takes
 #pragma unroll
     for (int a = 0; a < 3; a++) {
         s[a] = c[a];
@@ -525,7 +531,9 @@ __device__ __forceinline__ void fill_item(const Geom& g, const Comp& Q, int ncom
         if (c[a] < 0 || c[a] >= g.n[a]) {
             if (periodic[a] == 2) return;
             inside = false;
-            if (periodic[a] == 1) {
+            if (periodic[a] == 4) {
+                if (dside < 0) dside = 2 * a + (c[a] >= 0);
+            } else if (periodic[a] == 1) {
                 s[a] = ((c[a] % g.n[a]) + g.n[a]) % g.n[a];
             } else if (periodic[a] == 3) {
                 // reflecting wall: mirror image across the boundary face
@@ -540,6 +548,10 @@ __device__ __forceinline__ void fill_item(const Geom& g, const Comp& Q, int ncom
         }
     }
     if (inside) return;
+    if (dside >= 0) {
+        for (int e = 0; e < ncomp; e++) Q.p[e][x] = bv[dside * ncomp + e];
+        return;
+    }
     const long y = cidx<DIM>(g, s[0], s[1], s[2]);
     for (int e = 0; e < ncomp; e++) {
         const double v = Q.p[e][y];
@@ -551,17 +563,20 @@ __device__ __forceinline__ void fill_item(const Geom& g, const Comp& Q, int ncom
 // (local) of a patch at level index lo, outside the domain along an axis, takes the value of
 // the nearest in-domain cell (zero-gradient, dom_periodic 0) or of its mirror image across the
 // domain face with the normal momentum negated (reflecting wall, dom_periodic 3) -- the patch's
-// own interior or a ghost cell filled from a neighbour before.  Ghost cells inside the domain
-// are left alone (neighbour copies or provided values).
+// own interior or a ghost cell filled from a neighbour before -- or, beyond a Dirichlet face
+// (dom_periodic 4), that face's values (the lower axis's beyond two, as fill_item).  Ghost
+// cells inside the domain are left alone (neighbour copies or provided values).
 template <int DIM>
 __device__ __forceinline__ void domain_fill_item(const Geom& g, const Comp& Q, int ncomp, const int* lo,
-                                                 const int* dom, const int* dom_periodic, long x, int mom0) {
+                                                 const int* dom, const int* dom_periodic, long x, int mom0,
+                                                 const double* bv) {
     int c[3], s[3];
     c[0] = (int)(x % g.G[0]) - g.gh;
     c[1] = (int)((x / g.G[0]) % g.G[1]) - g.gh;
     c[2] = DIM == 3 ? (int)(x / ((long)g.G[0] * g.G[1])) - g.gh : 0;
     bool physical = false;
     int flip = -1, flip2 = -1, flip3 = -1;
+    int dside = -1;
 #pragma unroll
     for (int a = 0; a < 3; a++) {
         s[a] = c[a];
@@ -569,7 +584,9 @@ __device__ __forceinline__ void domain_fill_item(const Geom& g, const Comp& Q, i
         const int G = lo[a] + c[a];
         if (G >= 0 && G < dom[a]) continue;
         physical = true;
-        if (dom_periodic[a] == 3) {
+        if (dom_periodic[a] == 4) {
+            if (dside < 0) dside = 2 * a + (G >= 0);
+        } else if (dom_periodic[a] == 3) {
             // reflecting wall: mirror image across the domain face, in the level's index space
             s[a] = (G < 0 ? -G - 1 : 2 * dom[a] - 1 - G) - lo[a];
             if (flip < 0) flip = mom0 + a;
@@ -580,6 +597,10 @@ __device__ __forceinline__ void domain_fill_item(const Geom& g, const Comp& Q, i
         }
     }
     if (!physical) return;
+    if (dside >= 0) {
+        for (int e = 0; e < ncomp; e++) Q.p[e][x] = bv[dside * ncomp + e];
+        return;
+    }
     const long y = cidx<DIM>(g, s[0], s[1], s[2]);
     for (int e = 0; e < ncomp; e++) {
         const double v = Q.p[e][y];

@@ -187,8 +187,9 @@ struct LevelArgs {
     int ncopy;
     long total_copy;
     int dom[3];                      // domain extent in cells
-    int dom_periodic[3];             // per axis: 1 periodic, 0 zero-gradient or 3 reflecting wall faces
+    int dom_periodic[3];             // per axis: 1 periodic, 0 zero-gradient, 3 reflecting wall or 4 Dirichlet faces
     int mom0;                        // first momentum component (the normal one flips at a reflecting wall)
+    const double* bvals;             // device [6][ncomp]: the Dirichlet values per side (2 axis + high)
     // work splitting (autotuned; results do not depend on it): phase chunks of chunk_mult
     // block widths; split_mode 1 hands the cell-wise phases out by a fixed grid stride
     int chunk_mult;
@@ -202,14 +203,15 @@ int launch_cells(const hmr::Variant& v, const hmr::Params& P, const hmr::Geom& g
                  const hmr::Scratch& S, cudaStream_t st);
 int launch_sensor(const hmr::Variant& v, const hmr::Geom& g, const hmr::Scratch& S, cudaStream_t st);
 // Ghost fill of one patch per axis (hmr_fill_mode); mom0: the first momentum component, whose
-// normal one a reflecting wall negates.
+// normal one a reflecting wall negates; bv: device [6][ncomp] values of Dirichlet sides.
 int launch_fill(int dim, const hmr::Geom& g, const hmr::Comp& Q, int ncomp, const int* periodic, int mom0,
-                cudaStream_t st);
+                const double* bv, cudaStream_t st);
 int launch_fill_vjp(int dim, const hmr::Geom& g, const hmr::Comp& Qb, int ncomp, const int* periodic, int mom0,
                     cudaStream_t st);
 // Adjoint of the level's ghost fill with a layout (the exchange between patches, then the domain's
 // physical faces): the physical ghost cells first add their adjoints to the in-domain cells they
-// were copied from (negated normal momentum at reflecting walls), then the exchanged ghost cells
+// were copied from (negated normal momentum at reflecting walls; Dirichlet ghost cells copy no
+// cell and are only zeroed), then the exchanged ghost cells
 // to the patch interiors they were copied from; both are zeroed.  Ghost cells no copy wrote keep
 // theirs.  Sums of several ghost cells into one source cell are atomic.
 struct LevelFillVjpPatch {

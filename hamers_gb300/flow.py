@@ -52,7 +52,7 @@ _DIFFUSIVE = {
 RK3_ALPHA = [[1.0], [3.0 / 4.0, 1.0 / 4.0], [1.0 / 3.0, 0.0, 2.0 / 3.0]]
 
 # ghost-fill mode per axis (hmr_fill_mode of include/hmr.h)
-FILL_ZERO_GRADIENT, FILL_PERIODIC, FILL_PROVIDED, FILL_REFLECT = 0, 1, 2, 3
+FILL_ZERO_GRADIENT, FILL_PERIODIC, FILL_PROVIDED, FILL_REFLECT, FILL_DIRICHLET = 0, 1, 2, 3, 4
 RK3_BETA = [[1.0], [0.0, 1.0 / 4.0], [0.0, 0.0, 2.0 / 3.0]]
 RK3_GAMMA = [[1.0 / 6.0], [0.0, 1.0 / 6.0], [0.0, 0.0, 2.0 / 3.0]]
 
@@ -221,6 +221,18 @@ class ConvectiveFluxReconstructor:
         diffusive flux (NavierStokes.cpp:317-349 takes the larger of the two widths)."""
         return self._lib.hmr_num_patch_ghosts(self.ctx)
 
+    def setDirichletValues(self, axis, side, values):
+        """Conservative values (ncomp) that ghost cells beyond the FILL_DIRICHLET side `side`
+        (0 low, 1 high) of `axis` take in every fill of this context (the reference's DIRICHLET
+        boundary data, EulerBoundaryConditions::readDirichletBoundaryDataEntry, already
+        converted to conservative variables)."""
+        v = [float(x) for x in values]
+        if len(v) != self.ncomp:
+            raise ValueError(f"expected {self.ncomp} conservative values, got {len(v)}")
+        arr = (ctypes.c_double * len(v))(*v)
+        L.check("hmr_set_dirichlet_values", self._lib.hmr_set_dirichlet_values(
+            self.ctx, int(axis), int(side), ctypes.cast(arr, ctypes.POINTER(ctypes.c_double))))
+
     def allocateFlux(self, patch):
         dim = self.flow_model.dim
         n3 = list(patch.n) + [1] * (3 - len(patch.n))
@@ -305,8 +317,9 @@ class Euler:
 
     def fillGhosts(self, patch, periodic, stream=None):
         """Ghost fill of one patch, mode per axis: FILL_ZERO_GRADIENT (0, the extrapolation
-        boundary), FILL_PERIODIC (1), FILL_PROVIDED (2, left as supplied) or FILL_REFLECT (3, a
-        slip wall: mirror image with the normal momentum negated; needs >= 4 cells on the axis)."""
+        boundary), FILL_PERIODIC (1), FILL_PROVIDED (2, left as supplied), FILL_REFLECT (3, a
+        slip wall: mirror image with the normal momentum negated; needs >= 4 cells on the axis)
+        or FILL_DIRICHLET (4, the values of ConvectiveFluxReconstructor.setDirichletValues)."""
         g = patch.geometry()
         q, _k = L.ptr_array(_state_ptrs(self.rec, patch.n, patch.data))
         per = (ctypes.c_int * 3)(*(list(periodic) + [0] * (3 - len(periodic))))
@@ -695,8 +708,8 @@ class BatchedLevel:
 
     def set_layout(self, lo, domain, periodic):
         """Patch positions (first interior cell per patch, level index space), the domain's cells
-        per axis and its boundary per axis (FILL_PERIODIC, FILL_ZERO_GRADIENT or FILL_REFLECT
-        walls): enables the ghost exchange between patches."""
+        per axis and its boundary per axis (FILL_PERIODIC, FILL_ZERO_GRADIENT, FILL_REFLECT walls
+        or FILL_DIRICHLET faces): enables the ghost exchange between patches."""
         dim = self.rec.flow_model.dim
         flat = []
         for p in range(self.npatch):

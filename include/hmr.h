@@ -204,16 +204,29 @@ typedef enum {
     HMR_FILL_ZERO_GRADIENT = 0,   /* copy of the nearest interior cell (extrapolation boundary) */
     HMR_FILL_PERIODIC = 1,        /* periodic image within the patch */
     HMR_FILL_PROVIDED = 2,        /* ghost cells supplied by the caller are left untouched */
-    HMR_FILL_REFLECT = 3          /* reflecting (slip) wall: mirror image across the boundary face with the
+    HMR_FILL_REFLECT = 3,         /* reflecting (slip) wall: mirror image across the boundary face with the
                                      normal momentum negated -- the reference's REFLECT condition
                                      (BasicCartesianBoundaryUtilities2.cpp:349-440 with the scalar/vector
                                      split of EulerBoundaryConditions.cpp:205-297); needs >= 4 cells along
                                      the axis */
+    HMR_FILL_DIRICHLET = 4        /* the reference's DIRICHLET condition (BasicCartesianBoundaryUtilities2.cpp:
+                                     150-165, values from EulerBoundaryConditions::
+                                     readDirichletBoundaryDataEntry): every ghost cell beyond the side takes
+                                     the side's conservative values (hmr_set_dirichlet_values); a corner
+                                     beyond two Dirichlet sides takes the lower axis's, and one beyond a
+                                     Dirichlet side and another condition the Dirichlet values -- the corner
+                                     conditions XDIRICHLET / YDIRICHLET / ZDIRICHLET naming that axis */
 } hmr_fill_mode;
 
-/* Single-patch ghost fill, mode per axis (hmr_fill_mode; any other non-zero value of older callers
- * is rejected by hmr_level_set_periodic and read as zero-gradient here) -- the one-patch equivalent
- * of the SAMRAI fill schedule, RungeKuttaLevelIntegrator.cpp:1568,1701. */
+/* Values of the HMR_FILL_DIRICHLET side `side` (0 low, 1 high) of axis `axis`: ncomp conservative
+ * values (the reference converts the input's primitive values to these once, with the flow model's
+ * basic utilities, EulerBoundaryConditions.cpp:638-723).  Held by the context for every fill that
+ * runs on it afterwards, per patch and per level; 0.0 until set.  Rejects non-finite values. */
+int hmr_set_dirichlet_values(hmr_ctx* ctx, int axis, int side, const double* values);
+
+/* Single-patch ghost fill, mode per axis (hmr_fill_mode; other values are rejected with
+ * HMR_ERR_ARGUMENT) -- the one-patch equivalent of the SAMRAI fill schedule,
+ * RungeKuttaLevelIntegrator.cpp:1568,1701. */
 int hmr_fill_ghosts_patch(hmr_ctx* ctx, const hmr_patch_geometry* geom, double* const* Q,
                           const int* periodic, void* stream);
 
@@ -286,8 +299,9 @@ int hmr_rk_substep_vjp_patch(hmr_ctx* ctx, const hmr_patch_geometry* geom, int s
 
 /* Adjoint of hmr_fill_ghosts_patch: adds the adjoint of every filled ghost cell to the interior
  * cell it is copied from (negated for the normal momentum at a reflecting wall) and zeroes it;
- * ghost cells along HMR_FILL_PROVIDED axes keep their adjoints (they belong to whatever supplied
- * the values).  No counterpart in the reference. */
+ * Dirichlet ghost cells copy no cell (their adjoints are zeroed); ghost cells along
+ * HMR_FILL_PROVIDED axes keep their adjoints (they belong to whatever supplied the values).  No
+ * counterpart in the reference. */
 int hmr_fill_ghosts_vjp_patch(hmr_ctx* ctx, const hmr_patch_geometry* geom, double* const* Qbar,
                               const int* periodic, void* stream);
 
@@ -303,10 +317,11 @@ int hmr_level_destroy(hmr_level* level);
  * patches (and of their periodic images) that cover them, then cells outside the domain along
  * non-periodic axes take the nearest in-domain value (zero-gradient, the extrapolation boundary)
  * or, at reflecting walls, the mirror image across the domain face with the normal momentum
- * negated; ghost cells inside the domain covered by no patch of the level (a coarse-fine
- * boundary) are left as the caller provides them.  lo: 3 ints per patch (first interior cell),
- * domain: cells per axis, periodic per axis: 1 periodic, 0 zero-gradient faces,
- * HMR_FILL_REFLECT reflecting walls.  Boxes must lie in the domain and not overlap. */
+ * negated, or at Dirichlet faces the face's values (as hmr_fill_ghosts_patch); ghost cells inside
+ * the domain covered by no patch of the level (a coarse-fine boundary) are left as the caller
+ * provides them.  lo: 3 ints per patch (first interior cell), domain: cells per axis, periodic
+ * per axis: 1 periodic, 0 zero-gradient faces, HMR_FILL_REFLECT reflecting walls,
+ * HMR_FILL_DIRICHLET Dirichlet faces.  Boxes must lie in the domain and not overlap. */
 int hmr_level_set_layout(hmr_level* level, const int* lo, const int* domain, const int* periodic);
 /* Binds the caller's ghost-box arrays (ncomp device pointers) as slot 0 of a patch. */
 int hmr_level_bind_state(hmr_level* level, int patch, double* const* comps);

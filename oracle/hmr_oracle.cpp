@@ -201,6 +201,16 @@ int hmro_fill_ghosts(const hmro_config* cfg, const int* n, const int* periodic, 
     return 0;
 }
 
+// As hmro_fill_ghosts, with the values of DIRICHLET sides (mode 4): bvals[(2 axis + high) ncomp + e].
+int hmro_fill_ghosts_bv(const hmro_config* cfg, const int* n, const int* periodic, const double* bvals, double* Q) {
+    const Config c = to_cfg(cfg);
+    const Box b = make_box(c.dim, n, c.ghosts);
+    std::vector<double*> q(num_comp(c));
+    for (int e = 0; e < num_comp(c); e++) q[e] = Q + (size_t)e * b.ncell();
+    fill_ghosts<double>(c, n, periodic, q.data(), bvals);
+    return 0;
+}
+
 // SSPRK(3,3) weights, RungeKuttaLevelIntegrator.cpp:3909-3927.
 static const double RK3_ALPHA[3][3] = {{1.0, 0, 0}, {3.0/4.0, 1.0/4.0, 0}, {1.0/3.0, 0.0, 2.0/3.0}};
 static const double RK3_BETA[3][3]  = {{1.0, 0, 0}, {0.0, 1.0/4.0, 0}, {0.0, 0.0, 2.0/3.0}};
@@ -210,8 +220,17 @@ static const double RK3_GAMMA[3][3] = {{1.0/6.0, 0, 0}, {0.0, 1.0/6.0, 0}, {0.0,
 // stage (the stage loop of RungeKuttaLevelIntegrator::advanceLevel,
 // RungeKuttaLevelIntegrator.cpp:1672-1748).  Q holds the ghost box and is
 // updated in place (interior; ghosts are refilled).
+int hmro_rk3_advance_bv(const hmro_config* cfg, const int* n, const double* dx, double dt,
+                        const int* periodic, const double* bvals, int nsteps, double* Q, long* stats);
+
 int hmro_rk3_advance(const hmro_config* cfg, const int* n, const double* dx, double dt,
                      const int* periodic, int nsteps, double* Q, long* stats) {
+    return hmro_rk3_advance_bv(cfg, n, dx, dt, periodic, nullptr, nsteps, Q, stats);
+}
+
+// As hmro_rk3_advance, with the values of DIRICHLET sides (hmro_fill_ghosts_bv).
+int hmro_rk3_advance_bv(const hmro_config* cfg, const int* n, const double* dx, double dt,
+                        const int* periodic, const double* bvals, int nsteps, double* Q, long* stats) {
     const Config c = to_cfg(cfg);
     const Box b = make_box(c.dim, n, c.ghosts);
     const int ncomp = num_comp(c), neq = num_eqn(c);
@@ -224,7 +243,7 @@ int hmro_rk3_advance(const hmro_config* cfg, const int* n, const double* dx, dou
         for (int sn = 0; sn < 3; sn++) {
             // copyTimeDependentData(scratch -> intermediate[sn]) + ghost fill
             std::copy(Q, Q + qs, Qint.begin() + sn * qs);
-            hmro_fill_ghosts(cfg, n, periodic, Qint.data() + sn * qs);
+            hmro_fill_ghosts_bv(cfg, n, periodic, bvals, Qint.data() + sn * qs);
             std::fill(Sint.begin() + sn * (size_t)neq * nint, Sint.begin() + (sn + 1) * (size_t)neq * nint, 0.0);
             long st[3];
             hmro_conv_flux_source(cfg, n, dx, dt, Qint.data() + sn * qs, Fint.data() + sn * fl,
@@ -234,7 +253,7 @@ int hmro_rk3_advance(const hmro_config* cfg, const int* n, const double* dx, dou
                           Qint.data(), Fint.data(), Sint.data(), Qout.data(), nullptr, nullptr);
             std::copy(Qout.begin(), Qout.end(), Q);
         }
-        hmro_fill_ghosts(cfg, n, periodic, Q);
+        hmro_fill_ghosts_bv(cfg, n, periodic, bvals, Q);
     }
     if (stats) for (int i = 0; i < 3; i++) stats[i] = tot[i];
     (void)neq;

@@ -1804,7 +1804,12 @@ inline void refine_ghosts(const Config& c, const int* ratio, const int* fn, cons
 // to it negated (BasicCartesianBoundaryUtilities2.cpp:349-395 REFLECT for the momentum vector,
 // :397-440 SYMMETRY for the scalars, as EulerBoundaryConditions.cpp:205-297 assigns them).
 template <class T>
-void fill_ghosts(const Config& c, const int* n, const int* periodic, T* const* Q) {
+void fill_ghosts(const Config& c, const int* n, const int* periodic, T* const* Q, const double* bvals = nullptr) {
+    // Mode per axis: 0 FLOW (copy of the nearest interior cell), 1 periodic, 3 REFLECT (mirror
+    // image, normal momentum negated), 4 DIRICHLET: the side's values bvals[(2 axis + high) ncomp
+    // + e] (BasicCartesianBoundaryUtilities2.cpp:150-165); a cell beyond two Dirichlet sides takes
+    // the lower axis's values (the corner condition XDIRICHLET, :679-710), one beyond a Dirichlet
+    // side and another condition the Dirichlet values.
     const Box b = make_box(c.dim, n, c.ghosts);
     const int ncomp = num_comp(c);
     const int mom0 = vel_index(c);
@@ -1820,6 +1825,13 @@ void fill_ghosts(const Config& c, const int* n, const int* periodic, T* const* Q
         for (int i = -b.g[0]; i < b.n[0] + b.g[0]; i++) {
             if (i >= 0 && i < b.n[0] && j >= 0 && j < b.n[1] && k >= 0 && k < b.n[2]) continue;
             const int ijk[3] = {i, j, k};
+            int dside = -1;
+            for (int a = 0; a < c.dim && dside < 0; a++)
+                if (periodic[a] == 4 && (ijk[a] < 0 || ijk[a] >= b.n[a])) dside = 2 * a + (ijk[a] >= 0);
+            if (dside >= 0) {
+                Q[e][b.cell(i, j, k)] = T(bvals ? bvals[dside * ncomp + e] : 0.0);
+                continue;
+            }
             bool flip = false;
             for (int a = 0; a < c.dim; a++)
                 if (periodic[a] == 3 && (ijk[a] < 0 || ijk[a] >= b.n[a]) && e == mom0 + a) flip = !flip;

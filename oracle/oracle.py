@@ -78,7 +78,9 @@ def lib():
         L.hmro_conv_flux_source.argtypes = [cp, ip, dp, ctypes.c_double, dp, dp, dp, lp]
         L.hmro_rk_stage.argtypes = [cp, ip, dp, ctypes.c_int, dp, dp, dp, dp, dp, dp, dp, dp, dp]
         L.hmro_fill_ghosts.argtypes = [cp, ip, ip, dp]
+        L.hmro_fill_ghosts_bv.argtypes = [cp, ip, ip, dp, dp]
         L.hmro_rk3_advance.argtypes = [cp, ip, dp, ctypes.c_double, ip, ctypes.c_int, dp, lp]
+        L.hmro_rk3_advance_bv.argtypes = [cp, ip, dp, ctypes.c_double, ip, dp, ctypes.c_int, dp, lp]
         L.hmro_stage_threads.argtypes = [cp, ip, dp, ctypes.c_double, dp, ctypes.c_int]
         L.hmro_stage_threads.restype = ctypes.c_long
         L.hmro_spectral_radius.argtypes = [cp, ip, dp, dp]
@@ -215,6 +217,8 @@ def ref_lib():
         L.hmrref_diff_flux.restype = ctypes.c_int
         L.hmrref_fill_boundaries.argtypes = [ctypes.POINTER(_Cfg), ip, ip, ctypes.c_int, dp]
         L.hmrref_fill_boundaries.restype = ctypes.c_int
+        L.hmrref_fill_boundaries_bv.argtypes = [ctypes.POINTER(_Cfg), ip, ip, ctypes.c_int, dp, dp]
+        L.hmrref_fill_boundaries_bv.restype = ctypes.c_int
         _ref_lib = L
     return _ref_lib
 
@@ -299,21 +303,33 @@ def rk_stage(cfg, n, dx, alpha, beta, gamma, Q_int, F_int, S_int, F_acc=None, S_
     return Qo
 
 
-def fill_ghosts(cfg, n, periodic, Q):
-    """Ghost fill, mode per axis: 0 zero-gradient, 1 periodic, 3 reflecting wall."""
+def fill_ghosts(cfg, n, periodic, Q, dirichlet=None):
+    """Ghost fill, mode per axis: 0 zero-gradient, 1 periodic, 3 reflecting wall, 4 Dirichlet
+    (dirichlet: values per side, shape (2 dim, ncomp), row 2 axis + high)."""
     assert Q.flags["C_CONTIGUOUS"] and Q.dtype == np.float64
-    lib().hmro_fill_ghosts(ctypes.byref(cfg.c()), _ip(_n3(n)), _ip(list(periodic) + [0] * (3 - len(periodic))),
-                           _dp(Q))
+    per = _ip(list(periodic) + [0] * (3 - len(periodic)))
+    if dirichlet is None:
+        lib().hmro_fill_ghosts(ctypes.byref(cfg.c()), _ip(_n3(n)), per, _dp(Q))
+    else:
+        bv = np.zeros((6, Q.shape[0]))
+        d = np.asarray(dirichlet, dtype=np.float64)
+        bv[:d.shape[0]] = d
+        lib().hmro_fill_ghosts_bv(ctypes.byref(cfg.c()), _ip(_n3(n)), per, _dp(np.ascontiguousarray(bv)), _dp(Q))
     return Q
 
 
-def rk3_advance(cfg, n, dx, dt, periodic, nsteps, Q):
-    """nsteps SSPRK3 steps of one patch, in place; returns the face counters."""
+def rk3_advance(cfg, n, dx, dt, periodic, nsteps, Q, dirichlet=None):
+    """nsteps SSPRK3 steps of one patch, in place; returns the face counters.  dirichlet: values
+    of the Dirichlet sides (mode 4), as fill_ghosts takes them."""
     assert Q.flags["C_CONTIGUOUS"] and Q.dtype == np.float64
     stats = (ctypes.c_long * 3)()
-    lib().hmro_rk3_advance(ctypes.byref(cfg.c()), _ip(_n3(n)), _dv(list(dx) + [1.0] * (3 - len(dx))),
-                           float(dt), _ip(list(periodic) + [0] * (3 - len(periodic))), int(nsteps),
-                           _dp(Q), stats)
+    bv = np.zeros((6, Q.shape[0]))
+    if dirichlet is not None:
+        d = np.asarray(dirichlet, dtype=np.float64)
+        bv[:d.shape[0]] = d
+    lib().hmro_rk3_advance_bv(ctypes.byref(cfg.c()), _ip(_n3(n)), _dv(list(dx) + [1.0] * (3 - len(dx))),
+                              float(dt), _ip(list(periodic) + [0] * (3 - len(periodic))), _dp(bv), int(nsteps),
+                              _dp(Q), stats)
     return (stats[0], stats[1], stats[2])
 
 
@@ -334,15 +350,20 @@ def _split_flux(cfg, n, flat):
     return out
 
 
-def ref_fill_boundaries(cfg, n, mode, Q, corner_axis=0):
+def ref_fill_boundaries(cfg, n, mode, Q, corner_axis=0, dirichlet=None):
     """The reference's physical-boundary fill (EulerBoundaryConditions with
     BasicCartesianBoundaryUtilities2/3) of one patch covering the domain, in place: mode per
-    axis 0 (FLOW) or 3 (REFLECT); corner_axis picks the axis of the X/Y/Z-prefixed corner
-    conditions."""
+    axis 0 (FLOW), 3 (REFLECT) or 4 (DIRICHLET, values per side in dirichlet: shape
+    (2 dim, ncomp), row 2 axis + high); corner_axis picks the axis of the X/Y/Z-prefixed corner
+    conditions (a corner with a Dirichlet side takes the lowest Dirichlet axis's)."""
     assert Q.flags["C_CONTIGUOUS"] and Q.dtype == np.float64 and Q.shape == ghost_shape(cfg, n)
     L = ref_lib()
-    rc = L.hmrref_fill_boundaries(ctypes.byref(cfg.c()), _ip(_n3(n)), _ip(list(mode) + [0] * (3 - len(mode))),
-                                  int(corner_axis), _dp(Q))
+    per = _ip(list(mode) + [0] * (3 - len(mode)))
+    if dirichlet is None:
+        rc = L.hmrref_fill_boundaries(ctypes.byref(cfg.c()), _ip(_n3(n)), per, int(corner_axis), _dp(Q))
+    else:
+        bv = np.ascontiguousarray(dirichlet, dtype=np.float64)
+        rc = L.hmrref_fill_boundaries_bv(ctypes.byref(cfg.c()), _ip(_n3(n)), per, int(corner_axis), _dp(bv), _dp(Q))
     if rc != 0:
         raise RuntimeError("reference: " + L.hmrref_last_error().decode())
     return Q

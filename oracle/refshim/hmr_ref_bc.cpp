@@ -11,8 +11,13 @@
 // X/Y/Z-prefixed kind naming one of its axes; corner_axis picks which of its walls (the lowest
 // axis index >= corner_axis among them, else the lowest).
 //
+// hmrref_fill_boundaries_bv also takes DIRICHLET sides (mode 4) with their conservative values
+// bvals[(2 axis + high) ncomp + e], handed to the reference's routines per variable as
+// EulerBoundaryConditions holds them (d_bdry_edge/face_conservative_var, :638-723); a corner with a
+// Dirichlet side takes the condition naming the lowest such axis (XDIRICHLET before YDIRICHLET).
+//
 // Layout as hmro_fill_ghosts (oracle/hmr_oracle.cpp): ncomp arrays over the ghost box of width
-// 4, x fastest, filled in place.  mode per axis: 0 FLOW, 3 REFLECT.
+// 4, x fastest, filled in place.  mode per axis: 0 FLOW, 3 REFLECT (4 DIRICHLET with values).
 // Returns 0, or -1 with the reference's error text available from hmrref_last_error().
 #include "flow/flow_models/FlowModels.hpp"
 #include "util/basic_boundary_conditions/BasicBoundaryConditions.hpp"
@@ -44,18 +49,21 @@ namespace {
 
 using namespace BDRY_COND::BASIC;
 
-int axis_cond(int axis, bool reflect) {
+int axis_cond(int axis, int mode) {
     static const int flow[3] = {XFLOW, YFLOW, ZFLOW};
     static const int refl[3] = {XREFLECT, YREFLECT, ZREFLECT};
-    return reflect ? refl[axis] : flow[axis];
+    static const int diri[3] = {XDIRICHLET, YDIRICHLET, ZDIRICHLET};
+    return mode == 4 ? diri[axis] : (mode == 3 ? refl[axis] : flow[axis]);
 }
 
 // X/Y/Z-prefixed condition of a corner whose outward axes are `axes`.
 int corner_cond(const std::vector<int>& axes, const int* mode, int corner_axis) {
+    for (int a : axes)
+        if (mode[a] == 4) return axis_cond(a, 4);
     int pick = axes[0];
     for (int a : axes)
         if (a >= corner_axis) { pick = a; break; }
-    return axis_cond(pick, mode[pick] == 3);
+    return axis_cond(pick, mode[pick]);
 }
 
 int scalar_of(int c) {
@@ -68,15 +76,18 @@ int scalar_of(int c) {
 
 }  // namespace
 
-extern "C" int hmrref_fill_boundaries(const hmrref_config* cfg_opaque, const int* n, const int* mode, int corner_axis,
-                                      double* Q) {
+extern "C" int hmrref_fill_boundaries_bv(const hmrref_config* cfg_opaque, const int* n, const int* mode,
+                                         int corner_axis, const double* bvals, double* Q) {
     try {
         const hmrref_config_head* cfg = reinterpret_cast<const hmrref_config_head*>(cfg_opaque);
         const int D = cfg->dim;
         const tbox::Dimension dim((unsigned short)D);
         const int nsp = cfg->num_species;
-        for (int a = 0; a < D; a++)
-            if (mode[a] != 0 && mode[a] != 3) throw std::runtime_error("boundary mode must be 0 (FLOW) or 3 (REFLECT)");
+        for (int a = 0; a < D; a++) {
+            if (mode[a] != 0 && mode[a] != 3 && mode[a] != 4)
+                throw std::runtime_error("boundary mode must be 0 (FLOW), 3 (REFLECT) or 4 (DIRICHLET)");
+            if (mode[a] == 4 && !bvals) throw std::runtime_error("DIRICHLET sides need values");
+        }
 
         auto fm_db = HAMERS_MAKE_SHARED<tbox::Database>("Flow_model");
         fm_db->putString("equation_of_state", "IDEAL_GAS");
@@ -137,7 +148,8 @@ extern "C" int hmrref_fill_boundaries(const hmrref_config* cfg_opaque, const int
         // Conditions by location, as EulerBoundaryConditions holds them.
         const int nside = 2 * D;
         std::vector<int> side_conds(nside);
-        for (int l = 0; l < nside; l++) side_conds[l] = mode[l / 2] == 3 ? REFLECT : FLOW;
+        for (int l = 0; l < nside; l++)
+            side_conds[l] = mode[l / 2] == 4 ? DIRICHLET : (mode[l / 2] == 3 ? REFLECT : FLOW);
         std::vector<int> edge_conds(D == 3 ? 12 : 4, FLOW), node_conds(D == 3 ? 8 : 4, FLOW);
         std::vector<int>& c2 = D == 2 ? node_conds : edge_conds;
         for (size_t i = 0; i < bb[2].size(); i++) c2[bb[2][i].getLocationIndex()] = corner_cond(outward[2][i], mode, corner_axis);
@@ -168,20 +180,29 @@ extern "C" int hmrref_fill_boundaries(const hmrref_config* cfg_opaque, const int
         for (int l = 0; l < nside; l++) all_sides.push_back(l);
         for (int l = 0; l < (D == 3 ? 12 : 4); l++) all_edges.push_back(l);
         for (int l = 0; l < (D == 3 ? 8 : 4); l++) all_nodes.push_back(l);
-        std::vector<double> none(64, 0.0);
+        int ncomp = 0;
+        for (auto& d : data) ncomp += d->getDepth();
+        int off = 0;   // first component of variable vi
         for (size_t vi = 0; vi < data.size(); vi++) {
             const bool vec = types[vi] == "VECTOR";
             const std::vector<int> sc = vec ? side_conds : scalarise(side_conds);
             const std::vector<int> ec = vec ? edge_conds : scalarise(edge_conds);
             const std::vector<int> nc = vec ? node_conds : scalarise(node_conds);
+            // this variable's boundary values by side location, as d_bdry_edge/face_conservative_var
+            const int depth = data[vi]->getDepth();
+            std::vector<double> vals((size_t)nside * depth, 0.0);
+            if (bvals)
+                for (int l = 0; l < nside; l++)
+                    for (int di = 0; di < depth; di++) vals[(size_t)l * depth + di] = bvals[l * ncomp + off + di];
             if (D == 2) {
-                BasicCartesianBoundaryUtilities2::fillEdgeBoundaryData(names[vi], data[vi], patch, all_sides, sc, none, gcw);
-                BasicCartesianBoundaryUtilities2::fillNodeBoundaryData(names[vi], data[vi], patch, all_nodes, nc, none, gcw);
+                BasicCartesianBoundaryUtilities2::fillEdgeBoundaryData(names[vi], data[vi], patch, all_sides, sc, vals, gcw);
+                BasicCartesianBoundaryUtilities2::fillNodeBoundaryData(names[vi], data[vi], patch, all_nodes, nc, vals, gcw);
             } else {
-                BasicCartesianBoundaryUtilities3::fillFaceBoundaryData(names[vi], data[vi], patch, all_sides, sc, none, gcw);
-                BasicCartesianBoundaryUtilities3::fillEdgeBoundaryData(names[vi], data[vi], patch, all_edges, ec, none, gcw);
-                BasicCartesianBoundaryUtilities3::fillNodeBoundaryData(names[vi], data[vi], patch, all_nodes, nc, none, gcw);
+                BasicCartesianBoundaryUtilities3::fillFaceBoundaryData(names[vi], data[vi], patch, all_sides, sc, vals, gcw);
+                BasicCartesianBoundaryUtilities3::fillEdgeBoundaryData(names[vi], data[vi], patch, all_edges, ec, vals, gcw);
+                BasicCartesianBoundaryUtilities3::fillNodeBoundaryData(names[vi], data[vi], patch, all_nodes, nc, vals, gcw);
             }
+            off += depth;
         }
         q = Q;
         for (auto& d : data) {
@@ -196,4 +217,9 @@ extern "C" int hmrref_fill_boundaries(const hmrref_config* cfg_opaque, const int
         hmrref_set_error(ex.what());
         return -1;
     }
+}
+
+extern "C" int hmrref_fill_boundaries(const hmrref_config* cfg, const int* n, const int* mode, int corner_axis,
+                                      double* Q) {
+    return hmrref_fill_boundaries_bv(cfg, n, mode, corner_axis, nullptr, Q);
 }

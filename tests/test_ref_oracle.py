@@ -173,3 +173,39 @@ def test_oracle_ghost_fill_is_bitwise_the_reference(model, mn, gam, R, dim):
             O.ref_fill_boundaries(cfg, n, mode, Qr, corner_axis)
             assert not np.array_equal(Qr, Q)
             assert np.array_equal(Qo, Qr), (mode, corner_axis)
+
+
+# DIRICHLET sides (BasicCartesianBoundaryUtilities2.cpp:150-165 and the X/Y/Z-prefixed corner
+# conditions, :679-710) with per-side conservative values, alone and beside FLOW and REFLECT.
+DIRICHLET_MODES = {2: ([4, 4], [4, 0], [0, 4], [3, 4], [4, 3]),
+                   3: ([4, 4, 4], [4, 0, 3], [0, 4, 0], [3, 3, 4], [0, 3, 4])}
+
+
+def dirichlet_values(Q, dim, seed):
+    """Conservative values per side (2 dim rows, row 2 axis + high): interior cells of a physical
+    state, so that each side's values are a consistent state of the model."""
+    rng = np.random.default_rng(seed)
+    flat = Q.reshape(Q.shape[0], -1)
+    return np.ascontiguousarray(flat[:, rng.integers(0, flat.shape[1], 2 * dim)].T)
+
+
+@pytest.mark.parametrize("model,mn,gam,R", MODELS, ids=[m[1] for m in MODELS])
+@pytest.mark.parametrize("dim", [2, 3])
+def test_oracle_dirichlet_fill_is_bitwise_the_reference(model, mn, gam, R, dim):
+    n = [9, 7] if dim == 2 else [6, 5, 7]
+    cfg = O.Config(model, dim, gam, O.SCHEME_WCNS5_JS, species_R=R)
+    Q = smooth_state(model, dim, n, seed=3, species_gamma=gam)
+    bv = dirichlet_values(Q, dim, seed=11)
+    for mode in DIRICHLET_MODES[dim]:
+        for corner_axis in range(dim):   # decides the corners without a Dirichlet side
+            Qo = Q.copy()
+            O.fill_ghosts(cfg, n, mode, Qo, dirichlet=bv)
+            Qr = Q.copy()
+            O.ref_fill_boundaries(cfg, n, mode, Qr, corner_axis, dirichlet=bv)
+            assert not np.array_equal(Qr, Q)
+            assert np.array_equal(Qo, Qr), (mode, corner_axis)
+            # every ghost cell beyond a Dirichlet side holds one of the sides' values
+            d = [a for a in range(dim) if mode[a] == 4]
+            sl = (slice(None),) + tuple(slice(0, 4) if (2 - a) < dim and (2 - a) == d[0] else slice(None)
+                                        for a in range(3))
+            assert np.all(Qo[sl] == bv[2 * d[0]][:, None, None, None])
