@@ -106,8 +106,8 @@ static int momentum0(const Variant& v) { return v.model == SINGLE_SPECIES ? 1 : 
 static bool valid_fill_modes(int dim, const hmr_patch_geometry* pg, const int* mode, int gh) {
     if (!mode) return false;
     for (int a = 0; a < dim; a++) {
-        if (mode[a] < HMR_FILL_ZERO_GRADIENT || mode[a] > HMR_FILL_DIRICHLET) return false;
-        if (mode[a] == HMR_FILL_REFLECT && pg->n[a] < gh) return false;
+        if (mode[a] < HMR_FILL_ZERO_GRADIENT || mode[a] > HMR_FILL_SYMMETRY) return false;
+        if ((mode[a] == HMR_FILL_REFLECT || mode[a] == HMR_FILL_SYMMETRY) && pg->n[a] < gh) return false;
     }
     return true;
 }
@@ -923,9 +923,10 @@ int hmr_level_bind_state(hmr_level* lv, int p, double* const* comps) {
 int hmr_level_set_periodic(hmr_level* lv, int p, const int* periodic) {
     if (!lv || p < 0 || p >= lv->npatch || !periodic) return HMR_ERR_ARGUMENT;
     for (int a = 0; a < 3; a++) {
-        if (a < lv->ctx->v.dim && (periodic[a] < HMR_FILL_ZERO_GRADIENT || periodic[a] > HMR_FILL_DIRICHLET))
+        if (a < lv->ctx->v.dim && (periodic[a] < HMR_FILL_ZERO_GRADIENT || periodic[a] > HMR_FILL_SYMMETRY))
             return HMR_ERR_ARGUMENT;
-        if (a < lv->ctx->v.dim && periodic[a] == HMR_FILL_REFLECT && lv->geoms[p].n[a] < lv->geoms[p].gh)
+        if (a < lv->ctx->v.dim && (periodic[a] == HMR_FILL_REFLECT || periodic[a] == HMR_FILL_SYMMETRY) &&
+            lv->geoms[p].n[a] < lv->geoms[p].gh)
             return HMR_ERR_ARGUMENT;
         lv->work[p].periodic[a] = a < lv->ctx->v.dim ? periodic[a] : 0;
     }
@@ -940,10 +941,11 @@ int hmr_level_set_layout(hmr_level* lv, const int* lo, const int* domain, const 
     int dom[3] = {1, 1, 1}, per[3] = {0, 0, 0};
     for (int a = 0; a < dim; a++) {
         if (domain[a] < 1 || (periodic[a] != 0 && periodic[a] != 1 && periodic[a] != HMR_FILL_REFLECT &&
-                              periodic[a] != HMR_FILL_DIRICHLET))
+                              periodic[a] != HMR_FILL_DIRICHLET && periodic[a] != HMR_FILL_SYMMETRY))
             return HMR_ERR_ARGUMENT;
         // the mirror images of a reflecting wall's ghost cells lie in the domain
-        if (periodic[a] == HMR_FILL_REFLECT && domain[a] < gh) return HMR_ERR_ARGUMENT;
+        if ((periodic[a] == HMR_FILL_REFLECT || periodic[a] == HMR_FILL_SYMMETRY) && domain[a] < gh)
+            return HMR_ERR_ARGUMENT;
         dom[a] = domain[a];
         per[a] = periodic[a];
     }

@@ -104,7 +104,7 @@ int launch_fill(int dim, const Geom& g, const Comp& Q, int ncomp, const int* per
 __device__ __forceinline__ int fill_src(int v, int n, int periodic) {
     if (v >= 0 && v < n) return v;
     if (periodic == 1) return ((v % n) + n) % n;
-    if (periodic == 3) return v < 0 ? -v - 1 : 2 * n - 1 - v;
+    if (periodic == 3 || periodic == 5) return v < 0 ? -v - 1 : 2 * n - 1 - v;
     return v < 0 ? 0 : n - 1;
 }
 
@@ -780,9 +780,9 @@ __global__ void __launch_bounds__(THREADS) level_domain_vjp_kernel(const LevelFi
             physical = true;
             if (D.per[a] == 4) {
                 dirichlet = true;   // a constant: its adjoint reaches no cell
-            } else if (D.per[a] == 3) {
+            } else if (D.per[a] == 3 || D.per[a] == 5) {
                 s[a] = (G < 0 ? -G - 1 : 2 * D.dom[a] - 1 - G) - w.lo[a];
-                flip[a] = mom0 + a;
+                if (D.per[a] == 3) flip[a] = mom0 + a;
             } else {
                 s[a] = G < 0 ? -w.lo[a] : D.dom[a] - 1 - w.lo[a];
             }

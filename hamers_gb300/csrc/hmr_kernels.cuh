@@ -505,7 +505,8 @@ __device__ __forceinline__ void update_item(const Geom& g, const Scratch& S, con
 // ---------------------------------------------------------------------------
 // Ghost fill of a single patch, per axis: mode 0 zero-gradient, 1 periodic,
 // 2 provided by the caller (left untouched: neighbour copies, coarse-fine
-// interpolation or analytic values), 3 reflecting wall, 4 Dirichlet (the
+// interpolation or analytic values), 3 reflecting wall, 5 symmetry plane (the
+// mirror image without a sign change), 4 Dirichlet (the
 // side's constant values bv[(2 axis + side) ncomp + e],
 // BasicCartesianBoundaryUtilities2.cpp:150-165).  A ghost cell beyond a
 // Dirichlet side takes that side's values -- beyond two Dirichlet sides, those
@@ -535,13 +536,16 @@ __device__ __forceinline__ void fill_item(const Geom& g, const Comp& Q, int ncom
                 if (dside < 0) dside = 2 * a + (c[a] >= 0);
             } else if (periodic[a] == 1) {
                 s[a] = ((c[a] % g.n[a]) + g.n[a]) % g.n[a];
-            } else if (periodic[a] == 3) {
+            } else if (periodic[a] == 3 || periodic[a] == 5) {
                 // reflecting wall: mirror image across the boundary face
-                // (BasicCartesianBoundaryUtilities2.cpp:349-440), normal momentum negated
+                // (BasicCartesianBoundaryUtilities2.cpp:349-440), normal momentum negated;
+                // symmetry plane (:397-440 for every variable): the mirror image as it is
                 s[a] = c[a] < 0 ? -c[a] - 1 : 2 * g.n[a] - 1 - c[a];
-                if (flip < 0) flip = mom0 + a;
-                else if (flip2 < 0) flip2 = mom0 + a;
-                else flip3 = mom0 + a;
+                if (periodic[a] == 3) {
+                    if (flip < 0) flip = mom0 + a;
+                    else if (flip2 < 0) flip2 = mom0 + a;
+                    else flip3 = mom0 + a;
+                }
             } else {
                 s[a] = c[a] < 0 ? 0 : g.n[a] - 1;
             }
@@ -586,12 +590,15 @@ __device__ __forceinline__ void domain_fill_item(const Geom& g, const Comp& Q, i
         physical = true;
         if (dom_periodic[a] == 4) {
             if (dside < 0) dside = 2 * a + (G >= 0);
-        } else if (dom_periodic[a] == 3) {
-            // reflecting wall: mirror image across the domain face, in the level's index space
+        } else if (dom_periodic[a] == 3 || dom_periodic[a] == 5) {
+            // reflecting wall or symmetry plane: mirror image across the domain face, in the
+            // level's index space (the normal momentum negated at a reflecting wall)
             s[a] = (G < 0 ? -G - 1 : 2 * dom[a] - 1 - G) - lo[a];
-            if (flip < 0) flip = mom0 + a;
-            else if (flip2 < 0) flip2 = mom0 + a;
-            else flip3 = mom0 + a;
+            if (dom_periodic[a] == 3) {
+                if (flip < 0) flip = mom0 + a;
+                else if (flip2 < 0) flip2 = mom0 + a;
+                else flip3 = mom0 + a;
+            }
         } else {
             s[a] = G < 0 ? -lo[a] : dom[a] - 1 - lo[a];
         }

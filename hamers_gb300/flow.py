@@ -52,7 +52,7 @@ _DIFFUSIVE = {
 RK3_ALPHA = [[1.0], [3.0 / 4.0, 1.0 / 4.0], [1.0 / 3.0, 0.0, 2.0 / 3.0]]
 
 # ghost-fill mode per axis (hmr_fill_mode of include/hmr.h)
-FILL_ZERO_GRADIENT, FILL_PERIODIC, FILL_PROVIDED, FILL_REFLECT, FILL_DIRICHLET = 0, 1, 2, 3, 4
+FILL_ZERO_GRADIENT, FILL_PERIODIC, FILL_PROVIDED, FILL_REFLECT, FILL_DIRICHLET, FILL_SYMMETRY = 0, 1, 2, 3, 4, 5
 RK3_BETA = [[1.0], [0.0, 1.0 / 4.0], [0.0, 0.0, 2.0 / 3.0]]
 RK3_GAMMA = [[1.0 / 6.0], [0.0, 1.0 / 6.0], [0.0, 0.0, 2.0 / 3.0]]
 
@@ -318,8 +318,9 @@ class Euler:
     def fillGhosts(self, patch, periodic, stream=None):
         """Ghost fill of one patch, mode per axis: FILL_ZERO_GRADIENT (0, the extrapolation
         boundary), FILL_PERIODIC (1), FILL_PROVIDED (2, left as supplied), FILL_REFLECT (3, a
-        slip wall: mirror image with the normal momentum negated; needs >= 4 cells on the axis)
-        or FILL_DIRICHLET (4, the values of ConvectiveFluxReconstructor.setDirichletValues)."""
+        slip wall: mirror image with the normal momentum negated; needs >= 4 cells on the axis),
+        FILL_DIRICHLET (4, the values of ConvectiveFluxReconstructor.setDirichletValues) or
+        FILL_SYMMETRY (5, the mirror image of every variable as it is)."""
         g = patch.geometry()
         q, _k = L.ptr_array(_state_ptrs(self.rec, patch.n, patch.data))
         per = (ctypes.c_int * 3)(*(list(periodic) + [0] * (3 - len(periodic))))

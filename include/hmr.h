@@ -209,13 +209,17 @@ typedef enum {
                                      (BasicCartesianBoundaryUtilities2.cpp:349-440 with the scalar/vector
                                      split of EulerBoundaryConditions.cpp:205-297); needs >= 4 cells along
                                      the axis */
-    HMR_FILL_DIRICHLET = 4        /* the reference's DIRICHLET condition (BasicCartesianBoundaryUtilities2.cpp:
+    HMR_FILL_DIRICHLET = 4,       /* the reference's DIRICHLET condition (BasicCartesianBoundaryUtilities2.cpp:
                                      150-165, values from EulerBoundaryConditions::
                                      readDirichletBoundaryDataEntry): every ghost cell beyond the side takes
                                      the side's conservative values (hmr_set_dirichlet_values); a corner
                                      beyond two Dirichlet sides takes the lower axis's, and one beyond a
                                      Dirichlet side and another condition the Dirichlet values -- the corner
                                      conditions XDIRICHLET / YDIRICHLET / ZDIRICHLET naming that axis */
+    HMR_FILL_SYMMETRY = 5         /* the reference's SYMMETRY condition as the master condition of every
+                                     variable (BasicCartesianBoundaryUtilities2.cpp:397-440): the mirror
+                                     image across the boundary face, no component negated; needs >= 4
+                                     cells along the axis */
 } hmr_fill_mode;
 
 /* Values of the HMR_FILL_DIRICHLET side `side` (0 low, 1 high) of axis `axis`: ncomp conservative
@@ -321,7 +325,8 @@ int hmr_level_destroy(hmr_level* level);
  * the domain covered by no patch of the level (a coarse-fine boundary) are left as the caller
  * provides them.  lo: 3 ints per patch (first interior cell), domain: cells per axis, periodic
  * per axis: 1 periodic, 0 zero-gradient faces, HMR_FILL_REFLECT reflecting walls,
- * HMR_FILL_DIRICHLET Dirichlet faces.  Boxes must lie in the domain and not overlap. */
+ * HMR_FILL_DIRICHLET Dirichlet faces, HMR_FILL_SYMMETRY symmetry planes.  Boxes must lie in the
+ * domain and not overlap. */
 int hmr_level_set_layout(hmr_level* level, const int* lo, const int* domain, const int* periodic);
 /* Binds the caller's ghost-box arrays (ncomp device pointers) as slot 0 of a patch. */
 int hmr_level_bind_state(hmr_level* level, int patch, double* const* comps);

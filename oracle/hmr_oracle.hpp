@@ -1806,7 +1806,8 @@ inline void refine_ghosts(const Config& c, const int* ratio, const int* fn, cons
 template <class T>
 void fill_ghosts(const Config& c, const int* n, const int* periodic, T* const* Q, const double* bvals = nullptr) {
     // Mode per axis: 0 FLOW (copy of the nearest interior cell), 1 periodic, 3 REFLECT (mirror
-    // image, normal momentum negated), 4 DIRICHLET: the side's values bvals[(2 axis + high) ncomp
+    // image, normal momentum negated), 5 SYMMETRY (mirror image of every variable as it is,
+    // BasicCartesianBoundaryUtilities2.cpp:397-440), 4 DIRICHLET: the side's values bvals[(2 axis + high) ncomp
     // + e] (BasicCartesianBoundaryUtilities2.cpp:150-165); a cell beyond two Dirichlet sides takes
     // the lower axis's values (the corner condition XDIRICHLET, :679-710), one beyond a Dirichlet
     // side and another condition the Dirichlet values.
@@ -1816,7 +1817,7 @@ void fill_ghosts(const Config& c, const int* n, const int* periodic, T* const* Q
     auto src = [&](int v, int a) {
         if (v >= 0 && v < b.n[a]) return v;
         if (periodic[a] == 1) return ((v % b.n[a]) + b.n[a]) % b.n[a];
-        if (periodic[a] == 3) return v < 0 ? -v - 1 : 2 * b.n[a] - 1 - v;
+        if (periodic[a] == 3 || periodic[a] == 5) return v < 0 ? -v - 1 : 2 * b.n[a] - 1 - v;
         return v < 0 ? 0 : b.n[a] - 1;
     };
     for (int e = 0; e < ncomp; e++)

@@ -305,7 +305,7 @@ def rk_stage(cfg, n, dx, alpha, beta, gamma, Q_int, F_int, S_int, F_acc=None, S_
 
 def fill_ghosts(cfg, n, periodic, Q, dirichlet=None):
     """Ghost fill, mode per axis: 0 zero-gradient, 1 periodic, 3 reflecting wall, 4 Dirichlet
-    (dirichlet: values per side, shape (2 dim, ncomp), row 2 axis + high)."""
+    (dirichlet: values per side, shape (2 dim, ncomp), row 2 axis + high), 5 symmetry plane."""
     assert Q.flags["C_CONTIGUOUS"] and Q.dtype == np.float64
     per = _ip(list(periodic) + [0] * (3 - len(periodic)))
     if dirichlet is None:
@@ -353,7 +353,7 @@ def _split_flux(cfg, n, flat):
 def ref_fill_boundaries(cfg, n, mode, Q, corner_axis=0, dirichlet=None):
     """The reference's physical-boundary fill (EulerBoundaryConditions with
     BasicCartesianBoundaryUtilities2/3) of one patch covering the domain, in place: mode per
-    axis 0 (FLOW), 3 (REFLECT) or 4 (DIRICHLET, values per side in dirichlet: shape
+    axis 0 (FLOW), 3 (REFLECT), 5 (SYMMETRY) or 4 (DIRICHLET, values per side in dirichlet: shape
     (2 dim, ncomp), row 2 axis + high); corner_axis picks the axis of the X/Y/Z-prefixed corner
     conditions (a corner with a Dirichlet side takes the lowest Dirichlet axis's)."""
     assert Q.flags["C_CONTIGUOUS"] and Q.dtype == np.float64 and Q.shape == ghost_shape(cfg, n)

@@ -17,7 +17,8 @@
 // Dirichlet side takes the condition naming the lowest such axis (XDIRICHLET before YDIRICHLET).
 //
 // Layout as hmro_fill_ghosts (oracle/hmr_oracle.cpp): ncomp arrays over the ghost box of width
-// 4, x fastest, filled in place.  mode per axis: 0 FLOW, 3 REFLECT (4 DIRICHLET with values).
+// 4, x fastest, filled in place.  mode per axis: 0 FLOW, 3 REFLECT, 5 SYMMETRY (every variable
+// mirrored as it is) (4 DIRICHLET with values).
 // Returns 0, or -1 with the reference's error text available from hmrref_last_error().
 #include "flow/flow_models/FlowModels.hpp"
 #include "util/basic_boundary_conditions/BasicBoundaryConditions.hpp"
@@ -53,6 +54,8 @@ int axis_cond(int axis, int mode) {
     static const int flow[3] = {XFLOW, YFLOW, ZFLOW};
     static const int refl[3] = {XREFLECT, YREFLECT, ZREFLECT};
     static const int diri[3] = {XDIRICHLET, YDIRICHLET, ZDIRICHLET};
+    static const int symm[3] = {XSYMMETRY, YSYMMETRY, ZSYMMETRY};
+    if (mode == 5) return symm[axis];
     return mode == 4 ? diri[axis] : (mode == 3 ? refl[axis] : flow[axis]);
 }
 
@@ -84,8 +87,8 @@ extern "C" int hmrref_fill_boundaries_bv(const hmrref_config* cfg_opaque, const 
         const tbox::Dimension dim((unsigned short)D);
         const int nsp = cfg->num_species;
         for (int a = 0; a < D; a++) {
-            if (mode[a] != 0 && mode[a] != 3 && mode[a] != 4)
-                throw std::runtime_error("boundary mode must be 0 (FLOW), 3 (REFLECT) or 4 (DIRICHLET)");
+            if (mode[a] != 0 && mode[a] != 3 && mode[a] != 4 && mode[a] != 5)
+                throw std::runtime_error("boundary mode must be 0 (FLOW), 3 (REFLECT), 4 (DIRICHLET) or 5 (SYMMETRY)");
             if (mode[a] == 4 && !bvals) throw std::runtime_error("DIRICHLET sides need values");
         }
 
@@ -149,7 +152,7 @@ extern "C" int hmrref_fill_boundaries_bv(const hmrref_config* cfg_opaque, const 
         const int nside = 2 * D;
         std::vector<int> side_conds(nside);
         for (int l = 0; l < nside; l++)
-            side_conds[l] = mode[l / 2] == 4 ? DIRICHLET : (mode[l / 2] == 3 ? REFLECT : FLOW);
+            side_conds[l] = mode[l / 2] == 5 ? SYMMETRY : (mode[l / 2] == 4 ? DIRICHLET : (mode[l / 2] == 3 ? REFLECT : FLOW));
         std::vector<int> edge_conds(D == 3 ? 12 : 4, FLOW), node_conds(D == 3 ? 8 : 4, FLOW);
         std::vector<int>& c2 = D == 2 ? node_conds : edge_conds;
         for (size_t i = 0; i < bb[2].size(); i++) c2[bb[2][i].getLocationIndex()] = corner_cond(outward[2][i], mode, corner_axis);

@@ -1,13 +1,14 @@
-"""Dirichlet boundaries on the device (HMR_FILL_DIRICHLET, the reference's DIRICHLET condition of
-BasicCartesianBoundaryUtilities2/3 with EulerBoundaryConditions' conservative boundary values).
+"""Dirichlet boundaries and symmetry planes on the device (HMR_FILL_DIRICHLET, the reference's
+DIRICHLET condition of BasicCartesianBoundaryUtilities2/3 with EulerBoundaryConditions'
+conservative boundary values; HMR_FILL_SYMMETRY, its SYMMETRY condition for every variable).
 
-* the single-patch ghost fill equals the oracle's bitwise (the oracle's Dirichlet fill is the
-  reference's own, tests/test_ref_oracle.py), Dirichlet sides mixed with zero-gradient, periodic
-  and reflecting axes, for every flow model in 2D and 3D;
+* the single-patch ghost fill equals the oracle's bitwise (the oracle's Dirichlet and symmetry
+  fills are the reference's own, tests/test_ref_oracle.py), Dirichlet sides mixed with
+  zero-gradient, periodic, reflecting and symmetry axes, for every flow model in 2D and 3D;
 * two SSPRK3 steps of one patch with Dirichlet sides equal the oracle's bitwise (exact form);
 * the adjoint of the fill passes the dot-product test <w, F v> = <F^T w, v> (F's linear part:
   Dirichlet ghost cells copy no cell);
-* a level tiled by uneven patches with Dirichlet domain faces, advanced by the batched substeps
+* a level tiled by uneven patches with Dirichlet (and symmetry) domain faces, advanced by the batched substeps
   with the device ghost exchange, equals the oracle's single patch covering the domain bitwise,
   its fill adjoint passes the dot-product test and its reverse sweep gives the one patch's
   adjoint;
@@ -22,8 +23,8 @@ from tests.test_gpu_level_adjoint import _box, _inner, _layout, _level
 from tests.test_gpu_parity import IDS, VARIANTS, make, ocfg
 from tests.test_ref_oracle import dirichlet_values
 
-PER_2D = ([4, 4], [4, 1], [3, 4], [0, 4])
-PER_3D = ([4, 4, 4], [4, 0, 1], [1, 3, 4])
+PER_2D = ([4, 4], [4, 1], [3, 4], [0, 4], [5, 4], [5, 1])
+PER_3D = ([4, 4, 4], [4, 0, 1], [1, 3, 4], [5, 4, 3])
 
 
 def _pers(dim):
@@ -102,7 +103,8 @@ def test_dirichlet_fill_vjp_dot_product(cuda, variant):
         assert abs(lhs - rhs) <= 1e-12 * float(np.sum(np.abs(w * Fv))), (per, lhs, rhs)
 
 
-LEVEL_CASES = [(1, (30, 26), (4, 1)), (5, (28, 24), (4, 4)), (3, (13, 12, 11), (1, 4, 3)), (9, (26, 22), (3, 4))]
+LEVEL_CASES = [(1, (30, 26), (4, 1)), (5, (28, 24), (4, 4)), (3, (13, 12, 11), (1, 4, 3)), (9, (26, 22), (3, 4)),
+               (4, (30, 24), (5, 4)), (2, (12, 13, 11), (5, 1, 5))]
 LEVEL_IDS = ["%s-%s" % (IDS[i], "".join(map(str, per))) for i, _, per in LEVEL_CASES]
 
 

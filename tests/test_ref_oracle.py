@@ -154,9 +154,10 @@ def test_oracle_wider_ghost_box_changes_nothing_else():
 # Physical boundaries: the reference's EulerBoundaryConditions split (SCALAR variables SYMMETRY,
 # the momentum REFLECT, at REFLECT walls) over its BasicCartesianBoundaryUtilities2 / 3
 # (src/util/basic_boundary_conditions/), compiled into the same library, on a patch covering
-# the domain with FLOW or REFLECT on every side.
+# the domain with FLOW, REFLECT or SYMMETRY (mode 5, every variable) on every side.
 # ---------------------------------------------------------------------------
-BC_MODES = {2: ([3, 3], [0, 0], [3, 0], [0, 3]), 3: ([3, 3, 3], [0, 0, 0], [3, 0, 3], [0, 3, 0], [3, 3, 0])}
+BC_MODES = {2: ([3, 3], [0, 0], [3, 0], [0, 3], [5, 5], [5, 3], [0, 5]),
+            3: ([3, 3, 3], [0, 0, 0], [3, 0, 3], [0, 3, 0], [3, 3, 0], [5, 5, 5], [5, 3, 0], [0, 5, 3])}
 
 
 @pytest.mark.parametrize("model,mn,gam,R", MODELS, ids=[m[1] for m in MODELS])
@@ -177,8 +178,8 @@ def test_oracle_ghost_fill_is_bitwise_the_reference(model, mn, gam, R, dim):
 
 # DIRICHLET sides (BasicCartesianBoundaryUtilities2.cpp:150-165 and the X/Y/Z-prefixed corner
 # conditions, :679-710) with per-side conservative values, alone and beside FLOW and REFLECT.
-DIRICHLET_MODES = {2: ([4, 4], [4, 0], [0, 4], [3, 4], [4, 3]),
-                   3: ([4, 4, 4], [4, 0, 3], [0, 4, 0], [3, 3, 4], [0, 3, 4])}
+DIRICHLET_MODES = {2: ([4, 4], [4, 0], [0, 4], [3, 4], [4, 3], [5, 4]),
+                   3: ([4, 4, 4], [4, 0, 3], [0, 4, 0], [3, 3, 4], [0, 3, 4], [4, 5, 3])}
 
 
 def dirichlet_values(Q, dim, seed):
