@@ -125,10 +125,17 @@ static bool valid_geom(int dim, const hmr_patch_geometry* pg) {
 
 // Scratch size in doubles for one patch (cell data, midpoint fluxes and
 // velocities, and the queue of faces handed to the exact form).
+static long total_faces_of(int dim, const Geom& g) {
+    long t = 0;
+    for (int a = 0; a < dim; a++) t += nface_of(g, a);
+    return t;
+}
+
 static size_t scratch_doubles(const hmr_ctx* c, const Geom& g) {
     const long nc = ncell_of(g);
     size_t s = (size_t)(c->neq + 4) * nc;
     for (int a = 0; a < c->v.dim; a++) s += (size_t)(c->neq + 2) * nface_of(g, a);
+    s += (size_t)total_faces_of(c->v.dim, g);   // the fast form's lists of sorted faces
     if (c->P.dorder) {
         // NavierStokes: temperature, node velocity gradient, midpoint diffusive fluxes
         s += (size_t)(1 + c->v.dim * c->v.dim) * nc;
@@ -163,6 +170,7 @@ static Scratch carve_scratch(const hmr_ctx* c, const Geom& g, double* base) {
         }
     }
     p += total_faces(c, g);   // queue of faces for the exact pass (face_launch)
+    p += total_faces(c, g);   // the fast form's per-axis lists of HLLC faces (face_launch)
     S.Td = S.Gd = nullptr;
     for (int a = 0; a < 3; a++) S.Fd[a] = nullptr;
     if (c->P.dorder) {
@@ -191,6 +199,14 @@ static int face_launch(hmr_ctx* c, const Geom& g, const Scratch& S, cudaStream_t
     R.list = reinterpret_cast<unsigned long long*>(S.um[c->v.dim - 1] + nface_of(g, c->v.dim - 1));
     R.count = c->redo_count;
     R.cap = (unsigned long long)total_faces(c, g);
+    // Sorted faces (the fast form's HLLC faces beside the exact HLLC-HLL ones in one launch) pay on
+    // patches too small to fill the GPU with either set alone (256^2: 1.51e8 -> 1.67e8 cell-updates
+    // per second); on larger ones each set fills it and the sorting pass is a small extra cost.
+    if (total_faces(c, g) <= (1L << 20)) {
+        R.fast = R.list + total_faces(c, g);
+        R.fast_count = c->redo_count + 1;
+        for (int a = 1; a < c->v.dim; a++) R.fast_off[a] = R.fast_off[a - 1] + nface_of(g, a - 1);
+    }
     if (c->precision == HMR_PRECISION_EXACT) return hmr_exact::launch_faces(c->v, c->P, g, S, c->counters, R, st);
     return hmr_fast::launch_faces(c->v, c->P, g, S, c->counters, R, st);
 }
@@ -297,7 +313,8 @@ int hmr_ctx_create(const hmr_config* cfg, hmr_ctx** out) {
     c->ncomp = ncomp;
     cudaError_t e = cudaMalloc(&c->counters, sizeof(Counters));
     if (e == cudaSuccess) e = cudaMemset(c->counters, 0, sizeof(Counters));
-    if (e == cudaSuccess) e = cudaMalloc(&c->redo_count, sizeof(unsigned int));
+    // the queue's length, the three lists' lengths and the number of HLLC-HLL faces sorted
+    if (e == cudaSuccess) e = cudaMalloc(&c->redo_count, 5 * sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMalloc(&c->d_bvals, sizeof(c->h_bvals));
     if (e == cudaSuccess) e = cudaMemset(c->d_bvals, 0, sizeof(c->h_bvals));
     if (e != cudaSuccess) {

@@ -70,12 +70,102 @@ faces_kernel(Params P, Geom g, Scratch S, Counters* cnt, Redo R) {
     }
 }
 
+// Fast form with sorted faces: every face of axis A is classified by its sensor; the
+// HLLC-HLL ones go to the exact pass's queue, the others to the axis's list, both appended a
+// warp at a time (one atomic per warp and list), so a list holds runs of neighbouring faces.
+template <int DIM, int A>
+__global__ void __launch_bounds__(FACE_THREADS) classify_kernel(Geom g, Scratch S, Redo R) {
+    const long nf = nface_of(g, A);
+    const int e0 = g.n[0] + (A == 0 ? 3 : 0);
+    const int e1 = g.n[1] + (A == 1 ? 3 : 0);
+    const long st = (A == 0) ? 1 : (A == 1 ? (long)g.G[0] : (long)g.G[0] * g.G[1]);
+    unsigned long long* list = R.fast + R.fast_off[A];
+    const unsigned lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    // blockDim.x is a multiple of 32 and every thread runs the same iterations: the warp
+    // votes below see all 32 lanes
+    for (long t0 = (long)blockIdx.x * blockDim.x; t0 < nf; t0 += (long)gridDim.x * blockDim.x) {
+        const long t = t0 + threadIdx.x;
+        const bool valid = t < nf;
+        bool hll = false;
+        if (valid) {
+            const int i = (int)(t % e0) - (A == 0);
+            const int j = (int)((t / e0) % e1) - (A == 1);
+            const int k = DIM == 3 ? (int)(t / ((long)e0 * e1)) - (A == 2) : 0;
+            const long xR = cidx<DIM>(g, i, j, k);
+            hll = face_uses_hll(S, xR - st, xR);
+        }
+        const unsigned fm = __ballot_sync(0xffffffffu, valid && !hll);
+        const unsigned hm = __ballot_sync(0xffffffffu, valid && hll);
+        unsigned bf = 0, bh = 0;
+        if (lane == 0) {
+            if (fm) bf = atomicAdd(R.fast_count + A, (unsigned)__popc(fm));
+            if (hm) {
+                bh = atomicAdd(R.count, (unsigned)__popc(hm));
+                atomicAdd(R.fast_count + 3, (unsigned)__popc(hm));
+            }
+        }
+        bf = __shfl_sync(0xffffffffu, bf, 0);
+        bh = __shfl_sync(0xffffffffu, bh, 0);
+        if (valid && !hll) list[bf + __popc(fm & below)] = (unsigned long long)t;
+        if (valid && hll) {
+            const unsigned long long idx = bh + __popc(hm & below);
+            if (idx < R.cap) R.list[idx] = ((unsigned long long)A << 56) | (unsigned long long)t;
+        }
+    }
+}
+
+// The exact form of one queued face, kept out of line: inlined beside the fast form, the shared
+// subexpressions of the two would be merged and the fast form's multiply-add contraction (decided
+// per kernel) could change, and with it its last bits against the other kernels that run it.
+template <int DIM, int MODEL, int NSP, int SCHEME>
+__device__ __noinline__ void exact_queued_face(const Params& P, const Geom& g, const Scratch& S, Counters* cnt,
+                                               unsigned long long v) {
+    const int a = (int)(v >> 56);
+    const long t = (long)(v & ((1ull << 56) - 1));
+    if (a == 0) face_item<true, DIM, MODEL, NSP, SCHEME, 0>(P, g, S, t, cnt);
+    else if (a == 1) face_item<true, DIM, MODEL, NSP, SCHEME, 1>(P, g, S, t, cnt);
+    else if constexpr (DIM == 3) face_item<true, DIM, MODEL, NSP, SCHEME, 2>(P, g, S, t, cnt);
+}
+
+// One launch over the sorted faces: the HLLC faces of every axis in the fast form (listed by
+// classify_kernel), then the HLLC-HLL ones in the exact form (the first fast_count[3] entries
+// of the queue).  The two sets are disjoint and each face writes its own flux, so they run side
+// by side; faces the fast form hands back (first-order fallback, near a bounds threshold) are
+// queued behind the HLLC-HLL ones for redo_kernel.
+template <int DIM, int MODEL, int NSP, int SCHEME>
+__global__ void __launch_bounds__(FACE_THREADS)
+faces_sorted_kernel(Params P, Geom g, Scratch S, Counters* cnt, Redo R) {
+    const long n0 = (long)R.fast_count[0];
+    const long n01 = n0 + (long)R.fast_count[1];
+    const long nf = n01 + (DIM == 3 ? (long)R.fast_count[2] : 0);
+    const long total = nf + (long)min((unsigned long long)R.fast_count[3], R.cap);
+    for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < total; r += (long)gridDim.x * blockDim.x) {
+        if (r < n0) {
+            const long t = (long)R.fast[R.fast_off[0] + r];
+            if (face_item<false, DIM, MODEL, NSP, SCHEME, 0>(P, g, S, t, cnt)) redo_push(R, 0, t);
+        } else if (r < n01) {
+            const long t = (long)R.fast[R.fast_off[1] + (r - n0)];
+            if (face_item<false, DIM, MODEL, NSP, SCHEME, 1>(P, g, S, t, cnt)) redo_push(R, 1, t);
+        } else if (r < nf) {
+            if constexpr (DIM == 3) {
+                const long t = (long)R.fast[R.fast_off[2] + (r - n01)];
+                if (face_item<false, DIM, MODEL, NSP, SCHEME, 2>(P, g, S, t, cnt)) redo_push(R, 2, t);
+            }
+        } else {
+            exact_queued_face<DIM, MODEL, NSP, SCHEME>(P, g, S, cnt, R.list[r - nf]);
+        }
+    }
+}
+
 // Exact recomputation of the queued faces of one patch.
 template <int DIM, int MODEL, int NSP, int SCHEME>
 __global__ void __launch_bounds__(FACE_THREADS)
-redo_kernel(Params P, Geom g, Scratch S, Counters* cnt, Redo R) {
+redo_kernel(Params P, Geom g, Scratch S, Counters* cnt, Redo R, int after_sorted) {
     const unsigned long long n = min((unsigned long long)*R.count, R.cap);
-    for (unsigned long long r = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; r < n;
+    // after faces_sorted_kernel the HLLC-HLL entries at the head of the queue are done
+    const unsigned long long r0 = after_sorted ? (unsigned long long)R.fast_count[3] : 0ull;
+    for (unsigned long long r = r0 + (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; r < n;
          r += (unsigned long long)gridDim.x * blockDim.x) {
         const unsigned long long v = R.list[r];
         const int a = (int)(v >> 56);
@@ -105,22 +195,39 @@ int launch_faces(const Variant& v, const Params& P, const Geom& g, const Scratch
                  const Redo& R, cudaStream_t st) {
     return dispatch(v, [&](auto t) {
         using T = decltype(t);
+        const bool sorted = HMR_FAST && R.fast != nullptr && R.fast_count != nullptr;
         if (HMR_FAST) {
             cudaError_t e = cudaMemsetAsync(R.count, 0, sizeof(unsigned int), st);
+            if (e == cudaSuccess && sorted) e = cudaMemsetAsync(R.fast_count, 0, 4 * sizeof(unsigned int), st);
             if (e != cudaSuccess) return (int)e;
         }
-        faces_kernel<T::DIM, T::MODEL, T::NSP, T::SCHEME, 0>
-            <<<grid_for(nface_of(g, 0), FACE_THREADS), FACE_THREADS, 0, st>>>(P, g, S, cnt, R);
-        faces_kernel<T::DIM, T::MODEL, T::NSP, T::SCHEME, 1>
-            <<<grid_for(nface_of(g, 1), FACE_THREADS), FACE_THREADS, 0, st>>>(P, g, S, cnt, R);
-        if constexpr (T::DIM == 3)
-            faces_kernel<T::DIM, T::MODEL, T::NSP, T::SCHEME, 2>
-                <<<grid_for(nface_of(g, 2), FACE_THREADS), FACE_THREADS, 0, st>>>(P, g, S, cnt, R);
+        if constexpr (HMR_FAST != 0) {
+            if (sorted) {
+                classify_kernel<T::DIM, 0><<<grid_for(nface_of(g, 0), FACE_THREADS), FACE_THREADS, 0, st>>>(g, S, R);
+                classify_kernel<T::DIM, 1><<<grid_for(nface_of(g, 1), FACE_THREADS), FACE_THREADS, 0, st>>>(g, S, R);
+                if constexpr (T::DIM == 3)
+                    classify_kernel<T::DIM, 2><<<grid_for(nface_of(g, 2), FACE_THREADS), FACE_THREADS, 0, st>>>(g, S, R);
+                long nall = 0;
+                for (int a = 0; a < T::DIM; a++) nall += nface_of(g, a);
+                faces_sorted_kernel<T::DIM, T::MODEL, T::NSP, T::SCHEME>
+                    <<<grid_for(nall, FACE_THREADS), FACE_THREADS, 0, st>>>(P, g, S, cnt, R);
+            }
+        }
+        if (!sorted) {
+            faces_kernel<T::DIM, T::MODEL, T::NSP, T::SCHEME, 0>
+                <<<grid_for(nface_of(g, 0), FACE_THREADS), FACE_THREADS, 0, st>>>(P, g, S, cnt, R);
+            faces_kernel<T::DIM, T::MODEL, T::NSP, T::SCHEME, 1>
+                <<<grid_for(nface_of(g, 1), FACE_THREADS), FACE_THREADS, 0, st>>>(P, g, S, cnt, R);
+            if constexpr (T::DIM == 3)
+                faces_kernel<T::DIM, T::MODEL, T::NSP, T::SCHEME, 2>
+                    <<<grid_for(nface_of(g, 2), FACE_THREADS), FACE_THREADS, 0, st>>>(P, g, S, cnt, R);
+        }
         if (HMR_FAST) {
             int dev = 0, sms = 1;
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-            redo_kernel<T::DIM, T::MODEL, T::NSP, T::SCHEME><<<sms * 2, FACE_THREADS, 0, st>>>(P, g, S, cnt, R);
+            redo_kernel<T::DIM, T::MODEL, T::NSP, T::SCHEME><<<sms * 2, FACE_THREADS, 0, st>>>(P, g, S, cnt, R,
+                                                                                            sorted ? 1 : 0);
         }
         return (int)cudaPeekAtLastError();
     });

@@ -201,6 +201,15 @@ __device__ __forceinline__ bool face_eval(const Params& P, const FaceProj<DIM, M
     return ok;
 }
 
+// Ducros-like sensor of the face between cells xL and xR (WCNS56-HLLC-HLL.cpp:1066-1088),
+// from the exact cell dilatation and vorticity: true where the face takes HLLC-HLL.
+__device__ __forceinline__ bool face_uses_hll(const Scratch& S, long xL, long xR) {
+    const double theta_avg = 0.5*(S.theta[xL] + S.theta[xR]);
+    const double Omega_avg = 0.5*(S.Omega[xL] + S.Omega[xR]);
+    const double s = -theta_avg/(fabs(theta_avg) + Omega_avg + HMR_EPS);
+    return s > 0.65;
+}
+
 // ---------------------------------------------------------------------------
 // Phase 3: one midpoint face normal to axis A.  item over faces(A).
 //
@@ -228,11 +237,7 @@ __device__ __forceinline__ bool face_item(const Params& P, const Geom& g, const 
     const long xR = cidx<DIM>(g, i, j, k);      // cell on the + side of the face
     const long xL = xR - st;
 
-    // Ducros-like sensor (WCNS56-HLLC-HLL.cpp:1066-1088); exact inputs.
-    const double theta_avg = 0.5*(S.theta[xL] + S.theta[xR]);
-    const double Omega_avg = 0.5*(S.Omega[xL] + S.Omega[xR]);
-    const double s = -theta_avg/(fabs(theta_avg) + Omega_avg + HMR_EPS);
-    const bool use_hll = s > 0.65;
+    const bool use_hll = face_uses_hll(S, xL, xR);
     if (!X && use_hll) return true;
 
     // Projection means (SIMPLE averaging).
@@ -288,6 +293,13 @@ struct Redo {
     unsigned long long* list;
     unsigned int* count;
     unsigned long long cap;
+    // Optional (per-patch fast form): faces sorted before the fast pass -- the HLLC ones into
+    // per-axis lists (axis a at fast + fast_off[a], fast_count[a] entries), the HLLC-HLL ones
+    // (fast_count[3] of them) to the head of the queue above -- so that the fast pass runs full
+    // warps beside the exact pass over the HLLC-HLL faces.
+    unsigned long long* fast = nullptr;
+    unsigned int* fast_count = nullptr;
+    long fast_off[3] = {0, 0, 0};
 };
 
 __device__ __forceinline__ void redo_push(const Redo& R, int axis, long item) {
