@@ -286,7 +286,8 @@ def uneven_batched_vs_patch(args, flow):
             "batched_over_per_patch": t_patch / t_batched,
             "batched_ms_per_step": t_batched, "per_patch_ms_per_step": t_patch,
             "launch_shape": {"threads": tuned[0], "blocks_per_sm": tuned[1]},
-            "work_split": {"chunk_blocks": split[0], "cell_phases": "grid-stride" if split[1] else "chunks"},
+            "work_split": {"chunk_blocks": split[0], "cell_phases": "grid-stride" if split[1] & 1 else "chunks",
+                           "faces": "sorted" if split[1] & 2 else "in order"},
             "batched_roofline": roofline_fracs(cu / (t_batched * 1e-3), ALG_FP64_OPS_C3, alg_bytes(5),
                                                args.fp64_peak, args.hbm_peak),
             "per_patch_roofline": roofline_fracs(cu / (t_patch * 1e-3), ALG_FP64_OPS_C3, alg_bytes(5),
@@ -478,7 +479,8 @@ def c5_level_and_adjoint(args, flow, base=128, reps=3):
             "per_patch_substep_ms": t_patch, "per_patch_cell_updates_per_s": cells / (t_patch * 1e-3),
             "batched_over_per_patch": t_patch / t_batched,
             "launch_shape": {"threads": tuned[0], "blocks_per_sm": tuned[1]},
-            "work_split": {"chunk_blocks": split[0], "cell_phases": "grid-stride" if split[1] else "chunks"},
+            "work_split": {"chunk_blocks": split[0], "cell_phases": "grid-stride" if split[1] & 1 else "chunks",
+                           "faces": "sorted" if split[1] & 2 else "in order"},
             "batched_roofline": roofline_fracs(cells / (t_batched * 1e-3), ALG_FP64_OPS_C5, alg_bytes(7, (0,)),
                                                args.fp64_peak, args.hbm_peak),
             "per_patch_roofline": roofline_fracs(cells / (t_patch * 1e-3), ALG_FP64_OPS_C5, alg_bytes(7, (0,)),
@@ -658,6 +660,7 @@ def c1_per_patch(args, flow, N=256, steps=20):
     lv.bind(0, Qb)
     lv.set_periodic(0, [1, 1])
     lv.autotune(dt)
+    split_b = lv.work_split()
     for _ in range(3):
         lv.step(dt)
     torch.cuda.synchronize()
@@ -678,6 +681,9 @@ def c1_per_patch(args, flow, N=256, steps=20):
             "roofline": roofline_fracs(rate, ALG_FP64_OPS_C1, alg_bytes(4), args.fp64_peak, args.hbm_peak),
             "batched": {"form": "one-patch level, one persistent kernel per substep in a CUDA graph",
                         "ms_per_step": ms_b, "cell_updates_per_s": rate_b,
+                        "work_split": {"chunk_blocks": split_b[0],
+                                       "cell_phases": "grid-stride" if split_b[1] & 1 else "chunks",
+                                       "faces": "sorted" if split_b[1] & 2 else "in order"},
                         "roofline": roofline_fracs(rate_b, ALG_FP64_OPS_C1, alg_bytes(4), args.fp64_peak,
                                                    args.hbm_peak)},
             "l2": "working set 2.4 MB fits in L2: HBM fraction is an upper bound on DRAM use"}
@@ -909,8 +915,9 @@ def main():
                           else "per-patch kernels (fill, cells, sensor, faces x/y, update) per substep"),
                  "precision": args.precision,
                  "launch_shape": {"threads": tuned[0], "blocks_per_sm": tuned[1]},
-                 "work_split": None if split is None else {"chunk_blocks": split[0],
-                                                           "cell_phases": "grid-stride" if split[1] else "chunks"}},
+                 "work_split": None if split is None else {
+                     "chunk_blocks": split[0], "cell_phases": "grid-stride" if split[1] & 1 else "chunks",
+                     "faces": "sorted" if split[1] & 2 else "in order"}},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": state_bytes,
                 "d2h_bytes_per_step": state_bytes,
                 "note": "every step copies the host state in from pinned memory, advances it and copies the "

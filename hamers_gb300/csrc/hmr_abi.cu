@@ -30,7 +30,8 @@ struct hmr_ctx {
     double h_bvals[6 * MAX_COMP] = {};  // and their host copy
 };
 
-constexpr int LEVEL_COUNTERS = 9;   // barrier arrivals, redo-queue length, seven phase-chunk counters
+// barrier arrivals, redo-queue length, eight phase-chunk counters, four sorted-face counts
+constexpr int LEVEL_COUNTERS = 14;
 
 struct hmr_level {
     hmr_ctx* ctx;
@@ -45,6 +46,7 @@ struct hmr_level {
     unsigned int* d_barrier = nullptr;   // [0] barrier arrivals, [1] redo-queue length, [2..8] phase chunks
     int* d_status = nullptr;
     unsigned long long* d_redo = nullptr;
+    unsigned long long* d_sorted = nullptr;   // per-axis lists of sorted faces (redo_cap entries)
     long redo_cap = 0;
     int threads = 128;
     int blocks = 0;
@@ -739,6 +741,10 @@ static LevelArgs stage_args(hmr_level* lv, int stage, double dt) {
     L.redo.count = lv->d_barrier + 1;
     L.chunk = lv->d_barrier + 2;
     L.redo.cap = (unsigned long long)lv->redo_cap;
+    L.sorted = lv->d_sorted;
+    L.sort_count = lv->d_barrier + 10;
+    L.sort_off[0] = 0;
+    for (int a = 1; a < 3; a++) L.sort_off[a] = L.sort_off[a - 1] + L.total_face[a - 1];
     return L;
 }
 
@@ -858,6 +864,7 @@ int hmr_level_create(hmr_ctx* c, int np, const hmr_patch_geometry* geoms, hmr_le
     }
     cudaError_t e = cudaMalloc(&lv->d_state, state_tot * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&lv->d_redo, (size_t)lv->redo_cap * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc(&lv->d_sorted, (size_t)lv->redo_cap * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMemset(lv->d_state, 0, state_tot * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&lv->d_scratch, scratch_tot * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&lv->d_work, (size_t)3 * np * sizeof(PatchWork));
@@ -917,6 +924,7 @@ int hmr_level_destroy(hmr_level* lv) {
     if (lv->d_barrier) cudaFree(lv->d_barrier);
     if (lv->d_status) cudaFree(lv->d_status);
     if (lv->d_redo) cudaFree(lv->d_redo);
+    if (lv->d_sorted) cudaFree(lv->d_sorted);
     if (lv->d_srmax) cudaFree(lv->d_srmax);
     if (lv->d_copies) cudaFree(lv->d_copies);
     if (lv->d_dt) cudaFree(lv->d_dt);
@@ -1352,7 +1360,7 @@ int hmr_level_set_launch(hmr_level* lv, int threads, int blocks_per_sm) {
 }
 
 int hmr_level_set_work_split(hmr_level* lv, int chunk_blocks, int mode) {
-    if (!lv || (chunk_blocks != 1 && chunk_blocks != 2 && chunk_blocks != 4) || mode < 0 || mode > 1)
+    if (!lv || (chunk_blocks != 1 && chunk_blocks != 2 && chunk_blocks != 4) || mode < 0 || mode > 3)
         return HMR_ERR_ARGUMENT;
     if (chunk_blocks != lv->L.chunk_mult || mode != lv->L.split_mode) level_drop_graphs(lv);
     lv->L.chunk_mult = chunk_blocks;
@@ -1427,6 +1435,20 @@ int hmr_level_autotune(hmr_level* lv, double dt, int* threads_out, int* bpsm_out
             best = ms;
             best_m = splits[k][0];
             best_s = splits[k][1];
+        }
+    }
+    // and, in the fast form, the faces sorted by their sensor first (split_mode bit 1)
+    if (lv->ctx->precision == HMR_PRECISION_FAST) {
+        lv->L.chunk_mult = best_m;
+        lv->L.split_mode = best_s | 2;
+        if (level_enqueue(lv, 0, dt, best_t, best_b, st) == HMR_OK) {
+            cudaEventRecord(e0, st);
+            for (int rep = 0; rep < 2; rep++) level_enqueue(lv, 0, dt, best_t, best_b, st);
+            cudaEventRecord(e1, st);
+            float ms = 0.f;
+            if (cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess &&
+                ms < best)
+                best_s |= 2;
         }
     }
     lv->L.chunk_mult = best_m;

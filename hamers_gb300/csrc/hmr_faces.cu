@@ -328,7 +328,7 @@ __device__ __forceinline__ void level_chunks(unsigned int* counter, long total, 
 // work-splitting mode -- by a fixed grid-stride assignment.
 template <class F>
 __device__ __forceinline__ void level_cell_items(unsigned int* counter, long total, const LevelArgs& L, F f) {
-    if (L.split_mode == 1) {
+    if (L.split_mode & 1) {
         const long stride = (long)gridDim.x * blockDim.x;
         for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) f(t);
     } else {
@@ -337,7 +337,70 @@ __device__ __forceinline__ void level_cell_items(unsigned int* counter, long tot
 }
 
 // Chunk counters of LevelArgs::chunk.
-enum { CHUNK_FACE0 = 0, CHUNK_CELLS = 3, CHUNK_SENSOR = 4, CHUNK_UPDATE = 5, CHUNK_REDO = 6 };
+enum { CHUNK_FACE0 = 0, CHUNK_CELLS = 3, CHUNK_SENSOR = 4, CHUNK_UPDATE = 5, CHUNK_REDO = 6, CHUNK_SORTED = 7 };
+
+// The level's sorting of the faces of axis A (as classify_kernel, over the level's face items):
+// HLLC faces to the axis's list, HLLC-HLL faces to the head of the redo queue.  Every thread
+// of the grid runs the same iterations (the warp votes see all 32 lanes).
+template <int DIM, int A>
+__device__ __forceinline__ void level_classify(const LevelArgs& L, const PatchWork* W, int np) {
+    const long total = L.total_face[A];
+    unsigned long long* list = L.sorted + L.sort_off[A];
+    const unsigned lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    for (long t0 = (long)blockIdx.x * blockDim.x; t0 < total; t0 += (long)gridDim.x * blockDim.x) {
+        const long t = t0 + threadIdx.x;
+        const bool valid = t < total;
+        bool hll = false;
+        if (valid) {
+            const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_face[A]; });
+            const Geom& g = W[p].g;
+            const long u = t - W[p].off_face[A];
+            const int e0 = g.n[0] + (A == 0 ? 3 : 0);
+            const int e1 = g.n[1] + (A == 1 ? 3 : 0);
+            const int i = (int)(u % e0) - (A == 0);
+            const int j = (int)((u / e0) % e1) - (A == 1);
+            const int k = DIM == 3 ? (int)(u / ((long)e0 * e1)) - (A == 2) : 0;
+            const long st = (A == 0) ? 1 : (A == 1 ? (long)g.G[0] : (long)g.G[0] * g.G[1]);
+            const long xR = cidx<DIM>(g, i, j, k);
+            hll = face_uses_hll(W[p].S, xR - st, xR);
+        }
+        const unsigned fm = __ballot_sync(0xffffffffu, valid && !hll);
+        const unsigned hm = __ballot_sync(0xffffffffu, valid && hll);
+        unsigned bf = 0, bh = 0;
+        if (lane == 0) {
+            if (fm) bf = atomicAdd(L.sort_count + A, (unsigned)__popc(fm));
+            if (hm) {
+                bh = atomicAdd(L.redo.count, (unsigned)__popc(hm));
+                atomicAdd(L.sort_count + 3, (unsigned)__popc(hm));
+            }
+        }
+        bf = __shfl_sync(0xffffffffu, bf, 0);
+        bh = __shfl_sync(0xffffffffu, bh, 0);
+        if (valid && !hll) list[bf + __popc(fm & below)] = (unsigned long long)t;
+        if (valid && hll) {
+            const unsigned long long idx = bh + __popc(hm & below);
+            if (idx < L.redo.cap) L.redo.list[idx] = ((unsigned long long)A << 56) | (unsigned long long)t;
+        }
+    }
+}
+
+// The exact form of one queued level face, out of line (see exact_queued_face).
+template <int DIM, int MODEL, int NSP, int SCHEME>
+__device__ __noinline__ void level_exact_face(const Params& P, const PatchWork* W, int np, unsigned long long v) {
+    const int a = (int)(v >> 56);
+    const long t = (long)(v & ((1ull << 56) - 1));
+    if (a == 0) {
+        const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_face[0]; });
+        face_item<true, DIM, MODEL, NSP, SCHEME, 0>(P, W[p].g, W[p].S, t - W[p].off_face[0], nullptr);
+    } else if (a == 1) {
+        const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_face[1]; });
+        face_item<true, DIM, MODEL, NSP, SCHEME, 1>(P, W[p].g, W[p].S, t - W[p].off_face[1], nullptr);
+    } else if constexpr (DIM == 3) {
+        const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_face[2]; });
+        face_item<true, DIM, MODEL, NSP, SCHEME, 2>(P, W[p].g, W[p].S, t - W[p].off_face[2], nullptr);
+    }
+}
 
 // 128 threads per block at most, with registers for three such blocks per SM (at most 170 per
 // thread) in the fast form, as the per-patch face kernels use; the exact form's face item, the
@@ -438,6 +501,46 @@ level_kernel(Params P, LevelArgs L) {
         }
     }
     constexpr bool X = !HMR_FAST;
+    unsigned long long redo_from = 0;   // queue entries before this one were done beside the fast form
+    (void)redo_from;
+#if HMR_FAST
+    if (L.split_mode & 2) {
+        // faces sorted by their sensor, then the HLLC ones in the fast form beside the
+        // HLLC-HLL ones in the exact form (as faces_sorted_kernel)
+        level_classify<DIM, 0>(L, W, np);
+        level_classify<DIM, 1>(L, W, np);
+        if constexpr (DIM == 3) level_classify<DIM, 2>(L, W, np);
+        HMR_BARRIER();
+        const volatile unsigned int* sc = L.sort_count;
+        const long n0 = (long)sc[0];
+        const long n01 = n0 + (long)sc[1];
+        const long nf = n01 + (DIM == 3 ? (long)sc[2] : 0);
+        redo_from = min((unsigned long long)sc[3], L.redo.cap);
+        level_chunks(L.chunk + CHUNK_SORTED, nf + (long)redo_from, L.chunk_mult, [&](long r) {
+            if (r < n0) {
+                const long t = (long)L.sorted[L.sort_off[0] + r];
+                const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_face[0]; });
+                if (face_item<false, DIM, MODEL, NSP, SCHEME, 0>(P, W[p].g, W[p].S, t - W[p].off_face[0], nullptr))
+                    redo_push(L.redo, 0, t);
+            } else if (r < n01) {
+                const long t = (long)L.sorted[L.sort_off[1] + (r - n0)];
+                const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_face[1]; });
+                if (face_item<false, DIM, MODEL, NSP, SCHEME, 1>(P, W[p].g, W[p].S, t - W[p].off_face[1], nullptr))
+                    redo_push(L.redo, 1, t);
+            } else if (r < nf) {
+                if constexpr (DIM == 3) {
+                    const long t = (long)L.sorted[L.sort_off[2] + (r - n01)];
+                    const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_face[2]; });
+                    if (face_item<false, DIM, MODEL, NSP, SCHEME, 2>(P, W[p].g, W[p].S, t - W[p].off_face[2], nullptr))
+                        redo_push(L.redo, 2, t);
+                }
+            } else {
+                level_exact_face<DIM, MODEL, NSP, SCHEME>(P, W, np, L.redo.list[r - nf]);
+            }
+        });
+    } else
+#endif
+    {
     level_chunks(L.chunk + CHUNK_FACE0, L.total_face[0], L.chunk_mult, [&](long t) {
         const int p = find_patch(W, np, t, [](const PatchWork& w) { return w.off_face[0]; });
         if (face_item<X, DIM, MODEL, NSP, SCHEME, 0>(P, W[p].g, W[p].S, t - W[p].off_face[0], nullptr))
@@ -455,12 +558,15 @@ level_kernel(Params P, LevelArgs L) {
                 redo_push(L.redo, 2, t);
         });
     }
+    }
 #if HMR_FAST
     HMR_BARRIER();
     {
         // Exact recomputation of the faces the fast form handed back.
         const unsigned long long nredo = min((unsigned long long)*((volatile unsigned int*)L.redo.count), L.redo.cap);
-        level_chunks(L.chunk + CHUNK_REDO, (long)nredo, L.chunk_mult, [&](long r) {
+        const unsigned long long nleft = nredo > redo_from ? nredo - redo_from : 0ull;
+        level_chunks(L.chunk + CHUNK_REDO, (long)nleft, L.chunk_mult, [&](long rr) {
+            const unsigned long long r = redo_from + (unsigned long long)rr;
             const unsigned long long v = L.redo.list[r];
             const int a = (int)(v >> 56);
             const long t = (long)(v & ((1ull << 56) - 1));

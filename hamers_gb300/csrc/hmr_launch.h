@@ -191,9 +191,15 @@ struct LevelArgs {
     int mom0;                        // first momentum component (the normal one flips at a reflecting wall)
     const double* bvals;             // device [6][ncomp]: the Dirichlet values per side (2 axis + high)
     // work splitting (autotuned; results do not depend on it): phase chunks of chunk_mult
-    // block widths; split_mode 1 hands the cell-wise phases out by a fixed grid stride
+    // block widths; split_mode bit 0 hands the cell-wise phases out by a fixed grid stride,
+    // bit 1 (fast form) sorts the faces by their sensor before the face phase
     int chunk_mult;
     int split_mode;
+    // sorted faces: per axis a the level's face items taking HLLC at sorted + sort_off[a]
+    // (sort_count[a] of them); sort_count[3] HLLC-HLL faces at the head of the redo queue
+    unsigned long long* sorted;
+    long sort_off[3];
+    unsigned int* sort_count;
 };
 
 }  // namespace hmr

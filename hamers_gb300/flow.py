@@ -749,8 +749,9 @@ class BatchedLevel:
         L.check("hmr_level_set_launch", self._lib.hmr_level_set_launch(self.level, int(threads), int(blocks_per_sm)))
 
     def set_work_split(self, chunk_blocks, mode=0):
-        """Chunks of chunk_blocks (1, 2, 4) block widths per phase; mode 1: grid-stride hand-out
-        of the cell-wise phases."""
+        """Chunks of chunk_blocks (1, 2, 4) block widths per phase; mode bit 0: grid-stride
+        hand-out of the cell-wise phases; bit 1 (fast form): faces sorted by their sensor, the
+        HLLC ones in the fast form beside the HLLC-HLL ones in the exact form."""
         L.check("hmr_level_set_work_split", self._lib.hmr_level_set_work_split(self.level, int(chunk_blocks), int(mode)))
 
     def work_split(self):

@@ -388,9 +388,11 @@ int hmr_level_barrier_diagnostic(hmr_level* level, unsigned int extra_arrivals, 
  * maximum) blocks per SM; HMR_ERR_ARGUMENT for a shape that cannot be resident at once. */
 int hmr_level_set_launch(hmr_level* level, int threads, int blocks_per_sm);
 /* Work splitting of the persistent kernel: every phase's items are handed out in chunks of
- * chunk_blocks (1, 2 or 4) block widths taken from a counter in order; mode 1 hands the
- * cell-wise phases (cell data, sensor, update) out by a fixed grid stride instead.  Results do
- * not depend on either. */
+ * chunk_blocks (1, 2 or 4) block widths taken from a counter in order; mode bit 0 hands the
+ * cell-wise phases (cell data, sensor, update) out by a fixed grid stride instead; bit 1 (fast
+ * form) sorts the faces by their sensor first and runs the HLLC faces in the fast form beside the
+ * HLLC-HLL faces in the exact form (instead of the exact form in a phase of its own).  Results
+ * do not depend on any of them. */
 int hmr_level_set_work_split(hmr_level* level, int chunk_blocks, int mode);
 int hmr_level_work_split(hmr_level* level, int* chunk_blocks, int* mode);
 /* Autotuner: times the persistent kernel of this level at 64 and 128 threads per block and

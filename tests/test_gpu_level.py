@@ -105,14 +105,15 @@ def test_launch_shape_leaves_results_unchanged(cuda, precision):
     for bad in ((256, 1), (96, 1), (64, 0), (128, 1000)):
         with pytest.raises(RuntimeError):
             lv.set_launch(*bad)
-    for bad in ((3, 0), (0, 0), (1, 2), (2, -1)):
+    for bad in ((3, 0), (0, 0), (1, 4), (2, -1)):
         with pytest.raises(RuntimeError):
             lv.set_work_split(*bad)
     results = []
     # launch shapes and work splittings (chunk widths of 1, 2, 4 blocks; grid-stride hand-out
-    # of the cell-wise phases)
+    # of the cell-wise phases; faces sorted by their sensor, fast form)
     for shape, split in (((64, 1), (1, 0)), ((128, 1), (1, 0)), ((128, 2), (1, 0)), ((64, 3), (1, 0)),
-                         ((128, 2), (2, 0)), ((64, 2), (4, 0)), ((128, 1), (1, 1)), ((64, 3), (4, 1))):
+                         ((128, 2), (2, 0)), ((64, 2), (4, 0)), ((128, 1), (1, 1)), ((64, 3), (4, 1)),
+                         ((128, 2), (1, 2)), ((64, 3), (2, 3)), ((128, 1), (4, 2))):
         lv.set_launch(*shape)
         lv.set_work_split(*split)
         assert lv.work_split() == split
