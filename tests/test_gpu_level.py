@@ -84,15 +84,16 @@ def test_batched_level_matches_oracle(cuda, variant, precision):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("vi", [5, 7], ids=[IDS[5], IDS[7]])
 @pytest.mark.parametrize("precision", ["exact", "fast"])
-def test_launch_shape_leaves_results_unchanged(cuda, precision):
+def test_launch_shape_leaves_results_unchanged(cuda, precision, vi):
     """Every resident launch shape and work splitting gives the same bits (phase items are
     handed out in chunks from counters or by grid stride, and each item's arithmetic does not
     depend on which block runs it); shapes that cannot be resident, and unknown splittings, are
     rejected before any launch."""
     import torch
     from hamers_gb300 import flow
-    model, dim, scheme, _, gam = VARIANTS[5]
+    model, dim, scheme, _, gam = VARIANTS[vi]
     rec = make(model, dim, scheme, gam, precision)
     sizes, periodic = _patches(dim, 13)
     dt = 1.0e-3
