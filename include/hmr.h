@@ -225,7 +225,10 @@ typedef enum {
 /* Values of the HMR_FILL_DIRICHLET side `side` (0 low, 1 high) of axis `axis`: ncomp conservative
  * values (the reference converts the input's primitive values to these once, with the flow model's
  * basic utilities, EulerBoundaryConditions.cpp:638-723).  Held by the context for every fill that
- * runs on it afterwards, per patch and per level; 0.0 until set.  Rejects non-finite values. */
+ * runs on it afterwards, per patch and per level (captured level graphs included: they read the
+ * values from the context's device copy); 0.0 until set.  The device copy is written by a
+ * synchronous cudaMemcpy: set values between steps, not while a fill of this context is in
+ * flight on another stream.  Rejects non-finite values. */
 int hmr_set_dirichlet_values(hmr_ctx* ctx, int axis, int side, const double* values);
 
 /* Single-patch ghost fill, mode per axis (hmr_fill_mode; other values are rejected with
